@@ -1,0 +1,157 @@
+"""Seeded synthetic parity cases shared by the fixture generator and the tests.
+
+Each case is a small forward-modelling run (a few hundred time steps on a
+ragged grid) chosen to exercise one corner of the reference's time loop.
+``synthetic_model`` builds the material deterministically from the seed;
+``write_case`` writes the reference's own input files (parameter JSON, binary
+model files as NX traces of NY float32 samples, source and receiver files) so
+the compiled reference can run the case.
+"""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+
+WEQ_NAMES = {2: "EL_ISO", 3: "VEL_ISO", 4: "EL_VTI", 5: "VEL_VTI", 6: "EL_TTI", 7: "VEL_TTI"}
+
+
+def _case(name, **kw):
+    base = dict(name=name, weq=2, nx=123, ny=101, dh=2.0, dt=2.0e-4, nt=400, fdorder=4, maxrelerror=0, L=0,
+                fl=[], f_ref=30.0, fw=10, abs_type=1, free_surf=0, boundary=0, npower=2.0, k_max_cpml=1.0,
+                vppml=3500.0, fpml=30.0, damping=8.0, seismo=4, ndt=2, snap=4, tsnap=0.06, idx=2, idy=2,
+                sources=[[121.0, 99.0, 0.0, 40.0, 1.0]], source_type=1, receivers=None, seed=1)
+    base.update(kw)
+    return base
+
+
+CASES = [
+    _case("el_cpml_fd8", fdorder=8, maxrelerror=1, seed=11),
+    _case("el_abs_fd2", fdorder=2, abs_type=2, fw=8, seed=12, nx=97, ny=75),
+    _case("el_abs_fd10", fdorder=10, maxrelerror=3, abs_type=2, fw=12, seed=13),
+    _case("el_cpml_fd12", fdorder=12, maxrelerror=4, seed=14, nx=64, ny=48, fw=8,
+          sources=[[61.0, 45.0, 0.0, 40.0, 1.0]]),
+    _case("el_fs_cpml", free_surf=1, fdorder=6, maxrelerror=2, seed=15,
+          sources=[[121.0, 11.0, 0.0, 40.0, 1.0]]),
+    _case("el_fs_abs_force", free_surf=1, abs_type=2, fw=10, source_type=3, seed=16,
+          sources=[[121.0, 7.0, 0.0, 40.0, 1.0]]),
+    _case("visc_cpml_fs_l3", weq=3, L=3, fl=[5.0, 15.0, 50.0], f_ref=15.0, free_surf=1, fdorder=8,
+          source_type=3, seed=17, sources=[[121.0, 21.0, 0.0, 40.0, 1.0]]),
+    _case("visc_abs_l1", weq=3, L=1, fl=[40.0], f_ref=40.0, abs_type=2, seed=18),
+    _case("vti_cpml", dt=1.5e-4, nt=500, weq=4, fdorder=6, seed=19),
+    _case("vvti_cpml_l2", dt=1.5e-4, nt=500, weq=5, L=2, fl=[10.0, 50.0], f_ref=25.0, fdorder=4, seed=20),
+    _case("tti_cpml", dt=1.5e-4, nt=500, weq=6, fdorder=6, seed=21),
+    _case("tti_abs", dt=1.5e-4, nt=500, weq=6, fdorder=4, abs_type=2, seed=22),
+    _case("vtti_cpml_l1", dt=1.5e-4, nt=500, weq=7, L=1, fl=[30.0], f_ref=30.0, fdorder=4, seed=23),
+    _case("el_periodic_cpml", boundary=1, fdorder=4, seed=24),
+    _case("el_mixed_sources", fdorder=4, seed=25, source_type=2,
+          sources=[[101.0, 81.0, 0.0, 40.0, 1.0, 30.0, 4.0], [141.0, 111.0, 0.005, 35.0, 2.0, 0.0, 2.0],
+                   [121.0, 99.0, 0.0, 40.0, 1.5, 0.0, 1.0]]),
+    _case("el_moment_tensor", fdorder=4, seed=26, source_type=1,
+          sources=[[121.0, 99.0, 0.0, 40.0, 1.0, 35.0, 5.0]]),
+]
+
+
+def _smooth(a, w=7):
+    """Separable moving average over w cells (edges replicated), as float32."""
+    k = np.ones(w) / w
+    p = np.pad(a, w // 2, mode="edge")
+    p = np.apply_along_axis(lambda r: np.convolve(r, k, mode="valid"), 0, p)
+    p = np.apply_along_axis(lambda r: np.convolve(r, k, mode="valid"), 1, p)
+    return p.astype(np.float32)
+
+
+def synthetic_model(case) -> dict:
+    """Layered + 2% perturbed isotropic model (plus anisotropy / Q), [NX][NY] x-major."""
+    rng = np.random.default_rng(case["seed"])
+    nx, ny = case["nx"], case["ny"]
+    y = np.arange(ny)
+    layer = np.where(y < ny // 3, 0, np.where(y < 2 * ny // 3, 1, 2))
+    vp1 = np.array([2000.0, 2800.0, 3500.0])[layer]
+    rho1 = np.array([1800.0, 2100.0, 2400.0])[layer]
+    pert = 1.0 + 0.02 * rng.standard_normal((nx, ny))
+    vp = (vp1[None, :] * pert).astype(np.float32)
+    vs = (vp / 1.73).astype(np.float32)
+    rho = (rho1[None, :] * (1.0 + 0.02 * rng.standard_normal((nx, ny)))).astype(np.float32)
+    mats = {"vp": vp, "vs": vs, "rho": rho}
+    weq = case["weq"]
+    if weq in (4, 5, 6, 7):
+        mats["epsilon"] = _smooth(rng.uniform(0.0, 0.25, (nx, ny)))
+        mats["delta"] = _smooth(rng.uniform(-0.1, 0.15, (nx, ny)))
+    if weq in (6, 7):
+        mats["theta"] = _smooth(rng.uniform(0.0, 45.0, (nx, ny)))
+    if weq in (3, 5, 7):
+        mats["qp"] = _smooth(rng.uniform(20.0, 100.0, (nx, ny)))
+        mats["qs"] = (mats["qp"] * 0.7).astype(np.float32)
+    return {k: np.ascontiguousarray(v).reshape(-1) for k, v in mats.items()}
+
+
+def receivers(case):
+    if case["receivers"] is not None:
+        return case["receivers"]
+    nx, ny, dh = case["nx"], case["ny"], case["dh"]
+    out = []
+    for k in range(12):
+        x = (case["fw"] + 2 + k * (nx - 2 * case["fw"] - 4) / 11.0) * dh
+        out.append([round(x, 1), (3 if case["free_surf"] else case["fw"] + 5) * dh])
+    out.append([nx * dh / 2.0, ny * dh / 2.0])
+    out.append([(nx - 3) * dh, (ny - 3) * dh])  # inside the absorbing frame
+    return out
+
+
+def json_text(case) -> str:
+    weq = WEQ_NAMES[case["weq"]]
+    kv = {
+        "NPROCX": "1", "NPROCY": "1", "MODE": "FW", "FDORDER": str(case["fdorder"]), "FDORDER_TIME": "2",
+        "MAXRELERROR": str(case["maxrelerror"]), "NX": str(case["nx"]), "NY": str(case["ny"]),
+        "DH": repr(case["dh"]), "TIME": repr(case["nt"] * case["dt"]), "DT": repr(case["dt"]), "WEQ": weq,
+        "SOURCE_SHAPE": "1", "SIGNAL_FILE": "none", "SIGOUT": "0", "SOURCE_TYPE": str(case["source_type"]),
+        "SRCREC": "1", "SOURCE_FILE": "./source.dat", "RUN_MULTIPLE_SHOTS": "0", "PLANE_WAVE_DEPTH": "0.0",
+        "PLANE_WAVE_ANGLE": "0.0", "TS": "0.2", "READMOD": "1", "MFILE": "./model/m", "WRITE_MODELFILES": "0",
+        "L": str(case["L"]), "F_REF": repr(case["f_ref"]), "FREE_SURF": str(case["free_surf"]),
+        "BOUNDARY": str(case["boundary"]), "FW": str(case["fw"]), "ABS_TYPE": str(case["abs_type"]),
+        "NPOWER": repr(case["npower"]), "K_MAX_CPML": repr(case["k_max_cpml"]), "VPPML": repr(case["vppml"]),
+        "FPML": repr(case["fpml"]), "DAMPING": repr(case["damping"]), "SNAP": str(case["snap"]),
+        "TSNAP1": repr(case["tsnap"]), "TSNAP2": repr(case["tsnap"]), "TSNAPINC": "1.0",
+        "IDX": str(case["idx"]), "IDY": str(case["idy"]), "SNAP_FORMAT": "3", "SNAP_FILE": "./out/snap",
+        "SEISMO": str(case["seismo"]), "READREC": "1", "REC_FILE": "./receiver.dat", "REFRECX": "0.0",
+        "REFRECY": "0.0", "NGEOPH": "1", "REC_ARRAY": "0", "NDT": str(case["ndt"]), "SEIS_FORMAT": "1",
+        "SEIS_FILE": "./out/seis", "LOG_FILE": "./log/test.log", "LOG": "0", "LOG_VERBOSITY": "WARN",
+        "OUT_TIMESTEP_INFO": "100000",
+    }
+    for k, f in enumerate(case["fl"]):
+        kv[f"FL{k + 1}"] = repr(f)
+    lines = ["{"] + [f'"{k}" : "{v}",' for k, v in kv.items()]
+    lines[-1] = lines[-1].rstrip(",")
+    return "\n".join(lines + ["}"]) + "\n"
+
+
+def write_case(case, work):
+    os.makedirs(os.path.join(work, "model"), exist_ok=True)
+    os.makedirs(os.path.join(work, "out"), exist_ok=True)
+    os.makedirs(os.path.join(work, "log"), exist_ok=True)
+    mats = synthetic_model(case)
+    for k, v in mats.items():
+        v.astype(np.float32).tofile(os.path.join(work, "model", f"m.{k}"))
+    with open(os.path.join(work, "source.dat"), "w") as fh:
+        for s in case["sources"]:
+            fh.write(" ".join(repr(float(t)) for t in s) + "\n")
+    with open(os.path.join(work, "receiver.dat"), "w") as fh:
+        for r in receivers(case):
+            fh.write(f"{r[0]!r} {r[1]!r}\n")
+    jpath = os.path.join(work, "case.json")
+    with open(jpath, "w") as fh:
+        fh.write(json_text(case))
+    return jpath, mats
+
+
+def case_by_name(name):
+    for c in CASES:
+        if c["name"] == name:
+            return c
+    raise KeyError(name)
+
+
+if __name__ == "__main__":
+    print(json.dumps([c["name"] for c in CASES]))

@@ -1,0 +1,145 @@
+"""Generate the golden fixtures in tests/golden/ (run here, where the reference exists).
+
+Two kinds of fixture, both small enough to commit:
+
+* ``shipped_<weq>.npz`` -- the seismograms the reference ships in
+  examples/weqN_ref (produced by the reference itself on 2x2 ranks) plus a
+  subsample of its snapshot files, copied as numbers.
+* ``ref_<case>.npz``   -- outputs of the reference compiled from its own
+  sources by oracle/ref/Makefile (oracle/_ref/sofi2D, one rank) on seeded
+  synthetic cases that the shipped files do not cover: CPML, FDORDER 2-12,
+  MAXRELERROR 1-4, free surface (elastic and viscoelastic), L = 3, VTI/TTI with
+  CPML, periodic x, force / custom-force / moment-tensor sources and ragged
+  grid sizes. Models are regenerated from the seed by ``synthetic_model`` (a
+  CRC of the model bytes is stored to catch a drift).
+
+    python tests/golden/make_fixtures.py [--reference /root/reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+import zlib
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+from tests.golden.cases import CASES, synthetic_model, write_case  # noqa: E402
+
+SHIPPED = {"weq3": "EL_ISO", "weq4": "VEL_ISO", "weq5": "EL_VTI", "weq6": "VEL_VTI", "weq7": "EL_TTI",
+           "weq8": "VEL_TTI", "weq3_fy": "EL_ISO", "weq8_fy": "VEL_TTI"}
+
+
+def read_su(path):
+    b = np.fromfile(path, dtype=np.uint8)
+    ns = int(b[114:116].view(np.uint16)[0])
+    rec = 240 + 4 * ns
+    ntr = b.size // rec
+    b = b[: ntr * rec].reshape(ntr, rec)
+    return b[:, :240].copy(), b[:, 240:].copy().view(np.float32).reshape(ntr, ns)
+
+
+def shipped(reference):
+    ex = os.path.join(reference, "examples")
+    for name in SHIPPED:
+        base = name.split("_")[0]
+        suffix = "_fy" if name.endswith("_fy") else ""
+        out = {}
+        for comp in ["vx", "vy", "p", "div", "curl"]:
+            f = os.path.join(ex, f"{base}_ref", f"seis{suffix}_{comp}.su")
+            hdr, data = read_su(f)
+            out[f"seis_{comp}"] = data
+            out[f"hdr_{comp}"] = hdr
+            s = os.path.join(ex, f"{base}_ref", f"snap{suffix}.bin.{comp}")
+            if os.path.exists(s):
+                a = np.fromfile(s, dtype=np.float32).reshape(4, 200, 200)
+                out[f"snapnorm_{comp}"] = np.sqrt((a.astype(np.float64) ** 2).sum(axis=(1, 2)))
+                out[f"snapsub_{comp}"] = a[:, ::8, ::8].copy()
+        np.savez_compressed(os.path.join(HERE, f"shipped_{name}.npz"), **out)
+        print("wrote shipped", name)
+
+
+def run_reference(case, exe):
+    work = tempfile.mkdtemp(prefix="sofi_fix_")
+    try:
+        jpath, mats = write_case(case, work)
+        r = subprocess.run([exe, jpath], cwd=work, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"{case['name']}: reference failed\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}")
+        out = {}
+        for comp in ["vx", "vy", "p", "div", "curl"]:
+            f = os.path.join(work, "out", f"seis_{comp}.su")
+            if os.path.exists(f):
+                hdr, data = read_su(f)
+                out[f"seis_{comp}"] = data
+                out[f"hdr_{comp}"] = hdr
+            s = os.path.join(work, "out", f"snap.bin.{comp}.0.0")
+            if os.path.exists(s):
+                out[f"snap_{comp}"] = np.fromfile(s, dtype=np.float32)
+        crc = 0
+        for k in sorted(mats):
+            crc = zlib.crc32(mats[k].tobytes(), crc)
+        out["model_crc"] = np.array([crc], dtype=np.uint64)
+        out["case"] = np.frombuffer(json.dumps(case, sort_keys=True).encode(), dtype=np.uint8)
+        return out
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+
+
+def ref_examples(reference, exe):
+    """One-rank compiled-reference runs of the TTI examples (seismograms only)."""
+    ex = os.path.join(reference, "examples")
+    for name in ["weq7", "weq8", "weq8_fy"]:
+        work = tempfile.mkdtemp(prefix="sofi_ex_")
+        try:
+            for d in ["model", "sources", "receiver"]:
+                os.symlink(os.path.join(ex, d), os.path.join(work, d))
+            base = name.split("_")[0]
+            os.makedirs(os.path.join(work, base), exist_ok=True)
+            os.makedirs(os.path.join(work, "log"), exist_ok=True)
+            txt = open(os.path.join(ex, f"{name}.json")).read()
+            txt = txt.replace('"NPROCX" : "2"', '"NPROCX" : "1"').replace('"NPROCY" : "2"', '"NPROCY" : "1"')
+            txt = txt.replace('"SNAP" : "4"', '"SNAP" : "0"')
+            with open(os.path.join(work, "run.json"), "w") as fh:
+                fh.write(txt)
+            r = subprocess.run([exe, "run.json"], cwd=work, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(r.stdout[-2000:])
+            suffix = "_fy" if name.endswith("_fy") else ""
+            out = {}
+            for comp in ["vx", "vy", "p", "div", "curl"]:
+                _, out[f"seis_{comp}"] = read_su(os.path.join(work, base, f"seis{suffix}_{comp}.su"))
+            np.savez_compressed(os.path.join(HERE, f"ref1x1_{name}.npz"), **out)
+            print("wrote ref1x1", name)
+        finally:
+            shutil.rmtree(work, ignore_errors=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--only", default="")
+    a = ap.parse_args()
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle", "ref"), f"REFERENCE={a.reference}"],
+                   check=True)
+    exe = os.path.join(REPO, "oracle", "_ref", "sofi2D")
+    if not a.only:
+        shipped(a.reference)
+        ref_examples(a.reference, exe)
+    for case in CASES:
+        if a.only and case["name"] != a.only:
+            continue
+        out = run_reference(case, exe)
+        np.savez_compressed(os.path.join(HERE, f"ref_{case['name']}.npz"), **out)
+        print("wrote", case["name"], sorted(k for k in out if k.startswith("seis")))
+
+
+if __name__ == "__main__":
+    main()
