@@ -1,0 +1,718 @@
+// sofi_kernels.cuh -- device kernels of the SOFI2D time step on sm_103a.
+//
+// One time step of the reference's time_loop (src/time_loop.c:42-322) is
+//   k_force_src  force sources before the velocity update (update_v_interior.c:49-71)
+//   k_update_v   velocity update, all cells, CPML / damping frame by predicate
+//                (update_v_interior.c, update_v_PML.c, update_v_abs.c)
+//   k_wrap_x     periodic x only: ghost columns (exchange_v.c / exchange_s.c, one rank)
+//   k_update_s   stress update with the velocity derivatives recomputed from v in
+//                registers (v_derivatives.c fused away), CPML / damping by predicate
+//   k_tti_deriv + k_update_s_tti   TTI: derivatives (raw and CPML-stretched) are
+//                stored so the 4-point averages can follow the reference's
+//                region-by-region order (update_s_elastic_TTI_PML.c)
+//   k_seis_deriv div/curl sampling (derivatives as the stress update left them)
+//   k_stress_src explosive / moment-tensor sources + NaN probe (psource.c, eqsource.c)
+//   k_surface    free surface, one thread per column (surface_elastic.c, surface.c)
+//   k_seis       vx, vy, p sampling (seismo_ssg.c)
+//   k_snap       snapshot frame (snap_ssg.c)
+//
+// Layout: every 2-D field is a padded [NY + 2*HY][pitch] float array with the
+// interior cell (j, i) at ((j-1+HY) * pitch + (i-1+HX)); HX = HY = 8 >= ND + 1.
+// The shot index is the slowest dimension (field = base + shot * fsz). Ghost
+// cells stay zero (or hold the periodic copy), as the reference's edge ranks.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sofi {
+
+constexpr int HX = 8;
+constexpr int HY = 8;
+constexpr int MAXL = 8;
+constexpr int BX = 32;  // threads per block in x
+constexpr int BY = 8;   // threads per block in y
+
+enum Kind { ISO = 0, VTI = 1, TTI = 2 };
+
+struct Geo {
+    int nx, ny, pitch, nshots;
+    long long fsz;          // floats per 2-D field
+    int fw, fw2;            // frame width, 2*FW
+    int gx2, gx3, gy2, gy3; // reference subgrid_bounds (one rank)
+    int abs_type;           // 0 none, 1 CPML, 2 damping (0 when FW == 0)
+    int free_surf, boundary, L;
+    int model_stride_on;    // 1: model per shot, 0: shared
+    int el_tti_rb_short;    // EL_TTI CPML: right-bottom corner pass stops at NY-1
+    float dt, dh, dtdh, dhi, dthalbe;
+    float hc[7];
+};
+
+// Wavefield and CPML memory (per shot).
+struct Wave {
+    float *vx, *vy, *sxx, *syy, *sxy;
+    float *r, *p, *q;                          // L planes per shot: [(s*L + l-1) * fsz]
+    float *psi_sxx_x, *psi_sxy_x, *psi_vxx, *psi_vyx;  // [s][NY][2FW]
+    float *psi_syy_y, *psi_sxy_y, *psi_vyy, *psi_vxy;  // [s][2FW][NX]
+    float *draw, *dcor;                        // TTI: 4 derivative fields each, per shot
+};
+
+// Prepared model arrays (one per shot or shared) and 1-D vectors.
+struct Model {
+    const float *prip, *prjp;
+    const float *g, *f, *fipjp;                 // isotropic (unrelaxed for visco)
+    const float *db, *eb, *dipb;                // isotropic visco bases: pu*taus, pi*taup, uipjp*tausipjp
+    const float *c11, *c13, *c33, *c15, *c35, *c55ipjp, *c15ipjp, *c35ipjp;   // anisotropic (DT-scaled)
+    const float *c11b, *c13b, *c33b, *c15b, *c35b, *c55ipjpb, *c15ipjpb, *c35ipjpb;  // visco bases c*tau
+    const float *ppi, *pu, *taus, *taup;        // surface / sampling
+    const float *absorb;
+    const float *K_x, *a_x, *b_x, *K_x_half, *a_x_half, *b_x_half;
+    const float *K_y, *a_y, *b_y, *K_y_half, *a_y_half, *b_y_half;
+    float bip[MAXL], cip[MAXL], peta[MAXL];
+};
+
+// Sources / receivers / sections of all shots (flattened with per-shot offsets).
+struct Acq {
+    const int *src_off;      // [nshots+1] offsets into the source arrays
+    const int *src_ix, *src_iy, *src_type;
+    const float *src_amp, *src_sin, *src_cos, *src_sin2, *src_cos2;  // amplitude, sin/cos(azimuth), sin/cos(2 dip)
+    const float *signals;    // [total sources][nt]
+    const int *last_type;    // [nshots] type of each shot's last source
+    const int *rec_off;      // [nshots+1]
+    const int *rec_ix, *rec_iy;
+    float *sec;              // [total receivers][5][ns]
+    int nt, ns;
+    int *status;             // [nshots] 0 ok, else first unstable step
+};
+
+__device__ __forceinline__ long long cell(const Geo &G, int j, int i)
+{
+    return (long long)(j - 1 + HY) * G.pitch + (i - 1 + HX);
+}
+
+__device__ __forceinline__ long long moff(const Geo &G, int s)
+{
+    return G.model_stride_on ? (long long)s * G.fsz : 0;
+}
+
+// ------------------------------------------------------------ FD operators
+
+// op_v_fdN (reference initfd.c:97-183): stress derivatives, unscaled.
+template <int ND>
+__device__ __forceinline__ void op_v(const float *__restrict__ sxx, const float *__restrict__ syy,
+                                     const float *__restrict__ sxy, long long o, int P, const float *hc,
+                                     float &sxx_x, float &sxy_x, float &sxy_y, float &syy_y)
+{
+    sxx_x = hc[1] * (__ldg(sxx + o + 1) - __ldg(sxx + o));
+    sxy_x = hc[1] * (__ldg(sxy + o) - __ldg(sxy + o - 1));
+    sxy_y = hc[1] * (__ldg(sxy + o) - __ldg(sxy + o - P));
+    syy_y = hc[1] * (__ldg(syy + o + P) - __ldg(syy + o));
+#pragma unroll
+    for (int m = 2; m <= ND; m++) {
+        sxx_x += hc[m] * (__ldg(sxx + o + m) - __ldg(sxx + o - m + 1));
+        sxy_x += hc[m] * (__ldg(sxy + o + m - 1) - __ldg(sxy + o - m));
+        sxy_y += hc[m] * (__ldg(sxy + o + (long long)(m - 1) * P) - __ldg(sxy + o - (long long)m * P));
+        syy_y += hc[m] * (__ldg(syy + o + (long long)m * P) - __ldg(syy + o - (long long)(m - 1) * P));
+    }
+}
+
+// op_s_fdN (reference initfd.c:9-95): velocity derivatives, times 1/DH.
+template <int ND>
+__device__ __forceinline__ void op_s(const float *__restrict__ vx, const float *__restrict__ vy, long long o,
+                                     int P, const float *hc, float dhi, float &vxx, float &vyx, float &vxy,
+                                     float &vyy)
+{
+    vxx = hc[1] * (__ldg(vx + o) - __ldg(vx + o - 1));
+    vyx = hc[1] * (__ldg(vy + o + 1) - __ldg(vy + o));
+    vxy = hc[1] * (__ldg(vx + o + P) - __ldg(vx + o));
+    vyy = hc[1] * (__ldg(vy + o) - __ldg(vy + o - P));
+#pragma unroll
+    for (int m = 2; m <= ND; m++) {
+        vxx += hc[m] * (__ldg(vx + o + m - 1) - __ldg(vx + o - m));
+        vyx += hc[m] * (__ldg(vy + o + m) - __ldg(vy + o - m + 1));
+        vxy += hc[m] * (__ldg(vx + o + (long long)m * P) - __ldg(vx + o - (long long)(m - 1) * P));
+        vyy += hc[m] * (__ldg(vy + o + (long long)(m - 1) * P) - __ldg(vy + o - (long long)m * P));
+    }
+    vxx *= dhi;
+    vyx *= dhi;
+    vxy *= dhi;
+    vyy *= dhi;
+}
+
+// Frame membership of column i / row j: 0 middle, 1 left/top (h = i or j),
+// 2 right/bottom (h = i - NX + 2FW or j - NY + 2FW); reference update_v_PML.c.
+__device__ __forceinline__ int xside(const Geo &G, int i)
+{
+    return i <= G.gx2 ? 1 : (i > G.gx3 ? 2 : 0);
+}
+__device__ __forceinline__ int yside(const Geo &G, int j)
+{
+    return j <= G.gy2 ? 1 : (j > G.gy3 ? 2 : 0);
+}
+// Region order of the reference's drivers: 0 interior, 1 left, 2 right, 3 top,
+// 4 bottom, 5 left-top, 6 left-bottom, 7 right-top, 8 right-bottom.
+__device__ __forceinline__ int region(const Geo &G, int i, int j)
+{
+    int xr = xside(G, i), yr = yside(G, j);
+    if (!yr)
+        return xr;
+    if (!xr)
+        return 2 + yr;
+    return 4 + (xr - 1) * 2 + yr;
+}
+
+// -------------------------------------------------------------- sources
+
+// update_v_interior.c:49-71
+__global__ void k_force_src(Geo G, Wave W, Model M, Acq A, int nt)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= G.nshots)
+        return;
+    const float *prip = M.prip + moff(G, s), *prjp = M.prjp + moff(G, s);
+    float *vx = W.vx + (long long)s * G.fsz, *vy = W.vy + (long long)s * G.fsz;
+    for (int k = A.src_off[s]; k < A.src_off[s + 1]; k++) {
+        int t = A.src_type[k];
+        if (t < 2 || t > 4)
+            continue;
+        long long o = cell(G, A.src_iy[k], A.src_ix[k]);
+        float amp = (G.dt * A.signals[(long long)k * A.nt + (nt - 1)]) / (G.dh * G.dh);
+        if (t == 2)
+            vx[o] += prip[o] * amp;
+        else if (t == 3)
+            vy[o] += prjp[o] * amp;
+        else {
+            vx[o] += A.src_sin[k] * (prip[o] * amp);
+            vy[o] += A.src_cos[k] * (prjp[o] * amp);
+        }
+    }
+}
+
+// psource.c:27-54 and eqsource.c:25-52 (applied to all sources when the last
+// source's type selects them, time_loop.c:248-253) + the NaN probe of
+// time_loop.c:44-47 at (NY/2, NX/2).
+__global__ void k_stress_src(Geo G, Wave W, Acq A, int nt)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= G.nshots)
+        return;
+    long long so = (long long)s * G.fsz;
+    float *sxx = W.sxx + so, *syy = W.syy + so, *sxy = W.sxy + so;
+    int lt = A.last_type[s];
+    int NT = A.nt;
+    for (int k = A.src_off[s]; k < A.src_off[s + 1]; k++) {
+        long long o = cell(G, A.src_iy[k], A.src_ix[k]);
+        const float *sig = A.signals + (long long)k * NT - 1;  // 1-based: sig[1..NT]
+        if (lt == 1) {
+            // central difference of the signal (psource.c:41-49); a one-step run
+            // has no neighbouring sample and injects nothing
+            float amp = 0.0f;
+            float d2 = 2.0f * G.dh * G.dh;
+            if (NT >= 2) {
+                if (nt == 1)
+                    amp = sig[2] / d2;
+                else if (nt < NT)
+                    amp = (sig[nt + 1] - sig[nt - 1]) / d2;
+                else
+                    amp = -sig[nt - 1] / d2;
+            }
+            sxx[o] += amp;
+            syy[o] += amp;
+        } else if (lt == 5) {
+            float scale_amp = G.dt / (G.dh * G.dh);
+            float amp = A.src_amp[k] * scale_amp * sig[nt];
+            float m11 = -A.src_sin2[k], m12 = -A.src_cos2[k], m22 = A.src_sin2[k];
+            sxx[o] += amp * m11;
+            sxy[o] += 0.3f * amp * m12;
+            sxy[o - G.pitch] += 0.3f * amp * m12;
+            sxy[o - 1] += 0.3f * amp * m12;
+            syy[o] += amp * m22;
+        }
+    }
+    long long pc = cell(G, G.ny / 2 > 0 ? G.ny / 2 : 1, G.nx / 2 > 0 ? G.nx / 2 : 1);
+    float probe = W.vy[so + pc];
+    if (isnan(probe) && A.status[s] == 0)
+        A.status[s] = nt;
+}
+
+// ------------------------------------------------------- velocity update
+
+template <int ND>
+__global__ void __launch_bounds__(BX *BY) k_update_v(Geo G, Wave W, Model M)
+{
+    int i = blockIdx.x * BX + threadIdx.x + 1;
+    int j = blockIdx.y * BY + threadIdx.y + 1;
+    int s = blockIdx.z;
+    if (i > G.nx || j > G.ny)
+        return;
+    const int P = G.pitch;
+    long long o = cell(G, j, i);
+    long long so = (long long)s * G.fsz, mo = moff(G, s);
+    float sxx_x, sxy_x, sxy_y, syy_y;
+    op_v<ND>(W.sxx + so, W.syy + so, W.sxy + so, o, P, G.hc, sxx_x, sxy_x, sxy_y, syy_y);
+    int xr = xside(G, i), yr = yside(G, j);
+    if (G.abs_type == 1) {
+        if (xr) {
+            int h = xr == 1 ? i : i - G.nx + G.fw2;
+            long long q = ((long long)s * G.ny + (j - 1)) * G.fw2 + (h - 1);
+            float ps = M.b_x_half[h - 1] * W.psi_sxx_x[q] + M.a_x_half[h - 1] * sxx_x;
+            W.psi_sxx_x[q] = ps;
+            sxx_x = sxx_x / M.K_x_half[h - 1] + ps;
+            float py = M.b_x[h - 1] * W.psi_sxy_x[q] + M.a_x[h - 1] * sxy_x;
+            W.psi_sxy_x[q] = py;
+            sxy_x = sxy_x / M.K_x[h - 1] + py;
+        }
+        if (yr) {
+            int h = yr == 1 ? j : j - G.ny + G.fw2;
+            long long q = ((long long)s * G.fw2 + (h - 1)) * G.nx + (i - 1);
+            float ps = M.b_y_half[h - 1] * W.psi_syy_y[q] + M.a_y_half[h - 1] * syy_y;
+            W.psi_syy_y[q] = ps;
+            syy_y = syy_y / M.K_y_half[h - 1] + ps;
+            float py = M.b_y[h - 1] * W.psi_sxy_y[q] + M.a_y[h - 1] * sxy_y;
+            W.psi_sxy_y[q] = py;
+            sxy_y = sxy_y / M.K_y[h - 1] + py;
+        }
+    }
+    float *vx = W.vx + so, *vy = W.vy + so;
+    float nvx = vx[o] + (sxx_x + sxy_y) * G.dtdh * __ldg(M.prip + mo + o);
+    float nvy = vy[o] + (sxy_x + syy_y) * G.dtdh * __ldg(M.prjp + mo + o);
+    if (G.abs_type == 2 && (xr | yr)) {
+        float a = __ldg(M.absorb + mo + o);
+        nvx *= a;
+        nvy *= a;
+    }
+    vx[o] = nvx;
+    vy[o] = nvy;
+}
+
+// Periodic x (BOUNDARY = 1): ghost columns copy the opposite edge, as the one-
+// rank exchange_v / exchange_s do (every column the stencils read is covered).
+__global__ void k_wrap_x(Geo G, float *a, float *b, float *c, int nd)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    int s = blockIdx.y;
+    if (j > G.ny)
+        return;
+    float *f[3] = {a, b, c};
+    for (int t = 0; t < 3; t++) {
+        if (!f[t])
+            continue;
+        float *x = f[t] + (long long)s * G.fsz;
+        for (int l = 1; l <= nd + 1; l++) {
+            x[cell(G, j, G.nx + l)] = x[cell(G, j, l)];
+            x[cell(G, j, 1 - l)] = x[cell(G, j, G.nx - l + 1)];
+        }
+    }
+}
+
+// --------------------------------------------------------- stress update
+
+// CPML stretch of the four velocity derivatives of one cell, updating the
+// memory variables (cpml_update.c:30-46 with the drivers' h rules).
+__device__ __forceinline__ void cpml_s(const Geo &G, const Wave &W, const Model &M, int s, int i, int j, int xr,
+                                       int yr, float &vxx, float &vyx, float &vxy, float &vyy, bool write)
+{
+    if (xr) {
+        int h = xr == 1 ? i : i - G.nx + G.fw2;
+        long long q = ((long long)s * G.ny + (j - 1)) * G.fw2 + (h - 1);
+        float p1 = M.b_x[h - 1] * W.psi_vxx[q] + M.a_x[h - 1] * vxx;
+        vxx = vxx / M.K_x[h - 1] + p1;
+        float p2 = M.b_x_half[h - 1] * W.psi_vyx[q] + M.a_x_half[h - 1] * vyx;
+        vyx = vyx / M.K_x_half[h - 1] + p2;
+        if (write) {
+            W.psi_vxx[q] = p1;
+            W.psi_vyx[q] = p2;
+        }
+    }
+    if (yr) {
+        int h = yr == 1 ? j : j - G.ny + G.fw2;
+        long long q = ((long long)s * G.fw2 + (h - 1)) * G.nx + (i - 1);
+        float p1 = M.b_y[h - 1] * W.psi_vyy[q] + M.a_y[h - 1] * vyy;
+        vyy = vyy / M.K_y[h - 1] + p1;
+        float p2 = M.b_y_half[h - 1] * W.psi_vxy[q] + M.a_y_half[h - 1] * vxy;
+        vxy = vxy / M.K_y_half[h - 1] + p2;
+        if (write) {
+            W.psi_vyy[q] = p1;
+            W.psi_vxy[q] = p2;
+        }
+    }
+}
+
+// Isotropic and VTI stress update of one cell (wavefield_update_s_el.c,
+// _visc.c, _el_vti.c, _visc_VTI.c). Viscoelastic modulus defects are the
+// stored base (modulus * tau) times peta[l].
+template <int KIND, bool VISCO>
+__device__ __forceinline__ void stress_cell(const Geo &G, const Wave &W, const Model &M, int s, long long o,
+                                            long long so, long long mo, float vxx, float vyx, float vxy,
+                                            float vyy, float &u1, float &u2, float &u3)
+{
+    if (KIND == ISO) {
+        float g = __ldg(M.g + mo + o), f = __ldg(M.f + mo + o), fipjp = __ldg(M.fipjp + mo + o);
+        u1 = fipjp * (vyx + vxy);
+        float gd = g * (vxx + vyy);
+        u2 = gd - 2.0f * f * vyy;
+        u3 = gd - 2.0f * f * vxx;
+        if (VISCO) {
+            float db = __ldg(M.db + mo + o), eb = __ldg(M.eb + mo + o), dipb = __ldg(M.dipb + mo + o);
+            float sro = 0.f, spo = 0.f, sqo = 0.f, sr = 0.f, sp = 0.f, sq = 0.f;
+            for (int l = 0; l < G.L; l++) {
+                long long lo = ((long long)s * G.L + l) * G.fsz + o;
+                float r = W.r[lo], p = W.p[lo], q = W.q[lo];
+                sro += r, spo += p, sqo += q;
+                float pe = M.peta[l], b = M.bip[l], c = M.cip[l];
+                float dip = dipb * pe, d = db * pe, e = eb * pe;
+                r = b * (r * c - dip * (vxy + vyx));
+                p = b * (p * c - e * (vxx + vyy) + 2.0f * d * vyy);
+                q = b * (q * c - e * (vxx + vyy) + 2.0f * d * vxx);
+                W.r[lo] = r, W.p[lo] = p, W.q[lo] = q;
+                sr += r, sp += p, sq += q;
+            }
+            u1 += G.dthalbe * (sro + sr);
+            u2 += G.dthalbe * (spo + sp);
+            u3 += G.dthalbe * (sqo + sq);
+        }
+    } else {  // VTI
+        float c11 = __ldg(M.c11 + mo + o), c13 = __ldg(M.c13 + mo + o), c33 = __ldg(M.c33 + mo + o);
+        float c55 = __ldg(M.c55ipjp + mo + o);
+        u1 = c55 * (vxy + vyx);
+        u2 = c11 * vxx + c13 * vyy;
+        u3 = c13 * vxx + c33 * vyy;
+        if (VISCO) {
+            float b11 = __ldg(M.c11b + mo + o), b13 = __ldg(M.c13b + mo + o), b33 = __ldg(M.c33b + mo + o);
+            float b55 = __ldg(M.c55ipjpb + mo + o);
+            float sro = 0.f, spo = 0.f, sqo = 0.f, sr = 0.f, sp = 0.f, sq = 0.f;
+            for (int l = 0; l < G.L; l++) {
+                long long lo = ((long long)s * G.L + l) * G.fsz + o;
+                float r = W.r[lo], p = W.p[lo], q = W.q[lo];
+                sro += r, spo += p, sqo += q;
+                float pe = M.peta[l], b = M.bip[l], c = M.cip[l];
+                r = b * (r * c - (b55 * pe) * (vxy + vyx));
+                p = b * (p * c - (b11 * pe) * vxx - (b13 * pe) * vyy);
+                q = b * (q * c - (b13 * pe) * vxx - (b33 * pe) * vyy);
+                W.r[lo] = r, W.p[lo] = p, W.q[lo] = q;
+                sr += r, sp += p, sq += q;
+            }
+            u1 += G.dthalbe * (sro + sr);
+            u2 += G.dthalbe * (spo + sp);
+            u3 += G.dthalbe * (sqo + sq);
+        }
+    }
+}
+
+template <int ND, int KIND, bool VISCO>
+__global__ void __launch_bounds__(BX *BY) k_update_s(Geo G, Wave W, Model M)
+{
+    int i = blockIdx.x * BX + threadIdx.x + 1;
+    int j = blockIdx.y * BY + threadIdx.y + 1;
+    int s = blockIdx.z;
+    if (i > G.nx || j > G.ny)
+        return;
+    const int P = G.pitch;
+    long long o = cell(G, j, i);
+    long long so = (long long)s * G.fsz, mo = moff(G, s);
+    float vxx, vyx, vxy, vyy;
+    op_s<ND>(W.vx + so, W.vy + so, o, P, G.hc, G.dhi, vxx, vyx, vxy, vyy);
+    int xr = xside(G, i), yr = yside(G, j);
+    if (G.abs_type == 1)
+        cpml_s(G, W, M, s, i, j, xr, yr, vxx, vyx, vxy, vyy, true);
+    float u1, u2, u3;
+    stress_cell<KIND, VISCO>(G, W, M, s, o, so, mo, vxx, vyx, vxy, vyy, u1, u2, u3);
+    float nxy = W.sxy[so + o] + u1, nxx = W.sxx[so + o] + u2, nyy = W.syy[so + o] + u3;
+    if (G.abs_type == 2 && (xr | yr)) {
+        float a = __ldg(M.absorb + mo + o);
+        nxy *= a, nyy *= a, nxx *= a;
+    }
+    W.sxy[so + o] = nxy;
+    W.sxx[so + o] = nxx;
+    W.syy[so + o] = nyy;
+}
+
+// ------------------------------------------------------------------ TTI
+
+// Raw velocity derivatives of every cell and their CPML-stretched values
+// (equal to the raw ones outside the CPML passes); updates psi_v.
+template <int ND>
+__global__ void __launch_bounds__(BX *BY) k_tti_deriv(Geo G, Wave W, Model M)
+{
+    int i = blockIdx.x * BX + threadIdx.x + 1;
+    int j = blockIdx.y * BY + threadIdx.y + 1;
+    int s = blockIdx.z;
+    if (i > G.nx || j > G.ny)
+        return;
+    long long o = cell(G, j, i);
+    long long so = (long long)s * G.fsz;
+    float vxx, vyx, vxy, vyy;
+    op_s<ND>(W.vx + so, W.vy + so, o, G.pitch, G.hc, G.dhi, vxx, vyx, vxy, vyy);
+    float *dr = W.draw + 4 * so, *dc = W.dcor + 4 * so;
+    dr[o] = vxx, dr[G.fsz + o] = vyy, dr[2 * G.fsz + o] = vyx, dr[3 * G.fsz + o] = vxy;
+    if (G.abs_type == 1) {
+        int xr = xside(G, i), yr = yside(G, j);
+        bool skip = G.el_tti_rb_short && xr == 2 && yr == 2 && j == G.ny;
+        if (!skip)
+            cpml_s(G, W, M, s, i, j, xr, yr, vxx, vyx, vxy, vyy, true);
+    }
+    dc[o] = vxx, dc[G.fsz + o] = vyy, dc[2 * G.fsz + o] = vyx, dc[3 * G.fsz + o] = vxy;
+}
+
+// Derivative k (0 vxx, 1 vyy, 2 vyx, 3 vxy) of neighbour (jn, in) as the
+// reference's TTI update of a cell in region rc sees it: stretched if the
+// neighbour's region had its CPML pass before rc's update pass (regions are
+// processed in order, the interior first, each region's CPML pass before its
+// update pass), raw otherwise; zero outside the grid (periodic x: the raw
+// value of the wrapped column, copied before any stretch).
+__device__ __forceinline__ float tti_d(const Geo &G, const float *dr, const float *dc, int k, int jn, int in,
+                                       int rc)
+{
+    if (jn < 1 || jn > G.ny)
+        return 0.f;
+    if (in < 1 || in > G.nx) {
+        if (!G.boundary)
+            return 0.f;
+        in = in < 1 ? in + G.nx : in - G.nx;
+        return dr[k * G.fsz + cell(G, jn, in)];
+    }
+    long long o = cell(G, jn, in);
+    int rn = region(G, in, jn);
+    return (rn <= rc) ? dc[k * G.fsz + o] : dr[k * G.fsz + o];
+}
+
+// wavefield_update_s_el_tti.c:27-52 / wavefield_update_s_visc_TTI.c:27-84 with
+// the TTI CPML driver's skipped outer cells (update_s_elastic_TTI_PML.c).
+template <bool VISCO>
+__global__ void __launch_bounds__(BX *BY) k_update_s_tti(Geo G, Wave W, Model M)
+{
+    int i = blockIdx.x * BX + threadIdx.x + 1;
+    int j = blockIdx.y * BY + threadIdx.y + 1;
+    int s = blockIdx.z;
+    if (i > G.nx || j > G.ny)
+        return;
+    int xr = xside(G, i), yr = yside(G, j);
+    if (G.abs_type == 1) {
+        if ((xr == 1 && i < 3) || (xr == 2 && i > G.nx - 2) || (yr == 1 && j < 3) || (yr == 2 && j > G.ny - 2))
+            return;
+    }
+    long long o = cell(G, j, i);
+    long long so = (long long)s * G.fsz, mo = moff(G, s);
+    const float *dr = W.draw + 4 * so, *dc = W.dcor + 4 * so;
+    int rc = (G.abs_type == 1) ? region(G, i, j) : 0;
+    float vxx = tti_d(G, dr, dc, 0, j, i, rc), vyy = tti_d(G, dr, dc, 1, j, i, rc);
+    float vxxipjp = 0.25f * (vxx + tti_d(G, dr, dc, 0, j + 1, i, rc) + tti_d(G, dr, dc, 0, j, i + 1, rc) +
+                             tti_d(G, dr, dc, 0, j + 1, i + 1, rc));
+    float vyyipjp = 0.25f * (vyy + tti_d(G, dr, dc, 1, j + 1, i, rc) + tti_d(G, dr, dc, 1, j, i + 1, rc) +
+                             tti_d(G, dr, dc, 1, j + 1, i + 1, rc));
+    float vyx0 = tti_d(G, dr, dc, 2, j, i, rc), vxy0 = tti_d(G, dr, dc, 3, j, i, rc);
+    float vyxij = 0.25f * (vyx0 + tti_d(G, dr, dc, 2, j - 1, i, rc) + tti_d(G, dr, dc, 2, j, i - 1, rc) +
+                           tti_d(G, dr, dc, 2, j - 1, i - 1, rc));
+    float vxyij = 0.25f * (vxy0 + tti_d(G, dr, dc, 3, j - 1, i, rc) + tti_d(G, dr, dc, 3, j, i - 1, rc) +
+                           tti_d(G, dr, dc, 3, j - 1, i - 1, rc));
+    float vij = vyxij + vxyij;
+    float v = vxy0 + vyx0;
+    float u1, u2, u3;
+    if (!VISCO) {
+        u1 = __ldg(M.c55ipjp + mo + o) * v + __ldg(M.c15ipjp + mo + o) * vxxipjp +
+             __ldg(M.c35ipjp + mo + o) * vyyipjp;
+        u2 = __ldg(M.c11 + mo + o) * vxx + __ldg(M.c13 + mo + o) * vyy + __ldg(M.c15 + mo + o) * vij;
+        u3 = __ldg(M.c13 + mo + o) * vxx + __ldg(M.c33 + mo + o) * vyy + __ldg(M.c35 + mo + o) * vij;
+    } else {
+        u1 = __ldg(M.c55ipjp + mo + o) * v + __ldg(M.c15ipjp + mo + o) * vxxipjp +
+             __ldg(M.c35ipjp + mo + o) * vyyipjp;
+        u2 = __ldg(M.c11 + mo + o) * vxx + __ldg(M.c13 + mo + o) * vyy + __ldg(M.c15 + mo + o) * vij;
+        u3 = __ldg(M.c13 + mo + o) * vxx + __ldg(M.c33 + mo + o) * vyy + __ldg(M.c35 + mo + o) * vij;
+        float b55 = __ldg(M.c55ipjpb + mo + o), b15i = __ldg(M.c15ipjpb + mo + o), b35i = __ldg(M.c35ipjpb + mo + o);
+        float b11 = __ldg(M.c11b + mo + o), b13 = __ldg(M.c13b + mo + o), b33 = __ldg(M.c33b + mo + o);
+        float b15 = __ldg(M.c15b + mo + o), b35 = __ldg(M.c35b + mo + o);
+        float sro = 0.f, spo = 0.f, sqo = 0.f, sr = 0.f, sp = 0.f, sq = 0.f;
+        for (int l = 0; l < G.L; l++) {
+            long long lo = ((long long)s * G.L + l) * G.fsz + o;
+            float r = W.r[lo], p = W.p[lo], q = W.q[lo];
+            sro += r, spo += p, sqo += q;
+            float pe = M.peta[l], b = M.bip[l], c = M.cip[l];
+            r = b * (r * c - (b55 * pe) * v - (b15i * pe) * vxxipjp - (b35i * pe) * vyyipjp);
+            p = b * (p * c - (b11 * pe) * vxx - (b13 * pe) * vyy - (b15 * pe) * vij);
+            q = b * (q * c - (b13 * pe) * vxx - (b33 * pe) * vyy - (b35 * pe) * vij);
+            W.r[lo] = r, W.p[lo] = p, W.q[lo] = q;
+            sr += r, sp += p, sq += q;
+        }
+        u1 += G.dthalbe * (sro + sr);
+        u2 += G.dthalbe * (spo + sp);
+        u3 += G.dthalbe * (sqo + sq);
+    }
+    float nxy = W.sxy[so + o] + u1, nxx = W.sxx[so + o] + u2, nyy = W.syy[so + o] + u3;
+    if (G.abs_type == 2 && (xr | yr)) {
+        float a = __ldg(M.absorb + mo + o);
+        nxy *= a, nyy *= a, nxx *= a;
+    }
+    W.sxy[so + o] = nxy;
+    W.sxx[so + o] = nxx;
+    W.syy[so + o] = nyy;
+}
+
+// ---------------------------------------------------------- free surface
+
+// surface_elastic.c:27-90 / surface.c:27-113 at j = 1, one thread per column.
+template <int ND, bool VISCO>
+__global__ void k_surface(Geo G, Wave W, Model M)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    int s = blockIdx.y;
+    if (i > G.nx)
+        return;
+    const int P = G.pitch, j = 1;
+    long long so = (long long)s * G.fsz, mo = moff(G, s);
+    long long o = cell(G, j, i);
+    float *sxx = W.sxx + so, *syy = W.syy + so, *sxy = W.sxy + so;
+    const float *vx = W.vx + so, *vy = W.vy + so;
+    syy[o] = 0.0f;
+    if (VISCO)
+        for (int l = 0; l < G.L; l++)
+            W.q[((long long)s * G.L + l) * G.fsz + o] = 0.0f;
+    float vxx = 0.f, vyy = 0.f;
+#pragma unroll
+    for (int m = 1; m <= ND; m++) {
+        syy[o - (long long)m * P] = -syy[o + (long long)m * P];
+        sxy[o - (long long)m * P] = -sxy[o + (long long)(m - 1) * P];
+        vxx += G.hc[m] * (vx[o + m - 1] - vx[o - m]);
+        vyy += G.hc[m] * (vy[o + (long long)(m - 1) * P] - vy[o - (long long)m * P]);
+    }
+    vxx *= G.dhi;
+    vyy *= G.dhi;
+    if (G.abs_type == 1 && !G.boundary) {
+        int h = 0;
+        if (i <= G.fw)
+            h = i;
+        else if (i >= G.nx - G.fw + 1)
+            h = i - G.nx + G.fw2;
+        if (h) {
+            long long q = ((long long)s * G.ny + (j - 1)) * G.fw2 + (h - 1);
+            float ps = M.b_x[h - 1] * W.psi_vxx[q] + M.a_x[h - 1] * vxx;
+            W.psi_vxx[q] = ps;
+            vxx = vxx / M.K_x[h - 1] + ps;
+        }
+    }
+    float pu = M.pu[mo + o], ppi = M.ppi[mo + o];
+    if (!VISCO) {
+        float fjm = pu * 2.0f, g = ppi;
+        sxx[o] += -(G.dt * (g - fjm) * (g - fjm) * vxx / g) - (G.dt * (g - fjm) * vyy);
+    } else {
+        float taus = M.taus[mo + o], taup = M.taup[mo + o];
+        float sump = 0.f;
+        for (int l = 0; l < G.L; l++)
+            sump += W.p[((long long)s * G.L + l) * G.fsz + o];
+        float fjm = pu * 2.0f * (1.0f + G.L * taus);
+        float g = ppi * (1.0f + G.L * taup);
+        sxx[o] += -(G.dt * (g - fjm) * (g - fjm) * vxx / g) - (G.dt * (g - fjm) * vyy) - (G.dthalbe * sump);
+        sump = 0.f;
+        float djm = 2.0f * pu * taus, e = ppi * taup;
+        for (int l = 0; l < G.L; l++) {
+            float bjm = M.peta[l] / (1.0f + (M.peta[l] * 0.5f));
+            long long lo = ((long long)s * G.L + l) * G.fsz + o;
+            float pl = W.p[lo] + bjm * (((djm - e) * ((fjm / g) - 1.0f) * vxx) - ((djm - e) * vyy));
+            W.p[lo] = pl;
+            sump += pl;
+        }
+        sxx[o] += G.dthalbe * sump;
+    }
+}
+
+// ------------------------------------------------------------ sampling
+
+// div / curl of seismo_ssg.c:43-47 from the derivatives the stress update
+// used (CPML-stretched in the frame), before the free surface runs.
+template <int ND, bool TTIK>
+__global__ void k_seis_deriv(Geo G, Wave W, Model M, Acq A, int ins)
+{
+    int s = blockIdx.y;
+    int k = A.rec_off[s] + blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= A.rec_off[s + 1])
+        return;
+    int i = A.rec_ix[k], j = A.rec_iy[k];
+    long long o = cell(G, j, i);
+    long long so = (long long)s * G.fsz, mo = moff(G, s);
+    float vxx, vyx, vxy, vyy;
+    if (TTIK) {
+        const float *dc = W.dcor + 4 * so;
+        vxx = dc[o], vyy = dc[G.fsz + o], vyx = dc[2 * G.fsz + o], vxy = dc[3 * G.fsz + o];
+    } else {
+        op_s<ND>(W.vx + so, W.vy + so, o, G.pitch, G.hc, G.dhi, vxx, vyx, vxy, vyy);
+        if (G.abs_type == 1) {
+            // psi already holds this step's value (the stress update advanced
+            // it), so the stretched derivative is d / K + psi
+            int xr = xside(G, i), yr = yside(G, j);
+            if (xr) {
+                int h = xr == 1 ? i : i - G.nx + G.fw2;
+                long long q = ((long long)s * G.ny + (j - 1)) * G.fw2 + (h - 1);
+                vxx = vxx / M.K_x[h - 1] + W.psi_vxx[q];
+                vyx = vyx / M.K_x_half[h - 1] + W.psi_vyx[q];
+            }
+            if (yr) {
+                int h = yr == 1 ? j : j - G.ny + G.fw2;
+                long long q = ((long long)s * G.fw2 + (h - 1)) * G.nx + (i - 1);
+                vyy = vyy / M.K_y[h - 1] + W.psi_vyy[q];
+                vxy = vxy / M.K_y_half[h - 1] + W.psi_vxy[q];
+            }
+        }
+    }
+    float *sec = A.sec + (long long)k * 5 * A.ns + (ins - 1);
+    sec[3 * A.ns] = (vxx + vyy) * sqrtf(M.ppi[mo + o]);
+    sec[4 * A.ns] = (vxy - vyx) * sqrtf(M.pu[mo + o]);
+}
+
+// vx, vy and p of seismo_ssg.c:36-62 after the step.
+__global__ void k_seis(Geo G, Wave W, Model M, Acq A, int ins, int seismo)
+{
+    int s = blockIdx.y;
+    int k = A.rec_off[s] + blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= A.rec_off[s + 1])
+        return;
+    long long o = cell(G, A.rec_iy[k], A.rec_ix[k]);
+    long long so = (long long)s * G.fsz, mo = moff(G, s);
+    float *sec = A.sec + (long long)k * 5 * A.ns + (ins - 1);
+    if (seismo == 1 || seismo == 4) {
+        sec[0] = W.vx[so + o];
+        sec[A.ns] = W.vy[so + o];
+    }
+    float p = -W.sxx[so + o] - W.syy[so + o];
+    if (seismo == 2)
+        sec[2 * A.ns] = p;
+    if (seismo == 4) {
+        float ppi = M.ppi[mo + o], pu = M.pu[mo + o];
+        sec[2 * A.ns] = ((3.0f * ppi - 4.0f * pu) / (2.0f * ppi - 2.0f * pu)) * p / 3.0f;
+    }
+}
+
+// snap_ssg.c:86-205: one snapshot frame, file order (x outer, y inner).
+template <int ND>
+__global__ void k_snap(Geo G, Wave W, Model M, float *out, int nsx, int nsy, int idx, int idy, int type,
+                       long long frame_stride)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = blockIdx.y;
+    if (t >= nsx * nsy)
+        return;
+    int i = 1 + (t / nsy) * idx, j = 1 + (t % nsy) * idy;
+    long long o = cell(G, j, i);
+    long long so = (long long)s * G.fsz, mo = moff(G, s);
+    const float *vx = W.vx + so, *vy = W.vy + so;
+    float *f = out + (long long)s * frame_stride;
+    long long n = (long long)nsx * nsy;
+    if (type == 1 || type == 4) {
+        f[t] = vx[o];
+        f[n + t] = vy[o];
+    }
+    if (type == 2 || type == 4)
+        f[2 * n + t] = -W.sxx[so + o] - W.syy[so + o];
+    if (type == 3 || type == 4) {
+        const int P = G.pitch;
+        float vyx = 0.f, vxy = 0.f, vxx = 0.f, vyy = 0.f;
+#pragma unroll
+        for (int m = 1; m <= ND; m++) {
+            vyx += G.hc[m] * (vy[o + m] - vy[o - m + 1]);
+            vxy += G.hc[m] * (vx[o + (long long)m * P] - vx[o - (long long)(m - 1) * P]);
+            vxx += G.hc[m] * (vx[o + m - 1] - vx[o - m]);
+            vyy += G.hc[m] * (vy[o + (long long)(m - 1) * P] - vy[o - (long long)m * P]);
+        }
+        f[4 * n + t] = (vxy * G.dhi - vyx * G.dhi) * sqrtf(M.pu[mo + o]);
+        f[3 * n + t] = (vxx * G.dhi + vyy * G.dhi) * sqrtf(M.ppi[mo + o]);
+    }
+}
+
+}  // namespace sofi

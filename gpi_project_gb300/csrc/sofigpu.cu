@@ -1,0 +1,911 @@
+// sofigpu.cu -- C ABI of the GB300 time-stepping library (see include/sofigpu.h).
+//
+// A context owns, on one device and one CUDA stream, the wavefields of
+// `nshots` resident shots, the prepared model (shared or per shot), the CPML
+// memory, the acquisition and the sections. sofi_run() issues the kernels of
+// sofi_kernels.cuh in the reference's phase order for each time step.
+#include "sofigpu.h"
+#include "sofi_kernels.cuh"
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace sofi;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return fail(e_ == cudaErrorMemoryAllocation ? SOFI_E_NOMEM : SOFI_E_CUDA, "%s: %s (%s:%d)", \
+                        #call, cudaGetErrorString(e_), __FILE__, __LINE__);                        \
+    } while (0)
+
+// Holberg / Taylor operator coefficients (reference holbergcoeff.c:40-82; the
+// published tables: Taylor row, then Holberg 1987 for 0.1%, 0.5%, 1%, 3%).
+const double kHolberg[5][6][7] = {
+    {{23.0, 1.0, 0, 0, 0, 0, 0},
+     {8.0, 9.0 / 8.0, -1.0 / 24.0, 0, 0, 0, 0},
+     {6.0, 75.0 / 64.0, -25.0 / 384.0, 3.0 / 640.0, 0, 0, 0},
+     {5.0, 1225.0 / 1024.0, -245.0 / 3072.0, 49.0 / 5120.0, -5.0 / 7168.0, 0, 0},
+     {5.0, 19845.0 / 16384.0, -735.0 / 8192.0, 567.0 / 40960.0, -405.0 / 229376.0, 35.0 / 294912.0, 0},
+     {4.0, 160083.0 / 131072.0, -12705.0 / 131072.0, 22869.0 / 1310720.0, -5445.0 / 1835008.0,
+      847.0 / 2359296.0, -63.0 / 2883584.0}},
+    {{49.7, 1.0010, 0, 0, 0, 0, 0},
+     {8.32, 1.1382, -0.046414, 0, 0, 0, 0},
+     {4.77, 1.1965, -0.078804, 0.0081781, 0, 0, 0},
+     {3.69, 1.2257, -0.099537, 0.018063, -0.0026274, 0, 0},
+     {3.19, 1.2415, -0.11231, 0.026191, -0.0064682, 0.001191, 0},
+     {2.91, 1.2508, -0.12034, 0.032131, -0.010142, 0.0029857, -0.00066667}},
+    {{22.2, 1.0050, 0, 0, 0, 0, 0},
+     {5.65, 1.1534, -0.052806, 0, 0, 0, 0},
+     {3.74, 1.2111, -0.088313, 0.011768, 0, 0, 0},
+     {3.11, 1.2367, -0.10815, 0.023113, -0.0046905, 0, 0},
+     {2.80, 1.2496, -0.11921, 0.031130, -0.0093272, 0.0025161, 0},
+     {2.62, 1.2568, -0.12573, 0.036423, -0.013132, 0.0047484, -0.0015979}},
+    {{15.8, 1.0100, 0, 0, 0, 0, 0},
+     {4.80, 1.1640, -0.057991, 0, 0, 0, 0},
+     {3.39, 1.2192, -0.094070, 0.014608, 0, 0, 0},
+     {2.90, 1.2422, -0.11269, 0.026140, -0.0064054, 0, 0},
+     {2.65, 1.2534, -0.12257, 0.033755, -0.011081, 0.0036784, 0},
+     {2.51, 1.2596, -0.12825, 0.038550, -0.014763, 0.0058619, -0.0024538}},
+    {{9.16, 1.0300, 0, 0, 0, 0, 0},
+     {3.47, 1.1876, -0.072518, 0, 0, 0, 0},
+     {2.91, 1.2341, -0.10569, 0.022589, 0, 0, 0},
+     {2.61, 1.2516, -0.12085, 0.032236, -0.011459, 0, 0},
+     {2.45, 1.2596, -0.12829, 0.038533, -0.014681, 0.0072580, 0},
+     {2.36, 1.2640, -0.13239, 0.042217, -0.017803, 0.0081959, -0.0051848}},
+};
+
+bool is_visco(int weq) { return weq == SOFI_VEL_ISO || weq == SOFI_VEL_VTI || weq == SOFI_VEL_TTI; }
+int kind_of(int weq) { return (weq == SOFI_EL_ISO || weq == SOFI_VEL_ISO) ? ISO : (weq <= SOFI_VEL_VTI ? VTI : TTI); }
+
+struct FieldSlot {
+    const char *name;   // ABI name
+    const char *alt;    // accepted alias (e.g. unrelaxed name for viscoelastic media)
+    size_t off;         // offset of the const float* in Model
+};
+
+#define SLOT(n, a, m) {n, a, offsetof(Model, m)}
+const FieldSlot kSlots[] = {
+    SLOT("prip", nullptr, prip), SLOT("prjp", nullptr, prjp), SLOT("g", nullptr, g), SLOT("f", nullptr, f),
+    SLOT("fipjp", nullptr, fipjp), SLOT("d_base", nullptr, db), SLOT("e_base", nullptr, eb),
+    SLOT("dip_base", nullptr, dipb), SLOT("c11", "c11u", c11), SLOT("c13", "c13u", c13),
+    SLOT("c33", "c33u", c33), SLOT("c15", "c15u", c15), SLOT("c35", "c35u", c35),
+    SLOT("c55ipjp", "c55ipjpu", c55ipjp), SLOT("c15ipjp", "c15ipjpu", c15ipjp),
+    SLOT("c35ipjp", "c35ipjpu", c35ipjp), SLOT("c11d_base", nullptr, c11b), SLOT("c13d_base", nullptr, c13b),
+    SLOT("c33d_base", nullptr, c33b), SLOT("c15d_base", nullptr, c15b), SLOT("c35d_base", nullptr, c35b),
+    SLOT("c55ipjpd_base", nullptr, c55ipjpb), SLOT("c15ipjpd_base", nullptr, c15ipjpb),
+    SLOT("c35ipjpd_base", nullptr, c35ipjpb), SLOT("ppi", nullptr, ppi), SLOT("pu", nullptr, pu),
+    SLOT("taus", nullptr, taus), SLOT("taup", nullptr, taup), SLOT("absorb", nullptr, absorb),
+};
+#undef SLOT
+
+const char *kVectors[12] = {"K_x", "a_x", "b_x", "K_x_half", "a_x_half", "b_x_half",
+                            "K_y", "a_y", "b_y", "K_y_half", "a_y_half", "b_y_half"};
+
+// which model slots a wave equation reads
+std::vector<std::string> needed_fields(const sofi_config &c)
+{
+    std::vector<std::string> v = {"prip", "prjp", "ppi", "pu"};
+    int k = kind_of(c.weq);
+    bool visco = is_visco(c.weq);
+    if (k == ISO) {
+        v.insert(v.end(), {"g", "f", "fipjp"});
+        if (visco) {
+            v.insert(v.end(), {"d_base", "e_base", "dip_base"});
+            if (c.free_surf)
+                v.insert(v.end(), {"taus", "taup"});
+        }
+    } else {
+        v.insert(v.end(), {"c11", "c13", "c33", "c55ipjp"});
+        if (k == TTI)
+            v.insert(v.end(), {"c15", "c35", "c15ipjp", "c35ipjp"});
+        if (visco) {
+            v.insert(v.end(), {"c11d_base", "c13d_base", "c33d_base", "c55ipjpd_base"});
+            if (k == TTI)
+                v.insert(v.end(), {"c15d_base", "c35d_base", "c15ipjpd_base", "c35ipjpd_base"});
+        }
+    }
+    if (c.fw > 0 && c.abs_type == 2)
+        v.push_back("absorb");
+    return v;
+}
+
+struct ShotAcq {
+    std::vector<int> ix, iy, type;
+    std::vector<float> amp, sn, cs, sn2, cs2, sig;
+    std::vector<int> rix, riy;
+};
+
+int pitch_for(int nx) { return ((nx + 2 * HX + 31) / 32) * 32; }
+
+}  // namespace
+
+struct sofi_ctx {
+    sofi_config cfg{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    Geo G{};
+    Wave W{};
+    Model M{};
+    Acq A{};
+    int nmodels = 1;
+    int nd = 2;
+    std::vector<void *> allocs;
+    std::vector<ShotAcq> acq;
+    bool acq_dirty = true;
+    bool has_force = false;
+    int total_src = 0, total_rec = 0;
+    void *acq_buf = nullptr;
+    float *d_sec = nullptr;
+    int *d_status = nullptr;
+    int step = 0;
+    float last_ms = 0.f;
+    // snapshots
+    int snap_nx = 0, snap_ny = 0, snap_total = 0, nsnap = 0;
+    float *d_snap = nullptr;
+};
+
+namespace {
+
+int dalloc(sofi_ctx *c, void **p, size_t bytes)
+{
+    if (bytes == 0)
+        bytes = 16;
+    cudaError_t e = cudaMallocAsync(p, bytes, c->stream);
+    if (e != cudaSuccess)
+        return fail(SOFI_E_NOMEM, "device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+    c->allocs.push_back(*p);
+    e = cudaMemsetAsync(*p, 0, bytes, c->stream);
+    if (e != cudaSuccess)
+        return fail(SOFI_E_CUDA, "memset: %s", cudaGetErrorString(e));
+    return 0;
+}
+
+const float **slot_ptr(Model &M, const char *name, bool visco)
+{
+    for (const auto &s : kSlots) {
+        if (!strcmp(s.name, name) || (s.alt && !strcmp(s.alt, name) && visco))
+            return reinterpret_cast<const float **>(reinterpret_cast<char *>(&M) + s.off);
+    }
+    return nullptr;
+}
+
+int count_snapshots(const sofi_config &c)
+{
+    if (!c.snap)
+        return 0;
+    int n = 0;
+    for (int nt = c.snap_first; nt <= c.snap_last && nt <= c.nt && nt >= 1; nt += (c.snap_inc > 0 ? c.snap_inc : c.nt + 1))
+        n++;
+    return n;
+}
+
+long long fields_bytes(const sofi_config &c)
+{
+    long long pitch = pitch_for(c.nx), fsz = pitch * (c.ny + 2 * HY);
+    long long per_shot = 5 + 3LL * (is_visco(c.weq) ? c.L : 0) + (kind_of(c.weq) == TTI ? 8 : 0);
+    long long fw2 = 2LL * c.fw;
+    long long psi = (c.abs_type == 1 && c.fw > 0) ? 4 * ((long long)c.ny * fw2 + fw2 * c.nx) : 0;
+    long long nmod = c.shared_model ? 1 : c.nshots;
+    long long nfields = (long long)needed_fields(c).size();
+    long long bytes = 4 * (fsz * per_shot * c.nshots + psi * c.nshots + fsz * nfields * nmod);
+    int nsnap = count_snapshots(c);
+    if (nsnap) {
+        long long sx = (c.nx - 1) / c.idx + 1, sy = (c.ny - 1) / c.idy + 1;
+        bytes += 4LL * sx * sy * 5 * nsnap * c.nshots;
+    }
+    return bytes;
+}
+
+int check_config(const sofi_config *c)
+{
+    if (!c)
+        return fail(SOFI_E_ARG, "null config");
+    if (c->weq < SOFI_EL_ISO || c->weq > SOFI_VEL_TTI)
+        return fail(SOFI_E_ARG, "unsupported WEQ %d (EL_ISO..VEL_TTI = 2..7)", c->weq);
+    if (c->fdorder < 2 || c->fdorder > 12 || (c->fdorder & 1))
+        return fail(SOFI_E_ARG, "FDORDER must be 2,4,..,12 (got %d)", c->fdorder);
+    if (c->maxrelerror < 0 || c->maxrelerror > 4)
+        return fail(SOFI_E_ARG, "MAXRELERROR must be 0..4");
+    int nd = c->fdorder / 2;
+    if (c->nx < 2 * nd + 2 || c->ny < 2 * nd + 2)
+        return fail(SOFI_E_ARG, "grid %dx%d too small for FDORDER %d", c->nx, c->ny, c->fdorder);
+    if (c->nt < 1 || c->nshots < 1 || c->dt <= 0.f || c->dh <= 0.f)
+        return fail(SOFI_E_ARG, "NT, nshots, DT and DH must be positive");
+    if (is_visco(c->weq) && (c->L < 1 || c->L > MAXL))
+        return fail(SOFI_E_ARG, "viscoelastic media need 1 <= L <= %d", MAXL);
+    if (c->fw < 0 || 2 * c->fw > c->nx || 2 * c->fw > c->ny)
+        return fail(SOFI_E_ARG, "frame width FW=%d does not fit the grid", c->fw);
+    if (c->fw > 0 && c->abs_type != 1 && c->abs_type != 2)
+        return fail(SOFI_E_ARG, "ABS_TYPE must be 1 (CPML) or 2 (damping)");
+    if (c->abs_type == 2 && c->fw == 1)
+        return fail(SOFI_E_ARG, "damping frame needs FW >= 2");
+    if (c->free_surf && is_visco(c->weq) && kind_of(c->weq) != ISO)
+        return fail(SOFI_E_ARG, "free surface is not defined for viscoelastic VTI/TTI media");
+    if (c->seismo < 0 || c->seismo > 4 || c->snap < 0 || c->snap > 4)
+        return fail(SOFI_E_ARG, "SEISMO and SNAP must be 0..4");
+    if (c->seismo && c->ndt < 1)
+        return fail(SOFI_E_ARG, "NDT must be >= 1");
+    if (c->snap && (c->idx < 1 || c->idy < 1))
+        return fail(SOFI_E_ARG, "IDX and IDY must be >= 1");
+    return 0;
+}
+
+int upload_acq(sofi_ctx *c)
+{
+    // flatten per-shot sources / receivers into one device block
+    int S = c->cfg.nshots, NT = c->cfg.nt;
+    std::vector<int> soff(S + 1, 0), roff(S + 1, 0), last(S, 0);
+    for (int s = 0; s < S; s++) {
+        soff[s + 1] = soff[s] + (int)c->acq[s].ix.size();
+        roff[s + 1] = roff[s] + (int)c->acq[s].rix.size();
+        last[s] = c->acq[s].type.empty() ? 0 : c->acq[s].type.back();
+    }
+    int ns_src = soff[S], nrec = roff[S];
+    c->has_force = false;
+    std::vector<int> ix, iy, ty, rix, riy;
+    std::vector<float> amp, sn, cs, sn2, cs2, sig;
+    for (int s = 0; s < S; s++) {
+        auto &a = c->acq[s];
+        ix.insert(ix.end(), a.ix.begin(), a.ix.end());
+        iy.insert(iy.end(), a.iy.begin(), a.iy.end());
+        ty.insert(ty.end(), a.type.begin(), a.type.end());
+        amp.insert(amp.end(), a.amp.begin(), a.amp.end());
+        sn.insert(sn.end(), a.sn.begin(), a.sn.end());
+        cs.insert(cs.end(), a.cs.begin(), a.cs.end());
+        sn2.insert(sn2.end(), a.sn2.begin(), a.sn2.end());
+        cs2.insert(cs2.end(), a.cs2.begin(), a.cs2.end());
+        sig.insert(sig.end(), a.sig.begin(), a.sig.end());
+        rix.insert(rix.end(), a.rix.begin(), a.rix.end());
+        riy.insert(riy.end(), a.riy.begin(), a.riy.end());
+        for (int t : a.type)
+            if (t >= 2 && t <= 4)
+                c->has_force = true;
+    }
+    // one allocation: ints then floats, 256-byte aligned pieces
+    auto al = [](size_t n) { return (n + 63) / 64 * 64; };
+    size_t ni = al(S + 1) * 2 + al(S) + al(ns_src) * 3 + al(nrec) * 2;
+    size_t nf = al(ns_src) * 5 + al((size_t)ns_src * NT);
+    std::vector<int> hi(ni, 0);
+    std::vector<float> hf(nf, 0.f);
+    size_t pi = 0, pf = 0;
+    auto puti = [&](const std::vector<int> &v, size_t n) { std::copy(v.begin(), v.end(), hi.begin() + pi); size_t o = pi; pi += al(n); return o; };
+    auto putf = [&](const std::vector<float> &v, size_t n) { std::copy(v.begin(), v.end(), hf.begin() + pf); size_t o = pf; pf += al(n); return o; };
+    size_t o_soff = puti(soff, S + 1), o_roff = puti(roff, S + 1), o_last = puti(last, S);
+    size_t o_ix = puti(ix, ns_src), o_iy = puti(iy, ns_src), o_ty = puti(ty, ns_src);
+    size_t o_rix = puti(rix, nrec), o_riy = puti(riy, nrec);
+    size_t o_amp = putf(amp, ns_src), o_sn = putf(sn, ns_src), o_cs = putf(cs, ns_src), o_sn2 = putf(sn2, ns_src),
+           o_cs2 = putf(cs2, ns_src), o_sig = putf(sig, (size_t)ns_src * NT);
+    if (c->acq_buf) {
+        CK(cudaFreeAsync(c->acq_buf, c->stream));
+        for (auto &p : c->allocs)
+            if (p == c->acq_buf)
+                p = nullptr;
+        c->acq_buf = nullptr;
+    }
+    if (c->d_sec) {
+        CK(cudaFreeAsync(c->d_sec, c->stream));
+        for (auto &p : c->allocs)
+            if (p == c->d_sec)
+                p = nullptr;
+        c->d_sec = nullptr;
+    }
+    void *buf;
+    int rc = dalloc(c, &buf, ni * sizeof(int) + nf * sizeof(float));
+    if (rc)
+        return rc;
+    c->acq_buf = buf;
+    CK(cudaMemcpyAsync(buf, hi.data(), ni * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    float *fb = reinterpret_cast<float *>(reinterpret_cast<char *>(buf) + ni * sizeof(int));
+    CK(cudaMemcpyAsync(fb, hf.data(), nf * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));  // host vectors go out of scope
+    int *ib = reinterpret_cast<int *>(buf);
+    Acq &A = c->A;
+    A.src_off = ib + o_soff, A.rec_off = ib + o_roff, A.last_type = ib + o_last;
+    A.src_ix = ib + o_ix, A.src_iy = ib + o_iy, A.src_type = ib + o_ty;
+    A.rec_ix = ib + o_rix, A.rec_iy = ib + o_riy;
+    A.src_amp = fb + o_amp, A.src_sin = fb + o_sn, A.src_cos = fb + o_cs, A.src_sin2 = fb + o_sn2,
+    A.src_cos2 = fb + o_cs2, A.signals = fb + o_sig;
+    A.nt = NT;
+    A.ns = c->cfg.ndt > 0 ? NT / c->cfg.ndt : 0;
+    float *sec;
+    rc = dalloc(c, (void **)&sec, sizeof(float) * (size_t)(nrec > 0 ? nrec : 1) * 5 * (A.ns > 0 ? A.ns : 1));
+    if (rc)
+        return rc;
+    c->d_sec = sec;
+    A.sec = sec;
+    A.status = c->d_status;
+    c->total_src = ns_src;
+    c->total_rec = nrec;
+    c->acq_dirty = false;
+    return 0;
+}
+
+dim3 grid2d(const sofi_ctx *c)
+{
+    return dim3((c->cfg.nx + BX - 1) / BX, (c->cfg.ny + BY - 1) / BY, c->cfg.nshots);
+}
+
+#define DISPATCH_ND(ND_, ...)                        \
+    switch (ND_) {                                  \
+      case 1: { constexpr int ND = 1; __VA_ARGS__; } break; \
+      case 2: { constexpr int ND = 2; __VA_ARGS__; } break; \
+      case 3: { constexpr int ND = 3; __VA_ARGS__; } break; \
+      case 4: { constexpr int ND = 4; __VA_ARGS__; } break; \
+      case 5: { constexpr int ND = 5; __VA_ARGS__; } break; \
+      case 6: { constexpr int ND = 6; __VA_ARGS__; } break; \
+    }
+
+int launch_step(sofi_ctx *c, int nt)
+{
+    const sofi_config &cf = c->cfg;
+    cudaStream_t st = c->stream;
+    Geo &G = c->G;
+    dim3 blk(BX, BY), grd = grid2d(c);
+    int S = cf.nshots;
+    int nb = (S + 127) / 128;
+    int kind = kind_of(cf.weq);
+    bool visco = is_visco(cf.weq);
+    if (c->has_force)
+        k_force_src<<<nb, 128, 0, st>>>(G, c->W, c->M, c->A, nt);
+    DISPATCH_ND(c->nd, (k_update_v<ND><<<grd, blk, 0, st>>>(G, c->W, c->M)));
+    if (cf.boundary)
+        k_wrap_x<<<dim3((cf.ny + 127) / 128, S), 128, 0, st>>>(G, c->W.vx, c->W.vy, nullptr, c->nd);
+    if (kind == TTI) {
+        DISPATCH_ND(c->nd, (k_tti_deriv<ND><<<grd, blk, 0, st>>>(G, c->W, c->M)));
+        if (visco)
+            k_update_s_tti<true><<<grd, blk, 0, st>>>(G, c->W, c->M);
+        else
+            k_update_s_tti<false><<<grd, blk, 0, st>>>(G, c->W, c->M);
+    } else if (kind == ISO) {
+        if (visco)
+            DISPATCH_ND(c->nd, (k_update_s<ND, ISO, true><<<grd, blk, 0, st>>>(G, c->W, c->M)))
+        else
+            DISPATCH_ND(c->nd, (k_update_s<ND, ISO, false><<<grd, blk, 0, st>>>(G, c->W, c->M)))
+    } else {
+        if (visco)
+            DISPATCH_ND(c->nd, (k_update_s<ND, VTI, true><<<grd, blk, 0, st>>>(G, c->W, c->M)))
+        else
+            DISPATCH_ND(c->nd, (k_update_s<ND, VTI, false><<<grd, blk, 0, st>>>(G, c->W, c->M)))
+    }
+    bool sample = cf.seismo && c->total_rec > 0 && nt % cf.ndt == 0 && nt < cf.nt;
+    int ins = sample ? nt / cf.ndt : 0;
+    int maxrec = 0;
+    for (auto &a : c->acq)
+        maxrec = std::max(maxrec, (int)a.rix.size());
+    dim3 rg((maxrec + 127) / 128, S);
+    if (sample && (cf.seismo == 3 || cf.seismo == 4)) {
+        if (kind == TTI)
+            DISPATCH_ND(c->nd, (k_seis_deriv<ND, true><<<rg, 128, 0, st>>>(G, c->W, c->M, c->A, ins)))
+        else
+            DISPATCH_ND(c->nd, (k_seis_deriv<ND, false><<<rg, 128, 0, st>>>(G, c->W, c->M, c->A, ins)))
+    }
+    k_stress_src<<<nb, 128, 0, st>>>(G, c->W, c->A, nt);
+    if (cf.free_surf) {
+        dim3 sg((cf.nx + 127) / 128, S);
+        if (visco)
+            DISPATCH_ND(c->nd, (k_surface<ND, true><<<sg, 128, 0, st>>>(G, c->W, c->M)))
+        else
+            DISPATCH_ND(c->nd, (k_surface<ND, false><<<sg, 128, 0, st>>>(G, c->W, c->M)))
+    }
+    if (cf.boundary)
+        k_wrap_x<<<dim3((cf.ny + 127) / 128, S), 128, 0, st>>>(G, c->W.sxx, c->W.syy, c->W.sxy, c->nd);
+    if (sample && cf.seismo != 3)
+        k_seis<<<rg, 128, 0, st>>>(G, c->W, c->M, c->A, ins, cf.seismo);
+    if (cf.snap && nt >= cf.snap_first && nt <= cf.snap_last &&
+        (nt == cf.snap_first || (cf.snap_inc > 0 && (nt - cf.snap_first) % cf.snap_inc == 0)) &&
+        c->nsnap < c->snap_total) {
+        long long n = (long long)c->snap_nx * c->snap_ny;
+        long long frame_stride = n * 5 * c->snap_total;
+        float *out = c->d_snap + (long long)c->nsnap * 5 * n;
+        dim3 sg((unsigned)((n + 127) / 128), S);
+        DISPATCH_ND(c->nd, (k_snap<ND><<<sg, 128, 0, st>>>(G, c->W, c->M, out, c->snap_nx, c->snap_ny, cf.idx,
+                                                          cf.idy, cf.snap, frame_stride)));
+        c->nsnap++;
+    }
+    return 0;
+}
+
+int check_status(sofi_ctx *c)
+{
+    std::vector<int> st(c->cfg.nshots);
+    CK(cudaMemcpyAsync(st.data(), c->d_status, sizeof(int) * st.size(), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int s = 0; s < c->cfg.nshots; s++)
+        if (st[s])
+            return fail(SOFI_E_UNSTABLE, "shot %d: simulation is unstable (NaN at the probe cell after step %d)", s,
+                        st[s]);
+    return 0;
+}
+
+int copy_2d_in(sofi_ctx *c, float *dst, const float *host, long rs, long cs)
+{
+    const sofi_config &cf = c->cfg;
+    float *d0 = dst + (long long)HY * c->G.pitch + HX;
+    if (cs == 1) {
+        CK(cudaMemcpy2DAsync(d0, sizeof(float) * c->G.pitch, host, sizeof(float) * rs, sizeof(float) * cf.nx, cf.ny,
+                             cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        return 0;
+    }
+    std::vector<float> tmp((size_t)cf.nx * cf.ny);
+    for (int j = 0; j < cf.ny; j++)
+        for (int i = 0; i < cf.nx; i++)
+            tmp[(size_t)j * cf.nx + i] = host[(long long)j * rs + (long long)i * cs];
+    CK(cudaMemcpy2DAsync(d0, sizeof(float) * c->G.pitch, tmp.data(), sizeof(float) * cf.nx, sizeof(float) * cf.nx,
+                         cf.ny, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+float *field_ptr(sofi_ctx *c, int shot, const char *name)
+{
+    long long so = (long long)shot * c->G.fsz;
+    if (!strcmp(name, "vx")) return c->W.vx + so;
+    if (!strcmp(name, "vy")) return c->W.vy + so;
+    if (!strcmp(name, "sxx")) return c->W.sxx + so;
+    if (!strcmp(name, "syy")) return c->W.syy + so;
+    if (!strcmp(name, "sxy")) return c->W.sxy + so;
+    size_t n = strlen(name);
+    if ((name[0] == 'r' || name[0] == 'p' || name[0] == 'q') && n == 2 && name[1] >= '1' && name[1] <= '8') {
+        int l = name[1] - '1';
+        if (l >= c->G.L)
+            return nullptr;
+        float *b = name[0] == 'r' ? c->W.r : (name[0] == 'p' ? c->W.p : c->W.q);
+        return b + ((long long)shot * c->G.L + l) * c->G.fsz;
+    }
+    return nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *sofi_last_error(void) { return g_err.c_str(); }
+int sofi_abi_version(void) { return SOFI_ABI_VERSION; }
+
+int sofi_device_bytes(const sofi_config *cfg, long long *bytes)
+{
+    int rc = check_config(cfg);
+    if (rc)
+        return rc;
+    *bytes = fields_bytes(*cfg);
+    return 0;
+}
+
+int sofi_create(const sofi_config *cfg, int device, sofi_ctx **out)
+{
+    if (!out)
+        return fail(SOFI_E_ARG, "null output pointer");
+    *out = nullptr;
+    int rc = check_config(cfg);
+    if (rc)
+        return rc;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(SOFI_E_NODEV, "no CUDA device available: %s", cudaGetErrorString(e));
+    if (device < 0 || device >= ndev)
+        return fail(SOFI_E_ARG, "device %d out of range (%d devices)", device, ndev);
+    CK(cudaSetDevice(device));
+    sofi_ctx *c = new sofi_ctx();
+    c->cfg = *cfg;
+    c->device = device;
+    c->nd = cfg->fdorder / 2;
+    c->nmodels = cfg->shared_model ? 1 : cfg->nshots;
+    c->acq.resize(cfg->nshots);
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return fail(SOFI_E_CUDA, "stream creation: %s", cudaGetErrorString(e));
+    }
+    cudaEventCreate(&c->ev0);
+    cudaEventCreate(&c->ev1);
+    Geo &G = c->G;
+    G.nx = cfg->nx, G.ny = cfg->ny, G.pitch = pitch_for(cfg->nx), G.nshots = cfg->nshots;
+    G.fsz = (long long)G.pitch * (cfg->ny + 2 * HY);
+    G.fw = cfg->fw, G.fw2 = 2 * cfg->fw;
+    G.abs_type = cfg->fw > 0 ? cfg->abs_type : 0;
+    G.free_surf = cfg->free_surf, G.boundary = cfg->boundary;
+    G.L = is_visco(cfg->weq) ? cfg->L : 0;
+    G.model_stride_on = cfg->shared_model ? 0 : 1;
+    G.el_tti_rb_short = (cfg->weq == SOFI_EL_TTI);
+    // subgrid_bounds.c:65-66,260-270 (one rank); without a frame the whole grid is interior
+    int fw = G.abs_type ? cfg->fw : 0;
+    G.gx2 = fw, G.gx3 = cfg->nx - fw, G.gy2 = fw, G.gy3 = cfg->ny - fw;
+    if (cfg->free_surf)
+        G.gy2 = 0;
+    if (cfg->boundary)
+        G.gx2 = 0, G.gx3 = cfg->nx;
+    G.dt = cfg->dt, G.dh = cfg->dh;
+    G.dtdh = cfg->dt / cfg->dh;
+    G.dhi = 1.0f / cfg->dh;
+    G.dthalbe = cfg->dt / 2.0f;
+    for (int k = 0; k < 7; k++)
+        G.hc[k] = (float)kHolberg[cfg->maxrelerror][c->nd - 1][k];
+    // wavefields
+    size_t f = (size_t)G.fsz * cfg->nshots * sizeof(float);
+    float **w[5] = {&c->W.vx, &c->W.vy, &c->W.sxx, &c->W.syy, &c->W.sxy};
+    for (auto p : w)
+        if ((rc = dalloc(c, (void **)p, f)))
+            goto bad;
+    if (G.L) {
+        float **m[3] = {&c->W.r, &c->W.p, &c->W.q};
+        for (auto p : m)
+            if ((rc = dalloc(c, (void **)p, f * G.L)))
+                goto bad;
+    }
+    if (G.abs_type == 1) {
+        size_t px = sizeof(float) * (size_t)cfg->nshots * cfg->ny * G.fw2;
+        size_t py = sizeof(float) * (size_t)cfg->nshots * G.fw2 * cfg->nx;
+        float **a[4] = {&c->W.psi_sxx_x, &c->W.psi_sxy_x, &c->W.psi_vxx, &c->W.psi_vyx};
+        float **b[4] = {&c->W.psi_syy_y, &c->W.psi_sxy_y, &c->W.psi_vyy, &c->W.psi_vxy};
+        for (auto p : a)
+            if ((rc = dalloc(c, (void **)p, px)))
+                goto bad;
+        for (auto p : b)
+            if ((rc = dalloc(c, (void **)p, py)))
+                goto bad;
+        // profile vectors: 12 x 2FW, one block
+        float *pv;
+        if ((rc = dalloc(c, (void **)&pv, sizeof(float) * 12 * G.fw2)))
+            goto bad;
+        const float **slots[12] = {&c->M.K_x, &c->M.a_x, &c->M.b_x, &c->M.K_x_half, &c->M.a_x_half,
+                                   &c->M.b_x_half, &c->M.K_y, &c->M.a_y, &c->M.b_y, &c->M.K_y_half,
+                                   &c->M.a_y_half, &c->M.b_y_half};
+        for (int k = 0; k < 12; k++)
+            *slots[k] = pv + (size_t)k * G.fw2;
+    }
+    if (kind_of(cfg->weq) == TTI) {
+        if ((rc = dalloc(c, (void **)&c->W.draw, f * 4)) || (rc = dalloc(c, (void **)&c->W.dcor, f * 4)))
+            goto bad;
+    }
+    for (const auto &n : needed_fields(*cfg)) {
+        float *p;
+        if ((rc = dalloc(c, (void **)&p, (size_t)G.fsz * c->nmodels * sizeof(float))))
+            goto bad;
+        *slot_ptr(c->M, n.c_str(), true) = p;
+    }
+    if ((rc = dalloc(c, (void **)&c->d_status, sizeof(int) * cfg->nshots)))
+        goto bad;
+    c->A.status = c->d_status;
+    c->snap_total = count_snapshots(*cfg);
+    if (c->snap_total) {
+        c->snap_nx = (cfg->nx - 1) / cfg->idx + 1;
+        c->snap_ny = (cfg->ny - 1) / cfg->idy + 1;
+        size_t n = (size_t)c->snap_nx * c->snap_ny * 5 * c->snap_total * cfg->nshots;
+        if ((rc = dalloc(c, (void **)&c->d_snap, n * sizeof(float))))
+            goto bad;
+    }
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        rc = fail(SOFI_E_CUDA, "initialisation: %s", cudaGetErrorString(e));
+        goto bad;
+    }
+    *out = c;
+    return 0;
+bad:
+    sofi_destroy(c);
+    return rc;
+}
+
+int sofi_destroy(sofi_ctx *c)
+{
+    if (!c)
+        return 0;
+    cudaSetDevice(c->device);
+    if (c->stream) {
+        for (void *p : c->allocs)
+            if (p)
+                cudaFreeAsync(p, c->stream);
+        cudaStreamSynchronize(c->stream);
+        cudaStreamDestroy(c->stream);
+    }
+    if (c->ev0)
+        cudaEventDestroy(c->ev0);
+    if (c->ev1)
+        cudaEventDestroy(c->ev1);
+    delete c;
+    return 0;
+}
+
+int sofi_set_hc(sofi_ctx *c, const float *hc)
+{
+    if (!c || !hc)
+        return fail(SOFI_E_ARG, "null argument");
+    for (int k = 0; k < 7; k++)
+        c->G.hc[k] = hc[k];
+    return 0;
+}
+
+int sofi_set_model_field(sofi_ctx *c, int model, const char *name, const float *host, long row_stride,
+                         long col_stride)
+{
+    if (!c || !name || !host)
+        return fail(SOFI_E_ARG, "null argument");
+    if (model < 0 || model >= c->nmodels)
+        return fail(SOFI_E_ARG, "model index %d out of range (%d models)", model, c->nmodels);
+    CK(cudaSetDevice(c->device));
+    const float **slot = slot_ptr(c->M, name, is_visco(c->cfg.weq));
+    if (!slot)
+        return fail(SOFI_E_ARG, "unknown model field '%s'", name);
+    if (!*slot)
+        return fail(SOFI_E_ARG, "model field '%s' is not used by this wave equation", name);
+    float *dst = const_cast<float *>(*slot) + (long long)model * c->G.fsz;
+    return copy_2d_in(c, dst, host, row_stride, col_stride);
+}
+
+int sofi_set_model_vector(sofi_ctx *c, const char *name, const float *host, int n)
+{
+    if (!c || !name || !host)
+        return fail(SOFI_E_ARG, "null argument");
+    CK(cudaSetDevice(c->device));
+    if (!strcmp(name, "bip") || !strcmp(name, "cip") || !strcmp(name, "peta")) {
+        if (n != c->G.L)
+            return fail(SOFI_E_ARG, "%s needs L=%d values", name, c->G.L);
+        float *d = !strcmp(name, "bip") ? c->M.bip : (!strcmp(name, "cip") ? c->M.cip : c->M.peta);
+        for (int l = 0; l < n; l++)
+            d[l] = host[l];
+        return 0;
+    }
+    const float **slots[12] = {&c->M.K_x, &c->M.a_x, &c->M.b_x, &c->M.K_x_half, &c->M.a_x_half, &c->M.b_x_half,
+                               &c->M.K_y, &c->M.a_y, &c->M.b_y, &c->M.K_y_half, &c->M.a_y_half, &c->M.b_y_half};
+    for (int k = 0; k < 12; k++)
+        if (!strcmp(name, kVectors[k])) {
+            if (c->G.abs_type != 1)
+                return fail(SOFI_E_ARG, "CPML profile '%s' given without a CPML frame", name);
+            if (n != c->G.fw2)
+                return fail(SOFI_E_ARG, "%s needs 2*FW=%d values", name, c->G.fw2);
+            CK(cudaMemcpyAsync(const_cast<float *>(*slots[k]), host, sizeof(float) * n, cudaMemcpyHostToDevice,
+                               c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            return 0;
+        }
+    return fail(SOFI_E_ARG, "unknown model vector '%s'", name);
+}
+
+int sofi_set_sources(sofi_ctx *c, int shot, int nsrc, const float *srcpos, const float *signals)
+{
+    if (!c || shot < 0 || shot >= c->cfg.nshots || nsrc < 0 || (nsrc && (!srcpos || !signals)))
+        return fail(SOFI_E_ARG, "invalid source arguments");
+    ShotAcq &a = c->acq[shot];
+    a.ix.assign(nsrc, 0), a.iy.assign(nsrc, 0), a.type.assign(nsrc, 0);
+    a.amp.assign(nsrc, 0.f), a.sn.assign(nsrc, 0.f), a.cs.assign(nsrc, 0.f), a.sn2.assign(nsrc, 0.f),
+        a.cs2.assign(nsrc, 0.f);
+    a.sig.assign(signals, signals + (size_t)nsrc * c->cfg.nt);
+    for (int k = 0; k < nsrc; k++) {
+        int ix = (int)srcpos[0 * nsrc + k], iy = (int)srcpos[1 * nsrc + k], t = (int)srcpos[7 * nsrc + k];
+        if (ix < 1 || ix > c->cfg.nx || iy < 1 || iy > c->cfg.ny)
+            return fail(SOFI_E_ARG, "source %d at grid (%d,%d) outside 1..%d x 1..%d", k, ix, iy, c->cfg.nx,
+                        c->cfg.ny);
+        if (t < 1 || t > 5)
+            return fail(SOFI_E_ARG, "source %d has unsupported type %d", k, t);
+        if (t == 5 && (iy < 2 || ix < 2))
+            return fail(SOFI_E_ARG, "moment-tensor source %d needs i, j >= 2", k);
+        a.ix[k] = ix, a.iy[k] = iy, a.type[k] = t;
+        a.amp[k] = srcpos[5 * nsrc + k];
+        // update_v_interior.c:55 (azimuth, float radians) and eqsource.c:39 (dip)
+        float azi_rad = (float)(srcpos[6 * nsrc + k] * M_PI / 180);
+        a.sn[k] = (float)sin(azi_rad), a.cs[k] = (float)cos(azi_rad);
+        float dip = (float)(srcpos[6 * nsrc + k] * M_PI / 180.0);
+        a.sn2[k] = (float)sin(2 * dip), a.cs2[k] = (float)cos(2 * dip);
+    }
+    c->acq_dirty = true;
+    return 0;
+}
+
+int sofi_set_receivers(sofi_ctx *c, int shot, int ntr, const int *ix, const int *iy)
+{
+    if (!c || shot < 0 || shot >= c->cfg.nshots || ntr < 0 || (ntr && (!ix || !iy)))
+        return fail(SOFI_E_ARG, "invalid receiver arguments");
+    for (int k = 0; k < ntr; k++)
+        if (ix[k] < 1 || ix[k] > c->cfg.nx || iy[k] < 1 || iy[k] > c->cfg.ny)
+            return fail(SOFI_E_ARG, "receiver %d at grid (%d,%d) outside the grid", k, ix[k], iy[k]);
+    c->acq[shot].rix.assign(ix, ix + ntr);
+    c->acq[shot].riy.assign(iy, iy + ntr);
+    c->acq_dirty = true;
+    return 0;
+}
+
+int sofi_reset(sofi_ctx *c, int shot)
+{
+    if (!c || shot < -1 || shot >= c->cfg.nshots)
+        return fail(SOFI_E_ARG, "invalid shot");
+    CK(cudaSetDevice(c->device));
+    int s0 = shot < 0 ? 0 : shot, s1 = shot < 0 ? c->cfg.nshots : shot + 1;
+    size_t f = (size_t)c->G.fsz * sizeof(float);
+    for (int s = s0; s < s1; s++) {
+        float *w[5] = {c->W.vx, c->W.vy, c->W.sxx, c->W.syy, c->W.sxy};
+        for (auto p : w)
+            CK(cudaMemsetAsync(p + (long long)s * c->G.fsz, 0, f, c->stream));
+        if (c->G.L) {
+            float *m[3] = {c->W.r, c->W.p, c->W.q};
+            for (auto p : m)
+                CK(cudaMemsetAsync(p + (long long)s * c->G.L * c->G.fsz, 0, f * c->G.L, c->stream));
+        }
+        if (c->G.abs_type == 1) {
+            size_t px = sizeof(float) * (size_t)c->cfg.ny * c->G.fw2, py = sizeof(float) * (size_t)c->G.fw2 * c->cfg.nx;
+            float *a[4] = {c->W.psi_sxx_x, c->W.psi_sxy_x, c->W.psi_vxx, c->W.psi_vyx};
+            float *b[4] = {c->W.psi_syy_y, c->W.psi_sxy_y, c->W.psi_vyy, c->W.psi_vxy};
+            for (auto p : a)
+                CK(cudaMemsetAsync(reinterpret_cast<char *>(p) + s * px, 0, px, c->stream));
+            for (auto p : b)
+                CK(cudaMemsetAsync(reinterpret_cast<char *>(p) + s * py, 0, py, c->stream));
+        }
+        if (c->W.draw) {
+            CK(cudaMemsetAsync(c->W.draw + 4LL * s * c->G.fsz, 0, 4 * f, c->stream));
+            CK(cudaMemsetAsync(c->W.dcor + 4LL * s * c->G.fsz, 0, 4 * f, c->stream));
+        }
+    }
+    CK(cudaMemsetAsync(c->d_status, 0, sizeof(int) * c->cfg.nshots, c->stream));
+    if (c->d_sec && !c->acq_dirty) {
+        size_t n = (size_t)c->total_rec * 5 * (c->A.ns > 0 ? c->A.ns : 1);
+        CK(cudaMemsetAsync(c->d_sec, 0, n * sizeof(float), c->stream));
+    }
+    c->step = 0;
+    c->nsnap = 0;
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int sofi_run(sofi_ctx *c, int nsteps)
+{
+    if (!c || nsteps < 0)
+        return fail(SOFI_E_ARG, "invalid run arguments");
+    if (c->step + nsteps > c->cfg.nt)
+        return fail(SOFI_E_ARG, "step %d + %d exceeds NT=%d", c->step, nsteps, c->cfg.nt);
+    CK(cudaSetDevice(c->device));
+    if (c->G.abs_type == 1 && !c->M.K_x)
+        return fail(SOFI_E_STATE, "CPML profiles not set");
+    if (c->acq_dirty) {
+        int rc = upload_acq(c);
+        if (rc)
+            return rc;
+    }
+    CK(cudaEventRecord(c->ev0, c->stream));
+    for (int k = 0; k < nsteps; k++) {
+        int rc = launch_step(c, c->step + 1);
+        if (rc)
+            return rc;
+        c->step++;
+    }
+    CK(cudaEventRecord(c->ev1, c->stream));
+    CK(cudaGetLastError());
+    return 0;
+}
+
+int sofi_synchronize(sofi_ctx *c)
+{
+    if (!c)
+        return fail(SOFI_E_ARG, "null context");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1);
+    return check_status(c);
+}
+
+int sofi_current_step(sofi_ctx *c, int *step)
+{
+    if (!c || !step)
+        return fail(SOFI_E_ARG, "null argument");
+    *step = c->step;
+    return 0;
+}
+
+int sofi_num_samples(sofi_ctx *c, int *ns)
+{
+    if (!c || !ns)
+        return fail(SOFI_E_ARG, "null argument");
+    *ns = c->cfg.ndt > 0 ? c->cfg.nt / c->cfg.ndt : 0;
+    return 0;
+}
+
+int sofi_get_section(sofi_ctx *c, int shot, int comp, float *host)
+{
+    if (!c || !host || shot < 0 || shot >= c->cfg.nshots || comp < 1 || comp > 5)
+        return fail(SOFI_E_ARG, "invalid section arguments");
+    CK(cudaSetDevice(c->device));
+    if (c->acq_dirty) {
+        int rc = upload_acq(c);
+        if (rc)
+            return rc;
+    }
+    int rc = sofi_synchronize(c);
+    if (rc)
+        return rc;
+    int r0 = 0;
+    for (int s = 0; s < shot; s++)
+        r0 += (int)c->acq[s].rix.size();
+    int ntr = (int)c->acq[shot].rix.size(), ns = c->A.ns;
+    if (!ntr || !ns)
+        return 0;
+    CK(cudaMemcpy2DAsync(host, sizeof(float) * ns, c->d_sec + ((size_t)r0 * 5 + (comp - 1)) * ns,
+                         sizeof(float) * 5 * ns, sizeof(float) * ns, ntr, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int sofi_get_field(sofi_ctx *c, int shot, const char *name, float *host)
+{
+    if (!c || !name || !host || shot < 0 || shot >= c->cfg.nshots)
+        return fail(SOFI_E_ARG, "invalid field arguments");
+    CK(cudaSetDevice(c->device));
+    float *p = field_ptr(c, shot, name);
+    if (!p)
+        return fail(SOFI_E_ARG, "unknown wavefield '%s'", name);
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy2DAsync(host, sizeof(float) * c->cfg.nx, p + (long long)HY * c->G.pitch + HX,
+                         sizeof(float) * c->G.pitch, sizeof(float) * c->cfg.nx, c->cfg.ny, cudaMemcpyDeviceToHost,
+                         c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int sofi_set_field(sofi_ctx *c, int shot, const char *name, const float *host)
+{
+    if (!c || !name || !host || shot < 0 || shot >= c->cfg.nshots)
+        return fail(SOFI_E_ARG, "invalid field arguments");
+    CK(cudaSetDevice(c->device));
+    float *p = field_ptr(c, shot, name);
+    if (!p)
+        return fail(SOFI_E_ARG, "unknown wavefield '%s'", name);
+    return copy_2d_in(c, p, host, c->cfg.nx, 1);
+}
+
+int sofi_num_snapshots(sofi_ctx *c, int *count, int *frame_size)
+{
+    if (!c)
+        return fail(SOFI_E_ARG, "null context");
+    if (count)
+        *count = c->nsnap;
+    if (frame_size)
+        *frame_size = c->snap_nx * c->snap_ny;
+    return 0;
+}
+
+int sofi_get_snapshot(sofi_ctx *c, int shot, int k, int comp, float *host)
+{
+    if (!c || !host || shot < 0 || shot >= c->cfg.nshots || k < 0 || k >= c->nsnap || comp < 1 || comp > 5)
+        return fail(SOFI_E_ARG, "invalid snapshot arguments");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    long long n = (long long)c->snap_nx * c->snap_ny;
+    const float *src = c->d_snap + (long long)shot * n * 5 * c->snap_total + ((long long)k * 5 + (comp - 1)) * n;
+    CK(cudaMemcpyAsync(host, src, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int sofi_last_run_ms(sofi_ctx *c, float *ms)
+{
+    if (!c || !ms)
+        return fail(SOFI_E_ARG, "null argument");
+    int rc = sofi_synchronize(c);
+    *ms = c->last_ms;
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,175 @@
+/*
+ * sofigpu.h -- C ABI of the GB300 time-stepping library (libsofigpu.so).
+ *
+ * The library replaces the per-shot time loop of SOFI2D,
+ *     void time_loop(int iter, int ishot, int snapcheck, float *hc, float **srcpos_loc,
+ *                    float **signalx, float **signaly, int nsrc, int sw, AcqVar *acq,
+ *                    MemModel *mpm, MemWavefield *mpw, MemInv *minv, GlobVar *gv,
+ *                    GlobVarInv *vinv, Perform *perf)
+ * (reference src/fd.h:335-337, src/time_loop.c:27-326), by device kernels on one
+ * GPU. Inputs are what time_loop() reads: the prepared model arrays of MemModel
+ * (after prepmod.c / PML_pro.c / absorb.c), the sources and signals of the shot,
+ * the receiver grid positions; outputs are what it writes: the seismogram
+ * sections (gv->SECTIONVX/VY/P/DIV/CURL), the final wavefield and the snapshots.
+ *
+ * Conventions
+ *  - Every call returns 0 on success or a SOFI_E_* code; sofi_last_error() gives
+ *    the message of the calling thread's last failure. Nothing calls exit().
+ *  - Grid indices are the reference's: i = 1..NX (x), j = 1..NY (y, depth).
+ *  - 2-D host arrays are passed as a pointer to element (j=1, i=1) plus a row
+ *    stride and a column stride in floats, so a reference matrix m can be passed
+ *    as (&m[1][1], NX + 2*ND, 1) and an f3tensor plane l as
+ *    (&t[1][1][l], (NX + 2*ND) * L, L).
+ *  - One context holds `nshots` resident shots of one configuration; the model
+ *    is shared by all shots or given per shot (sofi_config.shared_model).
+ *  - A context is used by one host thread at a time. All device work of a
+ *    context is ordered on its own CUDA stream.
+ */
+#ifndef SOFIGPU_H
+#define SOFIGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SOFI_ABI_VERSION 1
+
+/* status codes */
+#define SOFI_OK 0
+#define SOFI_E_ARG 1       /* invalid argument or configuration */
+#define SOFI_E_CUDA 2      /* a CUDA runtime call failed */
+#define SOFI_E_STATE 3     /* call out of order (e.g. run before sources) */
+#define SOFI_E_NOMEM 4     /* device allocation failed */
+#define SOFI_E_UNSTABLE 5  /* NaN at the probe cell: reference time_loop.c:44-47 */
+#define SOFI_E_NODEV 6     /* no CUDA device / driver */
+
+/* wave equations: reference src/enums.h:22-31 */
+#define SOFI_EL_ISO 2
+#define SOFI_VEL_ISO 3
+#define SOFI_EL_VTI 4
+#define SOFI_VEL_VTI 5
+#define SOFI_EL_TTI 6
+#define SOFI_VEL_TTI 7
+
+/* seismogram components (gv->SECTIONVX, VY, P, DIV, CURL) */
+#define SOFI_COMP_VX 1
+#define SOFI_COMP_VY 2
+#define SOFI_COMP_P 3
+#define SOFI_COMP_DIV 4
+#define SOFI_COMP_CURL 5
+
+typedef struct sofi_ctx sofi_ctx;
+
+/* The GlobVar fields time_loop() reads (reference src/globvar_struct.h:40-203). */
+typedef struct {
+    int weq;            /* SOFI_EL_ISO .. SOFI_VEL_TTI                         (gv->WEQ) */
+    int nx, ny;         /* interior grid                                    (gv->NX, NY) */
+    int fdorder;        /* 2,4,...,12                                       (gv->FDORDER) */
+    int maxrelerror;    /* 0..4 Holberg table row                       (gv->MAXRELERROR) */
+    int L;              /* relaxation mechanisms (viscoelastic only)             (gv->L) */
+    float dt, dh;       /*                                                 (gv->DT, DH) */
+    int nt;             /* time steps per shot                                  (gv->NT) */
+    int fw;             /* absorbing frame width                                (gv->FW) */
+    int abs_type;       /* 1 CPML, 2 exponential damping                  (gv->ABS_TYPE) */
+    int free_surf;      /* stress-free top edge                          (gv->FREE_SURF) */
+    int boundary;       /* 1 = periodic in x                              (gv->BOUNDARY) */
+    int seismo;         /* 0 off, 1 v, 2 p, 3 div/curl, 4 all               (gv->SEISMO) */
+    int ndt;            /* sampling interval in steps                          (gv->NDT) */
+    int snap;           /* 0 off, 1 v, 2 p, 3 div/curl, 4 all                 (gv->SNAP) */
+    int snap_first;     /* first snapshot step  iround(TSNAP1/DT)  (time_loop.c:38) */
+    int snap_inc;       /* snapshot increment   iround(TSNAPINC/DT)(time_loop.c:39) */
+    int snap_last;      /* last snapshot step   iround(TSNAP2/DT)  (time_loop.c:40) */
+    int idx, idy;       /* snapshot subsampling                          (gv->IDX, IDY) */
+    int nshots;         /* resident shots in this context (>= 1) */
+    int shared_model;   /* 1: one model for all shots, 0: one model per shot */
+} sofi_config;
+
+/* ---- context ---------------------------------------------------------- */
+
+/* Check the configuration, select `device`, allocate every device array the
+ * time loop needs (wavefields zeroed) and create the context's stream. */
+int sofi_create(const sofi_config *cfg, int device, sofi_ctx **out);
+int sofi_destroy(sofi_ctx *ctx);
+const char *sofi_last_error(void);
+int sofi_abi_version(void);
+/* Device bytes the context holds (for admission by HBM budget). */
+int sofi_device_bytes(const sofi_config *cfg, long long *bytes);
+
+/* ---- model: the prepared MemModel arrays (reference src/memm_struct.h) ---- */
+
+/* Holberg coefficients hc[0..6] (reference holbergcoeff.c:38-100). Set by
+ * sofi_create from (fdorder, maxrelerror); this call overrides them. */
+int sofi_set_hc(sofi_ctx *ctx, const float *hc);
+
+/* A 2-D model array, interior 1..NY x 1..NX. `model` is 0 for a shared model,
+ * else the shot index. Names follow MemModel:
+ *   prip prjp                 reciprocal averaged density (av_rho.c)
+ *   g f fipjp                 DT-scaled (unrelaxed) moduli (prepare_update_s_*.c)
+ *   ppi pu                    pi, mu (free surface, div/curl, p sampling); for
+ *                             anisotropic media these are c11 and c55
+ *                             (initmem_model.c:87-91 aliases them)
+ *   taus taup                 (viscoelastic free surface, surface.c)
+ *   c11 c13 c33 c15 c35 c55ipjp c15ipjp c35ipjp            (elastic VTI/TTI, DT-scaled)
+ *   c11u c13u c33u c15u c35u c55ipjpu c15ipjpu c35ipjpu    (viscoelastic VTI/TTI)
+ *   absorb                    absorb_coeff of the damping frame (absorb.c)
+ * Viscoelastic modulus defects: the reference stores one array per mechanism,
+ * e.g. d[j][i][l] = pu * peta[l] * ptaus (prepare_update_s_visc.c:41-43). The
+ * device stores the mechanism-independent factor once and multiplies by
+ * peta[l] in the kernel, so L planes per defect cost one array of traffic:
+ *   d_base = pu*taus   e_base = ppi*taup   dip_base = puipjp*tausipjp   (isotropic)
+ *   c11d_base = c11*tau11, c13d_base, c33d_base, c55ipjpd_base              (VTI)
+ *   + c15d_base c35d_base c15ipjpd_base c35ipjpd_base                       (TTI)
+ * (relaxed moduli times tau; prepare_update_s_vti.c:40-43, _tti.c:40-55). */
+int sofi_set_model_field(sofi_ctx *ctx, int model, const char *name, const float *host, long row_stride,
+                         long col_stride);
+/* 1-D arrays: CPML profiles K_x a_x b_x K_x_half a_x_half b_x_half and the _y
+ * set (2*FW values, PML_pro.c), bip cip (L values, prepare_update_s_visc.c),
+ * peta (L values, readmod_visco.c:59). */
+int sofi_set_model_vector(sofi_ctx *ctx, const char *name, const float *host, int n);
+
+/* ---- acquisition ------------------------------------------------------- */
+
+/* Sources of one shot: srcpos is the reference's srcpos_loc rows 1..12 as a
+ * row-major [12][nsrc] array (row 1 grid x index, 2 grid y index, 6 amplitude,
+ * 7 azimuth/dip in degrees, 8 source type 1..5), signals is [nsrc][nt]
+ * (acq->signals of wavelet.c). */
+int sofi_set_sources(sofi_ctx *ctx, int shot, int nsrc, const float *srcpos, const float *signals);
+/* Receivers of one shot: grid indices (acq->recpos_loc rows 1 and 2). */
+int sofi_set_receivers(sofi_ctx *ctx, int shot, int ntr, const int *ix, const int *iy);
+
+/* ---- time stepping ----------------------------------------------------- */
+
+/* Zero the wavefield, CPML memory and sections of `shot` (-1: all shots) and
+ * rewind the context to step 0 (zero_wavefield.c). */
+int sofi_reset(sofi_ctx *ctx, int shot);
+/* Advance every resident shot by `nsteps` time steps (time_loop.c:42-322).
+ * Asynchronous with respect to the host except at snapshot steps; returns
+ * SOFI_E_UNSTABLE (checked at the next synchronising call) if the probe cell
+ * became NaN. */
+int sofi_run(sofi_ctx *ctx, int nsteps);
+/* Wait for the context's stream; reports a pending instability. */
+int sofi_synchronize(sofi_ctx *ctx);
+int sofi_current_step(sofi_ctx *ctx, int *step);
+
+/* ---- outputs ----------------------------------------------------------- */
+
+/* Seismogram section of one component, [ntr][ns] floats, ns = NT / NDT
+ * (gv->SECTION*; seismo_ssg.c). Synchronises the stream. */
+int sofi_get_section(sofi_ctx *ctx, int shot, int comp, float *host);
+int sofi_num_samples(sofi_ctx *ctx, int *ns);
+/* Interior 1..NY x 1..NX of a wavefield array (vx vy sxx syy sxy, r<l> p<l> q<l>)
+ * into host[(j-1)*NX + (i-1)]; set_field writes one (for restarts and tests). */
+int sofi_get_field(sofi_ctx *ctx, int shot, const char *name, float *host);
+int sofi_set_field(sofi_ctx *ctx, int shot, const char *name, const float *host);
+/* Snapshots taken so far (snap_ssg.c): frame k of component comp in the
+ * reference's file order (x outer, y inner, strides IDX/IDY). */
+int sofi_num_snapshots(sofi_ctx *ctx, int *count, int *frame_size);
+int sofi_get_snapshot(sofi_ctx *ctx, int shot, int k, int comp, float *host);
+
+/* Device time (ms, CUDA events on the context's stream) of the last sofi_run. */
+int sofi_last_run_ms(sofi_ctx *ctx, float *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -140,3 +140,59 @@ def run_oracle_example(name, precision="f32", nthreads=0, snap=True):
     o.set_receivers(ix, iy)
     o.run()
     return o
+
+
+# --- feeding oracle-prepared inputs to the GPU time loop ---------------------
+
+ISO_FIELDS = ["prip", "prjp", "ppi", "pu"]
+
+
+def gpu_config_from(cfg, nshots=1, shared_model=1, snap_override=None):
+    """sofi_config of include/sofigpu.h for an oracle SofiConfig."""
+    from gpi_project_gb300 import make_config
+    from oracle.oracle import iround
+    snap = cfg.snap if snap_override is None else snap_override
+    first = iround(cfg.tsnap1 / cfg.dt) if snap else 0
+    inc = iround(cfg.tsnapinc / cfg.dt) if snap else 0
+    last = iround(cfg.tsnap2 / cfg.dt) if snap else 0
+    return make_config(weq=cfg.weq, nx=cfg.nx, ny=cfg.ny, fdorder=cfg.fdorder, maxrelerror=cfg.maxrelerror,
+                       L=cfg.L, dt=cfg.dt, dh=cfg.dh, nt=cfg.nt, fw=cfg.fw, abs_type=cfg.abs_type,
+                       free_surf=cfg.free_surf, boundary=cfg.boundary, seismo=cfg.seismo, ndt=cfg.ndt,
+                       snap=snap, snap_first=first, snap_inc=inc, snap_last=last, idx=cfg.idx, idy=cfg.idy,
+                       nshots=nshots, shared_model=shared_model)
+
+
+def prepared_model(o, cfg):
+    """The prepared arrays the GPU kernels read, taken from an oracle context."""
+    weq, L = cfg.weq, cfg.L
+    f = {k: o.field(k) for k in ISO_FIELDS}
+    if weq in (2, 3):
+        for k in ["g", "f", "fipjp"]:
+            f[k] = o.field(k)
+        if weq == 3:
+            f["d_base"] = o.field("pu") * o.field("taus")
+            f["e_base"] = o.field("ppi") * o.field("taup")
+            f["dip_base"] = o.field("puipjp") * o.field("tausipjp")
+            if cfg.free_surf:
+                f["taus"], f["taup"] = o.field("taus"), o.field("taup")
+    else:
+        names = ["c11", "c13", "c33", "c55ipjp"] + (["c15", "c35", "c15ipjp", "c35ipjp"] if weq in (6, 7) else [])
+        visco = weq in (5, 7)
+        for k in names:
+            f[k + ("u" if visco else "")] = o.field(k + "u" if visco else k)
+        if visco:
+            taus = {"c11": "tau11", "c13": "tau13", "c33": "tau33", "c55ipjp": "tau55ipjp", "c15": "tau15",
+                    "c35": "tau35", "c15ipjp": "tau15ipjp", "c35ipjp": "tau35ipjp"}
+            for k in names:
+                f[k + "d_base"] = o.field(k) * o.field(taus[k])
+    if cfg.fw > 0 and cfg.abs_type == 2:
+        f["absorb"] = o.field("absorb")
+    vec = {}
+    if cfg.fw > 0 and cfg.abs_type == 1:
+        for k in ["K_x", "a_x", "b_x", "K_x_half", "a_x_half", "b_x_half", "K_y", "a_y", "b_y", "K_y_half",
+                  "a_y_half", "b_y_half"]:
+            vec[k] = o.vector(k, 2 * cfg.fw)
+    if L:
+        for k in ["bip", "cip", "peta"]:
+            vec[k] = o.vector(k, L)
+    return f, vec

@@ -1,0 +1,83 @@
+"""GPU time loop (libsofigpu via the C ABI) against the oracle on the same inputs.
+
+Inputs: the seeded synthetic cases of tests/golden/cases.py and the reference
+examples; the model is prepared by the oracle (the CPU restatement pinned to
+the reference) and handed to the GPU through sofi_set_model_*.
+Bar (float32; the GPU evaluates in float with fused multiply-adds where the
+reference rounds twice or promotes to double):
+    seismograms  relative L2 <= 1e-4 and relative max <= 1e-3 per component,
+                 denominators floored at the shot's dominant component;
+    snapshots    the same per frame.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from tests.golden.cases import CASES
+from tests.helpers import (COMPS, gpu_config_from, prepared_model, rel_l2, rel_max, run_oracle_case,
+                           run_oracle_example)
+
+pytestmark = pytest.mark.gpu
+
+L2_TOL, MAX_TOL = 1e-4, 1e-3
+
+
+def gpu_run_like(o, cfg, srcpos, signals, ix, iy):
+    from gpi_project_gb300 import TimeLoop
+    fields, vecs = prepared_model(o, cfg)
+    t = TimeLoop(gpu_config_from(cfg))
+    t.set_model(fields)
+    if vecs:
+        t.set_vectors(vecs)
+    t.set_sources(srcpos, signals)
+    t.set_receivers(ix, iy)
+    t.reset()
+    t.run()
+    return t
+
+
+def compare_sections(t, o, seismo, name):
+    comps = {1: ["vx", "vy"], 2: ["p"], 3: ["div", "curl"], 4: COMPS}[seismo]
+    secs = {c: (t.section(c), o.section(c)) for c in comps}
+    floor = max(np.linalg.norm(b) for a, b in secs.values() if np.isfinite(b).all())
+    mfloor = max(np.abs(b).max() for a, b in secs.values() if np.isfinite(b).all())
+    for c, (a, b) in secs.items():
+        assert np.array_equal(np.isfinite(a), np.isfinite(b)), (name, c)
+        fin = np.isfinite(b)
+        e2 = rel_l2(a[fin], b[fin], floor=floor * 1e-2 if c == "curl" else None)
+        em = rel_max(a[fin], b[fin], floor=mfloor * 1e-2 if c == "curl" else None)
+        assert e2 <= L2_TOL and em <= MAX_TOL, (name, c, e2, em)
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_gpu_matches_oracle_synthetic(case):
+    from oracle import oracle as O
+    from tests.helpers import case_receivers, case_sources
+    o = run_oracle_case(case, nthreads=os.cpu_count() or 1)
+    cfg = o.cfg
+    sp = case_sources(case, cfg)
+    t = gpu_run_like(o, cfg, sp, O.wavelet(1, cfg.nt, cfg.dt, sp), *case_receivers(case, cfg))
+    compare_sections(t, o, cfg.seismo, case["name"])
+    for comp in ["vx", "vy", "p", "div"]:
+        a, b = t.snapshots(comp), o.snapshots(comp)
+        assert a.shape == b.shape
+        for k in range(a.shape[0]):
+            assert rel_l2(a[k], b[k]) <= L2_TOL, (case["name"], "snap", comp, k, rel_l2(a[k], b[k]))
+    for name in ["vx", "vy", "sxx", "syy", "sxy"]:
+        assert rel_l2(t.field(name), o.field(name)) <= L2_TOL, (case["name"], name)
+    t.close()
+    o.close()
+
+
+@pytest.mark.parametrize("name", ["weq3", "weq4", "weq5", "weq6", "weq7", "weq8"])
+def test_gpu_matches_oracle_examples(name):
+    from oracle import oracle as O
+    from tests.helpers import example_config, example_inputs
+    o = run_oracle_example(name, nthreads=os.cpu_count() or 1)
+    cfg = o.cfg
+    mats, sp, ix, iy = example_inputs(name, cfg)
+    t = gpu_run_like(o, cfg, sp, O.wavelet(1, cfg.nt, cfg.dt, sp), ix, iy)
+    compare_sections(t, o, cfg.seismo, name)
+    t.close()
+    o.close()
