@@ -80,12 +80,12 @@ def build(verbose: bool = False) -> dict:
     if objs is not None:
         _run([NVCC, *ARCH, "-shared", "-o", gpu_lib, *objs, "-lcudart"])
     if host_build and hs:
-        _run(["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-fPIC", "-shared", "-Wall", "-I", INC, "-o", host_lib,
-              *hs, "-lm"])
+        _run(["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-fPIC", "-shared", "-fopenmp", "-Wall", "-I", INC,
+              "-o", host_lib, *hs, "-lm"])
         main = os.path.join(CSRC, "host", "sofi2d_main.c")
         if os.path.exists(main):
-            _run(["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-Wall", "-I", INC, "-o", cli, main, *hs,
-                  "-L", OUT, "-lsofigpu", f"-Wl,-rpath,{OUT}", "-lm"])
+            _run(["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-fopenmp", "-Wall", "-I", INC, "-o", cli, main, *hs,
+                  "-L", OUT, "-lsofigpu", "-Wl,-rpath,$ORIGIN", "-lm"])
     return {"gpu": gpu_lib, "host": host_lib, "cli": cli}
 
 

@@ -1,0 +1,330 @@
+/*
+ * acq_io.c -- model files, sources, receivers, wavelets and outputs.
+ *
+ *   model files      NX traces of NY float32 samples (readmod_elastic.c:103-111)
+ *   source file      x y tshift fc amp [azimuth [type]] per line, '#' comments
+ *                    (sources.c:60-118); grid index floor(x/DH)+1 (splitsrc.c:34-36)
+ *   receiver file    x y per line, '#'/'%' comments; duplicates dropped
+ *                    (receiver.c:48-110); or a line XREC1..XREC2 every NGEOPH
+ *   wavelets         Ricker, Fuchs-Mueller, sin^3 (wavelet.c:56-81)
+ *   SU traces        240-byte trace header + float32 samples (outseis_glob.c:40-81)
+ *   snapshots        float32 stream per component (snap_ssg.c, SNAP_FORMAT=3)
+ */
+#include "sofihost.h"
+
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define PI M_PI
+#define IROUND(x) ((int)floor((x) + 0.5))
+
+void sofih_set_error(const char *fmt, ...);
+
+static const char *SUFFIX[8][8] = {
+    {0}, {0}, {"vp", "vs", "rho"}, {"vp", "vs", "rho", "qp", "qs"}, {"vp", "vs", "rho", "epsilon", "delta"},
+    {"vp", "vs", "rho", "epsilon", "delta", "qp", "qs"}, {"vp", "vs", "rho", "epsilon", "delta", "theta"},
+    {"vp", "vs", "rho", "epsilon", "delta", "theta", "qp", "qs"}};
+
+int sofih_model_suffixes(int weq, const char **names, int max)
+{
+    if (weq < 2 || weq > 7)
+        return 0;
+    int n = 0;
+    while (n < 8 && SUFFIX[weq][n])
+        n++;
+    for (int k = 0; k < n && k < max; k++)
+        names[k] = SUFFIX[weq][k];
+    return n;
+}
+
+int sofih_read_model(const sofih_par *p, const char *mfile, float **out, int max)
+{
+    const char *names[8];
+    int n = sofih_model_suffixes(p->weq, names, 8);
+    size_t cnt = (size_t)p->nx * (size_t)p->ny;
+    for (int k = 0; k < n && k < max; k++) {
+        char path[600];
+        snprintf(path, sizeof path, "%s.%s", mfile, names[k]);
+        FILE *fp = fopen(path, "rb");
+        if (!fp) {
+            sofih_set_error("cannot open model file %s", path);
+            return 1;
+        }
+        out[k] = (float *)malloc(cnt * sizeof(float));
+        size_t got = fread(out[k], sizeof(float), cnt, fp);
+        fclose(fp);
+        if (got != cnt) {
+            sofih_set_error("%s holds %zu values, NX*NY = %zu needed", path, got, cnt);
+            return 1;
+        }
+    }
+    return 0;
+}
+
+static int is_data_line(const char *s, int allow_percent)
+{
+    if (strchr(s, '#') || (allow_percent && strchr(s, '%')))
+        return 0;
+    char tok[64];
+    return sscanf(s, "%63s", tok) == 1;
+}
+
+int sofih_read_sources(const sofih_par *p, const char *path, float **srcpos, float **xy, int *nsrc)
+{
+    FILE *fp = fopen(path, "r");
+    if (!fp) {
+        sofih_set_error("cannot open source file %s", path);
+        return 1;
+    }
+    char line[512];
+    int n = 0;
+    while (fgets(line, sizeof line, fp))
+        n += is_data_line(line, 0);
+    rewind(fp);
+    float *sp = (float *)calloc((size_t)12 * (n ? n : 1), sizeof(float));
+    float *pos = (float *)calloc((size_t)2 * (n ? n : 1), sizeof(float));
+    int l = 0;
+    while (fgets(line, sizeof line, fp)) {
+        if (!is_data_line(line, 0))
+            continue;
+        float v[7] = {0};
+        int k = sscanf(line, "%f%f%f%f%f%f%f", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6]);
+        if (k < 5) {
+            fclose(fp);
+            free(sp), free(pos);
+            sofih_set_error("%s: source %d lacks time shift, frequency or amplitude", path, l + 1);
+            return 1;
+        }
+        if (k < 6)
+            v[5] = 0.0f;
+        if (k < 7)
+            v[6] = (float)p->source_type;
+        sp[0 * n + l] = (float)((int)floor(v[0] / p->dh) + 1);
+        sp[1 * n + l] = (float)((int)floor(v[1] / p->dh) + 1);
+        sp[3 * n + l] = v[2], sp[4 * n + l] = v[3], sp[5 * n + l] = v[4];
+        sp[6 * n + l] = v[5], sp[7 * n + l] = v[6];
+        pos[l] = v[0], pos[n + l] = v[1];
+        l++;
+    }
+    fclose(fp);
+    *srcpos = sp, *xy = pos, *nsrc = n;
+    return 0;
+}
+
+int sofih_wavelet(int shape, int nt, float dt, int nsrc, const float *srcpos, float *signals)
+{
+    for (int k = 0; k < nsrc; k++) {
+        float tshift = srcpos[3 * nsrc + k], fc = srcpos[4 * nsrc + k], a = srcpos[5 * nsrc + k];
+        float ts = 1.0 / fc;
+        for (int n = 1; n <= nt; n++) {
+            float t = (float)n * dt, amp = 0.0, tau;
+            switch (shape) {
+              case 1:
+                  tau = PI * (t - 1.5 * ts - tshift) / (ts);
+                  amp = (((1.0 - 2.0 * tau * tau) * exp(-tau * tau)));
+                  break;
+              case 2:
+                  amp = ((t < tshift) || (t > (tshift + ts)))
+                            ? 0.0
+                            : (sin(2.0 * PI * (t - tshift) * fc) - 0.5 * sin(4.0 * PI * (t - tshift) * fc));
+                  break;
+              case 4:
+                  amp = ((t < tshift) || (t > (tshift + ts))) ? 0.0 : pow(sin(PI * (t - tshift) / ts), 3.0);
+                  break;
+              default:
+                  sofih_set_error("SOURCE_SHAPE %d is not supported (1 Ricker, 2 Fuchs-Mueller, 4 sin^3)", shape);
+                  return 1;
+            }
+            signals[(size_t)k * nt + (n - 1)] = amp * a;
+        }
+    }
+    return 0;
+}
+
+int sofih_read_receivers(const sofih_par *p, const char *path, int **ix, int **iy, int *ntr)
+{
+    int cap = 64, n = 0;
+    int *x = (int *)malloc(sizeof(int) * cap), *y = (int *)malloc(sizeof(int) * cap);
+    if (p->readrec) {
+        FILE *fp = fopen(path, "r");
+        if (!fp) {
+            free(x), free(y);
+            sofih_set_error("cannot open receiver file %s", path);
+            return 1;
+        }
+        char line[512];
+        while (fgets(line, sizeof line, fp)) {
+            if (!is_data_line(line, 1))
+                continue;
+            float xr, yr;
+            if (sscanf(line, "%f%f", &xr, &yr) != 2)
+                continue;
+            if (n == cap)
+                cap *= 2, x = realloc(x, sizeof(int) * cap), y = realloc(y, sizeof(int) * cap);
+            x[n] = (int)floor((xr + p->refrec[0]) / p->dh) + 1;
+            y[n] = (int)floor((yr + p->refrec[1]) / p->dh) + 1;
+            n++;
+        }
+        fclose(fp);
+    } else {
+        int x1 = (int)floor(p->xrec1 / p->dh) + 1, y1 = (int)floor(p->yrec1 / p->dh) + 1;
+        int x2 = (int)floor(p->xrec2 / p->dh) + 1, y2 = (int)floor(p->yrec2 / p->dh) + 1;
+        int step = p->ngeoph > 0 ? p->ngeoph : 1;
+        if (y1 != y2 && x1 != x2) {
+            free(x), free(y);
+            sofih_set_error("oblique receiver lines are not supported");
+            return 1;
+        }
+        int len = (y1 == y2) ? x2 - x1 : y2 - y1;
+        for (int k = 0; k <= len; k += step) {
+            if (n == cap)
+                cap *= 2, x = realloc(x, sizeof(int) * cap), y = realloc(y, sizeof(int) * cap);
+            x[n] = (y1 == y2) ? x1 + k : x1;
+            y[n] = (y1 == y2) ? y1 : y1 + k;
+            n++;
+        }
+    }
+    /* drop repeated grid points, keeping the first */
+    int m = 0;
+    for (int k = 0; k < n; k++) {
+        int dup = 0;
+        for (int q = 0; q < m && !dup; q++)
+            dup = (x[q] == x[k] && y[q] == y[k]);
+        if (!dup)
+            x[m] = x[k], y[m] = y[k], m++;
+    }
+    *ix = x, *iy = y, *ntr = m;
+    return 0;
+}
+
+/* SEG-Y trace header fields written by outseis_glob.c:46-81 (byte offsets of
+ * the standard 240-byte header). */
+static void put_i32(unsigned char *h, int off, int v) { memcpy(h + off, &v, 4); }
+static void put_i16(unsigned char *h, int off, short v) { memcpy(h + off, &v, 2); }
+static void put_u16(unsigned char *h, int off, unsigned short v) { memcpy(h + off, &v, 2); }
+static void put_f32(unsigned char *h, int off, float v) { memcpy(h + off, &v, 4); }
+
+int sofih_write_su(const char *path, const float *section, int ntr, int ns, const int *ix, const int *iy,
+                   float xs, float ys, const sofih_par *p, int ishot, int comp)
+{
+    (void)comp;
+    FILE *fp = fopen(path, "wb");
+    if (!fp) {
+        sofih_set_error("cannot write %s", path);
+        return 1;
+    }
+    const float xshift = 800.0, yshift = 800.0;
+    for (int t = 0; t < ntr; t++) {
+        unsigned char h[240];
+        memset(h, 0, sizeof h);
+        float xr = (ix[t] - 1) * p->dh, yr = (iy[t] - 1) * p->dh;
+        float x = xr - p->refrec[0], y = yr - p->refrec[1];
+        int tracl = t + 1;
+        put_i32(h, 0, tracl);                                                   /* tracl */
+        put_i32(h, 4, tracl);                                                   /* tracr */
+        put_i32(h, 8, ishot);                                                   /* fldr */
+        put_i32(h, 12, t + 1);                                                  /* tracf */
+        put_i32(h, 16, ishot);                                                  /* ep */
+        put_i32(h, 20, tracl);                                                  /* cdp */
+        put_i16(h, 28, 1);                                                      /* trid */
+        put_i32(h, 36, IROUND(sqrt((xs - xr) * (xs - xr) + (ys - yr) * (ys - yr)))); /* offset */
+        put_i32(h, 40, IROUND(yr * 1000.0));                                    /* gelev */
+        put_i32(h, 48, IROUND(ys * 1000.0));                                    /* sdepth */
+        put_i32(h, 60, IROUND(((360.0 / (2.0 * PI)) * atan2(x - xshift, y - yshift)) * 1000.0)); /* swdep */
+        put_i16(h, 68, -1000);                                                  /* scalel */
+        put_i16(h, 70, -1000);                                                  /* scalco */
+        put_i32(h, 72, IROUND(xs * 1000.0));                                    /* sx */
+        put_i32(h, 80, IROUND(xr * 1000.0));                                    /* gx */
+        put_u16(h, 114, (unsigned short)ns);                                    /* ns */
+        unsigned short dt_us = (unsigned short)IROUND((float)p->ndt * p->dt * 1.0e6);
+        put_u16(h, 116, dt_us);                                                 /* dt */
+        put_f32(h, 180, (float)dt_us * 1.0e-6);                                 /* d1 */
+        if (fwrite(h, 1, 240, fp) != 240 || fwrite(section + (size_t)t * ns, sizeof(float), ns, fp) != (size_t)ns) {
+            fclose(fp);
+            sofih_set_error("short write on %s", path);
+            return 1;
+        }
+    }
+    fclose(fp);
+    return 0;
+}
+
+int sofih_write_snap(const char *path, const float *frame, int n, int append)
+{
+    FILE *fp = fopen(path, append ? "ab" : "wb");
+    if (!fp) {
+        sofih_set_error("cannot write %s", path);
+        return 1;
+    }
+    size_t w = fwrite(frame, sizeof(float), (size_t)n, fp);
+    fclose(fp);
+    if (w != (size_t)n) {
+        sofih_set_error("short write on %s", path);
+        return 1;
+    }
+    return 0;
+}
+
+/* Holberg / Taylor operator coefficients (published tables; reference
+ * holbergcoeff.c:40-82): row MAXRELERROR, FDORDER/2 - 1; hc[0] is the
+ * operator's points-per-wavelength figure, hc[1..6] the coefficients. */
+static const double HOLBERG[5][6][7] = {
+    {{23.0, 1.0, 0, 0, 0, 0, 0}, {8.0, 9.0 / 8.0, -1.0 / 24.0, 0, 0, 0, 0},
+     {6.0, 75.0 / 64.0, -25.0 / 384.0, 3.0 / 640.0, 0, 0, 0},
+     {5.0, 1225.0 / 1024.0, -245.0 / 3072.0, 49.0 / 5120.0, -5.0 / 7168.0, 0, 0},
+     {5.0, 19845.0 / 16384.0, -735.0 / 8192.0, 567.0 / 40960.0, -405.0 / 229376.0, 35.0 / 294912.0, 0},
+     {4.0, 160083.0 / 131072.0, -12705.0 / 131072.0, 22869.0 / 1310720.0, -5445.0 / 1835008.0,
+      847.0 / 2359296.0, -63.0 / 2883584.0}},
+    {{49.7, 1.0010, 0, 0, 0, 0, 0}, {8.32, 1.1382, -0.046414, 0, 0, 0, 0},
+     {4.77, 1.1965, -0.078804, 0.0081781, 0, 0, 0}, {3.69, 1.2257, -0.099537, 0.018063, -0.0026274, 0, 0},
+     {3.19, 1.2415, -0.11231, 0.026191, -0.0064682, 0.001191, 0},
+     {2.91, 1.2508, -0.12034, 0.032131, -0.010142, 0.0029857, -0.00066667}},
+    {{22.2, 1.0050, 0, 0, 0, 0, 0}, {5.65, 1.1534, -0.052806, 0, 0, 0, 0},
+     {3.74, 1.2111, -0.088313, 0.011768, 0, 0, 0}, {3.11, 1.2367, -0.10815, 0.023113, -0.0046905, 0, 0},
+     {2.80, 1.2496, -0.11921, 0.031130, -0.0093272, 0.0025161, 0},
+     {2.62, 1.2568, -0.12573, 0.036423, -0.013132, 0.0047484, -0.0015979}},
+    {{15.8, 1.0100, 0, 0, 0, 0, 0}, {4.80, 1.1640, -0.057991, 0, 0, 0, 0},
+     {3.39, 1.2192, -0.094070, 0.014608, 0, 0, 0}, {2.90, 1.2422, -0.11269, 0.026140, -0.0064054, 0, 0},
+     {2.65, 1.2534, -0.12257, 0.033755, -0.011081, 0.0036784, 0},
+     {2.51, 1.2596, -0.12825, 0.038550, -0.014763, 0.0058619, -0.0024538}},
+    {{9.16, 1.0300, 0, 0, 0, 0, 0}, {3.47, 1.1876, -0.072518, 0, 0, 0, 0},
+     {2.91, 1.2341, -0.10569, 0.022589, 0, 0, 0}, {2.61, 1.2516, -0.12085, 0.032236, -0.011459, 0, 0},
+     {2.45, 1.2596, -0.12829, 0.038533, -0.014681, 0.0072580, 0},
+     {2.36, 1.2640, -0.13239, 0.042217, -0.017803, 0.0081959, -0.0051848}},
+};
+
+int sofih_holberg(int fdorder, int maxrelerror, float *hc)
+{
+    if (fdorder < 2 || fdorder > 12 || (fdorder & 1) || maxrelerror < 0 || maxrelerror > 4) {
+        sofih_set_error("no FD coefficients for FDORDER %d, MAXRELERROR %d", fdorder, maxrelerror);
+        return 1;
+    }
+    for (int k = 0; k < 7; k++)
+        hc[k] = (float)HOLBERG[maxrelerror][fdorder / 2 - 1][k];
+    return 0;
+}
+
+/* checkfd.c:41-52: DT must not exceed DH / (sqrt(2) * gamma * cmax) with
+ * gamma = sum |hc[1..6]| and cmax the largest velocity of the model. */
+int sofih_check_cfl(const sofih_par *p, const sofih_prep *m, float *dt_max)
+{
+    float hc[7];
+    if (sofih_holberg(p->fdorder, p->maxrelerror, hc))
+        return 1;
+    float vpmin, vpmax, vsmin, vsmax;
+    sofih_prep_vrange(m, &vpmin, &vpmax, &vsmin, &vsmax);
+    float cmax = vsmax > vpmax ? vsmax : vpmax;
+    double gamma = 0;
+    for (int k = 1; k <= 6; k++)
+        gamma += fabs(hc[k]);
+    double lim = p->dh / (sqrt(2) * gamma * cmax);
+    *dt_max = (float)lim;
+    if (p->dt > lim) {
+        sofih_set_error("unstable: DT=%g exceeds the stability limit %g (VMAX=%g)", p->dt, lim, cmax);
+        return 1;
+    }
+    return 0;
+}

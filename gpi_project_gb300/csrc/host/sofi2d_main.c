@@ -1,0 +1,185 @@
+/*
+ * sofi2d_main.c -- command-line forward modelling on one GPU.
+ *
+ *   sofi2d_gb300 par.json [device]
+ *
+ * Same inputs and outputs as the reference's forward mode (src/sofi2D.c
+ * main(), MODE=FW, FDORDER_TIME=2): parameter file, binary model files,
+ * source and receiver files; SU seismograms SEIS_FILE_<comp>.su (.shotN with
+ * RUN_MULTIPLE_SHOTS) and binary snapshots. The domain is never decomposed,
+ * so snapshots are written merged (the file snapmerge would produce,
+ * SNAP_FILE.bin.<comp>). With RUN_MULTIPLE_SHOTS = 1 every shot is resident
+ * in one context and advanced together instead of one after the other
+ * (reference sofi2D.c:325 loops over shots).
+ */
+#include "sofigpu.h"
+#include "sofihost.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#define IROUND(x) ((int)floor((x) + 0.5))
+
+static double now_s(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+#define DIE_H(...)                                                  \
+    do {                                                            \
+        fprintf(stderr, "sofi2d_gb300: %s\n", sofih_last_error());  \
+        return 1;                                                   \
+    } while (0)
+#define CHECK_G(call)                                                           \
+    do {                                                                        \
+        if ((call) != 0) {                                                      \
+            fprintf(stderr, "sofi2d_gb300: %s\n", sofi_last_error());           \
+            return 1;                                                           \
+        }                                                                       \
+    } while (0)
+
+int main(int argc, char **argv)
+{
+    if (argc < 2) {
+        fprintf(stderr, "usage: %s par.json [device]\n", argv[0]);
+        return 2;
+    }
+    int device = argc > 2 ? atoi(argv[2]) : 0;
+    double t0 = now_s();
+    sofih_par p;
+    if (sofih_read_par(argv[1], &p))
+        DIE_H();
+    float *mat[8] = {0};
+    if (sofih_read_model(&p, p.mfile, mat, 8))
+        DIE_H();
+    const char *names[8];
+    int nm = sofih_model_suffixes(p.weq, names, 8);
+    float *vp = NULL, *vs = NULL, *rho = NULL, *qp = NULL, *qs = NULL, *eps = NULL, *del = NULL, *tet = NULL;
+    for (int k = 0; k < nm; k++) {
+        float **dst = !strcmp(names[k], "vp") ? &vp : !strcmp(names[k], "vs") ? &vs : !strcmp(names[k], "rho") ? &rho
+                    : !strcmp(names[k], "qp") ? &qp : !strcmp(names[k], "qs") ? &qs
+                    : !strcmp(names[k], "epsilon") ? &eps : !strcmp(names[k], "delta") ? &del : &tet;
+        *dst = mat[k];
+    }
+    sofih_prep *prep;
+    if (sofih_prepare(&p, vp, vs, rho, qp, qs, eps, del, tet, 0, &prep))
+        DIE_H();
+    float dtmax;
+    if (sofih_check_cfl(&p, prep, &dtmax))
+        DIE_H();
+    float *srcpos, *srcxy;
+    int nsrc;
+    if (sofih_read_sources(&p, p.source_file, &srcpos, &srcxy, &nsrc))
+        DIE_H();
+    float *sig = (float *)malloc(sizeof(float) * (size_t)(nsrc ? nsrc : 1) * p.nt);
+    if (sofih_wavelet(p.source_shape, p.nt, p.dt, nsrc, srcpos, sig))
+        DIE_H();
+    int *rix = NULL, *riy = NULL, ntr = 0;
+    if (p.seismo && sofih_read_receivers(&p, p.rec_file, &rix, &riy, &ntr))
+        DIE_H();
+    int nshots = (p.run_multiple_shots && nsrc > 0) ? nsrc : 1;
+
+    sofi_config c;
+    memset(&c, 0, sizeof c);
+    c.weq = p.weq, c.nx = p.nx, c.ny = p.ny, c.fdorder = p.fdorder, c.maxrelerror = p.maxrelerror;
+    c.L = p.L, c.dt = p.dt, c.dh = p.dh, c.nt = p.nt, c.fw = p.fw, c.abs_type = p.abs_type;
+    c.free_surf = p.free_surf, c.boundary = p.boundary, c.seismo = p.seismo, c.ndt = p.ndt;
+    c.snap = p.snap;
+    c.snap_first = IROUND(p.tsnap1 / p.dt), c.snap_inc = IROUND(p.tsnapinc / p.dt), c.snap_last = IROUND(p.tsnap2 / p.dt);
+    c.idx = p.idx, c.idy = p.idy, c.nshots = nshots, c.shared_model = 1;
+    sofi_ctx *ctx;
+    CHECK_G(sofi_create(&c, device, &ctx));
+    float hc[7];
+    if (sofih_holberg(p.fdorder, p.maxrelerror, hc))
+        DIE_H();
+    CHECK_G(sofi_set_hc(ctx, hc));
+    for (int k = 0; k < sofih_prep_num_fields(prep); k++)
+        CHECK_G(sofi_set_model_field(ctx, 0, sofih_prep_field_name(prep, k), sofih_prep_field(prep, k), p.nx, 1));
+    const char *vecs[] = {"K_x", "a_x", "b_x", "K_x_half", "a_x_half", "b_x_half", "K_y", "a_y", "b_y",
+                          "K_y_half", "a_y_half", "b_y_half", "bip", "cip", "peta"};
+    for (size_t k = 0; k < sizeof vecs / sizeof vecs[0]; k++) {
+        const float *d;
+        int n = sofih_prep_vector(prep, vecs[k], &d);
+        if (n)
+            CHECK_G(sofi_set_model_vector(ctx, vecs[k], d, n));
+    }
+    for (int s = 0; s < nshots; s++) {
+        if (nshots == 1) {
+            CHECK_G(sofi_set_sources(ctx, 0, nsrc, srcpos, sig));
+        } else {
+            float one[12];
+            for (int r = 0; r < 12; r++)
+                one[r] = srcpos[r * nsrc + s];
+            CHECK_G(sofi_set_sources(ctx, s, 1, one, sig + (size_t)s * p.nt));
+        }
+        if (ntr)
+            CHECK_G(sofi_set_receivers(ctx, s, ntr, rix, riy));
+    }
+    CHECK_G(sofi_reset(ctx, -1));
+    double t1 = now_s();
+    CHECK_G(sofi_run(ctx, p.nt));
+    CHECK_G(sofi_synchronize(ctx));
+    double t2 = now_s();
+    float ms = 0;
+    sofi_last_run_ms(ctx, &ms);
+    double cells = (double)p.nx * p.ny * p.nt * nshots;
+    printf("sofi2d_gb300: %d shot(s), %dx%d, NT=%d: time loop %.3f s (device %.3f s), %.2f Gcell-updates/s\n",
+           nshots, p.nx, p.ny, p.nt, t2 - t1, ms * 1e-3, cells / (ms * 1e-3) / 1e9);
+
+    /* seismograms (saveseis_glob.c naming) */
+    if (p.seismo && ntr) {
+        int ns;
+        sofi_num_samples(ctx, &ns);
+        float *sec = (float *)malloc(sizeof(float) * (size_t)ntr * (ns ? ns : 1));
+        const char *cn[6] = {0, "vx", "vy", "p", "div", "curl"};
+        int comps[5], nc = 0;
+        if (p.seismo == 1) comps[nc++] = 1, comps[nc++] = 2;
+        if (p.seismo == 2) comps[nc++] = 3;
+        if (p.seismo == 3) comps[nc++] = 4, comps[nc++] = 5;
+        if (p.seismo == 4) for (int k = 1; k <= 5; k++) comps[nc++] = k;
+        for (int s = 0; s < nshots; s++)
+            for (int q = 0; q < nc; q++) {
+                CHECK_G(sofi_get_section(ctx, s, comps[q], sec));
+                char path[700];
+                if (p.run_multiple_shots)
+                    snprintf(path, sizeof path, "%s_%s.su.shot%d", p.seis_file, cn[comps[q]], s + 1);
+                else
+                    snprintf(path, sizeof path, "%s_%s.su", p.seis_file, cn[comps[q]]);
+                int src = nshots == 1 ? 0 : s;
+                if (sofih_write_su(path, sec, ntr, ns, rix, riy, srcxy[src], srcxy[nsrc + src], &p, s + 1,
+                                   comps[q]))
+                    DIE_H();
+            }
+        free(sec);
+    }
+    /* snapshots of the first shot (initsrc.c:96-98) */
+    int nsnap = 0, fsz = 0;
+    sofi_num_snapshots(ctx, &nsnap, &fsz);
+    if (nsnap) {
+        float *frame = (float *)malloc(sizeof(float) * (size_t)fsz);
+        const char *cn[6] = {0, "vx", "vy", "p", "div", "curl"};
+        for (int comp = 1; comp <= 5; comp++) {
+            int want = (p.snap == 4) || (p.snap == 1 && comp <= 2) || (p.snap == 2 && comp == 3) ||
+                       (p.snap == 3 && comp >= 4);
+            if (!want)
+                continue;
+            char path[700];
+            snprintf(path, sizeof path, "%s.bin.%s", p.snap_file, cn[comp]);
+            for (int k = 0; k < nsnap; k++) {
+                CHECK_G(sofi_get_snapshot(ctx, 0, k, comp, frame));
+                if (sofih_write_snap(path, frame, fsz, k > 0))
+                    DIE_H();
+            }
+        }
+        free(frame);
+    }
+    sofi_destroy(ctx);
+    sofih_prep_free(prep);
+    printf("sofi2d_gb300: total %.3f s\n", now_s() - t0);
+    return 0;
+}

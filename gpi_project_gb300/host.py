@@ -1,0 +1,166 @@
+"""ctypes binding of libsofihost.so (include/sofihost.h): parameter files,
+model preparation, acquisition and outputs on the host."""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from ._native import BUILD
+
+MAX_L = 8
+
+
+class SofihPar(ctypes.Structure):
+    _fields_ = [("weq", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("dh", ctypes.c_float),
+                ("dt", ctypes.c_float), ("time", ctypes.c_float), ("nt", ctypes.c_int),
+                ("fdorder", ctypes.c_int), ("maxrelerror", ctypes.c_int), ("L", ctypes.c_int),
+                ("f_ref", ctypes.c_float), ("fl", ctypes.c_float * MAX_L), ("fw", ctypes.c_int),
+                ("abs_type", ctypes.c_int), ("free_surf", ctypes.c_int), ("boundary", ctypes.c_int),
+                ("npower", ctypes.c_float), ("k_max_cpml", ctypes.c_float), ("vppml", ctypes.c_float),
+                ("fpml", ctypes.c_float), ("damping", ctypes.c_float), ("source_shape", ctypes.c_int),
+                ("source_type", ctypes.c_int), ("run_multiple_shots", ctypes.c_int),
+                ("source_file", ctypes.c_char * 256), ("seismo", ctypes.c_int), ("ndt", ctypes.c_int),
+                ("readrec", ctypes.c_int), ("seis_format", ctypes.c_int), ("rec_file", ctypes.c_char * 256),
+                ("seis_file", ctypes.c_char * 256), ("refrec", ctypes.c_float * 2), ("xrec1", ctypes.c_float),
+                ("yrec1", ctypes.c_float), ("xrec2", ctypes.c_float), ("yrec2", ctypes.c_float),
+                ("ngeoph", ctypes.c_int), ("snap", ctypes.c_int), ("snap_format", ctypes.c_int),
+                ("tsnap1", ctypes.c_float), ("tsnap2", ctypes.c_float), ("tsnapinc", ctypes.c_float),
+                ("idx", ctypes.c_int), ("idy", ctypes.c_int), ("snap_file", ctypes.c_char * 256),
+                ("mfile", ctypes.c_char * 256)]
+
+
+_LIB = None
+
+
+def load():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(BUILD, "libsofihost.so")
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: build gpi_project_gb300 first")
+        L = ctypes.CDLL(path)
+        P, vp, fp, ip = ctypes.POINTER, ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int)
+        L.sofih_last_error.restype = ctypes.c_char_p
+        L.sofih_read_par.argtypes = [ctypes.c_char_p, P(SofihPar)]
+        L.sofih_prepare.argtypes = [P(SofihPar)] + [fp] * 8 + [ctypes.c_int, P(vp)]
+        L.sofih_prep_free.argtypes = [vp]
+        L.sofih_prep_num_fields.argtypes = [vp]
+        L.sofih_prep_field_name.argtypes = [vp, ctypes.c_int]
+        L.sofih_prep_field_name.restype = ctypes.c_char_p
+        L.sofih_prep_field.argtypes = [vp, ctypes.c_int]
+        L.sofih_prep_field.restype = fp
+        L.sofih_prep_vector.argtypes = [vp, ctypes.c_char_p, P(fp)]
+        L.sofih_holberg.argtypes = [ctypes.c_int, ctypes.c_int, fp]
+        L.sofih_check_cfl.argtypes = [P(SofihPar), vp, fp]
+        L.sofih_wavelet.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int, fp, fp]
+        L.sofih_read_sources.argtypes = [P(SofihPar), ctypes.c_char_p, P(fp), P(fp), ip]
+        L.sofih_read_receivers.argtypes = [P(SofihPar), ctypes.c_char_p, P(ip), P(ip), ip]
+        L.sofih_write_su.argtypes = [ctypes.c_char_p, fp, ctypes.c_int, ctypes.c_int, ip, ip, ctypes.c_float,
+                                     ctypes.c_float, P(SofihPar), ctypes.c_int, ctypes.c_int]
+        _LIB = L
+    return _LIB
+
+
+def _err():
+    return RuntimeError(load().sofih_last_error().decode())
+
+
+def _fp(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def read_par(path: str) -> SofihPar:
+    p = SofihPar()
+    if load().sofih_read_par(path.encode(), ctypes.byref(p)):
+        raise _err()
+    return p
+
+
+def make_par(**kw) -> SofihPar:
+    p = SofihPar()
+    p.npower, p.k_max_cpml, p.damping, p.ndt, p.idx, p.idy, p.readrec = 2.0, 1.0, 8.0, 1, 1, 1, 1
+    for k, v in kw.items():
+        if k == "fl":
+            for i, f in enumerate(v):
+                p.fl[i] = f
+        elif k == "refrec":
+            p.refrec[0], p.refrec[1] = v
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def prepare(p: SofihPar, mats: dict, nthreads: int = 0):
+    """Prepared model: (fields {name: [NY][NX]}, vectors {name: array})."""
+    L = load()
+    order = ["vp", "vs", "rho", "qp", "qs", "epsilon", "delta", "theta"]
+    arrs = [None if mats.get(k) is None else np.ascontiguousarray(mats[k], dtype=np.float32).reshape(-1)
+            for k in order]
+    h = ctypes.c_void_p()
+    if L.sofih_prepare(ctypes.byref(p), *[_fp(a) for a in arrs], nthreads, ctypes.byref(h)):
+        raise _err()
+    try:
+        fields = {}
+        for k in range(L.sofih_prep_num_fields(h)):
+            name = L.sofih_prep_field_name(h, k).decode()
+            ptr = L.sofih_prep_field(h, k)
+            fields[name] = np.ctypeslib.as_array(ptr, shape=(p.ny, p.nx)).copy()
+        vecs = {}
+        for name in ["K_x", "a_x", "b_x", "K_x_half", "a_x_half", "b_x_half", "K_y", "a_y", "b_y", "K_y_half",
+                     "a_y_half", "b_y_half", "bip", "cip", "peta"]:
+            d = ctypes.POINTER(ctypes.c_float)()
+            n = L.sofih_prep_vector(h, name.encode(), ctypes.byref(d))
+            if n:
+                vecs[name] = np.ctypeslib.as_array(d, shape=(n,)).copy()
+        dtmax = ctypes.c_float()
+        stable = L.sofih_check_cfl(ctypes.byref(p), h, ctypes.byref(dtmax)) == 0
+        vecs["_dt_max"] = np.array([dtmax.value], np.float32)
+        vecs["_stable"] = np.array([stable], np.int32)
+    finally:
+        L.sofih_prep_free(h)
+    return fields, vecs
+
+
+def holberg(fdorder: int, maxrelerror: int) -> np.ndarray:
+    hc = np.zeros(7, np.float32)
+    if load().sofih_holberg(fdorder, maxrelerror, _fp(hc)):
+        raise _err()
+    return hc
+
+
+def wavelet(shape: int, nt: int, dt: float, srcpos: np.ndarray) -> np.ndarray:
+    sp = np.ascontiguousarray(srcpos, dtype=np.float32)
+    out = np.empty((sp.shape[1], nt), np.float32)
+    if load().sofih_wavelet(shape, nt, dt, sp.shape[1], _fp(sp), _fp(out)):
+        raise _err()
+    return out
+
+
+def read_sources(p: SofihPar, path: str):
+    L = load()
+    sp, xy, n = ctypes.POINTER(ctypes.c_float)(), ctypes.POINTER(ctypes.c_float)(), ctypes.c_int()
+    if L.sofih_read_sources(ctypes.byref(p), path.encode(), ctypes.byref(sp), ctypes.byref(xy), ctypes.byref(n)):
+        raise _err()
+    n = n.value
+    return (np.ctypeslib.as_array(sp, shape=(12, n)).copy(), np.ctypeslib.as_array(xy, shape=(2, n)).copy())
+
+
+def read_receivers(p: SofihPar, path: str):
+    L = load()
+    ix, iy, n = ctypes.POINTER(ctypes.c_int)(), ctypes.POINTER(ctypes.c_int)(), ctypes.c_int()
+    if L.sofih_read_receivers(ctypes.byref(p), path.encode(), ctypes.byref(ix), ctypes.byref(iy), ctypes.byref(n)):
+        raise _err()
+    n = n.value
+    return (np.ctypeslib.as_array(ix, shape=(n,)).copy(), np.ctypeslib.as_array(iy, shape=(n,)).copy())
+
+
+def write_su(path: str, section, ix, iy, xs: float, ys: float, p: SofihPar, ishot: int = 1, comp: int = 1):
+    sec = np.ascontiguousarray(section, dtype=np.float32)
+    ix = np.ascontiguousarray(ix, dtype=np.int32)
+    iy = np.ascontiguousarray(iy, dtype=np.int32)
+    ipp = ctypes.POINTER(ctypes.c_int)
+    if load().sofih_write_su(path.encode(), _fp(sec), sec.shape[0], sec.shape[1], ix.ctypes.data_as(ipp),
+                             iy.ctypes.data_as(ipp), xs, ys, ctypes.byref(p), ishot, comp):
+        raise _err()

@@ -1,0 +1,99 @@
+/*
+ * sofihost.h -- C host around the GPU time loop (libsofihost.so).
+ *
+ * Everything the reference does on the host before and after time_loop() for
+ * one forward-modelling run, kept file-compatible:
+ *   - the parameter file (reference src/json_parser.c, src/read_par_json.c),
+ *   - binary model files, NX traces of NY float32 samples (readmod_*.c),
+ *   - model preparation: media conversion (readmod_elastic/visco/_vti/_tti.c),
+ *     averaging and DT scaling (prepmod.c, av_*.c, prepare_update_s_*.c),
+ *     CPML profiles (PML_pro.c) and the damping frame (absorb.c),
+ *   - source and receiver files (sources.c, receiver.c), wavelets (wavelet.c),
+ *   - SU seismograms (outseis_glob.c, write_su.c) and binary snapshots (snap_ssg.c).
+ * Pure C; no CUDA types. Errors return non-zero with sofih_last_error().
+ */
+#ifndef SOFIHOST_H
+#define SOFIHOST_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SOFIH_MAX_L 8
+
+/* Parameters of one run (the GlobVar fields read_par_json.c fills). */
+typedef struct {
+    int weq;                   /* 2..7 (EL_ISO .. VEL_TTI) */
+    int nx, ny;
+    float dh, dt, time;
+    int nt;                    /* iround(TIME/DT) */
+    int fdorder, maxrelerror, L;
+    float f_ref, fl[SOFIH_MAX_L];
+    int fw, abs_type, free_surf, boundary;
+    float npower, k_max_cpml, vppml, fpml, damping;
+    int source_shape, source_type, run_multiple_shots;
+    char source_file[256];
+    int seismo, ndt, readrec, seis_format;
+    char rec_file[256], seis_file[256];
+    float refrec[2], xrec1, yrec1, xrec2, yrec2;
+    int ngeoph;
+    int snap, snap_format;
+    float tsnap1, tsnap2, tsnapinc;
+    int idx, idy;
+    char snap_file[256], mfile[256];
+} sofih_par;
+
+const char *sofih_last_error(void);
+
+/* Read a SOFI2D parameter file; `base_dir` (may be NULL) prefixes relative
+ * file names inside it. */
+int sofih_read_par(const char *path, sofih_par *p);
+
+/* Model-file suffixes the wave equation needs (vp vs rho [qp qs] [epsilon delta [theta]]). */
+int sofih_model_suffixes(int weq, const char **names, int max);
+/* Read MFILE.<suffix> for each needed suffix into out[k] (caller frees with free()). */
+int sofih_read_model(const sofih_par *p, const char *mfile, float **out, int max);
+
+/* ---- model preparation ---- */
+typedef struct sofih_prep sofih_prep;
+
+/* Prepare the arrays the time loop reads from the raw material of one model
+ * (arrays in model-file order [NX][NY], y fastest; unused ones may be NULL).
+ * nthreads <= 0 uses every core. */
+int sofih_prepare(const sofih_par *p, const float *vp, const float *vs, const float *rho, const float *qp,
+                  const float *qs, const float *eps, const float *del, const float *theta, int nthreads,
+                  sofih_prep **out);
+void sofih_prep_free(sofih_prep *m);
+/* Prepared 2-D arrays, each [NY][NX] (x fastest), named as sofi_set_model_field expects. */
+int sofih_prep_num_fields(const sofih_prep *m);
+const char *sofih_prep_field_name(const sofih_prep *m, int k);
+const float *sofih_prep_field(const sofih_prep *m, int k);
+/* 1-D arrays (CPML profiles, bip cip peta): returns the length, 0 if absent. */
+int sofih_prep_vector(const sofih_prep *m, const char *name, const float **data);
+/* Smallest / largest P velocity the model holds (for the CFL check). */
+void sofih_prep_vrange(const sofih_prep *m, float *vpmin, float *vpmax, float *vsmin, float *vsmax);
+/* FD coefficients hc[0..6] of holbergcoeff.c for (FDORDER, MAXRELERROR). */
+int sofih_holberg(int fdorder, int maxrelerror, float *hc);
+/* Stability bound of checkfd.c:41-52: DT <= DH / (sqrt(2) * sum|hc| * VMAX). */
+int sofih_check_cfl(const sofih_par *p, const sofih_prep *m, float *dt_max);
+
+/* ---- acquisition ---- */
+/* Sources: srcpos [12][nsrc] row-major in grid indices (reference srcpos_loc
+ * layout after splitsrc.c); xy [2][nsrc] physical coordinates. */
+int sofih_read_sources(const sofih_par *p, const char *path, float **srcpos, float **xy, int *nsrc);
+int sofih_wavelet(int shape, int nt, float dt, int nsrc, const float *srcpos, float *signals);
+/* Receivers (grid indices, duplicates removed, reference receiver.c). */
+int sofih_read_receivers(const sofih_par *p, const char *path, int **ix, int **iy, int *ntr);
+
+/* ---- output ---- */
+/* One SU file of a component; ep = energy source point (comp for the trace
+ * header's 'ep' as outseis_glob.c writes it). xs, ys: source position [m]. */
+int sofih_write_su(const char *path, const float *section, int ntr, int ns, const int *ix, const int *iy,
+                   float xs, float ys, const sofih_par *p, int ishot, int comp);
+/* Append frames to a binary snapshot file (float32, x outer, y inner). */
+int sofih_write_snap(const char *path, const float *frame, int n, int append);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

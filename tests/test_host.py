@@ -1,0 +1,104 @@
+"""The product's C host (libsofihost) against the oracle and the reference's files.
+
+Model preparation must equal the oracle's (itself bit-identical to the
+compiled reference) exactly: both evaluate the reference's float/double
+expressions in the same order on the same libm.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from tests.golden.cases import CASES, synthetic_model
+from tests.helpers import case_config, prepared_model, GOLDEN
+
+
+@pytest.fixture(scope="module")
+def H():
+    from gpi_project_gb300 import build, host
+    build.build()
+    return host
+
+
+def par_from_case(H, case, cfg):
+    return H.make_par(weq=cfg.weq, nx=cfg.nx, ny=cfg.ny, dh=cfg.dh, dt=cfg.dt, nt=cfg.nt, fdorder=cfg.fdorder,
+                      maxrelerror=cfg.maxrelerror, L=cfg.L, f_ref=cfg.f_ref, fl=cfg.fl, fw=cfg.fw,
+                      abs_type=cfg.abs_type, free_surf=cfg.free_surf, boundary=cfg.boundary, npower=cfg.npower,
+                      k_max_cpml=cfg.k_max_cpml, vppml=cfg.vppml, fpml=cfg.fpml, damping=cfg.damping)
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_host_prepare_equals_oracle(H, case, oracle_mod):
+    O = oracle_mod
+    cfg = case_config(case)
+    mats = synthetic_model(case)
+    o = O.Oracle(cfg, "f32", 1)
+    o.set_material(mats)
+    ref_f, ref_v = prepared_model(o, cfg)
+    got_f, got_v = H.prepare(par_from_case(H, case, cfg), mats, nthreads=4)
+    for k, a in ref_f.items():
+        assert k in got_f, k
+        np.testing.assert_array_equal(got_f[k], a, err_msg=f"{case['name']} {k}")
+    for k, a in ref_v.items():
+        np.testing.assert_array_equal(got_v[k], a, err_msg=f"{case['name']} {k}")
+    o.close()
+
+
+def test_host_wavelet_equals_oracle(H, oracle_mod):
+    sp = np.zeros((12, 3), np.float32)
+    sp[3] = [0.0, 0.01, 0.002]
+    sp[4] = [25.0, 10.0, 40.0]
+    sp[5] = [1.0, 2.0, 0.5]
+    for shape in (1, 2, 4):
+        np.testing.assert_array_equal(H.wavelet(shape, 500, 1e-4, sp), oracle_mod.wavelet(shape, 500, 1e-4, sp))
+
+
+def test_host_holberg_table(H, oracle_mod):
+    for fd in (2, 4, 6, 8, 10, 12):
+        for me in range(5):
+            cfg = oracle_mod.SofiConfig(weq=2, nx=40, ny=40, fdorder=fd, maxrelerror=me, nt=2)
+            o = oracle_mod.Oracle(cfg)
+            np.testing.assert_array_equal(H.holberg(fd, me), o.vector("hc", 7))
+            o.close()
+
+
+def test_parameter_file_and_acquisition(H, tmp_path):
+    from tests.golden.cases import case_by_name, write_case
+    from tests.helpers import case_receivers, case_sources
+    case = case_by_name("el_mixed_sources")
+    jpath, _ = write_case(case, str(tmp_path))
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        p = H.read_par(jpath)
+        assert (p.nx, p.ny, p.fdorder, p.fw, p.abs_type, p.nt) == (case["nx"], case["ny"], 4, 10, 1, case["nt"])
+        assert np.float32(p.dt) == np.float32(case["dt"]) and p.seismo == 4 and p.ndt == 2
+        sp, xy = H.read_sources(p, "source.dat")
+        cfg = case_config(case)
+        np.testing.assert_array_equal(sp, case_sources(case, cfg))
+        ix, iy = H.read_receivers(p, "receiver.dat")
+        rx, ry = case_receivers(case, cfg)
+        np.testing.assert_array_equal(ix, rx)
+        np.testing.assert_array_equal(iy, ry)
+    finally:
+        os.chdir(cwd)
+
+
+def test_su_writer_matches_reference_headers(H, tmp_path):
+    """Trace headers as the reference writes them (compared with its own SU files)."""
+    from tests.golden.cases import case_by_name
+    from tests.helpers import case_receivers
+    case = case_by_name("el_cpml_fd8")
+    g = np.load(os.path.join(GOLDEN, f"ref_{case['name']}.npz"))
+    cfg = case_config(case)
+    p = par_from_case(H, case, cfg)
+    p.ndt = case["ndt"]
+    ix, iy = case_receivers(case, cfg)
+    data = g["seis_vx"]
+    out = str(tmp_path / "x.su")
+    H.write_su(out, data, ix, iy, case["sources"][0][0], case["sources"][0][1], p, 1, 1)
+    b = np.fromfile(out, np.uint8)
+    rec = 240 + 4 * data.shape[1]
+    hdr = b.reshape(-1, rec)[:, :240]
+    np.testing.assert_array_equal(hdr, g["hdr_vx"])
+    np.testing.assert_array_equal(b.reshape(-1, rec)[:, 240:].copy().view(np.float32), data)
