@@ -1,0 +1,359 @@
+#!/usr/bin/env python3
+"""Benchmark of the SOFI2D time loop on GB300: Gcell-updates/s and % of the HBM roofline.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c2] [--impl gb300|reference]
+
+A step is one complete forward solve of the workload (reset + NT time steps,
+what one time_loop() call of the reference does for one shot). Default
+workload: c2 (viscoelastic 4000 x 2000, L = 3, FD8, CPML 30, free surface,
+NT 6000; see gpi_project_gb300/workloads.py), seeded synthetic inputs.
+
+value      NX*NY*NT*shots / device time of the K timed steps (inputs resident in
+           HBM; CUDA events on the library's stream), in Gcell-updates/s
+e2e        the same through the C ABI from pinned host buffers: model upload,
+           sources/receivers, run, section download inside the timed region
+roofline   dominant kernel (the stress update): algorithmic bytes per launch /
+           its mean event-timed duration, against the measured HBM copy peak
+cpu_baseline  the oracle (CPU restatement of the reference, all host threads)
+           on a bounded sample of the same grid
+--impl reference  times that CPU implementation as the reference arm.
+Multi-GPU: replicas only (independent solves, no collective); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="c2")
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=0, help="time steps of the CPU sample (0 = auto)")
+    ap.add_argument("--nt", type=int, default=0,
+                    help="time steps per solve (default: the workload's NT; a small value keeps profiler captures short)")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel: str, workload: str):
+    """DRAM bytes per cell of `kernel` from the committed ncu summary, if any."""
+    p = os.path.join(REPO, "profiles", "traffic.json")
+    try:
+        with open(p) as fh:
+            d = json.load(fh)
+        return d[workload][kernel]["dram_bytes_per_cell"]
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def host_par(W):
+    from gpi_project_gb300 import host
+    return host.make_par(**W["par"])
+
+
+def cpu_sample(W, nsteps, nthreads):
+    """Gcell-updates/s of the oracle on `nsteps` time steps of the workload grid."""
+    from oracle import oracle as O
+    par = W["par"]
+    cfg = O.SofiConfig()
+    for k in ["weq", "nx", "ny", "dh", "dt", "fdorder", "maxrelerror", "L", "fw", "abs_type", "free_surf",
+              "npower", "k_max_cpml", "vppml", "fpml", "seismo", "ndt"]:
+        if k in par:
+            setattr(cfg, k, par[k])
+    cfg.f_ref, cfg.fl = par.get("f_ref", 0.0), list(par.get("fl", []))
+    cfg.nt = par["nt"]
+    o = O.Oracle(cfg, "f32", nthreads)
+    o.set_material({k: v.reshape(-1) for k, v in W["mats"].items()})
+    src = W["src"] if isinstance(W["src"], np.ndarray) else W["src"][0]
+    o.set_sources(src, O.wavelet(1, cfg.nt, cfg.dt, src))
+    o.set_receivers(*W["rec"])
+    t0 = time.perf_counter()
+    o.run(nsteps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return cfg.nx * cfg.ny * nsteps / dt / 1e9, dt
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def auto_cpu_steps(W, target_s=12.0, rate_per_core=10e6):
+    cells = W["par"]["nx"] * W["par"]["ny"]
+    n = int(target_s * rate_per_core * cpu_threads() / cells)
+    return max(5, min(n, W["par"]["nt"]))
+
+
+def run_reference(args, W):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    n = args.cpu_steps or auto_cpu_steps(W, target_s=6.0)
+    nth = cpu_threads()
+    for _ in range(args.warmup):
+        cpu_sample(W, max(1, n // 4), nth)
+    rates, secs = [], 0.0
+    for _ in range(args.steps):
+        r, s = cpu_sample(W, n, nth)
+        rates.append(r)
+        secs += s
+    val = float(np.mean(rates))
+    par = W["par"]
+    line = {
+        "impl": "reference", "metric": "Gcell-updates/s", "value": round(val, 4), "unit": "Gcell-updates/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * secs / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": W["name"], "nx": par["nx"], "ny": par["ny"], "nt": par["nt"], "weq": par["weq"],
+                   "fdorder": par["fdorder"], "L": par.get("L", 0), "sample_time_steps": n},
+        "cpu_baseline": {"value": round(val, 4), "unit": "Gcell-updates/s", "cores": nth, "kind": "port",
+                         "sample": f"{n} time steps of the {par['nx']}x{par['ny']} grid per step"},
+        "e2e": {"value": round(val, 4), "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    from gpi_project_gb300 import workloads
+    W = workloads.workload(args.workload)
+    if args.nt:
+        W["par"]["nt"] = args.nt
+    if args.impl == "reference":
+        if world > 1 and rank != 0:
+            return
+        from oracle import oracle as O
+        O.build()
+        run_reference(args, W)
+        return
+
+    import torch
+    from gpi_project_gb300 import TimeLoop, make_config, host
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    par = W["par"]
+    p = host_par(W)
+    fields, vecs = host.prepare(p, W["mats"])
+    dt_max = float(vecs.pop("_dt_max")[0])
+    stable = int(vecs.pop("_stable")[0])
+    if not stable:
+        raise SystemExit(f"workload {W['name']} violates the stability bound (DT_max {dt_max})")
+    nshots = W["nshots"]
+    cfg = make_config(weq=par["weq"], nx=par["nx"], ny=par["ny"], fdorder=par["fdorder"],
+                      maxrelerror=par["maxrelerror"], L=par.get("L", 0), dt=par["dt"], dh=par["dh"], nt=par["nt"],
+                      fw=par["fw"], abs_type=par["abs_type"], free_surf=par.get("free_surf", 0), seismo=par["seismo"],
+                      ndt=par["ndt"], nshots=nshots, shared_model=1)
+    t = TimeLoop(cfg, device=local)
+    srcs = W["src"] if isinstance(W["src"], list) else [W["src"]]
+    sigs = [host.wavelet(1, par["nt"], par["dt"], s) for s in srcs]
+
+    # pinned host copies of every input, for the end-to-end leg
+    def pinned(a):
+        buf = torch.empty(a.shape, dtype=torch.float32, pin_memory=True)
+        buf.numpy()[...] = a
+        return buf
+
+    pin_fields = {k: pinned(v) for k, v in fields.items()}
+    h2d_bytes = sum(v.numel() * 4 for v in pin_fields.values())
+
+    def upload_all():
+        t.set_model({k: v.numpy() for k, v in pin_fields.items()})
+        t.set_vectors(vecs)
+        for s in range(nshots):
+            t.set_sources(srcs[s % len(srcs)], sigs[s % len(sigs)], shot=s)
+            t.set_receivers(*W["rec"], shot=s)
+
+    upload_all()
+    stream = torch.cuda.ExternalStream(t.stream_handle())
+    cells = par["nx"] * par["ny"] * par["nt"] * nshots
+
+    def solve():
+        t.reset()
+        t.run(sync=False)
+
+    for _ in range(args.warmup):
+        solve()
+    t.synchronize()
+
+    # ---- device-timed region: inputs resident in HBM ----
+    peak, peak_kind = measured_peaks()
+    bpc = workloads.bytes_per_cell(par["weq"], par.get("L", 0))
+    t.set_kernel_timing(10)
+    launches0 = t.launch_count()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            ev0.record()
+        for _ in range(args.steps):
+            solve()
+        with torch.cuda.stream(stream):
+            ev1.record()
+        t.synchronize()
+        torch.cuda.synchronize()
+    dev_ms = ev0.elapsed_time(ev1)
+    launches = t.launch_count() - launches0
+    ms_s, n_s = t.kernel_time("update_s")
+    ms_v, n_v = t.kernel_time("update_v")
+    t.set_kernel_timing(0)
+    if world > 1:
+        tt = torch.tensor([dev_ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        dev_ms = float(tt.item())
+    value = cells * args.steps * world / (dev_ms * 1e-3) / 1e9
+
+    # ---- end to end through the C ABI: host buffers in, sections out ----
+    ntr = len(W["rec"][0])
+    d2h_bytes = 0
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        upload_all()
+        solve()
+        comps = {1: ["vx", "vy"], 2: ["p"], 3: ["div", "curl"], 4: ["vx", "vy", "p", "div", "curl"]}[par["seismo"]]
+        for s in range(nshots):
+            for c in comps:
+                sec = t.section(c, shot=s)
+                d2h_bytes += sec.nbytes
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - w0
+    e2e_val = cells * args.steps * world / e2e_s / 1e9
+    d2h_bytes //= max(args.steps, 1)
+
+    # ---- roofline of the dominant kernel ----
+    ncell = par["nx"] * par["ny"] * nshots
+    ach_s = bpc["update_s"] * ncell / (ms_s * 1e-3) / 1e9 if ms_s else None
+    traffic = traffic_from_profiles("update_s", W["name"])
+    roof = {"kernel": "k_update_s (stress + memory variables)", "bound": "hbm",
+            "achieved": round(ach_s, 1) if ach_s else None, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+            "frac": round(ach_s / peak, 4) if ach_s else None,
+            "traffic": round(traffic * ncell) if traffic else None,
+            "algorithmic_bytes_per_launch": bpc["update_s"] * ncell,
+            "mean_launch_ms": round(ms_s, 4), "timed_launches": n_s}
+    step_roof = {"bytes_per_cell": bpc["step"], "achieved": round(bpc["step"] * value / world, 1),
+                 "frac": round(bpc["step"] * value / world / peak, 4), "unit": "GB/s",
+                 "update_v_mean_ms": round(ms_v, 4), "update_s_mean_ms": round(ms_s, 4)}
+    if rank != 0:
+        return
+    out = {
+        "metric": "Gcell-updates/s", "value": round(value, 4), "unit": "Gcell-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded; gpi_project_gb300/workloads.py)",
+        "config": {"workload": W["name"], "nx": par["nx"], "ny": par["ny"], "nt": par["nt"], "weq": par["weq"],
+                   "fdorder": par["fdorder"], "L": par.get("L", 0), "fw": par["fw"], "shots": nshots,
+                   "free_surf": par.get("free_surf", 0), "receivers": ntr,
+                   "l2": "inputs larger than L2 (wavefield + model ~0.85 GB)", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(e2e_val, 4), "unit": "Gcell-updates/s", "h2d_bytes_per_step": int(h2d_bytes),
+                "d2h_bytes_per_step": int(d2h_bytes)},
+        "roofline": roof, "step_roofline": step_roof, "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline and rank == 0:
+        n = args.cpu_steps or auto_cpu_steps(W)
+        from oracle import oracle as O
+        O.build()
+        r, s = cpu_sample(W, n, cpu_threads())
+        out["cpu_baseline"] = {"value": round(r, 4), "unit": "Gcell-updates/s", "cores": cpu_threads(),
+                               "kind": "port", "sample": f"{n} time steps of the {par['nx']}x{par['ny']} grid ({s:.1f} s)"}
+    print(json.dumps(out), flush=True)
+    t.close()
+
+
+if __name__ == "__main__":
+    main()

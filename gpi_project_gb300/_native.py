@@ -79,6 +79,10 @@ def load():
         "sofi_num_snapshots": ([vp, ip, ip], ctypes.c_int),
         "sofi_get_snapshot": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp], ctypes.c_int),
         "sofi_last_run_ms": ([vp, fp], ctypes.c_int),
+        "sofi_set_kernel_timing": ([vp, ctypes.c_int], ctypes.c_int),
+        "sofi_kernel_time": ([vp, ctypes.c_char_p, P(ctypes.c_double), P(ctypes.c_longlong)], ctypes.c_int),
+        "sofi_launch_count": ([vp, P(ctypes.c_longlong)], ctypes.c_int),
+        "sofi_get_stream": ([vp, P(vp)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

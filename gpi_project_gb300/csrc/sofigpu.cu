@@ -166,6 +166,13 @@ struct sofi_ctx {
     // snapshots
     int snap_nx = 0, snap_ny = 0, snap_total = 0, nsnap = 0;
     float *d_snap = nullptr;
+    // instrumentation
+    long long launches = 0;
+    int time_every = 0;
+    std::vector<cudaEvent_t> tev;   // 3 events per timed step: before v, after v, after s
+    size_t tev_used = 0;
+    double t_v_ms = 0, t_s_ms = 0;
+    long long t_count = 0;
 };
 
 namespace {
@@ -369,12 +376,36 @@ int launch_step(sofi_ctx *c, int nt)
     int nb = (S + 127) / 128;
     int kind = kind_of(cf.weq);
     bool visco = is_visco(cf.weq);
-    if (c->has_force)
+    if (c->has_force) {
         k_force_src<<<nb, 128, 0, st>>>(G, c->W, c->M, c->A, nt);
+        c->launches++;
+    }
+    bool timed = c->time_every > 0 && (nt % c->time_every) == 0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+    if (timed) {
+        if (c->tev_used + 3 > c->tev.size()) {
+            for (int k = 0; k < 3; k++) {
+                cudaEvent_t e;
+                CK(cudaEventCreate(&e));
+                c->tev.push_back(e);
+            }
+        }
+        e0 = c->tev[c->tev_used], e1 = c->tev[c->tev_used + 1], e2 = c->tev[c->tev_used + 2];
+        c->tev_used += 3;
+        CK(cudaEventRecord(e0, st));
+    }
     DISPATCH_ND(c->nd, (k_update_v<ND><<<grd, blk, 0, st>>>(G, c->W, c->M)));
-    if (cf.boundary)
+    c->launches++;
+    if (timed)
+        CK(cudaEventRecord(e1, st));
+    if (cf.boundary) {
         k_wrap_x<<<dim3((cf.ny + 127) / 128, S), 128, 0, st>>>(G, c->W.vx, c->W.vy, nullptr, c->nd);
+        c->launches++;
+    }
+    if (timed && cf.boundary)
+        CK(cudaEventRecord(e1, st));
     if (kind == TTI) {
+        c->launches++;
         DISPATCH_ND(c->nd, (k_tti_deriv<ND><<<grd, blk, 0, st>>>(G, c->W, c->M)));
         if (visco)
             k_update_s_tti<true><<<grd, blk, 0, st>>>(G, c->W, c->M);
@@ -391,6 +422,9 @@ int launch_step(sofi_ctx *c, int nt)
         else
             DISPATCH_ND(c->nd, (k_update_s<ND, VTI, false><<<grd, blk, 0, st>>>(G, c->W, c->M)))
     }
+    c->launches++;
+    if (timed)
+        CK(cudaEventRecord(e2, st));
     bool sample = cf.seismo && c->total_rec > 0 && nt % cf.ndt == 0 && nt < cf.nt;
     int ins = sample ? nt / cf.ndt : 0;
     int maxrec = 0;
@@ -402,19 +436,26 @@ int launch_step(sofi_ctx *c, int nt)
             DISPATCH_ND(c->nd, (k_seis_deriv<ND, true><<<rg, 128, 0, st>>>(G, c->W, c->M, c->A, ins)))
         else
             DISPATCH_ND(c->nd, (k_seis_deriv<ND, false><<<rg, 128, 0, st>>>(G, c->W, c->M, c->A, ins)))
+        c->launches++;
     }
     k_stress_src<<<nb, 128, 0, st>>>(G, c->W, c->A, nt);
+    c->launches++;
     if (cf.free_surf) {
         dim3 sg((cf.nx + 127) / 128, S);
         if (visco)
             DISPATCH_ND(c->nd, (k_surface<ND, true><<<sg, 128, 0, st>>>(G, c->W, c->M)))
         else
             DISPATCH_ND(c->nd, (k_surface<ND, false><<<sg, 128, 0, st>>>(G, c->W, c->M)))
+        c->launches++;
     }
-    if (cf.boundary)
+    if (cf.boundary) {
         k_wrap_x<<<dim3((cf.ny + 127) / 128, S), 128, 0, st>>>(G, c->W.sxx, c->W.syy, c->W.sxy, c->nd);
-    if (sample && cf.seismo != 3)
+        c->launches++;
+    }
+    if (sample && cf.seismo != 3) {
         k_seis<<<rg, 128, 0, st>>>(G, c->W, c->M, c->A, ins, cf.seismo);
+        c->launches++;
+    }
     if (cf.snap && nt >= cf.snap_first && nt <= cf.snap_last &&
         (nt == cf.snap_first || (cf.snap_inc > 0 && (nt - cf.snap_first) % cf.snap_inc == 0)) &&
         c->nsnap < c->snap_total) {
@@ -425,6 +466,7 @@ int launch_step(sofi_ctx *c, int nt)
         DISPATCH_ND(c->nd, (k_snap<ND><<<sg, 128, 0, st>>>(G, c->W, c->M, out, c->snap_nx, c->snap_ny, cf.idx,
                                                           cf.idy, cf.snap, frame_stride)));
         c->nsnap++;
+        c->launches++;
     }
     return 0;
 }
@@ -624,6 +666,8 @@ int sofi_destroy(sofi_ctx *c)
         cudaStreamSynchronize(c->stream);
         cudaStreamDestroy(c->stream);
     }
+    for (auto e : c->tev)
+        cudaEventDestroy(e);
     if (c->ev0)
         cudaEventDestroy(c->ev0);
     if (c->ev1)
@@ -804,7 +848,61 @@ int sofi_synchronize(sofi_ctx *c)
     CK(cudaSetDevice(c->device));
     CK(cudaStreamSynchronize(c->stream));
     cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1);
+    for (size_t k = 0; k + 3 <= c->tev_used; k += 3) {
+        float a = 0, b = 0;
+        CK(cudaEventElapsedTime(&a, c->tev[k], c->tev[k + 1]));
+        CK(cudaEventElapsedTime(&b, c->tev[k + 1], c->tev[k + 2]));
+        c->t_v_ms += a, c->t_s_ms += b, c->t_count++;
+    }
+    c->tev_used = 0;
     return check_status(c);
+}
+
+int sofi_set_kernel_timing(sofi_ctx *c, int every)
+{
+    if (!c || every < 0)
+        return fail(SOFI_E_ARG, "invalid timing arguments");
+    CK(cudaStreamSynchronize(c->stream));
+    c->time_every = every;
+    c->tev_used = 0;
+    c->t_v_ms = c->t_s_ms = 0;
+    c->t_count = 0;
+    return 0;
+}
+
+int sofi_kernel_time(sofi_ctx *c, const char *name, double *avg_ms, long long *count)
+{
+    if (!c || !name || !avg_ms || !count)
+        return fail(SOFI_E_ARG, "null argument");
+    int rc = sofi_synchronize(c);
+    if (rc)
+        return rc;
+    double t;
+    if (!strcmp(name, "update_v"))
+        t = c->t_v_ms;
+    else if (!strcmp(name, "update_s"))
+        t = c->t_s_ms;
+    else
+        return fail(SOFI_E_ARG, "unknown timed kernel '%s'", name);
+    *count = c->t_count;
+    *avg_ms = c->t_count ? t / c->t_count : 0.0;
+    return 0;
+}
+
+int sofi_get_stream(sofi_ctx *c, void **stream)
+{
+    if (!c || !stream)
+        return fail(SOFI_E_ARG, "null argument");
+    *stream = (void *)c->stream;
+    return 0;
+}
+
+int sofi_launch_count(sofi_ctx *c, long long *launches)
+{
+    if (!c || !launches)
+        return fail(SOFI_E_ARG, "null argument");
+    *launches = c->launches;
+    return 0;
 }
 
 int sofi_current_step(sofi_ctx *c, int *step)

@@ -101,6 +101,24 @@ class TimeLoop:
         N.check(self.lib.sofi_last_run_ms(self.h, ctypes.byref(ms)))
         return ms.value
 
+    def set_kernel_timing(self, every: int):
+        N.check(self.lib.sofi_set_kernel_timing(self.h, every))
+
+    def kernel_time(self, name: str):
+        ms, n = ctypes.c_double(), ctypes.c_longlong()
+        N.check(self.lib.sofi_kernel_time(self.h, name.encode(), ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
+    def stream_handle(self) -> int:
+        s = ctypes.c_void_p()
+        N.check(self.lib.sofi_get_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
+
+    def launch_count(self) -> int:
+        n = ctypes.c_longlong()
+        N.check(self.lib.sofi_launch_count(self.h, ctypes.byref(n)))
+        return n.value
+
     # -------------------------------------------------------------- outputs
     def section(self, comp, shot: int = 0) -> np.ndarray:
         ns = ctypes.c_int()

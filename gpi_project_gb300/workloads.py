@@ -1,0 +1,137 @@
+"""Seeded synthetic forward-modelling workloads.
+
+The reference publishes no benchmark suite; these stand in for the five
+benchmark configurations with their shapes, sizes and value distributions:
+
+  c1  isotropic elastic, 400 x 400, DH 1 m, DT 1e-4 s, NT 2000, FD8 Holberg,
+      CPML 20; three layers (Vp 2000/2800/3500, rho 1800/2100/2400, Vs = Vp/1.73)
+      with 2 % Gaussian perturbation; explosive Ricker 25 Hz at the top centre;
+      100 receivers at 10 m depth recording vx, vy
+  c2  viscoelastic, 4000 x 2000, DH 2 m, DT 2e-4 s, NT 6000, FD8, L = 3
+      (5/15/50 Hz, F_REF 15 Hz), CPML 30, free surface; smooth random Vp
+      1500-4500, Vs = Vp/1.8, Gardner density, smooth Q 20-100 (Qp = Qs);
+      Ricker 15 Hz vertical force; 1000 receivers
+  c3  TTI elastic, 2048 x 2048, DH 2.5 m, DT 2.5e-4 s, NT 4000, FD6, CPML 20;
+      Vp 2000-4000, Vs = Vp/1.8, rho 2000-2600, eps 0-0.25, delta -0.1-0.15,
+      tilt 0-45 deg smoothed over 20 cells; explosive Ricker 20 Hz; 512 receivers
+  c4  64 shots on the c1 layered model enlarged to 2000 x 1000 with c2's Q field
+      and L = 3, NT 4000, explosive sources spread across the surface
+Values are drawn from numpy's PCG64 with seed 1000 + config number.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def smooth_field(rng, nx, ny, corr_cells, lo, hi):
+    """Gaussian-correlated random field scaled to [lo, hi], shape [NX][NY]."""
+    w = rng.standard_normal((nx, ny))
+    kx = np.fft.fftfreq(nx)[:, None]
+    ky = np.fft.rfftfreq(ny)[None, :]
+    s = corr_cells / (2.0 * math.pi)
+    g = np.exp(-0.5 * ((kx * 2 * math.pi * s) ** 2 + (ky * 2 * math.pi * s) ** 2))
+    f = np.fft.irfft2(np.fft.rfft2(w) * g, s=(nx, ny))
+    f = (f - f.min()) / max(f.max() - f.min(), 1e-30)
+    return (lo + (hi - lo) * f).astype(np.float32)
+
+
+def layered(rng, nx, ny):
+    y = np.arange(ny)
+    layer = np.where(y < ny // 3, 0, np.where(y < 2 * ny // 3, 1, 2))
+    vp = np.array([2000.0, 2800.0, 3500.0])[layer][None, :] * (1.0 + 0.02 * rng.standard_normal((nx, ny)))
+    rho = np.array([1800.0, 2100.0, 2400.0])[layer][None, :] * (1.0 + 0.02 * rng.standard_normal((nx, ny)))
+    vp = vp.astype(np.float32)
+    return vp, (vp / 1.73).astype(np.float32), rho.astype(np.float32)
+
+
+def _srcpos(points, dh, fc, stype, tshift=0.0, amp=1.0):
+    """srcpos [12][n] in grid indices (reference srcpos_loc layout)."""
+    n = len(points)
+    sp = np.zeros((12, n), np.float32)
+    for k, (x, y) in enumerate(points):
+        sp[0, k] = math.floor(np.float32(x) / np.float32(dh)) + 1
+        sp[1, k] = math.floor(np.float32(y) / np.float32(dh)) + 1
+        sp[3, k], sp[4, k], sp[5, k], sp[7, k] = tshift, fc, amp, stype
+    return sp
+
+
+def workload(name: str) -> dict:
+    """Parameters (sofihost field names), material arrays, sources, receivers."""
+    if name == "c1":
+        rng = np.random.default_rng(1001)
+        nx = ny = 400
+        vp, vs, rho = layered(rng, nx, ny)
+        par = dict(weq=2, nx=nx, ny=ny, dh=1.0, dt=1e-4, nt=2000, fdorder=8, maxrelerror=1, fw=20, abs_type=1,
+                   npower=4.0, k_max_cpml=1.0, vppml=float(vp.max()), fpml=25.0, seismo=1, ndt=1)
+        mats = dict(vp=vp, vs=vs, rho=rho)
+        src = _srcpos([(200.0, 5.0)], 1.0, 25.0, 1)
+        xs = np.linspace(21.0, 378.0, 100)
+        rec = (np.floor(xs / 1.0).astype(np.int32) + 1, np.full(100, 11, np.int32))
+        nshots = 1
+    elif name == "c2":
+        rng = np.random.default_rng(1002)
+        nx, ny = 4000, 2000
+        vp = smooth_field(rng, nx, ny, 60, 1500.0, 4500.0)
+        vs = (vp / 1.8).astype(np.float32)
+        rho = (310.0 * vp.astype(np.float64) ** 0.25).astype(np.float32)
+        q = smooth_field(rng, nx, ny, 60, 20.0, 100.0)
+        par = dict(weq=3, nx=nx, ny=ny, dh=2.0, dt=2e-4, nt=6000, fdorder=8, maxrelerror=1, L=3, f_ref=15.0,
+                   fl=[5.0, 15.0, 50.0], fw=30, abs_type=1, free_surf=1, npower=4.0, k_max_cpml=1.0,
+                   vppml=4500.0, fpml=15.0, seismo=1, ndt=1)
+        mats = dict(vp=vp, vs=vs, rho=rho, qp=q, qs=q)
+        src = _srcpos([(4000.0, 10.0)], 2.0, 15.0, 3)
+        xs = np.linspace(31 * 2.0, (nx - 32) * 2.0, 1000)
+        rec = (np.floor(xs / 2.0).astype(np.int32) + 1, np.full(1000, 6, np.int32))
+        nshots = 1
+    elif name == "c3":
+        rng = np.random.default_rng(1003)
+        nx = ny = 2048
+        vp = smooth_field(rng, nx, ny, 20, 2000.0, 4000.0)
+        vs = (vp / 1.8).astype(np.float32)
+        rho = smooth_field(rng, nx, ny, 20, 2000.0, 2600.0)
+        mats = dict(vp=vp, vs=vs, rho=rho, epsilon=smooth_field(rng, nx, ny, 20, 0.0, 0.25),
+                    delta=smooth_field(rng, nx, ny, 20, -0.1, 0.15), theta=smooth_field(rng, nx, ny, 20, 0.0, 45.0))
+        par = dict(weq=6, nx=nx, ny=ny, dh=2.5, dt=2.5e-4, nt=4000, fdorder=6, maxrelerror=1, fw=20, abs_type=1,
+                   npower=4.0, k_max_cpml=1.0, vppml=5000.0, fpml=20.0, seismo=1, ndt=1)
+        src = _srcpos([(2560.0, 30.0)], 2.5, 20.0, 1)
+        xs = np.linspace(21 * 2.5, (nx - 22) * 2.5, 512)
+        rec = (np.floor(xs / 2.5).astype(np.int32) + 1, np.full(512, 25, np.int32))
+        nshots = 1
+    elif name == "c4":
+        rng = np.random.default_rng(1004)
+        nx, ny = 2000, 1000
+        vp, vs, rho = layered(rng, nx, ny)
+        q = smooth_field(rng, nx, ny, 30, 20.0, 100.0)
+        par = dict(weq=3, nx=nx, ny=ny, dh=1.0, dt=1e-4, nt=4000, fdorder=8, maxrelerror=1, L=3, f_ref=15.0,
+                   fl=[5.0, 15.0, 50.0], fw=20, abs_type=1, npower=4.0, k_max_cpml=1.0, vppml=3600.0,
+                   fpml=25.0, seismo=1, ndt=1)
+        mats = dict(vp=vp, vs=vs, rho=rho, qp=q, qs=q)
+        xsrc = np.linspace(30.0, nx - 31.0, 64)
+        src = [_srcpos([(x, 5.0)], 1.0, 25.0, 1) for x in xsrc]
+        xs = np.linspace(21.0, nx - 22.0, 200)
+        rec = (np.floor(xs).astype(np.int32) + 1, np.full(200, 11, np.int32))
+        nshots = 64
+    else:
+        raise KeyError(name)
+    par.setdefault("L", 0)
+    return dict(name=name, par=par, mats=mats, src=src, rec=rec, nshots=nshots)
+
+
+# Algorithmic bytes per cell-update (each evolving state array read and written
+# once, each per-cell coefficient array read once; CPML frame memory, sources
+# and receivers not credited).
+def bytes_per_cell(weq: int, L: int) -> dict:
+    """Per-kernel and whole-step algorithmic bytes of one cell-update."""
+    if weq == 2:
+        return {"update_v": 36, "update_s": 44, "step": 60}
+    if weq == 3:
+        return {"update_v": 36, "update_s": 8 + 24 + 24 * L + 24, "step": 8 * (5 + 3 * L) + 4 * 8}
+    if weq == 4:
+        return {"update_v": 36, "update_s": 8 + 24 + 16, "step": 64}
+    if weq == 6:
+        return {"update_v": 36, "update_s": 8 + 24 + 32, "step": 80}
+    if weq == 5:
+        return {"update_v": 36, "update_s": 8 + 24 + 24 * L + 32, "step": 8 * (5 + 3 * L) + 4 * 10}
+    return {"update_v": 36, "update_s": 8 + 24 + 24 * L + 64, "step": 8 * (5 + 3 * L) + 4 * 18}

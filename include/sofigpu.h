@@ -169,6 +169,20 @@ int sofi_get_snapshot(sofi_ctx *ctx, int shot, int k, int comp, float *host);
 /* Device time (ms, CUDA events on the context's stream) of the last sofi_run. */
 int sofi_last_run_ms(sofi_ctx *ctx, float *ms);
 
+/* ---- instrumentation (no counterpart in the reference; replaces its
+ * Perform timers, src/perform_struct.h) ---- */
+/* Bracket the velocity and stress kernels of every `every`-th time step with
+ * CUDA events on the context's stream (0 switches it off and clears totals). */
+int sofi_set_kernel_timing(sofi_ctx *ctx, int every);
+/* Mean device time per timed launch of kernel `name` ("update_v", "update_s")
+ * and the number of timed launches since timing was switched on. */
+int sofi_kernel_time(sofi_ctx *ctx, const char *name, double *avg_ms, long long *count);
+/* Kernels launched by sofi_run since the context was created. */
+int sofi_launch_count(sofi_ctx *ctx, long long *launches);
+/* The context's CUDA stream (a cudaStream_t), for callers that order their own
+ * work or events with the time loop. */
+int sofi_get_stream(sofi_ctx *ctx, void **stream);
+
 #ifdef __cplusplus
 }
 #endif
