@@ -163,6 +163,7 @@ struct sofi_ctx {
     int *d_status = nullptr;
     int step = 0;
     float last_ms = 0.f;
+    bool run_pending = false;  // ev0/ev1 recorded by a sofi_run not yet synchronised
     // snapshots
     int snap_nx = 0, snap_ny = 0, snap_total = 0, nsnap = 0;
     float *d_snap = nullptr;
@@ -838,6 +839,7 @@ int sofi_run(sofi_ctx *c, int nsteps)
     }
     CK(cudaEventRecord(c->ev1, c->stream));
     CK(cudaGetLastError());
+    c->run_pending = true;
     return 0;
 }
 
@@ -847,7 +849,10 @@ int sofi_synchronize(sofi_ctx *c)
         return fail(SOFI_E_ARG, "null context");
     CK(cudaSetDevice(c->device));
     CK(cudaStreamSynchronize(c->stream));
-    cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1);
+    if (c->run_pending) {
+        CK(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
+        c->run_pending = false;
+    }
     for (size_t k = 0; k + 3 <= c->tev_used; k += 3) {
         float a = 0, b = 0;
         CK(cudaEventElapsedTime(&a, c->tev[k], c->tev[k + 1]));
