@@ -38,7 +38,25 @@ class SofiConfig(ctypes.Structure):
         ("idx", ctypes.c_int), ("idy", ctypes.c_int), ("nshots", ctypes.c_int), ("shared_model", ctypes.c_int)]]
 
 
+class TtiStressArgs(ctypes.Structure):
+    """sofi_tti_stress_args of include/sofigpu.h (device pointers as integers)."""
+    _fields_ = ([(k, ctypes.c_void_p) for k in
+                 ["vx", "vy", "sxx", "syy", "sxy", "r", "p", "q", "psi_vxx", "psi_vyx", "psi_vyy", "psi_vxy",
+                  "c11", "c13", "c33", "c15", "c35", "c55ipjp", "c15ipjp", "c35ipjp", "c11d_base", "c13d_base",
+                  "c33d_base", "c15d_base", "c35d_base", "c55ipjpd_base", "c15ipjpd_base", "c35ipjpd_base",
+                  "absorb", "K_x", "a_x", "b_x", "K_x_half", "a_x_half", "b_x_half", "K_y", "a_y", "b_y",
+                  "K_y_half", "a_y_half", "b_y_half"]]
+                + [("bip", ctypes.c_float * 8), ("cip", ctypes.c_float * 8), ("peta", ctypes.c_float * 8),
+                   ("hc", ctypes.c_float * 7)])
+
+
+NOALLOC_MAX_CELLS = 1 << 20
 _LIB = None
+
+
+def padded_shape(nx: int, ny: int) -> tuple:
+    """(rows, pitch) of one 2-D field in the library's device layout."""
+    return ny + 16, ((nx + 16 + 31) // 32) * 32
 
 
 def lib_path() -> str:
@@ -83,6 +101,7 @@ def load():
         "sofi_kernel_time": ([vp, ctypes.c_char_p, P(ctypes.c_double), P(ctypes.c_longlong)], ctypes.c_int),
         "sofi_launch_count": ([vp, P(ctypes.c_longlong)], ctypes.c_int),
         "sofi_get_stream": ([vp, P(vp)], ctypes.c_int),
+        "sofi_tti_stress_noalloc": ([P(SofiConfig), P(TtiStressArgs), vp], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

@@ -1011,4 +1011,103 @@ int sofi_last_run_ms(sofi_ctx *c, float *ms)
     return rc;
 }
 
+// ---- allocation-free TTI stress update ------------------------------------
+//
+// The derivative fields of the TTI stress update (raw and CPML-stretched, 4
+// each) live here for sofi_tti_stress_noalloc: a fixed array that every GPU
+// loading the library holds until exit, so the entry point needs no
+// cudaMalloc. Host code must not use this name as a device address: it looks
+// the address up with cudaGetSymbolAddress once per device.
+static __device__ __align__(256) float g_noalloc_scratch[8 * SOFI_NOALLOC_MAX_CELLS];
+
+namespace {
+constexpr int kMaxDevices = 64;
+float *g_noalloc_ptr[kMaxDevices] = {};
+}  // namespace
+
+int sofi_tti_stress_noalloc(const sofi_config *cfg, const sofi_tti_stress_args *a, void *stream)
+{
+    if (!cfg || !a)
+        return fail(SOFI_E_ARG, "null argument");
+    if (cfg->weq != SOFI_EL_TTI && cfg->weq != SOFI_VEL_TTI)
+        return fail(SOFI_E_ARG, "sofi_tti_stress_noalloc: WEQ must be EL_TTI or VEL_TTI (got %d)", cfg->weq);
+    sofi_config c1 = *cfg;
+    c1.nshots = 1;
+    c1.seismo = 0;
+    c1.snap = 0;
+    int rc = check_config(&c1);
+    if (rc)
+        return rc;
+    int pitch = pitch_for(cfg->nx);
+    long long fsz = (long long)pitch * (cfg->ny + 2 * HY);
+    if (fsz > SOFI_NOALLOC_MAX_CELLS)
+        return fail(SOFI_E_ARG,
+                    "sofi_tti_stress_noalloc: padded grid of %lld cells exceeds the fixed scratch of %ld cells "
+                    "(NX %d x NY %d pads to %d x %d)",
+                    fsz, (long)SOFI_NOALLOC_MAX_CELLS, cfg->nx, cfg->ny, pitch, cfg->ny + 2 * HY);
+    bool visco = cfg->weq == SOFI_VEL_TTI;
+    int abs_type = cfg->fw > 0 ? cfg->abs_type : 0;
+    if (!a->vx || !a->vy || !a->sxx || !a->syy || !a->sxy || !a->c11 || !a->c13 || !a->c33 || !a->c15 || !a->c35 ||
+        !a->c55ipjp || !a->c15ipjp || !a->c35ipjp)
+        return fail(SOFI_E_ARG, "sofi_tti_stress_noalloc: a wavefield or modulus pointer is NULL");
+    if (visco && (!a->r || !a->p || !a->q || !a->c11d_base || !a->c13d_base || !a->c33d_base || !a->c15d_base ||
+                  !a->c35d_base || !a->c55ipjpd_base || !a->c15ipjpd_base || !a->c35ipjpd_base))
+        return fail(SOFI_E_ARG, "sofi_tti_stress_noalloc: VEL_TTI needs memory variables and defect bases");
+    if (abs_type == 1 && (!a->psi_vxx || !a->psi_vyx || !a->psi_vyy || !a->psi_vxy || !a->K_x || !a->a_x ||
+                          !a->b_x || !a->K_x_half || !a->a_x_half || !a->b_x_half || !a->K_y || !a->a_y ||
+                          !a->b_y || !a->K_y_half || !a->a_y_half || !a->b_y_half))
+        return fail(SOFI_E_ARG, "sofi_tti_stress_noalloc: CPML needs psi memory and profiles");
+    if (abs_type == 2 && !a->absorb)
+        return fail(SOFI_E_ARG, "sofi_tti_stress_noalloc: damping frame needs absorb");
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices)
+        return fail(SOFI_E_ARG, "device %d beyond the %d the scratch table covers", dev, kMaxDevices);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_ptr[dev] = static_cast<float *>(p);
+    }
+    Geo G{};
+    G.nx = cfg->nx, G.ny = cfg->ny, G.pitch = pitch, G.nshots = 1, G.fsz = fsz;
+    G.fw = cfg->fw, G.fw2 = 2 * cfg->fw, G.abs_type = abs_type;
+    G.free_surf = cfg->free_surf, G.boundary = cfg->boundary, G.L = visco ? cfg->L : 0;
+    G.model_stride_on = 0, G.el_tti_rb_short = (cfg->weq == SOFI_EL_TTI);
+    int fw = abs_type ? cfg->fw : 0;
+    G.gx2 = fw, G.gx3 = cfg->nx - fw, G.gy2 = fw, G.gy3 = cfg->ny - fw;
+    if (cfg->free_surf)
+        G.gy2 = 0;
+    if (cfg->boundary)
+        G.gx2 = 0, G.gx3 = cfg->nx;
+    G.dt = cfg->dt, G.dh = cfg->dh, G.dtdh = cfg->dt / cfg->dh, G.dhi = 1.0f / cfg->dh, G.dthalbe = cfg->dt / 2.0f;
+    for (int k = 0; k < 7; k++)
+        G.hc[k] = a->hc[k];
+    Wave W{};
+    W.vx = const_cast<float *>(a->vx), W.vy = const_cast<float *>(a->vy);
+    W.sxx = a->sxx, W.syy = a->syy, W.sxy = a->sxy, W.r = a->r, W.p = a->p, W.q = a->q;
+    W.psi_vxx = a->psi_vxx, W.psi_vyx = a->psi_vyx, W.psi_vyy = a->psi_vyy, W.psi_vxy = a->psi_vxy;
+    W.draw = g_noalloc_ptr[dev];
+    W.dcor = g_noalloc_ptr[dev] + 4 * fsz;
+    Model M{};
+    M.c11 = a->c11, M.c13 = a->c13, M.c33 = a->c33, M.c15 = a->c15, M.c35 = a->c35;
+    M.c55ipjp = a->c55ipjp, M.c15ipjp = a->c15ipjp, M.c35ipjp = a->c35ipjp;
+    M.c11b = a->c11d_base, M.c13b = a->c13d_base, M.c33b = a->c33d_base, M.c15b = a->c15d_base;
+    M.c35b = a->c35d_base, M.c55ipjpb = a->c55ipjpd_base, M.c15ipjpb = a->c15ipjpd_base;
+    M.c35ipjpb = a->c35ipjpd_base, M.absorb = a->absorb;
+    M.K_x = a->K_x, M.a_x = a->a_x, M.b_x = a->b_x, M.K_x_half = a->K_x_half, M.a_x_half = a->a_x_half;
+    M.b_x_half = a->b_x_half, M.K_y = a->K_y, M.a_y = a->a_y, M.b_y = a->b_y, M.K_y_half = a->K_y_half;
+    M.a_y_half = a->a_y_half, M.b_y_half = a->b_y_half;
+    for (int l = 0; l < G.L; l++)
+        M.bip[l] = a->bip[l], M.cip[l] = a->cip[l], M.peta[l] = a->peta[l];
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    dim3 blk(BX, BY), grd((cfg->nx + BX - 1) / BX, (cfg->ny + BY - 1) / BY, 1);
+    DISPATCH_ND(cfg->fdorder / 2, (k_tti_deriv<ND><<<grd, blk, 0, st>>>(G, W, M)));
+    if (visco)
+        k_update_s_tti<true><<<grd, blk, 0, st>>>(G, W, M);
+    else
+        k_update_s_tti<false><<<grd, blk, 0, st>>>(G, W, M);
+    CK(cudaGetLastError());
+    return 0;
+}
+
 }  // extern "C"

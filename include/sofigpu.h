@@ -183,6 +183,59 @@ int sofi_launch_count(sofi_ctx *ctx, long long *launches);
  * work or events with the time loop. */
 int sofi_get_stream(sofi_ctx *ctx, void **stream);
 
+/* ---- allocation-free TTI stress update ------------------------------- */
+
+/* Maximum padded cells (pitch * (NY + 16)) sofi_tti_stress_noalloc accepts. */
+#define SOFI_NOALLOC_MAX_CELLS (1L << 20)
+
+/* Device buffers of one shot for sofi_tti_stress_noalloc. Every 2-D field uses
+ * this library's padded layout: float[(NY + 16) * pitch] with
+ * pitch = ((NX + 16 + 31) / 32) * 32 and cell (j, i) at
+ * (j - 1 + 8) * pitch + (i - 1 + 8); ghost cells zero. */
+typedef struct {
+    const float *vx, *vy;               /* in: velocities after this step's velocity update */
+    float *sxx, *syy, *sxy;             /* in/out: stresses */
+    float *r, *p, *q;                   /* in/out, VEL_TTI only: L fields each, one after another */
+    float *psi_vxx, *psi_vyx;           /* in/out, CPML only: [NY][2FW] */
+    float *psi_vyy, *psi_vxy;           /* in/out, CPML only: [2FW][NX] */
+    /* in: the stress update's moduli (EL_TTI: DT-scaled c*, VEL_TTI: unrelaxed c*u) */
+    const float *c11, *c13, *c33, *c15, *c35, *c55ipjp, *c15ipjp, *c35ipjp;
+    /* in, VEL_TTI only: relaxed modulus * tau of each defect (see sofi_set_model_field) */
+    const float *c11d_base, *c13d_base, *c33d_base, *c15d_base, *c35d_base, *c55ipjpd_base, *c15ipjpd_base,
+        *c35ipjpd_base;
+    const float *absorb;                /* in, damping frame only */
+    /* in, CPML only: the 2*FW-value profiles of PML_pro.c, on the device */
+    const float *K_x, *a_x, *b_x, *K_x_half, *a_x_half, *b_x_half;
+    const float *K_y, *a_y, *b_y, *K_y_half, *a_y_half, *b_y_half;
+    float bip[8], cip[8], peta[8];      /* VEL_TTI: L values each (host values) */
+    float hc[7];                        /* FD coefficients (holbergcoeff.c) */
+} sofi_tti_stress_args;
+
+/* The stress half of one TTI time step -- the velocity derivatives, their
+ * CPML stretch and the stress / memory-variable update of
+ * update_s_{elastic,visc}_TTI_{interior,PML,abs}.c -- on buffers the caller
+ * owns, allocating nothing. It has no counterpart in the reference: it exists
+ * for callers that cannot allocate device memory (a host process that runs
+ * under a fixed memory budget set at start-up, or code already inside a
+ * stream capture where a cudaMalloc would break the capture), and runs the
+ * same kernels as sofi_run's TTI path.
+ *
+ * The eight derivative fields this update needs between its two kernels live
+ * in one array of the library, SOFI_NOALLOC_MAX_CELLS * 8 floats (32 MiB),
+ * which every GPU that loads the library holds until the process exits;
+ * grids whose padded size exceeds SOFI_NOALLOC_MAX_CELLS are rejected with
+ * SOFI_E_ARG. The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call before
+ * any stream capture. All calls share the array: calls whose work overlaps on
+ * the GPU (other streams, other host threads) race, so order them on one
+ * stream. Every value read from the array is written earlier in the same call,
+ * so nothing has to be cleared between calls.
+ *
+ * cfg: WEQ must be SOFI_EL_TTI or SOFI_VEL_TTI; nshots and the acquisition
+ * fields are ignored. stream: a cudaStream_t (NULL = legacy default stream).
+ * Returns after the work is queued; errors of the launch are reported. */
+int sofi_tti_stress_noalloc(const sofi_config *cfg, const sofi_tti_stress_args *args, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
