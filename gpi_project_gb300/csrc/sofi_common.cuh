@@ -1,0 +1,198 @@
+// sofi_common.cuh -- types, layout and inline device helpers shared by the kernels.
+//
+// (Kernel overview: see sofi_kernels.cuh.)
+//
+// sofi_kernels.cuh -- device kernels of the SOFI2D time step on sm_103a.
+//
+// One time step of the reference's time_loop (src/time_loop.c:42-322) is
+//   k_force_src  force sources before the velocity update (update_v_interior.c:49-71)
+//   k_update_v   velocity update, all cells, CPML / damping frame by predicate
+//                (update_v_interior.c, update_v_PML.c, update_v_abs.c)
+//   k_wrap_x     periodic x only: ghost columns (exchange_v.c / exchange_s.c, one rank)
+//   k_update_s   stress update with the velocity derivatives recomputed from v in
+//                registers (v_derivatives.c fused away), CPML / damping by predicate
+//   k_tti_deriv + k_update_s_tti   TTI: derivatives (raw and CPML-stretched) are
+//                stored so the 4-point averages can follow the reference's
+//                region-by-region order (update_s_elastic_TTI_PML.c)
+//   k_seis_deriv div/curl sampling (derivatives as the stress update left them)
+//   k_stress_src explosive / moment-tensor sources + NaN probe (psource.c, eqsource.c)
+//   k_surface    free surface, one thread per column (surface_elastic.c, surface.c)
+//   k_seis       vx, vy, p sampling (seismo_ssg.c)
+//   k_snap       snapshot frame (snap_ssg.c)
+//
+// Layout: every 2-D field is a padded [NY + 2*HY][pitch] float array with the
+// interior cell (j, i) at ((j-1+HY) * pitch + (i-1+HX)); HX = HY = 8 >= ND + 1.
+// The shot index is the slowest dimension (field = base + shot * fsz). Ghost
+// cells stay zero (or hold the periodic copy), as the reference's edge ranks.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sofi {
+
+constexpr int HX = 8;
+constexpr int HY = 8;
+constexpr int MAXL = 8;
+constexpr int BX = 32;  // threads per block in x
+constexpr int BY = 8;   // threads per block in y
+
+enum Kind { ISO = 0, VTI = 1, TTI = 2 };
+
+struct Geo {
+    int nx, ny, pitch, nshots;
+    long long fsz;          // floats per 2-D field
+    int fw, fw2;            // frame width, 2*FW
+    int gx2, gx3, gy2, gy3; // reference subgrid_bounds (one rank)
+    int abs_type;           // 0 none, 1 CPML, 2 damping (0 when FW == 0)
+    int free_surf, boundary, L;
+    int model_stride_on;    // 1: model per shot, 0: shared
+    int el_tti_rb_short;    // EL_TTI CPML: right-bottom corner pass stops at NY-1
+    float dt, dh, dtdh, dhi, dthalbe;
+    float hc[7];
+};
+
+// Wavefield and CPML memory (per shot).
+struct Wave {
+    float *vx, *vy, *sxx, *syy, *sxy;
+    float *r, *p, *q;                          // L planes per shot: [(s*L + l-1) * fsz]
+    float *psi_sxx_x, *psi_sxy_x, *psi_vxx, *psi_vyx;  // [s][NY][2FW]
+    float *psi_syy_y, *psi_sxy_y, *psi_vyy, *psi_vxy;  // [s][2FW][NX]
+    float *draw, *dcor;                        // TTI: 4 derivative fields each, per shot
+};
+
+// Prepared model arrays (one per shot or shared) and 1-D vectors.
+struct Model {
+    const float *prip, *prjp;
+    const float *g, *f, *fipjp;                 // isotropic (unrelaxed for visco)
+    const float *db, *eb, *dipb;                // isotropic visco bases: pu*taus, pi*taup, uipjp*tausipjp
+    const float *c11, *c13, *c33, *c15, *c35, *c55ipjp, *c15ipjp, *c35ipjp;   // anisotropic (DT-scaled)
+    const float *c11b, *c13b, *c33b, *c15b, *c35b, *c55ipjpb, *c15ipjpb, *c35ipjpb;  // visco bases c*tau
+    const float *ppi, *pu, *taus, *taup;        // surface / sampling
+    const float *absorb;
+    const float *K_x, *a_x, *b_x, *K_x_half, *a_x_half, *b_x_half;
+    const float *K_y, *a_y, *b_y, *K_y_half, *a_y_half, *b_y_half;
+    float bip[MAXL], cip[MAXL], peta[MAXL];
+};
+
+// Sources / receivers / sections of all shots (flattened with per-shot offsets).
+struct Acq {
+    const int *src_off;      // [nshots+1] offsets into the source arrays
+    const int *src_ix, *src_iy, *src_type;
+    const float *src_amp, *src_sin, *src_cos, *src_sin2, *src_cos2;  // amplitude, sin/cos(azimuth), sin/cos(2 dip)
+    const float *signals;    // [total sources][nt]
+    const int *last_type;    // [nshots] type of each shot's last source
+    const int *rec_off;      // [nshots+1]
+    const int *rec_ix, *rec_iy;
+    float *sec;              // [total receivers][5][ns]
+    int nt, ns;
+    int *status;             // [nshots] 0 ok, else first unstable step
+};
+
+__device__ __forceinline__ long long cell(const Geo &G, int j, int i)
+{
+    return (long long)(j - 1 + HY) * G.pitch + (i - 1 + HX);
+}
+
+__device__ __forceinline__ long long moff(const Geo &G, int s)
+{
+    return G.model_stride_on ? (long long)s * G.fsz : 0;
+}
+
+// ------------------------------------------------------------ FD operators
+
+// op_v_fdN (reference initfd.c:97-183): stress derivatives, unscaled.
+template <int ND>
+__device__ __forceinline__ void op_v(const float *__restrict__ sxx, const float *__restrict__ syy,
+                                     const float *__restrict__ sxy, long long o, int P, const float *hc,
+                                     float &sxx_x, float &sxy_x, float &sxy_y, float &syy_y)
+{
+    sxx_x = hc[1] * (__ldg(sxx + o + 1) - __ldg(sxx + o));
+    sxy_x = hc[1] * (__ldg(sxy + o) - __ldg(sxy + o - 1));
+    sxy_y = hc[1] * (__ldg(sxy + o) - __ldg(sxy + o - P));
+    syy_y = hc[1] * (__ldg(syy + o + P) - __ldg(syy + o));
+#pragma unroll
+    for (int m = 2; m <= ND; m++) {
+        sxx_x += hc[m] * (__ldg(sxx + o + m) - __ldg(sxx + o - m + 1));
+        sxy_x += hc[m] * (__ldg(sxy + o + m - 1) - __ldg(sxy + o - m));
+        sxy_y += hc[m] * (__ldg(sxy + o + (long long)(m - 1) * P) - __ldg(sxy + o - (long long)m * P));
+        syy_y += hc[m] * (__ldg(syy + o + (long long)m * P) - __ldg(syy + o - (long long)(m - 1) * P));
+    }
+}
+
+// op_s_fdN (reference initfd.c:9-95): velocity derivatives, times 1/DH.
+template <int ND>
+__device__ __forceinline__ void op_s(const float *__restrict__ vx, const float *__restrict__ vy, long long o,
+                                     int P, const float *hc, float dhi, float &vxx, float &vyx, float &vxy,
+                                     float &vyy)
+{
+    vxx = hc[1] * (__ldg(vx + o) - __ldg(vx + o - 1));
+    vyx = hc[1] * (__ldg(vy + o + 1) - __ldg(vy + o));
+    vxy = hc[1] * (__ldg(vx + o + P) - __ldg(vx + o));
+    vyy = hc[1] * (__ldg(vy + o) - __ldg(vy + o - P));
+#pragma unroll
+    for (int m = 2; m <= ND; m++) {
+        vxx += hc[m] * (__ldg(vx + o + m - 1) - __ldg(vx + o - m));
+        vyx += hc[m] * (__ldg(vy + o + m) - __ldg(vy + o - m + 1));
+        vxy += hc[m] * (__ldg(vx + o + (long long)m * P) - __ldg(vx + o - (long long)(m - 1) * P));
+        vyy += hc[m] * (__ldg(vy + o + (long long)(m - 1) * P) - __ldg(vy + o - (long long)m * P));
+    }
+    vxx *= dhi;
+    vyx *= dhi;
+    vxy *= dhi;
+    vyy *= dhi;
+}
+
+// Frame membership of column i / row j: 0 middle, 1 left/top (h = i or j),
+// 2 right/bottom (h = i - NX + 2FW or j - NY + 2FW); reference update_v_PML.c.
+__device__ __forceinline__ int xside(const Geo &G, int i)
+{
+    return i <= G.gx2 ? 1 : (i > G.gx3 ? 2 : 0);
+}
+__device__ __forceinline__ int yside(const Geo &G, int j)
+{
+    return j <= G.gy2 ? 1 : (j > G.gy3 ? 2 : 0);
+}
+// Region order of the reference's drivers: 0 interior, 1 left, 2 right, 3 top,
+// 4 bottom, 5 left-top, 6 left-bottom, 7 right-top, 8 right-bottom.
+__device__ __forceinline__ int region(const Geo &G, int i, int j)
+{
+    int xr = xside(G, i), yr = yside(G, j);
+    if (!yr)
+        return xr;
+    if (!xr)
+        return 2 + yr;
+    return 4 + (xr - 1) * 2 + yr;
+}
+
+// CPML stretch of the four velocity derivatives of one cell, updating the
+// memory variables (cpml_update.c:30-46 with the drivers' h rules).
+__device__ __forceinline__ void cpml_s(const Geo &G, const Wave &W, const Model &M, int s, int i, int j, int xr,
+                                       int yr, float &vxx, float &vyx, float &vxy, float &vyy, bool write)
+{
+    if (xr) {
+        int h = xr == 1 ? i : i - G.nx + G.fw2;
+        long long q = ((long long)s * G.ny + (j - 1)) * G.fw2 + (h - 1);
+        float p1 = M.b_x[h - 1] * W.psi_vxx[q] + M.a_x[h - 1] * vxx;
+        vxx = vxx / M.K_x[h - 1] + p1;
+        float p2 = M.b_x_half[h - 1] * W.psi_vyx[q] + M.a_x_half[h - 1] * vyx;
+        vyx = vyx / M.K_x_half[h - 1] + p2;
+        if (write) {
+            W.psi_vxx[q] = p1;
+            W.psi_vyx[q] = p2;
+        }
+    }
+    if (yr) {
+        int h = yr == 1 ? j : j - G.ny + G.fw2;
+        long long q = ((long long)s * G.fw2 + (h - 1)) * G.nx + (i - 1);
+        float p1 = M.b_y[h - 1] * W.psi_vyy[q] + M.a_y[h - 1] * vyy;
+        vyy = vyy / M.K_y[h - 1] + p1;
+        float p2 = M.b_y_half[h - 1] * W.psi_vxy[q] + M.a_y_half[h - 1] * vxy;
+        vxy = vxy / M.K_y_half[h - 1] + p2;
+        if (write) {
+            W.psi_vyy[q] = p1;
+            W.psi_vxy[q] = p2;
+        }
+    }
+}
+
+}  // namespace sofi

@@ -1,164 +1,8 @@
-// sofi_kernels.cuh -- device kernels of the SOFI2D time step on sm_103a.
-//
-// One time step of the reference's time_loop (src/time_loop.c:42-322) is
-//   k_force_src  force sources before the velocity update (update_v_interior.c:49-71)
-//   k_update_v   velocity update, all cells, CPML / damping frame by predicate
-//                (update_v_interior.c, update_v_PML.c, update_v_abs.c)
-//   k_wrap_x     periodic x only: ghost columns (exchange_v.c / exchange_s.c, one rank)
-//   k_update_s   stress update with the velocity derivatives recomputed from v in
-//                registers (v_derivatives.c fused away), CPML / damping by predicate
-//   k_tti_deriv + k_update_s_tti   TTI: derivatives (raw and CPML-stretched) are
-//                stored so the 4-point averages can follow the reference's
-//                region-by-region order (update_s_elastic_TTI_PML.c)
-//   k_seis_deriv div/curl sampling (derivatives as the stress update left them)
-//   k_stress_src explosive / moment-tensor sources + NaN probe (psource.c, eqsource.c)
-//   k_surface    free surface, one thread per column (surface_elastic.c, surface.c)
-//   k_seis       vx, vy, p sampling (seismo_ssg.c)
-//   k_snap       snapshot frame (snap_ssg.c)
-//
-// Layout: every 2-D field is a padded [NY + 2*HY][pitch] float array with the
-// interior cell (j, i) at ((j-1+HY) * pitch + (i-1+HX)); HX = HY = 8 >= ND + 1.
-// The shot index is the slowest dimension (field = base + shot * fsz). Ghost
-// cells stay zero (or hold the periodic copy), as the reference's edge ranks.
+// sofi_kernels.cuh -- the per-step kernels (see the overview in sofi_common.cuh).
 #pragma once
-#include <cuda_runtime.h>
-#include <stdint.h>
+#include "sofi_common.cuh"
 
 namespace sofi {
-
-constexpr int HX = 8;
-constexpr int HY = 8;
-constexpr int MAXL = 8;
-constexpr int BX = 32;  // threads per block in x
-constexpr int BY = 8;   // threads per block in y
-
-enum Kind { ISO = 0, VTI = 1, TTI = 2 };
-
-struct Geo {
-    int nx, ny, pitch, nshots;
-    long long fsz;          // floats per 2-D field
-    int fw, fw2;            // frame width, 2*FW
-    int gx2, gx3, gy2, gy3; // reference subgrid_bounds (one rank)
-    int abs_type;           // 0 none, 1 CPML, 2 damping (0 when FW == 0)
-    int free_surf, boundary, L;
-    int model_stride_on;    // 1: model per shot, 0: shared
-    int el_tti_rb_short;    // EL_TTI CPML: right-bottom corner pass stops at NY-1
-    float dt, dh, dtdh, dhi, dthalbe;
-    float hc[7];
-};
-
-// Wavefield and CPML memory (per shot).
-struct Wave {
-    float *vx, *vy, *sxx, *syy, *sxy;
-    float *r, *p, *q;                          // L planes per shot: [(s*L + l-1) * fsz]
-    float *psi_sxx_x, *psi_sxy_x, *psi_vxx, *psi_vyx;  // [s][NY][2FW]
-    float *psi_syy_y, *psi_sxy_y, *psi_vyy, *psi_vxy;  // [s][2FW][NX]
-    float *draw, *dcor;                        // TTI: 4 derivative fields each, per shot
-};
-
-// Prepared model arrays (one per shot or shared) and 1-D vectors.
-struct Model {
-    const float *prip, *prjp;
-    const float *g, *f, *fipjp;                 // isotropic (unrelaxed for visco)
-    const float *db, *eb, *dipb;                // isotropic visco bases: pu*taus, pi*taup, uipjp*tausipjp
-    const float *c11, *c13, *c33, *c15, *c35, *c55ipjp, *c15ipjp, *c35ipjp;   // anisotropic (DT-scaled)
-    const float *c11b, *c13b, *c33b, *c15b, *c35b, *c55ipjpb, *c15ipjpb, *c35ipjpb;  // visco bases c*tau
-    const float *ppi, *pu, *taus, *taup;        // surface / sampling
-    const float *absorb;
-    const float *K_x, *a_x, *b_x, *K_x_half, *a_x_half, *b_x_half;
-    const float *K_y, *a_y, *b_y, *K_y_half, *a_y_half, *b_y_half;
-    float bip[MAXL], cip[MAXL], peta[MAXL];
-};
-
-// Sources / receivers / sections of all shots (flattened with per-shot offsets).
-struct Acq {
-    const int *src_off;      // [nshots+1] offsets into the source arrays
-    const int *src_ix, *src_iy, *src_type;
-    const float *src_amp, *src_sin, *src_cos, *src_sin2, *src_cos2;  // amplitude, sin/cos(azimuth), sin/cos(2 dip)
-    const float *signals;    // [total sources][nt]
-    const int *last_type;    // [nshots] type of each shot's last source
-    const int *rec_off;      // [nshots+1]
-    const int *rec_ix, *rec_iy;
-    float *sec;              // [total receivers][5][ns]
-    int nt, ns;
-    int *status;             // [nshots] 0 ok, else first unstable step
-};
-
-__device__ __forceinline__ long long cell(const Geo &G, int j, int i)
-{
-    return (long long)(j - 1 + HY) * G.pitch + (i - 1 + HX);
-}
-
-__device__ __forceinline__ long long moff(const Geo &G, int s)
-{
-    return G.model_stride_on ? (long long)s * G.fsz : 0;
-}
-
-// ------------------------------------------------------------ FD operators
-
-// op_v_fdN (reference initfd.c:97-183): stress derivatives, unscaled.
-template <int ND>
-__device__ __forceinline__ void op_v(const float *__restrict__ sxx, const float *__restrict__ syy,
-                                     const float *__restrict__ sxy, long long o, int P, const float *hc,
-                                     float &sxx_x, float &sxy_x, float &sxy_y, float &syy_y)
-{
-    sxx_x = hc[1] * (__ldg(sxx + o + 1) - __ldg(sxx + o));
-    sxy_x = hc[1] * (__ldg(sxy + o) - __ldg(sxy + o - 1));
-    sxy_y = hc[1] * (__ldg(sxy + o) - __ldg(sxy + o - P));
-    syy_y = hc[1] * (__ldg(syy + o + P) - __ldg(syy + o));
-#pragma unroll
-    for (int m = 2; m <= ND; m++) {
-        sxx_x += hc[m] * (__ldg(sxx + o + m) - __ldg(sxx + o - m + 1));
-        sxy_x += hc[m] * (__ldg(sxy + o + m - 1) - __ldg(sxy + o - m));
-        sxy_y += hc[m] * (__ldg(sxy + o + (long long)(m - 1) * P) - __ldg(sxy + o - (long long)m * P));
-        syy_y += hc[m] * (__ldg(syy + o + (long long)m * P) - __ldg(syy + o - (long long)(m - 1) * P));
-    }
-}
-
-// op_s_fdN (reference initfd.c:9-95): velocity derivatives, times 1/DH.
-template <int ND>
-__device__ __forceinline__ void op_s(const float *__restrict__ vx, const float *__restrict__ vy, long long o,
-                                     int P, const float *hc, float dhi, float &vxx, float &vyx, float &vxy,
-                                     float &vyy)
-{
-    vxx = hc[1] * (__ldg(vx + o) - __ldg(vx + o - 1));
-    vyx = hc[1] * (__ldg(vy + o + 1) - __ldg(vy + o));
-    vxy = hc[1] * (__ldg(vx + o + P) - __ldg(vx + o));
-    vyy = hc[1] * (__ldg(vy + o) - __ldg(vy + o - P));
-#pragma unroll
-    for (int m = 2; m <= ND; m++) {
-        vxx += hc[m] * (__ldg(vx + o + m - 1) - __ldg(vx + o - m));
-        vyx += hc[m] * (__ldg(vy + o + m) - __ldg(vy + o - m + 1));
-        vxy += hc[m] * (__ldg(vx + o + (long long)m * P) - __ldg(vx + o - (long long)(m - 1) * P));
-        vyy += hc[m] * (__ldg(vy + o + (long long)(m - 1) * P) - __ldg(vy + o - (long long)m * P));
-    }
-    vxx *= dhi;
-    vyx *= dhi;
-    vxy *= dhi;
-    vyy *= dhi;
-}
-
-// Frame membership of column i / row j: 0 middle, 1 left/top (h = i or j),
-// 2 right/bottom (h = i - NX + 2FW or j - NY + 2FW); reference update_v_PML.c.
-__device__ __forceinline__ int xside(const Geo &G, int i)
-{
-    return i <= G.gx2 ? 1 : (i > G.gx3 ? 2 : 0);
-}
-__device__ __forceinline__ int yside(const Geo &G, int j)
-{
-    return j <= G.gy2 ? 1 : (j > G.gy3 ? 2 : 0);
-}
-// Region order of the reference's drivers: 0 interior, 1 left, 2 right, 3 top,
-// 4 bottom, 5 left-top, 6 left-bottom, 7 right-top, 8 right-bottom.
-__device__ __forceinline__ int region(const Geo &G, int i, int j)
-{
-    int xr = xside(G, i), yr = yside(G, j);
-    if (!yr)
-        return xr;
-    if (!xr)
-        return 2 + yr;
-    return 4 + (xr - 1) * 2 + yr;
-}
 
 // -------------------------------------------------------------- sources
 
@@ -236,20 +80,39 @@ __global__ void k_stress_src(Geo G, Wave W, Acq A, int nt)
 
 // ------------------------------------------------------- velocity update
 
+// One thread per cell; 32-bit offsets inside a shot's fields, read-only data
+// through the non-coherent cache, all per-cell loads ahead of the arithmetic.
 template <int ND>
 __global__ void __launch_bounds__(BX *BY) k_update_v(Geo G, Wave W, Model M)
 {
-    int i = blockIdx.x * BX + threadIdx.x + 1;
-    int j = blockIdx.y * BY + threadIdx.y + 1;
-    int s = blockIdx.z;
+    const int i = blockIdx.x * BX + threadIdx.x + 1;
+    const int j = blockIdx.y * BY + threadIdx.y + 1;
+    const int s = blockIdx.z;
     if (i > G.nx || j > G.ny)
         return;
     const int P = G.pitch;
-    long long o = cell(G, j, i);
-    long long so = (long long)s * G.fsz, mo = moff(G, s);
-    float sxx_x, sxy_x, sxy_y, syy_y;
-    op_v<ND>(W.sxx + so, W.syy + so, W.sxy + so, o, P, G.hc, sxx_x, sxy_x, sxy_y, syy_y);
-    int xr = xside(G, i), yr = yside(G, j);
+    const int o = (j - 1 + HY) * P + (i - 1 + HX);
+    const long long so = (long long)s * G.fsz, mo = moff(G, s);
+    const float *__restrict__ sxx = W.sxx + so;
+    const float *__restrict__ syy = W.syy + so;
+    const float *__restrict__ sxy = W.sxy + so;
+    float *__restrict__ vx = W.vx + so;
+    float *__restrict__ vy = W.vy + so;
+    const float ovx = vx[o], ovy = vy[o];
+    const float rip = __ldg(M.prip + mo + o), rjp = __ldg(M.prjp + mo + o);
+    const float *hc = G.hc;
+    float sxx_x = hc[1] * (__ldg(sxx + o + 1) - __ldg(sxx + o));
+    float sxy_x = hc[1] * (__ldg(sxy + o) - __ldg(sxy + o - 1));
+    float sxy_y = hc[1] * (__ldg(sxy + o) - __ldg(sxy + o - P));
+    float syy_y = hc[1] * (__ldg(syy + o + P) - __ldg(syy + o));
+#pragma unroll
+    for (int m = 2; m <= ND; m++) {
+        sxx_x += hc[m] * (__ldg(sxx + o + m) - __ldg(sxx + o - m + 1));
+        sxy_x += hc[m] * (__ldg(sxy + o + m - 1) - __ldg(sxy + o - m));
+        sxy_y += hc[m] * (__ldg(sxy + o + (m - 1) * P) - __ldg(sxy + o - m * P));
+        syy_y += hc[m] * (__ldg(syy + o + m * P) - __ldg(syy + o - (m - 1) * P));
+    }
+    const int xr = xside(G, i), yr = yside(G, j);
     if (G.abs_type == 1) {
         if (xr) {
             int h = xr == 1 ? i : i - G.nx + G.fw2;
@@ -272,9 +135,8 @@ __global__ void __launch_bounds__(BX *BY) k_update_v(Geo G, Wave W, Model M)
             sxy_y = sxy_y / M.K_y[h - 1] + py;
         }
     }
-    float *vx = W.vx + so, *vy = W.vy + so;
-    float nvx = vx[o] + (sxx_x + sxy_y) * G.dtdh * __ldg(M.prip + mo + o);
-    float nvy = vy[o] + (sxy_x + syy_y) * G.dtdh * __ldg(M.prjp + mo + o);
+    float nvx = ovx + (sxx_x + sxy_y) * G.dtdh * rip;
+    float nvy = ovy + (sxy_x + syy_y) * G.dtdh * rjp;
     if (G.abs_type == 2 && (xr | yr)) {
         float a = __ldg(M.absorb + mo + o);
         nvx *= a;
@@ -306,124 +168,119 @@ __global__ void k_wrap_x(Geo G, float *a, float *b, float *c, int nd)
 
 // --------------------------------------------------------- stress update
 
-// CPML stretch of the four velocity derivatives of one cell, updating the
-// memory variables (cpml_update.c:30-46 with the drivers' h rules).
-__device__ __forceinline__ void cpml_s(const Geo &G, const Wave &W, const Model &M, int s, int i, int j, int xr,
-                                       int yr, float &vxx, float &vyx, float &vxy, float &vyy, bool write)
-{
-    if (xr) {
-        int h = xr == 1 ? i : i - G.nx + G.fw2;
-        long long q = ((long long)s * G.ny + (j - 1)) * G.fw2 + (h - 1);
-        float p1 = M.b_x[h - 1] * W.psi_vxx[q] + M.a_x[h - 1] * vxx;
-        vxx = vxx / M.K_x[h - 1] + p1;
-        float p2 = M.b_x_half[h - 1] * W.psi_vyx[q] + M.a_x_half[h - 1] * vyx;
-        vyx = vyx / M.K_x_half[h - 1] + p2;
-        if (write) {
-            W.psi_vxx[q] = p1;
-            W.psi_vyx[q] = p2;
-        }
-    }
-    if (yr) {
-        int h = yr == 1 ? j : j - G.ny + G.fw2;
-        long long q = ((long long)s * G.fw2 + (h - 1)) * G.nx + (i - 1);
-        float p1 = M.b_y[h - 1] * W.psi_vyy[q] + M.a_y[h - 1] * vyy;
-        vyy = vyy / M.K_y[h - 1] + p1;
-        float p2 = M.b_y_half[h - 1] * W.psi_vxy[q] + M.a_y_half[h - 1] * vxy;
-        vxy = vxy / M.K_y_half[h - 1] + p2;
-        if (write) {
-            W.psi_vyy[q] = p1;
-            W.psi_vxy[q] = p2;
-        }
-    }
-}
-
-// Isotropic and VTI stress update of one cell (wavefield_update_s_el.c,
+// Isotropic and VTI stress update, one thread per cell (wavefield_update_s_el.c,
 // _visc.c, _el_vti.c, _visc_VTI.c). Viscoelastic modulus defects are the
-// stored base (modulus * tau) times peta[l].
-template <int KIND, bool VISCO>
-__device__ __forceinline__ void stress_cell(const Geo &G, const Wave &W, const Model &M, int s, long long o,
-                                            long long so, long long mo, float vxx, float vyx, float vxy,
-                                            float vyy, float &u1, float &u2, float &u3)
-{
-    if (KIND == ISO) {
-        float g = __ldg(M.g + mo + o), f = __ldg(M.f + mo + o), fipjp = __ldg(M.fipjp + mo + o);
-        u1 = fipjp * (vyx + vxy);
-        float gd = g * (vxx + vyy);
-        u2 = gd - 2.0f * f * vyy;
-        u3 = gd - 2.0f * f * vxx;
-        if (VISCO) {
-            float db = __ldg(M.db + mo + o), eb = __ldg(M.eb + mo + o), dipb = __ldg(M.dipb + mo + o);
-            float sro = 0.f, spo = 0.f, sqo = 0.f, sr = 0.f, sp = 0.f, sq = 0.f;
-            for (int l = 0; l < G.L; l++) {
-                long long lo = ((long long)s * G.L + l) * G.fsz + o;
-                float r = W.r[lo], p = W.p[lo], q = W.q[lo];
-                sro += r, spo += p, sqo += q;
-                float pe = M.peta[l], b = M.bip[l], c = M.cip[l];
-                float dip = dipb * pe, d = db * pe, e = eb * pe;
-                r = b * (r * c - dip * (vxy + vyx));
-                p = b * (p * c - e * (vxx + vyy) + 2.0f * d * vyy);
-                q = b * (q * c - e * (vxx + vyy) + 2.0f * d * vxx);
-                W.r[lo] = r, W.p[lo] = p, W.q[lo] = q;
-                sr += r, sp += p, sq += q;
-            }
-            u1 += G.dthalbe * (sro + sr);
-            u2 += G.dthalbe * (spo + sp);
-            u3 += G.dthalbe * (sqo + sq);
-        }
-    } else {  // VTI
-        float c11 = __ldg(M.c11 + mo + o), c13 = __ldg(M.c13 + mo + o), c33 = __ldg(M.c33 + mo + o);
-        float c55 = __ldg(M.c55ipjp + mo + o);
-        u1 = c55 * (vxy + vyx);
-        u2 = c11 * vxx + c13 * vyy;
-        u3 = c13 * vxx + c33 * vyy;
-        if (VISCO) {
-            float b11 = __ldg(M.c11b + mo + o), b13 = __ldg(M.c13b + mo + o), b33 = __ldg(M.c33b + mo + o);
-            float b55 = __ldg(M.c55ipjpb + mo + o);
-            float sro = 0.f, spo = 0.f, sqo = 0.f, sr = 0.f, sp = 0.f, sq = 0.f;
-            for (int l = 0; l < G.L; l++) {
-                long long lo = ((long long)s * G.L + l) * G.fsz + o;
-                float r = W.r[lo], p = W.p[lo], q = W.q[lo];
-                sro += r, spo += p, sqo += q;
-                float pe = M.peta[l], b = M.bip[l], c = M.cip[l];
-                r = b * (r * c - (b55 * pe) * (vxy + vyx));
-                p = b * (p * c - (b11 * pe) * vxx - (b13 * pe) * vyy);
-                q = b * (q * c - (b13 * pe) * vxx - (b33 * pe) * vyy);
-                W.r[lo] = r, W.p[lo] = p, W.q[lo] = q;
-                sr += r, sp += p, sq += q;
-            }
-            u1 += G.dthalbe * (sro + sr);
-            u2 += G.dthalbe * (spo + sp);
-            u3 += G.dthalbe * (sqo + sq);
-        }
-    }
-}
-
-template <int ND, int KIND, bool VISCO>
+// stored base (modulus * tau) times peta[l]; LT > 0 fixes the number of
+// mechanisms at compile time so every memory variable is loaded up front.
+template <int ND, int KIND, bool VISCO, int LT>
 __global__ void __launch_bounds__(BX *BY) k_update_s(Geo G, Wave W, Model M)
 {
-    int i = blockIdx.x * BX + threadIdx.x + 1;
-    int j = blockIdx.y * BY + threadIdx.y + 1;
-    int s = blockIdx.z;
+    const int i = blockIdx.x * BX + threadIdx.x + 1;
+    const int j = blockIdx.y * BY + threadIdx.y + 1;
+    const int s = blockIdx.z;
     if (i > G.nx || j > G.ny)
         return;
     const int P = G.pitch;
-    long long o = cell(G, j, i);
-    long long so = (long long)s * G.fsz, mo = moff(G, s);
+    const int o = (j - 1 + HY) * P + (i - 1 + HX);
+    const long long so = (long long)s * G.fsz, mo = moff(G, s);
+    float *__restrict__ sxx = W.sxx + so;
+    float *__restrict__ syy = W.syy + so;
+    float *__restrict__ sxy = W.sxy + so;
+    const float *__restrict__ vx = W.vx + so;
+    const float *__restrict__ vy = W.vy + so;
+    const float oxx = sxx[o], oyy = syy[o], oxy = sxy[o];
+    float m0, m1, m2, m3 = 0.f, b0 = 0.f, b1 = 0.f, b2 = 0.f, b3 = 0.f;
+    if (KIND == ISO) {
+        m0 = __ldg(M.g + mo + o), m1 = __ldg(M.f + mo + o), m2 = __ldg(M.fipjp + mo + o);
+        if (VISCO)
+            b0 = __ldg(M.db + mo + o), b1 = __ldg(M.eb + mo + o), b2 = __ldg(M.dipb + mo + o);
+    } else {
+        m0 = __ldg(M.c11 + mo + o), m1 = __ldg(M.c13 + mo + o), m2 = __ldg(M.c33 + mo + o);
+        m3 = __ldg(M.c55ipjp + mo + o);
+        if (VISCO)
+            b0 = __ldg(M.c11b + mo + o), b1 = __ldg(M.c13b + mo + o), b2 = __ldg(M.c33b + mo + o),
+            b3 = __ldg(M.c55ipjpb + mo + o);
+    }
+    constexpr int LN = LT > 0 ? LT : MAXL;
+    const int L = LT > 0 ? LT : G.L;
+    float *__restrict__ wr = W.r + (long long)s * G.L * G.fsz;
+    float *__restrict__ wp = W.p + (long long)s * G.L * G.fsz;
+    float *__restrict__ wq = W.q + (long long)s * G.L * G.fsz;
+    float rr[LN], pp[LN], qq[LN];
+    if (VISCO) {
+#pragma unroll
+        for (int l = 0; l < LN; l++) {
+            if (l < L) {
+                long long lo = (long long)l * G.fsz + o;
+                rr[l] = wr[lo], pp[l] = wp[lo], qq[l] = wq[lo];
+            }
+        }
+    }
     float vxx, vyx, vxy, vyy;
-    op_s<ND>(W.vx + so, W.vy + so, o, P, G.hc, G.dhi, vxx, vyx, vxy, vyy);
-    int xr = xside(G, i), yr = yside(G, j);
+    {
+        const float *hc = G.hc;
+        vxx = hc[1] * (__ldg(vx + o) - __ldg(vx + o - 1));
+        vyx = hc[1] * (__ldg(vy + o + 1) - __ldg(vy + o));
+        vxy = hc[1] * (__ldg(vx + o + P) - __ldg(vx + o));
+        vyy = hc[1] * (__ldg(vy + o) - __ldg(vy + o - P));
+#pragma unroll
+        for (int m = 2; m <= ND; m++) {
+            vxx += hc[m] * (__ldg(vx + o + m - 1) - __ldg(vx + o - m));
+            vyx += hc[m] * (__ldg(vy + o + m) - __ldg(vy + o - m + 1));
+            vxy += hc[m] * (__ldg(vx + o + m * P) - __ldg(vx + o - (m - 1) * P));
+            vyy += hc[m] * (__ldg(vy + o + (m - 1) * P) - __ldg(vy + o - m * P));
+        }
+        vxx *= G.dhi, vyx *= G.dhi, vxy *= G.dhi, vyy *= G.dhi;
+    }
+    const int xr = xside(G, i), yr = yside(G, j);
     if (G.abs_type == 1)
         cpml_s(G, W, M, s, i, j, xr, yr, vxx, vyx, vxy, vyy, true);
     float u1, u2, u3;
-    stress_cell<KIND, VISCO>(G, W, M, s, o, so, mo, vxx, vyx, vxy, vyy, u1, u2, u3);
-    float nxy = W.sxy[so + o] + u1, nxx = W.sxx[so + o] + u2, nyy = W.syy[so + o] + u3;
+    if (KIND == ISO) {
+        u1 = m2 * (vyx + vxy);
+        float gd = m0 * (vxx + vyy);
+        u2 = gd - 2.0f * m1 * vyy;
+        u3 = gd - 2.0f * m1 * vxx;
+    } else {
+        u1 = m3 * (vxy + vyx);
+        u2 = m0 * vxx + m1 * vyy;
+        u3 = m1 * vxx + m2 * vyy;
+    }
+    if (VISCO) {
+        float sro = 0.f, spo = 0.f, sqo = 0.f, sr = 0.f, sp = 0.f, sq = 0.f;
+#pragma unroll
+        for (int l = 0; l < LN; l++) {
+            if (l < L) {
+                float r = rr[l], p = pp[l], q = qq[l];
+                sro += r, spo += p, sqo += q;
+                float pe = M.peta[l], bb = M.bip[l], cc = M.cip[l];
+                if (KIND == ISO) {
+                    float dip = b2 * pe, d = b0 * pe, e = b1 * pe;
+                    r = bb * (r * cc - dip * (vxy + vyx));
+                    p = bb * (p * cc - e * (vxx + vyy) + 2.0f * d * vyy);
+                    q = bb * (q * cc - e * (vxx + vyy) + 2.0f * d * vxx);
+                } else {
+                    r = bb * (r * cc - (b3 * pe) * (vxy + vyx));
+                    p = bb * (p * cc - (b0 * pe) * vxx - (b1 * pe) * vyy);
+                    q = bb * (q * cc - (b1 * pe) * vxx - (b2 * pe) * vyy);
+                }
+                long long lo = (long long)l * G.fsz + o;
+                wr[lo] = r, wp[lo] = p, wq[lo] = q;
+                sr += r, sp += p, sq += q;
+            }
+        }
+        u1 += G.dthalbe * (sro + sr);
+        u2 += G.dthalbe * (spo + sp);
+        u3 += G.dthalbe * (sqo + sq);
+    }
+    float nxy = oxy + u1, nxx = oxx + u2, nyy = oyy + u3;
     if (G.abs_type == 2 && (xr | yr)) {
         float a = __ldg(M.absorb + mo + o);
         nxy *= a, nyy *= a, nxx *= a;
     }
-    W.sxy[so + o] = nxy;
-    W.sxx[so + o] = nxx;
-    W.syy[so + o] = nyy;
+    sxy[o] = nxy;
+    sxx[o] = nxx;
+    syy[o] = nyy;
 }
 
 // ------------------------------------------------------------------ TTI

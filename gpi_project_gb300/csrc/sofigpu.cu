@@ -6,12 +6,14 @@
 // sofi_kernels.cuh in the reference's phase order for each time step.
 #include "sofigpu.h"
 #include "sofi_kernels.cuh"
+#include "sofi_launch.h"
 
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -164,6 +166,8 @@ struct sofi_ctx {
     int step = 0;
     float last_ms = 0.f;
     bool run_pending = false;  // ev0/ev1 recorded by a sofi_run not yet synchronised
+    bool march = false;        // y-marching kernels (ISO/VTI stress, all velocity updates)
+    int march_sy = 32;         // rows per block of the y-marching kernels
     // snapshots
     int snap_nx = 0, snap_ny = 0, snap_total = 0, nsnap = 0;
     float *d_snap = nullptr;
@@ -367,6 +371,31 @@ dim3 grid2d(const sofi_ctx *c)
       case 6: { constexpr int ND = 6; __VA_ARGS__; } break; \
     }
 
+template <int KIND, bool VISCO>
+void cell_s_l(const Geo &G, const Wave &W, const Model &M, int nd, dim3 grd, dim3 blk, cudaStream_t st)
+{
+    int L = VISCO ? G.L : 0;
+    if (!VISCO)
+        DISPATCH_ND(nd, (k_update_s<ND, KIND, false, 0><<<grd, blk, 0, st>>>(G, W, M)))
+    else if (L == 1)
+        DISPATCH_ND(nd, (k_update_s<ND, KIND, true, 1><<<grd, blk, 0, st>>>(G, W, M)))
+    else if (L == 2)
+        DISPATCH_ND(nd, (k_update_s<ND, KIND, true, 2><<<grd, blk, 0, st>>>(G, W, M)))
+    else if (L == 3)
+        DISPATCH_ND(nd, (k_update_s<ND, KIND, true, 3><<<grd, blk, 0, st>>>(G, W, M)))
+    else
+        DISPATCH_ND(nd, (k_update_s<ND, KIND, true, 0><<<grd, blk, 0, st>>>(G, W, M)))
+}
+
+void launch_cell_s(const Geo &G, const Wave &W, const Model &M, int nd, int kind, bool visco, dim3 grd, dim3 blk,
+                   cudaStream_t st)
+{
+    if (kind == ISO)
+        visco ? cell_s_l<ISO, true>(G, W, M, nd, grd, blk, st) : cell_s_l<ISO, false>(G, W, M, nd, grd, blk, st);
+    else
+        visco ? cell_s_l<VTI, true>(G, W, M, nd, grd, blk, st) : cell_s_l<VTI, false>(G, W, M, nd, grd, blk, st);
+}
+
 int launch_step(sofi_ctx *c, int nt)
 {
     const sofi_config &cf = c->cfg;
@@ -395,7 +424,10 @@ int launch_step(sofi_ctx *c, int nt)
         c->tev_used += 3;
         CK(cudaEventRecord(e0, st));
     }
-    DISPATCH_ND(c->nd, (k_update_v<ND><<<grd, blk, 0, st>>>(G, c->W, c->M)));
+    if (c->march)
+        launch_march_v(G, c->W, c->M, c->nd, c->march_sy, st);
+    else
+        DISPATCH_ND(c->nd, (k_update_v<ND><<<grd, blk, 0, st>>>(G, c->W, c->M)));
     c->launches++;
     if (timed)
         CK(cudaEventRecord(e1, st));
@@ -412,16 +444,10 @@ int launch_step(sofi_ctx *c, int nt)
             k_update_s_tti<true><<<grd, blk, 0, st>>>(G, c->W, c->M);
         else
             k_update_s_tti<false><<<grd, blk, 0, st>>>(G, c->W, c->M);
-    } else if (kind == ISO) {
-        if (visco)
-            DISPATCH_ND(c->nd, (k_update_s<ND, ISO, true><<<grd, blk, 0, st>>>(G, c->W, c->M)))
-        else
-            DISPATCH_ND(c->nd, (k_update_s<ND, ISO, false><<<grd, blk, 0, st>>>(G, c->W, c->M)))
+    } else if (c->march) {
+        launch_march_s(G, c->W, c->M, c->nd, kind, visco, c->march_sy, st);
     } else {
-        if (visco)
-            DISPATCH_ND(c->nd, (k_update_s<ND, VTI, true><<<grd, blk, 0, st>>>(G, c->W, c->M)))
-        else
-            DISPATCH_ND(c->nd, (k_update_s<ND, VTI, false><<<grd, blk, 0, st>>>(G, c->W, c->M)))
+        launch_cell_s(G, c->W, c->M, c->nd, kind, visco, grd, blk, st);
     }
     c->launches++;
     if (timed)
@@ -560,6 +586,10 @@ int sofi_create(const sofi_config *cfg, int device, sofi_ctx **out)
     c->nd = cfg->fdorder / 2;
     c->nmodels = cfg->shared_model ? 1 : cfg->nshots;
     c->acq.resize(cfg->nshots);
+    if (const char *e = getenv("SOFI_KERNELS"))
+        c->march = strcmp(e, "march") == 0;
+    if (const char *e = getenv("SOFI_MARCH_ROWS"))
+        c->march_sy = atoi(e) > 0 ? atoi(e) : c->march_sy;
     e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete c;

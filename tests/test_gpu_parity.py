@@ -81,3 +81,25 @@ def test_gpu_matches_oracle_examples(name):
     compare_sections(t, o, cfg.seismo, name)
     t.close()
     o.close()
+
+
+@pytest.mark.parametrize("name", ["el_cpml_fd8", "visc_cpml_fs_l3", "vvti_cpml_l2", "el_abs_fd10"])
+def test_march_kernels_match_simple_kernels(name, monkeypatch):
+    """The y-marching kernels and the one-cell-per-thread kernels compute the same step."""
+    from oracle import oracle as O
+    from tests.golden.cases import case_by_name
+    from tests.helpers import case_receivers, case_sources
+    case = case_by_name(name)
+    o = run_oracle_case(case, nthreads=os.cpu_count() or 1, nsteps=1)
+    cfg = o.cfg
+    sp = case_sources(case, cfg)
+    sig = O.wavelet(1, cfg.nt, cfg.dt, sp)
+    out = {}
+    for variant in ["simple", "march"]:
+        monkeypatch.setenv("SOFI_KERNELS", variant)
+        t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
+        out[variant] = {k: t.field(k) for k in ["vx", "vy", "sxx", "syy", "sxy"]}
+        t.close()
+    for k in out["march"]:
+        assert rel_l2(out["march"][k], out["simple"][k]) < 1e-6, (name, k)
+    o.close()
