@@ -328,6 +328,32 @@ def main():
     step_roof = {"bytes_per_cell": bpc["step"], "achieved": round(bpc["step"] * value / world, 1),
                  "frac": round(bpc["step"] * value / world / peak, 4), "unit": "GB/s",
                  "update_v_mean_ms": round(ms_v, 4), "update_s_mean_ms": round(ms_s, 4)}
+    batched = None
+    if nshots > 1:
+        # the same shots one at a time: a single-shot context on the same model
+        t1 = TimeLoop(make_config(weq=par["weq"], nx=par["nx"], ny=par["ny"], fdorder=par["fdorder"],
+                                  maxrelerror=par["maxrelerror"], L=par.get("L", 0), dt=par["dt"], dh=par["dh"],
+                                  nt=par["nt"], fw=par["fw"], abs_type=par["abs_type"],
+                                  free_surf=par.get("free_surf", 0), seismo=par["seismo"], ndt=par["ndt"]),
+                      device=local)
+        t1.set_model(fields)
+        t1.set_vectors(vecs)
+        t1.set_sources(srcs[0], sigs[0])
+        t1.set_receivers(*W["rec"])
+        t1.reset()
+        t1.run()
+        torch.cuda.synchronize()
+        w1 = time.perf_counter()
+        nplain = 2
+        for _ in range(nplain):
+            t1.reset()
+            t1.run()
+        t1.synchronize()
+        plain_s = (time.perf_counter() - w1) / nplain
+        t1.close()
+        batched = {"shots": nshots, "shots_per_s": round(nshots * args.steps * world / (dev_ms * 1e-3), 3),
+                   "plain_shots_per_s": round(1.0 / plain_s, 3),
+                   "speedup_vs_plain": round(nshots * args.steps / (dev_ms * 1e-3) * plain_s, 3)}
     if rank != 0:
         return
     out = {
@@ -342,6 +368,7 @@ def main():
         "e2e": {"value": round(e2e_val, 4), "unit": "Gcell-updates/s", "h2d_bytes_per_step": int(h2d_bytes),
                 "d2h_bytes_per_step": int(d2h_bytes)},
         "roofline": roof, "step_roofline": step_roof, "gpu_launches": int(launches),
+        **({"batched": batched} if batched else {}),
         "clocks": clk.summary(),
     }
     if not args.no_cpu_baseline and rank == 0:

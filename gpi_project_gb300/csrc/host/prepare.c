@@ -306,8 +306,12 @@ int sofih_prepare(const sofih_par *p, const float *vp, const float *vs, const fl
             size_t k = (size_t)(i - 1) * NY + (j - 1);
             float v_p = vp[k], v_s = vs[k], r = rho[k];
             if (v_p > 1.0f) {
+                /* anisotropic media: horizontal P velocity vp*sqrt(1+2 eps) too
+                 * (readmod_elastic_tti.c:128-131) */
+                float v_h = weq >= 4 ? v_p * sqrtf(2.0f * eps[k] + 1.0f) : v_p;
                 vpmin = v_p < vpmin ? v_p : vpmin;
                 vpmax = v_p > vpmax ? v_p : vpmax;
+                vpmax = v_h > vpmax ? v_h : vpmax;
             }
             if (v_s > 1.0f) {
                 vsmin = v_s < vsmin ? v_s : vsmin;

@@ -47,6 +47,7 @@ struct Geo {
     int free_surf, boundary, L;
     int model_stride_on;    // 1: model per shot, 0: shared
     int el_tti_rb_short;    // EL_TTI CPML: right-bottom corner pass stops at NY-1
+    int shot_fast;          // block index: shot varies fastest (model tiles shared in L2)
     float dt, dh, dtdh, dhi, dthalbe;
     float hc[7];
 };
@@ -83,6 +84,8 @@ struct Acq {
     const int *last_type;    // [nshots] type of each shot's last source
     const int *rec_off;      // [nshots+1]
     const int *rec_ix, *rec_iy;
+    const int *rec_col_off;  // [nshots][NX+1]: receivers of column i at rec_col_idx[off[i-1] .. off[i])
+    const int *rec_col_idx;  // global receiver indices, grouped by shot and column
     float *sec;              // [total receivers][5][ns]
     int nt, ns;
     int *status;             // [nshots] 0 ok, else first unstable step
@@ -91,6 +94,20 @@ struct Acq {
 __device__ __forceinline__ long long cell(const Geo &G, int j, int i)
 {
     return (long long)(j - 1 + HY) * G.pitch + (i - 1 + HX);
+}
+
+// Tile column and shot of this block. With a shared model and several shots
+// the shot varies fastest in blockIdx.x, so the blocks that run together read
+// the same model tile and only the first of them fetches it from DRAM.
+__device__ __forceinline__ void block_xs(const Geo &G, int &bx, int &s)
+{
+    if (G.shot_fast) {
+        s = blockIdx.x % G.nshots;
+        bx = blockIdx.x / G.nshots;
+    } else {
+        s = blockIdx.z;
+        bx = blockIdx.x;
+    }
 }
 
 __device__ __forceinline__ long long moff(const Geo &G, int s)

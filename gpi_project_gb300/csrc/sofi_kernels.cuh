@@ -31,119 +31,92 @@ __global__ void k_force_src(Geo G, Wave W, Model M, Acq A, int nt)
     }
 }
 
-// psource.c:27-54 and eqsource.c:25-52 (applied to all sources when the last
-// source's type selects them, time_loop.c:248-253) + the NaN probe of
-// time_loop.c:44-47 at (NY/2, NX/2).
-__global__ void k_stress_src(Geo G, Wave W, Acq A, int nt)
-{
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= G.nshots)
-        return;
-    long long so = (long long)s * G.fsz;
-    float *sxx = W.sxx + so, *syy = W.syy + so, *sxy = W.sxy + so;
-    int lt = A.last_type[s];
-    int NT = A.nt;
-    for (int k = A.src_off[s]; k < A.src_off[s + 1]; k++) {
-        long long o = cell(G, A.src_iy[k], A.src_ix[k]);
-        const float *sig = A.signals + (long long)k * NT - 1;  // 1-based: sig[1..NT]
-        if (lt == 1) {
-            // central difference of the signal (psource.c:41-49); a one-step run
-            // has no neighbouring sample and injects nothing
-            float amp = 0.0f;
-            float d2 = 2.0f * G.dh * G.dh;
-            if (NT >= 2) {
-                if (nt == 1)
-                    amp = sig[2] / d2;
-                else if (nt < NT)
-                    amp = (sig[nt + 1] - sig[nt - 1]) / d2;
-                else
-                    amp = -sig[nt - 1] / d2;
-            }
-            sxx[o] += amp;
-            syy[o] += amp;
-        } else if (lt == 5) {
-            float scale_amp = G.dt / (G.dh * G.dh);
-            float amp = A.src_amp[k] * scale_amp * sig[nt];
-            float m11 = -A.src_sin2[k], m12 = -A.src_cos2[k], m22 = A.src_sin2[k];
-            sxx[o] += amp * m11;
-            sxy[o] += 0.3f * amp * m12;
-            sxy[o - G.pitch] += 0.3f * amp * m12;
-            sxy[o - 1] += 0.3f * amp * m12;
-            syy[o] += amp * m22;
-        }
-    }
-    long long pc = cell(G, G.ny / 2 > 0 ? G.ny / 2 : 1, G.nx / 2 > 0 ? G.nx / 2 : 1);
-    float probe = W.vy[so + pc];
-    if (isnan(probe) && A.status[s] == 0)
-        A.status[s] = nt;
-}
-
 // ------------------------------------------------------- velocity update
 
-// One thread per cell; 32-bit offsets inside a shot's fields, read-only data
-// through the non-coherent cache, all per-cell loads ahead of the arithmetic.
-template <int ND>
+// Velocity update, R consecutive rows per thread (the y-stencil windows of the
+// R cells overlap, so σxy and σyy are loaded R + 2ND - 1 times instead of
+// 2ND * R); 32-bit offsets inside a shot's fields, read-only data through the
+// non-coherent cache. Force sources are added by k_force_src beforehand.
+template <int ND, int R>
 __global__ void __launch_bounds__(BX *BY) k_update_v(Geo G, Wave W, Model M)
 {
-    const int i = blockIdx.x * BX + threadIdx.x + 1;
-    const int j = blockIdx.y * BY + threadIdx.y + 1;
-    const int s = blockIdx.z;
-    if (i > G.nx || j > G.ny)
+    int bx, s;
+    block_xs(G, bx, s);
+    const int i = bx * BX + threadIdx.x + 1;
+    const int jb = (blockIdx.y * BY + threadIdx.y) * R + 1;
+    if (i > G.nx || jb > G.ny)
         return;
     const int P = G.pitch;
-    const int o = (j - 1 + HY) * P + (i - 1 + HX);
+    const int ob = (jb - 1 + HY) * P + (i - 1 + HX);
     const long long so = (long long)s * G.fsz, mo = moff(G, s);
     const float *__restrict__ sxx = W.sxx + so;
     const float *__restrict__ syy = W.syy + so;
     const float *__restrict__ sxy = W.sxy + so;
     float *__restrict__ vx = W.vx + so;
     float *__restrict__ vy = W.vy + so;
-    const float ovx = vx[o], ovy = vy[o];
-    const float rip = __ldg(M.prip + mo + o), rjp = __ldg(M.prjp + mo + o);
     const float *hc = G.hc;
-    float sxx_x = hc[1] * (__ldg(sxx + o + 1) - __ldg(sxx + o));
-    float sxy_x = hc[1] * (__ldg(sxy + o) - __ldg(sxy + o - 1));
-    float sxy_y = hc[1] * (__ldg(sxy + o) - __ldg(sxy + o - P));
-    float syy_y = hc[1] * (__ldg(syy + o + P) - __ldg(syy + o));
+    // windows: wxy[k] = sxy(jb - ND + k), wyy[k] = syy(jb - ND + 1 + k); rows past
+    // NY + ND are read by no cell of the grid and are not loaded
+    constexpr int NW = R + 2 * ND - 1;
+    float wxy[NW], wyy[NW];
 #pragma unroll
-    for (int m = 2; m <= ND; m++) {
-        sxx_x += hc[m] * (__ldg(sxx + o + m) - __ldg(sxx + o - m + 1));
-        sxy_x += hc[m] * (__ldg(sxy + o + m - 1) - __ldg(sxy + o - m));
-        sxy_y += hc[m] * (__ldg(sxy + o + (m - 1) * P) - __ldg(sxy + o - m * P));
-        syy_y += hc[m] * (__ldg(syy + o + m * P) - __ldg(syy + o - (m - 1) * P));
+    for (int k = 0; k < NW; k++) {
+        wxy[k] = (jb - ND + k <= G.ny + ND) ? __ldg(sxy + ob + (k - ND) * P) : 0.f;
+        wyy[k] = (jb - ND + 1 + k <= G.ny + ND) ? __ldg(syy + ob + (k - ND + 1) * P) : 0.f;
     }
-    const int xr = xside(G, i), yr = yside(G, j);
-    if (G.abs_type == 1) {
-        if (xr) {
-            int h = xr == 1 ? i : i - G.nx + G.fw2;
-            long long q = ((long long)s * G.ny + (j - 1)) * G.fw2 + (h - 1);
-            float ps = M.b_x_half[h - 1] * W.psi_sxx_x[q] + M.a_x_half[h - 1] * sxx_x;
-            W.psi_sxx_x[q] = ps;
-            sxx_x = sxx_x / M.K_x_half[h - 1] + ps;
-            float py = M.b_x[h - 1] * W.psi_sxy_x[q] + M.a_x[h - 1] * sxy_x;
-            W.psi_sxy_x[q] = py;
-            sxy_x = sxy_x / M.K_x[h - 1] + py;
+    const int xr = xside(G, i);
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int j = jb + r;
+        if (j > G.ny)
+            break;
+        const int o = ob + r * P;
+        const float ovx = vx[o], ovy = vy[o];
+        const float rip = __ldg(M.prip + mo + o), rjp = __ldg(M.prjp + mo + o);
+        float sxx_x = hc[1] * (__ldg(sxx + o + 1) - __ldg(sxx + o));
+        float sxy_x = hc[1] * (__ldg(sxy + o) - __ldg(sxy + o - 1));
+        float sxy_y = hc[1] * (wxy[ND + r] - wxy[ND + r - 1]);
+        float syy_y = hc[1] * (wyy[ND + r] - wyy[ND + r - 1]);
+#pragma unroll
+        for (int m = 2; m <= ND; m++) {
+            sxx_x += hc[m] * (__ldg(sxx + o + m) - __ldg(sxx + o - m + 1));
+            sxy_x += hc[m] * (__ldg(sxy + o + m - 1) - __ldg(sxy + o - m));
+            sxy_y += hc[m] * (wxy[ND + r + m - 1] - wxy[ND + r - m]);
+            syy_y += hc[m] * (wyy[ND + r - 1 + m] - wyy[ND + r - m]);
         }
-        if (yr) {
-            int h = yr == 1 ? j : j - G.ny + G.fw2;
-            long long q = ((long long)s * G.fw2 + (h - 1)) * G.nx + (i - 1);
-            float ps = M.b_y_half[h - 1] * W.psi_syy_y[q] + M.a_y_half[h - 1] * syy_y;
-            W.psi_syy_y[q] = ps;
-            syy_y = syy_y / M.K_y_half[h - 1] + ps;
-            float py = M.b_y[h - 1] * W.psi_sxy_y[q] + M.a_y[h - 1] * sxy_y;
-            W.psi_sxy_y[q] = py;
-            sxy_y = sxy_y / M.K_y[h - 1] + py;
+        const int yr = yside(G, j);
+        if (G.abs_type == 1) {
+            if (xr) {
+                int h = xr == 1 ? i : i - G.nx + G.fw2;
+                long long q = ((long long)s * G.ny + (j - 1)) * G.fw2 + (h - 1);
+                float ps = M.b_x_half[h - 1] * W.psi_sxx_x[q] + M.a_x_half[h - 1] * sxx_x;
+                W.psi_sxx_x[q] = ps;
+                sxx_x = sxx_x / M.K_x_half[h - 1] + ps;
+                float py = M.b_x[h - 1] * W.psi_sxy_x[q] + M.a_x[h - 1] * sxy_x;
+                W.psi_sxy_x[q] = py;
+                sxy_x = sxy_x / M.K_x[h - 1] + py;
+            }
+            if (yr) {
+                int h = yr == 1 ? j : j - G.ny + G.fw2;
+                long long q = ((long long)s * G.fw2 + (h - 1)) * G.nx + (i - 1);
+                float ps = M.b_y_half[h - 1] * W.psi_syy_y[q] + M.a_y_half[h - 1] * syy_y;
+                W.psi_syy_y[q] = ps;
+                syy_y = syy_y / M.K_y_half[h - 1] + ps;
+                float py = M.b_y[h - 1] * W.psi_sxy_y[q] + M.a_y[h - 1] * sxy_y;
+                W.psi_sxy_y[q] = py;
+                sxy_y = sxy_y / M.K_y[h - 1] + py;
+            }
         }
+        float nvx = ovx + (sxx_x + sxy_y) * G.dtdh * rip;
+        float nvy = ovy + (sxy_x + syy_y) * G.dtdh * rjp;
+        if (G.abs_type == 2 && (xr | yr)) {
+            float a = __ldg(M.absorb + mo + o);
+            nvx *= a;
+            nvy *= a;
+        }
+        vx[o] = nvx;
+        vy[o] = nvy;
     }
-    float nvx = ovx + (sxx_x + sxy_y) * G.dtdh * rip;
-    float nvy = ovy + (sxy_x + syy_y) * G.dtdh * rjp;
-    if (G.abs_type == 2 && (xr | yr)) {
-        float a = __ldg(M.absorb + mo + o);
-        nvx *= a;
-        nvy *= a;
-    }
-    vx[o] = nvx;
-    vy[o] = nvy;
 }
 
 // Periodic x (BOUNDARY = 1): ghost columns copy the opposite edge, as the one-
@@ -175,9 +148,10 @@ __global__ void k_wrap_x(Geo G, float *a, float *b, float *c, int nd)
 template <int ND, int KIND, bool VISCO, int LT>
 __global__ void __launch_bounds__(BX *BY) k_update_s(Geo G, Wave W, Model M)
 {
-    const int i = blockIdx.x * BX + threadIdx.x + 1;
+    int bx, s;
+    block_xs(G, bx, s);
+    const int i = bx * BX + threadIdx.x + 1;
     const int j = blockIdx.y * BY + threadIdx.y + 1;
-    const int s = blockIdx.z;
     if (i > G.nx || j > G.ny)
         return;
     const int P = G.pitch;
@@ -290,9 +264,10 @@ __global__ void __launch_bounds__(BX *BY) k_update_s(Geo G, Wave W, Model M)
 template <int ND>
 __global__ void __launch_bounds__(BX *BY) k_tti_deriv(Geo G, Wave W, Model M)
 {
-    int i = blockIdx.x * BX + threadIdx.x + 1;
+    int bx, s;
+    block_xs(G, bx, s);
+    int i = bx * BX + threadIdx.x + 1;
     int j = blockIdx.y * BY + threadIdx.y + 1;
-    int s = blockIdx.z;
     if (i > G.nx || j > G.ny)
         return;
     long long o = cell(G, j, i);
@@ -337,9 +312,10 @@ __device__ __forceinline__ float tti_d(const Geo &G, const float *dr, const floa
 template <bool VISCO>
 __global__ void __launch_bounds__(BX *BY) k_update_s_tti(Geo G, Wave W, Model M)
 {
-    int i = blockIdx.x * BX + threadIdx.x + 1;
+    int bx, s;
+    block_xs(G, bx, s);
+    int i = bx * BX + threadIdx.x + 1;
     int j = blockIdx.y * BY + threadIdx.y + 1;
-    int s = blockIdx.z;
     if (i > G.nx || j > G.ny)
         return;
     int xr = xside(G, i), yr = yside(G, j);
@@ -403,19 +379,62 @@ __global__ void __launch_bounds__(BX *BY) k_update_s_tti(Geo G, Wave W, Model M)
     W.syy[so + o] = nyy;
 }
 
-// ---------------------------------------------------------- free surface
+// ------------------------------------------------ after the stress update
 
-// surface_elastic.c:27-90 / surface.c:27-113 at j = 1, one thread per column.
-template <int ND, bool VISCO>
-__global__ void k_surface(Geo G, Wave W, Model M)
+// psource.c:27-54 / eqsource.c:25-52 restricted to the cells of column i:
+// every source of the shot, in order, when the last source's type selects the
+// injection (time_loop.c:248-253); a moment tensor also reaches column i-1.
+__device__ __forceinline__ void post_sources(const Geo &G, const Wave &W, const Acq &A, int s, int i, int nt)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    int s = blockIdx.y;
-    if (i > G.nx)
+    const int lt = A.last_type[s];
+    if (lt != 1 && lt != 5)
         return;
+    const long long so = (long long)s * G.fsz;
+    float *sxx = W.sxx + so, *syy = W.syy + so, *sxy = W.sxy + so;
+    const int NT = A.nt;
+    for (int k = A.src_off[s]; k < A.src_off[s + 1]; k++) {
+        const int si = A.src_ix[k], sj = A.src_iy[k];
+        if (si != i && !(lt == 5 && si - 1 == i))
+            continue;
+        const float *sig = A.signals + (long long)k * NT - 1;  // 1-based: sig[1..NT]
+        const long long o = cell(G, sj, si);
+        if (lt == 1) {
+            // central difference of the signal (psource.c:41-49); a one-step
+            // run has no neighbouring sample and injects nothing
+            float amp = 0.0f;
+            const float d2 = 2.0f * G.dh * G.dh;
+            if (NT >= 2) {
+                if (nt == 1)
+                    amp = sig[2] / d2;
+                else if (nt < NT)
+                    amp = (sig[nt + 1] - sig[nt - 1]) / d2;
+                else
+                    amp = -sig[nt - 1] / d2;
+            }
+            sxx[o] += amp;
+            syy[o] += amp;
+        } else {
+            const float amp = A.src_amp[k] * (G.dt / (G.dh * G.dh)) * sig[nt];
+            const float m11 = -A.src_sin2[k], m12 = -A.src_cos2[k], m22 = A.src_sin2[k];
+            if (si == i) {
+                sxx[o] += amp * m11;
+                sxy[o] += 0.3f * amp * m12;
+                sxy[o - G.pitch] += 0.3f * amp * m12;
+                syy[o] += amp * m22;
+            } else {
+                sxy[o - 1] += 0.3f * amp * m12;
+            }
+        }
+    }
+}
+
+// surface_elastic.c:27-90 / surface.c:27-113 at j = 1 for column i.
+template <int ND, bool VISCO>
+__device__ __forceinline__ void post_surface(const Geo &G, const Wave &W, const Model &M, int s, int i)
+{
     const int P = G.pitch, j = 1;
-    long long so = (long long)s * G.fsz, mo = moff(G, s);
-    long long o = cell(G, j, i);
+    const long long so = (long long)s * G.fsz, mo = moff(G, s);
+    const long long o = cell(G, j, i);
     float *sxx = W.sxx + so, *syy = W.syy + so, *sxy = W.sxy + so;
     const float *vx = W.vx + so, *vy = W.vy + so;
     syy[o] = 0.0f;
@@ -445,7 +464,7 @@ __global__ void k_surface(Geo G, Wave W, Model M)
             vxx = vxx / M.K_x[h - 1] + ps;
         }
     }
-    float pu = M.pu[mo + o], ppi = M.ppi[mo + o];
+    const float pu = M.pu[mo + o], ppi = M.ppi[mo + o];
     if (!VISCO) {
         float fjm = pu * 2.0f, g = ppi;
         sxx[o] += -(G.dt * (g - fjm) * (g - fjm) * vxx / g) - (G.dt * (g - fjm) * vyy);
@@ -470,20 +489,16 @@ __global__ void k_surface(Geo G, Wave W, Model M)
     }
 }
 
-// ------------------------------------------------------------ sampling
-
-// div / curl of seismo_ssg.c:43-47 from the derivatives the stress update
-// used (CPML-stretched in the frame), before the free surface runs.
+// div / curl of seismo_ssg.c:43-47 for receiver k: the derivatives as the
+// stress update left them (CPML-stretched in the frame; psi already holds this
+// step's value, so the stretched derivative is d / K + psi).
 template <int ND, bool TTIK>
-__global__ void k_seis_deriv(Geo G, Wave W, Model M, Acq A, int ins)
+__device__ __forceinline__ void sample_div_curl(const Geo &G, const Wave &W, const Model &M, const Acq &A, int s,
+                                                int k, int ins)
 {
-    int s = blockIdx.y;
-    int k = A.rec_off[s] + blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= A.rec_off[s + 1])
-        return;
-    int i = A.rec_ix[k], j = A.rec_iy[k];
-    long long o = cell(G, j, i);
-    long long so = (long long)s * G.fsz, mo = moff(G, s);
+    const int i = A.rec_ix[k], j = A.rec_iy[k];
+    const long long o = cell(G, j, i);
+    const long long so = (long long)s * G.fsz, mo = moff(G, s);
     float vxx, vyx, vxy, vyy;
     if (TTIK) {
         const float *dc = W.dcor + 4 * so;
@@ -491,8 +506,6 @@ __global__ void k_seis_deriv(Geo G, Wave W, Model M, Acq A, int ins)
     } else {
         op_s<ND>(W.vx + so, W.vy + so, o, G.pitch, G.hc, G.dhi, vxx, vyx, vxy, vyy);
         if (G.abs_type == 1) {
-            // psi already holds this step's value (the stress update advanced
-            // it), so the stretched derivative is d / K + psi
             int xr = xside(G, i), yr = yside(G, j);
             if (xr) {
                 int h = xr == 1 ? i : i - G.nx + G.fw2;
@@ -513,15 +526,12 @@ __global__ void k_seis_deriv(Geo G, Wave W, Model M, Acq A, int ins)
     sec[4 * A.ns] = (vxy - vyx) * sqrtf(M.pu[mo + o]);
 }
 
-// vx, vy and p of seismo_ssg.c:36-62 after the step.
-__global__ void k_seis(Geo G, Wave W, Model M, Acq A, int ins, int seismo)
+// vx, vy and p of seismo_ssg.c:36-62 for receiver k after the step.
+__device__ __forceinline__ void sample_v_p(const Geo &G, const Wave &W, const Model &M, const Acq &A, int s, int k,
+                                           int ins, int seismo)
 {
-    int s = blockIdx.y;
-    int k = A.rec_off[s] + blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= A.rec_off[s + 1])
-        return;
-    long long o = cell(G, A.rec_iy[k], A.rec_ix[k]);
-    long long so = (long long)s * G.fsz, mo = moff(G, s);
+    const long long o = cell(G, A.rec_iy[k], A.rec_ix[k]);
+    const long long so = (long long)s * G.fsz, mo = moff(G, s);
     float *sec = A.sec + (long long)k * 5 * A.ns + (ins - 1);
     if (seismo == 1 || seismo == 4) {
         sec[0] = W.vx[so + o];
@@ -534,6 +544,37 @@ __global__ void k_seis(Geo G, Wave W, Model M, Acq A, int ins, int seismo)
         float ppi = M.ppi[mo + o], pu = M.pu[mo + o];
         sec[2 * A.ns] = ((3.0f * ppi - 4.0f * pu) / (2.0f * ppi - 2.0f * pu)) * p / 3.0f;
     }
+}
+
+// Everything of time_loop.c:247-285 after the stress update, one thread per
+// column: every operation below reads and writes only cells of its own column
+// (a moment tensor's column-(i-1) term is applied by that column's thread), so
+// columns are independent. Per column, in the reference's order: div/curl
+// sampling (from the stress update's derivatives), source injection, free
+// surface, the NaN probe of time_loop.c:44-47, vx/vy/p sampling.
+template <int ND, bool VISCO, bool TTIK>
+__global__ void k_post(Geo G, Wave W, Model M, Acq A, int nt, int ins, int seismo)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int s = blockIdx.y;
+    if (i > G.nx)
+        return;
+    const int *roff = A.rec_col_off ? A.rec_col_off + (long long)s * (G.nx + 1) : nullptr;
+    const int r0 = roff ? roff[i - 1] : 0, r1 = roff ? roff[i] : 0;
+    if (ins && (seismo == 3 || seismo == 4))
+        for (int r = r0; r < r1; r++)
+            sample_div_curl<ND, TTIK>(G, W, M, A, s, A.rec_col_idx[r], ins);
+    post_sources(G, W, A, s, i, nt);
+    if (G.free_surf)
+        post_surface<ND, VISCO>(G, W, M, s, i);
+    if (i == (G.nx / 2 > 0 ? G.nx / 2 : 1)) {
+        long long pc = cell(G, G.ny / 2 > 0 ? G.ny / 2 : 1, i);
+        if (isnan(W.vy[(long long)s * G.fsz + pc]) && A.status[s] == 0)
+            A.status[s] = nt;
+    }
+    if (ins && seismo != 3)
+        for (int r = r0; r < r1; r++)
+            sample_v_p(G, W, M, A, s, A.rec_col_idx[r], ins, seismo);
 }
 
 // snap_ssg.c:86-205: one snapshot frame, file order (x outer, y inner).

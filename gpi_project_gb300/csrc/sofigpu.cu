@@ -167,6 +167,7 @@ struct sofi_ctx {
     float last_ms = 0.f;
     bool run_pending = false;  // ev0/ev1 recorded by a sofi_run not yet synchronised
     bool march = false;        // y-marching kernels (ISO/VTI stress, all velocity updates)
+    int vrows = 1;             // rows per thread of the velocity kernel (1, 2 or 4)
     int march_sy = 32;         // rows per block of the y-marching kernels
     // snapshots
     int snap_nx = 0, snap_ny = 0, snap_total = 0, nsnap = 0;
@@ -278,6 +279,35 @@ int upload_acq(sofi_ctx *c)
     }
     int ns_src = soff[S], nrec = roff[S];
     c->has_force = false;
+    // receivers grouped by (shot, column): the post-stress kernel samples the
+    // receivers of its own column
+    std::vector<int> colcnt((size_t)S * (c->cfg.nx + 1), 0), colidx(nrec > 0 ? nrec : 1, 0);
+    for (int s = 0; s < S; s++)
+        for (int k = roff[s]; k < roff[s + 1]; k++)
+            colcnt[(size_t)s * (c->cfg.nx + 1) + c->acq[s].rix[k - roff[s]]]++;
+    for (int s = 0; s < S; s++) {  // counts -> start of each column's group
+        int *cc = &colcnt[(size_t)s * (c->cfg.nx + 1)];
+        int run = roff[s];
+        for (int i = 0; i <= c->cfg.nx; i++) {
+            int n = cc[i];
+            cc[i] = run;
+            run += n;
+        }
+    }
+    // colidx: receivers in column order; coloff[s][i-1] .. coloff[s][i] spans column i
+    {
+        std::vector<int> fill(colcnt);
+        for (int s = 0; s < S; s++)
+            for (int k = roff[s]; k < roff[s + 1]; k++) {
+                int x = c->acq[s].rix[k - roff[s]];
+                colidx[fill[(size_t)s * (c->cfg.nx + 1) + x]++] = k;
+            }
+    }
+    std::vector<int> coloff((size_t)S * (c->cfg.nx + 1));
+    for (int s = 0; s < S; s++)
+        for (int i = 0; i <= c->cfg.nx; i++)
+            coloff[(size_t)s * (c->cfg.nx + 1) + i] =
+                (i < c->cfg.nx) ? colcnt[(size_t)s * (c->cfg.nx + 1) + i + 1] : roff[s + 1];
     std::vector<int> ix, iy, ty, rix, riy;
     std::vector<float> amp, sn, cs, sn2, cs2, sig;
     for (int s = 0; s < S; s++) {
@@ -299,7 +329,7 @@ int upload_acq(sofi_ctx *c)
     }
     // one allocation: ints then floats, 256-byte aligned pieces
     auto al = [](size_t n) { return (n + 63) / 64 * 64; };
-    size_t ni = al(S + 1) * 2 + al(S) + al(ns_src) * 3 + al(nrec) * 2;
+    size_t ni = al(S + 1) * 2 + al(S) + al(ns_src) * 3 + al(nrec) * 2 + al(coloff.size()) + al(colidx.size());
     size_t nf = al(ns_src) * 5 + al((size_t)ns_src * NT);
     std::vector<int> hi(ni, 0);
     std::vector<float> hf(nf, 0.f);
@@ -309,6 +339,7 @@ int upload_acq(sofi_ctx *c)
     size_t o_soff = puti(soff, S + 1), o_roff = puti(roff, S + 1), o_last = puti(last, S);
     size_t o_ix = puti(ix, ns_src), o_iy = puti(iy, ns_src), o_ty = puti(ty, ns_src);
     size_t o_rix = puti(rix, nrec), o_riy = puti(riy, nrec);
+    size_t o_coff = puti(coloff, coloff.size()), o_cidx = puti(colidx, colidx.size());
     size_t o_amp = putf(amp, ns_src), o_sn = putf(sn, ns_src), o_cs = putf(cs, ns_src), o_sn2 = putf(sn2, ns_src),
            o_cs2 = putf(cs2, ns_src), o_sig = putf(sig, (size_t)ns_src * NT);
     if (c->acq_buf) {
@@ -339,6 +370,7 @@ int upload_acq(sofi_ctx *c)
     A.src_off = ib + o_soff, A.rec_off = ib + o_roff, A.last_type = ib + o_last;
     A.src_ix = ib + o_ix, A.src_iy = ib + o_iy, A.src_type = ib + o_ty;
     A.rec_ix = ib + o_rix, A.rec_iy = ib + o_riy;
+    A.rec_col_off = ib + o_coff, A.rec_col_idx = ib + o_cidx;
     A.src_amp = fb + o_amp, A.src_sin = fb + o_sn, A.src_cos = fb + o_cs, A.src_sin2 = fb + o_sn2,
     A.src_cos2 = fb + o_cs2, A.signals = fb + o_sig;
     A.nt = NT;
@@ -358,7 +390,10 @@ int upload_acq(sofi_ctx *c)
 
 dim3 grid2d(const sofi_ctx *c)
 {
-    return dim3((c->cfg.nx + BX - 1) / BX, (c->cfg.ny + BY - 1) / BY, c->cfg.nshots);
+    unsigned tx = (c->cfg.nx + BX - 1) / BX, ty = (c->cfg.ny + BY - 1) / BY;
+    if (c->G.shot_fast)
+        return dim3(tx * c->cfg.nshots, ty, 1);
+    return dim3(tx, ty, c->cfg.nshots);
 }
 
 #define DISPATCH_ND(ND_, ...)                        \
@@ -424,10 +459,19 @@ int launch_step(sofi_ctx *c, int nt)
         c->tev_used += 3;
         CK(cudaEventRecord(e0, st));
     }
-    if (c->march)
+    if (c->march) {
         launch_march_v(G, c->W, c->M, c->nd, c->march_sy, st);
-    else
-        DISPATCH_ND(c->nd, (k_update_v<ND><<<grd, blk, 0, st>>>(G, c->W, c->M)));
+    } else {
+        int R = c->vrows;
+        unsigned tx = (cf.nx + BX - 1) / BX, ty = (cf.ny + BY * R - 1) / (BY * R);
+        dim3 gv = G.shot_fast ? dim3(tx * S, ty, 1) : dim3(tx, ty, S);
+        if (R == 1)
+            DISPATCH_ND(c->nd, (k_update_v<ND, 1><<<gv, blk, 0, st>>>(G, c->W, c->M)))
+        else if (R == 2)
+            DISPATCH_ND(c->nd, (k_update_v<ND, 2><<<gv, blk, 0, st>>>(G, c->W, c->M)))
+        else
+            DISPATCH_ND(c->nd, (k_update_v<ND, 4><<<gv, blk, 0, st>>>(G, c->W, c->M)))
+    }
     c->launches++;
     if (timed)
         CK(cudaEventRecord(e1, st));
@@ -454,33 +498,16 @@ int launch_step(sofi_ctx *c, int nt)
         CK(cudaEventRecord(e2, st));
     bool sample = cf.seismo && c->total_rec > 0 && nt % cf.ndt == 0 && nt < cf.nt;
     int ins = sample ? nt / cf.ndt : 0;
-    int maxrec = 0;
-    for (auto &a : c->acq)
-        maxrec = std::max(maxrec, (int)a.rix.size());
-    dim3 rg((maxrec + 127) / 128, S);
-    if (sample && (cf.seismo == 3 || cf.seismo == 4)) {
-        if (kind == TTI)
-            DISPATCH_ND(c->nd, (k_seis_deriv<ND, true><<<rg, 128, 0, st>>>(G, c->W, c->M, c->A, ins)))
-        else
-            DISPATCH_ND(c->nd, (k_seis_deriv<ND, false><<<rg, 128, 0, st>>>(G, c->W, c->M, c->A, ins)))
-        c->launches++;
-    }
-    k_stress_src<<<nb, 128, 0, st>>>(G, c->W, c->A, nt);
+    dim3 pg((cf.nx + 127) / 128, S);
+    if (kind == TTI)
+        DISPATCH_ND(c->nd, (k_post<ND, false, true><<<pg, 128, 0, st>>>(G, c->W, c->M, c->A, nt, ins, cf.seismo)))
+    else if (visco)
+        DISPATCH_ND(c->nd, (k_post<ND, true, false><<<pg, 128, 0, st>>>(G, c->W, c->M, c->A, nt, ins, cf.seismo)))
+    else
+        DISPATCH_ND(c->nd, (k_post<ND, false, false><<<pg, 128, 0, st>>>(G, c->W, c->M, c->A, nt, ins, cf.seismo)))
     c->launches++;
-    if (cf.free_surf) {
-        dim3 sg((cf.nx + 127) / 128, S);
-        if (visco)
-            DISPATCH_ND(c->nd, (k_surface<ND, true><<<sg, 128, 0, st>>>(G, c->W, c->M)))
-        else
-            DISPATCH_ND(c->nd, (k_surface<ND, false><<<sg, 128, 0, st>>>(G, c->W, c->M)))
-        c->launches++;
-    }
     if (cf.boundary) {
         k_wrap_x<<<dim3((cf.ny + 127) / 128, S), 128, 0, st>>>(G, c->W.sxx, c->W.syy, c->W.sxy, c->nd);
-        c->launches++;
-    }
-    if (sample && cf.seismo != 3) {
-        k_seis<<<rg, 128, 0, st>>>(G, c->W, c->M, c->A, ins, cf.seismo);
         c->launches++;
     }
     if (cf.snap && nt >= cf.snap_first && nt <= cf.snap_last &&
@@ -588,6 +615,8 @@ int sofi_create(const sofi_config *cfg, int device, sofi_ctx **out)
     c->acq.resize(cfg->nshots);
     if (const char *e = getenv("SOFI_KERNELS"))
         c->march = strcmp(e, "march") == 0;
+    if (const char *e = getenv("SOFI_VROWS"))
+        c->vrows = (atoi(e) == 2 || atoi(e) == 4) ? atoi(e) : 1;
     if (const char *e = getenv("SOFI_MARCH_ROWS"))
         c->march_sy = atoi(e) > 0 ? atoi(e) : c->march_sy;
     e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
@@ -606,6 +635,9 @@ int sofi_create(const sofi_config *cfg, int device, sofi_ctx **out)
     G.L = is_visco(cfg->weq) ? cfg->L : 0;
     G.model_stride_on = cfg->shared_model ? 0 : 1;
     G.el_tti_rb_short = (cfg->weq == SOFI_EL_TTI);
+    G.shot_fast = (cfg->shared_model && cfg->nshots > 1) ? 1 : 0;
+    if (const char *e = getenv("SOFI_SHOT_ORDER"))
+        G.shot_fast = G.shot_fast && strcmp(e, "slow") != 0;
     // subgrid_bounds.c:65-66,260-270 (one rank); without a frame the whole grid is interior
     int fw = G.abs_type ? cfg->fw : 0;
     G.gx2 = fw, G.gx3 = cfg->nx - fw, G.gy2 = fw, G.gy3 = cfg->ny - fw;

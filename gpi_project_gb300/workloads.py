@@ -11,7 +11,7 @@ benchmark configurations with their shapes, sizes and value distributions:
       (5/15/50 Hz, F_REF 15 Hz), CPML 30, free surface; smooth random Vp
       1500-4500, Vs = Vp/1.8, Gardner density, smooth Q 20-100 (Qp = Qs);
       Ricker 15 Hz vertical force; 1000 receivers
-  c3  TTI elastic, 2048 x 2048, DH 2.5 m, DT 2.5e-4 s, NT 4000, FD6, CPML 20;
+  c3  TTI elastic, 2048 x 2048, DH 2.5 m, DT 2.0e-4 s, NT 4000, FD6, CPML 20;
       Vp 2000-4000, Vs = Vp/1.8, rho 2000-2600, eps 0-0.25, delta -0.1-0.15,
       tilt 0-45 deg smoothed over 20 cells; explosive Ricker 20 Hz; 512 receivers
   c4  64 shots on the c1 layered model enlarged to 2000 x 1000 with c2's Q field
@@ -93,7 +93,10 @@ def workload(name: str) -> dict:
         rho = smooth_field(rng, nx, ny, 20, 2000.0, 2600.0)
         mats = dict(vp=vp, vs=vs, rho=rho, epsilon=smooth_field(rng, nx, ny, 20, 0.0, 0.25),
                     delta=smooth_field(rng, nx, ny, 20, -0.1, 0.15), theta=smooth_field(rng, nx, ny, 20, 0.0, 45.0))
-        par = dict(weq=6, nx=nx, ny=ny, dh=2.5, dt=2.5e-4, nt=4000, fdorder=6, maxrelerror=1, fw=20, abs_type=1,
+        # DT 2.5e-4 passes the reference's CFL check but the staggered TTI update
+        # diverges inside this model after ~1400 steps (the reference's own
+        # algorithm does the same); 2.0e-4 is stable over the whole run
+        par = dict(weq=6, nx=nx, ny=ny, dh=2.5, dt=2.0e-4, nt=4000, fdorder=6, maxrelerror=1, fw=20, abs_type=1,
                    npower=4.0, k_max_cpml=1.0, vppml=5000.0, fpml=20.0, seismo=1, ndt=1)
         src = _srcpos([(2560.0, 30.0)], 2.5, 20.0, 1)
         xs = np.linspace(21 * 2.5, (nx - 22) * 2.5, 512)
