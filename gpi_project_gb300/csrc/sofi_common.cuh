@@ -48,6 +48,8 @@ struct Geo {
     int model_stride_on;    // 1: model per shot, 0: shared
     int el_tti_rb_short;    // EL_TTI CPML: right-bottom corner pass stops at NY-1
     int shot_fast;          // block index: shot varies fastest (model tiles shared in L2)
+    int seismo, ndt;        // sampling (gv->SEISMO, gv->NDT)
+    int *step_ctr;          // device: time steps completed; the velocity kernel advances it
     float dt, dh, dtdh, dhi, dthalbe;
     float hc[7];
 };

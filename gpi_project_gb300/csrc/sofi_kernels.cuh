@@ -6,12 +6,14 @@ namespace sofi {
 
 // -------------------------------------------------------------- sources
 
-// update_v_interior.c:49-71
-__global__ void k_force_src(Geo G, Wave W, Model M, Acq A, int nt)
+// update_v_interior.c:49-71. Runs before the velocity kernel advances the
+// step counter, so the step being computed is counter + 1.
+__global__ void k_force_src(Geo G, Wave W, Model M, Acq A)
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= G.nshots)
         return;
+    const int nt = *G.step_ctr + 1;
     const float *prip = M.prip + moff(G, s), *prjp = M.prjp + moff(G, s);
     float *vx = W.vx + (long long)s * G.fsz, *vy = W.vy + (long long)s * G.fsz;
     for (int k = A.src_off[s]; k < A.src_off[s + 1]; k++) {
@@ -44,6 +46,10 @@ __global__ void __launch_bounds__(BX *BY) k_update_v(Geo G, Wave W, Model M)
     block_xs(G, bx, s);
     const int i = bx * BX + threadIdx.x + 1;
     const int jb = (blockIdx.y * BY + threadIdx.y) * R + 1;
+    // one thread advances the step counter: every kernel queued before this
+    // one has read it, every kernel after it sees the step being computed
+    if (G.step_ctr && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+        *G.step_ctr += 1;
     if (i > G.nx || jb > G.ny)
         return;
     const int P = G.pitch;
@@ -553,12 +559,16 @@ __device__ __forceinline__ void sample_v_p(const Geo &G, const Wave &W, const Mo
 // sampling (from the stress update's derivatives), source injection, free
 // surface, the NaN probe of time_loop.c:44-47, vx/vy/p sampling.
 template <int ND, bool VISCO, bool TTIK>
-__global__ void k_post(Geo G, Wave W, Model M, Acq A, int nt, int ins, int seismo)
+__global__ void k_post(Geo G, Wave W, Model M, Acq A)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int s = blockIdx.y;
     if (i > G.nx)
         return;
+    const int nt = *G.step_ctr;  // the velocity kernel of this step advanced it
+    const int seismo = G.seismo;
+    // time_loop.c:282: sample at nt = NDT, 2 NDT, ... while nt < NT
+    const int ins = (seismo && G.ndt > 0 && nt % G.ndt == 0 && nt < A.nt) ? nt / G.ndt : 0;
     const int *roff = A.rec_col_off ? A.rec_col_off + (long long)s * (G.nx + 1) : nullptr;
     const int r0 = roff ? roff[i - 1] : 0, r1 = roff ? roff[i] : 0;
     if (ins && (seismo == 3 || seismo == 4))

@@ -52,6 +52,8 @@ __global__ void __launch_bounds__(TX) k_march_v(Geo G, Wave W, Model M, int SY)
     const int j1 = min(j0 + SY - 1, G.ny);
     const int s = blockIdx.z;
     const bool act = i <= G.nx;
+    if (G.step_ctr && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && tx == 0)
+        *G.step_ctr += 1;  // as k_update_v
     const long long so = (long long)s * G.fsz, mo = moff(G, s);
     const float *sxx = W.sxx + so, *syy = W.syy + so, *sxy = W.sxy + so;
     float *vx = W.vx + so, *vy = W.vy + so;

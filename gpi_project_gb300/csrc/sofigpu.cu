@@ -22,6 +22,8 @@ using namespace sofi;
 
 namespace {
 
+constexpr int kGraphSteps = 32;
+
 thread_local std::string g_err;
 
 int fail(int code, const char *fmt, ...)
@@ -168,6 +170,12 @@ struct sofi_ctx {
     bool run_pending = false;  // ev0/ev1 recorded by a sofi_run not yet synchronised
     bool march = false;        // y-marching kernels (ISO/VTI stress, all velocity updates)
     int vrows = 1;             // rows per thread of the velocity kernel (1, 2 or 4)
+    // CUDA graph of kGraphSteps time steps, replayed for every chunk without
+    // snapshot or timed steps (the step number lives in G.step_ctr)
+    bool use_graph = true;
+    bool graph_dirty = true;
+    cudaGraphExec_t graph_exec = nullptr;
+    long long graph_launches = 0;  // kernels per replay
     int march_sy = 32;         // rows per block of the y-marching kernels
     // snapshots
     int snap_nx = 0, snap_ny = 0, snap_total = 0, nsnap = 0;
@@ -385,6 +393,7 @@ int upload_acq(sofi_ctx *c)
     c->total_src = ns_src;
     c->total_rec = nrec;
     c->acq_dirty = false;
+    c->graph_dirty = true;
     return 0;
 }
 
@@ -431,7 +440,9 @@ void launch_cell_s(const Geo &G, const Wave &W, const Model &M, int nd, int kind
         visco ? cell_s_l<VTI, true>(G, W, M, nd, grd, blk, st) : cell_s_l<VTI, false>(G, W, M, nd, grd, blk, st);
 }
 
-int launch_step(sofi_ctx *c, int nt)
+// One time step. `capture`: being recorded into the step graph, so no host-
+// side step number exists (no timing events, no snapshot).
+int launch_step(sofi_ctx *c, int nt, bool capture = false)
 {
     const sofi_config &cf = c->cfg;
     cudaStream_t st = c->stream;
@@ -442,10 +453,10 @@ int launch_step(sofi_ctx *c, int nt)
     int kind = kind_of(cf.weq);
     bool visco = is_visco(cf.weq);
     if (c->has_force) {
-        k_force_src<<<nb, 128, 0, st>>>(G, c->W, c->M, c->A, nt);
+        k_force_src<<<nb, 128, 0, st>>>(G, c->W, c->M, c->A);
         c->launches++;
     }
-    bool timed = c->time_every > 0 && (nt % c->time_every) == 0;
+    bool timed = !capture && c->time_every > 0 && (nt % c->time_every) == 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
     if (timed) {
         if (c->tev_used + 3 > c->tev.size()) {
@@ -496,21 +507,19 @@ int launch_step(sofi_ctx *c, int nt)
     c->launches++;
     if (timed)
         CK(cudaEventRecord(e2, st));
-    bool sample = cf.seismo && c->total_rec > 0 && nt % cf.ndt == 0 && nt < cf.nt;
-    int ins = sample ? nt / cf.ndt : 0;
     dim3 pg((cf.nx + 127) / 128, S);
     if (kind == TTI)
-        DISPATCH_ND(c->nd, (k_post<ND, false, true><<<pg, 128, 0, st>>>(G, c->W, c->M, c->A, nt, ins, cf.seismo)))
+        DISPATCH_ND(c->nd, (k_post<ND, false, true><<<pg, 128, 0, st>>>(G, c->W, c->M, c->A)))
     else if (visco)
-        DISPATCH_ND(c->nd, (k_post<ND, true, false><<<pg, 128, 0, st>>>(G, c->W, c->M, c->A, nt, ins, cf.seismo)))
+        DISPATCH_ND(c->nd, (k_post<ND, true, false><<<pg, 128, 0, st>>>(G, c->W, c->M, c->A)))
     else
-        DISPATCH_ND(c->nd, (k_post<ND, false, false><<<pg, 128, 0, st>>>(G, c->W, c->M, c->A, nt, ins, cf.seismo)))
+        DISPATCH_ND(c->nd, (k_post<ND, false, false><<<pg, 128, 0, st>>>(G, c->W, c->M, c->A)))
     c->launches++;
     if (cf.boundary) {
         k_wrap_x<<<dim3((cf.ny + 127) / 128, S), 128, 0, st>>>(G, c->W.sxx, c->W.syy, c->W.sxy, c->nd);
         c->launches++;
     }
-    if (cf.snap && nt >= cf.snap_first && nt <= cf.snap_last &&
+    if (!capture && cf.snap && nt >= cf.snap_first && nt <= cf.snap_last &&
         (nt == cf.snap_first || (cf.snap_inc > 0 && (nt - cf.snap_first) % cf.snap_inc == 0)) &&
         c->nsnap < c->snap_total) {
         long long n = (long long)c->snap_nx * c->snap_ny;
@@ -636,6 +645,7 @@ int sofi_create(const sofi_config *cfg, int device, sofi_ctx **out)
     G.model_stride_on = cfg->shared_model ? 0 : 1;
     G.el_tti_rb_short = (cfg->weq == SOFI_EL_TTI);
     G.shot_fast = (cfg->shared_model && cfg->nshots > 1) ? 1 : 0;
+    G.seismo = cfg->seismo, G.ndt = cfg->ndt;
     if (const char *e = getenv("SOFI_SHOT_ORDER"))
         G.shot_fast = G.shot_fast && strcmp(e, "slow") != 0;
     // subgrid_bounds.c:65-66,260-270 (one rank); without a frame the whole grid is interior
@@ -694,8 +704,11 @@ int sofi_create(const sofi_config *cfg, int device, sofi_ctx **out)
             goto bad;
         *slot_ptr(c->M, n.c_str(), true) = p;
     }
-    if ((rc = dalloc(c, (void **)&c->d_status, sizeof(int) * cfg->nshots)))
+    if ((rc = dalloc(c, (void **)&c->d_status, sizeof(int) * (cfg->nshots + 1))))
         goto bad;
+    c->G.step_ctr = c->d_status + cfg->nshots;  // zeroed with the status words
+    if (const char *e = getenv("SOFI_GRAPH"))
+        c->use_graph = atoi(e) != 0;
     c->A.status = c->d_status;
     c->snap_total = count_snapshots(*cfg);
     if (c->snap_total) {
@@ -731,6 +744,8 @@ int sofi_destroy(sofi_ctx *c)
     }
     for (auto e : c->tev)
         cudaEventDestroy(e);
+    if (c->graph_exec)
+        cudaGraphExecDestroy(c->graph_exec);
     if (c->ev0)
         cudaEventDestroy(c->ev0);
     if (c->ev1)
@@ -743,6 +758,7 @@ int sofi_set_hc(sofi_ctx *c, const float *hc)
 {
     if (!c || !hc)
         return fail(SOFI_E_ARG, "null argument");
+    c->graph_dirty = true;
     for (int k = 0; k < 7; k++)
         c->G.hc[k] = hc[k];
     return 0;
@@ -769,6 +785,7 @@ int sofi_set_model_vector(sofi_ctx *c, const char *name, const float *host, int 
 {
     if (!c || !name || !host)
         return fail(SOFI_E_ARG, "null argument");
+    c->graph_dirty = true;
     CK(cudaSetDevice(c->device));
     if (!strcmp(name, "bip") || !strcmp(name, "cip") || !strcmp(name, "peta")) {
         if (n != c->G.L)
@@ -867,7 +884,7 @@ int sofi_reset(sofi_ctx *c, int shot)
             CK(cudaMemsetAsync(c->W.dcor + 4LL * s * c->G.fsz, 0, 4 * f, c->stream));
         }
     }
-    CK(cudaMemsetAsync(c->d_status, 0, sizeof(int) * c->cfg.nshots, c->stream));
+    CK(cudaMemsetAsync(c->d_status, 0, sizeof(int) * (c->cfg.nshots + 1), c->stream));  // + step counter
     if (c->d_sec && !c->acq_dirty) {
         size_t n = (size_t)c->total_rec * 5 * (c->A.ns > 0 ? c->A.ns : 1);
         CK(cudaMemsetAsync(c->d_sec, 0, n * sizeof(float), c->stream));
@@ -875,6 +892,47 @@ int sofi_reset(sofi_ctx *c, int shot)
     c->step = 0;
     c->nsnap = 0;
     CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+// Whether steps first..first+n-1 need a direct launch (snapshot or timed step).
+static bool chunk_has_event(const sofi_ctx *c, int first, int n)
+{
+    const sofi_config &cf = c->cfg;
+    for (int nt = first; nt < first + n; nt++) {
+        if (c->time_every > 0 && nt % c->time_every == 0)
+            return true;
+        if (cf.snap && nt >= cf.snap_first && nt <= cf.snap_last &&
+            (nt == cf.snap_first || (cf.snap_inc > 0 && (nt - cf.snap_first) % cf.snap_inc == 0)))
+            return true;
+    }
+    return false;
+}
+
+static int build_graph(sofi_ctx *c)
+{
+    if (c->graph_exec) {
+        cudaGraphExecDestroy(c->graph_exec);
+        c->graph_exec = nullptr;
+    }
+    long long before = c->launches;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = 0;
+    for (int k = 0; k < kGraphSteps && !rc; k++)
+        rc = launch_step(c, 0, true);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    if (rc)
+        return rc;
+    if (e != cudaSuccess)
+        return fail(SOFI_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&c->graph_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess)
+        return fail(SOFI_E_CUDA, "graph instantiation: %s", cudaGetErrorString(e));
+    c->graph_launches = c->launches - before;
+    c->launches = before;
+    c->graph_dirty = false;
     return 0;
 }
 
@@ -893,11 +951,25 @@ int sofi_run(sofi_ctx *c, int nsteps)
             return rc;
     }
     CK(cudaEventRecord(c->ev0, c->stream));
-    for (int k = 0; k < nsteps; k++) {
+    int left = nsteps;
+    while (left > 0) {
+        if (c->use_graph && left >= kGraphSteps && !chunk_has_event(c, c->step + 1, kGraphSteps)) {
+            if (c->graph_dirty || !c->graph_exec) {
+                int rc = build_graph(c);
+                if (rc)
+                    return rc;
+            }
+            CK(cudaGraphLaunch(c->graph_exec, c->stream));
+            c->launches += c->graph_launches;
+            c->step += kGraphSteps;
+            left -= kGraphSteps;
+            continue;
+        }
         int rc = launch_step(c, c->step + 1);
         if (rc)
             return rc;
         c->step++;
+        left--;
     }
     CK(cudaEventRecord(c->ev1, c->stream));
     CK(cudaGetLastError());

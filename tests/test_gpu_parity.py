@@ -103,3 +103,27 @@ def test_march_kernels_match_simple_kernels(name, monkeypatch):
     for k in out["march"]:
         assert rel_l2(out["march"][k], out["simple"][k]) < 1e-6, (name, k)
     o.close()
+
+
+@pytest.mark.parametrize("name", ["visc_cpml_fs_l3", "el_mixed_sources", "tti_cpml", "el_periodic_cpml"])
+def test_graph_replay_equals_direct_launches(name, monkeypatch):
+    """Steps replayed from the captured 32-step graph equal directly launched steps."""
+    from oracle import oracle as O
+    from tests.golden.cases import case_by_name
+    from tests.helpers import case_receivers, case_sources
+    case = case_by_name(name)
+    o = run_oracle_case(case, nthreads=os.cpu_count() or 1, nsteps=1)
+    cfg = o.cfg
+    sp = case_sources(case, cfg)
+    sig = O.wavelet(1, cfg.nt, cfg.dt, sp)
+    out = {}
+    for variant in ["0", "1"]:
+        monkeypatch.setenv("SOFI_GRAPH", variant)
+        t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
+        out[variant] = {k: t.field(k) for k in ["vx", "vy", "sxx", "syy", "sxy"]}
+        out[variant].update({c: t.section(c) for c in ["vx", "p", "div"]})
+        out[variant]["snap"] = t.snapshots("vx")
+        t.close()
+    for k in out["1"]:
+        np.testing.assert_array_equal(out["1"][k], out["0"][k], err_msg=f"{name} {k}")
+    o.close()
