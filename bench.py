@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=0, help="time steps of the CPU sample (0 = auto)")
+    ap.add_argument("--served-requests", type=int, default=24,
+                    help="requests of the served (c5) leg added to the line; 0 = none")
     ap.add_argument("--nt", type=int, default=0,
                     help="time steps per solve (default: the workload's NT; a small value keeps profiler captures short)")
     return ap.parse_args()
@@ -200,9 +202,122 @@ def run_reference(args, W):
     print(json.dumps(line), flush=True)
 
 
+def served_leg(n_req: int, device: int, passes: int = 1, seed: int = 1005) -> dict:
+    """c5: a seeded stream of uneven solves through the request loop.
+
+    Three runs of the same stream: the plain loop (one solve resident at a
+    time, the reference's one-shot-after-another order), the loop with every
+    request arriving at once (throughput, HBM roofline), and Poisson arrivals at
+    70 % of that throughput (latency). Host arrays in, sections out: every run
+    is end to end, model preparation included.
+    """
+    from gpi_project_gb300 import host, serve, workloads
+    reqs = workloads.request_stream(n_req, seed=seed)
+    cells = sum(r["cell_updates"] for r in reqs)
+    alg = sum(r["cell_updates"] * workloads.bytes_per_cell(r["par"]["weq"], r["par"]["L"])["step"] for r in reqs)
+    h2d = sum(sum(a.nbytes for a in r["mats"].values()) for r in reqs)
+
+    def run(max_resident, arrivals, stream=reqs):
+        with serve.Server(device=device, max_resident=max_resident) as srv:
+            t0 = srv.clock() + 0.01
+            ids = [srv.submit(host.make_par(**r["par"]), r["mats"], r["src"], *r["rec"], arrival=t0 + a)
+                   for r, a in zip(stream, arrivals)]
+            srv.drain()
+            st = srv.stats()
+            d2h = 0
+            for rid in ids:
+                i = srv.info(rid)
+                if i["state"] != serve.REQ_DONE:
+                    raise SystemExit(f"served request {rid} failed: {i['error']}")
+                d2h += i["ntr"] * i["ns"] * 4 * 2
+            st["d2h"] = d2h
+            st["makespan"] = st["last_finish"] - t0
+        return st
+
+    warm = workloads.request_stream(3, seed=seed + 100, nt_range=(64, 64), nx_range=(256, 512),
+                                    ny_range=(256, 512))
+    run(8, [0.0] * len(warm), warm)
+    zero = [0.0] * n_req
+    plain = run(1, zero)
+    sats = [run(64, zero) for _ in range(passes)]
+    sat = min(sats, key=lambda x: x["makespan"])
+    rate = 0.7 * n_req / sat["makespan"]
+    rng = __import__("numpy").random.default_rng(seed + 1)
+    arr = list(__import__("numpy").cumsum(rng.exponential(1.0 / rate, n_req)))
+    lat = run(64, arr)
+    peak, peak_kind = measured_peaks()
+    ach = alg / sat["makespan"] / 1e9
+    return {
+        "requests": n_req, "cell_updates": cells,
+        "grid": "NX 256-4096, NY 256-2048 log-uniform; NT 1000-6000; FDORDER 4/8; elastic or viscoelastic L=3",
+        "gcell_per_s": round(cells / sat["makespan"] / 1e9, 3),
+        "shots_per_s": round(n_req / sat["makespan"], 3),
+        "plain_gcell_per_s": round(cells / plain["makespan"] / 1e9, 3),
+        "plain_shots_per_s": round(n_req / plain["makespan"], 3),
+        "speedup_vs_plain": round(plain["makespan"] / sat["makespan"], 3),
+        "hbm_roofline": {"achieved": round(ach, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                         "frac": round(ach / peak, 4), "algorithmic_bytes": int(alg)},
+        "all_at_once": {"p50_s": round(sat["p50_s"], 3), "p99_s": round(sat["p99_s"], 3),
+                        "plain_p50_s": round(plain["p50_s"], 3), "plain_p99_s": round(plain["p99_s"], 3),
+                        "peak_resident": sat["peak_resident"], "peak_bytes": sat["peak_bytes"]},
+        "poisson": {"rate_per_s": round(rate, 3), "p50_s": round(lat["p50_s"], 3), "p99_s": round(lat["p99_s"], 3),
+                    "mean_s": round(lat["mean_s"], 3), "peak_resident": lat["peak_resident"]},
+        "h2d_bytes": int(h2d), "d2h_bytes": int(sat["d2h"]), "gpu_launches": int(sat["launches"]),
+    }
+
+
+def main_served(args):
+    """--workload c5: the request stream through the serving loop is the line."""
+    rank, world, local = dist_info()
+    from gpi_project_gb300 import workloads
+    n_req = args.served_requests or 24
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import oracle as O
+        O.build()
+        r = workloads.request_stream(1)[0]
+        W = dict(name="c5", par=r["par"], mats=r["mats"], src=r["src"], rec=r["rec"], nshots=1)
+        run_reference(args, W)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    with ClockSampler(local) as clk:
+        leg = served_leg(n_req, local, passes=max(1, args.steps))
+    if rank != 0:
+        return
+    cps = leg["shots_per_s"] and leg["requests"] / leg["shots_per_s"]
+    out = {
+        "metric": "Gcell-updates/s", "value": leg["gcell_per_s"], "unit": "Gcell-updates/s", "n_gpus": world,
+        "steps": max(1, args.steps), "warmup": 1, "ms_per_step": round(1e3 * cps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded request stream; gpi_project_gb300/workloads.py request_stream)",
+        "config": {"workload": "c5", "requests": n_req, "grid": leg["grid"],
+                   "l2": "inputs larger than L2 (the stream holds ~0.5 GB of models)", "parallelism": "replicas x1"},
+        "e2e": {"value": leg["gcell_per_s"], "unit": "Gcell-updates/s", "h2d_bytes_per_step": leg["h2d_bytes"],
+                "d2h_bytes_per_step": leg["d2h_bytes"]},
+        "roofline": {"kernel": "whole step of every resident solve", "bound": "hbm", **leg["hbm_roofline"],
+                     "traffic": None},
+        "gpu_launches": leg["gpu_launches"], "served": leg, "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.build()
+        r = workloads.request_stream(1)[0]
+        W = dict(name="c5", par=r["par"], mats=r["mats"], src=r["src"], rec=r["rec"], nshots=1)
+        n = args.cpu_steps or auto_cpu_steps(W)
+        v, sec = cpu_sample(W, n, cpu_threads())
+        out["cpu_baseline"] = {"value": round(v, 4), "unit": "Gcell-updates/s", "cores": cpu_threads(),
+                               "kind": "port", "sample": f"{n} time steps of the first request "
+                                                         f"({r['par']['nx']}x{r['par']['ny']}, {sec:.1f} s)"}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
+    if args.workload == "c5":
+        return main_served(args)
     from gpi_project_gb300 import workloads
     W = workloads.workload(args.workload)
     if args.nt:
@@ -371,6 +486,11 @@ def main():
         **({"batched": batched} if batched else {}),
         "clocks": clk.summary(),
     }
+    if args.served_requests > 0 and world == 1:
+        t.close()
+        with ClockSampler(local) as clk2:
+            out["served"] = served_leg(args.served_requests, local)
+        out["served"]["clocks"] = clk2.summary()
     if not args.no_cpu_baseline and rank == 0:
         n = args.cpu_steps or auto_cpu_steps(W)
         from oracle import oracle as O

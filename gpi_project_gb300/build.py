@@ -3,6 +3,8 @@
 * libsofigpu.so  -- CUDA kernels + C ABI (include/sofigpu.h), sm_103a only.
 * libsofihost.so -- C host: parameter/model/acquisition readers, model
                     preparation, SU/snapshot writers (include/sofihost.h).
+* libsofiserve.so -- continuous-batching request loop over the two above
+                    (include/sofiserve.h).
 * sofi2d_gb300   -- command-line driver (reads a SOFI2D parameter file).
 
 Sources compile in parallel; nvcc cross-compiles without a GPU.
@@ -60,6 +62,8 @@ def build(verbose: bool = False) -> dict:
     gpu_lib = os.path.join(OUT, "libsofigpu.so")
     host_lib = os.path.join(OUT, "libsofihost.so")
     cli = os.path.join(OUT, "sofi2d_gb300")
+    serve_lib = os.path.join(OUT, "libsofiserve.so")
+    serve_src = os.path.join(CSRC, "serve", "sofiserve.c")
     jobs = []
     cu = cuda_objects()
     deps_cu = _deps((".cu", ".cuh", ".h"))
@@ -86,7 +90,10 @@ def build(verbose: bool = False) -> dict:
         if os.path.exists(main):
             _run(["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-fopenmp", "-Wall", "-I", INC, "-o", cli, main, *hs,
                   "-L", OUT, "-lsofigpu", "-Wl,-rpath,$ORIGIN", "-lm"])
-    return {"gpu": gpu_lib, "host": host_lib, "cli": cli}
+    if _newer(serve_lib, [serve_src, gpu_lib, host_lib] + _deps((".h",))):
+        _run(["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-fPIC", "-shared", "-Wall", "-I", INC, "-o", serve_lib,
+              serve_src, "-L", OUT, "-lsofigpu", "-lsofihost", "-Wl,-rpath,$ORIGIN", "-lpthread", "-lm"])
+    return {"gpu": gpu_lib, "host": host_lib, "cli": cli, "serve": serve_lib}
 
 
 if __name__ == "__main__":

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <string>
 #include <vector>
 
@@ -187,6 +188,9 @@ struct sofi_ctx {
     size_t tev_used = 0;
     double t_v_ms = 0, t_s_ms = 0;
     long long t_count = 0;
+    // completion events of the sofi_run calls still in flight (oldest first)
+    std::deque<cudaEvent_t> run_ev;
+    std::vector<cudaEvent_t> ev_free;
 };
 
 namespace {
@@ -601,7 +605,44 @@ int sofi_device_bytes(const sofi_config *cfg, long long *bytes)
     return 0;
 }
 
+int sofi_stream_priority_range(int device, int *least, int *greatest)
+{
+    if (!least || !greatest)
+        return fail(SOFI_E_ARG, "null argument");
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(SOFI_E_NODEV, "no CUDA device available: %s", cudaGetErrorString(e));
+    if (device < 0 || device >= ndev)
+        return fail(SOFI_E_ARG, "device %d out of range (%d devices)", device, ndev);
+    CK(cudaSetDevice(device));
+    CK(cudaDeviceGetStreamPriorityRange(least, greatest));
+    return 0;
+}
+
+int sofi_device_memory(int device, long long *free_bytes, long long *total_bytes)
+{
+    if (!free_bytes || !total_bytes)
+        return fail(SOFI_E_ARG, "null argument");
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(SOFI_E_NODEV, "no CUDA device available: %s", cudaGetErrorString(e));
+    if (device < 0 || device >= ndev)
+        return fail(SOFI_E_ARG, "device %d out of range (%d devices)", device, ndev);
+    CK(cudaSetDevice(device));
+    size_t f = 0, t = 0;
+    CK(cudaMemGetInfo(&f, &t));
+    *free_bytes = (long long)f, *total_bytes = (long long)t;
+    return 0;
+}
+
 int sofi_create(const sofi_config *cfg, int device, sofi_ctx **out)
+{
+    return sofi_create_with_priority(cfg, device, 0, out);
+}
+
+int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, sofi_ctx **out)
 {
     if (!out)
         return fail(SOFI_E_ARG, "null output pointer");
@@ -616,6 +657,11 @@ int sofi_create(const sofi_config *cfg, int device, sofi_ctx **out)
     if (device < 0 || device >= ndev)
         return fail(SOFI_E_ARG, "device %d out of range (%d devices)", device, ndev);
     CK(cudaSetDevice(device));
+    {
+        int least = 0, greatest = 0;
+        CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        priority = priority < greatest ? greatest : (priority > least ? least : priority);
+    }
     sofi_ctx *c = new sofi_ctx();
     c->cfg = *cfg;
     c->device = device;
@@ -628,7 +674,7 @@ int sofi_create(const sofi_config *cfg, int device, sofi_ctx **out)
         c->vrows = (atoi(e) == 2 || atoi(e) == 4) ? atoi(e) : 1;
     if (const char *e = getenv("SOFI_MARCH_ROWS"))
         c->march_sy = atoi(e) > 0 ? atoi(e) : c->march_sy;
-    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    e = cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, priority);
     if (e != cudaSuccess) {
         delete c;
         return fail(SOFI_E_CUDA, "stream creation: %s", cudaGetErrorString(e));
@@ -743,6 +789,10 @@ int sofi_destroy(sofi_ctx *c)
         cudaStreamDestroy(c->stream);
     }
     for (auto e : c->tev)
+        cudaEventDestroy(e);
+    for (auto e : c->run_ev)
+        cudaEventDestroy(e);
+    for (auto e : c->ev_free)
         cudaEventDestroy(e);
     if (c->graph_exec)
         cudaGraphExecDestroy(c->graph_exec);
@@ -974,6 +1024,33 @@ int sofi_run(sofi_ctx *c, int nsteps)
     CK(cudaEventRecord(c->ev1, c->stream));
     CK(cudaGetLastError());
     c->run_pending = true;
+    cudaEvent_t done;
+    if (c->ev_free.empty()) {
+        CK(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+    } else {
+        done = c->ev_free.back();
+        c->ev_free.pop_back();
+    }
+    c->run_ev.push_back(done);
+    CK(cudaEventRecord(done, c->stream));
+    return 0;
+}
+
+int sofi_pending_runs(sofi_ctx *c, int *pending)
+{
+    if (!c || !pending)
+        return fail(SOFI_E_ARG, "null argument");
+    CK(cudaSetDevice(c->device));
+    while (!c->run_ev.empty()) {
+        cudaError_t e = cudaEventQuery(c->run_ev.front());
+        if (e == cudaErrorNotReady)
+            break;
+        if (e != cudaSuccess)
+            return fail(SOFI_E_CUDA, "run completion: %s", cudaGetErrorString(e));
+        c->ev_free.push_back(c->run_ev.front());
+        c->run_ev.pop_front();
+    }
+    *pending = (int)c->run_ev.size();
     return 0;
 }
 

@@ -13,7 +13,7 @@ benchmark configurations with their shapes, sizes and value distributions:
       Ricker 15 Hz vertical force; 1000 receivers
   c3  TTI elastic, 2048 x 2048, DH 2.5 m, DT 2.0e-4 s, NT 4000, FD6, CPML 20;
       Vp 2000-4000, Vs = Vp/1.8, rho 2000-2600, eps 0-0.25, delta -0.1-0.15,
-      tilt 0-45 deg smoothed over 20 cells; explosive Ricker 20 Hz; 512 receivers
+      tilt 0-45 deg, each field smoothed by a Gaussian of sigma 20 cells; explosive Ricker 20 Hz; 512 receivers
   c4  64 shots on the c1 layered model enlarged to 2000 x 1000 with c2's Q field
       and L = 3, NT 4000, explosive sources spread across the surface
 Values are drawn from numpy's PCG64 with seed 1000 + config number.
@@ -25,12 +25,16 @@ import math
 import numpy as np
 
 
-def smooth_field(rng, nx, ny, corr_cells, lo, hi):
-    """Gaussian-correlated random field scaled to [lo, hi], shape [NX][NY]."""
+def smooth_field(rng, nx, ny, corr_cells, lo, hi, sigma=None):
+    """Gaussian-correlated random field scaled to [lo, hi], shape [NX][NY].
+
+    The white noise is convolved with a Gaussian of standard deviation
+    ``sigma`` cells, or corr_cells / 2 pi cells when ``sigma`` is None.
+    """
     w = rng.standard_normal((nx, ny))
     kx = np.fft.fftfreq(nx)[:, None]
     ky = np.fft.rfftfreq(ny)[None, :]
-    s = corr_cells / (2.0 * math.pi)
+    s = corr_cells / (2.0 * math.pi) if sigma is None else float(sigma)
     g = np.exp(-0.5 * ((kx * 2 * math.pi * s) ** 2 + (ky * 2 * math.pi * s) ** 2))
     f = np.fft.irfft2(np.fft.rfft2(w) * g, s=(nx, ny))
     f = (f - f.min()) / max(f.max() - f.min(), 1e-30)
@@ -88,14 +92,13 @@ def workload(name: str) -> dict:
     elif name == "c3":
         rng = np.random.default_rng(1003)
         nx = ny = 2048
-        vp = smooth_field(rng, nx, ny, 20, 2000.0, 4000.0)
+        # every field is white noise smoothed by a Gaussian of sigma 20 cells
+        vp = smooth_field(rng, nx, ny, 0, 2000.0, 4000.0, sigma=20)
         vs = (vp / 1.8).astype(np.float32)
-        rho = smooth_field(rng, nx, ny, 20, 2000.0, 2600.0)
-        mats = dict(vp=vp, vs=vs, rho=rho, epsilon=smooth_field(rng, nx, ny, 20, 0.0, 0.25),
-                    delta=smooth_field(rng, nx, ny, 20, -0.1, 0.15), theta=smooth_field(rng, nx, ny, 20, 0.0, 45.0))
-        # DT 2.5e-4 passes the reference's CFL check but the staggered TTI update
-        # diverges inside this model after ~1400 steps (the reference's own
-        # algorithm does the same); 2.0e-4 is stable over the whole run
+        rho = smooth_field(rng, nx, ny, 0, 2000.0, 2600.0, sigma=20)
+        mats = dict(vp=vp, vs=vs, rho=rho, epsilon=smooth_field(rng, nx, ny, 0, 0.0, 0.25, sigma=20),
+                    delta=smooth_field(rng, nx, ny, 0, -0.1, 0.15, sigma=20),
+                    theta=smooth_field(rng, nx, ny, 0, 0.0, 45.0, sigma=20))
         par = dict(weq=6, nx=nx, ny=ny, dh=2.5, dt=2.0e-4, nt=4000, fdorder=6, maxrelerror=1, fw=20, abs_type=1,
                    npower=4.0, k_max_cpml=1.0, vppml=5000.0, fpml=20.0, seismo=1, ndt=1)
         src = _srcpos([(2560.0, 30.0)], 2.5, 20.0, 1)
@@ -138,3 +141,60 @@ def bytes_per_cell(weq: int, L: int) -> dict:
     if weq == 5:
         return {"update_v": 36, "update_s": 8 + 24 + 24 * L + 32, "step": 8 * (5 + 3 * L) + 4 * 10}
     return {"update_v": 36, "update_s": 8 + 24 + 24 * L + 64, "step": 8 * (5 + 3 * L) + 4 * 18}
+
+
+def request_stream(n: int, seed: int = 1005, rate: float | None = None, max_cells: int = 4096 * 2048,
+                   nt_range=(1000, 6000), nx_range=(256, 4096), ny_range=(256, 2048)) -> list[dict]:
+    """c5: a seeded stream of independent forward-modelling requests.
+
+    Grid sizes log-uniform from 256 x 256 to 4096 x 2048 (NX and NY drawn
+    separately, multiples of 16, capped at ``max_cells``), NT uniform in
+    ``nt_range``, FDORDER 4 or 8, elastic or viscoelastic (L = 3, Q 20-100 per
+    layer), three layers with 2 % perturbation, Ricker 10-40 Hz explosive
+    source 5 cells below the CPML frame and up to 128 receivers on that row.
+    DT is half the stability bound of the Holberg stencil for the largest
+    velocity. Arrival offsets are Poisson with ``rate`` per second, or all 0.
+    The ranges can be narrowed (tests use small grids and few steps).
+    """
+    from . import host as H
+
+    rng = np.random.default_rng(seed)
+    out, t = [], 0.0
+    for k in range(n):
+        nx = int(round(2.0 ** rng.uniform(math.log2(nx_range[0]), math.log2(nx_range[1])) / 16)) * 16
+        ny = int(round(2.0 ** rng.uniform(math.log2(ny_range[0]), math.log2(ny_range[1])) / 16)) * 16
+        while nx * ny > max_cells:
+            nx, ny = nx // 2, ny
+        nt = int(rng.integers(nt_range[0], nt_range[1] + 1))
+        fd = int(rng.choice([4, 8]))
+        visco = bool(rng.integers(0, 2))
+        fc = float(rng.uniform(10.0, 40.0))
+        dh = 2.0
+        vlay = np.sort(rng.uniform(1500.0, 4500.0, 3))
+        b1, b2 = sorted(rng.integers(ny // 5, 4 * ny // 5, 2).tolist())
+        y = np.arange(ny)
+        layer = np.where(y < b1, 0, np.where(y < b2, 1, 2))
+        vp = (vlay[layer][None, :] * (1.0 + 0.02 * rng.standard_normal((nx, ny)))).astype(np.float32)
+        vs = (vp / 1.73).astype(np.float32)
+        rho = (310.0 * vp.astype(np.float64) ** 0.25).astype(np.float32)
+        mats = dict(vp=vp, vs=vs, rho=rho)
+        fw = 20
+        hc = H.holberg(fd, 1)
+        vmax = float(vp.max()) * (1.1 if visco else 1.0)  # unrelaxed velocities exceed vp
+        dt = float(np.float32(0.5 * dh / (math.sqrt(2.0) * float(np.abs(hc).sum()) * vmax)))
+        par = dict(weq=3 if visco else 2, nx=nx, ny=ny, dh=dh, dt=dt, nt=nt, time=nt * dt, fdorder=fd,
+                   maxrelerror=1, fw=fw, abs_type=1, npower=4.0, k_max_cpml=1.0, vppml=float(vp.max()), fpml=fc,
+                   source_shape=1, seismo=1, ndt=1, L=0)
+        if visco:
+            q = np.array(rng.uniform(20.0, 100.0, 3))[layer][None, :].repeat(nx, 0).astype(np.float32)
+            mats.update(qp=q, qs=q)
+            par.update(L=3, f_ref=fc, fl=[fc / 3.0, fc, 3.0 * fc])
+        src = _srcpos([((nx // 2) * dh, (fw + 5) * dh)], dh, fc, 1)
+        ntr = max(1, min(128, nx - 2 * fw))
+        rix = np.linspace(fw + 1, nx - fw, ntr).astype(np.int32)
+        riy = np.full(ntr, fw + 6, np.int32)
+        if rate:
+            t += float(rng.exponential(1.0 / rate))
+        out.append(dict(par=par, mats=mats, src=src, rec=(rix, riy), arrival=t if rate else 0.0,
+                        cells=nx * ny, cell_updates=float(nx) * ny * nt))
+    return out

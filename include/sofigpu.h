@@ -42,6 +42,7 @@ extern "C" {
 #define SOFI_E_NOMEM 4     /* device allocation failed */
 #define SOFI_E_UNSTABLE 5  /* NaN at the probe cell: reference time_loop.c:44-47 */
 #define SOFI_E_NODEV 6     /* no CUDA device / driver */
+#define SOFI_E_BUSY 7      /* device work of the context still in flight */
 
 /* wave equations: reference src/enums.h:22-31 */
 #define SOFI_EL_ISO 2
@@ -89,6 +90,14 @@ typedef struct {
 /* Check the configuration, select `device`, allocate every device array the
  * time loop needs (wavefields zeroed) and create the context's stream. */
 int sofi_create(const sofi_config *cfg, int device, sofi_ctx **out);
+/* sofi_create with a stream priority (CUDA convention: lower is more urgent;
+ * clamped to the device's range). The block scheduler prefers the work of
+ * higher-priority streams when several contexts share the GPU. */
+int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, sofi_ctx **out);
+/* The device's stream priorities: least urgent and most urgent. */
+int sofi_stream_priority_range(int device, int *least, int *greatest);
+/* Free and total device memory in bytes (cudaMemGetInfo on `device`). */
+int sofi_device_memory(int device, long long *free_bytes, long long *total_bytes);
 int sofi_destroy(sofi_ctx *ctx);
 const char *sofi_last_error(void);
 int sofi_abi_version(void);
@@ -149,6 +158,9 @@ int sofi_reset(sofi_ctx *ctx, int shot);
 int sofi_run(sofi_ctx *ctx, int nsteps);
 /* Wait for the context's stream; reports a pending instability. */
 int sofi_synchronize(sofi_ctx *ctx);
+/* Number of sofi_run calls whose device work has not finished yet (never
+ * blocks): a host loop keeps a few runs in flight per context with it. */
+int sofi_pending_runs(sofi_ctx *ctx, int *pending);
 int sofi_current_step(sofi_ctx *ctx, int *step);
 
 /* ---- outputs ----------------------------------------------------------- */
