@@ -50,6 +50,11 @@ struct Geo {
     int shot_fast;          // block index: shot varies fastest (model tiles shared in L2)
     int seismo, ndt;        // sampling (gv->SEISMO, gv->NDT)
     int *step_ctr;          // device: time steps completed; the velocity kernel advances it
+    // TTI CPML memory of the velocity derivatives in two buffers (psi_pp = 1):
+    // step n reads buffer (n - 1) & 1 and writes buffer n & 1; the second
+    // buffer starts psi_xsz / psi_ysz floats after the first
+    int psi_pp;
+    long long psi_xsz, psi_ysz;
     float dt, dh, dtdh, dhi, dthalbe;
     float hc[7];
 };
@@ -183,35 +188,57 @@ __device__ __forceinline__ int region(const Geo &G, int i, int j)
     return 4 + (xr - 1) * 2 + yr;
 }
 
-// CPML stretch of the four velocity derivatives of one cell, updating the
-// memory variables (cpml_update.c:30-46 with the drivers' h rules).
-__device__ __forceinline__ void cpml_s(const Geo &G, const Wave &W, const Model &M, int s, int i, int j, int xr,
-                                       int yr, float &vxx, float &vyx, float &vxy, float &vyy, bool write)
+// CPML stretch of the four velocity derivatives of one cell (cpml_update.c:30-46
+// with the drivers' h rules): memory read from R, updated memory written to Wr
+// when `write` is set.
+__device__ __forceinline__ void cpml_s2(const Geo &G, const Wave &R, const Wave &Wr, const Model &M, int s, int i,
+                                        int j, int xr, int yr, float &vxx, float &vyx, float &vxy, float &vyy,
+                                        bool write)
 {
     if (xr) {
         int h = xr == 1 ? i : i - G.nx + G.fw2;
         long long q = ((long long)s * G.ny + (j - 1)) * G.fw2 + (h - 1);
-        float p1 = M.b_x[h - 1] * W.psi_vxx[q] + M.a_x[h - 1] * vxx;
+        float p1 = M.b_x[h - 1] * R.psi_vxx[q] + M.a_x[h - 1] * vxx;
         vxx = vxx / M.K_x[h - 1] + p1;
-        float p2 = M.b_x_half[h - 1] * W.psi_vyx[q] + M.a_x_half[h - 1] * vyx;
+        float p2 = M.b_x_half[h - 1] * R.psi_vyx[q] + M.a_x_half[h - 1] * vyx;
         vyx = vyx / M.K_x_half[h - 1] + p2;
         if (write) {
-            W.psi_vxx[q] = p1;
-            W.psi_vyx[q] = p2;
+            Wr.psi_vxx[q] = p1;
+            Wr.psi_vyx[q] = p2;
         }
     }
     if (yr) {
         int h = yr == 1 ? j : j - G.ny + G.fw2;
         long long q = ((long long)s * G.fw2 + (h - 1)) * G.nx + (i - 1);
-        float p1 = M.b_y[h - 1] * W.psi_vyy[q] + M.a_y[h - 1] * vyy;
+        float p1 = M.b_y[h - 1] * R.psi_vyy[q] + M.a_y[h - 1] * vyy;
         vyy = vyy / M.K_y[h - 1] + p1;
-        float p2 = M.b_y_half[h - 1] * W.psi_vxy[q] + M.a_y_half[h - 1] * vxy;
+        float p2 = M.b_y_half[h - 1] * R.psi_vxy[q] + M.a_y_half[h - 1] * vxy;
         vxy = vxy / M.K_y_half[h - 1] + p2;
         if (write) {
-            W.psi_vyy[q] = p1;
-            W.psi_vxy[q] = p2;
+            Wr.psi_vyy[q] = p1;
+            Wr.psi_vxy[q] = p2;
         }
     }
+}
+
+// The same with the memory updated in place.
+__device__ __forceinline__ void cpml_s(const Geo &G, const Wave &W, const Model &M, int s, int i, int j, int xr,
+                                       int yr, float &vxx, float &vyx, float &vxy, float &vyy, bool write)
+{
+    cpml_s2(G, W, W, M, s, i, j, xr, yr, vxx, vyx, vxy, vyy, write);
+}
+
+// Point W's velocity-derivative CPML memory at the buffer this step writes
+// (previous = false) or at the one the previous step wrote (previous = true).
+__device__ __forceinline__ void psi_buffers(const Geo &G, Wave &W, bool previous)
+{
+    if (!G.psi_pp)
+        return;
+    const long long b = (*G.step_ctr & 1) ^ (previous ? 1 : 0);
+    W.psi_vxx += b * G.psi_xsz;
+    W.psi_vyx += b * G.psi_xsz;
+    W.psi_vyy += b * G.psi_ysz;
+    W.psi_vxy += b * G.psi_ysz;
 }
 
 }  // namespace sofi

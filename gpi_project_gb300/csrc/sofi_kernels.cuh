@@ -40,7 +40,7 @@ __global__ void k_force_src(Geo G, Wave W, Model M, Acq A)
 // 2ND * R); 32-bit offsets inside a shot's fields, read-only data through the
 // non-coherent cache. Force sources are added by k_force_src beforehand.
 template <int ND, int R>
-__global__ void __launch_bounds__(BX *BY) k_update_v(Geo G, Wave W, Model M)
+__global__ void __launch_bounds__(BX *BY, R == 1 ? 8 : 1) k_update_v(Geo G, Wave W, Model M)
 {
     int bx, s;
     block_xs(G, bx, s);
@@ -62,13 +62,16 @@ __global__ void __launch_bounds__(BX *BY) k_update_v(Geo G, Wave W, Model M)
     float *__restrict__ vy = W.vy + so;
     const float *hc = G.hc;
     // windows: wxy[k] = sxy(jb - ND + k), wyy[k] = syy(jb - ND + 1 + k); rows past
-    // NY + ND are read by no cell of the grid and are not loaded
+    // NY + ND are read by no cell of the grid and are not loaded (one row per
+    // thread: the stencil reads the rows directly)
     constexpr int NW = R + 2 * ND - 1;
     float wxy[NW], wyy[NW];
+    if (R > 1) {
 #pragma unroll
-    for (int k = 0; k < NW; k++) {
-        wxy[k] = (jb - ND + k <= G.ny + ND) ? __ldg(sxy + ob + (k - ND) * P) : 0.f;
-        wyy[k] = (jb - ND + 1 + k <= G.ny + ND) ? __ldg(syy + ob + (k - ND + 1) * P) : 0.f;
+        for (int k = 0; k < NW; k++) {
+            wxy[k] = (jb - ND + k <= G.ny + ND) ? __ldg(sxy + ob + (k - ND) * P) : 0.f;
+            wyy[k] = (jb - ND + 1 + k <= G.ny + ND) ? __ldg(syy + ob + (k - ND + 1) * P) : 0.f;
+        }
     }
     const int xr = xside(G, i);
 #pragma unroll
@@ -79,16 +82,21 @@ __global__ void __launch_bounds__(BX *BY) k_update_v(Geo G, Wave W, Model M)
         const int o = ob + r * P;
         const float ovx = vx[o], ovy = vy[o];
         const float rip = __ldg(M.prip + mo + o), rjp = __ldg(M.prjp + mo + o);
-        float sxx_x = hc[1] * (__ldg(sxx + o + 1) - __ldg(sxx + o));
-        float sxy_x = hc[1] * (__ldg(sxy + o) - __ldg(sxy + o - 1));
-        float sxy_y = hc[1] * (wxy[ND + r] - wxy[ND + r - 1]);
-        float syy_y = hc[1] * (wyy[ND + r] - wyy[ND + r - 1]);
+        float sxx_x, sxy_x, sxy_y, syy_y;
+        if (R == 1) {
+            op_v<ND>(sxx, syy, sxy, o, P, hc, sxx_x, sxy_x, sxy_y, syy_y);
+        } else {
+            sxx_x = hc[1] * (__ldg(sxx + o + 1) - __ldg(sxx + o));
+            sxy_x = hc[1] * (__ldg(sxy + o) - __ldg(sxy + o - 1));
+            sxy_y = hc[1] * (wxy[ND + r] - wxy[ND + r - 1]);
+            syy_y = hc[1] * (wyy[ND + r] - wyy[ND + r - 1]);
 #pragma unroll
-        for (int m = 2; m <= ND; m++) {
-            sxx_x += hc[m] * (__ldg(sxx + o + m) - __ldg(sxx + o - m + 1));
-            sxy_x += hc[m] * (__ldg(sxy + o + m - 1) - __ldg(sxy + o - m));
-            sxy_y += hc[m] * (wxy[ND + r + m - 1] - wxy[ND + r - m]);
-            syy_y += hc[m] * (wyy[ND + r - 1 + m] - wyy[ND + r - m]);
+            for (int m = 2; m <= ND; m++) {
+                sxx_x += hc[m] * (__ldg(sxx + o + m) - __ldg(sxx + o - m + 1));
+                sxy_x += hc[m] * (__ldg(sxy + o + m - 1) - __ldg(sxy + o - m));
+                sxy_y += hc[m] * (wxy[ND + r + m - 1] - wxy[ND + r - m]);
+                syy_y += hc[m] * (wyy[ND + r - 1 + m] - wyy[ND + r - m]);
+            }
         }
         const int yr = yside(G, j);
         if (G.abs_type == 1) {
@@ -122,6 +130,163 @@ __global__ void __launch_bounds__(BX *BY) k_update_v(Geo G, Wave W, Model M)
         }
         vx[o] = nvx;
         vy[o] = nvy;
+    }
+}
+
+// The velocity update with VW adjacent cells per thread (VW = 2 or 4; columns
+// i .. i+VW-1, i = 1 mod VW): every field is read with 8- or 16-byte loads, the
+// x stencils from 2K+1 vectors of the row (K = ceil(ND/VW)) and the y stencils
+// one vector per row, a fraction of the load instructions of one cell per
+// thread. Same arithmetic, per cell and term by term, as k_update_v.
+// Reads reach columns up to i + VW(K+1) - 1 + HX - 1 of the padded row
+// (< pitch for VW = 2; for VW = 4 possibly the next row's first columns); the
+// values past column NX + ND only feed cells past NX, which are never stored.
+// Rows j - ND .. j + ND stay inside the HY ghost rows.
+template <int VW>
+__device__ __forceinline__ void ldv(const float *p, float *out)
+{
+    if (VW == 4) {
+        const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+        out[0] = a.x, out[1] = a.y, out[2] = a.z, out[3] = a.w;
+    } else {
+        const float2 a = __ldg(reinterpret_cast<const float2 *>(p));
+        out[0] = a.x, out[1] = a.y;
+    }
+}
+
+template <int VW>
+__device__ __forceinline__ void ldv_rw(const float *p, float *out)  // arrays this kernel writes
+{
+    if (VW == 4) {
+        const float4 a = *reinterpret_cast<const float4 *>(p);
+        out[0] = a.x, out[1] = a.y, out[2] = a.z, out[3] = a.w;
+    } else {
+        const float2 a = *reinterpret_cast<const float2 *>(p);
+        out[0] = a.x, out[1] = a.y;
+    }
+}
+
+template <int VW>
+__device__ __forceinline__ void stv(float *p, const float *v)
+{
+    if (VW == 4)
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    else
+        *reinterpret_cast<float2 *>(p) = make_float2(v[0], v[1]);
+}
+
+template <int ND, int VW>
+__global__ void __launch_bounds__(BX *BY) k_update_vw(Geo G, Wave W, Model M)
+{
+    constexpr int K = (ND + VW - 1) / VW;
+    constexpr int NXS = VW * (2 * K + 1);  // stencil row: columns i - VW K .. i + VW K + VW - 1
+    int bx, s;
+    block_xs(G, bx, s);
+    const int i = (bx * BX + threadIdx.x) * VW + 1;
+    const int j = blockIdx.y * BY + threadIdx.y + 1;
+    if (G.step_ctr && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+        *G.step_ctr += 1;
+    if (i > G.nx || j > G.ny)
+        return;
+    const int P = G.pitch;
+    const int o = (j - 1 + HY) * P + (i - 1 + HX);  // VW-aligned: HX = 8, P % 32 == 0, i - 1 = 0 mod VW
+    const long long so = (long long)s * G.fsz, mo = moff(G, s);
+    const float *__restrict__ sxx = W.sxx + so;
+    const float *__restrict__ syy = W.syy + so;
+    const float *__restrict__ sxy = W.sxy + so;
+    const float *hc = G.hc;
+    float sxx_x[VW], sxy_x[VW], sxy_y[VW], syy_y[VW];
+    {
+        float X[NXS], Y[NXS];  // X[k] = sxx(j, i - VW K + k), Y[k] = sxy(j, i - VW K + k)
+#pragma unroll
+        for (int q = 0; q < 2 * K + 1; q++) {
+            ldv<VW>(sxx + o + VW * (q - K), X + VW * q);
+            ldv<VW>(sxy + o + VW * (q - K), Y + VW * q);
+        }
+        constexpr int C = VW * K;  // index of column i
+#pragma unroll
+        for (int c = 0; c < VW; c++) {
+            sxx_x[c] = hc[1] * (X[C + c + 1] - X[C + c]);
+            sxy_x[c] = hc[1] * (Y[C + c] - Y[C + c - 1]);
+#pragma unroll
+            for (int m = 2; m <= ND; m++) {
+                sxx_x[c] += hc[m] * (X[C + c + m] - X[C + c - m + 1]);
+                sxy_x[c] += hc[m] * (Y[C + c + m - 1] - Y[C + c - m]);
+            }
+        }
+    }
+    {
+        // y stencils: sxy rows j - ND .. j + ND - 1, syy rows j - ND + 1 .. j + ND
+        float a1[VW], a0[VW], b1[VW], b0[VW];
+        ldv<VW>(sxy + o, a1), ldv<VW>(sxy + o - P, a0);
+        ldv<VW>(syy + o + P, b1), ldv<VW>(syy + o, b0);
+#pragma unroll
+        for (int c = 0; c < VW; c++) {
+            sxy_y[c] = hc[1] * (a1[c] - a0[c]);
+            syy_y[c] = hc[1] * (b1[c] - b0[c]);
+        }
+#pragma unroll
+        for (int m = 2; m <= ND; m++) {
+            ldv<VW>(sxy + o + (m - 1) * P, a1), ldv<VW>(sxy + o - m * P, a0);
+            ldv<VW>(syy + o + m * P, b1), ldv<VW>(syy + o - (m - 1) * P, b0);
+#pragma unroll
+            for (int c = 0; c < VW; c++) {
+                sxy_y[c] += hc[m] * (a1[c] - a0[c]);
+                syy_y[c] += hc[m] * (b1[c] - b0[c]);
+            }
+        }
+    }
+    float *__restrict__ vx = W.vx + so;
+    float *__restrict__ vy = W.vy + so;
+    float ox[VW], oy[VW], rp[VW], rq[VW];
+    ldv_rw<VW>(vx + o, ox), ldv_rw<VW>(vy + o, oy);
+    ldv<VW>(M.prip + mo + o, rp), ldv<VW>(M.prjp + mo + o, rq);
+    const int yr = yside(G, j);
+    const bool xframe = i <= G.gx2 || i + VW - 1 > G.gx3;  // any of the cells in a left/right frame
+    float nvx[VW], nvy[VW];
+#pragma unroll
+    for (int c = 0; c < VW; c++) {
+        const int ic = i + c;
+        float fx = sxx_x[c], fxy = sxy_x[c], fyx = sxy_y[c], fy = syy_y[c];
+        const int xr = xframe ? xside(G, ic) : 0;
+        if (G.abs_type == 1 && ic <= G.nx) {
+            if (xr) {
+                int h = xr == 1 ? ic : ic - G.nx + G.fw2;
+                long long q = ((long long)s * G.ny + (j - 1)) * G.fw2 + (h - 1);
+                float ps = M.b_x_half[h - 1] * W.psi_sxx_x[q] + M.a_x_half[h - 1] * fx;
+                W.psi_sxx_x[q] = ps;
+                fx = fx / M.K_x_half[h - 1] + ps;
+                float py = M.b_x[h - 1] * W.psi_sxy_x[q] + M.a_x[h - 1] * fxy;
+                W.psi_sxy_x[q] = py;
+                fxy = fxy / M.K_x[h - 1] + py;
+            }
+            if (yr) {
+                int h = yr == 1 ? j : j - G.ny + G.fw2;
+                long long q = ((long long)s * G.fw2 + (h - 1)) * G.nx + (ic - 1);
+                float ps = M.b_y_half[h - 1] * W.psi_syy_y[q] + M.a_y_half[h - 1] * fy;
+                W.psi_syy_y[q] = ps;
+                fy = fy / M.K_y_half[h - 1] + ps;
+                float py = M.b_y[h - 1] * W.psi_sxy_y[q] + M.a_y[h - 1] * fyx;
+                W.psi_sxy_y[q] = py;
+                fyx = fyx / M.K_y[h - 1] + py;
+            }
+        }
+        nvx[c] = ox[c] + (fx + fyx) * G.dtdh * rp[c];
+        nvy[c] = oy[c] + (fxy + fy) * G.dtdh * rq[c];
+        if (G.abs_type == 2 && (xr | yr)) {
+            float a = __ldg(M.absorb + mo + o + c);
+            nvx[c] *= a;
+            nvy[c] *= a;
+        }
+    }
+    if (i + VW - 1 <= G.nx) {
+        stv<VW>(vx + o, nvx);
+        stv<VW>(vy + o, nvy);
+    } else {
+#pragma unroll
+        for (int c = 0; c < VW; c++)
+            if (i + c <= G.nx)
+                vx[o + c] = nvx[c], vy[o + c] = nvy[c];
     }
 }
 
@@ -313,49 +478,22 @@ __device__ __forceinline__ float tti_d(const Geo &G, const float *dr, const floa
     return (rn <= rc) ? dc[k * G.fsz + o] : dr[k * G.fsz + o];
 }
 
-// wavefield_update_s_el_tti.c:27-52 / wavefield_update_s_visc_TTI.c:27-84 with
-// the TTI CPML driver's skipped outer cells (update_s_elastic_TTI_PML.c).
+// The stress / memory-variable arithmetic of wavefield_update_s_el_tti.c:27-52 and
+// wavefield_update_s_visc_TTI.c:27-84 for cell o, given the derivatives at the
+// cell and the 4-point averages the reference forms from its neighbours.
 template <bool VISCO>
-__global__ void __launch_bounds__(BX *BY) k_update_s_tti(Geo G, Wave W, Model M)
+__device__ __forceinline__ void tti_update(const Geo &G, const Wave &W, const Model &M, int s, long long o, int xr,
+                                           int yr, float vxx, float vyy, float vxxipjp, float vyyipjp, float vyx0,
+                                           float vxy0, float vyxij, float vxyij)
 {
-    int bx, s;
-    block_xs(G, bx, s);
-    int i = bx * BX + threadIdx.x + 1;
-    int j = blockIdx.y * BY + threadIdx.y + 1;
-    if (i > G.nx || j > G.ny)
-        return;
-    int xr = xside(G, i), yr = yside(G, j);
-    if (G.abs_type == 1) {
-        if ((xr == 1 && i < 3) || (xr == 2 && i > G.nx - 2) || (yr == 1 && j < 3) || (yr == 2 && j > G.ny - 2))
-            return;
-    }
-    long long o = cell(G, j, i);
-    long long so = (long long)s * G.fsz, mo = moff(G, s);
-    const float *dr = W.draw + 4 * so, *dc = W.dcor + 4 * so;
-    int rc = (G.abs_type == 1) ? region(G, i, j) : 0;
-    float vxx = tti_d(G, dr, dc, 0, j, i, rc), vyy = tti_d(G, dr, dc, 1, j, i, rc);
-    float vxxipjp = 0.25f * (vxx + tti_d(G, dr, dc, 0, j + 1, i, rc) + tti_d(G, dr, dc, 0, j, i + 1, rc) +
-                             tti_d(G, dr, dc, 0, j + 1, i + 1, rc));
-    float vyyipjp = 0.25f * (vyy + tti_d(G, dr, dc, 1, j + 1, i, rc) + tti_d(G, dr, dc, 1, j, i + 1, rc) +
-                             tti_d(G, dr, dc, 1, j + 1, i + 1, rc));
-    float vyx0 = tti_d(G, dr, dc, 2, j, i, rc), vxy0 = tti_d(G, dr, dc, 3, j, i, rc);
-    float vyxij = 0.25f * (vyx0 + tti_d(G, dr, dc, 2, j - 1, i, rc) + tti_d(G, dr, dc, 2, j, i - 1, rc) +
-                           tti_d(G, dr, dc, 2, j - 1, i - 1, rc));
-    float vxyij = 0.25f * (vxy0 + tti_d(G, dr, dc, 3, j - 1, i, rc) + tti_d(G, dr, dc, 3, j, i - 1, rc) +
-                           tti_d(G, dr, dc, 3, j - 1, i - 1, rc));
+    const long long so = (long long)s * G.fsz, mo = moff(G, s);
     float vij = vyxij + vxyij;
     float v = vxy0 + vyx0;
-    float u1, u2, u3;
-    if (!VISCO) {
-        u1 = __ldg(M.c55ipjp + mo + o) * v + __ldg(M.c15ipjp + mo + o) * vxxipjp +
-             __ldg(M.c35ipjp + mo + o) * vyyipjp;
-        u2 = __ldg(M.c11 + mo + o) * vxx + __ldg(M.c13 + mo + o) * vyy + __ldg(M.c15 + mo + o) * vij;
-        u3 = __ldg(M.c13 + mo + o) * vxx + __ldg(M.c33 + mo + o) * vyy + __ldg(M.c35 + mo + o) * vij;
-    } else {
-        u1 = __ldg(M.c55ipjp + mo + o) * v + __ldg(M.c15ipjp + mo + o) * vxxipjp +
-             __ldg(M.c35ipjp + mo + o) * vyyipjp;
-        u2 = __ldg(M.c11 + mo + o) * vxx + __ldg(M.c13 + mo + o) * vyy + __ldg(M.c15 + mo + o) * vij;
-        u3 = __ldg(M.c13 + mo + o) * vxx + __ldg(M.c33 + mo + o) * vyy + __ldg(M.c35 + mo + o) * vij;
+    float u1 = __ldg(M.c55ipjp + mo + o) * v + __ldg(M.c15ipjp + mo + o) * vxxipjp +
+               __ldg(M.c35ipjp + mo + o) * vyyipjp;
+    float u2 = __ldg(M.c11 + mo + o) * vxx + __ldg(M.c13 + mo + o) * vyy + __ldg(M.c15 + mo + o) * vij;
+    float u3 = __ldg(M.c13 + mo + o) * vxx + __ldg(M.c33 + mo + o) * vyy + __ldg(M.c35 + mo + o) * vij;
+    if (VISCO) {
         float b55 = __ldg(M.c55ipjpb + mo + o), b15i = __ldg(M.c15ipjpb + mo + o), b35i = __ldg(M.c35ipjpb + mo + o);
         float b11 = __ldg(M.c11b + mo + o), b13 = __ldg(M.c13b + mo + o), b33 = __ldg(M.c33b + mo + o);
         float b15 = __ldg(M.c15b + mo + o), b35 = __ldg(M.c35b + mo + o);
@@ -383,6 +521,159 @@ __global__ void __launch_bounds__(BX *BY) k_update_s_tti(Geo G, Wave W, Model M)
     W.sxy[so + o] = nxy;
     W.sxx[so + o] = nxx;
     W.syy[so + o] = nyy;
+}
+
+// TTI CPML driver: cells the reference's update_s_*_TTI_PML.c loops skip
+// (two outer cells of each frame side, update_s_elastic_TTI_PML.c:44,58,69,82).
+__device__ __forceinline__ bool tti_pml_skipped(const Geo &G, int i, int j, int xr, int yr)
+{
+    return G.abs_type == 1 &&
+           ((xr == 1 && i < 3) || (xr == 2 && i > G.nx - 2) || (yr == 1 && j < 3) || (yr == 2 && j > G.ny - 2));
+}
+
+// The stress update from the derivative fields k_tti_deriv stored.
+template <bool VISCO>
+__global__ void __launch_bounds__(BX *BY) k_update_s_tti(Geo G, Wave W, Model M)
+{
+    int bx, s;
+    block_xs(G, bx, s);
+    int i = bx * BX + threadIdx.x + 1;
+    int j = blockIdx.y * BY + threadIdx.y + 1;
+    if (i > G.nx || j > G.ny)
+        return;
+    int xr = xside(G, i), yr = yside(G, j);
+    if (tti_pml_skipped(G, i, j, xr, yr))
+        return;
+    long long o = cell(G, j, i);
+    long long so = (long long)s * G.fsz;
+    const float *dr = W.draw + 4 * so, *dc = W.dcor + 4 * so;
+    int rc = (G.abs_type == 1) ? region(G, i, j) : 0;
+    float vxx = tti_d(G, dr, dc, 0, j, i, rc), vyy = tti_d(G, dr, dc, 1, j, i, rc);
+    float vxxipjp = 0.25f * (vxx + tti_d(G, dr, dc, 0, j + 1, i, rc) + tti_d(G, dr, dc, 0, j, i + 1, rc) +
+                             tti_d(G, dr, dc, 0, j + 1, i + 1, rc));
+    float vyyipjp = 0.25f * (vyy + tti_d(G, dr, dc, 1, j + 1, i, rc) + tti_d(G, dr, dc, 1, j, i + 1, rc) +
+                             tti_d(G, dr, dc, 1, j + 1, i + 1, rc));
+    float vyx0 = tti_d(G, dr, dc, 2, j, i, rc), vxy0 = tti_d(G, dr, dc, 3, j, i, rc);
+    float vyxij = 0.25f * (vyx0 + tti_d(G, dr, dc, 2, j - 1, i, rc) + tti_d(G, dr, dc, 2, j, i - 1, rc) +
+                           tti_d(G, dr, dc, 2, j - 1, i - 1, rc));
+    float vxyij = 0.25f * (vxy0 + tti_d(G, dr, dc, 3, j - 1, i, rc) + tti_d(G, dr, dc, 3, j, i - 1, rc) +
+                           tti_d(G, dr, dc, 3, j - 1, i - 1, rc));
+    tti_update<VISCO>(G, W, M, s, o, xr, yr, vxx, vyy, vxxipjp, vyyipjp, vyx0, vxy0, vyxij, vxyij);
+}
+
+// The whole TTI stress half-step in one pass. A block derives the four velocity
+// derivatives of its 32 x 8 tile and of the one-cell ring around it (the cells
+// the 4-point averages reach) into shared memory, raw and CPML-stretched, then
+// updates its tile. A neighbour's derivative is taken stretched or raw by the
+// reference's region order, as tti_d does. Ring cells belong to other blocks,
+// which write their CPML memory: every block reads the memory of the previous
+// step's buffer and only the owner of a cell writes this step's buffer
+// (Geo::psi_pp), so no block sees a value another block has already advanced.
+template <int ND, bool VISCO, bool CPML>
+__global__ void __launch_bounds__(BX *BY) k_tti_fused(Geo G, Wave W, Model M)
+{
+    constexpr int SX = BX + 2, SY = BY + 2, NB = CPML ? 2 : 1;
+    constexpr int RING = 2 * SX + 2 * BY;
+    static_assert(RING <= BX * BY, "ring cells exceed the block");
+    __shared__ float sd[NB][4][SY][SX];  // [raw, stretched][vxx vyy vyx vxy][y][x]
+    int bx, s;
+    block_xs(G, bx, s);
+    const int i0 = bx * BX + 1, j0 = blockIdx.y * BY + 1;
+    const int tid = threadIdx.y * BX + threadIdx.x;
+    const long long so = (long long)s * G.fsz;
+    const float *vx = W.vx + so, *vy = W.vy + so;
+    Wave Wn = W, Wo = W;
+    if (CPML) {
+        psi_buffers(G, Wn, false);
+        psi_buffers(G, Wo, true);
+    }
+    // tile and ring wholly inside the interior region: no stretch, one region,
+    // raw and stretched derivatives coincide (block-uniform)
+    const bool frame = CPML && !(i0 - 1 > G.gx2 && i0 + BX <= G.gx3 && j0 - 1 > G.gy2 && j0 + BY <= G.gy3);
+    // pass 0: the tile (one cell per thread); pass 1: the ring (first RING threads)
+#pragma unroll 1
+    for (int pass = 0; pass < 2; pass++) {
+        int ly, lx;
+        if (pass == 0) {
+            ly = threadIdx.y + 1, lx = threadIdx.x + 1;
+        } else {
+            if (tid >= RING)
+                break;
+            if (tid < SX) {
+                ly = 0, lx = tid;
+            } else if (tid < 2 * SX) {
+                ly = SY - 1, lx = tid - SX;
+            } else {
+                const int t = tid - 2 * SX;
+                ly = 1 + (t >> 1), lx = (t & 1) ? SX - 1 : 0;
+            }
+        }
+        const int jn = j0 - 1 + ly, in = i0 - 1 + lx;
+        float d[4] = {0.f, 0.f, 0.f, 0.f};
+        float c[4];
+        int ic = 0;  // column the derivatives are taken at (0: none, zero)
+        if (jn >= 1 && jn <= G.ny) {
+            if (in >= 1 && in <= G.nx)
+                ic = in;
+            else if (G.boundary) {
+                ic = in < 1 ? in + G.nx : in - G.nx;  // periodic x: the wrapped column, raw
+                if (ic < 1 || ic > G.nx)              // past the ring no cell reads (grids < 32 wide)
+                    ic = 0;
+            }
+        }
+        if (ic)
+            op_s<ND>(vx, vy, cell(G, jn, ic), G.pitch, G.hc, G.dhi, d[0], d[2], d[3], d[1]);
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            c[k] = d[k];
+        if (frame && ic && ic == in) {
+            const int xr = xside(G, in), yr = yside(G, jn);
+            if (xr | yr) {
+                const bool own = pass == 0;
+                if (!(G.el_tti_rb_short && xr == 2 && yr == 2 && jn == G.ny)) {
+                    cpml_s2(G, Wo, Wn, M, s, in, jn, xr, yr, c[0], c[2], c[3], c[1], own);
+                } else if (own) {
+                    // the reference's right-bottom pass stops at NY-1: memory unchanged
+                    const int hx = in - G.nx + G.fw2, hy = jn - G.ny + G.fw2;
+                    const long long qx = ((long long)s * G.ny + (jn - 1)) * G.fw2 + (hx - 1);
+                    const long long qy = ((long long)s * G.fw2 + (hy - 1)) * G.nx + (in - 1);
+                    Wn.psi_vxx[qx] = Wo.psi_vxx[qx], Wn.psi_vyx[qx] = Wo.psi_vyx[qx];
+                    Wn.psi_vyy[qy] = Wo.psi_vyy[qy], Wn.psi_vxy[qy] = Wo.psi_vxy[qy];
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            sd[0][k][ly][lx] = d[k];
+            if (frame)
+                sd[NB - 1][k][ly][lx] = c[k];
+        }
+    }
+    __syncthreads();
+    const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+    if (i > G.nx || j > G.ny)
+        return;
+    const int xr = xside(G, i), yr = yside(G, j);
+    if (tti_pml_skipped(G, i, j, xr, yr))
+        return;
+    const int rc = frame ? region(G, i, j) : 0;
+    const int ty = threadIdx.y + 1, tx = threadIdx.x + 1;
+    // derivative k of neighbour (j + dy, i + dx) as the update of this cell sees it
+    auto D = [&](int k, int dy, int dx) -> float {
+        if (!frame)
+            return sd[0][k][ty + dy][tx + dx];
+        const int jn = j + dy, in = i + dx;
+        if (jn < 1 || jn > G.ny || in < 1 || in > G.nx)
+            return sd[0][k][ty + dy][tx + dx];
+        return region(G, in, jn) <= rc ? sd[NB - 1][k][ty + dy][tx + dx] : sd[0][k][ty + dy][tx + dx];
+    };
+    const float vxx = D(0, 0, 0), vyy = D(1, 0, 0);
+    const float vxxipjp = 0.25f * (vxx + D(0, 1, 0) + D(0, 0, 1) + D(0, 1, 1));
+    const float vyyipjp = 0.25f * (vyy + D(1, 1, 0) + D(1, 0, 1) + D(1, 1, 1));
+    const float vyx0 = D(2, 0, 0), vxy0 = D(3, 0, 0);
+    const float vyxij = 0.25f * (vyx0 + D(2, -1, 0) + D(2, 0, -1) + D(2, -1, -1));
+    const float vxyij = 0.25f * (vxy0 + D(3, -1, 0) + D(3, 0, -1) + D(3, -1, -1));
+    tti_update<VISCO>(G, W, M, s, cell(G, j, i), xr, yr, vxx, vyy, vxxipjp, vyyipjp, vyx0, vxy0, vyxij, vxyij);
 }
 
 // ------------------------------------------------ after the stress update
@@ -497,7 +788,8 @@ __device__ __forceinline__ void post_surface(const Geo &G, const Wave &W, const 
 
 // div / curl of seismo_ssg.c:43-47 for receiver k: the derivatives as the
 // stress update left them (CPML-stretched in the frame; psi already holds this
-// step's value, so the stretched derivative is d / K + psi).
+// step's value, so the stretched derivative is d / K + psi). W's CPML memory
+// must point at the buffer this step wrote.
 template <int ND, bool TTIK>
 __device__ __forceinline__ void sample_div_curl(const Geo &G, const Wave &W, const Model &M, const Acq &A, int s,
                                                 int k, int ins)
@@ -506,13 +798,13 @@ __device__ __forceinline__ void sample_div_curl(const Geo &G, const Wave &W, con
     const long long o = cell(G, j, i);
     const long long so = (long long)s * G.fsz, mo = moff(G, s);
     float vxx, vyx, vxy, vyy;
-    if (TTIK) {
-        const float *dc = W.dcor + 4 * so;
-        vxx = dc[o], vyy = dc[G.fsz + o], vyx = dc[2 * G.fsz + o], vxy = dc[3 * G.fsz + o];
-    } else {
+    {
         op_s<ND>(W.vx + so, W.vy + so, o, G.pitch, G.hc, G.dhi, vxx, vyx, vxy, vyy);
+        int xr = xside(G, i), yr = yside(G, j);
+        // the EL_TTI right-bottom CPML pass stops at NY-1: raw derivatives there
+        if (TTIK && G.el_tti_rb_short && xr == 2 && yr == 2 && j == G.ny)
+            xr = yr = 0;
         if (G.abs_type == 1) {
-            int xr = xside(G, i), yr = yside(G, j);
             if (xr) {
                 int h = xr == 1 ? i : i - G.nx + G.fw2;
                 long long q = ((long long)s * G.ny + (j - 1)) * G.fw2 + (h - 1);
@@ -567,6 +859,7 @@ __global__ void k_post(Geo G, Wave W, Model M, Acq A)
         return;
     const int nt = *G.step_ctr;  // the velocity kernel of this step advanced it
     const int seismo = G.seismo;
+    psi_buffers(G, W, false);    // TTI: the CPML memory this step's stress update wrote
     // time_loop.c:282: sample at nt = NDT, 2 NDT, ... while nt < NT
     const int ins = (seismo && G.ndt > 0 && nt % G.ndt == 0 && nt < A.nt) ? nt / G.ndt : 0;
     const int *roff = A.rec_col_off ? A.rec_col_off + (long long)s * (G.nx + 1) : nullptr;

@@ -16,6 +16,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <deque>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -170,7 +172,11 @@ struct sofi_ctx {
     float last_ms = 0.f;
     bool run_pending = false;  // ev0/ev1 recorded by a sofi_run not yet synchronised
     bool march = false;        // y-marching kernels (ISO/VTI stress, all velocity updates)
-    int vrows = 1;             // rows per thread of the velocity kernel (1, 2 or 4)
+    int vw = 4;                // velocity kernel: cells per thread in x (4 or 2), 0 = vrows rows per thread
+    int vrows = 1;             // rows per thread of the one-cell velocity kernel (1, 2 or 4)
+    bool tuned = false;        // autotuner ran (or was skipped) for this context
+    bool tune_fixed = false;   // SOFI_VROWS chose the variant
+    bool pristine = false;     // every state array zero: reset(-1) and no set_field since
     // CUDA graph of kGraphSteps time steps, replayed for every chunk without
     // snapshot or timed steps (the step number lives in G.step_ctr)
     bool use_graph = true;
@@ -178,6 +184,7 @@ struct sofi_ctx {
     cudaGraphExec_t graph_exec = nullptr;
     long long graph_launches = 0;  // kernels per replay
     int march_sy = 32;         // rows per block of the y-marching kernels
+    bool tti_split = false;    // TTI: derivative fields through HBM (two kernels) instead of fused
     // snapshots
     int snap_nx = 0, snap_ny = 0, snap_total = 0, nsnap = 0;
     float *d_snap = nullptr;
@@ -231,9 +238,13 @@ int count_snapshots(const sofi_config &c)
 long long fields_bytes(const sofi_config &c)
 {
     long long pitch = pitch_for(c.nx), fsz = pitch * (c.ny + 2 * HY);
-    long long per_shot = 5 + 3LL * (is_visco(c.weq) ? c.L : 0) + (kind_of(c.weq) == TTI ? 8 : 0);
+    // TTI: the fused stress kernel doubles the velocity-derivative CPML memory;
+    // the two-kernel form (SOFI_TTI=split) holds 8 derivative fields instead
+    const char *e = getenv("SOFI_TTI");
+    const bool tti = kind_of(c.weq) == TTI, split = tti && e && strcmp(e, "split") == 0;
+    long long per_shot = 5 + 3LL * (is_visco(c.weq) ? c.L : 0) + (split ? 8 : 0);
     long long fw2 = 2LL * c.fw;
-    long long psi = (c.abs_type == 1 && c.fw > 0) ? 4 * ((long long)c.ny * fw2 + fw2 * c.nx) : 0;
+    long long psi = (c.abs_type == 1 && c.fw > 0) ? (tti && !split ? 6 : 4) * ((long long)c.ny * fw2 + fw2 * c.nx) : 0;
     long long nmod = c.shared_model ? 1 : c.nshots;
     long long nfields = (long long)needed_fields(c).size();
     long long bytes = 4 * (fsz * per_shot * c.nshots + psi * c.nshots + fsz * nfields * nmod);
@@ -446,6 +457,94 @@ void launch_cell_s(const Geo &G, const Wave &W, const Model &M, int nd, int kind
 
 // One time step. `capture`: being recorded into the step graph, so no host-
 // side step number exists (no timing events, no snapshot).
+// The velocity kernel in the context's variant: c->vw cells per thread in x
+// (2 or 4), else c->vrows rows per thread, or the y-marching kernel.
+void launch_v(sofi_ctx *c, const Geo &G, cudaStream_t st)
+{
+    const sofi_config &cf = c->cfg;
+    const int S = cf.nshots;
+    const dim3 blk(BX, BY);
+    if (c->march) {
+        launch_march_v(G, c->W, c->M, c->nd, c->march_sy, st);
+        return;
+    }
+    const int R = c->vw ? 1 : c->vrows, cx = c->vw ? c->vw : 1;
+    const unsigned tx = (cf.nx + cx * BX - 1) / (cx * BX), ty = (cf.ny + BY * R - 1) / (BY * R);
+    const dim3 gv = G.shot_fast ? dim3(tx * S, ty, 1) : dim3(tx, ty, S);
+    if (c->vw == 4)
+        DISPATCH_ND(c->nd, (k_update_vw<ND, 4><<<gv, blk, 0, st>>>(G, c->W, c->M)))
+    else if (c->vw == 2)
+        DISPATCH_ND(c->nd, (k_update_vw<ND, 2><<<gv, blk, 0, st>>>(G, c->W, c->M)))
+    else if (R == 1)
+        DISPATCH_ND(c->nd, (k_update_v<ND, 1><<<gv, blk, 0, st>>>(G, c->W, c->M)))
+    else if (R == 2)
+        DISPATCH_ND(c->nd, (k_update_v<ND, 2><<<gv, blk, 0, st>>>(G, c->W, c->M)))
+    else
+        DISPATCH_ND(c->nd, (k_update_v<ND, 4><<<gv, blk, 0, st>>>(G, c->W, c->M)))
+}
+
+// Autotuner of the velocity kernel. Which variant is fastest depends on the
+// grid: four cells per thread issues the fewest loads but leaves few blocks on
+// a small grid. The candidates are timed (CUDA events, back-to-back launches)
+// on the context's own arrays while a reset leaves them all zero -- every
+// candidate maps that state to itself, so tuning changes nothing -- and the
+// winner is cached per grid shape for the process.
+std::mutex g_tune_mu;
+std::map<std::string, std::pair<int, int>> g_tune;  // key -> (vw, vrows)
+
+int autotune(sofi_ctx *c)
+{
+    c->tuned = true;
+    if (c->tune_fixed || c->march)
+        return 0;
+    const sofi_config &cf = c->cfg;
+    char key[160];
+    snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d/%d/%d/%d/%d", c->device, c->nd, cf.nx, cf.ny, cf.nshots,
+             c->G.shot_fast, c->G.abs_type, cf.fw, cf.free_surf, cf.boundary);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) {
+            c->vw = it->second.first, c->vrows = it->second.second;
+            c->graph_dirty = true;
+            return 0;
+        }
+    }
+    if (!c->pristine)
+        return 0;  // state not known to be zero: keep the default variant
+    Geo G = c->G;
+    G.step_ctr = nullptr;  // tuning launches are not steps
+    const std::pair<int, int> cand[3] = {{4, 1}, {2, 1}, {0, 1}};
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    std::pair<int, int> pick = cand[0];
+    constexpr int kWarm = 2, kTimed = 12;
+    for (const auto &v : cand) {
+        c->vw = v.first, c->vrows = v.second;
+        for (int k = 0; k < kWarm; k++)
+            launch_v(c, G, c->stream);
+        CK(cudaEventRecord(e0, c->stream));
+        for (int k = 0; k < kTimed; k++)
+            launch_v(c, G, c->stream);
+        CK(cudaEventRecord(e1, c->stream));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best)
+            best = ms, pick = v;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CK(cudaGetLastError());
+    c->vw = pick.first, c->vrows = pick.second;
+    c->graph_dirty = true;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = pick;
+    return 0;
+}
+
 int launch_step(sofi_ctx *c, int nt, bool capture = false)
 {
     const sofi_config &cf = c->cfg;
@@ -474,19 +573,7 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
         c->tev_used += 3;
         CK(cudaEventRecord(e0, st));
     }
-    if (c->march) {
-        launch_march_v(G, c->W, c->M, c->nd, c->march_sy, st);
-    } else {
-        int R = c->vrows;
-        unsigned tx = (cf.nx + BX - 1) / BX, ty = (cf.ny + BY * R - 1) / (BY * R);
-        dim3 gv = G.shot_fast ? dim3(tx * S, ty, 1) : dim3(tx, ty, S);
-        if (R == 1)
-            DISPATCH_ND(c->nd, (k_update_v<ND, 1><<<gv, blk, 0, st>>>(G, c->W, c->M)))
-        else if (R == 2)
-            DISPATCH_ND(c->nd, (k_update_v<ND, 2><<<gv, blk, 0, st>>>(G, c->W, c->M)))
-        else
-            DISPATCH_ND(c->nd, (k_update_v<ND, 4><<<gv, blk, 0, st>>>(G, c->W, c->M)))
-    }
+    launch_v(c, G, st);
     c->launches++;
     if (timed)
         CK(cudaEventRecord(e1, st));
@@ -496,13 +583,24 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
     }
     if (timed && cf.boundary)
         CK(cudaEventRecord(e1, st));
-    if (kind == TTI) {
+    if (kind == TTI && c->tti_split) {
         c->launches++;
         DISPATCH_ND(c->nd, (k_tti_deriv<ND><<<grd, blk, 0, st>>>(G, c->W, c->M)));
         if (visco)
             k_update_s_tti<true><<<grd, blk, 0, st>>>(G, c->W, c->M);
         else
             k_update_s_tti<false><<<grd, blk, 0, st>>>(G, c->W, c->M);
+    } else if (kind == TTI) {
+        const bool cpml = G.abs_type == 1;
+        if (visco && cpml) {
+            DISPATCH_ND(c->nd, (k_tti_fused<ND, true, true><<<grd, blk, 0, st>>>(G, c->W, c->M)));
+        } else if (visco) {
+            DISPATCH_ND(c->nd, (k_tti_fused<ND, true, false><<<grd, blk, 0, st>>>(G, c->W, c->M)));
+        } else if (cpml) {
+            DISPATCH_ND(c->nd, (k_tti_fused<ND, false, true><<<grd, blk, 0, st>>>(G, c->W, c->M)));
+        } else {
+            DISPATCH_ND(c->nd, (k_tti_fused<ND, false, false><<<grd, blk, 0, st>>>(G, c->W, c->M)));
+        }
     } else if (c->march) {
         launch_march_s(G, c->W, c->M, c->nd, kind, visco, c->march_sy, st);
     } else {
@@ -671,9 +769,17 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
     if (const char *e = getenv("SOFI_KERNELS"))
         c->march = strcmp(e, "march") == 0;
     if (const char *e = getenv("SOFI_VROWS"))
-        c->vrows = (atoi(e) == 2 || atoi(e) == 4) ? atoi(e) : 1;
+    {
+        // SOFI_VROWS: "w4" / "w2" cells per thread in x, "1" / "2" / "4" rows per thread
+        const int v = e[0] == 'w' ? atoi(e + 1) : atoi(e);
+        c->vw = e[0] == 'w' ? (v == 2 ? 2 : 4) : 0;
+        c->vrows = (v == 2 || v == 4) ? v : 1;
+        c->tune_fixed = true;
+    }
     if (const char *e = getenv("SOFI_MARCH_ROWS"))
         c->march_sy = atoi(e) > 0 ? atoi(e) : c->march_sy;
+    if (const char *e = getenv("SOFI_TTI"))
+        c->tti_split = strcmp(e, "split") == 0;
     e = cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, priority);
     if (e != cudaSuccess) {
         delete c;
@@ -724,11 +830,16 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
         size_t py = sizeof(float) * (size_t)cfg->nshots * G.fw2 * cfg->nx;
         float **a[4] = {&c->W.psi_sxx_x, &c->W.psi_sxy_x, &c->W.psi_vxx, &c->W.psi_vyx};
         float **b[4] = {&c->W.psi_syy_y, &c->W.psi_sxy_y, &c->W.psi_vyy, &c->W.psi_vxy};
-        for (auto p : a)
-            if ((rc = dalloc(c, (void **)p, px)))
+        // the fused TTI stress kernel keeps the derivative memory in two buffers
+        const int nb = (kind_of(cfg->weq) == TTI && !c->tti_split) ? 2 : 1;
+        G.psi_pp = nb == 2;
+        G.psi_xsz = (long long)cfg->nshots * cfg->ny * G.fw2;
+        G.psi_ysz = (long long)cfg->nshots * G.fw2 * cfg->nx;
+        for (int k = 0; k < 4; k++)
+            if ((rc = dalloc(c, (void **)a[k], px * (k >= 2 ? nb : 1))))
                 goto bad;
-        for (auto p : b)
-            if ((rc = dalloc(c, (void **)p, py)))
+        for (int k = 0; k < 4; k++)
+            if ((rc = dalloc(c, (void **)b[k], py * (k >= 2 ? nb : 1))))
                 goto bad;
         // profile vectors: 12 x 2FW, one block
         float *pv;
@@ -740,7 +851,7 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
         for (int k = 0; k < 12; k++)
             *slots[k] = pv + (size_t)k * G.fw2;
     }
-    if (kind_of(cfg->weq) == TTI) {
+    if (kind_of(cfg->weq) == TTI && c->tti_split) {
         if ((rc = dalloc(c, (void **)&c->W.draw, f * 4)) || (rc = dalloc(c, (void **)&c->W.dcor, f * 4)))
             goto bad;
     }
@@ -924,10 +1035,13 @@ int sofi_reset(sofi_ctx *c, int shot)
             size_t px = sizeof(float) * (size_t)c->cfg.ny * c->G.fw2, py = sizeof(float) * (size_t)c->G.fw2 * c->cfg.nx;
             float *a[4] = {c->W.psi_sxx_x, c->W.psi_sxy_x, c->W.psi_vxx, c->W.psi_vyx};
             float *b[4] = {c->W.psi_syy_y, c->W.psi_sxy_y, c->W.psi_vyy, c->W.psi_vxy};
-            for (auto p : a)
-                CK(cudaMemsetAsync(reinterpret_cast<char *>(p) + s * px, 0, px, c->stream));
-            for (auto p : b)
-                CK(cudaMemsetAsync(reinterpret_cast<char *>(p) + s * py, 0, py, c->stream));
+            for (int k = 0; k < 4; k++)
+                for (int bb = 0; bb < ((k >= 2 && c->G.psi_pp) ? 2 : 1); bb++) {
+                    CK(cudaMemsetAsync(a[k] + bb * c->G.psi_xsz + (long long)s * c->cfg.ny * c->G.fw2, 0, px,
+                                       c->stream));
+                    CK(cudaMemsetAsync(b[k] + bb * c->G.psi_ysz + (long long)s * c->G.fw2 * c->cfg.nx, 0, py,
+                                       c->stream));
+                }
         }
         if (c->W.draw) {
             CK(cudaMemsetAsync(c->W.draw + 4LL * s * c->G.fsz, 0, 4 * f, c->stream));
@@ -942,6 +1056,7 @@ int sofi_reset(sofi_ctx *c, int shot)
     c->step = 0;
     c->nsnap = 0;
     CK(cudaStreamSynchronize(c->stream));
+    c->pristine = shot < 0;
     return 0;
 }
 
@@ -1000,6 +1115,12 @@ int sofi_run(sofi_ctx *c, int nsteps)
         if (rc)
             return rc;
     }
+    if (!c->tuned && c->step == 0 && nsteps > 0) {
+        int rc = autotune(c);
+        if (rc)
+            return rc;
+    }
+    c->pristine = false;
     CK(cudaEventRecord(c->ev0, c->stream));
     int left = nsteps;
     while (left > 0) {
@@ -1113,6 +1234,15 @@ int sofi_get_stream(sofi_ctx *c, void **stream)
     return 0;
 }
 
+int sofi_velocity_variant(sofi_ctx *c, int *cells_per_thread, int *rows_per_thread)
+{
+    if (!c || !cells_per_thread || !rows_per_thread)
+        return fail(SOFI_E_ARG, "null argument");
+    *cells_per_thread = c->vw ? c->vw : 1;
+    *rows_per_thread = c->vw ? 1 : c->vrows;
+    return 0;
+}
+
 int sofi_launch_count(sofi_ctx *c, long long *launches)
 {
     if (!c || !launches)
@@ -1180,6 +1310,8 @@ int sofi_get_field(sofi_ctx *c, int shot, const char *name, float *host)
 
 int sofi_set_field(sofi_ctx *c, int shot, const char *name, const float *host)
 {
+    if (c)
+        c->pristine = false;
     if (!c || !name || !host || shot < 0 || shot >= c->cfg.nshots)
         return fail(SOFI_E_ARG, "invalid field arguments");
     CK(cudaSetDevice(c->device));

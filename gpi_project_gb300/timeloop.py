@@ -114,6 +114,12 @@ class TimeLoop:
         N.check(self.lib.sofi_get_stream(self.h, ctypes.byref(s)))
         return s.value or 0
 
+    def velocity_variant(self) -> tuple:
+        """(cells per thread in x, rows per thread) of the velocity kernel."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        N.check(self.lib.sofi_velocity_variant(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
     def launch_count(self) -> int:
         n = ctypes.c_longlong()
         N.check(self.lib.sofi_launch_count(self.h, ctypes.byref(n)))

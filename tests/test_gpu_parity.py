@@ -95,6 +95,7 @@ def test_march_kernels_match_simple_kernels(name, monkeypatch):
     sp = case_sources(case, cfg)
     sig = O.wavelet(1, cfg.nt, cfg.dt, sp)
     out = {}
+    monkeypatch.setenv("SOFI_VROWS", "1")  # the one-cell velocity kernel beside the marching one
     for variant in ["simple", "march"]:
         monkeypatch.setenv("SOFI_KERNELS", variant)
         t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
@@ -126,4 +127,106 @@ def test_graph_replay_equals_direct_launches(name, monkeypatch):
         t.close()
     for k in out["1"]:
         np.testing.assert_array_equal(out["1"][k], out["0"][k], err_msg=f"{name} {k}")
+    o.close()
+
+
+# The reference's free surface on TTI media diverges on these models after
+# ~100 steps (its isotropic formulas read c11 and c55 as pi and mu), in the
+# oracle as on the GPU, so those variants stop at step 60; it rejects VEL_TTI
+# with a free surface.
+TTI_VARIANTS = [("tti_cpml", {}), ("vtti_cpml_l1", {}), ("tti_abs", {}), ("tti_cpml", {"boundary": 1}),
+                ("vtti_cpml_l1", {"boundary": 1}), ("tti_cpml", {"free_surf": 1, "nt": 60}),
+                ("tti_abs", {"free_surf": 1, "nt": 60}), ("tti_cpml", {"boundary": 1, "free_surf": 1, "nt": 60})]
+
+
+@pytest.mark.parametrize("name,over", TTI_VARIANTS,
+                         ids=[n + "".join(f"-{k}{v}" for k, v in o.items()) for n, o in TTI_VARIANTS])
+def test_tti_fused_equals_two_kernel_form_and_oracle(name, over, monkeypatch):
+    """The one-pass TTI stress kernel (derivatives in shared memory, CPML memory
+    in two buffers) computes exactly what the two-kernel form computes, and
+    both match the oracle, also with periodic x and a free surface."""
+    from oracle import oracle as O
+    from tests.golden.cases import case_by_name
+    from tests.helpers import case_receivers, case_sources
+    case = dict(case_by_name(name), **over)
+    o = run_oracle_case(case, nthreads=os.cpu_count() or 1)
+    cfg = o.cfg
+    sp = case_sources(case, cfg)
+    sig = O.wavelet(1, cfg.nt, cfg.dt, sp)
+    out = {}
+    for variant in ["split", "fused"]:
+        monkeypatch.setenv("SOFI_TTI", variant)
+        t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
+        out[variant] = {k: t.field(k) for k in ["vx", "vy", "sxx", "syy", "sxy"]}
+        out[variant].update({c: t.section(c) for c in COMPS})
+        out[variant]["snap_div"] = t.snapshots("div")
+        if variant == "fused":
+            compare_sections(t, o, case["seismo"], name)
+        t.close()
+    for k in out["fused"]:
+        np.testing.assert_array_equal(out["fused"][k], out["split"][k], err_msg=f"{name} {over} {k}")
+    o.close()
+
+
+@pytest.mark.parametrize("name", ["el_cpml_fd8", "el_abs_fd2", "el_abs_fd10", "el_cpml_fd12", "el_fs_cpml",
+                                  "visc_cpml_fs_l3", "el_periodic_cpml", "tti_cpml", "el_mixed_sources"])
+def test_velocity_kernel_vector_widths_match_one_cell(name, monkeypatch):
+    """The vector velocity kernels (four or two cells per thread) and the one-
+    cell-per-thread kernel compute the same step. The compiler contracts the stencil sums
+    into FMAs differently in the two instruction streams, so results agree to
+    float32 rounding grown over the run (1e-6 relative after 400 steps at FD8,
+    1.2e-5 at FD12 with MAXRELERROR 4); both match the oracle within 1e-4."""
+    from oracle import oracle as O
+    from tests.golden.cases import case_by_name
+    from tests.helpers import case_receivers, case_sources
+    case = case_by_name(name)
+    o = run_oracle_case(case, nthreads=os.cpu_count() or 1, nsteps=1)
+    cfg = o.cfg
+    sp = case_sources(case, cfg)
+    sig = O.wavelet(1, cfg.nt, cfg.dt, sp)
+    out = {}
+    for variant in ["1", "w4", "w2"]:
+        monkeypatch.setenv("SOFI_VROWS", variant)
+        t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
+        assert t.velocity_variant() == {"1": (1, 1), "w4": (4, 1), "w2": (2, 1)}[variant]
+        out[variant] = {k: t.field(k) for k in ["vx", "vy", "sxx", "syy", "sxy"]}
+        out[variant].update({c: t.section(c) for c in ["vx", "vy", "div"]})
+        t.close()
+    for w in ["w4", "w2"]:
+        for k in out[w]:
+            assert rel_l2(out[w][k], out["1"][k]) < 5e-5, (name, w, k, rel_l2(out[w][k], out["1"][k]))
+    o.close()
+
+
+@pytest.mark.parametrize("name", ["el_cpml_fd8", "visc_cpml_fs_l3", "el_abs_fd2"])
+def test_autotuned_run_equals_fixed_variant(name, monkeypatch):
+    """The autotuner times the velocity kernels on the zeroed arrays before the
+    first step; every candidate maps zero to zero, so the tuned run is bit-
+    identical to a run with the chosen variant fixed from the start."""
+    from oracle import oracle as O
+    from tests.golden.cases import case_by_name
+    from tests.helpers import case_receivers, case_sources
+    case = case_by_name(name)
+    o = run_oracle_case(case, nthreads=os.cpu_count() or 1, nsteps=1)
+    cfg = o.cfg
+    sp = case_sources(case, cfg)
+    sig = O.wavelet(1, cfg.nt, cfg.dt, sp)
+    monkeypatch.delenv("SOFI_VROWS", raising=False)
+    t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
+    cells, rows = t.velocity_variant()
+
+    def outputs(t):
+        d = {"field " + k: t.field(k) for k in ["vx", "vy", "sxx", "syy", "sxy"]}
+        d.update({"section " + c: t.section(c) for c in ["vx", "vy", "div"]})
+        return d
+
+    tuned = outputs(t)
+    t.close()
+    monkeypatch.setenv("SOFI_VROWS", f"w{cells}" if cells > 1 else str(rows))
+    t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
+    assert t.velocity_variant() == (cells, rows)
+    fixed = outputs(t)
+    t.close()
+    for k in tuned:
+        np.testing.assert_array_equal(tuned[k], fixed[k], err_msg=f"{name} {k}")
     o.close()
