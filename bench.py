@@ -483,7 +483,8 @@ def main():
         "e2e": {"value": round(e2e_val, 4), "unit": "Gcell-updates/s", "h2d_bytes_per_step": int(h2d_bytes),
                 "d2h_bytes_per_step": int(d2h_bytes)},
         "roofline": roof, "step_roofline": step_roof, "gpu_launches": int(launches),
-        "autotune": dict(zip(["velocity_cells_per_thread", "velocity_rows_per_thread"], t.velocity_variant())),
+        "autotune": {**dict(zip(["velocity_cells_per_thread", "velocity_rows_per_thread"], t.velocity_variant())),
+                     "stress_cells_per_thread": t.stress_variant()},
         **({"batched": batched} if batched else {}),
         "clocks": clk.summary(),
     }

@@ -7,8 +7,9 @@ namespace sofi {
 // -------------------------------------------------------------- sources
 
 // update_v_interior.c:49-71. Runs before the velocity kernel advances the
-// step counter, so the step being computed is counter + 1.
-__global__ void k_force_src(Geo G, Wave W, Model M, Acq A)
+// step counter, so the step being computed is counter + 1. (static: the
+// header is included by several translation units; only sofigpu.cu launches it)
+static __global__ void k_force_src(Geo G, Wave W, Model M, Acq A)
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= G.nshots)
@@ -292,7 +293,7 @@ __global__ void __launch_bounds__(BX *BY) k_update_vw(Geo G, Wave W, Model M)
 
 // Periodic x (BOUNDARY = 1): ghost columns copy the opposite edge, as the one-
 // rank exchange_v / exchange_s do (every column the stencils read is covered).
-__global__ void k_wrap_x(Geo G, float *a, float *b, float *c, int nd)
+static __global__ void k_wrap_x(Geo G, float *a, float *b, float *c, int nd)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
     int s = blockIdx.y;
@@ -426,6 +427,188 @@ __global__ void __launch_bounds__(BX *BY) k_update_s(Geo G, Wave W, Model M)
     sxy[o] = nxy;
     sxx[o] = nxx;
     syy[o] = nyy;
+}
+
+// The stress update with VW adjacent cells per thread (VW = 2 or 4), the
+// counterpart of k_update_vw: velocity stencils from 2K+1 vectors of a row
+// (x) and one vector per row (y), model, memory variables and stresses as
+// vectors; per cell the arithmetic of k_update_s, term by term. Reads past
+// column NX + ND feed only cells past NX, which are never stored.
+template <int ND, int KIND, bool VISCO, int LT, int VW>
+__global__ void __launch_bounds__(BX *BY) k_update_sw(Geo G, Wave W, Model M)
+{
+    constexpr int K = (ND + VW - 1) / VW;
+    constexpr int NXS = VW * (2 * K + 1);
+    int bx, s;
+    block_xs(G, bx, s);
+    const int i = (bx * BX + threadIdx.x) * VW + 1;
+    const int j = blockIdx.y * BY + threadIdx.y + 1;
+    if (i > G.nx || j > G.ny)
+        return;
+    const int P = G.pitch;
+    const int o = (j - 1 + HY) * P + (i - 1 + HX);
+    const long long so = (long long)s * G.fsz, mo = moff(G, s);
+    float *__restrict__ sxx = W.sxx + so;
+    float *__restrict__ syy = W.syy + so;
+    float *__restrict__ sxy = W.sxy + so;
+    const float *__restrict__ vx = W.vx + so;
+    const float *__restrict__ vy = W.vy + so;
+    const float *hc = G.hc;
+    float vxx[VW], vyx[VW], vxy[VW], vyy[VW];
+    {
+        float X[NXS], Y[NXS];  // X[k] = vx(j, i - VW K + k), Y[k] = vy(j, i - VW K + k)
+#pragma unroll
+        for (int q = 0; q < 2 * K + 1; q++) {
+            ldv<VW>(vx + o + VW * (q - K), X + VW * q);
+            ldv<VW>(vy + o + VW * (q - K), Y + VW * q);
+        }
+        constexpr int C = VW * K;
+#pragma unroll
+        for (int c = 0; c < VW; c++) {
+            vxx[c] = hc[1] * (X[C + c] - X[C + c - 1]);
+            vyx[c] = hc[1] * (Y[C + c + 1] - Y[C + c]);
+#pragma unroll
+            for (int m = 2; m <= ND; m++) {
+                vxx[c] += hc[m] * (X[C + c + m - 1] - X[C + c - m]);
+                vyx[c] += hc[m] * (Y[C + c + m] - Y[C + c - m + 1]);
+            }
+        }
+    }
+    {
+        // y stencils: vx rows j - ND + 1 .. j + ND, vy rows j - ND .. j + ND - 1
+        float a1[VW], a0[VW], b1[VW], b0[VW];
+        ldv<VW>(vx + o + P, a1), ldv<VW>(vx + o, a0);
+        ldv<VW>(vy + o, b1), ldv<VW>(vy + o - P, b0);
+#pragma unroll
+        for (int c = 0; c < VW; c++) {
+            vxy[c] = hc[1] * (a1[c] - a0[c]);
+            vyy[c] = hc[1] * (b1[c] - b0[c]);
+        }
+#pragma unroll
+        for (int m = 2; m <= ND; m++) {
+            ldv<VW>(vx + o + m * P, a1), ldv<VW>(vx + o - (m - 1) * P, a0);
+            ldv<VW>(vy + o + (m - 1) * P, b1), ldv<VW>(vy + o - m * P, b0);
+#pragma unroll
+            for (int c = 0; c < VW; c++) {
+                vxy[c] += hc[m] * (a1[c] - a0[c]);
+                vyy[c] += hc[m] * (b1[c] - b0[c]);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < VW; c++)
+            vxx[c] *= G.dhi, vyx[c] *= G.dhi, vxy[c] *= G.dhi, vyy[c] *= G.dhi;
+    }
+    float m0[VW], m1[VW], m2[VW], m3[VW], b0[VW], b1[VW], b2[VW], b3[VW];
+#pragma unroll
+    for (int c = 0; c < VW; c++)
+        m3[c] = 0.f, b0[c] = b1[c] = b2[c] = b3[c] = 0.f;
+    if (KIND == ISO) {
+        ldv<VW>(M.g + mo + o, m0), ldv<VW>(M.f + mo + o, m1), ldv<VW>(M.fipjp + mo + o, m2);
+        if (VISCO)
+            ldv<VW>(M.db + mo + o, b0), ldv<VW>(M.eb + mo + o, b1), ldv<VW>(M.dipb + mo + o, b2);
+    } else {
+        ldv<VW>(M.c11 + mo + o, m0), ldv<VW>(M.c13 + mo + o, m1), ldv<VW>(M.c33 + mo + o, m2);
+        ldv<VW>(M.c55ipjp + mo + o, m3);
+        if (VISCO) {
+            ldv<VW>(M.c11b + mo + o, b0), ldv<VW>(M.c13b + mo + o, b1), ldv<VW>(M.c33b + mo + o, b2);
+            ldv<VW>(M.c55ipjpb + mo + o, b3);
+        }
+    }
+    constexpr int LN = LT > 0 ? LT : MAXL;
+    const int L = LT > 0 ? LT : G.L;
+    float *__restrict__ wr = W.r + (long long)s * G.L * G.fsz;
+    float *__restrict__ wp = W.p + (long long)s * G.L * G.fsz;
+    float *__restrict__ wq = W.q + (long long)s * G.L * G.fsz;
+    float rr[LN][VW], pp[LN][VW], qq[LN][VW];
+    if (VISCO) {
+#pragma unroll
+        for (int l = 0; l < LN; l++)
+            if (l < L) {
+                const long long lo = (long long)l * G.fsz + o;
+                ldv_rw<VW>(wr + lo, rr[l]), ldv_rw<VW>(wp + lo, pp[l]), ldv_rw<VW>(wq + lo, qq[l]);
+            }
+    }
+    float oxx[VW], oyy[VW], oxy[VW];
+    ldv_rw<VW>(sxx + o, oxx), ldv_rw<VW>(syy + o, oyy), ldv_rw<VW>(sxy + o, oxy);
+    const int yr = yside(G, j);
+    const bool xframe = i <= G.gx2 || i + VW - 1 > G.gx3;
+    float nxx[VW], nyy[VW], nxy[VW];
+#pragma unroll
+    for (int c = 0; c < VW; c++) {
+        const int ic = i + c;
+        const int xr = xframe ? xside(G, ic) : 0;
+        float dxx = vxx[c], dyx = vyx[c], dxy = vxy[c], dyy = vyy[c];
+        if (G.abs_type == 1 && ic <= G.nx)
+            cpml_s(G, W, M, s, ic, j, xr, yr, dxx, dyx, dxy, dyy, true);
+        float u1, u2, u3;
+        if (KIND == ISO) {
+            u1 = m2[c] * (dyx + dxy);
+            float gd = m0[c] * (dxx + dyy);
+            u2 = gd - 2.0f * m1[c] * dyy;
+            u3 = gd - 2.0f * m1[c] * dxx;
+        } else {
+            u1 = m3[c] * (dxy + dyx);
+            u2 = m0[c] * dxx + m1[c] * dyy;
+            u3 = m1[c] * dxx + m2[c] * dyy;
+        }
+        if (VISCO) {
+            float sro = 0.f, spo = 0.f, sqo = 0.f, sr = 0.f, sp = 0.f, sq = 0.f;
+#pragma unroll
+            for (int l = 0; l < LN; l++) {
+                if (l < L) {
+                    float r = rr[l][c], p = pp[l][c], q = qq[l][c];
+                    sro += r, spo += p, sqo += q;
+                    float pe = M.peta[l], bb = M.bip[l], cc = M.cip[l];
+                    if (KIND == ISO) {
+                        float dip = b2[c] * pe, d = b0[c] * pe, e = b1[c] * pe;
+                        r = bb * (r * cc - dip * (dxy + dyx));
+                        p = bb * (p * cc - e * (dxx + dyy) + 2.0f * d * dyy);
+                        q = bb * (q * cc - e * (dxx + dyy) + 2.0f * d * dxx);
+                    } else {
+                        r = bb * (r * cc - (b3[c] * pe) * (dxy + dyx));
+                        p = bb * (p * cc - (b0[c] * pe) * dxx - (b1[c] * pe) * dyy);
+                        q = bb * (q * cc - (b1[c] * pe) * dxx - (b2[c] * pe) * dyy);
+                    }
+                    rr[l][c] = r, pp[l][c] = p, qq[l][c] = q;
+                    sr += r, sp += p, sq += q;
+                }
+            }
+            u1 += G.dthalbe * (sro + sr);
+            u2 += G.dthalbe * (spo + sp);
+            u3 += G.dthalbe * (sqo + sq);
+        }
+        nxy[c] = oxy[c] + u1, nxx[c] = oxx[c] + u2, nyy[c] = oyy[c] + u3;
+        if (G.abs_type == 2 && (xr | yr)) {
+            float a = __ldg(M.absorb + mo + o + c);
+            nxy[c] *= a, nyy[c] *= a, nxx[c] *= a;
+        }
+    }
+    if (i + VW - 1 <= G.nx) {
+        if (VISCO) {
+#pragma unroll
+            for (int l = 0; l < LN; l++)
+                if (l < L) {
+                    const long long lo = (long long)l * G.fsz + o;
+                    stv<VW>(wr + lo, rr[l]), stv<VW>(wp + lo, pp[l]), stv<VW>(wq + lo, qq[l]);
+                }
+        }
+        stv<VW>(sxy + o, nxy), stv<VW>(sxx + o, nxx), stv<VW>(syy + o, nyy);
+    } else {
+#pragma unroll
+        for (int c = 0; c < VW; c++) {
+            if (i + c > G.nx)
+                continue;
+            if (VISCO) {
+#pragma unroll
+                for (int l = 0; l < LN; l++)
+                    if (l < L) {
+                        const long long lo = (long long)l * G.fsz + o + c;
+                        wr[lo] = rr[l][c], wp[lo] = pp[l][c], wq[lo] = qq[l][c];
+                    }
+            }
+            sxy[o + c] = nxy[c], sxx[o + c] = nxx[c], syy[o + c] = nyy[c];
+        }
+    }
 }
 
 // ------------------------------------------------------------------ TTI

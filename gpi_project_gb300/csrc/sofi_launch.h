@@ -1,4 +1,5 @@
-// sofi_launch.h -- host launchers of kernels compiled in other translation units.
+// sofi_launch.h -- host launchers of kernels compiled in other translation
+// units (so that the template instantiations compile in parallel).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -11,4 +12,15 @@ void launch_march_v(const Geo &G, const Wave &W, const Model &M, int nd, int sy,
 // stress update of isotropic / VTI media, y-marching
 void launch_march_s(const Geo &G, const Wave &W, const Model &M, int nd, int kind, bool visco, int sy,
                     cudaStream_t st);
+// velocity update: vw cells per thread in x (4 or 2), else vrows rows per thread (1, 2, 4)
+void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw, int vrows, dim3 grid,
+                     cudaStream_t st);
+// ISO / VTI stress update (KIND 0 ISO, 1 VTI): sw cells per thread in x (4, 2 or 0 = one)
+template <int KIND, bool VISCO>
+void launch_stress_kv(const Geo &G, const Wave &W, const Model &M, int nd, int sw, dim3 grid, cudaStream_t st);
+// TTI stress update: one pass (derivatives in shared memory) or the two-kernel
+// form (derivative fields in W.draw / W.dcor)
+void launch_tti_fused(const Geo &G, const Wave &W, const Model &M, int nd, bool visco, bool cpml, dim3 grid,
+                      cudaStream_t st);
+void launch_tti_split(const Geo &G, const Wave &W, const Model &M, int nd, bool visco, dim3 grid, cudaStream_t st);
 }  // namespace sofi

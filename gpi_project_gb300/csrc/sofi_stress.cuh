@@ -1,0 +1,48 @@
+// sofi_stress.cuh -- launcher template of the ISO / VTI stress kernels; each
+// (kind, visco) pair is instantiated in its own translation unit.
+#pragma once
+#include "sofi_dispatch.cuh"
+#include "sofi_kernels.cuh"
+#include "sofi_launch.h"
+
+namespace sofi {
+
+template <int KIND, bool VISCO, int VW>
+void stress_w(const Geo &G, const Wave &W, const Model &M, int nd, dim3 grd, cudaStream_t st)
+{
+    const dim3 blk(BX, BY);
+    const int L = VISCO ? G.L : 0;
+    if (!VISCO)
+        DISPATCH_ND(nd, (k_update_sw<ND, KIND, false, 0, VW><<<grd, blk, 0, st>>>(G, W, M)))
+    else if (L == 1)
+        DISPATCH_ND(nd, (k_update_sw<ND, KIND, true, 1, VW><<<grd, blk, 0, st>>>(G, W, M)))
+    else if (L == 2)
+        DISPATCH_ND(nd, (k_update_sw<ND, KIND, true, 2, VW><<<grd, blk, 0, st>>>(G, W, M)))
+    else if (L == 3)
+        DISPATCH_ND(nd, (k_update_sw<ND, KIND, true, 3, VW><<<grd, blk, 0, st>>>(G, W, M)))
+    else
+        DISPATCH_ND(nd, (k_update_sw<ND, KIND, true, 0, VW><<<grd, blk, 0, st>>>(G, W, M)))
+}
+
+template <int KIND, bool VISCO>
+void launch_stress_kv(const Geo &G, const Wave &W, const Model &M, int nd, int sw, dim3 grd, cudaStream_t st)
+{
+    if (sw == 4)
+        return stress_w<KIND, VISCO, 4>(G, W, M, nd, grd, st);
+    if (sw == 2)
+        return stress_w<KIND, VISCO, 2>(G, W, M, nd, grd, st);
+    const dim3 blk(BX, BY);
+    const int L = VISCO ? G.L : 0;
+    if (!VISCO)
+        DISPATCH_ND(nd, (k_update_s<ND, KIND, false, 0><<<grd, blk, 0, st>>>(G, W, M)))
+    else if (L == 1)
+        DISPATCH_ND(nd, (k_update_s<ND, KIND, true, 1><<<grd, blk, 0, st>>>(G, W, M)))
+    else if (L == 2)
+        DISPATCH_ND(nd, (k_update_s<ND, KIND, true, 2><<<grd, blk, 0, st>>>(G, W, M)))
+    else if (L == 3)
+        DISPATCH_ND(nd, (k_update_s<ND, KIND, true, 3><<<grd, blk, 0, st>>>(G, W, M)))
+    else
+        DISPATCH_ND(nd, (k_update_s<ND, KIND, true, 0><<<grd, blk, 0, st>>>(G, W, M)))
+}
+
+}  // namespace sofi

@@ -1,0 +1,24 @@
+// sofi_velocity.cu -- instantiations and launcher of the velocity kernels.
+#include "sofi_dispatch.cuh"
+#include "sofi_kernels.cuh"
+#include "sofi_launch.h"
+
+namespace sofi {
+
+void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw, int vrows, dim3 gv,
+                     cudaStream_t st)
+{
+    const dim3 blk(BX, BY);
+    if (vw == 4)
+        DISPATCH_ND(nd, (k_update_vw<ND, 4><<<gv, blk, 0, st>>>(G, W, M)))
+    else if (vw == 2)
+        DISPATCH_ND(nd, (k_update_vw<ND, 2><<<gv, blk, 0, st>>>(G, W, M)))
+    else if (vrows == 2)
+        DISPATCH_ND(nd, (k_update_v<ND, 2><<<gv, blk, 0, st>>>(G, W, M)))
+    else if (vrows == 4)
+        DISPATCH_ND(nd, (k_update_v<ND, 4><<<gv, blk, 0, st>>>(G, W, M)))
+    else
+        DISPATCH_ND(nd, (k_update_v<ND, 1><<<gv, blk, 0, st>>>(G, W, M)))
+}
+
+}  // namespace sofi

@@ -7,6 +7,7 @@
 #include "sofigpu.h"
 #include "sofi_kernels.cuh"
 #include "sofi_launch.h"
+#include "sofi_dispatch.cuh"
 
 #include <cuda_runtime.h>
 
@@ -174,6 +175,8 @@ struct sofi_ctx {
     bool march = false;        // y-marching kernels (ISO/VTI stress, all velocity updates)
     int vw = 4;                // velocity kernel: cells per thread in x (4 or 2), 0 = vrows rows per thread
     int vrows = 1;             // rows per thread of the one-cell velocity kernel (1, 2 or 4)
+    int sw = 0;                // ISO / VTI stress kernel: cells per thread in x (4 or 2), 0 = one
+    bool sw_fixed = false;     // SOFI_SW chose it
     bool tuned = false;        // autotuner ran (or was skipped) for this context
     bool tune_fixed = false;   // SOFI_VROWS chose the variant
     bool pristine = false;     // every state array zero: reset(-1) and no set_field since
@@ -420,39 +423,17 @@ dim3 grid2d(const sofi_ctx *c)
     return dim3(tx, ty, c->cfg.nshots);
 }
 
-#define DISPATCH_ND(ND_, ...)                        \
-    switch (ND_) {                                  \
-      case 1: { constexpr int ND = 1; __VA_ARGS__; } break; \
-      case 2: { constexpr int ND = 2; __VA_ARGS__; } break; \
-      case 3: { constexpr int ND = 3; __VA_ARGS__; } break; \
-      case 4: { constexpr int ND = 4; __VA_ARGS__; } break; \
-      case 5: { constexpr int ND = 5; __VA_ARGS__; } break; \
-      case 6: { constexpr int ND = 6; __VA_ARGS__; } break; \
-    }
-
-template <int KIND, bool VISCO>
-void cell_s_l(const Geo &G, const Wave &W, const Model &M, int nd, dim3 grd, dim3 blk, cudaStream_t st)
+// The ISO / VTI stress kernel with sw cells per thread in x (0: one).
+void launch_cell_s(const Geo &G, const Wave &W, const Model &M, int nd, int kind, bool visco, int sw, int nx,
+                   int ny, int nshots, cudaStream_t st)
 {
-    int L = VISCO ? G.L : 0;
-    if (!VISCO)
-        DISPATCH_ND(nd, (k_update_s<ND, KIND, false, 0><<<grd, blk, 0, st>>>(G, W, M)))
-    else if (L == 1)
-        DISPATCH_ND(nd, (k_update_s<ND, KIND, true, 1><<<grd, blk, 0, st>>>(G, W, M)))
-    else if (L == 2)
-        DISPATCH_ND(nd, (k_update_s<ND, KIND, true, 2><<<grd, blk, 0, st>>>(G, W, M)))
-    else if (L == 3)
-        DISPATCH_ND(nd, (k_update_s<ND, KIND, true, 3><<<grd, blk, 0, st>>>(G, W, M)))
-    else
-        DISPATCH_ND(nd, (k_update_s<ND, KIND, true, 0><<<grd, blk, 0, st>>>(G, W, M)))
-}
-
-void launch_cell_s(const Geo &G, const Wave &W, const Model &M, int nd, int kind, bool visco, dim3 grd, dim3 blk,
-                   cudaStream_t st)
-{
+    const int cx = sw ? sw : 1;
+    const unsigned tx = (nx + cx * BX - 1) / (cx * BX), ty = (ny + BY - 1) / BY;
+    const dim3 grd = G.shot_fast ? dim3(tx * nshots, ty, 1) : dim3(tx, ty, nshots);
     if (kind == ISO)
-        visco ? cell_s_l<ISO, true>(G, W, M, nd, grd, blk, st) : cell_s_l<ISO, false>(G, W, M, nd, grd, blk, st);
+        visco ? launch_stress_kv<ISO, true>(G, W, M, nd, sw, grd, st) : launch_stress_kv<ISO, false>(G, W, M, nd, sw, grd, st);
     else
-        visco ? cell_s_l<VTI, true>(G, W, M, nd, grd, blk, st) : cell_s_l<VTI, false>(G, W, M, nd, grd, blk, st);
+        visco ? launch_stress_kv<VTI, true>(G, W, M, nd, sw, grd, st) : launch_stress_kv<VTI, false>(G, W, M, nd, sw, grd, st);
 }
 
 // One time step. `capture`: being recorded into the step graph, so no host-
@@ -463,7 +444,6 @@ void launch_v(sofi_ctx *c, const Geo &G, cudaStream_t st)
 {
     const sofi_config &cf = c->cfg;
     const int S = cf.nshots;
-    const dim3 blk(BX, BY);
     if (c->march) {
         launch_march_v(G, c->W, c->M, c->nd, c->march_sy, st);
         return;
@@ -471,77 +451,106 @@ void launch_v(sofi_ctx *c, const Geo &G, cudaStream_t st)
     const int R = c->vw ? 1 : c->vrows, cx = c->vw ? c->vw : 1;
     const unsigned tx = (cf.nx + cx * BX - 1) / (cx * BX), ty = (cf.ny + BY * R - 1) / (BY * R);
     const dim3 gv = G.shot_fast ? dim3(tx * S, ty, 1) : dim3(tx, ty, S);
-    if (c->vw == 4)
-        DISPATCH_ND(c->nd, (k_update_vw<ND, 4><<<gv, blk, 0, st>>>(G, c->W, c->M)))
-    else if (c->vw == 2)
-        DISPATCH_ND(c->nd, (k_update_vw<ND, 2><<<gv, blk, 0, st>>>(G, c->W, c->M)))
-    else if (R == 1)
-        DISPATCH_ND(c->nd, (k_update_v<ND, 1><<<gv, blk, 0, st>>>(G, c->W, c->M)))
-    else if (R == 2)
-        DISPATCH_ND(c->nd, (k_update_v<ND, 2><<<gv, blk, 0, st>>>(G, c->W, c->M)))
-    else
-        DISPATCH_ND(c->nd, (k_update_v<ND, 4><<<gv, blk, 0, st>>>(G, c->W, c->M)))
+    launch_velocity(G, c->W, c->M, c->nd, c->vw, R, gv, st);
 }
 
-// Autotuner of the velocity kernel. Which variant is fastest depends on the
-// grid: four cells per thread issues the fewest loads but leaves few blocks on
-// a small grid. The candidates are timed (CUDA events, back-to-back launches)
-// on the context's own arrays while a reset leaves them all zero -- every
-// candidate maps that state to itself, so tuning changes nothing -- and the
-// winner is cached per grid shape for the process.
+// Autotuner of the velocity and (ISO / VTI) stress kernels. Which variant is
+// fastest depends on the grid: several cells per thread issue the fewest
+// loads but leave few blocks on a small grid. The candidates are timed (CUDA
+// events, back-to-back launches) on the context's own arrays while a reset
+// leaves them all zero -- every candidate maps that state to itself, so
+// tuning changes nothing -- and the winners are cached per configuration for
+// the process. SOFI_VROWS / SOFI_SW fix a choice.
+struct Tuned {
+    int vw, vrows, sw;
+};
 std::mutex g_tune_mu;
-std::map<std::string, std::pair<int, int>> g_tune;  // key -> (vw, vrows)
+std::map<std::string, Tuned> g_tune;
+
+template <typename F>
+int time_launches(sofi_ctx *c, F launch, float *ms)
+{
+    constexpr int kWarm = 2, kTimed = 12;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    for (int k = 0; k < kWarm; k++)
+        launch();
+    cudaEventRecord(e0, c->stream);
+    for (int k = 0; k < kTimed; k++)
+        launch();
+    cudaEventRecord(e1, c->stream);
+    cudaError_t e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess)
+        e = cudaEventElapsedTime(ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess)
+        return fail(SOFI_E_CUDA, "autotune timing: %s", cudaGetErrorString(e));
+    CK(cudaGetLastError());
+    return 0;
+}
 
 int autotune(sofi_ctx *c)
 {
     c->tuned = true;
-    if (c->tune_fixed || c->march)
+    if (c->march)
         return 0;
     const sofi_config &cf = c->cfg;
-    char key[160];
-    snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d/%d/%d/%d/%d", c->device, c->nd, cf.nx, cf.ny, cf.nshots,
-             c->G.shot_fast, c->G.abs_type, cf.fw, cf.free_surf, cf.boundary);
+    const int kind = kind_of(cf.weq);
+    const bool visco = is_visco(cf.weq);
+    const bool tune_s = kind != TTI && !c->sw_fixed;
+    if (c->tune_fixed && !tune_s)
+        return 0;
+    char key[200];
+    snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d", c->device, c->nd, cf.nx, cf.ny, cf.nshots,
+             c->G.shot_fast, c->G.abs_type, cf.fw, cf.free_surf, cf.boundary, kind, visco ? c->G.L : -1,
+             c->nmodels);
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune.find(key);
         if (it != g_tune.end()) {
-            c->vw = it->second.first, c->vrows = it->second.second;
+            if (!c->tune_fixed)
+                c->vw = it->second.vw, c->vrows = it->second.vrows;
+            if (tune_s)
+                c->sw = it->second.sw;
             c->graph_dirty = true;
             return 0;
         }
     }
     if (!c->pristine)
-        return 0;  // state not known to be zero: keep the default variant
+        return 0;  // state not known to be zero: keep the default variants
     Geo G = c->G;
     G.step_ctr = nullptr;  // tuning launches are not steps
-    const std::pair<int, int> cand[3] = {{4, 1}, {2, 1}, {0, 1}};
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0));
-    CK(cudaEventCreate(&e1));
-    float best = 1e30f;
-    std::pair<int, int> pick = cand[0];
-    constexpr int kWarm = 2, kTimed = 12;
-    for (const auto &v : cand) {
-        c->vw = v.first, c->vrows = v.second;
-        for (int k = 0; k < kWarm; k++)
-            launch_v(c, G, c->stream);
-        CK(cudaEventRecord(e0, c->stream));
-        for (int k = 0; k < kTimed; k++)
-            launch_v(c, G, c->stream);
-        CK(cudaEventRecord(e1, c->stream));
-        CK(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        CK(cudaEventElapsedTime(&ms, e0, e1));
-        if (ms < best)
-            best = ms, pick = v;
+    Tuned pick{c->vw, c->vrows, c->sw};
+    float best = 1e30f, ms = 0.f;
+    int rc;
+    if (!c->tune_fixed) {
+        const int cand[3][2] = {{4, 1}, {2, 1}, {0, 1}};
+        for (const auto &v : cand) {
+            c->vw = v[0], c->vrows = v[1];
+            if ((rc = time_launches(c, [&] { launch_v(c, G, c->stream); }, &ms)))
+                return rc;
+            if (ms < best)
+                best = ms, pick.vw = v[0], pick.vrows = v[1];
+        }
+        c->vw = pick.vw, c->vrows = pick.vrows;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    CK(cudaGetLastError());
-    c->vw = pick.first, c->vrows = pick.second;
+    if (tune_s) {
+        best = 1e30f;
+        for (int w : {4, 2, 0}) {
+            if ((rc = time_launches(
+                     c, [&] { launch_cell_s(G, c->W, c->M, c->nd, kind, visco, w, cf.nx, cf.ny, cf.nshots, c->stream); },
+                     &ms)))
+                return rc;
+            if (ms < best)
+                best = ms, pick.sw = w;
+        }
+        c->sw = pick.sw;
+    }
     c->graph_dirty = true;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune[key] = pick;
+    g_tune[key] = Tuned{c->vw, c->vrows, c->sw};
     return 0;
 }
 
@@ -585,26 +594,13 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
         CK(cudaEventRecord(e1, st));
     if (kind == TTI && c->tti_split) {
         c->launches++;
-        DISPATCH_ND(c->nd, (k_tti_deriv<ND><<<grd, blk, 0, st>>>(G, c->W, c->M)));
-        if (visco)
-            k_update_s_tti<true><<<grd, blk, 0, st>>>(G, c->W, c->M);
-        else
-            k_update_s_tti<false><<<grd, blk, 0, st>>>(G, c->W, c->M);
+        launch_tti_split(G, c->W, c->M, c->nd, visco, grd, st);
     } else if (kind == TTI) {
-        const bool cpml = G.abs_type == 1;
-        if (visco && cpml) {
-            DISPATCH_ND(c->nd, (k_tti_fused<ND, true, true><<<grd, blk, 0, st>>>(G, c->W, c->M)));
-        } else if (visco) {
-            DISPATCH_ND(c->nd, (k_tti_fused<ND, true, false><<<grd, blk, 0, st>>>(G, c->W, c->M)));
-        } else if (cpml) {
-            DISPATCH_ND(c->nd, (k_tti_fused<ND, false, true><<<grd, blk, 0, st>>>(G, c->W, c->M)));
-        } else {
-            DISPATCH_ND(c->nd, (k_tti_fused<ND, false, false><<<grd, blk, 0, st>>>(G, c->W, c->M)));
-        }
+        launch_tti_fused(G, c->W, c->M, c->nd, visco, G.abs_type == 1, grd, st);
     } else if (c->march) {
         launch_march_s(G, c->W, c->M, c->nd, kind, visco, c->march_sy, st);
     } else {
-        launch_cell_s(G, c->W, c->M, c->nd, kind, visco, grd, blk, st);
+        launch_cell_s(G, c->W, c->M, c->nd, kind, visco, c->sw, cf.nx, cf.ny, S, st);
     }
     c->launches++;
     if (timed)
@@ -775,6 +771,10 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
         c->vw = e[0] == 'w' ? (v == 2 ? 2 : 4) : 0;
         c->vrows = (v == 2 || v == 4) ? v : 1;
         c->tune_fixed = true;
+    }
+    if (const char *e = getenv("SOFI_SW")) {
+        c->sw = (atoi(e) == 2 || atoi(e) == 4) ? atoi(e) : 0;
+        c->sw_fixed = true;
     }
     if (const char *e = getenv("SOFI_MARCH_ROWS"))
         c->march_sy = atoi(e) > 0 ? atoi(e) : c->march_sy;
@@ -1243,6 +1243,14 @@ int sofi_velocity_variant(sofi_ctx *c, int *cells_per_thread, int *rows_per_thre
     return 0;
 }
 
+int sofi_stress_variant(sofi_ctx *c, int *cells_per_thread)
+{
+    if (!c || !cells_per_thread)
+        return fail(SOFI_E_ARG, "null argument");
+    *cells_per_thread = kind_of(c->cfg.weq) == TTI ? 1 : (c->sw ? c->sw : 1);
+    return 0;
+}
+
 int sofi_launch_count(sofi_ctx *c, long long *launches)
 {
     if (!c || !launches)
@@ -1444,11 +1452,7 @@ int sofi_tti_stress_noalloc(const sofi_config *cfg, const sofi_tti_stress_args *
         M.bip[l] = a->bip[l], M.cip[l] = a->cip[l], M.peta[l] = a->peta[l];
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     dim3 blk(BX, BY), grd((cfg->nx + BX - 1) / BX, (cfg->ny + BY - 1) / BY, 1);
-    DISPATCH_ND(cfg->fdorder / 2, (k_tti_deriv<ND><<<grd, blk, 0, st>>>(G, W, M)));
-    if (visco)
-        k_update_s_tti<true><<<grd, blk, 0, st>>>(G, W, M);
-    else
-        k_update_s_tti<false><<<grd, blk, 0, st>>>(G, W, M);
+    launch_tti_split(G, W, M, cfg->fdorder / 2, visco, grd, st);
     CK(cudaGetLastError());
     return 0;
 }

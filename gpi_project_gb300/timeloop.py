@@ -120,6 +120,12 @@ class TimeLoop:
         N.check(self.lib.sofi_velocity_variant(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    def stress_variant(self) -> int:
+        """Cells per thread in x of the stress kernel."""
+        a = ctypes.c_int()
+        N.check(self.lib.sofi_stress_variant(self.h, ctypes.byref(a)))
+        return a.value
+
     def launch_count(self) -> int:
         n = ctypes.c_longlong()
         N.check(self.lib.sofi_launch_count(self.h, ctypes.byref(n)))

@@ -194,6 +194,9 @@ int sofi_kernel_time(sofi_ctx *ctx, const char *name, double *avg_ms, long long 
  * times the variants on the zeroed arrays (where each leaves them zero) and
  * keeps the fastest for the grid shape; SOFI_VROWS=w4|w2|1|2|4 fixes it. */
 int sofi_velocity_variant(sofi_ctx *ctx, int *cells_per_thread, int *rows_per_thread);
+/* Stress-kernel variant in use: cells per thread along x (1, 2 or 4; TTI: 1),
+ * chosen by the same autotuning run; SOFI_SW=0|2|4 fixes it. */
+int sofi_stress_variant(sofi_ctx *ctx, int *cells_per_thread);
 /* Kernels launched by sofi_run since the context was created. */
 int sofi_launch_count(sofi_ctx *ctx, long long *launches);
 /* The context's CUDA stream (a cudaStream_t), for callers that order their own
