@@ -1,29 +1,31 @@
 // sofi_common.cuh -- types, layout and inline device helpers shared by the kernels.
 //
-// (Kernel overview: see sofi_kernels.cuh.)
-//
-// sofi_kernels.cuh -- device kernels of the SOFI2D time step on sm_103a.
-//
 // One time step of the reference's time_loop (src/time_loop.c:42-322) is
-//   k_force_src  force sources before the velocity update (update_v_interior.c:49-71)
-//   k_update_v   velocity update, all cells, CPML / damping frame by predicate
-//                (update_v_interior.c, update_v_PML.c, update_v_abs.c)
-//   k_wrap_x     periodic x only: ghost columns (exchange_v.c / exchange_s.c, one rank)
-//   k_update_s   stress update with the velocity derivatives recomputed from v in
-//                registers (v_derivatives.c fused away), CPML / damping by predicate
-//   k_tti_deriv + k_update_s_tti   TTI: derivatives (raw and CPML-stretched) are
-//                stored so the 4-point averages can follow the reference's
-//                region-by-region order (update_s_elastic_TTI_PML.c)
-//   k_seis_deriv div/curl sampling (derivatives as the stress update left them)
-//   k_stress_src explosive / moment-tensor sources + NaN probe (psource.c, eqsource.c)
-//   k_surface    free surface, one thread per column (surface_elastic.c, surface.c)
-//   k_seis       vx, vy, p sampling (seismo_ssg.c)
-//   k_snap       snapshot frame (snap_ssg.c)
+//   k_force_src    force sources before the velocity update (update_v_interior.c:49-71)
+//   k_update_vw    velocity update, 2 or 4 cells per thread (k_update_v: one cell, or
+//                  R rows per thread), CPML / damping frame by predicate
+//                  (update_v_interior.c, update_v_PML.c, update_v_abs.c); advances
+//                  the device step counter
+//   k_wrap_x       periodic x only: ghost columns (exchange_v.c / exchange_s.c, one rank)
+//   k_update_sw    ISO / VTI stress update, 2 or 4 cells per thread (k_update_s: one
+//                  cell), velocity derivatives recomputed from v in registers
+//                  (v_derivatives.c fused away), CPML / damping by predicate
+//   k_tti_fused    TTI stress update in one pass: derivatives of the tile and its
+//                  ring in shared memory, the reference's region order for the
+//                  4-point averages (update_s_elastic_TTI_PML.c); k_tti_deriv +
+//                  k_update_s_tti are the two-kernel form
+//   k_post         per column: div/curl sampling, explosive / moment-tensor sources,
+//                  free surface, NaN probe, v/p sampling (psource.c, eqsource.c,
+//                  surface_elastic.c, surface.c, seismo_ssg.c)
+//   k_snap         snapshot frame (snap_ssg.c)
+// The kernels live in sofi_kernels.cuh; sofi_velocity.cu, sofi_stress_*.cu and
+// sofi_tti.cu instantiate them in separate translation units.
 //
 // Layout: every 2-D field is a padded [NY + 2*HY][pitch] float array with the
-// interior cell (j, i) at ((j-1+HY) * pitch + (i-1+HX)); HX = HY = 8 >= ND + 1.
-// The shot index is the slowest dimension (field = base + shot * fsz). Ghost
-// cells stay zero (or hold the periodic copy), as the reference's edge ranks.
+// interior cell (j, i) at ((j-1+HY) * pitch + (i-1+HX)); HX = HY = 8 >= ND + 1,
+// pitch a multiple of 32 floats. The shot index is the slowest dimension
+// (field = base + shot * fsz). Ghost cells stay zero (or hold the periodic
+// copy), as the reference's edge ranks.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>

@@ -237,8 +237,10 @@ typedef struct {
  * owns, allocating nothing. It has no counterpart in the reference: it exists
  * for callers that cannot allocate device memory (a host process that runs
  * under a fixed memory budget set at start-up, or code already inside a
- * stream capture where a cudaMalloc would break the capture), and runs the
- * same kernels as sofi_run's TTI path.
+ * stream capture where a cudaMalloc would break the capture). It runs the
+ * two-kernel form of the TTI stress update (derivative fields between the
+ * kernels; sofi_run uses it with SOFI_TTI=split, and by default a one-pass
+ * kernel with the same results).
  *
  * The eight derivative fields this update needs between its two kernels live
  * in one array of the library, SOFI_NOALLOC_MAX_CELLS * 8 floats (32 MiB),
