@@ -24,13 +24,13 @@
 void sofih_set_error(const char *fmt, ...);
 
 static const char *SUFFIX[8][8] = {
-    {0}, {0}, {"vp", "vs", "rho"}, {"vp", "vs", "rho", "qp", "qs"}, {"vp", "vs", "rho", "epsilon", "delta"},
+    {"vp", "rho"}, {0}, {"vp", "vs", "rho"}, {"vp", "vs", "rho", "qp", "qs"}, {"vp", "vs", "rho", "epsilon", "delta"},
     {"vp", "vs", "rho", "epsilon", "delta", "qp", "qs"}, {"vp", "vs", "rho", "epsilon", "delta", "theta"},
     {"vp", "vs", "rho", "epsilon", "delta", "theta", "qp", "qs"}};
 
 int sofih_model_suffixes(int weq, const char **names, int max)
 {
-    if (weq < 2 || weq > 7)
+    if (weq < 0 || weq == 1 || weq > 7)
         return 0;
     int n = 0;
     while (n < 8 && SUFFIX[weq][n])

@@ -145,8 +145,8 @@ int sofih_read_par(const char *path, sofih_par *p)
         for (int k = 0; k < 8; k++)
             if (!strcmp(w, names[k]))
                 p->weq = k;
-    if (p->weq < 2) {
-        sofih_set_error("WEQ %s: acoustic media are not supported", w);
+    if (p->weq == 1) {
+        sofih_set_error("WEQ %s: viscoacoustic media are not supported (nor by the reference)", w);
         free(kv);
         return 1;
     }

@@ -256,11 +256,11 @@ int sofih_prepare(const sofih_par *p, const float *vp, const float *vs, const fl
 {
     int weq = p->weq, NX = p->nx, NY = p->ny, L = is_visco(weq) ? p->L : 0;
     *out = NULL;
-    if (weq < 2 || weq > 7 || NX < 1 || NY < 1) {
+    if (weq < 0 || weq == 1 || weq > 7 || NX < 1 || NY < 1) {
         sofih_set_error("prepare: unsupported WEQ %d or empty grid", weq);
         return 1;
     }
-    if (!vp || !vs || !rho || (L && (!qp || !qs)) || (weq >= 4 && (!eps || !del)) || (is_tti(weq) && !theta)) {
+    if (!vp || (!vs && weq != 0) || !rho || (L && (!qp || !qs)) || (weq >= 4 && (!eps || !del)) || (is_tti(weq) && !theta)) {
         sofih_set_error("prepare: missing material arrays for WEQ %d", weq);
         return 1;
     }
@@ -304,7 +304,7 @@ int sofih_prepare(const sofih_par *p, const float *vp, const float *vs, const fl
     for (int i = 1; i <= NX; i++)
         for (int j = 1; j <= NY; j++) {
             size_t k = (size_t)(i - 1) * NY + (j - 1);
-            float v_p = vp[k], v_s = vs[k], r = rho[k];
+            float v_p = vp[k], v_s = vs ? vs[k] : 0.0f, r = rho[k];
             if (v_p > 1.0f) {
                 /* anisotropic media: horizontal P velocity vp*sqrt(1+2 eps) too
                  * (readmod_elastic_tti.c:128-131) */
@@ -318,7 +318,9 @@ int sofih_prepare(const sofih_par *p, const float *vp, const float *vs, const fl
                 vsmax = v_s > vsmax ? v_s : vsmax;
             }
             H(prho, j, i) = r;
-            if (weq == 2) {
+            if (weq == 0) {
+                H(ppi, j, i) = v_p * v_p * r; /* readmod_acoustic.c:121 */
+            } else if (weq == 2) {
                 H(pu, j, i) = v_s * v_s * r;
                 H(ppi, j, i) = v_p * v_p * r;
             } else if (weq == 3) {
@@ -380,7 +382,9 @@ int sofih_prepare(const sofih_par *p, const float *vp, const float *vs, const fl
 
     /* halo + averaging (prepmod.c:42-120) */
     h1 rip = h1_new(NX, NY), rjp = h1_new(NX, NY);
-    if (weq == 2 || weq == 3) {
+    if (weq == 0) {
+        model_halo(p, prho, 0), model_halo(p, ppi, 0); /* matcopy_elastic(prho, ppi, ppi), prepmod.c:41 */
+    } else if (weq == 2 || weq == 3) {
         h1 hs[5] = {prho, ppi, pu, taus, taup};
         for (int k = 0; k < (weq == 3 ? 5 : 3); k++)
             model_halo(p, hs[k], weq == 3);
@@ -398,7 +402,16 @@ int sofih_prepare(const sofih_par *p, const float *vp, const float *vs, const fl
         }
     emit(m, "prip", rip);
     emit(m, "prjp", rjp);
-    if (weq == 2 || weq == 3) {
+    if (weq == 0) {
+        /* prepare_update_s_ac.c:27-34 */
+        h1 g = h1_new(NX, NY);
+#pragma omp parallel for schedule(static)
+        for (int j = 1; j <= NY; j++)
+            for (int i = 1; i <= NX; i++)
+                H(g, j, i) = H(ppi, j, i) * DT;
+        emit(m, "g", g);
+        free(g.p);
+    } else if (weq == 2 || weq == 3) {
         h1 uipjp = harmonic4(p, pu);
         h1 tsip = weq == 3 ? mean4(p, taus) : (h1){0};
         h1 g = h1_new(NX, NY), f = h1_new(NX, NY), fip = h1_new(NX, NY);

@@ -38,7 +38,7 @@ constexpr int MAXL = 8;
 constexpr int BX = 32;  // threads per block in x
 constexpr int BY = 8;   // threads per block in y
 
-enum Kind { ISO = 0, VTI = 1, TTI = 2 };
+enum Kind { ISO = 0, VTI = 1, TTI = 2, AC = 3 };  // AC: acoustic, one pressure field
 
 struct Geo {
     int nx, ny, pitch, nshots;

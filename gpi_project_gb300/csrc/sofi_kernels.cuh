@@ -146,7 +146,9 @@ __global__ void __launch_bounds__(BX *BY, R == 1 ? 8 : 1) k_update_v(Geo G, Wave
 template <int VW>
 __device__ __forceinline__ void ldv(const float *p, float *out)
 {
-    if (VW == 4) {
+    if (VW == 1) {
+        out[0] = __ldg(p);
+    } else if (VW == 4) {
         const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
         out[0] = a.x, out[1] = a.y, out[2] = a.z, out[3] = a.w;
     } else {
@@ -158,7 +160,9 @@ __device__ __forceinline__ void ldv(const float *p, float *out)
 template <int VW>
 __device__ __forceinline__ void ldv_rw(const float *p, float *out)  // arrays this kernel writes
 {
-    if (VW == 4) {
+    if (VW == 1) {
+        out[0] = *p;
+    } else if (VW == 4) {
         const float4 a = *reinterpret_cast<const float4 *>(p);
         out[0] = a.x, out[1] = a.y, out[2] = a.z, out[3] = a.w;
     } else {
@@ -170,7 +174,9 @@ __device__ __forceinline__ void ldv_rw(const float *p, float *out)  // arrays th
 template <int VW>
 __device__ __forceinline__ void stv(float *p, const float *v)
 {
-    if (VW == 4)
+    if (VW == 1)
+        *p = v[0];
+    else if (VW == 4)
         *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
     else
         *reinterpret_cast<float2 *>(p) = make_float2(v[0], v[1]);
@@ -608,6 +614,105 @@ __global__ void __launch_bounds__(BX *BY) k_update_sw(Geo G, Wave W, Model M)
             }
             sxy[o + c] = nxy[c], sxx[o + c] = nxx[c], syy[o + c] = nyy[c];
         }
+    }
+}
+
+// Acoustic stress update (wavefield_update_s_ac.c, update_s_acoustic_{interior,
+// PML,abs}.c), VW cells per thread (1, 2 or 4). The reference allocates one
+// array for sxx and syy (initmem_wavefield.c:34), so the pressure p = sxx = syy
+// gets g*vxx and then g*vyy, rounded in that order; the velocity update reads
+// the same array for its x and y derivatives. CPML stretches vxx in the left /
+// right frame and vyy in the top / bottom frame (cpml_update_s_x_ac,
+// cpml_update_s_y_ac); the damping frame multiplies p once (abs_update_s_ac2).
+template <int ND, int VW>
+__global__ void __launch_bounds__(BX *BY) k_update_s_ac(Geo G, Wave W, Model M)
+{
+    constexpr int K = (ND + VW - 1) / VW;
+    constexpr int NXS = VW * (2 * K + 1);
+    int bx, s;
+    block_xs(G, bx, s);
+    const int i = (bx * BX + threadIdx.x) * VW + 1;
+    const int j = blockIdx.y * BY + threadIdx.y + 1;
+    if (i > G.nx || j > G.ny)
+        return;
+    const int P = G.pitch;
+    const int o = (j - 1 + HY) * P + (i - 1 + HX);
+    const long long so = (long long)s * G.fsz, mo = moff(G, s);
+    float *__restrict__ pr = W.sxx + so;
+    const float *__restrict__ vx = W.vx + so;
+    const float *__restrict__ vy = W.vy + so;
+    const float *hc = G.hc;
+    float vxx[VW], vyy[VW];
+    {
+        float X[NXS];  // X[k] = vx(j, i - VW K + k)
+#pragma unroll
+        for (int q = 0; q < 2 * K + 1; q++)
+            ldv<VW>(vx + o + VW * (q - K), X + VW * q);
+        constexpr int C = VW * K;
+#pragma unroll
+        for (int c = 0; c < VW; c++) {
+            vxx[c] = hc[1] * (X[C + c] - X[C + c - 1]);
+#pragma unroll
+            for (int m = 2; m <= ND; m++)
+                vxx[c] += hc[m] * (X[C + c + m - 1] - X[C + c - m]);
+        }
+    }
+    {
+        float b1[VW], b0[VW];  // vy rows j - ND .. j + ND - 1
+        ldv<VW>(vy + o, b1), ldv<VW>(vy + o - P, b0);
+#pragma unroll
+        for (int c = 0; c < VW; c++)
+            vyy[c] = hc[1] * (b1[c] - b0[c]);
+#pragma unroll
+        for (int m = 2; m <= ND; m++) {
+            ldv<VW>(vy + o + (m - 1) * P, b1), ldv<VW>(vy + o - m * P, b0);
+#pragma unroll
+            for (int c = 0; c < VW; c++)
+                vyy[c] += hc[m] * (b1[c] - b0[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < VW; c++)
+            vxx[c] *= G.dhi, vyy[c] *= G.dhi;
+    }
+    float g[VW], op[VW], np[VW];
+    ldv<VW>(M.g + mo + o, g);
+    ldv_rw<VW>(pr + o, op);
+    const int yr = yside(G, j);
+    const bool xframe = i <= G.gx2 || i + VW - 1 > G.gx3;
+#pragma unroll
+    for (int c = 0; c < VW; c++) {
+        const int ic = i + c;
+        const int xr = xframe ? xside(G, ic) : 0;
+        float dxx = vxx[c], dyy = vyy[c];
+        if (G.abs_type == 1 && ic <= G.nx) {
+            if (xr) {
+                const int h = xr == 1 ? ic : ic - G.nx + G.fw2;
+                const long long q = ((long long)s * G.ny + (j - 1)) * G.fw2 + (h - 1);
+                const float ps = M.b_x[h - 1] * W.psi_vxx[q] + M.a_x[h - 1] * dxx;
+                W.psi_vxx[q] = ps;
+                dxx = dxx / M.K_x[h - 1] + ps;
+            }
+            if (yr) {
+                const int h = yr == 1 ? j : j - G.ny + G.fw2;
+                const long long q = ((long long)s * G.fw2 + (h - 1)) * G.nx + (ic - 1);
+                const float ps = M.b_y[h - 1] * W.psi_vyy[q] + M.a_y[h - 1] * dyy;
+                W.psi_vyy[q] = ps;
+                dyy = dyy / M.K_y[h - 1] + ps;
+            }
+        }
+        float t = op[c] + g[c] * dxx;
+        t = t + g[c] * dyy;
+        if (G.abs_type == 2 && (xr | yr))
+            t *= __ldg(M.absorb + mo + o + c);
+        np[c] = t;
+    }
+    if (i + VW - 1 <= G.nx) {
+        stv<VW>(pr + o, np);
+    } else {
+#pragma unroll
+        for (int c = 0; c < VW; c++)
+            if (i + c <= G.nx)
+                pr[o + c] = np[c];
     }
 }
 

@@ -18,6 +18,8 @@ void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw
 // ISO / VTI stress update (KIND 0 ISO, 1 VTI): sw cells per thread in x (4, 2 or 0 = one)
 template <int KIND, bool VISCO>
 void launch_stress_kv(const Geo &G, const Wave &W, const Model &M, int nd, int sw, dim3 grid, cudaStream_t st);
+// acoustic stress update: sw cells per thread in x (4, 2 or 0/1 = one)
+void launch_stress_ac(const Geo &G, const Wave &W, const Model &M, int nd, int sw, dim3 grid, cudaStream_t st);
 // TTI stress update: one pass (derivatives in shared memory) or the two-kernel
 // form (derivative fields in W.draw / W.dcor)
 void launch_tti_fused(const Geo &G, const Wave &W, const Model &M, int nd, bool visco, bool cpml, dim3 grid,

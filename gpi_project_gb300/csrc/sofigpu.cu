@@ -86,7 +86,12 @@ const double kHolberg[5][6][7] = {
 };
 
 bool is_visco(int weq) { return weq == SOFI_VEL_ISO || weq == SOFI_VEL_VTI || weq == SOFI_VEL_TTI; }
-int kind_of(int weq) { return (weq == SOFI_EL_ISO || weq == SOFI_VEL_ISO) ? ISO : (weq <= SOFI_VEL_VTI ? VTI : TTI); }
+int kind_of(int weq)
+{
+    if (weq == SOFI_AC_ISO)
+        return AC;
+    return (weq == SOFI_EL_ISO || weq == SOFI_VEL_ISO) ? ISO : (weq <= SOFI_VEL_VTI ? VTI : TTI);
+}
 
 struct FieldSlot {
     const char *name;   // ABI name
@@ -115,9 +120,16 @@ const char *kVectors[12] = {"K_x", "a_x", "b_x", "K_x_half", "a_x_half", "b_x_ha
 // which model slots a wave equation reads
 std::vector<std::string> needed_fields(const sofi_config &c)
 {
-    std::vector<std::string> v = {"prip", "prjp", "ppi", "pu"};
     int k = kind_of(c.weq);
     bool visco = is_visco(c.weq);
+    if (k == AC) {
+        // initmem_model.c:33-39: the acoustic model has no mu
+        std::vector<std::string> a = {"prip", "prjp", "g"};
+        if (c.fw > 0 && c.abs_type == 2)
+            a.push_back("absorb");
+        return a;
+    }
+    std::vector<std::string> v = {"prip", "prjp", "ppi", "pu"};
     if (k == ISO) {
         v.insert(v.end(), {"g", "f", "fipjp"});
         if (visco) {
@@ -245,7 +257,8 @@ long long fields_bytes(const sofi_config &c)
     // the two-kernel form (SOFI_TTI=split) holds 8 derivative fields instead
     const char *e = getenv("SOFI_TTI");
     const bool tti = kind_of(c.weq) == TTI, split = tti && e && strcmp(e, "split") == 0;
-    long long per_shot = 5 + 3LL * (is_visco(c.weq) ? c.L : 0) + (split ? 8 : 0);
+    // acoustic: sxx and syy are one array
+    long long per_shot = (c.weq == SOFI_AC_ISO ? 4 : 5) + 3LL * (is_visco(c.weq) ? c.L : 0) + (split ? 8 : 0);
     long long fw2 = 2LL * c.fw;
     long long psi = (c.abs_type == 1 && c.fw > 0) ? (tti && !split ? 6 : 4) * ((long long)c.ny * fw2 + fw2 * c.nx) : 0;
     long long nmod = c.shared_model ? 1 : c.nshots;
@@ -263,8 +276,13 @@ int check_config(const sofi_config *c)
 {
     if (!c)
         return fail(SOFI_E_ARG, "null config");
-    if (c->weq < SOFI_EL_ISO || c->weq > SOFI_VEL_TTI)
-        return fail(SOFI_E_ARG, "unsupported WEQ %d (EL_ISO..VEL_TTI = 2..7)", c->weq);
+    if (c->weq < SOFI_AC_ISO || c->weq == 1 || c->weq > SOFI_VEL_TTI)
+        return fail(SOFI_E_ARG, "unsupported WEQ %d (AC_ISO = 0, EL_ISO..VEL_TTI = 2..7)", c->weq);
+    // the reference allocates neither mu nor sxy for acoustic media
+    // (initmem_model.c:33-39, initmem_wavefield.c:32-39): its free surface and
+    // div/curl outputs would read them
+    if (c->weq == SOFI_AC_ISO && (c->free_surf || c->seismo >= 3 || c->snap >= 3))
+        return fail(SOFI_E_ARG, "acoustic media: no free surface and no div/curl (SEISMO, SNAP <= 2)");
     if (c->fdorder < 2 || c->fdorder > 12 || (c->fdorder & 1))
         return fail(SOFI_E_ARG, "FDORDER must be 2,4,..,12 (got %d)", c->fdorder);
     if (c->maxrelerror < 0 || c->maxrelerror > 4)
@@ -430,7 +448,9 @@ void launch_cell_s(const Geo &G, const Wave &W, const Model &M, int nd, int kind
     const int cx = sw ? sw : 1;
     const unsigned tx = (nx + cx * BX - 1) / (cx * BX), ty = (ny + BY - 1) / BY;
     const dim3 grd = G.shot_fast ? dim3(tx * nshots, ty, 1) : dim3(tx, ty, nshots);
-    if (kind == ISO)
+    if (kind == AC)
+        launch_stress_ac(G, W, M, nd, sw, grd, st);
+    else if (kind == ISO)
         visco ? launch_stress_kv<ISO, true>(G, W, M, nd, sw, grd, st) : launch_stress_kv<ISO, false>(G, W, M, nd, sw, grd, st);
     else
         visco ? launch_stress_kv<VTI, true>(G, W, M, nd, sw, grd, st) : launch_stress_kv<VTI, false>(G, W, M, nd, sw, grd, st);
@@ -597,7 +617,7 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
         launch_tti_split(G, c->W, c->M, c->nd, visco, grd, st);
     } else if (kind == TTI) {
         launch_tti_fused(G, c->W, c->M, c->nd, visco, G.abs_type == 1, grd, st);
-    } else if (c->march) {
+    } else if (c->march && kind != AC) {
         launch_march_s(G, c->W, c->M, c->nd, kind, visco, c->march_sy, st);
     } else {
         launch_cell_s(G, c->W, c->M, c->nd, kind, visco, c->sw, cf.nx, cf.ny, S, st);
@@ -816,9 +836,14 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
     // wavefields
     size_t f = (size_t)G.fsz * cfg->nshots * sizeof(float);
     float **w[5] = {&c->W.vx, &c->W.vy, &c->W.sxx, &c->W.syy, &c->W.sxy};
-    for (auto p : w)
+    for (auto p : w) {
+        if (p == &c->W.syy && cfg->weq == SOFI_AC_ISO)
+            continue;  // initmem_wavefield.c:34: one pressure array
         if ((rc = dalloc(c, (void **)p, f)))
             goto bad;
+    }
+    if (cfg->weq == SOFI_AC_ISO)
+        c->W.syy = c->W.sxx;
     if (G.L) {
         float **m[3] = {&c->W.r, &c->W.p, &c->W.q};
         for (auto p : m)

@@ -14,7 +14,7 @@ import numpy as np
 
 from . import _native as N
 
-WEQ = {"EL_ISO": 2, "VEL_ISO": 3, "EL_VTI": 4, "VEL_VTI": 5, "EL_TTI": 6, "VEL_TTI": 7}
+WEQ = {"AC_ISO": 0, "EL_ISO": 2, "VEL_ISO": 3, "EL_VTI": 4, "VEL_VTI": 5, "EL_TTI": 6, "VEL_TTI": 7}
 COMP = {"vx": 1, "vy": 2, "p": 3, "div": 4, "curl": 5}
 
 

@@ -45,6 +45,7 @@ extern "C" {
 #define SOFI_E_BUSY 7      /* device work of the context still in flight */
 
 /* wave equations: reference src/enums.h:22-31 */
+#define SOFI_AC_ISO 0      /* acoustic: one pressure field; no free surface, no div/curl */
 #define SOFI_EL_ISO 2
 #define SOFI_VEL_ISO 3
 #define SOFI_EL_VTI 4

@@ -125,7 +125,12 @@ static int is_visco(int weq)
 
 static int is_iso(int weq)
 {
-    return weq == ORC_EL_ISO || weq == ORC_VEL_ISO;
+    return weq == ORC_AC_ISO || weq == ORC_EL_ISO || weq == ORC_VEL_ISO;
+}
+
+static int is_ac(int weq)
+{
+    return weq == ORC_AC_ISO;
 }
 
 static int is_vti(int weq)
@@ -189,6 +194,11 @@ orc_ctx *orc_create(const orc_params *p)
      * viscoelastic readers never fill. */
     if ((is_visco(p->weq) && p->L < 1) || (p->free_surf && is_visco(p->weq) && !is_iso(p->weq)))
         return NULL;
+    /* Acoustic media have no mu and no sxy (initmem_model.c:33-39,
+     * initmem_wavefield.c:32-39); the free surface (surface_elastic.c) and
+     * the div/curl outputs (seismo_ssg.c:49-59, snap_ssg.c:166) read them. */
+    if (is_ac(p->weq) && (p->free_surf || p->seismo >= 3 || p->snap >= 3))
+        return NULL;
     orc_ctx *c = (orc_ctx *)calloc(1, sizeof(orc_ctx));
     c->P = *p;
     if (!is_visco(p->weq))
@@ -233,6 +243,12 @@ orc_ctx *orc_create(const orc_params *p)
     if (!is_iso(p->weq)) {
         free2(&c->ppi), free2(&c->pu), free2(&c->puipjp);
         c->ppi = c->pc11, c->pu = c->pc55, c->puipjp = c->pc55ipjp;
+    }
+    /* initmem_wavefield.c:34: the acoustic psyy is psxx (one pressure field,
+     * updated by g*vxx and then by g*vyy); sxy stays zero */
+    if (is_ac(p->weq)) {
+        free2(&c->syy);
+        c->syy = c->sxx;
     }
     for (int l = 1; l <= L; l++) {
         c->dip[l] = alloc2(c), c->d[l] = alloc2(c), c->e[l] = alloc2(c);
@@ -282,6 +298,8 @@ void orc_destroy(orc_ctx *c)
         return;
     if (!is_iso(c->P.weq))
         c->ppi.p = c->pu.p = c->puipjp.p = NULL; /* aliases of pc11/pc55/pc55ipjp */
+    if (is_ac(c->P.weq))
+        c->syy.p = NULL; /* alias of sxx */
     arr2 *all[] = {&c->prho, &c->ppi, &c->pu, &c->ptaus, &c->ptaup, &c->prip, &c->prjp, &c->puipjp,
                    &c->ptausipjp, &c->g, &c->f, &c->fipjp, &c->absorb, &c->pc11, &c->pc13, &c->pc33,
                    &c->pc55, &c->pc15, &c->pc35, &c->pc55ipjp, &c->pc15ipjp, &c->pc35ipjp, &c->ptau11,
@@ -365,6 +383,17 @@ static void readmod_elastic(orc_ctx *c)
         for (int j = 1; j <= c->P.ny; j++) {
             real vp = MAT(c->mat_vp, j, i), vs = MAT(c->mat_vs, j, i), rho = MAT(c->mat_rho, j, i);
             A(c->pu, j, i) = vs * vs * rho;
+            A(c->prho, j, i) = rho;
+            A(c->ppi, j, i) = vp * vp * rho;
+        }
+}
+
+/* readmod_acoustic.c:105-122 */
+static void readmod_acoustic(orc_ctx *c)
+{
+    for (int i = 1; i <= c->P.nx; i++)
+        for (int j = 1; j <= c->P.ny; j++) {
+            real vp = MAT(c->mat_vp, j, i), rho = MAT(c->mat_rho, j, i);
             A(c->prho, j, i) = rho;
             A(c->ppi, j, i) = vp * vp * rho;
         }
@@ -566,7 +595,9 @@ static void prepare_update(orc_ctx *c)
     }
     for (int j = 1; j <= c->P.ny; j++)
         for (int i = 1; i <= c->P.nx; i++) {
-            if (weq == ORC_EL_ISO) {
+            if (weq == ORC_AC_ISO) {
+                A(c->g, j, i) = A(c->ppi, j, i) * DT; /* prepare_update_s_ac.c:27-34 */
+            } else if (weq == ORC_EL_ISO) {
                 A(c->fipjp, j, i) = A(c->puipjp, j, i) * DT;
                 A(c->f, j, i) = A(c->pu, j, i) * DT;
                 A(c->g, j, i) = A(c->ppi, j, i) * DT;
@@ -620,6 +651,12 @@ static void prepmod(orc_ctx *c)
 {
     int weq = c->P.weq;
     switch (weq) {
+      case ORC_AC_ISO: {
+          arr2 m[3] = {c->prho, c->ppi, c->ppi}; /* prepmod.c:40-43 */
+          matcopy_wrap(c, m, 3, 0);
+          av_rho(c);
+          break;
+      }
       case ORC_EL_ISO: {
           arr2 m[3] = {c->prho, c->ppi, c->pu};
           matcopy_wrap(c, m, 3, 0);
@@ -830,7 +867,7 @@ static void absorb(orc_ctx *c)
 int orc_prepare(orc_ctx *c)
 {
     int weq = c->P.weq;
-    if (!c->mat_vp || !c->mat_vs || !c->mat_rho) {
+    if (!c->mat_vp || (!c->mat_vs && !is_ac(weq)) || !c->mat_rho) {
         snprintf(c->err, sizeof c->err, "vp/vs/rho missing");
         return 1;
     }
@@ -842,7 +879,9 @@ int orc_prepare(orc_ctx *c)
         snprintf(c->err, sizeof c->err, "anisotropy parameters missing");
         return 1;
     }
-    if (weq == ORC_EL_ISO)
+    if (weq == ORC_AC_ISO)
+        readmod_acoustic(c);
+    else if (weq == ORC_EL_ISO)
         readmod_elastic(c);
     else if (weq == ORC_VEL_ISO)
         readmod_visco(c);
@@ -1277,9 +1316,18 @@ static inline void wf_s_visc_tti(orc_ctx *c, int i, int j)
     A(c->syy, j, i) += u3;
 }
 
+/* wavefield_update_s_ac.c:27-33: sxx and syy are one array, so the pressure
+ * gets g*vxx and then g*vyy */
+static inline void wf_s_ac(orc_ctx *c, int i, int j)
+{
+    A(c->sxx, j, i) += (A(c->g, j, i) * A(c->vxx, j, i));
+    A(c->syy, j, i) += (A(c->g, j, i) * A(c->vyy, j, i));
+}
+
 static inline void wf_s(orc_ctx *c, int i, int j)
 {
     switch (c->P.weq) {
+      case ORC_AC_ISO: wf_s_ac(c, i, j); break;
       case ORC_EL_ISO: wf_s_el(c, i, j); break;
       case ORC_VEL_ISO: wf_s_visc(c, i, j); break;
       case ORC_EL_VTI: wf_s_el_vti(c, i, j); break;
@@ -1316,7 +1364,9 @@ static void s_region(orc_ctx *c, int j0, int j1, int i0, int i1, int modex, int 
             if (modey == 1) cpml_s_y(c, i, j, j);
             else if (modey == 2) cpml_s_y(c, i, j, j - NY + 2 * FW);
             wf_s(c, i, j);
-            if (damp) { /* abs_update.c:39-44 */
+            if (damp && is_ac(c->P.weq)) { /* abs_update.c:28-31 (abs_update_s_ac2): once */
+                A(c->sxx, j, i) *= A(c->absorb, j, i);
+            } else if (damp) { /* abs_update.c:39-44 */
                 A(c->sxy, j, i) *= A(c->absorb, j, i);
                 A(c->syy, j, i) *= A(c->absorb, j, i);
                 A(c->sxx, j, i) *= A(c->absorb, j, i);

@@ -14,7 +14,7 @@ import os
 
 import numpy as np
 
-WEQ_NAMES = {2: "EL_ISO", 3: "VEL_ISO", 4: "EL_VTI", 5: "VEL_VTI", 6: "EL_TTI", 7: "VEL_TTI"}
+WEQ_NAMES = {0: "AC_ISO", 2: "EL_ISO", 3: "VEL_ISO", 4: "EL_VTI", 5: "VEL_VTI", 6: "EL_TTI", 7: "VEL_TTI"}
 
 
 def _case(name, **kw):
@@ -50,6 +50,12 @@ CASES = [
                    [121.0, 99.0, 0.0, 40.0, 1.5, 0.0, 1.0]]),
     _case("el_moment_tensor", fdorder=4, seed=26, source_type=1,
           sources=[[121.0, 99.0, 0.0, 40.0, 1.0, 35.0, 5.0]]),
+    # acoustic (WEQ = AC_ISO): one pressure field; no free surface and no
+    # div/curl output (the reference has no mu and no sxy for it)
+    _case("ac_cpml_fd8", weq=0, fdorder=8, maxrelerror=1, seismo=2, snap=1, seed=31),
+    _case("ac_abs_fd4", weq=0, fdorder=4, abs_type=2, seismo=1, snap=2, seed=32),
+    _case("ac_periodic_force", weq=0, fdorder=6, boundary=1, seismo=1, snap=0, seed=33, source_type=2,
+          sources=[[121.0, 99.0, 0.0, 40.0, 1.0, 0.0, 2.0], [141.0, 111.0, 0.0, 35.0, 1.0, 0.0, 3.0]]),
 ]
 
 

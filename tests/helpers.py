@@ -165,7 +165,10 @@ def gpu_config_from(cfg, nshots=1, shared_model=1, snap_override=None):
 def prepared_model(o, cfg):
     """The prepared arrays the GPU kernels read, taken from an oracle context."""
     weq, L = cfg.weq, cfg.L
-    f = {k: o.field(k) for k in ISO_FIELDS}
+    if weq == 0:  # acoustic: no mu
+        f = {k: o.field(k) for k in ["prip", "prjp", "g"]}
+    else:
+        f = {k: o.field(k) for k in ISO_FIELDS}
     if weq in (2, 3):
         for k in ["g", "f", "fipjp"]:
             f[k] = o.field(k)
@@ -175,7 +178,7 @@ def prepared_model(o, cfg):
             f["dip_base"] = o.field("puipjp") * o.field("tausipjp")
             if cfg.free_surf:
                 f["taus"], f["taup"] = o.field("taus"), o.field("taup")
-    else:
+    elif weq != 0:
         names = ["c11", "c13", "c33", "c55ipjp"] + (["c15", "c35", "c15ipjp", "c35ipjp"] if weq in (6, 7) else [])
         visco = weq in (5, 7)
         for k in names:

@@ -233,7 +233,8 @@ def test_autotuned_run_equals_fixed_variant(name, monkeypatch):
 
 
 @pytest.mark.parametrize("name", ["el_cpml_fd8", "el_abs_fd10", "el_cpml_fd12", "visc_cpml_fs_l3", "visc_abs_l1",
-                                  "vti_cpml", "vvti_cpml_l2", "el_periodic_cpml"])
+                                  "vti_cpml", "vvti_cpml_l2", "el_periodic_cpml", "ac_cpml_fd8", "ac_abs_fd4",
+                                  "ac_periodic_force"])
 def test_stress_kernel_vector_widths_match_one_cell(name, monkeypatch):
     """The vector stress kernels (four or two cells per thread) and the one-cell
     kernel compute the same step, to float32 rounding grown over the run (the
