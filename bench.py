@@ -434,7 +434,8 @@ def main():
     ncell = par["nx"] * par["ny"] * nshots
     ach_s = bpc["update_s"] * ncell / (ms_s * 1e-3) / 1e9 if ms_s else None
     traffic = traffic_from_profiles("update_s", W["name"])
-    roof = {"kernel": "k_update_s (stress + memory variables)", "bound": "hbm",
+    kname = {0: "k_update_s_ac (pressure)", 6: "k_tti_fused (TTI stress)", 7: "k_tti_fused (TTI stress + memory variables)"}
+    roof = {"kernel": kname.get(par["weq"], "k_update_sw / k_update_s (stress + memory variables)"), "bound": "hbm",
             "achieved": round(ach_s, 1) if ach_s else None, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
             "frac": round(ach_s / peak, 4) if ach_s else None,
             "traffic": round(traffic * ncell) if traffic else None,

@@ -182,7 +182,10 @@ __device__ __forceinline__ void stv(float *p, const float *v)
         *reinterpret_cast<float2 *>(p) = make_float2(v[0], v[1]);
 }
 
-template <int ND, int VW>
+// SXY = false: the acoustic update (wavefield_update_v_ac.c), which has no
+// sxy: vx += sxx_x * DT/DH * rip, vy += syy_y * DT/DH * rjp (sxx and syy are
+// one pressure array); VW may then also be 1.
+template <int ND, int VW, bool SXY = true>
 __global__ void __launch_bounds__(BX *BY) k_update_vw(Geo G, Wave W, Model M)
 {
     constexpr int K = (ND + VW - 1) / VW;
@@ -208,37 +211,42 @@ __global__ void __launch_bounds__(BX *BY) k_update_vw(Geo G, Wave W, Model M)
 #pragma unroll
         for (int q = 0; q < 2 * K + 1; q++) {
             ldv<VW>(sxx + o + VW * (q - K), X + VW * q);
-            ldv<VW>(sxy + o + VW * (q - K), Y + VW * q);
+            if (SXY)
+                ldv<VW>(sxy + o + VW * (q - K), Y + VW * q);
         }
         constexpr int C = VW * K;  // index of column i
 #pragma unroll
         for (int c = 0; c < VW; c++) {
             sxx_x[c] = hc[1] * (X[C + c + 1] - X[C + c]);
-            sxy_x[c] = hc[1] * (Y[C + c] - Y[C + c - 1]);
+            sxy_x[c] = SXY ? hc[1] * (Y[C + c] - Y[C + c - 1]) : 0.f;
 #pragma unroll
             for (int m = 2; m <= ND; m++) {
                 sxx_x[c] += hc[m] * (X[C + c + m] - X[C + c - m + 1]);
-                sxy_x[c] += hc[m] * (Y[C + c + m - 1] - Y[C + c - m]);
+                if (SXY)
+                    sxy_x[c] += hc[m] * (Y[C + c + m - 1] - Y[C + c - m]);
             }
         }
     }
     {
         // y stencils: sxy rows j - ND .. j + ND - 1, syy rows j - ND + 1 .. j + ND
         float a1[VW], a0[VW], b1[VW], b0[VW];
-        ldv<VW>(sxy + o, a1), ldv<VW>(sxy + o - P, a0);
+        if (SXY)
+            ldv<VW>(sxy + o, a1), ldv<VW>(sxy + o - P, a0);
         ldv<VW>(syy + o + P, b1), ldv<VW>(syy + o, b0);
 #pragma unroll
         for (int c = 0; c < VW; c++) {
-            sxy_y[c] = hc[1] * (a1[c] - a0[c]);
+            sxy_y[c] = SXY ? hc[1] * (a1[c] - a0[c]) : 0.f;
             syy_y[c] = hc[1] * (b1[c] - b0[c]);
         }
 #pragma unroll
         for (int m = 2; m <= ND; m++) {
-            ldv<VW>(sxy + o + (m - 1) * P, a1), ldv<VW>(sxy + o - m * P, a0);
+            if (SXY)
+                ldv<VW>(sxy + o + (m - 1) * P, a1), ldv<VW>(sxy + o - m * P, a0);
             ldv<VW>(syy + o + m * P, b1), ldv<VW>(syy + o - (m - 1) * P, b0);
 #pragma unroll
             for (int c = 0; c < VW; c++) {
-                sxy_y[c] += hc[m] * (a1[c] - a0[c]);
+                if (SXY)
+                    sxy_y[c] += hc[m] * (a1[c] - a0[c]);
                 syy_y[c] += hc[m] * (b1[c] - b0[c]);
             }
         }
@@ -263,9 +271,11 @@ __global__ void __launch_bounds__(BX *BY) k_update_vw(Geo G, Wave W, Model M)
                 float ps = M.b_x_half[h - 1] * W.psi_sxx_x[q] + M.a_x_half[h - 1] * fx;
                 W.psi_sxx_x[q] = ps;
                 fx = fx / M.K_x_half[h - 1] + ps;
-                float py = M.b_x[h - 1] * W.psi_sxy_x[q] + M.a_x[h - 1] * fxy;
-                W.psi_sxy_x[q] = py;
-                fxy = fxy / M.K_x[h - 1] + py;
+                if (SXY) {
+                    float py = M.b_x[h - 1] * W.psi_sxy_x[q] + M.a_x[h - 1] * fxy;
+                    W.psi_sxy_x[q] = py;
+                    fxy = fxy / M.K_x[h - 1] + py;
+                }
             }
             if (yr) {
                 int h = yr == 1 ? j : j - G.ny + G.fw2;
@@ -273,13 +283,20 @@ __global__ void __launch_bounds__(BX *BY) k_update_vw(Geo G, Wave W, Model M)
                 float ps = M.b_y_half[h - 1] * W.psi_syy_y[q] + M.a_y_half[h - 1] * fy;
                 W.psi_syy_y[q] = ps;
                 fy = fy / M.K_y_half[h - 1] + ps;
-                float py = M.b_y[h - 1] * W.psi_sxy_y[q] + M.a_y[h - 1] * fyx;
-                W.psi_sxy_y[q] = py;
-                fyx = fyx / M.K_y[h - 1] + py;
+                if (SXY) {
+                    float py = M.b_y[h - 1] * W.psi_sxy_y[q] + M.a_y[h - 1] * fyx;
+                    W.psi_sxy_y[q] = py;
+                    fyx = fyx / M.K_y[h - 1] + py;
+                }
             }
         }
-        nvx[c] = ox[c] + (fx + fyx) * G.dtdh * rp[c];
-        nvy[c] = oy[c] + (fxy + fy) * G.dtdh * rq[c];
+        if (SXY) {
+            nvx[c] = ox[c] + (fx + fyx) * G.dtdh * rp[c];
+            nvy[c] = oy[c] + (fxy + fy) * G.dtdh * rq[c];
+        } else {
+            nvx[c] = ox[c] + fx * G.dtdh * rp[c];
+            nvy[c] = oy[c] + fy * G.dtdh * rq[c];
+        }
         if (G.abs_type == 2 && (xr | yr)) {
             float a = __ldg(M.absorb + mo + o + c);
             nvx[c] *= a;

@@ -12,9 +12,10 @@ void launch_march_v(const Geo &G, const Wave &W, const Model &M, int nd, int sy,
 // stress update of isotropic / VTI media, y-marching
 void launch_march_s(const Geo &G, const Wave &W, const Model &M, int nd, int kind, bool visco, int sy,
                     cudaStream_t st);
-// velocity update: vw cells per thread in x (4 or 2), else vrows rows per thread (1, 2, 4)
-void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw, int vrows, dim3 grid,
-                     cudaStream_t st);
+// velocity update: vw cells per thread in x (4 or 2), else vrows rows per thread (1, 2, 4);
+// acoustic: no sxy terms, vw 4, 2 or else one cell per thread
+void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw, int vrows, bool acoustic,
+                     dim3 grid, cudaStream_t st);
 // ISO / VTI stress update (KIND 0 ISO, 1 VTI): sw cells per thread in x (4, 2 or 0 = one)
 template <int KIND, bool VISCO>
 void launch_stress_kv(const Geo &G, const Wave &W, const Model &M, int nd, int sw, dim3 grid, cudaStream_t st);

@@ -5,10 +5,19 @@
 
 namespace sofi {
 
-void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw, int vrows, dim3 gv,
-                     cudaStream_t st)
+void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw, int vrows, bool acoustic,
+                     dim3 gv, cudaStream_t st)
 {
     const dim3 blk(BX, BY);
+    if (acoustic) {
+        if (vw == 4)
+            DISPATCH_ND(nd, (k_update_vw<ND, 4, false><<<gv, blk, 0, st>>>(G, W, M)))
+        else if (vw == 2)
+            DISPATCH_ND(nd, (k_update_vw<ND, 2, false><<<gv, blk, 0, st>>>(G, W, M)))
+        else
+            DISPATCH_ND(nd, (k_update_vw<ND, 1, false><<<gv, blk, 0, st>>>(G, W, M)))
+        return;
+    }
     if (vw == 4)
         DISPATCH_ND(nd, (k_update_vw<ND, 4><<<gv, blk, 0, st>>>(G, W, M)))
     else if (vw == 2)

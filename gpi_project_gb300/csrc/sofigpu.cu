@@ -468,10 +468,11 @@ void launch_v(sofi_ctx *c, const Geo &G, cudaStream_t st)
         launch_march_v(G, c->W, c->M, c->nd, c->march_sy, st);
         return;
     }
-    const int R = c->vw ? 1 : c->vrows, cx = c->vw ? c->vw : 1;
+    const bool ac = cf.weq == SOFI_AC_ISO;  // acoustic: one cell per thread when not vectorised
+    const int R = (c->vw || ac) ? 1 : c->vrows, cx = c->vw ? c->vw : 1;
     const unsigned tx = (cf.nx + cx * BX - 1) / (cx * BX), ty = (cf.ny + BY * R - 1) / (BY * R);
     const dim3 gv = G.shot_fast ? dim3(tx * S, ty, 1) : dim3(tx, ty, S);
-    launch_velocity(G, c->W, c->M, c->nd, c->vw, R, gv, st);
+    launch_velocity(G, c->W, c->M, c->nd, c->vw, R, ac, gv, st);
 }
 
 // Autotuner of the velocity and (ISO / VTI) stress kernels. Which variant is

@@ -16,6 +16,9 @@ benchmark configurations with their shapes, sizes and value distributions:
       tilt 0-45 deg, each field smoothed by a Gaussian of sigma 20 cells; explosive Ricker 20 Hz; 512 receivers
   c4  64 shots on the c1 layered model enlarged to 2000 x 1000 with c2's Q field
       and L = 3, NT 4000, explosive sources spread across the surface
+  ac  acoustic (AC_ISO) on c2's geometry: 4000 x 2000, DH 2 m, DT 2e-4 s, NT 6000,
+      FD8, CPML 30; c2's smooth Vp field and Gardner density; explosive Ricker
+      15 Hz; 1000 receivers recording pressure
 Values are drawn from numpy's PCG64 with seed 1000 + config number.
 """
 from __future__ import annotations
@@ -105,6 +108,18 @@ def workload(name: str) -> dict:
         xs = np.linspace(21 * 2.5, (nx - 22) * 2.5, 512)
         rec = (np.floor(xs / 2.5).astype(np.int32) + 1, np.full(512, 25, np.int32))
         nshots = 1
+    elif name == "ac":
+        rng = np.random.default_rng(1002)
+        nx, ny = 4000, 2000
+        vp = smooth_field(rng, nx, ny, 60, 1500.0, 4500.0)
+        rho = (310.0 * vp.astype(np.float64) ** 0.25).astype(np.float32)
+        par = dict(weq=0, nx=nx, ny=ny, dh=2.0, dt=2e-4, nt=6000, fdorder=8, maxrelerror=1, fw=30, abs_type=1,
+                   npower=4.0, k_max_cpml=1.0, vppml=4500.0, fpml=15.0, seismo=2, ndt=1)
+        mats = dict(vp=vp, rho=rho)
+        src = _srcpos([(4000.0, 100.0)], 2.0, 15.0, 1)
+        xs = np.linspace(31 * 2.0, (nx - 32) * 2.0, 1000)
+        rec = (np.floor(xs / 2.0).astype(np.int32) + 1, np.full(1000, 40, np.int32))
+        nshots = 1
     elif name == "c4":
         rng = np.random.default_rng(1004)
         nx, ny = 2000, 1000
@@ -130,6 +145,8 @@ def workload(name: str) -> dict:
 # and receivers not credited).
 def bytes_per_cell(weq: int, L: int) -> dict:
     """Per-kernel and whole-step algorithmic bytes of one cell-update."""
+    if weq == 0:  # acoustic: vx, vy, p; rip, rjp, g
+        return {"update_v": 28, "update_s": 20, "step": 36}
     if weq == 2:
         return {"update_v": 36, "update_s": 44, "step": 60}
     if weq == 3:
