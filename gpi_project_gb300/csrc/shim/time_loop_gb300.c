@@ -13,7 +13,7 @@
  * the receivers acq->recpos_loc[1..2][1..NTR]; outputs gv->SECTION*[1..NTR][1..NS],
  * the final wavefield in *mpw and the snapshot files of snap().
  * Supported: MODE=FW (sw = 0), FDORDER_TIME = 2, one domain (NPROCX = NPROCY = 1),
- * WEQ EL_ISO..VEL_TTI; anything else stops the run through log_fatal like the
+ * WEQ AC_ISO and EL_ISO..VEL_TTI; anything else stops the run through log_fatal like the
  * reference's own checks. The GPU context (device 0, or $SOFI_GPU_DEVICE)
  * is created on the first call and reused while the configuration holds;
  * the model is uploaded once per iteration `iter` (prepmod runs per iteration).
@@ -59,8 +59,13 @@ static void upload_model(MemModel *mpm, GlobVar *gv, float *hc)
     GPU_CHECK(sofi_set_hc(g_ctx, hc));
     upload("prip", mpm->prip, gv);
     upload("prjp", mpm->prjp, gv);
-    upload("ppi", mpm->ppi, gv);
-    upload("pu", mpm->pu, gv);
+    if (weq == AC_ISO) {
+        /* initmem_model.c:33-39: no mu; g = ppi * DT (prepare_update_s_ac.c) */
+        upload("g", mpm->g, gv);
+    } else {
+        upload("ppi", mpm->ppi, gv);
+        upload("pu", mpm->pu, gv);
+    }
     if (weq == EL_ISO || weq == VEL_ISO) {
         upload("g", mpm->g, gv);
         upload("f", mpm->f, gv);
@@ -74,7 +79,7 @@ static void upload_model(MemModel *mpm, GlobVar *gv, float *hc)
                 upload("taup", mpm->ptaup, gv);
             }
         }
-    } else {
+    } else if (weq != AC_ISO) {
         int tti = (weq == EL_TTI || weq == VEL_TTI), visco = (weq == VEL_VTI || weq == VEL_TTI);
         if (!visco) {
             upload("c11", mpm->pc11, gv);
