@@ -40,12 +40,70 @@ int sofih_model_suffixes(int weq, const char **names, int max)
     return n;
 }
 
+/* One model in SU format (readmod_elastic.c:62-96 with read_su.c): NX traces
+ * of at least NY samples, 240-byte headers, native endian; ns from the first
+ * header. out: [NX][NY], y fastest. */
+static int read_su_model(const char *path, int nx, int ny, float *out)
+{
+    FILE *fp = fopen(path, "rb");
+    if (!fp) {
+        sofih_set_error("cannot open model file %s", path);
+        return 1;
+    }
+    unsigned char h[240];
+    unsigned short ns = 0;
+    if (fread(h, 1, 240, fp) != 240) {
+        fclose(fp);
+        sofih_set_error("short read in SU file %s", path);
+        return 1;
+    }
+    memcpy(&ns, h + 114, 2);
+    fseek(fp, 0, SEEK_END);
+    long size = ftell(fp);
+    long tracelen = 240 + 4L * ns;
+    long ntr = ns ? size / tracelen : 0;
+    if (ns < 1 || ntr < nx || ns < ny) {
+        fclose(fp);
+        sofih_set_error("%s: %ld traces of %u samples, NX=%d traces of NY=%d samples needed", path, ntr,
+                        (unsigned)ns, nx, ny);
+        return 1;
+    }
+    float *tr = (float *)malloc(sizeof(float) * ns);
+    int bad = !tr;
+    for (int i = 0; i < nx && !bad; i++) {
+        bad = fseek(fp, (long)i * tracelen + 240, SEEK_SET) != 0 || fread(tr, sizeof(float), ns, fp) != ns;
+        if (!bad)
+            memcpy(out + (size_t)i * ny, tr, sizeof(float) * (size_t)ny);
+    }
+    free(tr);
+    fclose(fp);
+    if (bad) {
+        sofih_set_error("short read in SU file %s", path);
+        return 1;
+    }
+    return 0;
+}
+
 int sofih_read_model(const sofih_par *p, const char *mfile, float **out, int max)
 {
     const char *names[8];
     int n = sofih_model_suffixes(p->weq, names, 8);
     size_t cnt = (size_t)p->nx * (size_t)p->ny;
+    char probe[600];
+    snprintf(probe, sizeof probe, "%s.vp.su", mfile);
+    FILE *pf = fopen(probe, "rb");
+    const int su = pf != NULL; /* readmod_elastic.c:50-58: vp.su decides for all models */
+    if (pf)
+        fclose(pf);
     for (int k = 0; k < n && k < max; k++) {
+        if (su) {
+            char path[600];
+            snprintf(path, sizeof path, "%s.%s.su", mfile, names[k]);
+            out[k] = (float *)malloc(cnt * sizeof(float));
+            if (!out[k] || read_su_model(path, p->nx, p->ny, out[k]))
+                return 1;
+            continue;
+        }
         char path[600];
         snprintf(path, sizeof path, "%s.%s", mfile, names[k]);
         FILE *fp = fopen(path, "rb");
@@ -207,10 +265,11 @@ static void put_i16(unsigned char *h, int off, short v) { memcpy(h + off, &v, 2)
 static void put_u16(unsigned char *h, int off, unsigned short v) { memcpy(h + off, &v, 2); }
 static void put_f32(unsigned char *h, int off, float v) { memcpy(h + off, &v, 4); }
 
-int sofih_write_su(const char *path, const float *section, int ntr, int ns, const int *ix, const int *iy,
-                   float xs, float ys, const sofih_par *p, int ishot, int comp)
+/* SU traces as outseis_glob.c:40-82 writes them; tracl_of[t] is the trace
+ * number field (recpos[3]), NULL for 1..ntr. */
+static int write_su_traces(const char *path, const float *section, int ntr, int ns, const int *ix, const int *iy,
+                           const int *tracl_of, float xs, float ys, const sofih_par *p, int ishot)
 {
-    (void)comp;
     FILE *fp = fopen(path, "wb");
     if (!fp) {
         sofih_set_error("cannot write %s", path);
@@ -222,7 +281,7 @@ int sofih_write_su(const char *path, const float *section, int ntr, int ns, cons
         memset(h, 0, sizeof h);
         float xr = (ix[t] - 1) * p->dh, yr = (iy[t] - 1) * p->dh;
         float x = xr - p->refrec[0], y = yr - p->refrec[1];
-        int tracl = t + 1;
+        int tracl = tracl_of ? tracl_of[t] : t + 1;
         put_i32(h, 0, tracl);                                                   /* tracl */
         put_i32(h, 4, tracl);                                                   /* tracr */
         put_i32(h, 8, ishot);                                                   /* fldr */
@@ -249,6 +308,45 @@ int sofih_write_su(const char *path, const float *section, int ntr, int ns, cons
         }
     }
     fclose(fp);
+    return 0;
+}
+
+int sofih_write_su(const char *path, const float *section, int ntr, int ns, const int *ix, const int *iy,
+                   float xs, float ys, const sofih_par *p, int ishot, int comp)
+{
+    (void)comp; /* outseis_glob.c:55,79: ep is set to comp, then to ishot */
+    return write_su_traces(path, section, ntr, ns, ix, iy, NULL, xs, ys, p, ishot);
+}
+
+int sofih_write_signal(const sofih_par *p, int ishot, const float *signal, int nt, int ix, int iy, float xs,
+                       float ys, char *path_out, int path_len)
+{
+    static const char *ext[4] = {"", "su", "txt", "bin"};
+    int fmt = p->sigout_format;
+    if (fmt < 1 || fmt > 3) {
+        sofih_set_error("Unknown SIGOUT_FORMAT %d", fmt);
+        return 1;
+    }
+    char path[600];
+    snprintf(path, sizeof path, "%s.shot%d.%s", p->sigout_file, ishot, ext[fmt]);
+    if (path_out && path_len > 0)
+        snprintf(path_out, (size_t)path_len, "%s", path);
+    if (fmt == 1) {
+        const int zero = 0; /* initsrc.c:82: the dummy receiver's trace number */
+        return write_su_traces(path, signal, 1, nt, &ix, &iy, &zero, xs, ys, p, ishot);
+    }
+    FILE *fp = fopen(path, fmt == 2 ? "w" : "wb");
+    if (!fp) {
+        sofih_set_error("cannot write %s", path);
+        return 1;
+    }
+    int bad = 0;
+    for (int k = 0; k < nt && !bad; k++)
+        bad = fmt == 2 ? fprintf(fp, "%e\n", signal[k]) < 0 : fwrite(signal + k, sizeof(float), 1, fp) != 1;
+    if (fclose(fp) || bad) {
+        sofih_set_error("short write on %s", path);
+        return 1;
+    }
     return 0;
 }
 

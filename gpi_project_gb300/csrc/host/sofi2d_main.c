@@ -82,6 +82,17 @@ int main(int argc, char **argv)
     int *rix = NULL, *riy = NULL, ntr = 0;
     if (p.seismo && sofih_read_receivers(&p, p.rec_file, &rix, &riy, &ntr))
         DIE_H();
+    /* source wavelet files (initsrc.c:64-93): per shot, the first source of the
+     * shot, at its grid position and with its coordinates */
+    if (p.sigout == 1 && nsrc > 0) {
+        int nsh = p.run_multiple_shots ? nsrc : 1;
+        for (int s = 0; s < nsh; s++) {
+            char path[600];
+            if (sofih_write_signal(&p, s + 1, sig + (size_t)s * p.nt, p.nt, (int)srcpos[s], (int)srcpos[nsrc + s],
+                                   srcxy[s], srcxy[nsrc + s], path, sizeof path))
+                fprintf(stderr, "warning: %s - no signature written\n", sofih_last_error());
+        }
+    }
     int nshots = (p.run_multiple_shots && nsrc > 0) ? nsrc : 1;
 
     sofi_config c;

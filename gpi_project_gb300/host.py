@@ -28,7 +28,8 @@ class SofihPar(ctypes.Structure):
                 ("ngeoph", ctypes.c_int), ("snap", ctypes.c_int), ("snap_format", ctypes.c_int),
                 ("tsnap1", ctypes.c_float), ("tsnap2", ctypes.c_float), ("tsnapinc", ctypes.c_float),
                 ("idx", ctypes.c_int), ("idy", ctypes.c_int), ("snap_file", ctypes.c_char * 256),
-                ("mfile", ctypes.c_char * 256)]
+                ("mfile", ctypes.c_char * 256), ("sigout", ctypes.c_int), ("sigout_format", ctypes.c_int),
+                ("sigout_file", ctypes.c_char * 256)]
 
 
 _LIB = None
@@ -57,6 +58,10 @@ def load():
         L.sofih_wavelet.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int, fp, fp]
         L.sofih_read_sources.argtypes = [P(SofihPar), ctypes.c_char_p, P(fp), P(fp), ip]
         L.sofih_read_receivers.argtypes = [P(SofihPar), ctypes.c_char_p, P(ip), P(ip), ip]
+        L.sofih_write_signal.argtypes = [P(SofihPar), ctypes.c_int, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_float, ctypes.c_float, ctypes.c_char_p, ctypes.c_int]
+        L.sofih_read_model.argtypes = [P(SofihPar), ctypes.c_char_p, P(fp), ctypes.c_int]
+        L.sofih_model_suffixes.argtypes = [ctypes.c_int, P(ctypes.c_char_p), ctypes.c_int]
         L.sofih_write_su.argtypes = [ctypes.c_char_p, fp, ctypes.c_int, ctypes.c_int, ip, ip, ctypes.c_float,
                                      ctypes.c_float, P(SofihPar), ctypes.c_int, ctypes.c_int]
         _LIB = L
@@ -164,3 +169,28 @@ def write_su(path: str, section, ix, iy, xs: float, ys: float, p: SofihPar, isho
     if load().sofih_write_su(path.encode(), _fp(sec), sec.shape[0], sec.shape[1], ix.ctypes.data_as(ipp),
                              iy.ctypes.data_as(ipp), xs, ys, ctypes.byref(p), ishot, comp):
         raise _err()
+
+
+def write_signal(p: SofihPar, ishot: int, signal, ix: int, iy: int, xs: float, ys: float) -> str:
+    """Source wavelet file <SIGOUT_FILE>.shot<ishot>.<ext> (initsrc.c:64-93); returns its path."""
+    sig = np.ascontiguousarray(signal, dtype=np.float32).reshape(-1)
+    buf = ctypes.create_string_buffer(600)
+    if load().sofih_write_signal(ctypes.byref(p), ishot, _fp(sig), sig.size, ix, iy, xs, ys, buf, 600):
+        raise _err()
+    return buf.value.decode()
+
+
+def read_model(p: SofihPar, mfile: str) -> dict:
+    """Material arrays [NX][NY] of MFILE.<suffix> (binary) or MFILE.<suffix>.su."""
+    L = load()
+    names = (ctypes.c_char_p * 8)()
+    n = L.sofih_model_suffixes(p.weq, names, 8)
+    out = (ctypes.POINTER(ctypes.c_float) * 8)()
+    if L.sofih_read_model(ctypes.byref(p), mfile.encode(), out, 8):
+        raise _err()
+    libc = ctypes.CDLL(None)
+    res = {}
+    for k in range(n):
+        res[names[k].decode()] = np.ctypeslib.as_array(out[k], shape=(p.nx, p.ny)).copy()
+        libc.free(ctypes.cast(out[k], ctypes.c_void_p))
+    return res

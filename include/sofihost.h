@@ -41,6 +41,8 @@ typedef struct {
     float tsnap1, tsnap2, tsnapinc;
     int idx, idy;
     char snap_file[256], mfile[256];
+    int sigout, sigout_format;  /* source wavelet output (initsrc.c:64-93): 1 SU, 2 ASCII, 3 binary */
+    char sigout_file[256];
 } sofih_par;
 
 const char *sofih_last_error(void);
@@ -51,7 +53,10 @@ int sofih_read_par(const char *path, sofih_par *p);
 
 /* Model-file suffixes the wave equation needs (vp vs rho [qp qs] [epsilon delta [theta]]). */
 int sofih_model_suffixes(int weq, const char **names, int max);
-/* Read MFILE.<suffix> for each needed suffix into out[k] (caller frees with free()). */
+/* Read MFILE.<suffix> for each needed suffix into out[k] (caller frees with free()).
+ * When MFILE.vp.su exists every model is read from MFILE.<suffix>.su instead
+ * (readmod_*.c): one SU trace per x column; traces past NX and samples past NY
+ * are ignored, fewer is an error. */
 int sofih_read_model(const sofih_par *p, const char *mfile, float **out, int max);
 
 /* ---- model preparation ---- */
@@ -90,6 +95,12 @@ int sofih_read_receivers(const sofih_par *p, const char *path, int **ix, int **i
  * header's 'ep' as outseis_glob.c writes it). xs, ys: source position [m]. */
 int sofih_write_su(const char *path, const float *section, int ntr, int ns, const int *ix, const int *iy,
                    float xs, float ys, const sofih_par *p, int ishot, int comp);
+/* The source wavelet file of initsrc.c:64-93: <SIGOUT_FILE>.shot<ishot>.<su|txt|bin>
+ * holding signal[0..nt-1] as one trace (format 1 SU, 2 one value per line
+ * "%e", 3 float32). (ix, iy): the source's grid position, (xs, ys) its
+ * coordinates [m]. Writes the file name used into path_out (may be NULL). */
+int sofih_write_signal(const sofih_par *p, int ishot, const float *signal, int nt, int ix, int iy, float xs,
+                       float ys, char *path_out, int path_len);
 /* Append frames to a binary snapshot file (float32, x outer, y inner). */
 int sofih_write_snap(const char *path, const float *frame, int n, int append);
 

@@ -66,6 +66,15 @@ def shipped(reference):
         print("wrote shipped", name)
 
 
+def shipped_sigout(reference):
+    """The source wavelet file the reference writes with SIGOUT = 1 (SU) for
+    examples/weq3.json, byte for byte."""
+    f = os.path.join(reference, "examples", "weq3_ref", "signal_out.shot1.su")
+    raw = np.fromfile(f, dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "shipped_sigout_weq3.npz"), raw=raw)
+    print("wrote shipped sigout", raw.size, "bytes")
+
+
 def run_reference(case, exe):
     work = tempfile.mkdtemp(prefix="sofi_fix_")
     try:
@@ -133,6 +142,10 @@ def main():
     if not a.only:
         shipped(a.reference)
         ref_examples(a.reference, exe)
+    if not a.only or a.only == "sigout":
+        shipped_sigout(a.reference)
+        if a.only:
+            return
     for case in CASES:
         if a.only and case["name"] != a.only:
             continue

@@ -102,3 +102,69 @@ def test_su_writer_matches_reference_headers(H, tmp_path):
     hdr = b.reshape(-1, rec)[:, :240]
     np.testing.assert_array_equal(hdr, g["hdr_vx"])
     np.testing.assert_array_equal(b.reshape(-1, rec)[:, 240:].copy().view(np.float32), data)
+
+
+def test_sigout_su_file_equals_reference(tmp_path):
+    """SIGOUT = 1, SU: the wavelet file the reference ships for
+    examples/weq3.json (Ricker 50 Hz, DT 1e-4, NT 2000, NDT 10), byte for byte.
+    Its headers place the source at (200 m, 200 m), grid (101, 101), whereas
+    the example's source file (and the seismograms shipped beside it) use
+    (398 m, 398 m); the samples do not depend on the position, so the file is
+    reproduced with the position it records."""
+    from gpi_project_gb300 import host
+    from tests.helpers import EXAMPLE_SOURCE
+    dt = float(np.float32(1e-4))
+    p = host.make_par(weq=2, nx=400, ny=400, dh=2.0, dt=dt, nt=2000, ndt=10, refrec=(0.0, 0.0), sigout=1,
+                      sigout_format=1, sigout_file=str(tmp_path / "signal_out").encode())
+    _, _, ts, fc, amp = EXAMPLE_SOURCE
+    x = y = 200.0
+    sp = np.zeros((12, 1), np.float32)
+    sp[0, 0], sp[1, 0] = np.floor(np.float32(x) / np.float32(2.0)) + 1, np.floor(np.float32(y) / np.float32(2.0)) + 1
+    sp[3, 0], sp[4, 0], sp[5, 0], sp[7, 0] = ts, fc, amp, 1
+    sig = host.wavelet(1, 2000, dt, sp)[0]
+    path = host.write_signal(p, 1, sig, int(sp[0, 0]), int(sp[1, 0]), x, y)
+    assert path.endswith("signal_out.shot1.su")
+    ref = np.load(os.path.join(GOLDEN, "shipped_sigout_weq3.npz"))["raw"]
+    got = np.fromfile(path, dtype=np.uint8)
+    assert got.size == ref.size
+    np.testing.assert_array_equal(got, ref)
+
+
+def test_sigout_ascii_and_binary(tmp_path):
+    from gpi_project_gb300 import host
+    sig = np.linspace(-1.0, 1.0, 37, dtype=np.float32) ** 3
+    for fmt, ext in ((2, "txt"), (3, "bin")):
+        p = host.make_par(weq=2, nx=10, ny=10, dh=1.0, dt=1e-3, nt=37, sigout=1, sigout_format=fmt,
+                          sigout_file=str(tmp_path / "w").encode())
+        path = host.write_signal(p, 3, sig, 5, 5, 4.0, 4.0)
+        assert path.endswith(f"w.shot3.{ext}")
+        back = np.loadtxt(path, dtype=np.float64) if fmt == 2 else np.fromfile(path, dtype=np.float32)
+        np.testing.assert_allclose(back, sig, rtol=1e-6, atol=1e-30)
+    p = host.make_par(weq=2, nx=10, ny=10, dh=1.0, dt=1e-3, nt=37, sigout=1, sigout_format=4,
+                      sigout_file=str(tmp_path / "w").encode())
+    with pytest.raises(RuntimeError, match="SIGOUT_FORMAT"):
+        host.write_signal(p, 1, sig, 5, 5, 4.0, 4.0)
+
+
+def test_su_model_files_read_like_binary(tmp_path):
+    """MFILE.vp.su present: every model comes from MFILE.<suffix>.su, one trace
+    per x column; extra traces and samples are ignored (readmod_elastic.c)."""
+    from gpi_project_gb300 import host
+    nx, ny = 23, 17
+    rng = np.random.default_rng(5)
+    mats = {k: rng.uniform(1.0, 3.0, (nx, ny)).astype(np.float32) for k in ("vp", "vs", "rho")}
+    p = host.make_par(weq=2, nx=nx, ny=ny, dh=1.0, dt=1e-4, nt=10)
+    for k, a in mats.items():
+        a.tofile(tmp_path / f"bin.{k}")
+        big = np.concatenate([a, rng.uniform(0, 1, (nx, 5)).astype(np.float32)], axis=1)  # ns = NY + 5
+        big = np.concatenate([big, rng.uniform(0, 1, (3, ny + 5)).astype(np.float32)], axis=0)  # NX + 3 traces
+        ix = np.arange(1, big.shape[0] + 1, dtype=np.int32)
+        host.write_su(str(tmp_path / f"su.{k}.su"), big, ix, np.ones_like(ix), 0.0, 0.0, p)
+    a = host.read_model(p, str(tmp_path / "bin"))
+    b = host.read_model(p, str(tmp_path / "su"))
+    for k in mats:
+        np.testing.assert_array_equal(a[k], mats[k])
+        np.testing.assert_array_equal(b[k], mats[k])
+    short = host.make_par(weq=2, nx=nx, ny=ny + 6, dh=1.0, dt=1e-4, nt=10)
+    with pytest.raises(RuntimeError, match="samples"):
+        host.read_model(short, str(tmp_path / "su"))
