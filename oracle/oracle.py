@@ -54,7 +54,7 @@ class OrcParams(ctypes.Structure):
                 ("f_ref", ctypes.c_float), ("fl", ctypes.c_float * 8), ("seismo", ctypes.c_int),
                 ("ndt", ctypes.c_int), ("snap", ctypes.c_int), ("tsnap1", ctypes.c_float),
                 ("tsnap2", ctypes.c_float), ("tsnapinc", ctypes.c_float), ("idx", ctypes.c_int),
-                ("idy", ctypes.c_int), ("nthreads", ctypes.c_int)]
+                ("idy", ctypes.c_int), ("nthreads", ctypes.c_int), ("fdorder_time", ctypes.c_int)]
 
 
 _LIBS: dict = {}
@@ -117,6 +117,7 @@ class SofiConfig:
     time: float = 0.1
     nt: int = 1000
     fdorder: int = 4
+    fdorder_time: int = 2
     maxrelerror: int = 0
     L: int = 0
     f_ref: float = 0.0
@@ -168,6 +169,7 @@ class SofiConfig:
         p.snap, p.tsnap1, p.tsnap2, p.tsnapinc = self.snap, self.tsnap1, self.tsnap2, self.tsnapinc
         p.idx, p.idy = self.idx, self.idy
         p.nthreads = nthreads
+        p.fdorder_time = self.fdorder_time
         return p
 
 
@@ -205,6 +207,7 @@ def config_from_json(path: str) -> SofiConfig:
     c.dh, c.dt, c.time = f32("DH"), f32("DT"), f32("TIME")
     c.nt = iround(float(np.float32(c.time) / np.float32(c.dt)))
     c.fdorder, c.maxrelerror = i("FDORDER", 4), i("MAXRELERROR", 0)
+    c.fdorder_time = i("FDORDER_TIME", 2)
     c.L = i("L", 0)
     if c.weq in (2, 4, 6):
         c.L = 0

@@ -67,6 +67,13 @@ struct orc_ctx {
     /* wavefield */
     arr2 vx, vy, sxx, syy, sxy, vxx, vyy, vyx, vxy;
     arr2 pr[ORC_MAX_L + 1], pp[ORC_MAX_L + 1], pq[ORC_MAX_L + 1];
+    /* FDORDER_TIME = 4 (Adams-Bashforth): histories of the stress-derivative
+     * sums svx/svy and of the velocity derivatives, levels 1..4
+     * (memw_struct.h: svx_1..4, vxx_1..4, ...), and levels 2..4 of the
+     * memory variables ([k][l], k = 2..4; level 1 is pr/pp/pq) */
+    int ab4;
+    arr2 svx[5], svy[5], hxx[5], hyy[5], hxy[5], hyx[5];
+    arr2 pr_h[5][ORC_MAX_L + 1], pp_h[5][ORC_MAX_L + 1], pq_h[5][ORC_MAX_L + 1];
     /* raw material input [NX][NY] */
     float *mat_vp, *mat_vs, *mat_rho, *mat_qp, *mat_qs, *mat_eps, *mat_del, *mat_tet;
     /* acquisition */
@@ -85,6 +92,10 @@ struct orc_ctx {
     int prepared;
     double tim[4];
 };
+
+/* Adams-Bashforth coefficients of FDORDER_TIME = 4, float as the reference
+ * declares them (wavefield_update_v_4.c:29-32) */
+static const float AB1 = 13.0 / 12.0, AB2 = -5.0 / 24.0, AB3 = 1.0 / 6.0, AB4 = -1.0 / 24.0;
 
 /* ----------------------------------------------------------------- helpers */
 
@@ -199,11 +210,18 @@ orc_ctx *orc_create(const orc_params *p)
      * the div/curl outputs (seismo_ssg.c:49-59, snap_ssg.c:166) read them. */
     if (is_ac(p->weq) && (p->free_surf || p->seismo >= 3 || p->snap >= 3))
         return NULL;
+    /* FDORDER_TIME = 4 exists for EL_ISO and VEL_ISO only (prepmod.c:160-186);
+     * the free surface is not restated for it */
+    if (p->fdorder_time == 4 && (!(p->weq == ORC_EL_ISO || p->weq == ORC_VEL_ISO) || p->free_surf))
+        return NULL;
+    if (p->fdorder_time != 0 && p->fdorder_time != 2 && p->fdorder_time != 4)
+        return NULL;
     orc_ctx *c = (orc_ctx *)calloc(1, sizeof(orc_ctx));
     c->P = *p;
     if (!is_visco(p->weq))
         c->P.L = 0; /* read_par_json.c:308-311 */
     c->ND = p->fdorder / 2;           /* initmem.c:59 */
+    c->ab4 = p->fdorder_time == 4;
     c->pitch = p->nx + 2 * c->ND;
     c->rows = p->ny + 2 * c->ND;
     c->NT = p->nt;
@@ -249,6 +267,15 @@ orc_ctx *orc_create(const orc_params *p)
     if (is_ac(p->weq)) {
         free2(&c->syy);
         c->syy = c->sxx;
+    }
+    if (c->ab4) {
+        for (int k = 1; k <= 4; k++) {
+            c->svx[k] = alloc2(c), c->svy[k] = alloc2(c);
+            c->hxx[k] = alloc2(c), c->hyy[k] = alloc2(c), c->hxy[k] = alloc2(c), c->hyx[k] = alloc2(c);
+        }
+        for (int l = 1; l <= L; l++)
+            for (int k = 2; k <= 4; k++)
+                c->pr_h[k][l] = alloc2(c), c->pp_h[k][l] = alloc2(c), c->pq_h[k][l] = alloc2(c);
     }
     for (int l = 1; l <= L; l++) {
         c->dip[l] = alloc2(c), c->d[l] = alloc2(c), c->e[l] = alloc2(c);
@@ -309,6 +336,12 @@ void orc_destroy(orc_ctx *c)
                    &c->syy, &c->sxy, &c->vxx, &c->vyy, &c->vyx, &c->vxy};
     for (size_t k = 0; k < sizeof(all) / sizeof(all[0]); k++)
         free2(all[k]);
+    for (int k = 1; k <= 4; k++) {
+        free2(&c->svx[k]), free2(&c->svy[k]);
+        free2(&c->hxx[k]), free2(&c->hyy[k]), free2(&c->hxy[k]), free2(&c->hyx[k]);
+        for (int l = 1; l <= c->P.L; l++)
+            free2(&c->pr_h[k][l]), free2(&c->pp_h[k][l]), free2(&c->pq_h[k][l]);
+    }
     for (int l = 1; l <= c->P.L; l++) {
         free2(&c->dip[l]), free2(&c->d[l]), free2(&c->e[l]);
         free2(&c->pr[l]), free2(&c->pp[l]), free2(&c->pq[l]);
@@ -590,8 +623,13 @@ static void prepare_update(orc_ctx *c)
     int L = c->P.L, weq = c->P.weq;
     real DT = c->DT;
     for (int l = 1; l <= L; l++) {
-        c->bip[l] = 1.0 / (1.0 + (c->peta[l] * 0.5));
-        c->cip[l] = 1.0 - (c->peta[l] * 0.5);
+        if (c->ab4) { /* prepare_update_s_visc_4.c:40-45 */
+            c->bip[l] = 1.0 / (1.0 + (AB1 * c->peta[l] * 0.5));
+            c->cip[l] = 1.0 - (AB1 * c->peta[l] * 0.5);
+        } else {
+            c->bip[l] = 1.0 / (1.0 + (c->peta[l] * 0.5));
+            c->cip[l] = 1.0 - (c->peta[l] * 0.5);
+        }
     }
     for (int j = 1; j <= c->P.ny; j++)
         for (int i = 1; i <= c->P.nx; i++) {
@@ -1052,6 +1090,25 @@ static inline void wf_update_v(orc_ctx *c, int i, int j, real sxx_x, real sxy_x,
     A(c->vy, j, i) += (sxy_x + syy_y) * c->DTDH * A(c->prjp, j, i);
 }
 
+/* shift_var2 / shift_var3 (util.c:89-109): level 4 <- 3 <- 2 <- 1, the old
+ * level 4 array becomes level 1 */
+static void shift4(arr2 *h)
+{
+    arr2 t = h[4];
+    h[4] = h[3], h[3] = h[2], h[2] = h[1], h[1] = t;
+}
+
+/* wavefield_update_v_4.c:26-46 */
+static inline void wf_update_v4(orc_ctx *c, int i, int j, real sxx_x, real sxy_x, real sxy_y, real syy_y)
+{
+    A(c->svx[1], j, i) = sxx_x + sxy_y;
+    A(c->svy[1], j, i) = sxy_x + syy_y;
+    A(c->vx, j, i) += (AB1 * A(c->svx[1], j, i) + AB2 * A(c->svx[2], j, i) + AB3 * A(c->svx[3], j, i) +
+                       AB4 * A(c->svx[4], j, i)) * c->DTDH * A(c->prip, j, i);
+    A(c->vy, j, i) += (AB1 * A(c->svy[1], j, i) + AB2 * A(c->svy[2], j, i) + AB3 * A(c->svy[3], j, i) +
+                       AB4 * A(c->svy[4], j, i)) * c->DTDH * A(c->prjp, j, i);
+}
+
 /* ------------------------------------------------------- velocity update */
 
 /* update_v_interior.c:49-71: force sources before the velocity loop */
@@ -1103,10 +1160,63 @@ static void v_region(orc_ctx *c, int j0, int j1, int i0, int i1, int modex, int 
         }
 }
 
+/* The FDORDER_TIME = 4 drivers (update_v_interior_4.c, update_v_PML_4.c,
+ * update_v_abs_4.c). upd = 0: the region gets its CPML pass but no update --
+ * update_v_PML_4.c leaves the velocity of the left frame and of all four
+ * corners untouched. */
+static void v_region4(orc_ctx *c, int j0, int j1, int i0, int i1, int modex, int modey, int damp, int upd)
+{
+    int NX = c->P.nx, NY = c->P.ny, FW = c->P.fw;
+#pragma omp parallel for schedule(static)
+    for (int j = j0; j <= j1; j++)
+        for (int i = i0; i <= i1; i++) {
+            real sxx_x, sxy_x, sxy_y, syy_y;
+            op_v(c, i, j, &sxx_x, &sxy_x, &sxy_y, &syy_y);
+            if (modex == 1)
+                cpml_v_x(c, i, j, &sxx_x, &sxy_x);
+            else if (modex == 2)
+                cpml_v_x(c, i - NX + 2 * FW, j, &sxx_x, &sxy_x);
+            if (modey == 1)
+                cpml_v_y(c, i, j, &sxy_y, &syy_y);
+            else if (modey == 2)
+                cpml_v_y(c, i, j - NY + 2 * FW, &sxy_y, &syy_y);
+            if (upd)
+                wf_update_v4(c, i, j, sxx_x, sxy_x, sxy_y, syy_y);
+            if (damp) {
+                A(c->vx, j, i) *= A(c->absorb, j, i); /* abs_update.c:46-50 */
+                A(c->vy, j, i) *= A(c->absorb, j, i);
+            }
+        }
+}
+
+static void update_v4(orc_ctx *c)
+{
+    int *GX = c->GX, *GY = c->GY;
+    v_region4(c, GY[2] + 1, GY[3], GX[2] + 1, GX[3], 0, 0, 0, 1);
+    if (c->P.fw && (c->P.abs_type == 1 || c->P.abs_type == 2)) {
+        int pml = c->P.abs_type == 1, dmp = c->P.abs_type == 2;
+        v_region4(c, GY[2] + 1, GY[3], GX[1], GX[2], pml ? 1 : 0, 0, dmp, dmp);
+        v_region4(c, GY[2] + 1, GY[3], GX[3] + 1, GX[4], pml ? 2 : 0, 0, dmp, 1);
+        v_region4(c, GY[1], GY[2], GX[2] + 1, GX[3], 0, pml ? 1 : 0, dmp, 1);
+        v_region4(c, GY[3] + 1, GY[4], GX[2] + 1, GX[3], 0, pml ? 2 : 0, dmp, 1);
+        v_region4(c, GY[1], GY[2], GX[1], GX[2], pml ? 1 : 0, pml ? 1 : 0, dmp, dmp);
+        v_region4(c, GY[3] + 1, GY[4], GX[1], GX[2], pml ? 1 : 0, pml ? 2 : 0, dmp, dmp);
+        v_region4(c, GY[1], GY[2], GX[3] + 1, GX[4], pml ? 2 : 0, pml ? 1 : 0, dmp, dmp);
+        v_region4(c, GY[3] + 1, GY[4], GX[3] + 1, GX[4], pml ? 2 : 0, pml ? 2 : 0, dmp, dmp);
+    }
+    /* time_loop.c:89-91 */
+    shift4(c->svx);
+    shift4(c->svy);
+}
+
 static void update_v(orc_ctx *c, int nt)
 {
     int *GX = c->GX, *GY = c->GY;
     force_sources(c, nt);
+    if (c->ab4) {
+        update_v4(c);
+        return;
+    }
     v_region(c, GY[2] + 1, GY[3], GX[2] + 1, GX[3], 0, 0, 0);
     if (c->P.fw) {
         int pml = c->P.abs_type == 1, dmp = c->P.abs_type == 2;
@@ -1324,8 +1434,84 @@ static inline void wf_s_ac(orc_ctx *c, int i, int j)
     A(c->syy, j, i) += (A(c->g, j, i) * A(c->vyy, j, i));
 }
 
+/* wavefield_update_s_el_4.c:26-60 (the stored derivatives times DH, their
+ * Adams-Bashforth sums, the update scaled back by dhi) */
+static inline void wf_s_el4(orc_ctx *c, int i, int j)
+{
+    real dhi = 1.0 / c->DH;
+    A(c->hxx[1], j, i) = A(c->vxx, j, i) * c->DH;
+    A(c->hyy[1], j, i) = A(c->vyy, j, i) * c->DH;
+    A(c->hxy[1], j, i) = A(c->vxy, j, i) * c->DH;
+    A(c->hyx[1], j, i) = A(c->vyx, j, i) * c->DH;
+    real sumxx = AB1 * A(c->hxx[1], j, i) + AB2 * A(c->hxx[2], j, i) + AB3 * A(c->hxx[3], j, i) + AB4 * A(c->hxx[4], j, i);
+    real sumyy = AB1 * A(c->hyy[1], j, i) + AB2 * A(c->hyy[2], j, i) + AB3 * A(c->hyy[3], j, i) + AB4 * A(c->hyy[4], j, i);
+    real sumxy = AB1 * A(c->hxy[1], j, i) + AB2 * A(c->hxy[2], j, i) + AB3 * A(c->hxy[3], j, i) + AB4 * A(c->hxy[4], j, i);
+    real sumyx = AB1 * A(c->hyx[1], j, i) + AB2 * A(c->hyx[2], j, i) + AB3 * A(c->hyx[3], j, i) + AB4 * A(c->hyx[4], j, i);
+    real u1 = A(c->fipjp, j, i) * (sumxy + sumyx) * dhi;
+    real u2 = ((A(c->g, j, i) * (sumxx + sumyy)) - (2.0 * A(c->f, j, i) * sumyy)) * dhi;
+    real u3 = ((A(c->g, j, i) * (sumxx + sumyy)) - (2.0 * A(c->f, j, i) * sumxx)) * dhi;
+    A(c->sxy, j, i) += u1;
+    A(c->sxx, j, i) += u2;
+    A(c->syy, j, i) += u3;
+}
+
+/* wavefield_update_s_visc_4.c:27-91: memory variables of level 4 are
+ * overwritten with the new values (they become level 1 after the shift) */
+static inline void wf_s_visc4(orc_ctx *c, int i, int j)
+{
+    real sumr_old = 0.0f, sump_old = 0.0f, sumq_old = 0.0f, sumr = 0.0f, sump = 0.0f, sumq = 0.0f;
+    real dhi = 1.0 / c->DH;
+    real dthalbe = c->DT / 2.0;
+    A(c->hxx[1], j, i) = A(c->vxx, j, i) * c->DH;
+    A(c->hyy[1], j, i) = A(c->vyy, j, i) * c->DH;
+    A(c->hxy[1], j, i) = A(c->vxy, j, i) * c->DH;
+    A(c->hyx[1], j, i) = A(c->vyx, j, i) * c->DH;
+    real sumxx = AB1 * A(c->hxx[1], j, i) + AB2 * A(c->hxx[2], j, i) + AB3 * A(c->hxx[3], j, i) + AB4 * A(c->hxx[4], j, i);
+    real sumyy = AB1 * A(c->hyy[1], j, i) + AB2 * A(c->hyy[2], j, i) + AB3 * A(c->hyy[3], j, i) + AB4 * A(c->hyy[4], j, i);
+    real sumxy = AB1 * A(c->hxy[1], j, i) + AB2 * A(c->hxy[2], j, i) + AB3 * A(c->hxy[3], j, i) + AB4 * A(c->hxy[4], j, i);
+    real sumyx = AB1 * A(c->hyx[1], j, i) + AB2 * A(c->hyx[2], j, i) + AB3 * A(c->hyx[3], j, i) + AB4 * A(c->hyx[4], j, i);
+    for (int l = 1; l <= c->P.L; l++) {
+        real r = A(c->pr[l], j, i), r2 = A(c->pr_h[2][l], j, i), r3 = A(c->pr_h[3][l], j, i), r4 = A(c->pr_h[4][l], j, i);
+        real p = A(c->pp[l], j, i), p2 = A(c->pp_h[2][l], j, i), p3 = A(c->pp_h[3][l], j, i), p4 = A(c->pp_h[4][l], j, i);
+        real q = A(c->pq[l], j, i), q2 = A(c->pq_h[2][l], j, i), q3 = A(c->pq_h[3][l], j, i), q4 = A(c->pq_h[4][l], j, i);
+        sumr_old += AB1 * r + AB2 * r2 + AB3 * r3 + AB4 * r4;
+        sump_old += AB1 * p + AB2 * p2 + AB3 * p3 + AB4 * p4;
+        sumq_old += AB1 * q + AB2 * q2 + AB3 * q3 + AB4 * q4;
+        real ctemp = 2 * (1 - c->cip[l]) / AB1;
+        real nr = c->bip[l] * (r * c->cip[l] - ctemp * AB2 * (r + r2) - ctemp * AB3 * (r2 + r3) -
+                               ctemp * AB4 * (r3 + r4) - (A(c->dip[l], j, i) * (sumxy + sumyx) * dhi));
+        real np = c->bip[l] * (p * c->cip[l] - ctemp * AB2 * (p + p2) - ctemp * AB3 * (p2 + p3) -
+                               ctemp * AB4 * (p3 + p4) - (A(c->e[l], j, i) * (sumxx + sumyy) * dhi) +
+                               (2.0 * A(c->d[l], j, i) * sumyy * dhi));
+        real nq = c->bip[l] * (q * c->cip[l] - ctemp * AB2 * (q + q2) - ctemp * AB3 * (q2 + q3) -
+                               ctemp * AB4 * (q3 + q4) - (A(c->e[l], j, i) * (sumxx + sumyy) * dhi) +
+                               (2.0 * A(c->d[l], j, i) * sumxx * dhi));
+        A(c->pr_h[4][l], j, i) = nr;
+        A(c->pp_h[4][l], j, i) = np;
+        A(c->pq_h[4][l], j, i) = nq;
+        sumr += AB1 * nr + AB2 * r + AB3 * r2 + AB4 * r3;
+        sump += AB1 * np + AB2 * p + AB3 * p2 + AB4 * p3;
+        sumq += AB1 * nq + AB2 * q + AB3 * q2 + AB4 * q3;
+    }
+    real u1 = (A(c->fipjp, j, i) * (sumxy + sumyx)) * dhi + (dthalbe * (sumr_old + sumr));
+    real u2 = (A(c->g, j, i) * (sumxx + sumyy) * dhi) - (2.0 * A(c->f, j, i) * sumyy * dhi) +
+              (dthalbe * (sump_old + sump));
+    real u3 = (A(c->g, j, i) * (sumxx + sumyy) * dhi) - (2.0 * A(c->f, j, i) * sumxx * dhi) +
+              (dthalbe * (sumq_old + sumq));
+    A(c->sxy, j, i) += u1;
+    A(c->sxx, j, i) += u2;
+    A(c->syy, j, i) += u3;
+}
+
 static inline void wf_s(orc_ctx *c, int i, int j)
 {
+    if (c->ab4) {
+        if (c->P.weq == ORC_VEL_ISO)
+            wf_s_visc4(c, i, j);
+        else
+            wf_s_el4(c, i, j);
+        return;
+    }
     switch (c->P.weq) {
       case ORC_AC_ISO: wf_s_ac(c, i, j); break;
       case ORC_EL_ISO: wf_s_el(c, i, j); break;
@@ -1374,7 +1560,27 @@ static void s_region(orc_ctx *c, int j0, int j1, int i0, int i1, int modex, int 
         }
 }
 
+static void update_s_regions(orc_ctx *c);
+
 static void update_s(orc_ctx *c)
+{
+    update_s_regions(c);
+    if (c->ab4) {
+        /* time_loop.c:228-230, 241-244 */
+        for (int l = 1; l <= c->P.L; l++) {
+            arr2 hr[5] = {{0}, c->pr[l], c->pr_h[2][l], c->pr_h[3][l], c->pr_h[4][l]};
+            arr2 hp[5] = {{0}, c->pp[l], c->pp_h[2][l], c->pp_h[3][l], c->pp_h[4][l]};
+            arr2 hq[5] = {{0}, c->pq[l], c->pq_h[2][l], c->pq_h[3][l], c->pq_h[4][l]};
+            shift4(hr), shift4(hp), shift4(hq);
+            c->pr[l] = hr[1], c->pr_h[2][l] = hr[2], c->pr_h[3][l] = hr[3], c->pr_h[4][l] = hr[4];
+            c->pp[l] = hp[1], c->pp_h[2][l] = hp[2], c->pp_h[3][l] = hp[3], c->pp_h[4][l] = hp[4];
+            c->pq[l] = hq[1], c->pq_h[2][l] = hq[2], c->pq_h[3][l] = hq[3], c->pq_h[4][l] = hq[4];
+        }
+        shift4(c->hxx), shift4(c->hyy), shift4(c->hxy), shift4(c->hyx);
+    }
+}
+
+static void update_s_regions(orc_ctx *c)
 {
     int *GX = c->GX, *GY = c->GY;
     s_region(c, GY[2] + 1, GY[3], GX[2] + 1, GX[3], 0, 0, 0);
@@ -1620,6 +1826,16 @@ int orc_reset(orc_ctx *c)
         memset(c->pr[l].p, 0, n2 * sizeof(real));
         memset(c->pp[l].p, 0, n2 * sizeof(real));
         memset(c->pq[l].p, 0, n2 * sizeof(real));
+    }
+    for (int k = 1; c->ab4 && k <= 4; k++) {
+        arr2 *h[] = {&c->svx[k], &c->svy[k], &c->hxx[k], &c->hyy[k], &c->hxy[k], &c->hyx[k]};
+        for (size_t q = 0; q < sizeof(h) / sizeof(h[0]); q++)
+            memset(h[q]->p, 0, n2 * sizeof(real));
+        for (int l = 1; k >= 2 && l <= c->P.L; l++) {
+            memset(c->pr_h[k][l].p, 0, n2 * sizeof(real));
+            memset(c->pp_h[k][l].p, 0, n2 * sizeof(real));
+            memset(c->pq_h[k][l].p, 0, n2 * sizeof(real));
+        }
     }
     int fw2 = 2 * (c->P.fw > 0 ? c->P.fw : 1);
     size_t nxf = (size_t)c->P.ny * fw2, nyf = (size_t)fw2 * c->P.nx;

@@ -47,6 +47,7 @@ typedef struct {
     float tsnap1, tsnap2, tsnapinc;
     int idx, idy;
     int nthreads;           /* OpenMP threads for the cell loops (0 = default) */
+    int fdorder_time;       /* 2 (or 0) leapfrog, 4 Adams-Bashforth (gv->FDORDER_TIME) */
 } orc_params;
 
 typedef struct orc_ctx orc_ctx;

@@ -34,7 +34,8 @@ sys.path.insert(0, REPO)
 from tests.golden.cases import CASES, synthetic_model, write_case  # noqa: E402
 
 SHIPPED = {"weq3": "EL_ISO", "weq4": "VEL_ISO", "weq5": "EL_VTI", "weq6": "VEL_VTI", "weq7": "EL_TTI",
-           "weq8": "VEL_TTI", "weq3_fy": "EL_ISO", "weq8_fy": "VEL_TTI"}
+           "weq8": "VEL_TTI", "weq3_fy": "EL_ISO", "weq8_fy": "VEL_TTI", "weq3_fdt4": "EL_ISO",
+           "weq4_fdt4": "VEL_ISO"}
 
 
 def read_su(path):
@@ -50,7 +51,7 @@ def shipped(reference):
     ex = os.path.join(reference, "examples")
     for name in SHIPPED:
         base = name.split("_")[0]
-        suffix = "_fy" if name.endswith("_fy") else ""
+        suffix = name[len(base):]  # "", "_fy" or "_fdt4"
         out = {}
         for comp in ["vx", "vy", "p", "div", "curl"]:
             f = os.path.join(ex, f"{base}_ref", f"seis{suffix}_{comp}.su")
@@ -147,7 +148,7 @@ def main():
         if a.only:
             return
     for case in CASES:
-        if a.only and case["name"] != a.only:
+        if (a.only and case["name"] != a.only) or not case.get("compiled_ref", True):
             continue
         out = run_reference(case, exe)
         np.savez_compressed(os.path.join(HERE, f"ref_{case['name']}.npz"), **out)

@@ -19,6 +19,7 @@ def case_config(case):
     c.dh, c.dt = float(np.float32(case["dh"])), float(np.float32(case["dt"]))
     c.nt = O.iround(float(np.float32(case["nt"] * case["dt"]) / np.float32(case["dt"])))
     c.fdorder, c.maxrelerror, c.L = case["fdorder"], case["maxrelerror"], case["L"]
+    c.fdorder_time = case.get("fdorder_time", 2)
     c.fl, c.f_ref = [float(np.float32(f)) for f in case["fl"]], float(np.float32(case["f_ref"]))
     c.fw, c.abs_type, c.free_surf, c.boundary = case["fw"], case["abs_type"], case["free_surf"], case["boundary"]
     c.npower, c.k_max_cpml = float(np.float32(case["npower"])), float(np.float32(case["k_max_cpml"]))
@@ -85,7 +86,8 @@ def rel_max(a, b, floor=None):
 
 # --- the reference's examples/weqN.json runs (all share weq3.json's settings) ---
 EXAMPLE_WEQ = {"weq3": (2, 0, 1), "weq4": (3, 1, 1), "weq5": (4, 0, 1), "weq6": (5, 1, 1), "weq7": (6, 0, 1),
-               "weq8": (7, 1, 1), "weq3_fy": (2, 0, 3), "weq8_fy": (7, 1, 3)}
+               "weq8": (7, 1, 1), "weq3_fy": (2, 0, 3), "weq8_fy": (7, 1, 3), "weq3_fdt4": (2, 0, 1),
+               "weq4_fdt4": (3, 1, 1)}
 # homogeneous examples/model/TTI_Thomsen_1.* (every cell holds these values)
 EXAMPLE_MODEL = {"vp": 3369.0, "vs": 1643.0, "rho": 2000.0, "qp": 20.0, "qs": 10.0, "epsilon": 0.26,
                  "delta": -0.05, "theta": 30.0}
@@ -110,6 +112,7 @@ def example_config(name):
     c.snap, c.idx, c.idy = 4, 2, 2
     c.tsnap1, c.tsnap2, c.tsnapinc = (float(np.float32(0.06)), float(np.float32(0.18)), float(np.float32(0.04)))
     c.source_type = stype
+    c.fdorder_time = 4 if name.endswith("_fdt4") else 2  # weqN_fdt4.json: FDORDER_TIME = 4
     return c
 
 

@@ -18,7 +18,8 @@ from tests.helpers import COMPS, GOLDEN, rel_l2, rel_max, run_oracle_case, run_o
 # agrees to float round-off (relative L2 bound per example; measured values
 # are 2e-6..2.3e-5). The TTI examples' shipped files carry the 2x2 seam
 # artefact and are pinned against the one-rank compiled reference instead.
-SHIPPED_TOL = {"weq3": 5e-5, "weq4": 5e-5, "weq5": 5e-5, "weq6": 5e-5, "weq3_fy": 5e-5}
+SHIPPED_TOL = {"weq3": 5e-5, "weq4": 5e-5, "weq5": 5e-5, "weq6": 5e-5, "weq3_fy": 5e-5, "weq3_fdt4": 5e-5,
+               "weq4_fdt4": 5e-5}
 
 
 @pytest.mark.parametrize("name", sorted(SHIPPED_TOL))
@@ -64,6 +65,8 @@ def test_tti_shipped_files_carry_decomposition_seam():
 @pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
 def test_oracle_vs_compiled_reference(case):
     """Bit-level agreement with the reference compiled from its sources (x86-64 here)."""
+    if not case.get("compiled_ref", True):
+        pytest.skip("the compiled reference has no working output for this case (see tests/golden/cases.py)")
     g = np.load(os.path.join(GOLDEN, f"ref_{case['name']}.npz"))
     import zlib
     crc = 0
