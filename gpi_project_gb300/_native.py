@@ -35,7 +35,8 @@ class SofiConfig(ctypes.Structure):
         ("nt", ctypes.c_int), ("fw", ctypes.c_int), ("abs_type", ctypes.c_int), ("free_surf", ctypes.c_int),
         ("boundary", ctypes.c_int), ("seismo", ctypes.c_int), ("ndt", ctypes.c_int), ("snap", ctypes.c_int),
         ("snap_first", ctypes.c_int), ("snap_inc", ctypes.c_int), ("snap_last", ctypes.c_int),
-        ("idx", ctypes.c_int), ("idy", ctypes.c_int), ("nshots", ctypes.c_int), ("shared_model", ctypes.c_int)]]
+        ("idx", ctypes.c_int), ("idy", ctypes.c_int), ("nshots", ctypes.c_int), ("shared_model", ctypes.c_int),
+        ("fdorder_time", ctypes.c_int)]]
 
 
 class TtiStressArgs(ctypes.Structure):

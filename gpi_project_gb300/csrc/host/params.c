@@ -184,6 +184,7 @@ int sofih_read_par(const char *path, sofih_par *p)
     gets_(kv, "REC_FILE", p->rec_file, sizeof p->rec_file);
     gets_(kv, "SEIS_FILE", p->seis_file, sizeof p->seis_file);
     p->sigout = geti(kv, "SIGOUT", 0), p->sigout_format = geti(kv, "SIGOUT_FORMAT", 1);
+    p->fdorder_time = geti(kv, "FDORDER_TIME", 2);
     gets_(kv, "SIGOUT_FILE", p->sigout_file, sizeof p->sigout_file);
     p->refrec[0] = getf(kv, "REFRECX", 0.f), p->refrec[1] = getf(kv, "REFRECY", 0.f);
     p->xrec1 = getf(kv, "XREC1", 0.f), p->yrec1 = getf(kv, "YREC1", 0.f);

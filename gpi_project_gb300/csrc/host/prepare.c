@@ -489,8 +489,14 @@ int sofih_prepare(const sofih_par *p, const float *vp, const float *vs, const fl
     if (L) {
         float *bip = out_vec(m, "bip", L), *cip = out_vec(m, "cip", L), *pe = out_vec(m, "peta", L);
         for (int l = 1; l <= L; l++) {
-            bip[l - 1] = 1.0 / (1.0 + (peta[l] * 0.5));
-            cip[l - 1] = 1.0 - (peta[l] * 0.5);
+            if (p->fdorder_time == 4) { /* prepare_update_s_visc_4.c:40-45 (c1 = 13/12) */
+                const float c1 = 13.0 / 12.0;
+                bip[l - 1] = 1.0 / (1.0 + (c1 * peta[l] * 0.5));
+                cip[l - 1] = 1.0 - (c1 * peta[l] * 0.5);
+            } else {
+                bip[l - 1] = 1.0 / (1.0 + (peta[l] * 0.5));
+                cip[l - 1] = 1.0 - (peta[l] * 0.5);
+            }
             pe[l - 1] = peta[l];
         }
     }

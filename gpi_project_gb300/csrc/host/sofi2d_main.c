@@ -103,6 +103,7 @@ int main(int argc, char **argv)
     c.snap = p.snap;
     c.snap_first = IROUND(p.tsnap1 / p.dt), c.snap_inc = IROUND(p.tsnapinc / p.dt), c.snap_last = IROUND(p.tsnap2 / p.dt);
     c.idx = p.idx, c.idy = p.idy, c.nshots = nshots, c.shared_model = 1;
+    c.fdorder_time = p.fdorder_time;
     sofi_ctx *ctx;
     CHECK_G(sofi_create(&c, device, &ctx));
     float hc[7];

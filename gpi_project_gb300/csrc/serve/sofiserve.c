@@ -166,6 +166,7 @@ static int prepare_request(const sofi_server *s, req_t *q)
     c->free_surf = p->free_surf, c->boundary = p->boundary, c->seismo = q->r.ntr > 0 ? p->seismo : 0;
     c->ndt = p->ndt > 0 ? p->ndt : 1;
     c->idx = c->idy = 1, c->nshots = 1, c->shared_model = 1;
+    c->fdorder_time = p->fdorder_time;
     if ((rc = sofi_device_bytes(c, &q->bytes)))
         return fail(rc, "%s", sofi_last_error());
     components(c->seismo, q->comps, &q->ncomp);

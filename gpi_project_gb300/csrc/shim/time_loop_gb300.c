@@ -12,7 +12,8 @@
  * shot's sources srcpos_loc[1..12][1..nsrc] with signals signalx[1..nsrc][1..NT],
  * the receivers acq->recpos_loc[1..2][1..NTR]; outputs gv->SECTION*[1..NTR][1..NS],
  * the final wavefield in *mpw and the snapshot files of snap().
- * Supported: MODE=FW (sw = 0), FDORDER_TIME = 2, one domain (NPROCX = NPROCY = 1),
+ * Supported: MODE=FW (sw = 0), FDORDER_TIME = 2 (and 4 for EL_ISO / VEL_ISO without
+ * free surface; the moduli are uploaded as prepmod() left them), one domain (NPROCX = NPROCY = 1),
  * WEQ AC_ISO and EL_ISO..VEL_TTI; anything else stops the run through log_fatal like the
  * reference's own checks. The GPU context (device 0, or $SOFI_GPU_DEVICE)
  * is created on the first call and reused while the configuration holds;
@@ -167,8 +168,8 @@ void time_loop(int iter, int ishot, int snapcheck, float *hc, float **srcpos_loc
     (void)signaly, (void)minv, (void)vinv, (void)perf, (void)ishot;
     if (sw != 0 || gv->MODE != FW)
         log_fatal("GPU time loop: only forward modelling (MODE=FW) is supported\n");
-    if (gv->FDORDER_TIME != 2)
-        log_fatal("GPU time loop: FDORDER_TIME=4 is not supported\n");
+    if (gv->FDORDER_TIME != 2 && gv->FDORDER_TIME != 4)
+        log_fatal("GPU time loop: FDORDER_TIME must be 2 or 4\n");
     if (gv->NPROCX != 1 || gv->NPROCY != 1)
         log_fatal("GPU time loop: run one domain (NPROCX = NPROCY = 1); the GPU holds the whole grid\n");
     if (gv->FW > 0 && gv->ABS_TYPE == 2 && gv->SNAP && gv->SNAP_FORMAT != 3)
@@ -176,6 +177,7 @@ void time_loop(int iter, int ishot, int snapcheck, float *hc, float **srcpos_loc
 
     sofi_config c;
     memset(&c, 0, sizeof c);
+    c.fdorder_time = gv->FDORDER_TIME;
     c.weq = gv->WEQ, c.nx = gv->NX, c.ny = gv->NY, c.fdorder = gv->FDORDER, c.maxrelerror = gv->MAXRELERROR;
     c.L = gv->L, c.dt = gv->DT, c.dh = gv->DH, c.nt = gv->NT, c.fw = gv->FW, c.abs_type = gv->ABS_TYPE;
     c.free_surf = gv->FREE_SURF, c.boundary = gv->BOUNDARY, c.seismo = gv->SEISMO, c.ndt = gv->NDT;

@@ -57,6 +57,8 @@ struct Geo {
     // buffer starts psi_xsz / psi_ysz floats after the first
     int psi_pp;
     long long psi_xsz, psi_ysz;
+    int ab4;                // FDORDER_TIME = 4 (Adams-Bashforth)
+    float dhi4;             // 1.0 / DH rounded to float, as the 4th-order updates compute it
     float dt, dh, dtdh, dhi, dthalbe;
     float hc[7];
 };
@@ -68,6 +70,11 @@ struct Wave {
     float *psi_sxx_x, *psi_sxy_x, *psi_vxx, *psi_vyx;  // [s][NY][2FW]
     float *psi_syy_y, *psi_sxy_y, *psi_vyy, *psi_vxy;  // [s][2FW][NX]
     float *draw, *dcor;                        // TTI: 4 derivative fields each, per shot
+    // FDORDER_TIME = 4: four buffers of each history (stress-derivative sums,
+    // velocity derivatives); buffer k of shot s at base + k*ab_lvl + s*fsz.
+    // The memory variables then hold four levels too, ab_mlvl apart.
+    float *svx4, *svy4, *hxx4, *hyy4, *hxy4, *hyx4;
+    long long ab_lvl, ab_mlvl;
 };
 
 // Prepared model arrays (one per shot or shared) and 1-D vectors.

@@ -258,7 +258,10 @@ long long fields_bytes(const sofi_config &c)
     const char *e = getenv("SOFI_TTI");
     const bool tti = kind_of(c.weq) == TTI, split = tti && e && strcmp(e, "split") == 0;
     // acoustic: sxx and syy are one array
-    long long per_shot = (c.weq == SOFI_AC_ISO ? 4 : 5) + 3LL * (is_visco(c.weq) ? c.L : 0) + (split ? 8 : 0);
+    // FDORDER_TIME = 4: 24 history fields, memory variables in four levels
+    const int ab = c.fdorder_time == 4;
+    long long per_shot = (c.weq == SOFI_AC_ISO ? 4 : 5) + 3LL * (is_visco(c.weq) ? c.L : 0) * (ab ? 4 : 1) +
+                         (split ? 8 : 0) + (ab ? 24 : 0);
     long long fw2 = 2LL * c.fw;
     long long psi = (c.abs_type == 1 && c.fw > 0) ? (tti && !split ? 6 : 4) * ((long long)c.ny * fw2 + fw2 * c.nx) : 0;
     long long nmod = c.shared_model ? 1 : c.nshots;
@@ -281,6 +284,11 @@ int check_config(const sofi_config *c)
     // the reference allocates neither mu nor sxy for acoustic media
     // (initmem_model.c:33-39, initmem_wavefield.c:32-39): its free surface and
     // div/curl outputs would read them
+    if (c->fdorder_time != 0 && c->fdorder_time != 2 && c->fdorder_time != 4)
+        return fail(SOFI_E_ARG, "FDORDER_TIME must be 2 or 4 (got %d)", c->fdorder_time);
+    // prepmod.c:160-186: 4th order in time exists for EL_ISO and VEL_ISO only
+    if (c->fdorder_time == 4 && ((c->weq != SOFI_EL_ISO && c->weq != SOFI_VEL_ISO) || c->free_surf))
+        return fail(SOFI_E_ARG, "FDORDER_TIME=4: EL_ISO or VEL_ISO without free surface only");
     if (c->weq == SOFI_AC_ISO && (c->free_surf || c->seismo >= 3 || c->snap >= 3))
         return fail(SOFI_E_ARG, "acoustic media: no free surface and no div/curl (SEISMO, SNAP <= 2)");
     if (c->fdorder < 2 || c->fdorder > 12 || (c->fdorder & 1))
@@ -515,7 +523,7 @@ int time_launches(sofi_ctx *c, F launch, float *ms)
 int autotune(sofi_ctx *c)
 {
     c->tuned = true;
-    if (c->march)
+    if (c->march || c->G.ab4)
         return 0;
     const sofi_config &cf = c->cfg;
     const int kind = kind_of(cf.weq);
@@ -589,6 +597,10 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
         k_force_src<<<nb, 128, 0, st>>>(G, c->W, c->M, c->A);
         c->launches++;
     }
+    if (G.ab4) {  // 4th order: every block of the velocity kernel reads the step number
+        launch_ab4_begin(G, st);
+        c->launches++;
+    }
     bool timed = !capture && c->time_every > 0 && (nt % c->time_every) == 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
     if (timed) {
@@ -603,7 +615,10 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
         c->tev_used += 3;
         CK(cudaEventRecord(e0, st));
     }
-    launch_v(c, G, st);
+    if (G.ab4)
+        launch_ab4_v(G, c->W, c->M, c->nd, grd, st);
+    else
+        launch_v(c, G, st);
     c->launches++;
     if (timed)
         CK(cudaEventRecord(e1, st));
@@ -613,7 +628,9 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
     }
     if (timed && cf.boundary)
         CK(cudaEventRecord(e1, st));
-    if (kind == TTI && c->tti_split) {
+    if (G.ab4) {
+        launch_ab4_s(G, c->W, c->M, c->nd, visco, grd, st);
+    } else if (kind == TTI && c->tti_split) {
         c->launches++;
         launch_tti_split(G, c->W, c->M, c->nd, visco, grd, st);
     } else if (kind == TTI) {
@@ -699,6 +716,8 @@ float *field_ptr(sofi_ctx *c, int shot, const char *name)
         if (l >= c->G.L)
             return nullptr;
         float *b = name[0] == 'r' ? c->W.r : (name[0] == 'p' ? c->W.p : c->W.q);
+        if (c->G.ab4)  // the level the last step wrote
+            b += (long long)(c->step & 3) * c->W.ab_mlvl;
         return b + ((long long)shot * c->G.L + l) * c->G.fsz;
     }
     return nullptr;
@@ -819,6 +838,9 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
     G.el_tti_rb_short = (cfg->weq == SOFI_EL_TTI);
     G.shot_fast = (cfg->shared_model && cfg->nshots > 1) ? 1 : 0;
     G.seismo = cfg->seismo, G.ndt = cfg->ndt;
+    G.ab4 = cfg->fdorder_time == 4;
+    G.dhi4 = (float)(1.0 / (double)cfg->dh);
+    c->W.ab_lvl = (long long)G.fsz * cfg->nshots;
     if (const char *e = getenv("SOFI_SHOT_ORDER"))
         G.shot_fast = G.shot_fast && strcmp(e, "slow") != 0;
     // subgrid_bounds.c:65-66,260-270 (one rank); without a frame the whole grid is interior
@@ -848,7 +870,14 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
     if (G.L) {
         float **m[3] = {&c->W.r, &c->W.p, &c->W.q};
         for (auto p : m)
-            if ((rc = dalloc(c, (void **)p, f * G.L)))
+            if ((rc = dalloc(c, (void **)p, f * G.L * (G.ab4 ? 4 : 1))))
+                goto bad;
+    }
+    c->W.ab_mlvl = (long long)G.fsz * cfg->nshots * G.L;
+    if (G.ab4) {
+        float **h[6] = {&c->W.svx4, &c->W.svy4, &c->W.hxx4, &c->W.hyy4, &c->W.hxy4, &c->W.hyx4};
+        for (auto p : h)
+            if ((rc = dalloc(c, (void **)p, f * 4)))
                 goto bad;
     }
     if (G.abs_type == 1) {
@@ -1054,8 +1083,16 @@ int sofi_reset(sofi_ctx *c, int shot)
             CK(cudaMemsetAsync(p + (long long)s * c->G.fsz, 0, f, c->stream));
         if (c->G.L) {
             float *m[3] = {c->W.r, c->W.p, c->W.q};
-            for (auto p : m)
-                CK(cudaMemsetAsync(p + (long long)s * c->G.L * c->G.fsz, 0, f * c->G.L, c->stream));
+            for (int k = 0; k < (c->G.ab4 ? 4 : 1); k++)
+                for (auto p : m)
+                    CK(cudaMemsetAsync(p + k * c->W.ab_mlvl + (long long)s * c->G.L * c->G.fsz, 0, f * c->G.L,
+                                       c->stream));
+        }
+        if (c->G.ab4) {
+            float *h[6] = {c->W.svx4, c->W.svy4, c->W.hxx4, c->W.hyy4, c->W.hxy4, c->W.hyx4};
+            for (int k = 0; k < 4; k++)
+                for (auto p : h)
+                    CK(cudaMemsetAsync(p + k * c->W.ab_lvl + (long long)s * c->G.fsz, 0, f, c->stream));
         }
         if (c->G.abs_type == 1) {
             size_t px = sizeof(float) * (size_t)c->cfg.ny * c->G.fw2, py = sizeof(float) * (size_t)c->G.fw2 * c->cfg.nx;

@@ -29,7 +29,7 @@ class SofihPar(ctypes.Structure):
                 ("tsnap1", ctypes.c_float), ("tsnap2", ctypes.c_float), ("tsnapinc", ctypes.c_float),
                 ("idx", ctypes.c_int), ("idy", ctypes.c_int), ("snap_file", ctypes.c_char * 256),
                 ("mfile", ctypes.c_char * 256), ("sigout", ctypes.c_int), ("sigout_format", ctypes.c_int),
-                ("sigout_file", ctypes.c_char * 256)]
+                ("sigout_file", ctypes.c_char * 256), ("fdorder_time", ctypes.c_int)]
 
 
 _LIB = None
@@ -86,6 +86,7 @@ def read_par(path: str) -> SofihPar:
 def make_par(**kw) -> SofihPar:
     p = SofihPar()
     p.npower, p.k_max_cpml, p.damping, p.ndt, p.idx, p.idy, p.readrec = 2.0, 1.0, 8.0, 1, 1, 1, 1
+    p.fdorder_time = 2
     for k, v in kw.items():
         if k == "fl":
             for i, f in enumerate(v):

@@ -33,7 +33,8 @@ def _ip(a: np.ndarray):
 def make_config(**kw) -> N.SofiConfig:
     c = N.SofiConfig()
     defaults = dict(weq=2, fdorder=4, maxrelerror=0, L=0, fw=0, abs_type=0, free_surf=0, boundary=0, seismo=0,
-                    ndt=1, snap=0, snap_first=0, snap_inc=0, snap_last=0, idx=1, idy=1, nshots=1, shared_model=1)
+                    ndt=1, snap=0, snap_first=0, snap_inc=0, snap_last=0, idx=1, idy=1, nshots=1, shared_model=1,
+                    fdorder_time=2)
     defaults.update(kw)
     for k, v in defaults.items():
         if isinstance(v, str) and k == "weq":

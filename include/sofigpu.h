@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define SOFI_ABI_VERSION 1
+#define SOFI_ABI_VERSION 2
 
 /* status codes */
 #define SOFI_OK 0
@@ -84,6 +84,8 @@ typedef struct {
     int idx, idy;       /* snapshot subsampling                          (gv->IDX, IDY) */
     int nshots;         /* resident shots in this context (>= 1) */
     int shared_model;   /* 1: one model for all shots, 0: one model per shot */
+    int fdorder_time;   /* 2 (or 0): leapfrog; 4: Adams-Bashforth, EL_ISO / VEL_ISO
+                           without free surface                 (gv->FDORDER_TIME) */
 } sofi_config;
 
 /* ---- context ---------------------------------------------------------- */

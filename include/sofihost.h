@@ -43,6 +43,7 @@ typedef struct {
     char snap_file[256], mfile[256];
     int sigout, sigout_format;  /* source wavelet output (initsrc.c:64-93): 1 SU, 2 ASCII, 3 binary */
     char sigout_file[256];
+    int fdorder_time;           /* 2 leapfrog, 4 Adams-Bashforth (gv->FDORDER_TIME) */
 } sofih_par;
 
 const char *sofih_last_error(void);

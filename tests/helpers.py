@@ -162,7 +162,7 @@ def gpu_config_from(cfg, nshots=1, shared_model=1, snap_override=None):
                        L=cfg.L, dt=cfg.dt, dh=cfg.dh, nt=cfg.nt, fw=cfg.fw, abs_type=cfg.abs_type,
                        free_surf=cfg.free_surf, boundary=cfg.boundary, seismo=cfg.seismo, ndt=cfg.ndt,
                        snap=snap, snap_first=first, snap_inc=inc, snap_last=last, idx=cfg.idx, idy=cfg.idy,
-                       nshots=nshots, shared_model=shared_model)
+                       nshots=nshots, shared_model=shared_model, fdorder_time=getattr(cfg, "fdorder_time", 2))
 
 
 def prepared_model(o, cfg):

@@ -26,7 +26,9 @@ def test_library_exports_every_declared_symbol(built):
 
 
 def test_abi_version(built):
-    assert N.load().sofi_abi_version() == 1
+    assert N.load().sofi_abi_version() == 2  # 2: sofi_config gained fdorder_time
+    import ctypes
+    assert ctypes.sizeof(N.SofiConfig) == 24 * 4  # the C struct: 22 ints and 2 floats
 
 
 def test_bad_config_reports_error_without_gpu(built):

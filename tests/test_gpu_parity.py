@@ -72,7 +72,7 @@ def test_gpu_matches_oracle_synthetic(case):
     o.close()
 
 
-@pytest.mark.parametrize("name", ["weq3", "weq4", "weq5", "weq6", "weq7", "weq8"])
+@pytest.mark.parametrize("name", ["weq3", "weq4", "weq5", "weq6", "weq7", "weq8", "weq3_fdt4", "weq4_fdt4"])
 def test_gpu_matches_oracle_examples(name):
     from oracle import oracle as O
     from tests.helpers import example_config, example_inputs

@@ -24,7 +24,8 @@ def par_from_case(H, case, cfg):
     return H.make_par(weq=cfg.weq, nx=cfg.nx, ny=cfg.ny, dh=cfg.dh, dt=cfg.dt, nt=cfg.nt, fdorder=cfg.fdorder,
                       maxrelerror=cfg.maxrelerror, L=cfg.L, f_ref=cfg.f_ref, fl=cfg.fl, fw=cfg.fw,
                       abs_type=cfg.abs_type, free_surf=cfg.free_surf, boundary=cfg.boundary, npower=cfg.npower,
-                      k_max_cpml=cfg.k_max_cpml, vppml=cfg.vppml, fpml=cfg.fpml, damping=cfg.damping)
+                      k_max_cpml=cfg.k_max_cpml, vppml=cfg.vppml, fpml=cfg.fpml, damping=cfg.damping,
+                      fdorder_time=cfg.fdorder_time)
 
 
 @pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
