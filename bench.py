@@ -144,7 +144,7 @@ def cpu_sample(W, nsteps, nthreads):
     par = W["par"]
     cfg = O.SofiConfig()
     for k in ["weq", "nx", "ny", "dh", "dt", "fdorder", "maxrelerror", "L", "fw", "abs_type", "free_surf",
-              "npower", "k_max_cpml", "vppml", "fpml", "seismo", "ndt"]:
+              "npower", "k_max_cpml", "vppml", "fpml", "seismo", "ndt", "fdorder_time"]:
         if k in par:
             setattr(cfg, k, par[k])
     cfg.f_ref, cfg.fl = par.get("f_ref", 0.0), list(par.get("fl", []))
@@ -345,7 +345,7 @@ def main():
     if not stable:
         raise SystemExit(f"workload {W['name']} violates the stability bound (DT_max {dt_max})")
     nshots = W["nshots"]
-    cfg = make_config(weq=par["weq"], nx=par["nx"], ny=par["ny"], fdorder=par["fdorder"],
+    cfg = make_config(weq=par["weq"], nx=par["nx"], ny=par["ny"], fdorder=par["fdorder"], fdorder_time=par.get("fdorder_time", 2),
                       maxrelerror=par["maxrelerror"], L=par.get("L", 0), dt=par["dt"], dh=par["dh"], nt=par["nt"],
                       fw=par["fw"], abs_type=par["abs_type"], free_surf=par.get("free_surf", 0), seismo=par["seismo"],
                       ndt=par["ndt"], nshots=nshots, shared_model=1)
@@ -383,7 +383,7 @@ def main():
 
     # ---- device-timed region: inputs resident in HBM ----
     peak, peak_kind = measured_peaks()
-    bpc = workloads.bytes_per_cell(par["weq"], par.get("L", 0))
+    bpc = workloads.bytes_per_cell(par["weq"], par.get("L", 0), par.get("fdorder_time", 2))
     t.set_kernel_timing(33)  # graph chunks of 32 steps run between the timed direct steps
     launches0 = t.launch_count()
     if world > 1:
@@ -435,6 +435,8 @@ def main():
     ach_s = bpc["update_s"] * ncell / (ms_s * 1e-3) / 1e9 if ms_s else None
     traffic = traffic_from_profiles("update_s", W["name"])
     kname = {0: "k_update_s_ac (pressure)", 6: "k_tti_fused (TTI stress)", 7: "k_tti_fused (TTI stress + memory variables)"}
+    if par.get("fdorder_time", 2) == 4:
+        kname = {par["weq"]: "k_update_s_ab4 (Adams-Bashforth stress, histories, memory variables)"}
     roof = {"kernel": kname.get(par["weq"], "k_update_sw / k_update_s (stress + memory variables)"), "bound": "hbm",
             "achieved": round(ach_s, 1) if ach_s else None, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
             "frac": round(ach_s / peak, 4) if ach_s else None,
@@ -447,7 +449,7 @@ def main():
     batched = None
     if nshots > 1:
         # the same shots one at a time: a single-shot context on the same model
-        t1 = TimeLoop(make_config(weq=par["weq"], nx=par["nx"], ny=par["ny"], fdorder=par["fdorder"],
+        t1 = TimeLoop(make_config(weq=par["weq"], nx=par["nx"], ny=par["ny"], fdorder=par["fdorder"], fdorder_time=par.get("fdorder_time", 2),
                                   maxrelerror=par["maxrelerror"], L=par.get("L", 0), dt=par["dt"], dh=par["dh"],
                                   nt=par["nt"], fw=par["fw"], abs_type=par["abs_type"],
                                   free_surf=par.get("free_surf", 0), seismo=par["seismo"], ndt=par["ndt"]),

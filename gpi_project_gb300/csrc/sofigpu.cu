@@ -1301,8 +1301,8 @@ int sofi_velocity_variant(sofi_ctx *c, int *cells_per_thread, int *rows_per_thre
 {
     if (!c || !cells_per_thread || !rows_per_thread)
         return fail(SOFI_E_ARG, "null argument");
-    *cells_per_thread = c->vw ? c->vw : 1;
-    *rows_per_thread = c->vw ? 1 : c->vrows;
+    *cells_per_thread = (c->vw && !c->G.ab4) ? c->vw : 1;  // 4th order: one cell per thread
+    *rows_per_thread = (c->vw || c->G.ab4) ? 1 : c->vrows;
     return 0;
 }
 
@@ -1310,7 +1310,7 @@ int sofi_stress_variant(sofi_ctx *c, int *cells_per_thread)
 {
     if (!c || !cells_per_thread)
         return fail(SOFI_E_ARG, "null argument");
-    *cells_per_thread = kind_of(c->cfg.weq) == TTI ? 1 : (c->sw ? c->sw : 1);
+    *cells_per_thread = (kind_of(c->cfg.weq) == TTI || c->G.ab4) ? 1 : (c->sw ? c->sw : 1);
     return 0;
 }
 

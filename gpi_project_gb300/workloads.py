@@ -16,6 +16,9 @@ benchmark configurations with their shapes, sizes and value distributions:
       tilt 0-45 deg, each field smoothed by a Gaussian of sigma 20 cells; explosive Ricker 20 Hz; 512 receivers
   c4  64 shots on the c1 layered model enlarged to 2000 x 1000 with c2's Q field
       and L = 3, NT 4000, explosive sources spread across the surface
+  fdt4  c2's viscoelastic model and grid with 4th-order Adams-Bashforth time
+      stepping (FDORDER_TIME 4): no free surface (the reference has none for
+      it), DT 1e-4 s (the smaller stability region of the scheme), NT 6000
   ac  acoustic (AC_ISO) on c2's geometry: 4000 x 2000, DH 2 m, DT 2e-4 s, NT 6000,
       FD8, CPML 30; c2's smooth Vp field and Gardner density; explosive Ricker
       15 Hz; 1000 receivers recording pressure
@@ -108,6 +111,13 @@ def workload(name: str) -> dict:
         xs = np.linspace(21 * 2.5, (nx - 22) * 2.5, 512)
         rec = (np.floor(xs / 2.5).astype(np.int32) + 1, np.full(512, 25, np.int32))
         nshots = 1
+    elif name == "fdt4":
+        W = workload("c2")
+        W["name"] = "fdt4"
+        W["par"].update(free_surf=0, dt=1e-4, fdorder_time=4)
+        W["src"] = _srcpos([(4000.0, 100.0)], 2.0, 15.0, 3)
+        W["rec"] = (W["rec"][0], np.full(1000, 40, np.int32))
+        return W
     elif name == "ac":
         rng = np.random.default_rng(1002)
         nx, ny = 4000, 2000
@@ -143,8 +153,16 @@ def workload(name: str) -> dict:
 # Algorithmic bytes per cell-update (each evolving state array read and written
 # once, each per-cell coefficient array read once; CPML frame memory, sources
 # and receivers not credited).
-def bytes_per_cell(weq: int, L: int) -> dict:
-    """Per-kernel and whole-step algorithmic bytes of one cell-update."""
+def bytes_per_cell(weq: int, L: int, fdorder_time: int = 2) -> dict:
+    """Per-kernel and whole-step algorithmic bytes of one cell-update.
+
+    FDORDER_TIME 4 (EL_ISO / VEL_ISO): each history (svx, svy; vxx, vyy, vxy,
+    vyx) reads three levels and writes one (16 B), each memory variable reads
+    four levels and writes one (20 B)."""
+    if fdorder_time == 4:
+        v = 36 + 2 * 16
+        s = 8 + 24 + 4 * 16 + (12 + 60 * L + 12 if weq == 3 else 12)
+        return {"update_v": v, "update_s": s, "step": 40 + 2 * 16 + 4 * 16 + 60 * L + (32 if weq == 3 else 20)}
     if weq == 0:  # acoustic: vx, vy, p; rip, rjp, g
         return {"update_v": 28, "update_s": 20, "step": 36}
     if weq == 2:
