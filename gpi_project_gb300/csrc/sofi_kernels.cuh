@@ -458,7 +458,7 @@ __global__ void __launch_bounds__(BX *BY) k_update_s(Geo G, Wave W, Model M)
 // vectors; per cell the arithmetic of k_update_s, term by term. Reads past
 // column NX + ND feed only cells past NX, which are never stored.
 template <int ND, int KIND, bool VISCO, int LT, int VW>
-__global__ void __launch_bounds__(BX *BY) k_update_sw(Geo G, Wave W, Model M)
+__global__ void __launch_bounds__(BX *BY, VW == 4 ? 2 : 1) k_update_sw(Geo G, Wave W, Model M)
 {
     constexpr int K = (ND + VW - 1) / VW;
     constexpr int NXS = VW * (2 * K + 1);
