@@ -487,7 +487,7 @@ def main():
                 "d2h_bytes_per_step": int(d2h_bytes)},
         "roofline": roof, "step_roofline": step_roof, "gpu_launches": int(launches),
         "autotune": {**dict(zip(["velocity_cells_per_thread", "velocity_rows_per_thread"], t.velocity_variant())),
-                     "stress_cells_per_thread": t.stress_variant()},
+                     "velocity_pipelined": t.velocity_pipelined(), "stress_cells_per_thread": t.stress_variant()},
         **({"batched": batched} if batched else {}),
         "clocks": clk.summary(),
     }

@@ -103,6 +103,7 @@ def load():
         "sofi_launch_count": ([vp, P(ctypes.c_longlong)], ctypes.c_int),
         "sofi_velocity_variant": ([vp, P(ctypes.c_int), P(ctypes.c_int)], ctypes.c_int),
         "sofi_stress_variant": ([vp, P(ctypes.c_int)], ctypes.c_int),
+        "sofi_velocity_pipelined": ([vp, P(ctypes.c_int)], ctypes.c_int),
         "sofi_get_stream": ([vp, P(vp)], ctypes.c_int),
         "sofi_tti_stress_noalloc": ([P(SofiConfig), P(TtiStressArgs), vp], ctypes.c_int),
     }

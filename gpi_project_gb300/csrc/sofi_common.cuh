@@ -6,6 +6,9 @@
 //                  R rows per thread), CPML / damping frame by predicate
 //                  (update_v_interior.c, update_v_PML.c, update_v_abs.c); advances
 //                  the device step counter
+//   k_update_vt    the same velocity update fed by TMA copies of the stress tiles
+//                  into a ring of shared-memory stages, marching down column
+//                  strips (sofi_vpipe.cuh)
 //   k_wrap_x       periodic x only: ghost columns (exchange_v.c / exchange_s.c, one rank)
 //   k_update_sw    ISO / VTI stress update, 2 or 4 cells per thread (k_update_s: one
 //                  cell), velocity derivatives recomputed from v in registers
@@ -52,6 +55,7 @@ struct Geo {
     int shot_fast;          // block index: shot varies fastest (model tiles shared in L2)
     int seismo, ndt;        // sampling (gv->SEISMO, gv->NDT)
     int *step_ctr;          // device: time steps completed; the velocity kernel advances it
+    int *fault;             // device: bits set by a pipelined kernel whose bounded wait gave up
     // TTI CPML memory of the velocity derivatives in two buffers (psi_pp = 1):
     // step n reads buffer (n - 1) & 1 and writes buffer n & 1; the second
     // buffer starts psi_xsz / psi_ysz floats after the first

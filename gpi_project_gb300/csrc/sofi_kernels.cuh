@@ -182,11 +182,81 @@ __device__ __forceinline__ void stv(float *p, const float *v)
         *reinterpret_cast<float2 *>(p) = make_float2(v[0], v[1]);
 }
 
+// The end of a velocity update of VW adjacent cells (columns i .. i+VW-1, row
+// j, padded offset o) from the four stress derivatives: CPML stretch and
+// memory (cpml_update.c), vx/vy update (wavefield_update_v.c / _ac.c),
+// damping frame (update_v_abs.c) and the store of the cells i + c <= NX.
+// ox/oy: the old velocities, rp/rq: the cells' rip / rjp.
+template <int VW, bool SXY>
+__device__ __forceinline__ void v_finish(const Geo &G, const Wave &W, const Model &M, int s, int i, int j, int o,
+                                         long long mo, float *__restrict__ vx, float *__restrict__ vy,
+                                         const float *ox, const float *oy, const float *rp, const float *rq,
+                                         const float *sxx_x, const float *sxy_x, const float *sxy_y,
+                                         const float *syy_y)
+{
+    const int yr = yside(G, j);
+    const bool xframe = i <= G.gx2 || i + VW - 1 > G.gx3;  // any of the cells in a left/right frame
+    float nvx[VW], nvy[VW];
+#pragma unroll
+    for (int c = 0; c < VW; c++) {
+        const int ic = i + c;
+        float fx = sxx_x[c], fxy = sxy_x[c], fyx = sxy_y[c], fy = syy_y[c];
+        const int xr = xframe ? xside(G, ic) : 0;
+        if (G.abs_type == 1 && ic <= G.nx) {
+            if (xr) {
+                int h = xr == 1 ? ic : ic - G.nx + G.fw2;
+                long long q = ((long long)s * G.ny + (j - 1)) * G.fw2 + (h - 1);
+                float ps = M.b_x_half[h - 1] * W.psi_sxx_x[q] + M.a_x_half[h - 1] * fx;
+                W.psi_sxx_x[q] = ps;
+                fx = fx / M.K_x_half[h - 1] + ps;
+                if (SXY) {
+                    float py = M.b_x[h - 1] * W.psi_sxy_x[q] + M.a_x[h - 1] * fxy;
+                    W.psi_sxy_x[q] = py;
+                    fxy = fxy / M.K_x[h - 1] + py;
+                }
+            }
+            if (yr) {
+                int h = yr == 1 ? j : j - G.ny + G.fw2;
+                long long q = ((long long)s * G.fw2 + (h - 1)) * G.nx + (ic - 1);
+                float ps = M.b_y_half[h - 1] * W.psi_syy_y[q] + M.a_y_half[h - 1] * fy;
+                W.psi_syy_y[q] = ps;
+                fy = fy / M.K_y_half[h - 1] + ps;
+                if (SXY) {
+                    float py = M.b_y[h - 1] * W.psi_sxy_y[q] + M.a_y[h - 1] * fyx;
+                    W.psi_sxy_y[q] = py;
+                    fyx = fyx / M.K_y[h - 1] + py;
+                }
+            }
+        }
+        if (SXY) {
+            nvx[c] = ox[c] + (fx + fyx) * G.dtdh * rp[c];
+            nvy[c] = oy[c] + (fxy + fy) * G.dtdh * rq[c];
+        } else {
+            nvx[c] = ox[c] + fx * G.dtdh * rp[c];
+            nvy[c] = oy[c] + fy * G.dtdh * rq[c];
+        }
+        if (G.abs_type == 2 && (xr | yr)) {
+            float a = __ldg(M.absorb + mo + o + c);
+            nvx[c] *= a;
+            nvy[c] *= a;
+        }
+    }
+    if (i + VW - 1 <= G.nx) {
+        stv<VW>(vx + o, nvx);
+        stv<VW>(vy + o, nvy);
+    } else {
+#pragma unroll
+        for (int c = 0; c < VW; c++)
+            if (i + c <= G.nx)
+                vx[o + c] = nvx[c], vy[o + c] = nvy[c];
+    }
+}
+
 // SXY = false: the acoustic update (wavefield_update_v_ac.c), which has no
 // sxy: vx += sxx_x * DT/DH * rip, vy += syy_y * DT/DH * rjp (sxx and syy are
 // one pressure array); VW may then also be 1.
 template <int ND, int VW, bool SXY = true>
-__global__ void __launch_bounds__(BX *BY) k_update_vw(Geo G, Wave W, Model M)
+__global__ void __launch_bounds__(BX *BY, VW == 4 ? 4 : 1) k_update_vw(Geo G, Wave W, Model M)
 {
     constexpr int K = (ND + VW - 1) / VW;
     constexpr int NXS = VW * (2 * K + 1);  // stencil row: columns i - VW K .. i + VW K + VW - 1
@@ -256,62 +326,7 @@ __global__ void __launch_bounds__(BX *BY) k_update_vw(Geo G, Wave W, Model M)
     float ox[VW], oy[VW], rp[VW], rq[VW];
     ldv_rw<VW>(vx + o, ox), ldv_rw<VW>(vy + o, oy);
     ldv<VW>(M.prip + mo + o, rp), ldv<VW>(M.prjp + mo + o, rq);
-    const int yr = yside(G, j);
-    const bool xframe = i <= G.gx2 || i + VW - 1 > G.gx3;  // any of the cells in a left/right frame
-    float nvx[VW], nvy[VW];
-#pragma unroll
-    for (int c = 0; c < VW; c++) {
-        const int ic = i + c;
-        float fx = sxx_x[c], fxy = sxy_x[c], fyx = sxy_y[c], fy = syy_y[c];
-        const int xr = xframe ? xside(G, ic) : 0;
-        if (G.abs_type == 1 && ic <= G.nx) {
-            if (xr) {
-                int h = xr == 1 ? ic : ic - G.nx + G.fw2;
-                long long q = ((long long)s * G.ny + (j - 1)) * G.fw2 + (h - 1);
-                float ps = M.b_x_half[h - 1] * W.psi_sxx_x[q] + M.a_x_half[h - 1] * fx;
-                W.psi_sxx_x[q] = ps;
-                fx = fx / M.K_x_half[h - 1] + ps;
-                if (SXY) {
-                    float py = M.b_x[h - 1] * W.psi_sxy_x[q] + M.a_x[h - 1] * fxy;
-                    W.psi_sxy_x[q] = py;
-                    fxy = fxy / M.K_x[h - 1] + py;
-                }
-            }
-            if (yr) {
-                int h = yr == 1 ? j : j - G.ny + G.fw2;
-                long long q = ((long long)s * G.fw2 + (h - 1)) * G.nx + (ic - 1);
-                float ps = M.b_y_half[h - 1] * W.psi_syy_y[q] + M.a_y_half[h - 1] * fy;
-                W.psi_syy_y[q] = ps;
-                fy = fy / M.K_y_half[h - 1] + ps;
-                if (SXY) {
-                    float py = M.b_y[h - 1] * W.psi_sxy_y[q] + M.a_y[h - 1] * fyx;
-                    W.psi_sxy_y[q] = py;
-                    fyx = fyx / M.K_y[h - 1] + py;
-                }
-            }
-        }
-        if (SXY) {
-            nvx[c] = ox[c] + (fx + fyx) * G.dtdh * rp[c];
-            nvy[c] = oy[c] + (fxy + fy) * G.dtdh * rq[c];
-        } else {
-            nvx[c] = ox[c] + fx * G.dtdh * rp[c];
-            nvy[c] = oy[c] + fy * G.dtdh * rq[c];
-        }
-        if (G.abs_type == 2 && (xr | yr)) {
-            float a = __ldg(M.absorb + mo + o + c);
-            nvx[c] *= a;
-            nvy[c] *= a;
-        }
-    }
-    if (i + VW - 1 <= G.nx) {
-        stv<VW>(vx + o, nvx);
-        stv<VW>(vy + o, nvy);
-    } else {
-#pragma unroll
-        for (int c = 0; c < VW; c++)
-            if (i + c <= G.nx)
-                vx[o + c] = nvx[c], vy[o + c] = nvy[c];
-    }
+    v_finish<VW, SXY>(G, W, M, s, i, j, o, mo, vx, vy, ox, oy, rp, rq, sxx_x, sxy_x, sxy_y, syy_y);
 }
 
 // Periodic x (BOUNDARY = 1): ghost columns copy the opposite edge, as the one-

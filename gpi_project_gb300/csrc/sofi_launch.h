@@ -1,6 +1,7 @@
 // sofi_launch.h -- host launchers of kernels compiled in other translation
 // units (so that the template instantiations compile in parallel).
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace sofi {
@@ -16,6 +17,18 @@ void launch_march_s(const Geo &G, const Wave &W, const Model &M, int nd, int kin
 // acoustic: no sxy terms, vw 4, 2 or else one cell per thread
 void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw, int vrows, bool acoustic,
                      dim3 grid, cudaStream_t st);
+// The TMA-fed velocity pipeline (k_update_vt): tensor maps of sxx / sxy / syy
+// over all shots' padded fields, and the number of row segments per strip
+// that fills the GPU's resident blocks once.
+struct VtPlan {
+    CUtensorMap xx, xy, yy;
+    int segs = 0;      // 0: the pipeline is not available for this context
+    int strips = 0;
+};
+// 0, or a message (static storage) naming what failed
+const char *plan_velocity_pipeline(const Geo &G, const Wave &W, int nd, int device, VtPlan *plan);
+void launch_velocity_pipeline(const Geo &G, const Wave &W, const Model &M, int nd, const VtPlan &plan,
+                              cudaStream_t st);
 // ISO / VTI stress update (KIND 0 ISO, 1 VTI): sw cells per thread in x (4, 2 or 0 = one)
 template <int KIND, bool VISCO>
 void launch_stress_kv(const Geo &G, const Wave &W, const Model &M, int nd, int sw, dim3 grid, cudaStream_t st);

@@ -187,6 +187,8 @@ struct sofi_ctx {
     bool march = false;        // y-marching kernels (ISO/VTI stress, all velocity updates)
     int vw = 4;                // velocity kernel: cells per thread in x (4 or 2), 0 = vrows rows per thread
     int vrows = 1;             // rows per thread of the one-cell velocity kernel (1, 2 or 4)
+    bool vpipe = false;        // the TMA-fed velocity pipeline (needs vplan.segs > 0)
+    VtPlan vplan;              // its tensor maps and segments (segs 0: not available)
     int sw = 0;                // ISO / VTI stress kernel: cells per thread in x (4 or 2), 0 = one
     bool sw_fixed = false;     // SOFI_SW chose it
     bool tuned = false;        // autotuner ran (or was skipped) for this context
@@ -467,7 +469,8 @@ void launch_cell_s(const Geo &G, const Wave &W, const Model &M, int nd, int kind
 // One time step. `capture`: being recorded into the step graph, so no host-
 // side step number exists (no timing events, no snapshot).
 // The velocity kernel in the context's variant: c->vw cells per thread in x
-// (2 or 4), else c->vrows rows per thread, or the y-marching kernel.
+// (2 or 4), else c->vrows rows per thread, the TMA-fed pipeline (c->vpipe)
+// or the y-marching kernel.
 void launch_v(sofi_ctx *c, const Geo &G, cudaStream_t st)
 {
     const sofi_config &cf = c->cfg;
@@ -477,6 +480,10 @@ void launch_v(sofi_ctx *c, const Geo &G, cudaStream_t st)
         return;
     }
     const bool ac = cf.weq == SOFI_AC_ISO;  // acoustic: one cell per thread when not vectorised
+    if (c->vpipe && c->vplan.segs && !ac) {
+        launch_velocity_pipeline(G, c->W, c->M, c->nd, c->vplan, st);
+        return;
+    }
     const int R = (c->vw || ac) ? 1 : c->vrows, cx = c->vw ? c->vw : 1;
     const unsigned tx = (cf.nx + cx * BX - 1) / (cx * BX), ty = (cf.ny + BY * R - 1) / (BY * R);
     const dim3 gv = G.shot_fast ? dim3(tx * S, ty, 1) : dim3(tx, ty, S);
@@ -492,6 +499,7 @@ void launch_v(sofi_ctx *c, const Geo &G, cudaStream_t st)
 // the process. SOFI_VROWS / SOFI_SW fix a choice.
 struct Tuned {
     int vw, vrows, sw;
+    bool vpipe;
 };
 std::mutex g_tune_mu;
 std::map<std::string, Tuned> g_tune;
@@ -540,7 +548,7 @@ int autotune(sofi_ctx *c)
         auto it = g_tune.find(key);
         if (it != g_tune.end()) {
             if (!c->tune_fixed)
-                c->vw = it->second.vw, c->vrows = it->second.vrows;
+                c->vw = it->second.vw, c->vrows = it->second.vrows, c->vpipe = it->second.vpipe;
             if (tune_s)
                 c->sw = it->second.sw;
             c->graph_dirty = true;
@@ -551,7 +559,7 @@ int autotune(sofi_ctx *c)
         return 0;  // state not known to be zero: keep the default variants
     Geo G = c->G;
     G.step_ctr = nullptr;  // tuning launches are not steps
-    Tuned pick{c->vw, c->vrows, c->sw};
+    Tuned pick{c->vw, c->vrows, c->sw, c->vpipe};
     float best = 1e30f, ms = 0.f;
     int rc;
     // two interleaved rounds over the candidates, each candidate's best time:
@@ -559,19 +567,21 @@ int autotune(sofi_ctx *c)
     // L2, which would otherwise penalise whichever candidate goes first
     constexpr int kRounds = 2;
     if (!c->tune_fixed) {
-        const int cand[3][2] = {{4, 1}, {2, 1}, {0, 1}};
-        float t[3] = {1e30f, 1e30f, 1e30f};
+        // {cells per thread, rows per thread, pipeline}; the acoustic update has no pipelined form
+        const int cand[4][3] = {{4, 1, 0}, {2, 1, 0}, {0, 1, 0}, {4, 1, 1}};
+        const int nc = (cf.weq == SOFI_AC_ISO || !c->vplan.segs) ? 3 : 4;
+        float t[4] = {1e30f, 1e30f, 1e30f, 1e30f};
         for (int r = 0; r < kRounds; r++)
-            for (int k = 0; k < 3; k++) {
-                c->vw = cand[k][0], c->vrows = cand[k][1];
+            for (int k = 0; k < nc; k++) {
+                c->vw = cand[k][0], c->vrows = cand[k][1], c->vpipe = cand[k][2];
                 if ((rc = time_launches(c, [&] { launch_v(c, G, c->stream); }, &ms)))
                     return rc;
                 t[k] = ms < t[k] ? ms : t[k];
             }
-        for (int k = 0; k < 3; k++)
+        for (int k = 0; k < nc; k++)
             if (t[k] < best)
-                best = t[k], pick.vw = cand[k][0], pick.vrows = cand[k][1];
-        c->vw = pick.vw, c->vrows = pick.vrows;
+                best = t[k], pick.vw = cand[k][0], pick.vrows = cand[k][1], pick.vpipe = cand[k][2];
+        c->vw = pick.vw, c->vrows = pick.vrows, c->vpipe = pick.vpipe;
     }
     if (tune_s) {
         const int cand[3] = {4, 2, 0};
@@ -593,7 +603,7 @@ int autotune(sofi_ctx *c)
     }
     c->graph_dirty = true;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune[key] = Tuned{c->vw, c->vrows, c->sw};
+    g_tune[key] = Tuned{c->vw, c->vrows, c->sw, c->vpipe};
     return 0;
 }
 
@@ -686,9 +696,12 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
 
 int check_status(sofi_ctx *c)
 {
-    std::vector<int> st(c->cfg.nshots);
+    std::vector<int> st(c->cfg.nshots + 2);  // shots, step counter, fault word
     CK(cudaMemcpyAsync(st.data(), c->d_status, sizeof(int) * st.size(), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    if (st[c->cfg.nshots + 1])
+        return fail(SOFI_E_CUDA, "velocity pipeline: a bounded shared-memory stage wait gave up (fault bits %#x)",
+                    st[c->cfg.nshots + 1]);
     for (int s = 0; s < c->cfg.nshots; s++)
         if (st[s])
             return fail(SOFI_E_UNSTABLE, "shot %d: simulation is unstable (NaN at the probe cell after step %d)", s,
@@ -820,9 +833,12 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
         c->march = strcmp(e, "march") == 0;
     if (const char *e = getenv("SOFI_VROWS"))
     {
-        // SOFI_VROWS: "w4" / "w2" cells per thread in x, "1" / "2" / "4" rows per thread
-        const int v = e[0] == 'w' ? atoi(e + 1) : atoi(e);
-        c->vw = e[0] == 'w' ? (v == 2 ? 2 : 4) : 0;
+        // SOFI_VROWS: "w4" / "w2" cells per thread in x, "t4" the TMA-fed pipeline
+        // (four cells per thread), "1" / "2" / "4" rows per thread
+        const bool wide = e[0] == 'w' || e[0] == 't';
+        const int v = wide ? atoi(e + 1) : atoi(e);
+        c->vw = wide ? (v == 2 && e[0] == 'w' ? 2 : 4) : 0;
+        c->vpipe = e[0] == 't';
         c->vrows = (v == 2 || v == 4) ? v : 1;
         c->tune_fixed = true;
     }
@@ -930,12 +946,24 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
             goto bad;
         *slot_ptr(c->M, n.c_str(), true) = p;
     }
-    if ((rc = dalloc(c, (void **)&c->d_status, sizeof(int) * (cfg->nshots + 1))))
+    if ((rc = dalloc(c, (void **)&c->d_status, sizeof(int) * (cfg->nshots + 2))))
         goto bad;
     c->G.step_ctr = c->d_status + cfg->nshots;  // zeroed with the status words
+    c->G.fault = c->d_status + cfg->nshots + 1;
     if (const char *e = getenv("SOFI_GRAPH"))
         c->use_graph = atoi(e) != 0;
     c->A.status = c->d_status;
+    // the TMA-fed velocity pipeline, offered to the autotuner where it applies
+    // (vplan.segs stays 0 where a tensor map or the launch shape is unavailable)
+    if (!G.ab4 && !c->march && cfg->weq != SOFI_AC_ISO) {
+        plan_velocity_pipeline(G, c->W, c->nd, device, &c->vplan);
+        // SOFI_VT_SEGS: row segments per strip (1 .. chunks of 8 rows), instead of one wave
+        if (const char *e = getenv("SOFI_VT_SEGS"))
+            if (c->vplan.segs && atoi(e) > 0) {
+                const int nck = (cfg->ny + 7) / 8;
+                c->vplan.segs = atoi(e) < nck ? atoi(e) : nck;
+            }
+    }
     c->snap_total = count_snapshots(*cfg);
     if (c->snap_total) {
         c->snap_nx = (cfg->nx - 1) / cfg->idx + 1;
@@ -1125,7 +1153,7 @@ int sofi_reset(sofi_ctx *c, int shot)
             CK(cudaMemsetAsync(c->W.dcor + 4LL * s * c->G.fsz, 0, 4 * f, c->stream));
         }
     }
-    CK(cudaMemsetAsync(c->d_status, 0, sizeof(int) * (c->cfg.nshots + 1), c->stream));  // + step counter
+    CK(cudaMemsetAsync(c->d_status, 0, sizeof(int) * (c->cfg.nshots + 2), c->stream));  // + step counter, fault
     if (c->d_sec && !c->acq_dirty) {
         size_t n = (size_t)c->total_rec * 5 * (c->A.ns > 0 ? c->A.ns : 1);
         CK(cudaMemsetAsync(c->d_sec, 0, n * sizeof(float), c->stream));
@@ -1317,6 +1345,14 @@ int sofi_velocity_variant(sofi_ctx *c, int *cells_per_thread, int *rows_per_thre
         return fail(SOFI_E_ARG, "null argument");
     *cells_per_thread = (c->vw && !c->G.ab4) ? c->vw : 1;  // 4th order: one cell per thread
     *rows_per_thread = (c->vw || c->G.ab4) ? 1 : c->vrows;
+    return 0;
+}
+
+int sofi_velocity_pipelined(sofi_ctx *c, int *pipelined)
+{
+    if (!c || !pipelined)
+        return fail(SOFI_E_ARG, "null argument");
+    *pipelined = c->vpipe && c->vplan.segs && !c->G.ab4 && !c->march && c->cfg.weq != SOFI_AC_ISO;
     return 0;
 }
 

@@ -121,6 +121,12 @@ class TimeLoop:
         N.check(self.lib.sofi_velocity_variant(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    def velocity_pipelined(self) -> bool:
+        """Whether the velocity update is the TMA-fed pipeline."""
+        a = ctypes.c_int()
+        N.check(self.lib.sofi_velocity_pipelined(self.h, ctypes.byref(a)))
+        return bool(a.value)
+
     def stress_variant(self) -> int:
         """Cells per thread in x of the stress kernel."""
         a = ctypes.c_int()

@@ -195,8 +195,13 @@ int sofi_kernel_time(sofi_ctx *ctx, const char *name, double *avg_ms, long long 
 /* Velocity-kernel variant in use: cells per thread along x (1, 2 or 4) and
  * rows per thread (1, 2 or 4). The first sofi_run after sofi_reset(ctx, -1)
  * times the variants on the zeroed arrays (where each leaves them zero) and
- * keeps the fastest for the grid shape; SOFI_VROWS=w4|w2|1|2|4 fixes it. */
+ * keeps the fastest for the grid shape; SOFI_VROWS=w4|w2|t4|1|2|4 fixes it. */
 int sofi_velocity_variant(sofi_ctx *ctx, int *cells_per_thread, int *rows_per_thread);
+/* 1 when the velocity update in use is the TMA-fed pipeline (stress tiles
+ * copied into a ring of shared-memory stages, blocks marching down column
+ * strips; second-order time stepping, not acoustic; SOFI_VROWS=t4 fixes it),
+ * else 0. */
+int sofi_velocity_pipelined(sofi_ctx *ctx, int *pipelined);
 /* Stress-kernel variant in use: cells per thread along x (1, 2 or 4; TTI: 1),
  * chosen by the same autotuning run; SOFI_SW=0|2|4 fixes it. */
 int sofi_stress_variant(sofi_ctx *ctx, int *cells_per_thread);

@@ -187,16 +187,59 @@ def test_velocity_kernel_vector_widths_match_one_cell(name, monkeypatch):
     sp = case_sources(case, cfg)
     sig = O.wavelet(1, cfg.nt, cfg.dt, sp)
     out = {}
-    for variant in ["1", "w4", "w2"]:
+    for variant in ["1", "w4", "w2", "t4"]:
         monkeypatch.setenv("SOFI_VROWS", variant)
         t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
-        assert t.velocity_variant() == {"1": (1, 1), "w4": (4, 1), "w2": (2, 1)}[variant]
+        assert t.velocity_variant() == {"1": (1, 1), "w4": (4, 1), "w2": (2, 1), "t4": (4, 1)}[variant]
+        assert t.velocity_pipelined() == (variant == "t4")
         out[variant] = {k: t.field(k) for k in ["vx", "vy", "sxx", "syy", "sxy"]}
         out[variant].update({c: t.section(c) for c in ["vx", "vy", "div"]})
         t.close()
-    for w in ["w4", "w2"]:
+    # the pipelined kernel (TMA copies of the stress tiles into shared memory)
+    # sums the same values in the same order as the four-cell kernel; it is
+    # held to the same bound, as the compiler may contract the sums differently
+    for w in ["w4", "w2", "t4"]:
         for k in out[w]:
             assert rel_l2(out[w][k], out["1"][k]) < 5e-5, (name, w, k, rel_l2(out[w][k], out["1"][k]))
+    o.close()
+
+
+@pytest.mark.parametrize("name", ["el_cpml_fd8", "el_cpml_fd12", "el_abs_fd2", "visc_cpml_fs_l3",
+                                  "el_periodic_cpml", "tti_abs"])
+def test_velocity_pipeline_segments(name, monkeypatch):
+    """The TMA-fed velocity pipeline gives the same step whatever the number of
+    row segments per strip: one segment walks all chunks of a strip through
+    the six-stage ring (it wraps), the planned count gives each block one or
+    two chunks. Every segment count is bit-identical, and matches the four-
+    cell kernel to float32 rounding."""
+    from oracle import oracle as O
+    from tests.golden.cases import case_by_name
+    from tests.helpers import case_receivers, case_sources
+    case = case_by_name(name)
+    o = run_oracle_case(case, nthreads=os.cpu_count() or 1, nsteps=1)
+    cfg = o.cfg
+    sp = case_sources(case, cfg)
+    sig = O.wavelet(1, cfg.nt, cfg.dt, sp)
+    out = {}
+    for vrows, segs in [("w4", None), ("t4", None), ("t4", "1"), ("t4", "2"), ("t4", "5")]:
+        monkeypatch.setenv("SOFI_VROWS", vrows)
+        if segs:
+            monkeypatch.setenv("SOFI_VT_SEGS", segs)
+        else:
+            monkeypatch.delenv("SOFI_VT_SEGS", raising=False)
+        t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
+        assert t.velocity_pipelined() == (vrows == "t4")
+        out[(vrows, segs)] = {k: t.field(k) for k in ["vx", "vy", "sxx", "syy", "sxy"]}
+        out[(vrows, segs)].update({"section " + c: t.section(c) for c in ["vx", "vy"]})
+        t.close()
+    ref = out[("t4", None)]
+    for key, d in out.items():
+        for k in d:
+            if key[0] == "t4":
+                np.testing.assert_array_equal(d[k], ref[k], err_msg=f"{name} segments {key[1]} {k}")
+            else:
+                assert rel_l2(d[k], ref[k]) < 5e-5, (name, k, rel_l2(d[k], ref[k]))
+            assert np.abs(d[k]).max() > 0
     o.close()
 
 
@@ -216,6 +259,7 @@ def test_autotuned_run_equals_fixed_variant(name, monkeypatch):
     monkeypatch.delenv("SOFI_VROWS", raising=False)
     t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
     cells, rows = t.velocity_variant()
+    piped = t.velocity_pipelined()
 
     def outputs(t):
         d = {"field " + k: t.field(k) for k in ["vx", "vy", "sxx", "syy", "sxy"]}
@@ -224,9 +268,9 @@ def test_autotuned_run_equals_fixed_variant(name, monkeypatch):
 
     tuned = outputs(t)
     t.close()
-    monkeypatch.setenv("SOFI_VROWS", f"w{cells}" if cells > 1 else str(rows))
+    monkeypatch.setenv("SOFI_VROWS", "t4" if piped else (f"w{cells}" if cells > 1 else str(rows)))
     t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
-    assert t.velocity_variant() == (cells, rows)
+    assert t.velocity_variant() == (cells, rows) and t.velocity_pipelined() == piped
     fixed = outputs(t)
     t.close()
     for k in tuned:
