@@ -386,6 +386,11 @@ static int make_resident(sofi_server *s, req_t *q)
     q->priority = s->o.use_priorities ? sofi_server_priority(work, s->prio_least, s->prio_greatest) : 0;
     if ((rc = sofi_create_with_priority(&q->cfg, s->o.device, q->priority, &q->ctx)))
         return rc;
+    if (s->o.persistent) {
+        int on = 0, blocks = 0;
+        if ((rc = sofi_persistent(q->ctx, &on, &blocks)) == 0 && blocks && !on)
+            rc = sofi_set_persistent(q->ctx, 1);
+    }
     for (int k = 0; k < sofih_prep_num_fields(q->prep) && !rc; k++)
         rc = sofi_set_model_field(q->ctx, 0, sofih_prep_field_name(q->prep, k), sofih_prep_field(q->prep, k),
                                   q->cfg.nx, 1);

@@ -81,6 +81,15 @@ struct Wave {
     long long ab_lvl, ab_mlvl;
 };
 
+// Launch arguments of the persistent step kernel (sofi_persist.cuh).
+struct PersistArgs {
+    int nsteps;
+    int has_force;
+    unsigned vg[3];   // velocity tiles: the plain launch's grid (x, y, z)
+    unsigned sg[3];   // stress tiles
+    unsigned *bar;    // [0] arrivals, [1] generation
+};
+
 // Prepared model arrays (one per shot or shared) and 1-D vectors.
 struct Model {
     const float *prip, *prjp;
@@ -119,15 +128,20 @@ __device__ __forceinline__ long long cell(const Geo &G, int j, int i)
 // Tile column and shot of this block. With a shared model and several shots
 // the shot varies fastest in blockIdx.x, so the blocks that run together read
 // the same model tile and only the first of them fetches it from DRAM.
-__device__ __forceinline__ void block_xs(const Geo &G, int &bx, int &s)
+// `b` is blockIdx for a plain launch, or a persistent kernel's tile.
+__device__ __forceinline__ void block_xs(const Geo &G, const uint3 &b, int &bx, int &s)
 {
     if (G.shot_fast) {
-        s = blockIdx.x % G.nshots;
-        bx = blockIdx.x / G.nshots;
+        s = b.x % G.nshots;
+        bx = b.x / G.nshots;
     } else {
-        s = blockIdx.z;
-        bx = blockIdx.x;
+        s = b.z;
+        bx = b.x;
     }
+}
+__device__ __forceinline__ void block_xs(const Geo &G, int &bx, int &s)
+{
+    block_xs(G, blockIdx, bx, s);
 }
 
 __device__ __forceinline__ long long moff(const Geo &G, int s)

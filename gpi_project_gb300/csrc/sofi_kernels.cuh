@@ -9,11 +9,8 @@ namespace sofi {
 // update_v_interior.c:49-71. Runs before the velocity kernel advances the
 // step counter, so the step being computed is counter + 1. (static: the
 // header is included by several translation units; only sofigpu.cu launches it)
-static __global__ void k_force_src(Geo G, Wave W, Model M, Acq A)
+__device__ __forceinline__ void force_shot(const Geo &G, const Wave &W, const Model &M, const Acq &A, int s)
 {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= G.nshots)
-        return;
     const int nt = *G.step_ctr + 1;
     const float *prip = M.prip + moff(G, s), *prjp = M.prjp + moff(G, s);
     float *vx = W.vx + (long long)s * G.fsz, *vy = W.vy + (long long)s * G.fsz;
@@ -32,6 +29,13 @@ static __global__ void k_force_src(Geo G, Wave W, Model M, Acq A)
             vy[o] += A.src_cos[k] * (prjp[o] * amp);
         }
     }
+}
+
+static __global__ void k_force_src(Geo G, Wave W, Model M, Acq A)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < G.nshots)
+        force_shot(G, W, M, A, s);
 }
 
 // ------------------------------------------------------- velocity update
@@ -143,16 +147,19 @@ __global__ void __launch_bounds__(BX *BY, R == 1 ? 8 : 1) k_update_v(Geo G, Wave
 // (< pitch for VW = 2; for VW = 4 possibly the next row's first columns); the
 // values past column NX + ND only feed cells past NX, which are never stored.
 // Rows j - ND .. j + ND stay inside the HY ghost rows.
-template <int VW>
+// COH: the array changes while the kernel runs (a persistent kernel's later
+// phase writes it), so the load bypasses L1 (ld.global.cg) instead of going
+// through the read-only path.
+template <int VW, bool COH = false>
 __device__ __forceinline__ void ldv(const float *p, float *out)
 {
     if (VW == 1) {
-        out[0] = __ldg(p);
+        out[0] = COH ? __ldcg(p) : __ldg(p);
     } else if (VW == 4) {
-        const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+        const float4 a = COH ? __ldcg(reinterpret_cast<const float4 *>(p)) : __ldg(reinterpret_cast<const float4 *>(p));
         out[0] = a.x, out[1] = a.y, out[2] = a.z, out[3] = a.w;
     } else {
-        const float2 a = __ldg(reinterpret_cast<const float2 *>(p));
+        const float2 a = COH ? __ldcg(reinterpret_cast<const float2 *>(p)) : __ldg(reinterpret_cast<const float2 *>(p));
         out[0] = a.x, out[1] = a.y;
     }
 }
@@ -255,16 +262,16 @@ __device__ __forceinline__ void v_finish(const Geo &G, const Wave &W, const Mode
 // SXY = false: the acoustic update (wavefield_update_v_ac.c), which has no
 // sxy: vx += sxx_x * DT/DH * rip, vy += syy_y * DT/DH * rjp (sxx and syy are
 // one pressure array); VW may then also be 1.
-template <int ND, int VW, bool SXY = true>
-__global__ void __launch_bounds__(BX *BY, VW == 4 ? 4 : 1) k_update_vw(Geo G, Wave W, Model M)
+template <int ND, int VW, bool SXY, bool COH>
+__device__ __forceinline__ void vw_tile(const Geo &G, const Wave &W, const Model &M, const uint3 b)
 {
     constexpr int K = (ND + VW - 1) / VW;
     constexpr int NXS = VW * (2 * K + 1);  // stencil row: columns i - VW K .. i + VW K + VW - 1
     int bx, s;
-    block_xs(G, bx, s);
+    block_xs(G, b, bx, s);
     const int i = (bx * BX + threadIdx.x) * VW + 1;
-    const int j = blockIdx.y * BY + threadIdx.y + 1;
-    if (G.step_ctr && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+    const int j = b.y * BY + threadIdx.y + 1;
+    if (G.step_ctr && b.x == 0 && b.y == 0 && b.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
         *G.step_ctr += 1;
     if (i > G.nx || j > G.ny)
         return;
@@ -280,9 +287,9 @@ __global__ void __launch_bounds__(BX *BY, VW == 4 ? 4 : 1) k_update_vw(Geo G, Wa
         float X[NXS], Y[NXS];  // X[k] = sxx(j, i - VW K + k), Y[k] = sxy(j, i - VW K + k)
 #pragma unroll
         for (int q = 0; q < 2 * K + 1; q++) {
-            ldv<VW>(sxx + o + VW * (q - K), X + VW * q);
+            ldv<VW, COH>(sxx + o + VW * (q - K), X + VW * q);
             if (SXY)
-                ldv<VW>(sxy + o + VW * (q - K), Y + VW * q);
+                ldv<VW, COH>(sxy + o + VW * (q - K), Y + VW * q);
         }
         constexpr int C = VW * K;  // index of column i
 #pragma unroll
@@ -301,8 +308,8 @@ __global__ void __launch_bounds__(BX *BY, VW == 4 ? 4 : 1) k_update_vw(Geo G, Wa
         // y stencils: sxy rows j - ND .. j + ND - 1, syy rows j - ND + 1 .. j + ND
         float a1[VW], a0[VW], b1[VW], b0[VW];
         if (SXY)
-            ldv<VW>(sxy + o, a1), ldv<VW>(sxy + o - P, a0);
-        ldv<VW>(syy + o + P, b1), ldv<VW>(syy + o, b0);
+            ldv<VW, COH>(sxy + o, a1), ldv<VW, COH>(sxy + o - P, a0);
+        ldv<VW, COH>(syy + o + P, b1), ldv<VW, COH>(syy + o, b0);
 #pragma unroll
         for (int c = 0; c < VW; c++) {
             sxy_y[c] = SXY ? hc[1] * (a1[c] - a0[c]) : 0.f;
@@ -311,8 +318,8 @@ __global__ void __launch_bounds__(BX *BY, VW == 4 ? 4 : 1) k_update_vw(Geo G, Wa
 #pragma unroll
         for (int m = 2; m <= ND; m++) {
             if (SXY)
-                ldv<VW>(sxy + o + (m - 1) * P, a1), ldv<VW>(sxy + o - m * P, a0);
-            ldv<VW>(syy + o + m * P, b1), ldv<VW>(syy + o - (m - 1) * P, b0);
+                ldv<VW, COH>(sxy + o + (m - 1) * P, a1), ldv<VW, COH>(sxy + o - m * P, a0);
+            ldv<VW, COH>(syy + o + m * P, b1), ldv<VW, COH>(syy + o - (m - 1) * P, b0);
 #pragma unroll
             for (int c = 0; c < VW; c++) {
                 if (SXY)
@@ -327,6 +334,12 @@ __global__ void __launch_bounds__(BX *BY, VW == 4 ? 4 : 1) k_update_vw(Geo G, Wa
     ldv_rw<VW>(vx + o, ox), ldv_rw<VW>(vy + o, oy);
     ldv<VW>(M.prip + mo + o, rp), ldv<VW>(M.prjp + mo + o, rq);
     v_finish<VW, SXY>(G, W, M, s, i, j, o, mo, vx, vy, ox, oy, rp, rq, sxx_x, sxy_x, sxy_y, syy_y);
+}
+
+template <int ND, int VW, bool SXY = true>
+__global__ void __launch_bounds__(BX *BY, VW == 4 ? 4 : 1) k_update_vw(Geo G, Wave W, Model M)
+{
+    vw_tile<ND, VW, SXY, false>(G, W, M, blockIdx);
 }
 
 // Periodic x (BOUNDARY = 1): ghost columns copy the opposite edge, as the one-
@@ -472,15 +485,15 @@ __global__ void __launch_bounds__(BX *BY) k_update_s(Geo G, Wave W, Model M)
 // (x) and one vector per row (y), model, memory variables and stresses as
 // vectors; per cell the arithmetic of k_update_s, term by term. Reads past
 // column NX + ND feed only cells past NX, which are never stored.
-template <int ND, int KIND, bool VISCO, int LT, int VW>
-__global__ void __launch_bounds__(BX *BY, VW == 4 ? 2 : 1) k_update_sw(Geo G, Wave W, Model M)
+template <int ND, int KIND, bool VISCO, int LT, int VW, bool COH>
+__device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model &M, const uint3 b)
 {
     constexpr int K = (ND + VW - 1) / VW;
     constexpr int NXS = VW * (2 * K + 1);
     int bx, s;
-    block_xs(G, bx, s);
+    block_xs(G, b, bx, s);
     const int i = (bx * BX + threadIdx.x) * VW + 1;
-    const int j = blockIdx.y * BY + threadIdx.y + 1;
+    const int j = b.y * BY + threadIdx.y + 1;
     if (i > G.nx || j > G.ny)
         return;
     const int P = G.pitch;
@@ -497,8 +510,8 @@ __global__ void __launch_bounds__(BX *BY, VW == 4 ? 2 : 1) k_update_sw(Geo G, Wa
         float X[NXS], Y[NXS];  // X[k] = vx(j, i - VW K + k), Y[k] = vy(j, i - VW K + k)
 #pragma unroll
         for (int q = 0; q < 2 * K + 1; q++) {
-            ldv<VW>(vx + o + VW * (q - K), X + VW * q);
-            ldv<VW>(vy + o + VW * (q - K), Y + VW * q);
+            ldv<VW, COH>(vx + o + VW * (q - K), X + VW * q);
+            ldv<VW, COH>(vy + o + VW * (q - K), Y + VW * q);
         }
         constexpr int C = VW * K;
 #pragma unroll
@@ -515,8 +528,8 @@ __global__ void __launch_bounds__(BX *BY, VW == 4 ? 2 : 1) k_update_sw(Geo G, Wa
     {
         // y stencils: vx rows j - ND + 1 .. j + ND, vy rows j - ND .. j + ND - 1
         float a1[VW], a0[VW], b1[VW], b0[VW];
-        ldv<VW>(vx + o + P, a1), ldv<VW>(vx + o, a0);
-        ldv<VW>(vy + o, b1), ldv<VW>(vy + o - P, b0);
+        ldv<VW, COH>(vx + o + P, a1), ldv<VW, COH>(vx + o, a0);
+        ldv<VW, COH>(vy + o, b1), ldv<VW, COH>(vy + o - P, b0);
 #pragma unroll
         for (int c = 0; c < VW; c++) {
             vxy[c] = hc[1] * (a1[c] - a0[c]);
@@ -524,8 +537,8 @@ __global__ void __launch_bounds__(BX *BY, VW == 4 ? 2 : 1) k_update_sw(Geo G, Wa
         }
 #pragma unroll
         for (int m = 2; m <= ND; m++) {
-            ldv<VW>(vx + o + m * P, a1), ldv<VW>(vx + o - (m - 1) * P, a0);
-            ldv<VW>(vy + o + (m - 1) * P, b1), ldv<VW>(vy + o - m * P, b0);
+            ldv<VW, COH>(vx + o + m * P, a1), ldv<VW, COH>(vx + o - (m - 1) * P, a0);
+            ldv<VW, COH>(vy + o + (m - 1) * P, b1), ldv<VW, COH>(vy + o - m * P, b0);
 #pragma unroll
             for (int c = 0; c < VW; c++) {
                 vxy[c] += hc[m] * (a1[c] - a0[c]);
@@ -649,6 +662,12 @@ __global__ void __launch_bounds__(BX *BY, VW == 4 ? 2 : 1) k_update_sw(Geo G, Wa
     }
 }
 
+template <int ND, int KIND, bool VISCO, int LT, int VW>
+__global__ void __launch_bounds__(BX *BY, VW == 4 ? 2 : 1) k_update_sw(Geo G, Wave W, Model M)
+{
+    sw_tile<ND, KIND, VISCO, LT, VW, false>(G, W, M, blockIdx);
+}
+
 // Acoustic stress update (wavefield_update_s_ac.c, update_s_acoustic_{interior,
 // PML,abs}.c), VW cells per thread (1, 2 or 4). The reference allocates one
 // array for sxx and syy (initmem_wavefield.c:34), so the pressure p = sxx = syy
@@ -656,15 +675,15 @@ __global__ void __launch_bounds__(BX *BY, VW == 4 ? 2 : 1) k_update_sw(Geo G, Wa
 // the same array for its x and y derivatives. CPML stretches vxx in the left /
 // right frame and vyy in the top / bottom frame (cpml_update_s_x_ac,
 // cpml_update_s_y_ac); the damping frame multiplies p once (abs_update_s_ac2).
-template <int ND, int VW>
-__global__ void __launch_bounds__(BX *BY) k_update_s_ac(Geo G, Wave W, Model M)
+template <int ND, int VW, bool COH>
+__device__ __forceinline__ void sac_tile(const Geo &G, const Wave &W, const Model &M, const uint3 b)
 {
     constexpr int K = (ND + VW - 1) / VW;
     constexpr int NXS = VW * (2 * K + 1);
     int bx, s;
-    block_xs(G, bx, s);
+    block_xs(G, b, bx, s);
     const int i = (bx * BX + threadIdx.x) * VW + 1;
-    const int j = blockIdx.y * BY + threadIdx.y + 1;
+    const int j = b.y * BY + threadIdx.y + 1;
     if (i > G.nx || j > G.ny)
         return;
     const int P = G.pitch;
@@ -679,7 +698,7 @@ __global__ void __launch_bounds__(BX *BY) k_update_s_ac(Geo G, Wave W, Model M)
         float X[NXS];  // X[k] = vx(j, i - VW K + k)
 #pragma unroll
         for (int q = 0; q < 2 * K + 1; q++)
-            ldv<VW>(vx + o + VW * (q - K), X + VW * q);
+            ldv<VW, COH>(vx + o + VW * (q - K), X + VW * q);
         constexpr int C = VW * K;
 #pragma unroll
         for (int c = 0; c < VW; c++) {
@@ -691,13 +710,13 @@ __global__ void __launch_bounds__(BX *BY) k_update_s_ac(Geo G, Wave W, Model M)
     }
     {
         float b1[VW], b0[VW];  // vy rows j - ND .. j + ND - 1
-        ldv<VW>(vy + o, b1), ldv<VW>(vy + o - P, b0);
+        ldv<VW, COH>(vy + o, b1), ldv<VW, COH>(vy + o - P, b0);
 #pragma unroll
         for (int c = 0; c < VW; c++)
             vyy[c] = hc[1] * (b1[c] - b0[c]);
 #pragma unroll
         for (int m = 2; m <= ND; m++) {
-            ldv<VW>(vy + o + (m - 1) * P, b1), ldv<VW>(vy + o - m * P, b0);
+            ldv<VW, COH>(vy + o + (m - 1) * P, b1), ldv<VW, COH>(vy + o - m * P, b0);
 #pragma unroll
             for (int c = 0; c < VW; c++)
                 vyy[c] += hc[m] * (b1[c] - b0[c]);
@@ -746,6 +765,12 @@ __global__ void __launch_bounds__(BX *BY) k_update_s_ac(Geo G, Wave W, Model M)
             if (i + c <= G.nx)
                 pr[o + c] = np[c];
     }
+}
+
+template <int ND, int VW>
+__global__ void __launch_bounds__(BX *BY) k_update_s_ac(Geo G, Wave W, Model M)
+{
+    sac_tile<ND, VW, false>(G, W, M, blockIdx);
 }
 
 // ------------------------------------------------------------------ TTI
@@ -1171,12 +1196,8 @@ __device__ __forceinline__ void sample_v_p(const Geo &G, const Wave &W, const Mo
 // sampling (from the stress update's derivatives), source injection, free
 // surface, the NaN probe of time_loop.c:44-47, vx/vy/p sampling.
 template <int ND, bool VISCO, bool TTIK>
-__global__ void k_post(Geo G, Wave W, Model M, Acq A)
+__device__ __forceinline__ void post_column(const Geo &G, Wave W, const Model &M, const Acq &A, int i, int s)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int s = blockIdx.y;
-    if (i > G.nx)
-        return;
     const int nt = *G.step_ctr;  // the velocity kernel of this step advanced it
     const int seismo = G.seismo;
     psi_buffers(G, W, false);    // TTI: the CPML memory this step's stress update wrote
@@ -1198,6 +1219,14 @@ __global__ void k_post(Geo G, Wave W, Model M, Acq A)
     if (ins && seismo != 3)
         for (int r = r0; r < r1; r++)
             sample_v_p(G, W, M, A, s, A.rec_col_idx[r], ins, seismo);
+}
+
+template <int ND, bool VISCO, bool TTIK>
+__global__ void k_post(Geo G, Wave W, Model M, Acq A)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i <= G.nx)
+        post_column<ND, VISCO, TTIK>(G, W, M, A, i, blockIdx.y);
 }
 
 // snap_ssg.c:86-205: one snapshot frame, file order (x outer, y inner).

@@ -8,6 +8,16 @@ namespace sofi {
 struct Geo;
 struct Wave;
 struct Model;
+struct Acq;
+struct PersistArgs;
+// The persistent step kernel of ISO / VTI / acoustic media (sofi_persist.cuh;
+// instantiated beside the stress kernels of each kind): how many of its blocks
+// fit the GPU at once, and a cooperative launch of `blocks` of them.
+template <int KIND, bool VISCO>
+int persist_capacity_kv(int nd, int L, int device);
+template <int KIND, bool VISCO>
+cudaError_t launch_persist_kv(const Geo &G, const Wave &W, const Model &M, const Acq &A, int nd,
+                              const PersistArgs &P, int blocks, cudaStream_t st);
 // velocity update, y-marching (any WEQ): rows per block `sy`
 void launch_march_v(const Geo &G, const Wave &W, const Model &M, int nd, int sy, cudaStream_t st);
 // stress update of isotropic / VTI media, y-marching

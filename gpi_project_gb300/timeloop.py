@@ -121,6 +121,15 @@ class TimeLoop:
         N.check(self.lib.sofi_velocity_variant(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    def persistent(self) -> tuple:
+        """(on, blocks per launch) of the persistent step kernel."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        N.check(self.lib.sofi_persistent(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return bool(a.value), b.value
+
+    def set_persistent(self, on: bool) -> None:
+        N.check(self.lib.sofi_set_persistent(self.h, int(bool(on))))
+
     def velocity_pipelined(self) -> bool:
         """Whether the velocity update is the TMA-fed pipeline."""
         a = ctypes.c_int()

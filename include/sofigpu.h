@@ -197,6 +197,18 @@ int sofi_kernel_time(sofi_ctx *ctx, const char *name, double *avg_ms, long long 
  * times the variants on the zeroed arrays (where each leaves them zero) and
  * keeps the fastest for the grid shape; SOFI_VROWS=w4|w2|t4|1|2|4 fixes it. */
 int sofi_velocity_variant(sofi_ctx *ctx, int *cells_per_thread, int *rows_per_thread);
+/* The persistent step kernel: chunks of up to 128 time steps (until the next
+ * snapshot or timed step) run as one cooperative launch whose blocks step
+ * through the velocity, stress and post phases with a grid-wide barrier
+ * between them. Available for ISO / VTI / acoustic media with FDORDER_TIME 2
+ * and no periodic edge; off unless SOFI_PERSIST=1 or sofi_set_persistent turns
+ * it on (the captured graph of plain kernels is faster on the grids measured).
+ * `blocks`: blocks per launch (0: unavailable).
+ * Steps outside the persistent launches then run the four-cell kernels, the
+ * same arithmetic. sofi_set_persistent switches it (SOFI_E_STATE where it is
+ * unavailable); the autotuner does not run while it is on. */
+int sofi_persistent(sofi_ctx *ctx, int *on, int *blocks);
+int sofi_set_persistent(sofi_ctx *ctx, int on);
 /* 1 when the velocity update in use is the TMA-fed pipeline (stress tiles
  * copied into a ring of shared-memory stages, blocks marching down column
  * strips; second-order time stepping, not acoustic; SOFI_VROWS=t4 fixes it),

@@ -88,6 +88,8 @@ typedef struct {
     int prep_threads;       /* host workers; <= 0: 2 */
     int prep_omp_threads;   /* OpenMP threads per worker; <= 0: cores / workers */
     int use_priorities;     /* 1: smaller solves get more urgent streams */
+    int persistent;         /* 1: solves run the persistent step kernel where it is
+                               available (sofi_set_persistent); 0: as the context sets it */
 } sofi_server_options;
 
 const char *sofi_server_last_error(void);
