@@ -138,7 +138,10 @@ def test_graph_replay_equals_direct_launches(name, monkeypatch):
 # with a free surface.
 TTI_VARIANTS = [("tti_cpml", {}), ("vtti_cpml_l1", {}), ("tti_abs", {}), ("tti_cpml", {"boundary": 1}),
                 ("vtti_cpml_l1", {"boundary": 1}), ("tti_cpml", {"free_surf": 1, "nt": 60}),
-                ("tti_abs", {"free_surf": 1, "nt": 60}), ("tti_cpml", {"boundary": 1, "free_surf": 1, "nt": 60})]
+                ("tti_abs", {"free_surf": 1, "nt": 60}), ("tti_cpml", {"boundary": 1, "free_surf": 1, "nt": 60}),
+                # tiles clear of the CPML frame beside frame tiles
+                ("tti_cpml", {"nx": 300, "ny": 120}), ("vtti_cpml_l1", {"nx": 300, "ny": 120}),
+                ("tti_abs", {"nx": 300, "ny": 120}), ("tti_cpml", {"nx": 300, "ny": 120, "boundary": 1})]
 
 
 @pytest.mark.parametrize("name,over", TTI_VARIANTS,
