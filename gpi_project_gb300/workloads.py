@@ -80,6 +80,18 @@ def workload(name: str) -> dict:
         xs = np.linspace(21.0, 378.0, 100)
         rec = (np.floor(xs / 1.0).astype(np.int32) + 1, np.full(100, 11, np.int32))
         nshots = 1
+    elif name == "c1b":
+        # the 400 x 400 elastic solve above, 64 shots (sources along the top) batched on one model
+        rng = np.random.default_rng(1001)
+        nx = ny = 400
+        vp, vs, rho = layered(rng, nx, ny)
+        par = dict(weq=2, nx=nx, ny=ny, dh=1.0, dt=1e-4, nt=2000, fdorder=8, maxrelerror=1, fw=20, abs_type=1,
+                   npower=4.0, k_max_cpml=1.0, vppml=float(vp.max()), fpml=25.0, seismo=1, ndt=1)
+        mats = dict(vp=vp, vs=vs, rho=rho)
+        src = [_srcpos([(x, 5.0)], 1.0, 25.0, 1) for x in np.linspace(30.0, 370.0, 64)]
+        xs = np.linspace(21.0, 378.0, 100)
+        rec = (np.floor(xs / 1.0).astype(np.int32) + 1, np.full(100, 11, np.int32))
+        nshots = 64
     elif name == "c2":
         rng = np.random.default_rng(1002)
         nx, ny = 4000, 2000

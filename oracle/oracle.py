@@ -91,6 +91,9 @@ def _lib(precision: str = "f32"):
         lib.orc_snapshot_size.argtypes = [ctypes.c_void_p]
         lib.orc_get_snapshot.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, fp]
         lib.orc_timings.argtypes = [ctypes.c_void_p, P(ctypes.c_double)]
+        lib.orc_fwi_begin.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        lib.orc_fwi_backward.argtypes = [ctypes.c_void_p, fp, fp]
+        lib.orc_fwi_gradients.argtypes = [ctypes.c_void_p, fp, fp, fp]
         _LIBS[precision] = lib
     return _LIBS[precision]
 
@@ -422,6 +425,63 @@ class Oracle:
         out = (ctypes.c_double * 4)()
         self.lib.orc_timings(self.h, out)
         return np.array(list(out))
+
+    # ---- MODE = FWI (EL_ISO): one gradient pass of inversion.c
+    def fwi_begin(self, velocity: int = 1, adjoint_type: int = 1):
+        self._check(self.lib.orc_fwi_begin(self.h, velocity, adjoint_type))
+
+    def fwi_backward(self, adj_x: np.ndarray, adj_y: np.ndarray):
+        ax = np.ascontiguousarray(adj_x, dtype=np.float32)
+        ay = np.ascontiguousarray(adj_y, dtype=np.float32)
+        assert ax.shape == ay.shape == (self.ntr, self.cfg.nt)
+        self._check(self.lib.orc_fwi_backward(self.h, _fptr(ax), _fptr(ay)))
+
+    def fwi_gradients(self) -> tuple:
+        """(gradLam_shot, gradMu_shot, gradRhos_shot) as [NY][NX] float32."""
+        out = [np.empty((self.cfg.ny, self.cfg.nx), dtype=np.float32) for _ in range(3)]
+        self._check(self.lib.orc_fwi_gradients(self.h, *[_fptr(a) for a in out]))
+        return tuple(out)
+
+
+# ------------------------------------------------------------------ FWI
+
+
+def fwi_residual(calc: np.ndarray, data: np.ndarray, velocity: int, dt: float) -> tuple:
+    """calc_res.c:136-160 and :216-262 for LNORM = 2 (no trace kill, time
+    window or normalisation): with VELOCITY = 0 both sections are integrated
+    (running float sum times DT), the residual is synthetic minus observed,
+    stored time-reversed (sample j at NS - j + 1), and L2 sums its squares.
+    Returns (residual [ntr][ns], L2)."""
+    calc = np.asarray(calc, dtype=np.float32)
+    data = np.asarray(data, dtype=np.float32)
+    if velocity == 0:
+        dt32 = np.float32(dt)
+        ic = np.empty_like(calc)
+        idata = np.empty_like(data)
+        for a, out in ((calc, ic), (data, idata)):
+            acc = np.zeros(a.shape[0], dtype=np.float32)
+            for j in range(a.shape[1]):
+                acc = (acc + a[:, j]).astype(np.float32)
+                out[:, j] = acc * dt32
+        calc, data = ic, idata
+    diff = (calc - data).astype(np.float32)[:, ::-1].copy()
+    l2 = float(np.sum(diff.astype(np.float64) ** 2))
+    return diff, l2
+
+
+def fwi_model_gradients(lam, mu, rhos, vp, vs, rho) -> tuple:
+    """inversion.c:225-240: the vp / vs / rho' gradients of one shot from the
+    Lame / density sums ([NY][NX]) and the model ([NY][NX]), with the
+    reference's types (double constants, float arrays); its vs gradient takes
+    Vp0 in the mu term."""
+    f8 = np.float64
+    lam, mu, rhos = (np.asarray(a, dtype=np.float32) for a in (lam, mu, rhos))
+    vp, vs, rho = (np.asarray(a, dtype=np.float32) for a in (vp, vs, rho))
+    gvp = (2.0 * rho.astype(f8) * vp * lam).astype(np.float32)
+    gvs = ((-4.0 * vs.astype(f8) * rho * lam) + 2.0 * rho.astype(f8) * vp * mu).astype(np.float32)
+    grho = ((((vp * vp).astype(f8) - (2.0 * vs.astype(f8) * vs)) * lam) + (vs * vs * mu).astype(f8)
+            + rhos).astype(np.float32)
+    return gvp, gvs, grho
 
 
 def wavelet(shape: int, nt: int, dt: float, srcpos: np.ndarray, precision: str = "f32") -> np.ndarray:

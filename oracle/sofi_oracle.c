@@ -91,6 +91,16 @@ struct orc_ctx {
     int step;
     int prepared;
     double tim[4];
+    /* MODE = FWI, EL_ISO (inversion.c, snap_store.c, calc_conv.c): the
+     * quantities wavefield_update_v.c:31-44 and wavefield_update_s_el.c:43-47
+     * keep for the gradient, the forward ones of every step ([NT][5][NY][NX]),
+     * the adjoint signals at the receivers ([2][ntr][NT]) and the per-shot
+     * gradient sums ([NY][NX]) */
+    int fwi, fwi_vel, fwi_adj, fwi_back;
+    arr2 pvxp1, pvyp1, ux, uy, uxy;
+    float *fwd;
+    float *adj;
+    float *g_lam, *g_mu, *g_rhos;
 };
 
 /* Adams-Bashforth coefficients of FDORDER_TIME = 4, float as the reference
@@ -366,6 +376,8 @@ void orc_destroy(orc_ctx *c)
     }
     free(c->rx);
     free(c->ry);
+    free2(&c->pvxp1), free2(&c->pvyp1), free2(&c->ux), free2(&c->uy), free2(&c->uxy);
+    free(c->fwd), free(c->adj), free(c->g_lam), free(c->g_mu), free(c->g_rhos);
     free(c);
 }
 
@@ -1086,6 +1098,19 @@ static inline void cpml_s_y(orc_ctx *c, int i, int j, int h2)
 /* wavefield_update_v.c:46-47 */
 static inline void wf_update_v(orc_ctx *c, int i, int j, real sxx_x, real sxy_x, real sxy_y, real syy_y)
 {
+    if (c->fwi) {
+        /* wavefield_update_v.c:31-44 */
+        if (!c->fwi_back) {
+            A(c->pvxp1, j, i) = A(c->prip, j, i) * (sxx_x + sxy_y) / c->DH;
+            A(c->pvyp1, j, i) = A(c->prjp, j, i) * (sxy_x + syy_y) / c->DH;
+        } else if (c->fwi_vel == 0) {
+            A(c->pvxp1, j, i) += A(c->vx, j, i) * c->DT;
+            A(c->pvyp1, j, i) += A(c->vy, j, i) * c->DT;
+        } else {
+            A(c->pvxp1, j, i) = A(c->vx, j, i);
+            A(c->pvyp1, j, i) = A(c->vy, j, i);
+        }
+    }
     A(c->vx, j, i) += (sxx_x + sxy_y) * c->DTDH * A(c->prip, j, i);
     A(c->vy, j, i) += (sxy_x + syy_y) * c->DTDH * A(c->prjp, j, i);
 }
@@ -1114,6 +1139,20 @@ static inline void wf_update_v4(orc_ctx *c, int i, int j, real sxx_x, real sxy_x
 /* update_v_interior.c:49-71: force sources before the velocity loop */
 static void force_sources(orc_ctx *c, int nt)
 {
+    if (c->fwi_back) {
+        /* update_v_interior.c:72-90: the time-reversed residuals at the
+         * receivers, unscaled (ADJOINT_TYPE 1: x and y, 2: y, 3: x) */
+        for (int l = 1; l <= c->ntr; l++) {
+            int i = c->rx[l - 1], j = c->ry[l - 1];
+            float sx = c->adj[((size_t)(l - 1)) * (size_t)c->NT + (size_t)(nt - 1)];
+            float sy = c->adj[((size_t)(c->ntr + l - 1)) * (size_t)c->NT + (size_t)(nt - 1)];
+            if (c->fwi_adj == 1 || c->fwi_adj == 3)
+                A(c->vx, j, i) += sx;
+            if (c->fwi_adj == 1 || c->fwi_adj == 2)
+                A(c->vy, j, i) += sy;
+        }
+        return;
+    }
     for (int l = 1; l <= c->nsrc; l++) {
         int i = (int)SRC(1, l), j = (int)SRC(2, l);
         real azi_rad = SRC(7, l) * PI / 180;
@@ -1305,6 +1344,11 @@ static inline void wf_s_el(orc_ctx *c, int i, int j)
     A(c->sxy, j, i) += u1;
     A(c->sxx, j, i) += u2;
     A(c->syy, j, i) += u3;
+    if (c->fwi) { /* wavefield_update_s_el.c:43-47 */
+        A(c->uxy, j, i) = u1 / c->DT;
+        A(c->ux, j, i) = u2 / c->DT;
+        A(c->uy, j, i) = u3 / c->DT;
+    }
 }
 
 /* wavefield_update_s_visc.c:27-68 */
@@ -1631,7 +1675,7 @@ static int last_source_type(orc_ctx *c)
 static void psource(orc_ctx *c, int nt)
 {
     int NT = c->NT;
-    if (last_source_type(c) != 1)
+    if (last_source_type(c) != 1 || c->fwi_back) /* time_loop.c:248: sw == 0 only */
         return;
     for (int l = 1; l <= c->nsrc; l++) {
         int i = (int)SRC(1, l), j = (int)SRC(2, l);
@@ -1650,7 +1694,7 @@ static void psource(orc_ctx *c, int nt)
 /* eqsource.c:25-52 (moment tensor; applied to every source) */
 static void eqsource(orc_ctx *c, int nt)
 {
-    if (last_source_type(c) != 5)
+    if (last_source_type(c) != 5 || c->fwi_back) /* time_loop.c:252: sw == 0 only */
         return;
     for (int l = 1; l <= c->nsrc; l++) {
         int i = (int)SRC(1, l), j = (int)SRC(2, l);
@@ -1815,6 +1859,107 @@ static void snap(orc_ctx *c)
 
 /* ------------------------------------------------------------- time loop */
 
+/* snap_store.c:26-45 (DTINV = 1: every step, slot nt) */
+static void fwi_store(orc_ctx *c, int nt)
+{
+    size_t n = (size_t)c->P.nx * (size_t)c->P.ny;
+    float *slot = c->fwd + (size_t)(nt - 1) * 5 * n;
+    arr2 *src[5] = {&c->pvxp1, &c->pvyp1, c->fwi_vel ? &c->ux : &c->sxx, c->fwi_vel ? &c->uy : &c->syy,
+                    c->fwi_vel ? &c->uxy : &c->sxy};
+    for (int k = 0; k < 5; k++)
+        for (int j = 1; j <= c->P.ny; j++)
+            for (int i = 1; i <= c->P.nx; i++)
+                slot[(size_t)k * n + (size_t)(j - 1) * c->P.nx + (size_t)(i - 1)] = (float)A(*src[k], j, i);
+}
+
+/* calc_conv.c:34-71 at backward step nt: the forward quantities of step
+ * NT - nt + 1 against the adjoint ones. The reference declares muss / lamss
+ * float and the constants double, so lamss and the lambda / mu terms are
+ * formed in double and rounded into the float sums. */
+static void fwi_conv(orc_ctx *c, int nt)
+{
+    size_t n = (size_t)c->P.nx * (size_t)c->P.ny;
+    const float *slot = c->fwd + (size_t)(c->NT - nt) * 5 * n;
+    const float DT = (float)c->DT;
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= c->P.ny; j++)
+        for (int i = 1; i <= c->P.nx; i++) {
+            const size_t q = (size_t)(j - 1) * c->P.nx + (size_t)(i - 1);
+            const float rx = slot[q], ry = slot[n + q], fx = slot[2 * n + q], fy = slot[3 * n + q],
+                        fu = slot[4 * n + q];
+            const float vs0 = MAT(c->mat_vs, j, i), vp0 = MAT(c->mat_vp, j, i), rho0 = MAT(c->mat_rho, j, i);
+            const float muss = vs0 * vs0 * rho0;
+            const float lamss = vp0 * vp0 * rho0 - 2.0 * muss;
+            const float sxx = (float)A(c->sxx, j, i), syy = (float)A(c->syy, j, i), sxy = (float)A(c->sxy, j, i);
+            c->g_rhos[q] += -DT * (((float)A(c->pvxp1, j, i) * rx) + ((float)A(c->pvyp1, j, i) * ry));
+            c->g_lam[q] += -DT * (1.0 / (4.0 * (lamss + muss) * (lamss + muss))) * ((fx + fy) * (sxx + syy));
+            if (A(c->pu, j, i) > 0.0)
+                c->g_mu[q] += -DT * (((1.0 / (muss * muss)) * (fu * sxy)) +
+                                     ((1.0 / 4.0) * ((fx + fy) * (sxx + syy)) / ((lamss + muss) * (lamss + muss))) +
+                                     ((1.0 / 4.0) * ((fx - fy) * (sxx - syy)) / (muss * muss)));
+        }
+}
+
+int orc_fwi_begin(orc_ctx *c, int velocity, int adjoint_type)
+{
+    if (c->P.weq != 2) {
+        snprintf(c->err, sizeof c->err, "FWI gradients need WEQ = EL_ISO");
+        return 1;
+    }
+    if (adjoint_type < 1 || adjoint_type > 3 || (velocity != 0 && velocity != 1)) {
+        snprintf(c->err, sizeof c->err, "ADJOINT_TYPE 1-3 and VELOCITY 0/1 only");
+        return 1;
+    }
+    size_t n = (size_t)c->P.nx * (size_t)c->P.ny;
+    if (!c->fwd) {
+        c->fwd = (float *)calloc((size_t)c->NT * 5 * n, sizeof(float));
+        c->g_lam = (float *)calloc(n, sizeof(float));
+        c->g_mu = (float *)calloc(n, sizeof(float));
+        c->g_rhos = (float *)calloc(n, sizeof(float));
+        c->pvxp1 = alloc2(c), c->pvyp1 = alloc2(c), c->ux = alloc2(c), c->uy = alloc2(c), c->uxy = alloc2(c);
+        if (!c->fwd || !c->g_lam || !c->g_mu || !c->g_rhos) {
+            snprintf(c->err, sizeof c->err, "out of memory for the forward wavefields");
+            return 1;
+        }
+    }
+    memset(c->g_lam, 0, n * sizeof(float));
+    memset(c->g_mu, 0, n * sizeof(float));
+    memset(c->g_rhos, 0, n * sizeof(float));
+    c->fwi = 1, c->fwi_vel = velocity, c->fwi_adj = adjoint_type, c->fwi_back = 0;
+    return 0;
+}
+
+int orc_fwi_backward(orc_ctx *c, const float *adj_x, const float *adj_y)
+{
+    if (!c->fwi || c->step != c->NT) {
+        snprintf(c->err, sizeof c->err, "FWI backward pass needs a completed forward pass (orc_fwi_begin, NT steps)");
+        return 1;
+    }
+    size_t m = (size_t)(c->ntr > 0 ? c->ntr : 1) * (size_t)c->NT;
+    free(c->adj);
+    c->adj = (float *)malloc(2 * m * sizeof(float));
+    memcpy(c->adj, adj_x, m * sizeof(float));
+    memcpy(c->adj + m, adj_y, m * sizeof(float));
+    orc_reset(c); /* zero_wavefield.c */
+    c->fwi_back = 1;
+    int rc = orc_run(c, c->NT);
+    c->fwi_back = 0;
+    return rc;
+}
+
+int orc_fwi_gradients(orc_ctx *c, float *lam, float *mu, float *rhos)
+{
+    if (!c->fwi) {
+        snprintf(c->err, sizeof c->err, "FWI not begun");
+        return 1;
+    }
+    size_t n = (size_t)c->P.nx * (size_t)c->P.ny;
+    memcpy(lam, c->g_lam, n * sizeof(float));
+    memcpy(mu, c->g_mu, n * sizeof(float));
+    memcpy(rhos, c->g_rhos, n * sizeof(float));
+    return 0;
+}
+
 int orc_reset(orc_ctx *c)
 {
     /* zero_wavefield.c */
@@ -1859,6 +2004,10 @@ int orc_reset(orc_ctx *c)
         if (c->sec[k])
             memset(c->sec[k], 0, sizeof(float) * (size_t)c->ntr * (size_t)c->ns);
     memset(c->tim, 0, sizeof c->tim);
+    arr2 *fw[] = {&c->pvxp1, &c->pvyp1, &c->ux, &c->uy, &c->uxy};
+    for (size_t k = 0; k < sizeof(fw) / sizeof(fw[0]); k++)
+        if (fw[k]->p)
+            memset(fw[k]->p, 0, n2 * sizeof(real));
     return 0;
 }
 
@@ -1900,6 +2049,12 @@ int orc_run(orc_ctx *c, int nsteps)
         if (c->P.seismo && nt == c->lsamp && nt < c->NT) {
             seismo(c, c->lsamp);
             c->lsamp += c->P.ndt;
+        }
+        if (c->fwi) { /* time_loop.c:288-296 */
+            if (!c->fwi_back)
+                fwi_store(c, nt);
+            else
+                fwi_conv(c, nt);
         }
         if (c->P.snap && nt == c->lsnap && nt <= c->esnap) {
             snap(c);

@@ -104,6 +104,19 @@ int orc_get_snapshot(orc_ctx *c, int k, int comp, float *out);
 /* Time-loop phase timings of the last run, seconds: v, v-derivatives, s, total. */
 void orc_timings(orc_ctx *c, double out[4]);
 
+/* MODE = FWI, EL_ISO (inversion.c, snap_store.c, calc_conv.c; DTINV = 1):
+ * orc_fwi_begin makes the next forward run of NT steps keep the gradient's
+ * forward quantities of every step (VELOCITY 1: rho-weighted accelerations
+ * and stress rates, 0: accelerations and stresses). orc_fwi_backward then
+ * zeroes the wavefield and runs NT steps with the adjoint signals ([ntr][NT]
+ * each, already time-reversed, as calc_res.c leaves them) injected at the
+ * receivers (ADJOINT_TYPE 1: x and y, 2: y, 3: x), correlating every step
+ * with the forward step NT - nt + 1. orc_fwi_gradients returns the per-shot
+ * sums gradLam_shot, gradMu_shot, gradRhos_shot ([NY][NX], row-major). */
+int orc_fwi_begin(orc_ctx *c, int velocity, int adjoint_type);
+int orc_fwi_backward(orc_ctx *c, const float *adj_x, const float *adj_y);
+int orc_fwi_gradients(orc_ctx *c, float *lam, float *mu, float *rhos);
+
 #ifdef __cplusplus
 }
 #endif

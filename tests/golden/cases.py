@@ -70,6 +70,18 @@ CASES = [
     _case("el_fdt4_cpml", fdorder=6, fdorder_time=4, dt=1.0e-4, nt=600, seed=43, compiled_ref=False),
 ]
 
+# MODE = FWI (one gradient pass, ITERMAX 1, DTINV 1, LNORM 2): EL_ISO only,
+# NDT = 1 and full-grid gradients (IDX = IDY = 1). The observed data come from
+# the same acquisition on `true_model` (a faster, denser blob).
+FWI_CASES = [
+    _case("fwi_el_cpml", fdorder=8, maxrelerror=1, seed=51, nt=300, source_type=3, seismo=1, snap=0, ndt=1,
+          idx=1, idy=1, velocity=1, adjoint_type=1),
+    _case("fwi_el_abs_v0", fdorder=4, abs_type=2, fw=10, seed=52, nt=300, source_type=1, seismo=1, snap=0, ndt=1,
+          idx=1, idy=1, velocity=0, adjoint_type=2),
+    _case("fwi_el_fs", fdorder=6, maxrelerror=2, free_surf=1, seed=53, nt=300, source_type=2, seismo=1, snap=0,
+          ndt=1, idx=1, idy=1, velocity=1, adjoint_type=3, sources=[[121.0, 11.0, 0.0, 40.0, 1.0]]),
+]
+
 
 def _smooth(a, w=7):
     """Separable moving average over w cells (edges replicated), as float32."""
@@ -103,6 +115,16 @@ def synthetic_model(case) -> dict:
         mats["qp"] = _smooth(rng.uniform(20.0, 100.0, (nx, ny)))
         mats["qs"] = (mats["qp"] * 0.7).astype(np.float32)
     return {k: np.ascontiguousarray(v).reshape(-1) for k, v in mats.items()}
+
+
+def true_model(case, mats) -> dict:
+    """The FWI cases' true model: vp, vs x 1.05 and rho x 1.03 in a blob."""
+    nx, ny = case["nx"], case["ny"]
+    out = {k: v.copy() for k, v in mats.items()}
+    for k, f in (("vp", 1.05), ("vs", 1.05), ("rho", 1.03)):
+        a = out[k].reshape(nx, ny)
+        a[nx * 2 // 5: nx * 3 // 5, ny * 2 // 5: ny * 3 // 5] *= np.float32(f)
+    return out
 
 
 def receivers(case):
@@ -162,6 +184,31 @@ def write_case(case, work):
     with open(jpath, "w") as fh:
         fh.write(json_text(case))
     return jpath, mats
+
+
+def fwi_json_text(case) -> str:
+    """The case's parameter file in MODE = FWI (read_par_json_fwi.c keys):
+    observed data under ./obs/seis, gradients under ./grad/g."""
+    kv = {"MODE": "FWI", "RUN_MULTIPLE_SHOTS": "1", "ITERMAX": "1", "DATA_DIR": "./obs/seis",
+          "PARAMETERIZATION": "1", "ADJOINT_TYPE": str(case["adjoint_type"]), "VELOCITY": str(case["velocity"]),
+          "INV_VP_ITER": "1", "INV_VS_ITER": "1", "INV_RHO_ITER": "1", "TIME_FILT": "0", "USE_WORKFLOW": "0",
+          "INV_MODELFILE": "./inv/model", "NFSTART": "1", "NF": "1", "GRADIENT": "./grad/g", "NFSTART_GRAD": "1",
+          "NF_GRAD": "1", "GRAD_METHOD": "2", "LNORM": "2", "NORMALIZE": "0", "DTINV": "1", "WRITE_DIFF": "0",
+          "EPS_SCALE": "0.01", "STEPMAX": "4", "SCALEFAC": "4.0", "TESTSHOT_START": "1", "TESTSHOT_END": "1",
+          "TESTSHOT_INCR": "1", "PRO": "0.01", "MISFIT_LOG_FILE": "./log/L2.dat"}
+    lines = json_text(case).rstrip().splitlines()
+    body = [ln for ln in lines[1:-1] if not any(f'"{k}" :' in ln for k in kv)]
+    body[-1] = body[-1].rstrip(",") + ","
+    extra = [f'"{k}" : "{v}",' for k, v in kv.items()]
+    extra[-1] = extra[-1].rstrip(",")
+    return "\n".join(["{"] + body + extra + ["}"]) + "\n"
+
+
+def fwi_case_by_name(name):
+    for c in FWI_CASES:
+        if c["name"] == name:
+            return c
+    raise KeyError(name)
 
 
 def case_by_name(name):

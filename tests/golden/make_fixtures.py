@@ -31,7 +31,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
-from tests.golden.cases import CASES, synthetic_model, write_case  # noqa: E402
+from tests.golden.cases import CASES, FWI_CASES, fwi_json_text, json_text, synthetic_model, true_model, write_case  # noqa: E402
 
 SHIPPED = {"weq3": "EL_ISO", "weq4": "VEL_ISO", "weq5": "EL_VTI", "weq6": "VEL_VTI", "weq7": "EL_TTI",
            "weq8": "VEL_TTI", "weq3_fy": "EL_ISO", "weq8_fy": "VEL_TTI", "weq3_fdt4": "EL_ISO",
@@ -132,6 +132,48 @@ def ref_examples(reference, exe):
             shutil.rmtree(work, ignore_errors=True)
 
 
+def run_reference_fwi(case, exe):
+    """Observed data from a forward run on the case's true model, then one
+    FWI gradient pass on its model (MODE = FWI), both with the compiled
+    reference: the observed sections, the FWI forward sections and the
+    per-shot vp / vs / rho' gradients ([NY][NX])."""
+    work = tempfile.mkdtemp(prefix="sofi_fwi_")
+    try:
+        jpath, mats = write_case(case, work)
+        nx, ny = case["nx"], case["ny"]
+        true = true_model(case, mats)
+        os.makedirs(os.path.join(work, "true"), exist_ok=True)
+        for k, v in true.items():
+            v.astype(np.float32).tofile(os.path.join(work, "true", f"m.{k}"))
+        for d in ("obs", "grad", "inv"):
+            os.makedirs(os.path.join(work, d), exist_ok=True)
+        txt = json_text(case).replace('"MFILE" : "./model/m"', '"MFILE" : "./true/m"')
+        txt = txt.replace('"SEIS_FILE" : "./out/seis"', '"SEIS_FILE" : "./obs/seis"')
+        with open(os.path.join(work, "true.json"), "w") as fh:
+            fh.write(txt)
+        with open(os.path.join(work, "fwi.json"), "w") as fh:
+            fh.write(fwi_json_text(case))
+        for run in ("true.json", "fwi.json"):
+            r = subprocess.run([exe, run], cwd=work, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"{case['name']} {run}: reference failed\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}")
+            if run == "true.json":
+                for comp in ("vx", "vy"):
+                    shutil.copy(os.path.join(work, "obs", f"seis_{comp}.su"),
+                                os.path.join(work, "obs", f"seis_{comp}.su.shot1"))
+        out = {}
+        for comp in ("vx", "vy"):
+            _, out[f"obs_{comp}"] = read_su(os.path.join(work, "obs", f"seis_{comp}.su"))
+            _, out[f"fwd_{comp}"] = read_su(os.path.join(work, "out", f"seis_{comp}.su.shot1"))
+        for g in ("vp", "vs", "rho"):
+            a = np.fromfile(os.path.join(work, "grad", f"g_gradient.{g}.shot1"), dtype=np.float32)
+            out[f"grad_{g}"] = a.reshape(nx, ny).T.copy()  # writemod.c: x outer, y inner
+        out["case"] = np.frombuffer(json.dumps(case, sort_keys=True).encode(), dtype=np.uint8)
+        return out
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -147,6 +189,12 @@ def main():
         shipped_sigout(a.reference)
         if a.only:
             return
+    for case in FWI_CASES:
+        if a.only and case["name"] != a.only:
+            continue
+        out = run_reference_fwi(case, exe)
+        np.savez_compressed(os.path.join(HERE, f"ref_{case['name']}.npz"), **out)
+        print("wrote", case["name"], "gradients", [float(np.abs(out[f"grad_{g}"]).max()) for g in ("vp", "vs", "rho")])
     for case in CASES:
         if (a.only and case["name"] != a.only) or not case.get("compiled_ref", True):
             continue
