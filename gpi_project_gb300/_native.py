@@ -105,6 +105,10 @@ def load():
         "sofi_stress_variant": ([vp, P(ctypes.c_int)], ctypes.c_int),
         "sofi_velocity_pipelined": ([vp, P(ctypes.c_int)], ctypes.c_int),
         "sofi_persistent": ([vp, P(ctypes.c_int), P(ctypes.c_int)], ctypes.c_int),
+        "sofi_fwi_begin": ([vp, ctypes.c_int, ctypes.c_int, P(ctypes.c_float), P(ctypes.c_float),
+                            P(ctypes.c_float)], ctypes.c_int),
+        "sofi_fwi_backward": ([vp, P(ctypes.c_float), P(ctypes.c_float)], ctypes.c_int),
+        "sofi_fwi_gradients": ([vp, P(ctypes.c_float), P(ctypes.c_float), P(ctypes.c_float)], ctypes.c_int),
         "sofi_set_persistent": ([vp, ctypes.c_int], ctypes.c_int),
         "sofi_get_stream": ([vp, P(vp)], ctypes.c_int),
         "sofi_tti_stress_noalloc": ([P(SofiConfig), P(TtiStressArgs), vp], ctypes.c_int),

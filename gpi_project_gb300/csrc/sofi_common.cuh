@@ -79,6 +79,23 @@ struct Wave {
     // The memory variables then hold four levels too, ab_mlvl apart.
     float *svx4, *svy4, *hxx4, *hyy4, *hxy4, *hyx4;
     long long ab_lvl, ab_mlvl;
+    // MODE = FWI forward pass (null otherwise): the velocity update writes
+    // rip (sxx_x + sxy_y) / DH and rjp (sxy_x + syy_y) / DH of every cell
+    // (wavefield_update_v.c:31-35), the EL_ISO stress update u1..u3 / DT
+    // (wavefield_update_s_el.c:43-47; VELOCITY = 1)
+    float *fa_x, *fa_y, *fu_x, *fu_y, *fu_xy;
+};
+
+// Device state of an FWI gradient pass (sofi_fwi.cu); one shot per context.
+struct FwiDev {
+    float *store;                   // [NT][5][NY][NX] forward quantities, slot nt - 1
+    float *px, *py;                 // backward, VELOCITY = 0: running sums of v * DT ([NY][NX])
+    float *g_lam, *g_mu, *g_rhos;   // per-shot gradient sums ([NY][NX])
+    const float *vp, *vs, *rho;     // the model as read ([NY][NX])
+    const float *adj;               // [2][ntr][NT] adjoint signals (x, y)
+    const int *cell_off, *cell_rec; // receivers by cell: cell k holds cell_rec[cell_off[k] .. cell_off[k+1])
+    const int *cell_ix, *cell_iy;
+    int ncell, ntr, nt, velocity, adjoint;
 };
 
 // Launch arguments of the persistent step kernel (sofi_persist.cuh).

@@ -1,0 +1,132 @@
+// sofi_fwi.cu -- the FWI gradient pass of one shot (MODE = FWI, EL_ISO) on
+// the device: inversion.c's forward run with snap_store.c, its backward run
+// with the residuals injected at the receivers (update_v_interior.c:72-90) and
+// calc_conv.c's correlation at every step (time_loop.c:288-303, DTINV = 1).
+//
+// Forward: the velocity and stress kernels write this step's gradient
+// quantities (Wave::fa_*, fu_*); k_fwi_store copies them, or the stresses for
+// VELOCITY = 0, into slot nt of the store ([NT][5][NY][NX] floats).
+// Backward, per step: k_fwi_adj adds the adjoint signals at the receivers
+// before the velocity update; k_fwi_rho forms the reference's pvxp1 / pvyp1
+// (the injected velocity, or its running sum times DT for VELOCITY = 0) and
+// adds the density term; after the stress update and the free surface
+// k_fwi_conv adds the lambda and mu terms against forward slot NT - nt + 1.
+// Every kernel takes the step number from the device counter, so the steps
+// replay from the captured graph like the plain ones.
+#include "sofi_common.cuh"
+#include "sofi_launch.h"
+
+namespace sofi {
+
+__global__ void k_fwi_store(Geo G, Wave W, FwiDev F)
+{
+    const long long n = (long long)G.nx * G.ny;
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n)
+        return;
+    const int nt = *G.step_ctr;  // the step just completed
+    const int j = (int)(q / G.nx) + 1, i = (int)(q % G.nx) + 1;
+    const long long o = cell(G, j, i);
+    float *slot = F.store + (long long)(nt - 1) * 5 * n + q;
+    slot[0] = W.fa_x[o];
+    slot[n] = W.fa_y[o];
+    if (F.velocity) {
+        slot[2 * n] = W.fu_x[o], slot[3 * n] = W.fu_y[o], slot[4 * n] = W.fu_xy[o];
+    } else {
+        slot[2 * n] = W.sxx[o], slot[3 * n] = W.syy[o], slot[4 * n] = W.sxy[o];
+    }
+}
+
+// One thread per receiver cell; a cell's receivers in the reference's order.
+__global__ void k_fwi_adj(Geo G, Wave W, FwiDev F)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= F.ncell)
+        return;
+    const int nt = *G.step_ctr + 1;  // before the velocity kernel advances it
+    const long long o = cell(G, F.cell_iy[k], F.cell_ix[k]);
+    float vx = W.vx[o], vy = W.vy[o];
+    for (int r = F.cell_off[k]; r < F.cell_off[k + 1]; r++) {
+        const int l = F.cell_rec[r];
+        if (F.adjoint == 1 || F.adjoint == 3)
+            vx += F.adj[(long long)l * F.nt + (nt - 1)];
+        if (F.adjoint == 1 || F.adjoint == 2)
+            vy += F.adj[((long long)F.ntr + l) * F.nt + (nt - 1)];
+    }
+    W.vx[o] = vx, W.vy[o] = vy;
+}
+
+__global__ void k_fwi_rho(Geo G, Wave W, FwiDev F)
+{
+    const long long n = (long long)G.nx * G.ny;
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n)
+        return;
+    const int nt = *G.step_ctr + 1;
+    const int j = (int)(q / G.nx) + 1, i = (int)(q % G.nx) + 1;
+    const long long o = cell(G, j, i);
+    float px = W.vx[o], py = W.vy[o];
+    if (!F.velocity) {  // wavefield_update_v.c:37-39
+        px = __fadd_rn(F.px[q], __fmul_rn(px, G.dt));
+        py = __fadd_rn(F.py[q], __fmul_rn(py, G.dt));
+        F.px[q] = px, F.py[q] = py;
+    }
+    const float *slot = F.store + (long long)(F.nt - nt) * 5 * n + q;
+    // each product and sum rounded on its own, as the reference evaluates it
+    const float t = __fadd_rn(__fmul_rn(px, slot[0]), __fmul_rn(py, slot[n]));
+    F.g_rhos[q] = __fadd_rn(F.g_rhos[q], __fmul_rn(-G.dt, t));
+}
+
+// calc_conv.c:34-71: muss / lamss are floats, the constants double, so the
+// lambda and mu terms are formed in double and rounded into the float sums.
+__global__ void k_fwi_conv(Geo G, Wave W, Model M, FwiDev F)
+{
+    const long long n = (long long)G.nx * G.ny;
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n)
+        return;
+    const int nt = *G.step_ctr;
+    const int j = (int)(q / G.nx) + 1, i = (int)(q % G.nx) + 1;
+    const long long o = cell(G, j, i);
+    const float *slot = F.store + (long long)(F.nt - nt) * 5 * n + q;
+    const float fx = slot[2 * n], fy = slot[3 * n], fu = slot[4 * n];
+    const float vs0 = F.vs[q], vp0 = F.vp[q], rho0 = F.rho[q];
+    const float muss = __fmul_rn(__fmul_rn(vs0, vs0), rho0);
+    const float lamss = (float)__dadd_rn((double)__fmul_rn(__fmul_rn(vp0, vp0), rho0), -2.0 * (double)muss);
+    const float sxx = W.sxx[o], syy = W.syy[o], sxy = W.sxy[o];
+    const double mDT = -(double)G.dt;
+    const float lm = __fadd_rn(lamss, muss);
+    const float mm = __fmul_rn(muss, muss), lm2 = __fmul_rn(lm, lm);
+    const float sum_f = __fmul_rn(__fadd_rn(fx, fy), __fadd_rn(sxx, syy));
+    const double inv_lm2 = 1.0 / __dmul_rn(__dmul_rn(4.0, (double)lm), (double)lm);
+    F.g_lam[q] = (float)__dadd_rn((double)F.g_lam[q], __dmul_rn(__dmul_rn(mDT, inv_lm2), (double)sum_f));
+    if (M.pu[o] > 0.0f) {
+        const double t1 = __dmul_rn(1.0 / (double)mm, (double)__fmul_rn(fu, sxy));
+        const double t2 = __dmul_rn(0.25, (double)sum_f) / (double)lm2;
+        const double t3 =
+            __dmul_rn(0.25, (double)__fmul_rn(__fsub_rn(fx, fy), __fsub_rn(sxx, syy))) / (double)mm;
+        F.g_mu[q] = (float)__dadd_rn((double)F.g_mu[q], __dmul_rn(mDT, __dadd_rn(__dadd_rn(t1, t2), t3)));
+    }
+}
+
+void launch_fwi_store(const Geo &G, const Wave &W, const FwiDev &F, cudaStream_t st)
+{
+    const long long n = (long long)G.nx * G.ny;
+    k_fwi_store<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(G, W, F);
+}
+
+void launch_fwi_backward_pre(const Geo &G, const Wave &W, const FwiDev &F, cudaStream_t st)
+{
+    const long long n = (long long)G.nx * G.ny;
+    if (F.ncell)
+        k_fwi_adj<<<(F.ncell + 127) / 128, 128, 0, st>>>(G, W, F);
+    k_fwi_rho<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(G, W, F);
+}
+
+void launch_fwi_conv(const Geo &G, const Wave &W, const Model &M, const FwiDev &F, cudaStream_t st)
+{
+    const long long n = (long long)G.nx * G.ny;
+    k_fwi_conv<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(G, W, M, F);
+}
+
+}  // namespace sofi

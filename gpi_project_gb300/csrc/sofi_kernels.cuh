@@ -236,6 +236,10 @@ __device__ __forceinline__ void v_finish(const Geo &G, const Wave &W, const Mode
             }
         }
         if (SXY) {
+            if (W.fa_x && ic <= G.nx) {
+                W.fa_x[(long long)s * G.fsz + o + c] = rp[c] * (fx + fyx) / G.dh;
+                W.fa_y[(long long)s * G.fsz + o + c] = rq[c] * (fxy + fy) / G.dh;
+            }
             nvx[c] = ox[c] + (fx + fyx) * G.dtdh * rp[c];
             nvy[c] = oy[c] + (fxy + fy) * G.dtdh * rq[c];
         } else {
@@ -597,6 +601,10 @@ __device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model
             float gd = m0[c] * (dxx + dyy);
             u2 = gd - 2.0f * m1[c] * dyy;
             u3 = gd - 2.0f * m1[c] * dxx;
+            if (!VISCO && W.fu_x && ic <= G.nx) {
+                const long long q = (long long)s * G.fsz + o + c;
+                W.fu_xy[q] = u1 / G.dt, W.fu_x[q] = u2 / G.dt, W.fu_y[q] = u3 / G.dt;
+            }
         } else {
             u1 = m3[c] * (dxy + dyx);
             u2 = m0[c] * dxx + m1[c] * dyy;

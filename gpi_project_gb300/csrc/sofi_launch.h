@@ -10,6 +10,13 @@ struct Wave;
 struct Model;
 struct Acq;
 struct PersistArgs;
+struct FwiDev;
+// FWI gradient pass (sofi_fwi.cu): forward storage after a step; adjoint
+// injection and the density term before the velocity update; the lambda /
+// mu terms after the post kernel
+void launch_fwi_store(const Geo &G, const Wave &W, const FwiDev &F, cudaStream_t st);
+void launch_fwi_backward_pre(const Geo &G, const Wave &W, const FwiDev &F, cudaStream_t st);
+void launch_fwi_conv(const Geo &G, const Wave &W, const Model &M, const FwiDev &F, cudaStream_t st);
 // The persistent step kernel of ISO / VTI / acoustic media (sofi_persist.cuh;
 // instantiated beside the stress kernels of each kind): how many of its blocks
 // fit the GPU at once, and a cooperative launch of `blocks` of them.

@@ -193,6 +193,12 @@ struct sofi_ctx {
     bool persist = false;
     int persist_blocks = 0;    // blocks per launch (0: not available for this configuration)
     unsigned *d_bar = nullptr; // its grid barrier: arrivals, generation (after the status words)
+    // FWI gradient pass of one shot (sofi_fwi_*; sofi_fwi.cu)
+    bool fwi = false;          // the forward runs store the gradient quantities
+    bool fwi_back = false;     // the backward run is being issued
+    FwiDev F{};
+    int *d_noacq = nullptr;    // two zero ints: the backward run's empty source list
+    size_t fwi_cells_cap = 0;  // capacity of the receiver-cell arrays
     int sw = 0;                // ISO / VTI stress kernel: cells per thread in x (4 or 2), 0 = one
     bool sw_fixed = false;     // SOFI_SW chose it
     bool tuned = false;        // autotuner ran (or was skipped) for this context
@@ -702,6 +708,10 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
         k_force_src<<<nb, 128, 0, st>>>(G, c->W, c->M, c->A);
         c->launches++;
     }
+    if (c->fwi_back) {  // adjoint signals at the receivers, then the density term
+        launch_fwi_backward_pre(G, c->W, c->F, st);
+        c->launches += c->F.ncell ? 2 : 1;
+    }
     if (G.ab4) {  // 4th order: every block of the velocity kernel reads the step number
         launch_ab4_begin(G, st);
         c->launches++;
@@ -758,6 +768,13 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
     c->launches++;
     if (cf.boundary) {
         k_wrap_x<<<dim3((cf.ny + 127) / 128, S), 128, 0, st>>>(G, c->W.sxx, c->W.syy, c->W.sxy, c->nd);
+        c->launches++;
+    }
+    if (c->fwi) {  // time_loop.c:288-296
+        if (c->fwi_back)
+            launch_fwi_conv(G, c->W, c->M, c->F, st);
+        else
+            launch_fwi_store(G, c->W, c->F, st);
         c->launches++;
     }
     if (!capture && cf.snap && nt >= cf.snap_first && nt <= cf.snap_last &&
@@ -1445,12 +1462,151 @@ int sofi_velocity_variant(sofi_ctx *c, int *cells_per_thread, int *rows_per_thre
     return 0;
 }
 
+int sofi_fwi_begin(sofi_ctx *c, int velocity, int adjoint_type, const float *vp, const float *vs, const float *rho)
+{
+    if (!c || !vp || !vs || !rho)
+        return fail(SOFI_E_ARG, "null argument");
+    const sofi_config &cf = c->cfg;
+    if (cf.weq != SOFI_EL_ISO || cf.nshots != 1 || c->G.ab4 || c->march)
+        return fail(SOFI_E_ARG, "FWI gradients need WEQ = EL_ISO, one shot, FDORDER_TIME = 2 and the plain kernels");
+    if (cf.ndt != 1 || (cf.seismo != 1 && cf.seismo != 4))
+        return fail(SOFI_E_ARG, "FWI gradients need NDT = 1 and vx / vy seismograms (SEISMO 1 or 4)");
+    if ((velocity != 0 && velocity != 1) || adjoint_type < 1 || adjoint_type > 3)
+        return fail(SOFI_E_ARG, "VELOCITY 0 / 1 and ADJOINT_TYPE 1-3 are supported");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    const size_t n = (size_t)cf.nx * cf.ny, f = (size_t)c->G.fsz * sizeof(float);
+    int rc;
+    if (!c->F.store) {
+        size_t need = (size_t)cf.nt * 5 * n * sizeof(float), fr = 0, tot = 0;
+        CK(cudaMemGetInfo(&fr, &tot));
+        if (need + 16 * n * sizeof(float) + 5 * f > fr)
+            return fail(SOFI_E_NOMEM, "the forward wavefields of %d steps need %zu bytes, %zu free", cf.nt, need, fr);
+        float **fl[] = {&c->F.store, &c->F.px, &c->F.py, &c->F.g_lam, &c->F.g_mu, &c->F.g_rhos};
+        size_t sz[] = {need, n * sizeof(float), n * sizeof(float), n * sizeof(float), n * sizeof(float),
+                       n * sizeof(float)};
+        for (int k = 0; k < 6; k++)
+            if ((rc = dalloc(c, (void **)fl[k], sz[k])))
+                return rc;
+        float *m[3];
+        for (int k = 0; k < 3; k++)
+            if ((rc = dalloc(c, (void **)&m[k], n * sizeof(float))))
+                return rc;
+        c->F.vp = m[0], c->F.vs = m[1], c->F.rho = m[2];
+        float **wf[] = {&c->W.fa_x, &c->W.fa_y, &c->W.fu_x, &c->W.fu_y, &c->W.fu_xy};
+        for (auto p : wf)
+            if ((rc = dalloc(c, (void **)p, f)))
+                return rc;
+        if ((rc = dalloc(c, (void **)&c->d_noacq, 2 * sizeof(int))))
+            return rc;
+    }
+    CK(cudaMemcpyAsync((void *)c->F.vp, vp, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync((void *)c->F.vs, vs, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync((void *)c->F.rho, rho, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    for (float *p : {c->F.g_lam, c->F.g_mu, c->F.g_rhos})
+        CK(cudaMemsetAsync(p, 0, n * sizeof(float), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->F.nt = cf.nt, c->F.velocity = velocity, c->F.adjoint = adjoint_type;
+    // the kernels whose bodies write the gradient quantities, fixed for the pass
+    c->vw = 4, c->vrows = 1, c->vpipe = false, c->sw = 4, c->persist = false, c->tuned = true;
+    c->fwi = true, c->fwi_back = false, c->graph_dirty = true;
+    return 0;
+}
+
+int sofi_fwi_backward(sofi_ctx *c, const float *adj_x, const float *adj_y)
+{
+    if (!c || !adj_x || !adj_y)
+        return fail(SOFI_E_ARG, "null argument");
+    if (!c->fwi || c->fwi_back)
+        return fail(SOFI_E_STATE, "sofi_fwi_begin first");
+    int rc = sofi_synchronize(c);
+    if (rc)
+        return rc;
+    if (c->step != c->cfg.nt)
+        return fail(SOFI_E_STATE, "the forward run has done %d of NT = %d steps", c->step, c->cfg.nt);
+    // receivers grouped by cell, each cell's in the reference's order
+    const ShotAcq &a = c->acq[0];
+    const int ntr = (int)a.rix.size(), NT = c->cfg.nt;
+    std::map<std::pair<int, int>, std::vector<int>> cells;
+    std::vector<std::pair<int, int>> order;
+    for (int l = 0; l < ntr; l++) {
+        auto key = std::make_pair(a.riy[l], a.rix[l]);
+        if (!cells.count(key))
+            order.push_back(key);
+        cells[key].push_back(l);
+    }
+    std::vector<int> off(1, 0), rec, cx, cy;
+    for (auto &k : order) {
+        for (int l : cells[k])
+            rec.push_back(l);
+        off.push_back((int)rec.size());
+        cy.push_back(k.first), cx.push_back(k.second);
+    }
+    const size_t nc = order.size();
+    if (nc + 1 > c->fwi_cells_cap || !c->F.adj) {
+        int *ib;
+        float *adj;
+        const size_t cap = (nc + 1) > 1 ? nc + 1 : 2;
+        if ((rc = dalloc(c, (void **)&ib, (4 * cap + (size_t)ntr) * sizeof(int))) ||
+            (rc = dalloc(c, (void **)&adj, 2 * (size_t)(ntr > 0 ? ntr : 1) * NT * sizeof(float))))
+            return rc;
+        c->F.cell_off = ib, c->F.cell_ix = ib + cap, c->F.cell_iy = ib + 2 * cap, c->F.cell_rec = ib + 3 * cap;
+        c->F.adj = adj;
+        c->fwi_cells_cap = cap;
+    }
+    CK(cudaMemcpyAsync((void *)c->F.cell_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    if (nc) {
+        CK(cudaMemcpyAsync((void *)c->F.cell_ix, cx.data(), nc * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync((void *)c->F.cell_iy, cy.data(), nc * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync((void *)c->F.cell_rec, rec.data(), rec.size() * sizeof(int), cudaMemcpyHostToDevice,
+                           c->stream));
+    }
+    const size_t m = (size_t)ntr * NT;
+    CK(cudaMemcpyAsync((void *)c->F.adj, adj_x, m * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync((void *)(c->F.adj + m), adj_y, m * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    c->F.ncell = (int)nc, c->F.ntr = ntr;
+    // zero_wavefield.c, and no source but the residuals (time_loop.c:248-253 with sw = 1)
+    if ((rc = sofi_reset(c, -1)))
+        return rc;
+    const size_t n = (size_t)c->cfg.nx * c->cfg.ny;
+    CK(cudaMemsetAsync(c->F.px, 0, n * sizeof(float), c->stream));
+    CK(cudaMemsetAsync(c->F.py, 0, n * sizeof(float), c->stream));
+    const Acq saved = c->A;
+    const bool saved_force = c->has_force;
+    c->A.src_off = c->d_noacq, c->A.last_type = c->d_noacq;
+    c->has_force = false;
+    c->fwi_back = true, c->graph_dirty = true;
+    rc = sofi_run(c, NT);
+    if (!rc)
+        rc = sofi_synchronize(c);
+    c->A = saved, c->has_force = saved_force;
+    c->fwi_back = false, c->graph_dirty = true;
+    return rc;
+}
+
+int sofi_fwi_gradients(sofi_ctx *c, float *lam, float *mu, float *rhos)
+{
+    if (!c || !lam || !mu || !rhos)
+        return fail(SOFI_E_ARG, "null argument");
+    if (!c->fwi)
+        return fail(SOFI_E_STATE, "sofi_fwi_begin first");
+    CK(cudaSetDevice(c->device));
+    const size_t b = (size_t)c->cfg.nx * c->cfg.ny * sizeof(float);
+    CK(cudaMemcpyAsync(lam, c->F.g_lam, b, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(mu, c->F.g_mu, b, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(rhos, c->F.g_rhos, b, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
 int sofi_set_persistent(sofi_ctx *c, int on)
 {
     if (!c)
         return fail(SOFI_E_ARG, "null context");
     if (on && !c->persist_blocks)
         return fail(SOFI_E_STATE, "no persistent step kernel for this configuration");
+    if (on && c->fwi)
+        return fail(SOFI_E_STATE, "the FWI gradient pass runs the plain kernels");
     CK(cudaStreamSynchronize(c->stream));
     c->persist = on != 0;
     c->graph_dirty = true;

@@ -64,6 +64,12 @@ def load():
         L.sofih_model_suffixes.argtypes = [ctypes.c_int, P(ctypes.c_char_p), ctypes.c_int]
         L.sofih_write_su.argtypes = [ctypes.c_char_p, fp, ctypes.c_int, ctypes.c_int, ip, ip, ctypes.c_float,
                                      ctypes.c_float, P(SofihPar), ctypes.c_int, ctypes.c_int]
+        L.sofih_fwi_read_data.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, fp]
+        L.sofih_fwi_residual.argtypes = [fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, fp,
+                                         P(ctypes.c_double)]
+        L.sofih_fwi_model_gradients.argtypes = [ctypes.c_size_t] + [fp] * 9
+        L.sofih_fwi_model_gradients.restype = None
+        L.sofih_write_gradient.argtypes = [ctypes.c_char_p, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         _LIB = L
     return _LIB
 
@@ -195,3 +201,39 @@ def read_model(p: SofihPar, mfile: str) -> dict:
         res[names[k].decode()] = np.ctypeslib.as_array(out[k], shape=(p.nx, p.ny)).copy()
         libc.free(ctypes.cast(out[k], ctypes.c_void_p))
     return res
+
+
+# ---- FWI gradient pass (host side)
+def fwi_read_data(path: str, ntr: int, ns: int) -> np.ndarray:
+    """The first ntr traces of ns samples of an observed SU file (inseis.c)."""
+    out = np.empty((ntr, ns), dtype=np.float32)
+    if load().sofih_fwi_read_data(path.encode(), ntr, ns, _fp(out)):
+        raise _err()
+    return out
+
+
+def fwi_residual(calc, data, velocity: int, dt: float) -> tuple:
+    """calc_res.c (LNORM 2): the time-reversed residual [ntr][ns] and its L2."""
+    c = np.ascontiguousarray(calc, dtype=np.float32)
+    d = np.ascontiguousarray(data, dtype=np.float32)
+    assert c.shape == d.shape
+    out = np.empty_like(c)
+    l2 = ctypes.c_double()
+    if load().sofih_fwi_residual(_fp(c), _fp(d), c.shape[0], c.shape[1], velocity, dt, _fp(out), ctypes.byref(l2)):
+        raise _err()
+    return out, l2.value
+
+
+def fwi_model_gradients(lam, mu, rhos, vp, vs, rho) -> tuple:
+    """inversion.c:225-240: (vp, vs, rho') gradients, any common layout."""
+    a = [np.ascontiguousarray(x, dtype=np.float32) for x in (lam, mu, rhos, vp, vs, rho)]
+    out = [np.empty_like(a[0]) for _ in range(3)]
+    load().sofih_fwi_model_gradients(a[0].size, *[_fp(x) for x in a + out])
+    return tuple(out)
+
+
+def write_gradient(path: str, g, idx: int = 1, idy: int = 1):
+    """A [ny][nx] gradient file as the reference writes it (writemod.c, format 3)."""
+    a = np.ascontiguousarray(g, dtype=np.float32)
+    if load().sofih_write_gradient(path.encode(), _fp(a), a.shape[1], a.shape[0], idx, idy):
+        raise _err()

@@ -121,6 +121,24 @@ class TimeLoop:
         N.check(self.lib.sofi_velocity_variant(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    # ---- FWI gradient pass (EL_ISO, one shot)
+    def fwi_begin(self, vp, vs, rho, velocity: int = 1, adjoint_type: int = 1):
+        """vp / vs / rho as [NY][NX]; the next reset + run is the forward run."""
+        m = [_f32(a).reshape(self.cfg.ny, self.cfg.nx) for a in (vp, vs, rho)]
+        self._fwi_model = m
+        N.check(self.lib.sofi_fwi_begin(self.h, velocity, adjoint_type, *[_fp(a) for a in m]))
+
+    def fwi_backward(self, adj_x, adj_y):
+        ax, ay = _f32(adj_x), _f32(adj_y)
+        assert ax.shape == ay.shape == (self.ntr[0], self.cfg.nt)
+        N.check(self.lib.sofi_fwi_backward(self.h, _fp(ax), _fp(ay)))
+
+    def fwi_gradients(self) -> tuple:
+        """(gradLam_shot, gradMu_shot, gradRhos_shot), [NY][NX] float32."""
+        out = [np.empty((self.cfg.ny, self.cfg.nx), dtype=np.float32) for _ in range(3)]
+        N.check(self.lib.sofi_fwi_gradients(self.h, *[_fp(a) for a in out]))
+        return tuple(out)
+
     def persistent(self) -> tuple:
         """(on, blocks per launch) of the persistent step kernel."""
         a, b = ctypes.c_int(), ctypes.c_int()

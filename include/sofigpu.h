@@ -197,6 +197,30 @@ int sofi_kernel_time(sofi_ctx *ctx, const char *name, double *avg_ms, long long 
  * times the variants on the zeroed arrays (where each leaves them zero) and
  * keeps the fastest for the grid shape; SOFI_VROWS=w4|w2|t4|1|2|4 fixes it. */
 int sofi_velocity_variant(sofi_ctx *ctx, int *cells_per_thread, int *rows_per_thread);
+/* ---- FWI gradient pass of one shot (MODE = FWI, ITERMAX 1, DTINV 1) ------
+ * Replaces the gradient part of the reference's inversion()
+ * (src/inversion.c:32-252 with snap_store.c, calc_conv.c and the sw = 1
+ * branches of time_loop.c:288-303, update_v_interior.c:72-90 and
+ * wavefield_update_v.c:31-44) for WEQ = EL_ISO, one shot per context,
+ * NDT = 1, SEISMO 1 or 4.
+ * sofi_fwi_begin: the model as read (vp, vs, rho; [NY][NX] row-major) and the
+ *   pass's VELOCITY (1: velocities, 0: displacements) and ADJOINT_TYPE (1:
+ *   x and y residuals, 2: y, 3: x); allocates the forward store (NT x 5 x
+ *   NX x NY floats; SOFI_E_NOMEM if it does not fit) and zeroes the sums. The
+ *   next sofi_reset(ctx, -1) + sofi_run of NT steps is the forward run; it
+ *   keeps every step's gradient quantities.
+ * sofi_fwi_backward: the adjoint signals ([ntr][NT] each, time-reversed
+ *   residuals as calc_res.c forms them, sofih_fwi_residual) after a complete
+ *   forward run: zeroes the wavefield and runs NT steps with them injected at
+ *   the receivers, no other source, correlating every step with forward step
+ *   NT - nt + 1. Synchronous. The sections then hold the backward run's.
+ * sofi_fwi_gradients: gradLam_shot, gradMu_shot, gradRhos_shot ([NY][NX]);
+ *   sofih_fwi_model_gradients turns them into the vp / vs / rho' gradients. */
+int sofi_fwi_begin(sofi_ctx *ctx, int velocity, int adjoint_type, const float *vp, const float *vs,
+                   const float *rho);
+int sofi_fwi_backward(sofi_ctx *ctx, const float *adj_x, const float *adj_y);
+int sofi_fwi_gradients(sofi_ctx *ctx, float *grad_lam, float *grad_mu, float *grad_rhos);
+
 /* The persistent step kernel: chunks of up to 128 time steps (until the next
  * snapshot or timed step) run as one cooperative launch whose blocks step
  * through the velocity, stress and post phases with a grid-wide barrier

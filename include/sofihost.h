@@ -9,11 +9,16 @@
  *     averaging and DT scaling (prepmod.c, av_*.c, prepare_update_s_*.c),
  *     CPML profiles (PML_pro.c) and the damping frame (absorb.c),
  *   - source and receiver files (sources.c, receiver.c), wavelets (wavelet.c),
- *   - SU seismograms (outseis_glob.c, write_su.c) and binary snapshots (snap_ssg.c).
+ *   - SU seismograms (outseis_glob.c, write_su.c) and binary snapshots (snap_ssg.c),
+ *   - the host side of an FWI gradient pass: observed data, residuals, the
+ *     vp / vs / rho' gradients and their files (inseis.c, calc_res.c,
+ *     inversion.c, output_gradient.c).
  * Pure C; no CUDA types. Errors return non-zero with sofih_last_error().
  */
 #ifndef SOFIHOST_H
 #define SOFIHOST_H
+
+#include <stddef.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -104,6 +109,25 @@ int sofih_write_signal(const sofih_par *p, int ishot, const float *signal, int n
                        float ys, char *path_out, int path_len);
 /* Append frames to a binary snapshot file (float32, x outer, y inner). */
 int sofih_write_snap(const char *path, const float *frame, int n, int append);
+
+/* ---- FWI gradient pass (MODE = FWI; with sofi_fwi_* of sofigpu.h) ------
+ * sofih_fwi_read_data: the first ntr traces of ns samples of an observed SU
+ *   file (inseis.c; "<DATA_DIR>_vx.su.shot<n>") into out [ntr][ns].
+ * sofih_fwi_residual: calc_res.c for LNORM = 2 -- with velocity = 0 both
+ *   sections are integrated (running float sum times DT) -- synthetic minus
+ *   observed, reversed in time: diff [ntr][ns] drives the backward run; l2 =
+ *   sum of its squares.
+ * sofih_fwi_model_gradients: inversion.c:225-240 per cell (n cells, any
+ *   common layout): the vp / vs / rho' gradients from the Lame / density sums
+ *   and the model.
+ * sofih_write_gradient: a [ny][nx] gradient as the reference writes it
+ *   (writemod.c format 3: x outer, y inner, every idx-th / idy-th cell). */
+int sofih_fwi_read_data(const char *path, int ntr, int ns, float *out);
+int sofih_fwi_residual(const float *calc, const float *data, int ntr, int ns, int velocity, float dt, float *diff,
+                       double *l2);
+void sofih_fwi_model_gradients(size_t n, const float *lam, const float *mu, const float *rhos, const float *vp,
+                               const float *vs, const float *rho, float *gvp, float *gvs, float *grho);
+int sofih_write_gradient(const char *path, const float *g, int nx, int ny, int idx, int idy);
 
 #ifdef __cplusplus
 }

@@ -87,7 +87,10 @@ def test_gpu_matches_oracle_examples(name):
 
 @pytest.mark.parametrize("name", ["el_cpml_fd8", "visc_cpml_fs_l3", "vvti_cpml_l2", "el_abs_fd10"])
 def test_march_kernels_match_simple_kernels(name, monkeypatch):
-    """The y-marching kernels and the one-cell-per-thread kernels compute the same step."""
+    """The y-marching kernels and the one-cell-per-thread kernels compute the same
+    step, to float32 rounding grown over the run: the two instruction streams
+    contract the stencil sums into fused multiply-adds differently (the bound
+    of the vector-width tests)."""
     from oracle import oracle as O
     from tests.golden.cases import case_by_name
     from tests.helpers import case_receivers, case_sources
@@ -97,14 +100,15 @@ def test_march_kernels_match_simple_kernels(name, monkeypatch):
     sp = case_sources(case, cfg)
     sig = O.wavelet(1, cfg.nt, cfg.dt, sp)
     out = {}
-    monkeypatch.setenv("SOFI_VROWS", "1")  # the one-cell velocity kernel beside the marching one
+    monkeypatch.setenv("SOFI_VROWS", "1")  # the one-cell kernels beside the marching ones
+    monkeypatch.setenv("SOFI_SW", "0")
     for variant in ["simple", "march"]:
         monkeypatch.setenv("SOFI_KERNELS", variant)
         t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
         out[variant] = {k: t.field(k) for k in ["vx", "vy", "sxx", "syy", "sxy"]}
         t.close()
     for k in out["march"]:
-        assert rel_l2(out["march"][k], out["simple"][k]) < 1e-6, (name, k)
+        assert rel_l2(out["march"][k], out["simple"][k]) < 5e-5, (name, k, rel_l2(out["march"][k], out["simple"][k]))
     o.close()
 
 
