@@ -160,8 +160,8 @@ int sofih_read_par(const char *path, sofih_par *p)
     float ratio = p->time / p->dt;
     p->nt = (int)floor(ratio + 0.5);
     p->fdorder = geti(kv, "FDORDER", 4), p->maxrelerror = geti(kv, "MAXRELERROR", 0);
-    if (geti(kv, "FDORDER_TIME", 2) != 2) {
-        sofih_set_error("FDORDER_TIME=4 is not supported");
+    if (geti(kv, "FDORDER_TIME", 2) != 2 && geti(kv, "FDORDER_TIME", 2) != 4) {
+        sofih_set_error("FDORDER_TIME must be 2 or 4 (read_par_json.c)");
         free(kv);
         return 1;
     }
@@ -195,6 +195,14 @@ int sofih_read_par(const char *path, sofih_par *p)
     p->idx = geti(kv, "IDX", 1), p->idy = geti(kv, "IDY", 1);
     gets_(kv, "SNAP_FILE", p->snap_file, sizeof p->snap_file);
     gets_(kv, "MFILE", p->mfile, sizeof p->mfile);
+    /* MODE = FWI (read_par_json_fwi.c): the keys one gradient pass reads */
+    const char *mode = get(kv, "MODE");
+    p->mode_fwi = mode && !strcmp(mode, "FWI");
+    p->fwi_itermax = geti(kv, "ITERMAX", 1), p->fwi_velocity = geti(kv, "VELOCITY", 0);
+    p->fwi_adjoint = geti(kv, "ADJOINT_TYPE", 1), p->fwi_lnorm = geti(kv, "LNORM", 2);
+    p->fwi_dtinv = geti(kv, "DTINV", 1);
+    gets_(kv, "DATA_DIR", p->data_dir, sizeof p->data_dir);
+    gets_(kv, "GRADIENT", p->gradient, sizeof p->gradient);
     free(kv);
     return 0;
 }

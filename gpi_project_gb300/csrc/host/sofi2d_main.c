@@ -4,13 +4,22 @@
  *   sofi2d_gb300 par.json [device]
  *
  * Same inputs and outputs as the reference's forward mode (src/sofi2D.c
- * main(), MODE=FW, FDORDER_TIME=2): parameter file, binary model files,
+ * main(), MODE=FW, FDORDER_TIME 2 or 4): parameter file, binary model files,
  * source and receiver files; SU seismograms SEIS_FILE_<comp>.su (.shotN with
  * RUN_MULTIPLE_SHOTS) and binary snapshots. The domain is never decomposed,
  * so snapshots are written merged (the file snapmerge would produce,
  * SNAP_FILE.bin.<comp>). With RUN_MULTIPLE_SHOTS = 1 every shot is resident
  * in one context and advanced together instead of one after the other
  * (reference sofi2D.c:325 loops over shots).
+ *
+ * MODE = FWI runs the gradient pass of the first iteration (sofi2D.c:277-393
+ * with inversion.c, ITERMAX treated as 1) for EL_ISO with LNORM = 2 and
+ * DTINV = 1: per shot a forward run keeping the gradient quantities, its
+ * seismograms (SEIS_FILE_<comp>.su.shot<n>), the residuals against
+ * DATA_DIR_<comp>.su.shot<n>, the backward run, and the gradient files
+ * GRADIENT_gradient.{vp,vs,rho}.shot<n>; after the last shot their sums
+ * GRADIENT_gradient.{vp,vs,rho} (output_gradient.c). Model updates, step
+ * length search and L-BFGS are not part of it.
  */
 #include "sofigpu.h"
 #include "sofihost.h"
@@ -42,6 +51,93 @@ static double now_s(void)
             return 1;                                                           \
         }                                                                       \
     } while (0)
+
+/* [NX][NY] (model files) -> [NY][NX] */
+static float *transpose_xy(const float *a, int nx, int ny)
+{
+    float *t = (float *)malloc(sizeof(float) * (size_t)nx * ny);
+    for (int i = 0; i < nx; i++)
+        for (int j = 0; j < ny; j++)
+            t[(size_t)j * nx + i] = a[(size_t)i * ny + j];
+    return t;
+}
+
+/* One FWI gradient pass over the shots (inversion.c, output_gradient.c). */
+static int run_fwi(const sofih_par *p, sofi_ctx *ctx, int nsrc, const float *srcpos, const float *srcxy,
+                   const float *sig, int ntr, const int *rix, const int *riy, const float *vp, const float *vs,
+                   const float *rho)
+{
+    if (p->weq != 2 || p->fwi_lnorm != 2 || p->fwi_dtinv != 1) {
+        fprintf(stderr, "sofi2d_gb300: MODE = FWI needs WEQ = EL_ISO, LNORM = 2 and DTINV = 1\n");
+        return 1;
+    }
+    if (!ntr || !nsrc) {
+        fprintf(stderr, "sofi2d_gb300: MODE = FWI needs sources and receivers\n");
+        return 1;
+    }
+    const int nx = p->nx, ny = p->ny, nt = p->nt;
+    const size_t n = (size_t)nx * ny;
+    float *mv = transpose_xy(vp, nx, ny), *ms = transpose_xy(vs, nx, ny), *mr = transpose_xy(rho, nx, ny);
+    float *buf = (float *)calloc(12 * n + 6 * (size_t)ntr * nt, sizeof(float));
+    float *lam = buf, *mu = buf + n, *rhos = buf + 2 * n, *g = buf + 3 * n, *sum = buf + 6 * n;
+    float *cx = buf + 12 * n, *cy = cx + (size_t)ntr * nt, *dx = cy + (size_t)ntr * nt;
+    float *dy = dx + (size_t)ntr * nt, *rx = dy + (size_t)ntr * nt, *ry = rx + (size_t)ntr * nt;
+    const int nshots = p->run_multiple_shots ? nsrc : 1;
+    const char *gn[3] = {"vp", "vs", "rho"};
+    int rc = 0;
+    for (int s = 0; s < nshots && !rc; s++) {
+        if (nshots == 1) {
+            CHECK_G(sofi_set_sources(ctx, 0, nsrc, srcpos, sig));
+        } else {
+            float one[12];
+            for (int r = 0; r < 12; r++)
+                one[r] = srcpos[r * nsrc + s];
+            CHECK_G(sofi_set_sources(ctx, 0, 1, one, sig + (size_t)s * nt));
+        }
+        CHECK_G(sofi_fwi_begin(ctx, p->fwi_velocity, p->fwi_adjoint, mv, ms, mr));
+        CHECK_G(sofi_reset(ctx, -1));
+        CHECK_G(sofi_run(ctx, nt));
+        CHECK_G(sofi_synchronize(ctx));
+        CHECK_G(sofi_get_section(ctx, 0, 1, cx));
+        CHECK_G(sofi_get_section(ctx, 0, 2, cy));
+        char path[700];
+        const int src = nshots == 1 ? 0 : s;
+        for (int q = 0; q < 2; q++) { /* the forward seismograms, as the reference writes them in FWI mode */
+            snprintf(path, sizeof path, "%s_%s.su.shot%d", p->seis_file, q ? "vy" : "vx", s + 1);
+            if (sofih_write_su(path, q ? cy : cx, ntr, nt, rix, riy, srcxy[src], srcxy[nsrc + src], p, s + 1,
+                               q + 1))
+                DIE_H();
+        }
+        double l2x = 0, l2y = 0;
+        snprintf(path, sizeof path, "%s_vx.su.shot%d", p->data_dir, s + 1);
+        if (sofih_fwi_read_data(path, ntr, nt, dx) ||
+            sofih_fwi_residual(cx, dx, ntr, nt, p->fwi_velocity, p->dt, rx, &l2x))
+            DIE_H();
+        snprintf(path, sizeof path, "%s_vy.su.shot%d", p->data_dir, s + 1);
+        if (sofih_fwi_read_data(path, ntr, nt, dy) ||
+            sofih_fwi_residual(cy, dy, ntr, nt, p->fwi_velocity, p->dt, ry, &l2y))
+            DIE_H();
+        CHECK_G(sofi_fwi_backward(ctx, rx, ry));
+        CHECK_G(sofi_fwi_gradients(ctx, lam, mu, rhos));
+        sofih_fwi_model_gradients(n, lam, mu, rhos, mv, ms, mr, g, g + n, g + 2 * n);
+        for (int k = 0; k < 3 && !rc; k++) {
+            snprintf(path, sizeof path, "%s_gradient.%s.shot%d", p->gradient, gn[k], s + 1);
+            rc = sofih_write_gradient(path, g + k * n, nx, ny, p->idx, p->idy);
+            for (size_t q = 0; q < n; q++) /* inversion.c:243-251 */
+                sum[k * n + q] += g[k * n + q];
+        }
+        printf("sofi2d_gb300: FWI shot %d: L2 (x, y) %.6e %.6e\n", s + 1, l2x, l2y);
+    }
+    for (int k = 0; k < 3 && !rc; k++) {
+        char path[700];
+        snprintf(path, sizeof path, "%s_gradient.%s", p->gradient, gn[k]);
+        rc = sofih_write_gradient(path, sum + k * n, nx, ny, p->idx, p->idy);
+    }
+    if (rc)
+        DIE_H();
+    free(buf), free(mv), free(ms), free(mr);
+    return 0;
+}
 
 int main(int argc, char **argv)
 {
@@ -93,7 +189,7 @@ int main(int argc, char **argv)
                 fprintf(stderr, "warning: %s - no signature written\n", sofih_last_error());
         }
     }
-    int nshots = (p.run_multiple_shots && nsrc > 0) ? nsrc : 1;
+    int nshots = (p.run_multiple_shots && nsrc > 0 && !p.mode_fwi) ? nsrc : 1;  /* FWI: one shot at a time */
 
     sofi_config c;
     memset(&c, 0, sizeof c);
@@ -119,6 +215,15 @@ int main(int argc, char **argv)
         int n = sofih_prep_vector(prep, vecs[k], &d);
         if (n)
             CHECK_G(sofi_set_model_vector(ctx, vecs[k], d, n));
+    }
+    if (p.mode_fwi) {
+        if (ntr)
+            CHECK_G(sofi_set_receivers(ctx, 0, ntr, rix, riy));
+        int rc = run_fwi(&p, ctx, nsrc, srcpos, srcxy, sig, ntr, rix, riy, vp, vs, rho);
+        sofi_destroy(ctx);
+        sofih_prep_free(prep);
+        printf("sofi2d_gb300: total %.3f s\n", now_s() - t0);
+        return rc;
     }
     for (int s = 0; s < nshots; s++) {
         if (nshots == 1) {

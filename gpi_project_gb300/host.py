@@ -29,7 +29,10 @@ class SofihPar(ctypes.Structure):
                 ("tsnap1", ctypes.c_float), ("tsnap2", ctypes.c_float), ("tsnapinc", ctypes.c_float),
                 ("idx", ctypes.c_int), ("idy", ctypes.c_int), ("snap_file", ctypes.c_char * 256),
                 ("mfile", ctypes.c_char * 256), ("sigout", ctypes.c_int), ("sigout_format", ctypes.c_int),
-                ("sigout_file", ctypes.c_char * 256), ("fdorder_time", ctypes.c_int)]
+                ("sigout_file", ctypes.c_char * 256), ("fdorder_time", ctypes.c_int),
+                ("mode_fwi", ctypes.c_int), ("fwi_itermax", ctypes.c_int), ("fwi_velocity", ctypes.c_int),
+                ("fwi_adjoint", ctypes.c_int), ("fwi_lnorm", ctypes.c_int), ("fwi_dtinv", ctypes.c_int),
+                ("data_dir", ctypes.c_char * 256), ("gradient", ctypes.c_char * 256)]
 
 
 _LIB = None

@@ -49,6 +49,10 @@ typedef struct {
     int sigout, sigout_format;  /* source wavelet output (initsrc.c:64-93): 1 SU, 2 ASCII, 3 binary */
     char sigout_file[256];
     int fdorder_time;           /* 2 leapfrog, 4 Adams-Bashforth (gv->FDORDER_TIME) */
+    /* MODE = FWI (read_par_json_fwi.c): one gradient pass per shot */
+    int mode_fwi;
+    int fwi_itermax, fwi_velocity, fwi_adjoint, fwi_lnorm, fwi_dtinv;
+    char data_dir[256], gradient[256];
 } sofih_par;
 
 const char *sofih_last_error(void);

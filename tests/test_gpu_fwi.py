@@ -76,3 +76,42 @@ def test_gpu_fwi_rejects_unsupported(monkeypatch):
         with pytest.raises(Exception):
             t.fwi_begin(z, z, z, velocity=1, adjoint_type=1)
         t.close()
+
+
+@pytest.mark.parametrize("name", ["fwi_el_cpml", "fwi_el_abs_v0"])
+def test_cli_fwi_writes_the_reference_gradient_files(name, tmp_path):
+    """sofi2d_gb300 on the reference's own MODE = FWI parameter file: the
+    forward seismograms and the gradient files (per shot and summed) it
+    writes match the compiled reference's."""
+    import subprocess
+    from gpi_project_gb300 import build as B
+    from gpi_project_gb300 import host as H
+    from tests.golden.cases import fwi_case_by_name, fwi_json_text, write_case
+    case = fwi_case_by_name(name)
+    g = np.load(os.path.join(HERE, "golden", f"ref_{name}.npz"))
+    work = str(tmp_path)
+    write_case(case, work)
+    for d in ("obs", "grad"):
+        os.makedirs(os.path.join(work, d), exist_ok=True)
+    with open(os.path.join(work, "fwi.json"), "w") as fh:
+        fh.write(fwi_json_text(case))
+    p = H.read_par(os.path.join(work, "fwi.json"))
+    assert p.mode_fwi == 1 and p.fwi_velocity == case["velocity"] and p.fwi_adjoint == case["adjoint_type"]
+    ntr = g["obs_vx"].shape[0]
+    ix = np.arange(1, ntr + 1, dtype=np.int32)
+    for comp, k in (("vx", 1), ("vy", 2)):
+        H.write_su(os.path.join(work, "obs", f"seis_{comp}.su.shot1"), g[f"obs_{comp}"], ix, ix, 0.0, 0.0, p, 1, k)
+    cli = B.build()["cli"]
+    r = subprocess.run([cli, "fwi.json"], cwd=work, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    nx, ny = case["nx"], case["ny"]
+    from oracle.oracle import read_su
+    for comp in ("vx", "vy"):
+        _, sec = read_su(os.path.join(work, "out", f"seis_{comp}.su.shot1"))
+        assert rel_l2(sec, g[f"fwd_{comp}"]) <= L2_TOL and rel_max(sec, g[f"fwd_{comp}"]) <= MAX_TOL
+    for k in ("vp", "vs", "rho"):
+        for suffix in (".shot1", ""):
+            a = np.fromfile(os.path.join(work, "grad", f"g_gradient.{k}{suffix}"), dtype=np.float32)
+            a = a.reshape(nx, ny).T
+            ref = g[f"grad_{k}"]
+            assert rel_l2(a, ref) <= GRAD_L2 and rel_max(a, ref) <= GRAD_MAX, (name, k, suffix, rel_l2(a, ref))

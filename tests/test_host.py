@@ -169,3 +169,27 @@ def test_su_model_files_read_like_binary(tmp_path):
     short = host.make_par(weq=2, nx=nx, ny=ny + 6, dh=1.0, dt=1e-4, nt=10)
     with pytest.raises(RuntimeError, match="samples"):
         host.read_model(short, str(tmp_path / "su"))
+
+
+def test_parameter_file_fdorder_time_and_fwi_keys(tmp_path):
+    """FDORDER_TIME 4 is read (2 and 4 only, read_par_json.c); MODE = FWI and
+    the keys of one gradient pass (read_par_json_fwi.c) are read."""
+    from gpi_project_gb300 import host as H
+    from tests.golden.cases import FWI_CASES, fwi_json_text
+    base = '{\n"NX" : "10",\n"NY" : "12",\n"DH" : "1.0",\n"DT" : "1e-4",\n"TIME" : "0.01",\n"WEQ" : "VEL_ISO",\n'
+    path = str(tmp_path / "p.json")
+    with open(path, "w") as fh:
+        fh.write(base + '"FDORDER_TIME" : "4"\n}\n')
+    p = H.read_par(path)
+    assert p.fdorder_time == 4 and p.mode_fwi == 0
+    with open(path, "w") as fh:
+        fh.write(base + '"FDORDER_TIME" : "3"\n}\n')
+    with pytest.raises(RuntimeError):
+        H.read_par(path)
+    case = FWI_CASES[1]
+    with open(path, "w") as fh:
+        fh.write(fwi_json_text(case))
+    p = H.read_par(path)
+    assert (p.mode_fwi, p.fwi_velocity, p.fwi_adjoint, p.fwi_lnorm, p.fwi_dtinv) == (
+        1, case["velocity"], case["adjoint_type"], 2, 1)
+    assert p.data_dir.decode() == "./obs/seis" and p.gradient.decode() == "./grad/g"
