@@ -313,11 +313,136 @@ def main_served(args):
     print(json.dumps(out), flush=True)
 
 
+def main_fwi(args):
+    """--workload fwi: a step is one FWI gradient pass of one shot (forward run
+    keeping every step's gradient quantities, residuals against the observed
+    data, backward run with the correlation) through the C ABI; value counts
+    both runs' cell updates."""
+    rank, world, local = dist_info()
+    from gpi_project_gb300 import workloads
+    W = workloads.workload("fwi")
+    par = W["par"]
+    if args.nt:
+        par["nt"] = args.nt
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps({"impl": "reference", "unavailable": "the FWI workload has no CPU reference arm here; "
+                          "its cpu_baseline is the oracle's gradient pass"}))
+        return
+    import torch
+    from gpi_project_gb300 import TimeLoop, host, make_config
+    torch.cuda.set_device(local)
+    nx, ny, nt = par["nx"], par["ny"], par["nt"]
+    cfg = make_config(weq=2, nx=nx, ny=ny, fdorder=par["fdorder"], maxrelerror=par["maxrelerror"], dt=par["dt"],
+                      dh=par["dh"], nt=nt, fw=par["fw"], abs_type=par["abs_type"], seismo=1, ndt=1, nshots=1,
+                      shared_model=1)
+    p = host_par(W)
+    sig = host.wavelet(1, nt, par["dt"], W["src"])
+
+    def context(mats):
+        fields, vecs = host.prepare(p, mats)
+        vecs.pop("_dt_max"), vecs.pop("_stable")
+        t = TimeLoop(cfg, device=local)
+        t.set_model(fields)
+        t.set_vectors(vecs)
+        t.set_sources(W["src"], sig)
+        t.set_receivers(*W["rec"])
+        return t
+
+    tt = context(W["true_mats"])  # the observed data (not timed)
+    tt.reset()
+    tt.run()
+    obs = [tt.section("vx"), tt.section("vy")]
+    tt.close()
+    t = context(W["mats"])
+    model = [W["mats"][k].T.copy() for k in ("vp", "vs", "rho")]
+    l2 = [0.0]
+
+    def gradient_pass():
+        t.fwi_begin(*model, velocity=1, adjoint_type=1)
+        t.reset()
+        t.run()
+        rx, lx = host.fwi_residual(t.section("vx"), obs[0], 1, par["dt"])
+        ry, ly = host.fwi_residual(t.section("vy"), obs[1], 1, par["dt"])
+        t.fwi_backward(rx, ry)
+        g = t.fwi_gradients()
+        l2[0] = lx + ly
+        return g
+
+    for _ in range(max(1, args.warmup)):
+        gradient_pass()
+    torch.cuda.synchronize()
+    launches0 = t.launch_count()
+    with ClockSampler(local) as clk:
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            g = gradient_pass()
+        torch.cuda.synchronize()
+        sec = (time.perf_counter() - w0) / args.steps
+    launches = t.launch_count() - launches0
+    updates = 2.0 * nx * ny * nt
+    value = updates / sec / 1e9
+    peak, peak_kind = measured_peaks()
+    # algorithmic bytes per cell update: the EL_ISO step (60 B) plus, forward, the kernels' gradient
+    # quantities (20 B written) and their copy into the store (20 B read, 20 B written); backward, the
+    # density term (v, store 2 x 4 B, sum read + written: 24 B) and the lambda / mu terms (store 3 x 4,
+    # stresses 12, model 4 x 4, two sums read + written: 56 B)
+    bpc = (60 + 20 + 40 + 60 + 24 + 56) / 2.0
+    store_gb = 5.0 * nx * ny * nt * 4 / 1e9
+    t.close()
+    if rank != 0:
+        return
+    out = {
+        "metric": "Gcell-updates/s", "value": round(value, 4), "unit": "Gcell-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": max(1, args.warmup), "ms_per_step": round(1e3 * sec, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded; gpi_project_gb300/workloads.py 'fwi', observed data from a perturbed model)",
+        "config": {"workload": "fwi", "nx": nx, "ny": ny, "nt": nt, "weq": 2, "fdorder": par["fdorder"],
+                   "fw": par["fw"], "velocity": 1, "adjoint_type": 1, "receivers": len(W["rec"][0]),
+                   "forward_store_gb": round(store_gb, 2),
+                   "l2": "inputs larger than L2 (forward store %.1f GB)" % store_gb, "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(value, 4), "unit": "Gcell-updates/s",
+                "h2d_bytes_per_step": int(2 * len(W["rec"][0]) * nt * 4 + 3 * nx * ny * 4),
+                "d2h_bytes_per_step": int(2 * len(W["rec"][0]) * nt * 4 + 3 * nx * ny * 4)},
+        "step_roofline": {"bytes_per_cell": bpc, "achieved": round(bpc * value, 1),
+                          "frac": round(bpc * value / peak, 4), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s"},
+        "gpu_launches": int(launches), "misfit_l2": l2[0], "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.build()
+        ocfg = O.SofiConfig()
+        for k in ["weq", "nx", "ny", "dh", "dt", "fdorder", "maxrelerror", "fw", "abs_type", "npower", "k_max_cpml",
+                  "vppml", "fpml", "seismo", "ndt"]:
+            setattr(ocfg, k, par[k])
+        ns = args.cpu_steps or max(20, min(nt, auto_cpu_steps(W) // 2))
+        ocfg.nt = ns
+        o = O.Oracle(ocfg, "f32", cpu_threads())
+        o.set_material({k: v.reshape(-1) for k, v in W["mats"].items()})
+        o.set_sources(W["src"], O.wavelet(1, ns, ocfg.dt, W["src"]))
+        o.set_receivers(*W["rec"])
+        w0 = time.perf_counter()
+        o.reset()
+        o.fwi_begin(1, 1)
+        o.run()
+        cx, cy = o.section("vx"), o.section("vy")
+        o.fwi_backward(*[np.ascontiguousarray(O.fwi_residual(c, c * 0.99, 1, ocfg.dt)[0]) for c in (cx, cy)])
+        csec = time.perf_counter() - w0
+        o.close()
+        out["cpu_baseline"] = {"value": round(2.0 * nx * ny * ns / csec / 1e9, 4), "unit": "Gcell-updates/s",
+                               "cores": cpu_threads(), "kind": "port",
+                               "sample": f"the oracle's gradient pass with NT = {ns} on the same grid ({csec:.1f} s)"}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
     if args.workload == "c5":
         return main_served(args)
+    if args.workload == "fwi":
+        return main_fwi(args)
     from gpi_project_gb300 import workloads
     W = workloads.workload(args.workload)
     if args.nt:

@@ -92,6 +92,7 @@ struct FwiDev {
     float *px, *py;                 // backward, VELOCITY = 0: running sums of v * DT ([NY][NX])
     float *g_lam, *g_mu, *g_rhos;   // per-shot gradient sums ([NY][NX])
     const float *vp, *vs, *rho;     // the model as read ([NY][NX])
+    double *rc;                     // [3][NY][NX]: 1 / (4 (lam+mu)^2), 1 / mu^2, 1 / (lam+mu)^2 (calc_conv.c)
     const float *adj;               // [2][ntr][NT] adjoint signals (x, y)
     const int *cell_off, *cell_rec; // receivers by cell: cell k holds cell_rec[cell_off[k] .. cell_off[k+1])
     const int *cell_ix, *cell_iy;

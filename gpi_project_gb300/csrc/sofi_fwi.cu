@@ -77,8 +77,28 @@ __global__ void k_fwi_rho(Geo G, Wave W, FwiDev F)
     F.g_rhos[q] = __fadd_rn(F.g_rhos[q], __fmul_rn(-G.dt, t));
 }
 
-// calc_conv.c:34-71: muss / lamss are floats, the constants double, so the
-// lambda and mu terms are formed in double and rounded into the float sums.
+// The model-only divisors of calc_conv.c:42-67, once per pass: muss / lamss
+// are floats and the constants double there, so 1 / (4 (lamss + muss)^2) is
+// formed in double; 1 / muss^2 and 1 / (lamss + muss)^2 are the double
+// reciprocals of the float squares the reference divides by.
+__global__ void k_fwi_coef(int n, FwiDev F)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n)
+        return;
+    const float vs0 = F.vs[q], vp0 = F.vp[q], rho0 = F.rho[q];
+    const float muss = __fmul_rn(__fmul_rn(vs0, vs0), rho0);
+    const float lamss = (float)__dadd_rn((double)__fmul_rn(__fmul_rn(vp0, vp0), rho0), -2.0 * (double)muss);
+    const float lm = __fadd_rn(lamss, muss);
+    F.rc[q] = 1.0 / __dmul_rn(__dmul_rn(4.0, (double)lm), (double)lm);
+    F.rc[n + q] = 1.0 / (double)__fmul_rn(muss, muss);
+    F.rc[2 * n + q] = 1.0 / (double)__fmul_rn(lm, lm);
+}
+
+// calc_conv.c:34-71: the lambda and mu terms are formed in double and rounded
+// into the float sums. The reference divides by (lamss + muss)^2 and muss^2;
+// here their double reciprocals multiply (at most one double ulp apart
+// before the rounding to float).
 __global__ void k_fwi_conv(Geo G, Wave W, Model M, FwiDev F)
 {
     const long long n = (long long)G.nx * G.ny;
@@ -90,23 +110,22 @@ __global__ void k_fwi_conv(Geo G, Wave W, Model M, FwiDev F)
     const long long o = cell(G, j, i);
     const float *slot = F.store + (long long)(F.nt - nt) * 5 * n + q;
     const float fx = slot[2 * n], fy = slot[3 * n], fu = slot[4 * n];
-    const float vs0 = F.vs[q], vp0 = F.vp[q], rho0 = F.rho[q];
-    const float muss = __fmul_rn(__fmul_rn(vs0, vs0), rho0);
-    const float lamss = (float)__dadd_rn((double)__fmul_rn(__fmul_rn(vp0, vp0), rho0), -2.0 * (double)muss);
     const float sxx = W.sxx[o], syy = W.syy[o], sxy = W.sxy[o];
     const double mDT = -(double)G.dt;
-    const float lm = __fadd_rn(lamss, muss);
-    const float mm = __fmul_rn(muss, muss), lm2 = __fmul_rn(lm, lm);
     const float sum_f = __fmul_rn(__fadd_rn(fx, fy), __fadd_rn(sxx, syy));
-    const double inv_lm2 = 1.0 / __dmul_rn(__dmul_rn(4.0, (double)lm), (double)lm);
-    F.g_lam[q] = (float)__dadd_rn((double)F.g_lam[q], __dmul_rn(__dmul_rn(mDT, inv_lm2), (double)sum_f));
+    F.g_lam[q] = (float)__dadd_rn((double)F.g_lam[q], __dmul_rn(__dmul_rn(mDT, F.rc[q]), (double)sum_f));
     if (M.pu[o] > 0.0f) {
-        const double t1 = __dmul_rn(1.0 / (double)mm, (double)__fmul_rn(fu, sxy));
-        const double t2 = __dmul_rn(0.25, (double)sum_f) / (double)lm2;
-        const double t3 =
-            __dmul_rn(0.25, (double)__fmul_rn(__fsub_rn(fx, fy), __fsub_rn(sxx, syy))) / (double)mm;
+        const double r_mm = F.rc[n + q], r_lm2 = F.rc[2 * n + q];
+        const double t1 = __dmul_rn(r_mm, (double)__fmul_rn(fu, sxy));
+        const double t2 = __dmul_rn(__dmul_rn(0.25, (double)sum_f), r_lm2);
+        const double t3 = __dmul_rn(__dmul_rn(0.25, (double)__fmul_rn(__fsub_rn(fx, fy), __fsub_rn(sxx, syy))), r_mm);
         F.g_mu[q] = (float)__dadd_rn((double)F.g_mu[q], __dmul_rn(mDT, __dadd_rn(__dadd_rn(t1, t2), t3)));
     }
+}
+
+void launch_fwi_coef(int n, const FwiDev &F, cudaStream_t st)
+{
+    k_fwi_coef<<<(n + 255) / 256, 256, 0, st>>>(n, F);
 }
 
 void launch_fwi_store(const Geo &G, const Wave &W, const FwiDev &F, cudaStream_t st)

@@ -14,6 +14,7 @@ struct FwiDev;
 // FWI gradient pass (sofi_fwi.cu): forward storage after a step; adjoint
 // injection and the density term before the velocity update; the lambda /
 // mu terms after the post kernel
+void launch_fwi_coef(int n, const FwiDev &F, cudaStream_t st);  // the model-only divisors, once per pass
 void launch_fwi_store(const Geo &G, const Wave &W, const FwiDev &F, cudaStream_t st);
 void launch_fwi_backward_pre(const Geo &G, const Wave &W, const FwiDev &F, cudaStream_t st);
 void launch_fwi_conv(const Geo &G, const Wave &W, const Model &M, const FwiDev &F, cudaStream_t st);

@@ -1493,6 +1493,8 @@ int sofi_fwi_begin(sofi_ctx *c, int velocity, int adjoint_type, const float *vp,
             if ((rc = dalloc(c, (void **)&m[k], n * sizeof(float))))
                 return rc;
         c->F.vp = m[0], c->F.vs = m[1], c->F.rho = m[2];
+        if ((rc = dalloc(c, (void **)&c->F.rc, 3 * n * sizeof(double))))
+            return rc;
         float **wf[] = {&c->W.fa_x, &c->W.fa_y, &c->W.fu_x, &c->W.fu_y, &c->W.fu_xy};
         for (auto p : wf)
             if ((rc = dalloc(c, (void **)p, f)))
@@ -1505,6 +1507,8 @@ int sofi_fwi_begin(sofi_ctx *c, int velocity, int adjoint_type, const float *vp,
     CK(cudaMemcpyAsync((void *)c->F.rho, rho, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
     for (float *p : {c->F.g_lam, c->F.g_mu, c->F.g_rhos})
         CK(cudaMemsetAsync(p, 0, n * sizeof(float), c->stream));
+    launch_fwi_coef((int)n, c->F, c->stream);
+    CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->stream));
     c->F.nt = cf.nt, c->F.velocity = velocity, c->F.adjoint = adjoint_type;
     // the kernels whose bodies write the gradient quantities, fixed for the pass

@@ -92,6 +92,23 @@ def workload(name: str) -> dict:
         xs = np.linspace(21.0, 378.0, 100)
         rec = (np.floor(xs / 1.0).astype(np.int32) + 1, np.full(100, 11, np.int32))
         nshots = 64
+    elif name == "fwi":
+        # one FWI gradient pass (MODE = FWI, EL_ISO, VELOCITY 1, ADJOINT_TYPE 1) on the 400 x 400 grid above,
+        # force-y source; the observed data come from `true_mats` (a 5 % faster, 3 % denser blob)
+        rng = np.random.default_rng(1006)
+        nx = ny = 400
+        vp, vs, rho = layered(rng, nx, ny)
+        par = dict(weq=2, nx=nx, ny=ny, dh=1.0, dt=1e-4, nt=2000, fdorder=8, maxrelerror=1, fw=20, abs_type=1,
+                   npower=4.0, k_max_cpml=1.0, vppml=float(vp.max()), fpml=25.0, seismo=1, ndt=1)
+        mats = dict(vp=vp, vs=vs, rho=rho)
+        true = {k: v.copy() for k, v in mats.items()}
+        for k, f in (("vp", 1.05), ("vs", 1.05), ("rho", 1.03)):
+            true[k][160:240, 180:260] *= np.float32(f)
+        src = _srcpos([(200.0, 5.0)], 1.0, 25.0, 3)
+        xs = np.linspace(21.0, 378.0, 100)
+        rec = (np.floor(xs / 1.0).astype(np.int32) + 1, np.full(100, 11, np.int32))
+        nshots = 1
+        return dict(name=name, par=dict(par, L=0), mats=mats, true_mats=true, src=src, rec=rec, nshots=nshots)
     elif name == "c2":
         rng = np.random.default_rng(1002)
         nx, ny = 4000, 2000
