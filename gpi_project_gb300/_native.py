@@ -109,6 +109,7 @@ def load():
                             P(ctypes.c_float)], ctypes.c_int),
         "sofi_fwi_backward": ([vp, P(ctypes.c_float), P(ctypes.c_float)], ctypes.c_int),
         "sofi_fwi_gradients": ([vp, P(ctypes.c_float), P(ctypes.c_float), P(ctypes.c_float)], ctypes.c_int),
+        "sofi_fwi_checkpoints": ([vp, P(ctypes.c_int), P(ctypes.c_int)], ctypes.c_int),
         "sofi_set_persistent": ([vp, ctypes.c_int], ctypes.c_int),
         "sofi_get_stream": ([vp, P(vp)], ctypes.c_int),
         "sofi_tti_stress_noalloc": ([P(SofiConfig), P(TtiStressArgs), vp], ctypes.c_int),

@@ -88,7 +88,8 @@ struct Wave {
 
 // Device state of an FWI gradient pass (sofi_fwi.cu); one shot per context.
 struct FwiDev {
-    float *store;                   // [NT][5][NY][NX] forward quantities, slot nt - 1
+    float *store;                   // [slots][5][NY][NX] forward quantities of step nt in slot nt - 1 - *base
+    const int *base;                // device: the step before the store's first slot (0, or a segment's start)
     float *px, *py;                 // backward, VELOCITY = 0: running sums of v * DT ([NY][NX])
     float *g_lam, *g_mu, *g_rhos;   // per-shot gradient sums ([NY][NX])
     const float *vp, *vs, *rho;     // the model as read ([NY][NX])

@@ -5,7 +5,9 @@
 //
 // Forward: the velocity and stress kernels write this step's gradient
 // quantities (Wave::fa_*, fu_*); k_fwi_store copies them, or the stresses for
-// VELOCITY = 0, into slot nt of the store ([NT][5][NY][NX] floats).
+// VELOCITY = 0, into the store ([slots][5][NY][NX] floats): slot nt - 1 when
+// the whole run is kept, slot nt - 1 - base for a recomputed segment of a
+// checkpointed pass (base = the segment's first step - 1).
 // Backward, per step: k_fwi_adj adds the adjoint signals at the receivers
 // before the velocity update; k_fwi_rho forms the reference's pvxp1 / pvyp1
 // (the injected velocity, or its running sum times DT for VELOCITY = 0) and
@@ -27,7 +29,7 @@ __global__ void k_fwi_store(Geo G, Wave W, FwiDev F)
     const int nt = *G.step_ctr;  // the step just completed
     const int j = (int)(q / G.nx) + 1, i = (int)(q % G.nx) + 1;
     const long long o = cell(G, j, i);
-    float *slot = F.store + (long long)(nt - 1) * 5 * n + q;
+    float *slot = F.store + (long long)(nt - 1 - *F.base) * 5 * n + q;
     slot[0] = W.fa_x[o];
     slot[n] = W.fa_y[o];
     if (F.velocity) {
@@ -71,7 +73,7 @@ __global__ void k_fwi_rho(Geo G, Wave W, FwiDev F)
         py = __fadd_rn(F.py[q], __fmul_rn(py, G.dt));
         F.px[q] = px, F.py[q] = py;
     }
-    const float *slot = F.store + (long long)(F.nt - nt) * 5 * n + q;
+    const float *slot = F.store + (long long)(F.nt - nt - *F.base) * 5 * n + q;
     // each product and sum rounded on its own, as the reference evaluates it
     const float t = __fadd_rn(__fmul_rn(px, slot[0]), __fmul_rn(py, slot[n]));
     F.g_rhos[q] = __fadd_rn(F.g_rhos[q], __fmul_rn(-G.dt, t));
@@ -108,7 +110,7 @@ __global__ void k_fwi_conv(Geo G, Wave W, Model M, FwiDev F)
     const int nt = *G.step_ctr;
     const int j = (int)(q / G.nx) + 1, i = (int)(q % G.nx) + 1;
     const long long o = cell(G, j, i);
-    const float *slot = F.store + (long long)(F.nt - nt) * 5 * n + q;
+    const float *slot = F.store + (long long)(F.nt - nt - *F.base) * 5 * n + q;
     const float fx = slot[2 * n], fy = slot[3 * n], fu = slot[4 * n];
     const float sxx = W.sxx[o], syy = W.syy[o], sxy = W.sxy[o];
     const double mDT = -(double)G.dt;

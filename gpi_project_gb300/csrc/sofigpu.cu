@@ -11,6 +11,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -199,6 +200,19 @@ struct sofi_ctx {
     FwiDev F{};
     int *d_noacq = nullptr;    // two zero ints: the backward run's empty source list
     size_t fwi_cells_cap = 0;  // capacity of the receiver-cell arrays
+    // checkpointed pass (the store does not hold NT steps): the state after
+    // steps K, 2K, ... of the forward run; every segment is recomputed into a
+    // K-slot store before its backward steps
+    int fwi_K = 0;             // 0: the forward run is stored whole
+    int fwi_nseg = 1;
+    size_t fwi_state = 0;      // floats of one state (wavefield and CPML memory)
+    size_t fwi_slots = 0;      // slots the store holds
+    float *fwi_ckpt = nullptr; // [nseg - 1][fwi_state]
+    size_t fwi_ckpt_cap = 0;
+    float *fwi_tmp = nullptr;  // the backward state while a segment is recomputed
+    bool fwi_store_on = true;  // k_fwi_store runs (off in the checkpointing forward run)
+    bool fwi_nosnap = false;   // a recomputed segment takes no snapshots
+    int *d_fwi_base = nullptr; // device: FwiDev::base
     int sw = 0;                // ISO / VTI stress kernel: cells per thread in x (4 or 2), 0 = one
     bool sw_fixed = false;     // SOFI_SW chose it
     bool tuned = false;        // autotuner ran (or was skipped) for this context
@@ -770,14 +784,14 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
         k_wrap_x<<<dim3((cf.ny + 127) / 128, S), 128, 0, st>>>(G, c->W.sxx, c->W.syy, c->W.sxy, c->nd);
         c->launches++;
     }
-    if (c->fwi) {  // time_loop.c:288-296
+    if (c->fwi && (c->fwi_back || c->fwi_store_on)) {  // time_loop.c:288-296
         if (c->fwi_back)
             launch_fwi_conv(G, c->W, c->M, c->F, st);
         else
             launch_fwi_store(G, c->W, c->F, st);
         c->launches++;
     }
-    if (!capture && cf.snap && nt >= cf.snap_first && nt <= cf.snap_last &&
+    if (!capture && !c->fwi_nosnap && cf.snap && nt >= cf.snap_first && nt <= cf.snap_last &&
         (nt == cf.snap_first || (cf.snap_inc > 0 && (nt - cf.snap_first) % cf.snap_inc == 0)) &&
         c->nsnap < c->snap_total) {
         long long n = (long long)c->snap_nx * c->snap_ny;
@@ -1306,6 +1320,8 @@ static int build_graph(sofi_ctx *c)
     return 0;
 }
 
+static int fwi_copy_state(sofi_ctx *c, float *buf, bool save);
+
 int sofi_run(sofi_ctx *c, int nsteps)
 {
     if (!c || nsteps < 0)
@@ -1327,6 +1343,8 @@ int sofi_run(sofi_ctx *c, int nsteps)
     }
     c->pristine = false;
     CK(cudaEventRecord(c->ev0, c->stream));
+    // the forward run of a checkpointed FWI pass keeps the state after steps K, 2K, ...
+    const bool ckpt_fwd = c->fwi && c->fwi_K && !c->fwi_back && !c->fwi_store_on;
     int left = nsteps;
     while (left > 0) {
         if (c->persist) {
@@ -1342,7 +1360,8 @@ int sofi_run(sofi_ctx *c, int nsteps)
                 continue;
             }
         }
-        if (c->use_graph && left >= kGraphSteps && !chunk_has_event(c, c->step + 1, kGraphSteps)) {
+        const int lim = ckpt_fwd ? std::min(left, c->fwi_K - c->step % c->fwi_K) : left;
+        if (c->use_graph && lim >= kGraphSteps && !chunk_has_event(c, c->step + 1, kGraphSteps)) {
             if (c->graph_dirty || !c->graph_exec) {
                 int rc = build_graph(c);
                 if (rc)
@@ -1352,13 +1371,18 @@ int sofi_run(sofi_ctx *c, int nsteps)
             c->launches += c->graph_launches;
             c->step += kGraphSteps;
             left -= kGraphSteps;
-            continue;
+        } else {
+            int rc = launch_step(c, c->step + 1);
+            if (rc)
+                return rc;
+            c->step++;
+            left--;
         }
-        int rc = launch_step(c, c->step + 1);
-        if (rc)
-            return rc;
-        c->step++;
-        left--;
+        if (ckpt_fwd && c->step % c->fwi_K == 0 && c->step < c->cfg.nt) {
+            int rc = fwi_copy_state(c, c->fwi_ckpt + (size_t)(c->step / c->fwi_K - 1) * c->fwi_state, true);
+            if (rc)
+                return rc;
+        }
     }
     CK(cudaEventRecord(c->ev1, c->stream));
     CK(cudaGetLastError());
@@ -1462,6 +1486,50 @@ int sofi_velocity_variant(sofi_ctx *c, int *cells_per_thread, int *rows_per_thre
     return 0;
 }
 
+// The state a forward or backward FWI run carries from step to step: the
+// wavefield (one shot, padded fields) and, with CPML, the eight memory arrays.
+static std::vector<std::pair<float *, size_t>> fwi_state_parts(sofi_ctx *c)
+{
+    std::vector<std::pair<float *, size_t>> v;
+    const size_t f = (size_t)c->G.fsz;
+    for (float *p : {c->W.vx, c->W.vy, c->W.sxx, c->W.syy, c->W.sxy})
+        v.push_back({p, f});
+    if (c->G.abs_type == 1) {
+        const size_t px = (size_t)c->cfg.ny * c->G.fw2, py = (size_t)c->G.fw2 * c->cfg.nx;
+        for (float *p : {c->W.psi_sxx_x, c->W.psi_sxy_x, c->W.psi_vxx, c->W.psi_vyx})
+            v.push_back({p, px});
+        for (float *p : {c->W.psi_syy_y, c->W.psi_sxy_y, c->W.psi_vyy, c->W.psi_vxy})
+            v.push_back({p, py});
+    }
+    return v;
+}
+
+// save: state -> buf; else buf -> state (buf null: zero the state)
+static int fwi_copy_state(sofi_ctx *c, float *buf, bool save)
+{
+    size_t off = 0;
+    for (auto &pt : fwi_state_parts(c)) {
+        const size_t b = pt.second * sizeof(float);
+        if (save)
+            CK(cudaMemcpyAsync(buf + off, pt.first, b, cudaMemcpyDeviceToDevice, c->stream));
+        else if (buf)
+            CK(cudaMemcpyAsync(pt.first, buf + off, b, cudaMemcpyDeviceToDevice, c->stream));
+        else
+            CK(cudaMemsetAsync(pt.first, 0, b, c->stream));
+        off += pt.second;
+    }
+    return 0;
+}
+
+static int fwi_set_step(sofi_ctx *c, int step, int base)
+{
+    c->step = step;
+    CK(cudaMemcpyAsync(c->G.step_ctr, &step, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_fwi_base, &base, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));  // the host ints above are locals
+    return 0;
+}
+
 int sofi_fwi_begin(sofi_ctx *c, int velocity, int adjoint_type, const float *vp, const float *vs, const float *rho)
 {
     if (!c || !vp || !vs || !rho)
@@ -1477,16 +1545,47 @@ int sofi_fwi_begin(sofi_ctx *c, int velocity, int adjoint_type, const float *vp,
     CK(cudaStreamSynchronize(c->stream));
     const size_t n = (size_t)cf.nx * cf.ny, f = (size_t)c->G.fsz * sizeof(float);
     int rc;
-    if (!c->F.store) {
-        size_t need = (size_t)cf.nt * 5 * n * sizeof(float), fr = 0, tot = 0;
-        CK(cudaMemGetInfo(&fr, &tot));
-        if (need + 16 * n * sizeof(float) + 5 * f > fr)
-            return fail(SOFI_E_NOMEM, "the forward wavefields of %d steps need %zu bytes, %zu free", cf.nt, need, fr);
-        float **fl[] = {&c->F.store, &c->F.px, &c->F.py, &c->F.g_lam, &c->F.g_mu, &c->F.g_rhos};
-        size_t sz[] = {need, n * sizeof(float), n * sizeof(float), n * sizeof(float), n * sizeof(float),
-                       n * sizeof(float)};
-        for (int k = 0; k < 6; k++)
-            if ((rc = dalloc(c, (void **)fl[k], sz[k])))
+    // the whole forward run in the store when it fits, else checkpoints every K
+    // steps (SOFI_FWI_CHECKPOINT=K forces it): memory (nseg - 1 + 1) states + K
+    // slots, one extra forward run per pass whatever K is
+    c->fwi_state = 0;
+    for (auto &pt : fwi_state_parts(c))
+        c->fwi_state += pt.second;
+    const size_t slot = 5 * n * sizeof(float), state = c->fwi_state * sizeof(float);
+    size_t fr = 0, tot = 0;
+    CK(cudaMemGetInfo(&fr, &tot));
+    const size_t reserve = (16 * n) * sizeof(float) + 5 * f + (64u << 20);
+    const size_t have = (c->F.store ? c->fwi_slots * slot : 0) + (c->fwi_ckpt ? c->fwi_ckpt_cap * state : 0) + fr;
+    int K = 0;
+    if (const char *e = getenv("SOFI_FWI_CHECKPOINT"))
+        K = atoi(e) > 0 ? (atoi(e) < cf.nt ? atoi(e) : cf.nt) : 0;
+    if (!K && (size_t)cf.nt * slot + reserve > have) {
+        K = (int)ceil(sqrt((double)cf.nt * (double)state / (double)slot));
+        K = K < 1 ? 1 : (K > cf.nt ? cf.nt : K);
+    }
+    const int nseg = K ? (cf.nt + K - 1) / K : 1;
+    const size_t slots = K ? (size_t)K : (size_t)cf.nt;
+    const size_t nck = K ? (size_t)nseg : 0;  // nseg - 1 checkpoints + the backward state
+    if (slots * slot + nck * state + reserve > have)
+        return fail(SOFI_E_NOMEM, "the FWI pass needs %zu bytes of forward store and checkpoints, %zu free",
+                    slots * slot + nck * state, have);
+    if (slots > c->fwi_slots) {
+        if ((rc = dalloc(c, (void **)&c->F.store, slots * slot)))
+            return rc;
+        c->fwi_slots = slots;
+    }
+    if (nck > c->fwi_ckpt_cap) {
+        if ((rc = dalloc(c, (void **)&c->fwi_ckpt, nck * state)))
+            return rc;
+        c->fwi_ckpt_cap = nck;
+    }
+    c->fwi_tmp = nck ? c->fwi_ckpt + (nck - 1) * c->fwi_state : nullptr;
+    c->fwi_K = K, c->fwi_nseg = nseg;
+    c->fwi_store_on = K == 0;
+    if (!c->F.px) {
+        float **fl[] = {&c->F.px, &c->F.py, &c->F.g_lam, &c->F.g_mu, &c->F.g_rhos};
+        for (int k = 0; k < 5; k++)
+            if ((rc = dalloc(c, (void **)fl[k], n * sizeof(float))))
                 return rc;
         float *m[3];
         for (int k = 0; k < 3; k++)
@@ -1499,9 +1598,12 @@ int sofi_fwi_begin(sofi_ctx *c, int velocity, int adjoint_type, const float *vp,
         for (auto p : wf)
             if ((rc = dalloc(c, (void **)p, f)))
                 return rc;
-        if ((rc = dalloc(c, (void **)&c->d_noacq, 2 * sizeof(int))))
+        if ((rc = dalloc(c, (void **)&c->d_noacq, 2 * sizeof(int))) ||
+            (rc = dalloc(c, (void **)&c->d_fwi_base, sizeof(int))))
             return rc;
+        c->F.base = c->d_fwi_base;
     }
+    CK(cudaMemsetAsync(c->d_fwi_base, 0, sizeof(int), c->stream));
     CK(cudaMemcpyAsync((void *)c->F.vp, vp, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync((void *)c->F.vs, vs, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync((void *)c->F.rho, rho, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
@@ -1577,15 +1679,57 @@ int sofi_fwi_backward(sofi_ctx *c, const float *adj_x, const float *adj_y)
     CK(cudaMemsetAsync(c->F.py, 0, n * sizeof(float), c->stream));
     const Acq saved = c->A;
     const bool saved_force = c->has_force;
-    c->A.src_off = c->d_noacq, c->A.last_type = c->d_noacq;
-    c->has_force = false;
-    c->fwi_back = true, c->graph_dirty = true;
-    rc = sofi_run(c, NT);
+    auto backward_mode = [&](bool on) {
+        if (on)
+            c->A.src_off = c->d_noacq, c->A.last_type = c->d_noacq, c->has_force = false;
+        else
+            c->A = saved, c->has_force = saved_force;
+        c->fwi_back = on, c->graph_dirty = true;
+    };
+    if (!c->fwi_K) {
+        backward_mode(true);
+        rc = sofi_run(c, NT);
+    } else {
+        // segments last to first: recompute the segment's forward steps from
+        // its checkpoint into the store, then run the backward steps that read them
+        const int K = c->fwi_K;
+        int done = 0;
+        for (int seg = c->fwi_nseg - 1; seg >= 0 && !rc; seg--) {
+            const int s0 = seg * K, k = std::min(K, NT - s0);
+            if (done)
+                rc = fwi_copy_state(c, c->fwi_tmp, true);
+            if (!rc)
+                rc = fwi_copy_state(c, seg ? c->fwi_ckpt + (size_t)(seg - 1) * c->fwi_state : nullptr, false);
+            if (!rc)
+                rc = fwi_set_step(c, s0, s0);
+            if (rc)
+                break;
+            backward_mode(false);
+            c->fwi_store_on = true, c->fwi_nosnap = true;
+            if ((rc = sofi_run(c, k)))
+                break;
+            if ((rc = fwi_copy_state(c, done ? c->fwi_tmp : nullptr, false)) || (rc = fwi_set_step(c, done, s0)))
+                break;
+            backward_mode(true);
+            rc = sofi_run(c, k);
+            done += k;
+        }
+        c->fwi_store_on = false, c->fwi_nosnap = false;
+    }
     if (!rc)
         rc = sofi_synchronize(c);
-    c->A = saved, c->has_force = saved_force;
-    c->fwi_back = false, c->graph_dirty = true;
+    backward_mode(false);
     return rc;
+}
+
+int sofi_fwi_checkpoints(sofi_ctx *c, int *interval, int *segments)
+{
+    if (!c || !interval || !segments)
+        return fail(SOFI_E_ARG, "null argument");
+    if (!c->fwi)
+        return fail(SOFI_E_STATE, "sofi_fwi_begin first");
+    *interval = c->fwi_K, *segments = c->fwi_nseg;
+    return 0;
 }
 
 int sofi_fwi_gradients(sofi_ctx *c, float *lam, float *mu, float *rhos)

@@ -133,6 +133,12 @@ class TimeLoop:
         assert ax.shape == ay.shape == (self.ntr[0], self.cfg.nt)
         N.check(self.lib.sofi_fwi_backward(self.h, _fp(ax), _fp(ay)))
 
+    def fwi_checkpoints(self) -> tuple:
+        """(interval K, segments) of the pass's checkpoints (K = 0: whole store)."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        N.check(self.lib.sofi_fwi_checkpoints(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
     def fwi_gradients(self) -> tuple:
         """(gradLam_shot, gradMu_shot, gradRhos_shot), [NY][NX] float32."""
         out = [np.empty((self.cfg.ny, self.cfg.nx), dtype=np.float32) for _ in range(3)]

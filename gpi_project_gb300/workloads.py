@@ -109,6 +109,22 @@ def workload(name: str) -> dict:
         rec = (np.floor(xs / 1.0).astype(np.int32) + 1, np.full(100, 11, np.int32))
         nshots = 1
         return dict(name=name, par=dict(par, L=0), mats=mats, true_mats=true, src=src, rec=rec, nshots=nshots)
+    elif name == "fwi2":
+        # the gradient pass on a 4000 x 2000 EL_ISO grid, NT 4000: 640 GB of forward quantities, so the pass
+        # checkpoints (about 63 states of the wavefield and CPML memory) and recomputes each segment once
+        rng = np.random.default_rng(1007)
+        nx, ny = 4000, 2000
+        vp, vs, rho = layered(rng, nx, ny)
+        par = dict(weq=2, nx=nx, ny=ny, dh=1.0, dt=1e-4, nt=4000, fdorder=8, maxrelerror=1, fw=30, abs_type=1,
+                   npower=4.0, k_max_cpml=1.0, vppml=float(vp.max()), fpml=25.0, seismo=1, ndt=1)
+        mats = dict(vp=vp, vs=vs, rho=rho)
+        true = {k: v.copy() for k, v in mats.items()}
+        for k, f in (("vp", 1.05), ("vs", 1.05), ("rho", 1.03)):
+            true[k][1800:2200, 600:1000] *= np.float32(f)
+        src = _srcpos([(2000.0, 5.0)], 1.0, 25.0, 3)
+        xs = np.linspace(31.0, nx - 32.0, 1000)
+        rec = (np.floor(xs).astype(np.int32) + 1, np.full(1000, 11, np.int32))
+        return dict(name=name, par=dict(par, L=0), mats=mats, true_mats=true, src=src, rec=rec, nshots=1)
     elif name == "c2":
         rng = np.random.default_rng(1002)
         nx, ny = 4000, 2000

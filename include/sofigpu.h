@@ -215,11 +215,20 @@ int sofi_velocity_variant(sofi_ctx *ctx, int *cells_per_thread, int *rows_per_th
  *   the receivers, no other source, correlating every step with forward step
  *   NT - nt + 1. Synchronous. The sections then hold the backward run's.
  * sofi_fwi_gradients: gradLam_shot, gradMu_shot, gradRhos_shot ([NY][NX]);
- *   sofih_fwi_model_gradients turns them into the vp / vs / rho' gradients. */
+ *   sofih_fwi_model_gradients turns them into the vp / vs / rho' gradients.
+ * When NT steps of forward quantities do not fit the device, sofi_fwi_begin
+ * plans checkpoints instead (SOFI_FWI_CHECKPOINT=K forces an interval): the
+ * forward run keeps the wavefield and CPML memory after steps K, 2K, ...
+ * (about sqrt(NT) states), and sofi_fwi_backward recomputes each segment's
+ * forward steps from its checkpoint before the backward steps that read
+ * them -- one extra forward run, the same gradients bit for bit.
+ * sofi_fwi_checkpoints reports the interval (0: the whole run is stored) and
+ * the number of segments. */
 int sofi_fwi_begin(sofi_ctx *ctx, int velocity, int adjoint_type, const float *vp, const float *vs,
                    const float *rho);
 int sofi_fwi_backward(sofi_ctx *ctx, const float *adj_x, const float *adj_y);
 int sofi_fwi_gradients(sofi_ctx *ctx, float *grad_lam, float *grad_mu, float *grad_rhos);
+int sofi_fwi_checkpoints(sofi_ctx *ctx, int *interval, int *segments);
 
 /* The persistent step kernel: chunks of up to 128 time steps (until the next
  * snapshot or timed step) run as one cooperative launch whose blocks step

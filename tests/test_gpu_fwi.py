@@ -115,3 +115,20 @@ def test_cli_fwi_writes_the_reference_gradient_files(name, tmp_path):
             a = a.reshape(nx, ny).T
             ref = g[f"grad_{k}"]
             assert rel_l2(a, ref) <= GRAD_L2 and rel_max(a, ref) <= GRAD_MAX, (name, k, suffix, rel_l2(a, ref))
+
+
+@pytest.mark.parametrize("case", FWI_CASES, ids=[c["name"] for c in FWI_CASES])
+def test_gpu_fwi_checkpointed_equals_whole_store(case, monkeypatch):
+    """With checkpoints every K steps (the whole forward run does not fit the
+    store), each segment's forward steps are recomputed from its checkpoint
+    before the backward steps that read them: the same kernels on the same
+    state, so the gradients equal the whole-store pass bit for bit, for
+    segment lengths that divide NT and that do not."""
+    g = np.load(os.path.join(HERE, "golden", f"ref_{case['name']}.npz"))
+    monkeypatch.delenv("SOFI_FWI_CHECKPOINT", raising=False)
+    _, whole = gpu_fwi(case, g["obs_vx"], g["obs_vy"])
+    for k in ("7", "64", str(case["nt"])):
+        monkeypatch.setenv("SOFI_FWI_CHECKPOINT", k)
+        fwd, ck = gpu_fwi(case, g["obs_vx"], g["obs_vy"])
+        for name in ("vp", "vs", "rho"):
+            np.testing.assert_array_equal(ck[name], whole[name], err_msg=f"{case['name']} K={k} {name}")
