@@ -1,0 +1,7 @@
+// sofi_fused_vti_el.cu -- the fused velocity + stress step of VTI media, elastic.
+#include "sofi_fused.cuh"
+#include "sofi_launch.h"
+
+namespace sofi {
+template void launch_fused_kv<VTI, false>(const Geo &, const Wave &, const Wave &, const Model &, int, cudaStream_t);
+}

@@ -194,16 +194,14 @@ __device__ __forceinline__ void stv(float *p, const float *v)
 // memory (cpml_update.c), vx/vy update (wavefield_update_v.c / _ac.c),
 // damping frame (update_v_abs.c) and the store of the cells i + c <= NX.
 // ox/oy: the old velocities, rp/rq: the cells' rip / rjp.
-template <int VW, bool SXY>
-__device__ __forceinline__ void v_finish(const Geo &G, const Wave &W, const Model &M, int s, int i, int j, int o,
-                                         long long mo, float *__restrict__ vx, float *__restrict__ vy,
-                                         const float *ox, const float *oy, const float *rp, const float *rq,
-                                         const float *sxx_x, const float *sxy_x, const float *sxy_y,
-                                         const float *syy_y)
+template <int VW, bool SXY, bool FWI = false>
+__device__ __forceinline__ void v_compute(const Geo &G, const Wave &Wr, const Wave &Ww, const Model &M, int s, int i,
+                                          int j, int o, long long mo, const float *ox, const float *oy,
+                                          const float *rp, const float *rq, const float *sxx_x, const float *sxy_x,
+                                          const float *sxy_y, const float *syy_y, float *nvx, float *nvy, bool own)
 {
     const int yr = yside(G, j);
     const bool xframe = i <= G.gx2 || i + VW - 1 > G.gx3;  // any of the cells in a left/right frame
-    float nvx[VW], nvy[VW];
 #pragma unroll
     for (int c = 0; c < VW; c++) {
         const int ic = i + c;
@@ -213,32 +211,36 @@ __device__ __forceinline__ void v_finish(const Geo &G, const Wave &W, const Mode
             if (xr) {
                 int h = xr == 1 ? ic : ic - G.nx + G.fw2;
                 long long q = ((long long)s * G.ny + (j - 1)) * G.fw2 + (h - 1);
-                float ps = M.b_x_half[h - 1] * W.psi_sxx_x[q] + M.a_x_half[h - 1] * fx;
-                W.psi_sxx_x[q] = ps;
+                float ps = M.b_x_half[h - 1] * Wr.psi_sxx_x[q] + M.a_x_half[h - 1] * fx;
+                if (own)
+                    Ww.psi_sxx_x[q] = ps;
                 fx = fx / M.K_x_half[h - 1] + ps;
                 if (SXY) {
-                    float py = M.b_x[h - 1] * W.psi_sxy_x[q] + M.a_x[h - 1] * fxy;
-                    W.psi_sxy_x[q] = py;
+                    float py = M.b_x[h - 1] * Wr.psi_sxy_x[q] + M.a_x[h - 1] * fxy;
+                    if (own)
+                        Ww.psi_sxy_x[q] = py;
                     fxy = fxy / M.K_x[h - 1] + py;
                 }
             }
             if (yr) {
                 int h = yr == 1 ? j : j - G.ny + G.fw2;
                 long long q = ((long long)s * G.fw2 + (h - 1)) * G.nx + (ic - 1);
-                float ps = M.b_y_half[h - 1] * W.psi_syy_y[q] + M.a_y_half[h - 1] * fy;
-                W.psi_syy_y[q] = ps;
+                float ps = M.b_y_half[h - 1] * Wr.psi_syy_y[q] + M.a_y_half[h - 1] * fy;
+                if (own)
+                    Ww.psi_syy_y[q] = ps;
                 fy = fy / M.K_y_half[h - 1] + ps;
                 if (SXY) {
-                    float py = M.b_y[h - 1] * W.psi_sxy_y[q] + M.a_y[h - 1] * fyx;
-                    W.psi_sxy_y[q] = py;
+                    float py = M.b_y[h - 1] * Wr.psi_sxy_y[q] + M.a_y[h - 1] * fyx;
+                    if (own)
+                        Ww.psi_sxy_y[q] = py;
                     fyx = fyx / M.K_y[h - 1] + py;
                 }
             }
         }
         if (SXY) {
-            if (W.fa_x && ic <= G.nx) {
-                W.fa_x[(long long)s * G.fsz + o + c] = rp[c] * (fx + fyx) / G.dh;
-                W.fa_y[(long long)s * G.fsz + o + c] = rq[c] * (fxy + fy) / G.dh;
+            if (FWI && own && ic <= G.nx) {
+                Ww.fa_x[(long long)s * G.fsz + o + c] = rp[c] * (fx + fyx) / G.dh;
+                Ww.fa_y[(long long)s * G.fsz + o + c] = rq[c] * (fxy + fy) / G.dh;
             }
             nvx[c] = ox[c] + (fx + fyx) * G.dtdh * rp[c];
             nvy[c] = oy[c] + (fxy + fy) * G.dtdh * rq[c];
@@ -252,6 +254,17 @@ __device__ __forceinline__ void v_finish(const Geo &G, const Wave &W, const Mode
             nvy[c] *= a;
         }
     }
+}
+
+template <int VW, bool SXY, bool FWI = false>
+__device__ __forceinline__ void v_finish(const Geo &G, const Wave &W, const Model &M, int s, int i, int j, int o,
+                                         long long mo, float *__restrict__ vx, float *__restrict__ vy,
+                                         const float *ox, const float *oy, const float *rp, const float *rq,
+                                         const float *sxx_x, const float *sxy_x, const float *sxy_y,
+                                         const float *syy_y)
+{
+    float nvx[VW], nvy[VW];
+    v_compute<VW, SXY, FWI>(G, W, W, M, s, i, j, o, mo, ox, oy, rp, rq, sxx_x, sxy_x, sxy_y, syy_y, nvx, nvy, true);
     if (i + VW - 1 <= G.nx) {
         stv<VW>(vx + o, nvx);
         stv<VW>(vy + o, nvy);
@@ -263,10 +276,69 @@ __device__ __forceinline__ void v_finish(const Geo &G, const Wave &W, const Mode
     }
 }
 
+// The stress derivatives of VW adjacent cells for the velocity update
+// (op_v_fdN, initfd.c:97-183, unscaled): ld(f, dy, dx, out) loads VW values
+// of sxx (f = 0), sxy (1) or syy (2) at row j + dy, columns i + dx ..
+// i + dx + VW - 1. The fused step kernel uses it; vw_tile writes the same
+// expressions out inline (through a loader they cost the 64-register
+// four-cell kernel a spill).
+template <int ND, int VW, bool SXY, class LD>
+__device__ __forceinline__ void v_derivs(const Geo &G, LD ld, float *sxx_x, float *sxy_x, float *sxy_y, float *syy_y)
+{
+    constexpr int K = (ND + VW - 1) / VW;
+    constexpr int NXS = VW * (2 * K + 1);  // stencil row: columns i - VW K .. i + VW K + VW - 1
+    const float *hc = G.hc;
+    {
+        float X[NXS], Y[NXS];  // X[k] = sxx(j, i - VW K + k), Y[k] = sxy(j, i - VW K + k)
+#pragma unroll
+        for (int q = 0; q < 2 * K + 1; q++) {
+            ld(0, 0, VW * (q - K), X + VW * q);
+            if (SXY)
+                ld(1, 0, VW * (q - K), Y + VW * q);
+        }
+        constexpr int C = VW * K;  // index of column i
+#pragma unroll
+        for (int c = 0; c < VW; c++) {
+            sxx_x[c] = hc[1] * (X[C + c + 1] - X[C + c]);
+            sxy_x[c] = SXY ? hc[1] * (Y[C + c] - Y[C + c - 1]) : 0.f;
+#pragma unroll
+            for (int m = 2; m <= ND; m++) {
+                sxx_x[c] += hc[m] * (X[C + c + m] - X[C + c - m + 1]);
+                if (SXY)
+                    sxy_x[c] += hc[m] * (Y[C + c + m - 1] - Y[C + c - m]);
+            }
+        }
+    }
+    {
+        // y stencils: sxy rows j - ND .. j + ND - 1, syy rows j - ND + 1 .. j + ND
+        float a1[VW], a0[VW], b1[VW], b0[VW];
+        if (SXY)
+            ld(1, 0, 0, a1), ld(1, -1, 0, a0);
+        ld(2, 1, 0, b1), ld(2, 0, 0, b0);
+#pragma unroll
+        for (int c = 0; c < VW; c++) {
+            sxy_y[c] = SXY ? hc[1] * (a1[c] - a0[c]) : 0.f;
+            syy_y[c] = hc[1] * (b1[c] - b0[c]);
+        }
+#pragma unroll
+        for (int m = 2; m <= ND; m++) {
+            if (SXY)
+                ld(1, m - 1, 0, a1), ld(1, -m, 0, a0);
+            ld(2, m, 0, b1), ld(2, -(m - 1), 0, b0);
+#pragma unroll
+            for (int c = 0; c < VW; c++) {
+                if (SXY)
+                    sxy_y[c] += hc[m] * (a1[c] - a0[c]);
+                syy_y[c] += hc[m] * (b1[c] - b0[c]);
+            }
+        }
+    }
+}
+
 // SXY = false: the acoustic update (wavefield_update_v_ac.c), which has no
 // sxy: vx += sxx_x * DT/DH * rip, vy += syy_y * DT/DH * rjp (sxx and syy are
 // one pressure array); VW may then also be 1.
-template <int ND, int VW, bool SXY, bool COH>
+template <int ND, int VW, bool SXY, bool COH, bool FWI = false>
 __device__ __forceinline__ void vw_tile(const Geo &G, const Wave &W, const Model &M, const uint3 b)
 {
     constexpr int K = (ND + VW - 1) / VW;
@@ -337,13 +409,16 @@ __device__ __forceinline__ void vw_tile(const Geo &G, const Wave &W, const Model
     float ox[VW], oy[VW], rp[VW], rq[VW];
     ldv_rw<VW>(vx + o, ox), ldv_rw<VW>(vy + o, oy);
     ldv<VW>(M.prip + mo + o, rp), ldv<VW>(M.prjp + mo + o, rq);
-    v_finish<VW, SXY>(G, W, M, s, i, j, o, mo, vx, vy, ox, oy, rp, rq, sxx_x, sxy_x, sxy_y, syy_y);
+    v_finish<VW, SXY, FWI>(G, W, M, s, i, j, o, mo, vx, vy, ox, oy, rp, rq, sxx_x, sxy_x, sxy_y, syy_y);
 }
 
-template <int ND, int VW, bool SXY = true>
+// FWI: the forward run of an FWI gradient pass also writes the gradient
+// quantities (Wave::fa_x / fa_y); a separate instantiation, so that the plain
+// kernels carry no trace of it
+template <int ND, int VW, bool SXY = true, bool FWI = false>
 __global__ void __launch_bounds__(BX *BY, VW == 4 ? 4 : 1) k_update_vw(Geo G, Wave W, Model M)
 {
-    vw_tile<ND, VW, SXY, false>(G, W, M, blockIdx);
+    vw_tile<ND, VW, SXY, false, FWI>(G, W, M, blockIdx);
 }
 
 // Periodic x (BOUNDARY = 1): ghost columns copy the opposite edge, as the one-
@@ -489,33 +564,23 @@ __global__ void __launch_bounds__(BX *BY) k_update_s(Geo G, Wave W, Model M)
 // (x) and one vector per row (y), model, memory variables and stresses as
 // vectors; per cell the arithmetic of k_update_s, term by term. Reads past
 // column NX + ND feed only cells past NX, which are never stored.
-template <int ND, int KIND, bool VISCO, int LT, int VW, bool COH>
-__device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model &M, const uint3 b)
+// The velocity derivatives of VW adjacent cells for the stress update
+// (op_s_fdN, initfd.c:9-95, times 1/DH): ld(f, dy, dx, out) loads VW values
+// of vx (f = 0) or vy (f = 1) at row j + dy, columns i + dx .. i + dx + VW - 1,
+// from global memory in the stress kernels, from shared memory in the fused
+// step kernel.
+template <int ND, int VW, class LD>
+__device__ __forceinline__ void s_derivs(const Geo &G, LD ld, float *vxx, float *vyx, float *vxy, float *vyy)
 {
     constexpr int K = (ND + VW - 1) / VW;
     constexpr int NXS = VW * (2 * K + 1);
-    int bx, s;
-    block_xs(G, b, bx, s);
-    const int i = (bx * BX + threadIdx.x) * VW + 1;
-    const int j = b.y * BY + threadIdx.y + 1;
-    if (i > G.nx || j > G.ny)
-        return;
-    const int P = G.pitch;
-    const int o = (j - 1 + HY) * P + (i - 1 + HX);
-    const long long so = (long long)s * G.fsz, mo = moff(G, s);
-    float *__restrict__ sxx = W.sxx + so;
-    float *__restrict__ syy = W.syy + so;
-    float *__restrict__ sxy = W.sxy + so;
-    const float *__restrict__ vx = W.vx + so;
-    const float *__restrict__ vy = W.vy + so;
     const float *hc = G.hc;
-    float vxx[VW], vyx[VW], vxy[VW], vyy[VW];
     {
         float X[NXS], Y[NXS];  // X[k] = vx(j, i - VW K + k), Y[k] = vy(j, i - VW K + k)
 #pragma unroll
         for (int q = 0; q < 2 * K + 1; q++) {
-            ldv<VW, COH>(vx + o + VW * (q - K), X + VW * q);
-            ldv<VW, COH>(vy + o + VW * (q - K), Y + VW * q);
+            ld(0, 0, VW * (q - K), X + VW * q);
+            ld(1, 0, VW * (q - K), Y + VW * q);
         }
         constexpr int C = VW * K;
 #pragma unroll
@@ -532,8 +597,8 @@ __device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model
     {
         // y stencils: vx rows j - ND + 1 .. j + ND, vy rows j - ND .. j + ND - 1
         float a1[VW], a0[VW], b1[VW], b0[VW];
-        ldv<VW, COH>(vx + o + P, a1), ldv<VW, COH>(vx + o, a0);
-        ldv<VW, COH>(vy + o, b1), ldv<VW, COH>(vy + o - P, b0);
+        ld(0, 1, 0, a1), ld(0, 0, 0, a0);
+        ld(1, 0, 0, b1), ld(1, -1, 0, b0);
 #pragma unroll
         for (int c = 0; c < VW; c++) {
             vxy[c] = hc[1] * (a1[c] - a0[c]);
@@ -541,8 +606,8 @@ __device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model
         }
 #pragma unroll
         for (int m = 2; m <= ND; m++) {
-            ldv<VW, COH>(vx + o + m * P, a1), ldv<VW, COH>(vx + o - (m - 1) * P, a0);
-            ldv<VW, COH>(vy + o + (m - 1) * P, b1), ldv<VW, COH>(vy + o - m * P, b0);
+            ld(0, m, 0, a1), ld(0, -(m - 1), 0, a0);
+            ld(1, m - 1, 0, b1), ld(1, -m, 0, b0);
 #pragma unroll
             for (int c = 0; c < VW; c++) {
                 vxy[c] += hc[m] * (a1[c] - a0[c]);
@@ -553,6 +618,22 @@ __device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model
         for (int c = 0; c < VW; c++)
             vxx[c] *= G.dhi, vyx[c] *= G.dhi, vxy[c] *= G.dhi, vyy[c] *= G.dhi;
     }
+}
+
+// The stress and memory-variable update of VW adjacent cells (columns
+// i .. i+VW-1, row j, padded offset o) from their velocity derivatives: CPML
+// of the derivatives, isotropic / VTI stresses, L memory variables, damping
+// frame; old stresses from Wr, new ones to Ww (the same arrays except in the
+// fused step kernel), memory variables and CPML memory in place.
+template <int ND, int KIND, bool VISCO, int LT, int VW, bool FWI = false>
+__device__ __forceinline__ void s_update(const Geo &G, const Wave &Wr, const Wave &Ww, const Model &M, int s, int i,
+                                         int j, int o, long long mo, float *vxx, float *vyx, float *vxy, float *vyy)
+{
+    const long long so = (long long)s * G.fsz;
+    // old and new stresses are the same arrays outside the fused step kernel: no restrict here
+    const float *sxx_o = Wr.sxx + so, *syy_o = Wr.syy + so, *sxy_o = Wr.sxy + so;
+    float *sxx = Ww.sxx + so, *syy = Ww.syy + so, *sxy = Ww.sxy + so;
+    const Wave &W = Wr;
     float m0[VW], m1[VW], m2[VW], m3[VW], b0[VW], b1[VW], b2[VW], b3[VW];
 #pragma unroll
     for (int c = 0; c < VW; c++)
@@ -584,7 +665,7 @@ __device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model
             }
     }
     float oxx[VW], oyy[VW], oxy[VW];
-    ldv_rw<VW>(sxx + o, oxx), ldv_rw<VW>(syy + o, oyy), ldv_rw<VW>(sxy + o, oxy);
+    ldv_rw<VW>(sxx_o + o, oxx), ldv_rw<VW>(syy_o + o, oyy), ldv_rw<VW>(sxy_o + o, oxy);
     const int yr = yside(G, j);
     const bool xframe = i <= G.gx2 || i + VW - 1 > G.gx3;
     float nxx[VW], nyy[VW], nxy[VW];
@@ -601,7 +682,7 @@ __device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model
             float gd = m0[c] * (dxx + dyy);
             u2 = gd - 2.0f * m1[c] * dyy;
             u3 = gd - 2.0f * m1[c] * dxx;
-            if (!VISCO && W.fu_x && ic <= G.nx) {
+            if (FWI && !VISCO && ic <= G.nx) {
                 const long long q = (long long)s * G.fsz + o + c;
                 W.fu_xy[q] = u1 / G.dt, W.fu_x[q] = u2 / G.dt, W.fu_y[q] = u3 / G.dt;
             }
@@ -670,10 +751,31 @@ __device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model
     }
 }
 
-template <int ND, int KIND, bool VISCO, int LT, int VW>
+template <int ND, int KIND, bool VISCO, int LT, int VW, bool COH, bool FWI = false>
+__device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model &M, const uint3 b)
+{
+    int bx, s;
+    block_xs(G, b, bx, s);
+    const int i = (bx * BX + threadIdx.x) * VW + 1;
+    const int j = b.y * BY + threadIdx.y + 1;
+    if (i > G.nx || j > G.ny)
+        return;
+    const int P = G.pitch;
+    const int o = (j - 1 + HY) * P + (i - 1 + HX);
+    const long long so = (long long)s * G.fsz, mo = moff(G, s);
+    const float *__restrict__ vx = W.vx + so;
+    const float *__restrict__ vy = W.vy + so;
+    float vxx[VW], vyx[VW], vxy[VW], vyy[VW];
+    s_derivs<ND, VW>(
+        G, [&](int f, int dy, int dx, float *out) { ldv<VW, COH>((f ? vy : vx) + o + dy * P + dx, out); }, vxx, vyx,
+        vxy, vyy);
+    s_update<ND, KIND, VISCO, LT, VW, FWI>(G, W, W, M, s, i, j, o, mo, vxx, vyx, vxy, vyy);
+}
+
+template <int ND, int KIND, bool VISCO, int LT, int VW, bool FWI = false>
 __global__ void __launch_bounds__(BX *BY, VW == 4 ? 2 : 1) k_update_sw(Geo G, Wave W, Model M)
 {
-    sw_tile<ND, KIND, VISCO, LT, VW, false>(G, W, M, blockIdx);
+    sw_tile<ND, KIND, VISCO, LT, VW, false, FWI>(G, W, M, blockIdx);
 }
 
 // Acoustic stress update (wavefield_update_s_ac.c, update_s_acoustic_{interior,

@@ -23,6 +23,10 @@ void launch_fwi_conv(const Geo &G, const Wave &W, const Model &M, const FwiDev &
 // fit the GPU at once, and a cooperative launch of `blocks` of them.
 template <int KIND, bool VISCO>
 int persist_capacity_kv(int nd, int L, int device);
+// The fused velocity + stress step (sofi_fused.cuh, ISO / VTI): reads the
+// current buffers Wc, writes v, s and the velocity CPML memory to Wn.
+template <int KIND, bool VISCO>
+void launch_fused_kv(const Geo &G, const Wave &Wc, const Wave &Wn, const Model &M, int nd, cudaStream_t st);
 template <int KIND, bool VISCO>
 cudaError_t launch_persist_kv(const Geo &G, const Wave &W, const Model &M, const Acq &A, int nd,
                               const PersistArgs &P, int blocks, cudaStream_t st);

@@ -1,0 +1,9 @@
+// sofi_persist_iso_el.cu -- the persistent step kernel of ISO media, elastic.
+#include "sofi_launch.h"
+#include "sofi_persist.cuh"
+
+namespace sofi {
+template int persist_capacity_kv<ISO, false>(int, int, int);
+template cudaError_t launch_persist_kv<ISO, false>(const Geo &, const Wave &, const Model &, const Acq &, int,
+                                                   const PersistArgs &, int, cudaStream_t);
+}

@@ -2,7 +2,6 @@
 #include "sofi_dispatch.cuh"
 #include "sofi_kernels.cuh"
 #include "sofi_launch.h"
-#include "sofi_persist.cuh"
 
 namespace sofi {
 
@@ -16,9 +15,5 @@ void launch_stress_ac(const Geo &G, const Wave &W, const Model &M, int nd, int s
     else
         DISPATCH_ND(nd, (k_update_s_ac<ND, 1><<<grd, blk, 0, st>>>(G, W, M)))
 }
-
-template int persist_capacity_kv<AC, false>(int, int, int);
-template cudaError_t launch_persist_kv<AC, false>(const Geo &, const Wave &, const Model &, const Acq &, int,
-                                                 const PersistArgs &, int, cudaStream_t);
 
 }  // namespace sofi

@@ -1,10 +1,6 @@
 // sofi_stress_vti_el.cu -- stress kernels of VTI media, VISCO = false.
-#include "sofi_persist.cuh"
 #include "sofi_stress.cuh"
 
 namespace sofi {
 template void launch_stress_kv<VTI, false>(const Geo &, const Wave &, const Model &, int, int, dim3, cudaStream_t);
-template int persist_capacity_kv<VTI, false>(int, int, int);
-template cudaError_t launch_persist_kv<VTI, false>(const Geo &, const Wave &, const Model &, const Acq &, int,
-                                                   const PersistArgs &, int, cudaStream_t);
 }

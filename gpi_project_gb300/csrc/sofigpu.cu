@@ -222,8 +222,18 @@ struct sofi_ctx {
     // snapshot or timed steps (the step number lives in G.step_ctr)
     bool use_graph = true;
     bool graph_dirty = true;
-    cudaGraphExec_t graph_exec = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;   // the step graph (fused mode: current buffers are the first set)
+    cudaGraphExec_t graph_exec1 = nullptr;  // fused mode, current buffers the second set
+    bool graph_ok[2] = {false, false};
     long long graph_launches = 0;  // kernels per replay
+    // fused velocity + stress step (sofi_fused.cuh): v, s and the velocity CPML
+    // memory held twice; W is always the current set, W2 the other, swapped
+    // after every fused launch; parity says which allocation W holds
+    bool fused = false;
+    bool fused_fixed = false;  // SOFI_FUSED chose it
+    bool w2_ready = false;
+    Wave W2{};
+    int parity = 0;
     int march_sy = 32;         // rows per block of the y-marching kernels
     bool tti_split = false;    // TTI: derivative fields through HBM (two kernels) instead of fused
     // snapshots
@@ -240,6 +250,16 @@ struct sofi_ctx {
     std::deque<cudaEvent_t> run_ev;
     std::vector<cudaEvent_t> ev_free;
 };
+
+static void drop_graphs(sofi_ctx *c)
+{
+    for (cudaGraphExec_t *g : {&c->graph_exec, &c->graph_exec1})
+        if (*g) {
+            cudaGraphExecDestroy(*g);
+            *g = nullptr;
+        }
+    c->graph_ok[0] = c->graph_ok[1] = false;
+}
 
 namespace {
 
@@ -276,6 +296,12 @@ int count_snapshots(const sofi_config &c)
     return n;
 }
 
+bool fused_env_on()
+{
+    const char *e = getenv("SOFI_FUSED");
+    return e && atoi(e) != 0;
+}
+
 long long fields_bytes(const sofi_config &c)
 {
     long long pitch = pitch_for(c.nx), fsz = pitch * (c.ny + 2 * HY);
@@ -292,6 +318,10 @@ long long fields_bytes(const sofi_config &c)
     long long psi = (c.abs_type == 1 && c.fw > 0) ? (tti && !split ? 6 : 4) * ((long long)c.ny * fw2 + fw2 * c.nx) : 0;
     long long nmod = c.shared_model ? 1 : c.nshots;
     long long nfields = (long long)needed_fields(c).size();
+    // the fused step (opt-in, SOFI_FUSED=1 / sofi_set_fused) holds v, s and the
+    // velocity CPML memory twice
+    if (fused_env_on() && (kind_of(c.weq) == ISO || kind_of(c.weq) == VTI) && !ab && !c.boundary)
+        per_shot += 5, psi += psi / 2;
     long long bytes = 4 * (fsz * per_shot * c.nshots + psi * c.nshots + fsz * nfields * nmod);
     int nsnap = count_snapshots(c);
     if (nsnap) {
@@ -490,6 +520,19 @@ void launch_cell_s(const Geo &G, const Wave &W, const Model &M, int nd, int kind
         visco ? launch_stress_kv<VTI, true>(G, W, M, nd, sw, grd, st) : launch_stress_kv<VTI, false>(G, W, M, nd, sw, grd, st);
 }
 
+// The wave fields a step's kernels get: the gradient quantities of an FWI
+// pass (Wave::fa_* / fu_*) only on its forward steps, so that the backward
+// steps and every run outside a pass use the kernels that do not write them.
+// All forward steps, stored or not, run the same kernels: a segment
+// recomputed from a checkpoint then repeats the first run's arithmetic.
+Wave step_wave(const sofi_ctx *c)
+{
+    Wave W = c->W;
+    if (!c->fwi || c->fwi_back)
+        W.fa_x = W.fa_y = W.fu_x = W.fu_y = W.fu_xy = nullptr;
+    return W;
+}
+
 // One time step. `capture`: being recorded into the step graph, so no host-
 // side step number exists (no timing events, no snapshot).
 // The velocity kernel in the context's variant: c->vw cells per thread in x
@@ -512,7 +555,54 @@ void launch_v(sofi_ctx *c, const Geo &G, cudaStream_t st)
     const int R = (vw || ac) ? 1 : c->vrows, cx = vw ? vw : 1;
     const unsigned tx = (cf.nx + cx * BX - 1) / (cx * BX), ty = (cf.ny + BY * R - 1) / (BY * R);
     const dim3 gv = G.shot_fast ? dim3(tx * S, ty, 1) : dim3(tx, ty, S);
-    launch_velocity(G, c->W, c->M, c->nd, vw, R, ac, gv, st);
+    launch_velocity(G, step_wave(c), c->M, c->nd, vw, R, ac, gv, st);
+}
+
+// The fused step applies to ISO / VTI media with second-order time stepping,
+// no periodic edge and none of the other step forms (y-marching, persistent,
+// FWI pass).
+static bool fused_applies(const sofi_ctx *c)
+{
+    const int kind = kind_of(c->cfg.weq);
+    return (kind == ISO || kind == VTI) && !c->G.ab4 && !c->cfg.boundary && !c->march && !c->persist && !c->fwi;
+}
+
+// The second buffer set: v, s and the velocity CPML memory of every shot.
+static int alloc_w2(sofi_ctx *c)
+{
+    if (c->w2_ready)
+        return 0;
+    Wave W2 = c->W;
+    const size_t f = (size_t)c->G.fsz * c->cfg.nshots * sizeof(float);
+    int rc;
+    for (float **p : {&W2.vx, &W2.vy, &W2.sxx, &W2.syy, &W2.sxy})
+        if ((rc = dalloc(c, (void **)p, f)))
+            return rc;
+    if (c->G.abs_type == 1) {
+        const size_t px = sizeof(float) * (size_t)c->cfg.nshots * c->cfg.ny * c->G.fw2;
+        const size_t py = sizeof(float) * (size_t)c->cfg.nshots * c->G.fw2 * c->cfg.nx;
+        for (float **p : {&W2.psi_sxx_x, &W2.psi_sxy_x})
+            if ((rc = dalloc(c, (void **)p, px)))
+                return rc;
+        for (float **p : {&W2.psi_syy_y, &W2.psi_sxy_y})
+            if ((rc = dalloc(c, (void **)p, py)))
+                return rc;
+    }
+    c->W2 = W2;
+    c->w2_ready = true;
+    return 0;
+}
+
+static void launch_fused(sofi_ctx *c, const Geo &G, cudaStream_t st)
+{
+    const int kind = kind_of(c->cfg.weq);
+    const bool visco = is_visco(c->cfg.weq);
+    if (kind == ISO)
+        visco ? launch_fused_kv<ISO, true>(G, c->W, c->W2, c->M, c->nd, st)
+              : launch_fused_kv<ISO, false>(G, c->W, c->W2, c->M, c->nd, st);
+    else
+        visco ? launch_fused_kv<VTI, true>(G, c->W, c->W2, c->M, c->nd, st)
+              : launch_fused_kv<VTI, false>(G, c->W, c->W2, c->M, c->nd, st);
 }
 
 // Autotuner of the velocity and (ISO / VTI) stress kernels. Which variant is
@@ -524,7 +614,7 @@ void launch_v(sofi_ctx *c, const Geo &G, cudaStream_t st)
 // the process. SOFI_VROWS / SOFI_SW fix a choice.
 struct Tuned {
     int vw, vrows, sw;
-    bool vpipe;
+    bool vpipe, fused;
 };
 std::mutex g_tune_mu;
 std::map<std::string, Tuned> g_tune;
@@ -584,7 +674,7 @@ int autotune(sofi_ctx *c)
         return 0;  // state not known to be zero: keep the default variants
     Geo G = c->G;
     G.step_ctr = nullptr;  // tuning launches are not steps
-    Tuned pick{c->vw, c->vrows, c->sw, c->vpipe};
+    Tuned pick{c->vw, c->vrows, c->sw, c->vpipe, false};
     float best = 1e30f, ms = 0.f;
     int rc;
     // two interleaved rounds over the candidates, each candidate's best time:
@@ -628,7 +718,7 @@ int autotune(sofi_ctx *c)
     }
     c->graph_dirty = true;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune[key] = Tuned{c->vw, c->vrows, c->sw, c->vpipe};
+    g_tune[key] = Tuned{c->vw, c->vrows, c->sw, c->vpipe, c->fused};
     return 0;
 }
 
@@ -713,7 +803,7 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
     const sofi_config &cf = c->cfg;
     cudaStream_t st = c->stream;
     Geo &G = c->G;
-    dim3 blk(BX, BY), grd = grid2d(c);
+    dim3 grd = grid2d(c);
     int S = cf.nshots;
     int nb = (S + 127) / 128;
     int kind = kind_of(cf.weq);
@@ -744,6 +834,17 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
         c->tev_used += 3;
         CK(cudaEventRecord(e0, st));
     }
+    if (c->fused) {  // velocity and stress in one kernel (timed as the stress update); then the next buffers are current
+        if (timed)
+            CK(cudaEventRecord(e1, st));
+        launch_fused(c, G, st);
+        std::swap(c->W, c->W2);
+        c->parity ^= 1;
+        c->launches++;
+        if (timed)
+            CK(cudaEventRecord(e2, st));
+        goto post;
+    }
     if (G.ab4)
         launch_ab4_v(G, c->W, c->M, c->nd, grd, st);
     else
@@ -767,11 +868,12 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
     } else if (c->march && kind != AC) {
         launch_march_s(G, c->W, c->M, c->nd, kind, visco, c->march_sy, st);
     } else {
-        launch_cell_s(G, c->W, c->M, c->nd, kind, visco, c->persist ? 4 : c->sw, cf.nx, cf.ny, S, st);
+        launch_cell_s(G, step_wave(c), c->M, c->nd, kind, visco, c->persist ? 4 : c->sw, cf.nx, cf.ny, S, st);
     }
     c->launches++;
     if (timed)
         CK(cudaEventRecord(e2, st));
+post:
     dim3 pg((cf.nx + 127) / 128, S);
     if (kind == TTI)
         DISPATCH_ND(c->nd, (k_post<ND, false, true><<<pg, 128, 0, st>>>(G, c->W, c->M, c->A)))
@@ -1078,6 +1180,15 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
             }
     }
     plan_persist(c);
+    // SOFI_FUSED=0|1: the fused velocity + stress step off / on (where it applies)
+    if (const char *e = getenv("SOFI_FUSED")) {
+        c->fused_fixed = true;
+        if (atoi(e) != 0 && fused_applies(c)) {
+            if ((rc = alloc_w2(c)))
+                goto bad;
+            c->fused = true;
+        }
+    }
     c->snap_total = count_snapshots(*cfg);
     if (c->snap_total) {
         c->snap_nx = (cfg->nx - 1) / cfg->idx + 1;
@@ -1116,8 +1227,7 @@ int sofi_destroy(sofi_ctx *c)
         cudaEventDestroy(e);
     for (auto e : c->ev_free)
         cudaEventDestroy(e);
-    if (c->graph_exec)
-        cudaGraphExecDestroy(c->graph_exec);
+    drop_graphs(c);
     if (c->ev0)
         cudaEventDestroy(c->ev0);
     if (c->ev1)
@@ -1293,11 +1403,15 @@ static bool chunk_has_event(const sofi_ctx *c, int first, int n)
     return false;
 }
 
+// Graph of kGraphSteps steps from the current buffer parity (an even number of
+// steps: the fused mode's swaps leave the parity where the capture began).
 static int build_graph(sofi_ctx *c)
 {
-    if (c->graph_exec) {
-        cudaGraphExecDestroy(c->graph_exec);
-        c->graph_exec = nullptr;
+    const int slot = c->fused ? c->parity : 0;
+    cudaGraphExec_t &gx = slot ? c->graph_exec1 : c->graph_exec;
+    if (gx) {
+        cudaGraphExecDestroy(gx);
+        gx = nullptr;
     }
     long long before = c->launches;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
@@ -1310,13 +1424,13 @@ static int build_graph(sofi_ctx *c)
         return rc;
     if (e != cudaSuccess)
         return fail(SOFI_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&c->graph_exec, graph, 0);
+    e = cudaGraphInstantiate(&gx, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess)
         return fail(SOFI_E_CUDA, "graph instantiation: %s", cudaGetErrorString(e));
     c->graph_launches = c->launches - before;
     c->launches = before;
-    c->graph_dirty = false;
+    c->graph_ok[slot] = true;
     return 0;
 }
 
@@ -1362,12 +1476,17 @@ int sofi_run(sofi_ctx *c, int nsteps)
         }
         const int lim = ckpt_fwd ? std::min(left, c->fwi_K - c->step % c->fwi_K) : left;
         if (c->use_graph && lim >= kGraphSteps && !chunk_has_event(c, c->step + 1, kGraphSteps)) {
-            if (c->graph_dirty || !c->graph_exec) {
+            if (c->graph_dirty) {
+                drop_graphs(c);
+                c->graph_dirty = false;
+            }
+            const int slot = c->fused ? c->parity : 0;
+            if (!c->graph_ok[slot]) {
                 int rc = build_graph(c);
                 if (rc)
                     return rc;
             }
-            CK(cudaGraphLaunch(c->graph_exec, c->stream));
+            CK(cudaGraphLaunch(slot ? c->graph_exec1 : c->graph_exec, c->stream));
             c->launches += c->graph_launches;
             c->step += kGraphSteps;
             left -= kGraphSteps;
@@ -1614,7 +1733,7 @@ int sofi_fwi_begin(sofi_ctx *c, int velocity, int adjoint_type, const float *vp,
     CK(cudaStreamSynchronize(c->stream));
     c->F.nt = cf.nt, c->F.velocity = velocity, c->F.adjoint = adjoint_type;
     // the kernels whose bodies write the gradient quantities, fixed for the pass
-    c->vw = 4, c->vrows = 1, c->vpipe = false, c->sw = 4, c->persist = false, c->tuned = true;
+    c->vw = 4, c->vrows = 1, c->vpipe = false, c->sw = 4, c->persist = false, c->fused = false, c->tuned = true;
     c->fwi = true, c->fwi_back = false, c->graph_dirty = true;
     return 0;
 }
@@ -1747,6 +1866,33 @@ int sofi_fwi_gradients(sofi_ctx *c, float *lam, float *mu, float *rhos)
     return 0;
 }
 
+int sofi_fused(sofi_ctx *c, int *on)
+{
+    if (!c || !on)
+        return fail(SOFI_E_ARG, "null argument");
+    *on = c->fused ? 1 : 0;
+    return 0;
+}
+
+int sofi_set_fused(sofi_ctx *c, int on)
+{
+    if (!c)
+        return fail(SOFI_E_ARG, "null context");
+    if (on && !fused_applies(c))
+        return fail(SOFI_E_STATE, "no fused step for this configuration");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    if (on) {
+        int rc = alloc_w2(c);
+        if (rc)
+            return rc;
+    }
+    c->fused = on != 0;
+    c->fused_fixed = true;
+    c->graph_dirty = true;
+    return 0;
+}
+
 int sofi_set_persistent(sofi_ctx *c, int on)
 {
     if (!c)
@@ -1757,6 +1903,8 @@ int sofi_set_persistent(sofi_ctx *c, int on)
         return fail(SOFI_E_STATE, "the FWI gradient pass runs the plain kernels");
     CK(cudaStreamSynchronize(c->stream));
     c->persist = on != 0;
+    if (c->persist)
+        c->fused = false;
     c->graph_dirty = true;
     return 0;
 }
@@ -1987,7 +2135,7 @@ int sofi_tti_stress_noalloc(const sofi_config *cfg, const sofi_tti_stress_args *
     for (int l = 0; l < G.L; l++)
         M.bip[l] = a->bip[l], M.cip[l] = a->cip[l], M.peta[l] = a->peta[l];
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    dim3 blk(BX, BY), grd((cfg->nx + BX - 1) / BX, (cfg->ny + BY - 1) / BY, 1);
+    dim3 grd((cfg->nx + BX - 1) / BX, (cfg->ny + BY - 1) / BY, 1);
     launch_tti_split(G, W, M, cfg->fdorder / 2, visco, grd, st);
     CK(cudaGetLastError());
     return 0;

@@ -145,6 +145,15 @@ class TimeLoop:
         N.check(self.lib.sofi_fwi_gradients(self.h, *[_fp(a) for a in out]))
         return tuple(out)
 
+    def fused(self) -> bool:
+        """Whether the fused velocity + stress step is in use."""
+        a = ctypes.c_int()
+        N.check(self.lib.sofi_fused(self.h, ctypes.byref(a)))
+        return bool(a.value)
+
+    def set_fused(self, on: bool) -> None:
+        N.check(self.lib.sofi_set_fused(self.h, int(bool(on))))
+
     def persistent(self) -> tuple:
         """(on, blocks per launch) of the persistent step kernel."""
         a, b = ctypes.c_int(), ctypes.c_int()

@@ -230,6 +230,18 @@ int sofi_fwi_backward(sofi_ctx *ctx, const float *adj_x, const float *adj_y);
 int sofi_fwi_gradients(sofi_ctx *ctx, float *grad_lam, float *grad_mu, float *grad_rhos);
 int sofi_fwi_checkpoints(sofi_ctx *ctx, int *interval, int *segments);
 
+/* The fused step (ISO / VTI, FDORDER_TIME 2, no periodic edge): the velocity
+ * and the stress update of a step in one kernel. Each tile computes the new
+ * velocities on itself and an ND-cell halo into shared memory and the new
+ * stresses of its own cells from them, so the stresses are read once per
+ * step instead of twice; v, s and the velocity CPML memory are then held
+ * twice and swapped every step. It is off unless SOFI_FUSED=1 (then
+ * sofi_device_bytes counts the second set) or sofi_set_fused turns it on: on
+ * the grids measured the two separate kernels are faster. Results equal the
+ * four-cell kernels' bit for bit. */
+int sofi_fused(sofi_ctx *ctx, int *on);
+int sofi_set_fused(sofi_ctx *ctx, int on);
+
 /* The persistent step kernel: chunks of up to 128 time steps (until the next
  * snapshot or timed step) run as one cooperative launch whose blocks step
  * through the velocity, stress and post phases with a grid-wide barrier
