@@ -1181,6 +1181,10 @@ __device__ __forceinline__ void post_sources(const Geo &G, const Wave &W, const 
 }
 
 // surface_elastic.c:27-90 / surface.c:27-113 at j = 1 for column i.
+// Every value is loaded before the first store: the rows written (the
+// surface cell's syy, sxx, memory variables, and the mirrored ghost rows
+// above it) are none of the rows read below it, and with all loads issued
+// together a column costs one memory round trip instead of one per row.
 template <int ND, bool VISCO>
 __device__ __forceinline__ void post_surface(const Geo &G, const Wave &W, const Model &M, int s, int i)
 {
@@ -1189,6 +1193,37 @@ __device__ __forceinline__ void post_surface(const Geo &G, const Wave &W, const 
     const long long o = cell(G, j, i);
     float *sxx = W.sxx + so, *syy = W.syy + so, *sxy = W.sxy + so;
     const float *vx = W.vx + so, *vy = W.vy + so;
+    // ---- loads
+    float syb[ND], sxb[ND], vxp[ND], vxm[ND], vyp[ND], vym[ND];
+#pragma unroll
+    for (int m = 1; m <= ND; m++) {
+        syb[m - 1] = syy[o + (long long)m * P];
+        sxb[m - 1] = sxy[o + (long long)(m - 1) * P];
+        vxp[m - 1] = vx[o + m - 1], vxm[m - 1] = vx[o - m];
+        vyp[m - 1] = vy[o + (long long)(m - 1) * P], vym[m - 1] = vy[o - (long long)m * P];
+    }
+    int h = 0;
+    long long q = 0;
+    float psi = 0.f;
+    if (G.abs_type == 1 && !G.boundary) {
+        if (i <= G.fw)
+            h = i;
+        else if (i >= G.nx - G.fw + 1)
+            h = i - G.nx + G.fw2;
+        if (h) {
+            q = ((long long)s * G.ny + (j - 1)) * G.fw2 + (h - 1);
+            psi = W.psi_vxx[q];
+        }
+    }
+    const float pu = M.pu[mo + o], ppi = M.ppi[mo + o], sxx0 = sxx[o];
+    float taus = 0.f, taup = 0.f, pl[MAXL];
+    if (VISCO) {
+        taus = M.taus[mo + o], taup = M.taup[mo + o];
+#pragma unroll
+        for (int l = 0; l < MAXL; l++)
+            pl[l] = l < G.L ? W.p[((long long)s * G.L + l) * G.fsz + o] : 0.f;
+    }
+    // ---- arithmetic and stores, in the reference's order
     syy[o] = 0.0f;
     if (VISCO)
         for (int l = 0; l < G.L; l++)
@@ -1196,48 +1231,42 @@ __device__ __forceinline__ void post_surface(const Geo &G, const Wave &W, const 
     float vxx = 0.f, vyy = 0.f;
 #pragma unroll
     for (int m = 1; m <= ND; m++) {
-        syy[o - (long long)m * P] = -syy[o + (long long)m * P];
-        sxy[o - (long long)m * P] = -sxy[o + (long long)(m - 1) * P];
-        vxx += G.hc[m] * (vx[o + m - 1] - vx[o - m]);
-        vyy += G.hc[m] * (vy[o + (long long)(m - 1) * P] - vy[o - (long long)m * P]);
+        syy[o - (long long)m * P] = -syb[m - 1];
+        sxy[o - (long long)m * P] = -sxb[m - 1];
+        vxx += G.hc[m] * (vxp[m - 1] - vxm[m - 1]);
+        vyy += G.hc[m] * (vyp[m - 1] - vym[m - 1]);
     }
     vxx *= G.dhi;
     vyy *= G.dhi;
-    if (G.abs_type == 1 && !G.boundary) {
-        int h = 0;
-        if (i <= G.fw)
-            h = i;
-        else if (i >= G.nx - G.fw + 1)
-            h = i - G.nx + G.fw2;
-        if (h) {
-            long long q = ((long long)s * G.ny + (j - 1)) * G.fw2 + (h - 1);
-            float ps = M.b_x[h - 1] * W.psi_vxx[q] + M.a_x[h - 1] * vxx;
-            W.psi_vxx[q] = ps;
-            vxx = vxx / M.K_x[h - 1] + ps;
-        }
+    if (h) {
+        float ps = M.b_x[h - 1] * psi + M.a_x[h - 1] * vxx;
+        W.psi_vxx[q] = ps;
+        vxx = vxx / M.K_x[h - 1] + ps;
     }
-    const float pu = M.pu[mo + o], ppi = M.ppi[mo + o];
     if (!VISCO) {
         float fjm = pu * 2.0f, g = ppi;
-        sxx[o] += -(G.dt * (g - fjm) * (g - fjm) * vxx / g) - (G.dt * (g - fjm) * vyy);
+        sxx[o] = sxx0 + (-(G.dt * (g - fjm) * (g - fjm) * vxx / g) - (G.dt * (g - fjm) * vyy));
     } else {
-        float taus = M.taus[mo + o], taup = M.taup[mo + o];
         float sump = 0.f;
-        for (int l = 0; l < G.L; l++)
-            sump += W.p[((long long)s * G.L + l) * G.fsz + o];
+#pragma unroll
+        for (int l = 0; l < MAXL; l++)
+            if (l < G.L)
+                sump += pl[l];
         float fjm = pu * 2.0f * (1.0f + G.L * taus);
         float g = ppi * (1.0f + G.L * taup);
-        sxx[o] += -(G.dt * (g - fjm) * (g - fjm) * vxx / g) - (G.dt * (g - fjm) * vyy) - (G.dthalbe * sump);
+        float sx = sxx0 + (-(G.dt * (g - fjm) * (g - fjm) * vxx / g) - (G.dt * (g - fjm) * vyy) - (G.dthalbe * sump));
         sump = 0.f;
         float djm = 2.0f * pu * taus, e = ppi * taup;
-        for (int l = 0; l < G.L; l++) {
-            float bjm = M.peta[l] / (1.0f + (M.peta[l] * 0.5f));
-            long long lo = ((long long)s * G.L + l) * G.fsz + o;
-            float pl = W.p[lo] + bjm * (((djm - e) * ((fjm / g) - 1.0f) * vxx) - ((djm - e) * vyy));
-            W.p[lo] = pl;
-            sump += pl;
+#pragma unroll
+        for (int l = 0; l < MAXL; l++) {
+            if (l < G.L) {
+                float bjm = M.peta[l] / (1.0f + (M.peta[l] * 0.5f));
+                float p = pl[l] + bjm * (((djm - e) * ((fjm / g) - 1.0f) * vxx) - ((djm - e) * vyy));
+                W.p[((long long)s * G.L + l) * G.fsz + o] = p;
+                sump += p;
+            }
         }
-        sxx[o] += G.dthalbe * sump;
+        sxx[o] = sx + G.dthalbe * sump;
     }
 }
 
@@ -1279,23 +1308,26 @@ __device__ __forceinline__ void sample_div_curl(const Geo &G, const Wave &W, con
     sec[4 * A.ns] = (vxy - vyx) * sqrtf(M.pu[mo + o]);
 }
 
-// vx, vy and p of seismo_ssg.c:36-62 for receiver k after the step.
+// vx, vy and p of seismo_ssg.c:36-62 for receiver k after the step; (o, vxk,
+// vyk): the receiver's cell and its velocities, loaded by the caller (nothing
+// after the velocity update writes v).
 __device__ __forceinline__ void sample_v_p(const Geo &G, const Wave &W, const Model &M, const Acq &A, int s, int k,
-                                           int ins, int seismo)
+                                           long long o, float vxk, float vyk, int ins, int seismo)
 {
-    const long long o = cell(G, A.rec_iy[k], A.rec_ix[k]);
     const long long so = (long long)s * G.fsz, mo = moff(G, s);
     float *sec = A.sec + (long long)k * 5 * A.ns + (ins - 1);
     if (seismo == 1 || seismo == 4) {
-        sec[0] = W.vx[so + o];
-        sec[A.ns] = W.vy[so + o];
+        sec[0] = vxk;
+        sec[A.ns] = vyk;
     }
-    float p = -W.sxx[so + o] - W.syy[so + o];
-    if (seismo == 2)
-        sec[2 * A.ns] = p;
-    if (seismo == 4) {
-        float ppi = M.ppi[mo + o], pu = M.pu[mo + o];
-        sec[2 * A.ns] = ((3.0f * ppi - 4.0f * pu) / (2.0f * ppi - 2.0f * pu)) * p / 3.0f;
+    if (seismo == 2 || seismo == 4) {
+        float p = -W.sxx[so + o] - W.syy[so + o];
+        if (seismo == 2)
+            sec[2 * A.ns] = p;
+        else {
+            float ppi = M.ppi[mo + o], pu = M.pu[mo + o];
+            sec[2 * A.ns] = ((3.0f * ppi - 4.0f * pu) / (2.0f * ppi - 2.0f * pu)) * p / 3.0f;
+        }
     }
 }
 
@@ -1315,6 +1347,16 @@ __device__ __forceinline__ void post_column(const Geo &G, Wave W, const Model &M
     const int ins = (seismo && G.ndt > 0 && nt % G.ndt == 0 && nt < A.nt) ? nt / G.ndt : 0;
     const int *roff = A.rec_col_off ? A.rec_col_off + (long long)s * (G.nx + 1) : nullptr;
     const int r0 = roff ? roff[i - 1] : 0, r1 = roff ? roff[i] : 0;
+    // the column's first receiver, loaded ahead of the stores below
+    const long long so = (long long)s * G.fsz;
+    int k0 = 0;
+    long long o0 = 0;
+    float vx0 = 0.f, vy0 = 0.f;
+    if (r0 < r1) {
+        k0 = A.rec_col_idx[r0];
+        o0 = cell(G, A.rec_iy[k0], A.rec_ix[k0]);
+        vx0 = W.vx[so + o0], vy0 = W.vy[so + o0];
+    }
     if (ins && (seismo == 3 || seismo == 4))
         for (int r = r0; r < r1; r++)
             sample_div_curl<ND, TTIK>(G, W, M, A, s, A.rec_col_idx[r], ins);
@@ -1323,12 +1365,19 @@ __device__ __forceinline__ void post_column(const Geo &G, Wave W, const Model &M
         post_surface<ND, VISCO>(G, W, M, s, i);
     if (i == (G.nx / 2 > 0 ? G.nx / 2 : 1)) {
         long long pc = cell(G, G.ny / 2 > 0 ? G.ny / 2 : 1, i);
-        if (isnan(W.vy[(long long)s * G.fsz + pc]) && A.status[s] == 0)
+        if (isnan(W.vy[so + pc]) && A.status[s] == 0)
             A.status[s] = nt;
     }
     if (ins && seismo != 3)
-        for (int r = r0; r < r1; r++)
-            sample_v_p(G, W, M, A, s, A.rec_col_idx[r], ins, seismo);
+        for (int r = r0; r < r1; r++) {
+            if (r == r0) {
+                sample_v_p(G, W, M, A, s, k0, o0, vx0, vy0, ins, seismo);
+            } else {
+                const int k = A.rec_col_idx[r];
+                const long long o = cell(G, A.rec_iy[k], A.rec_ix[k]);
+                sample_v_p(G, W, M, A, s, k, o, W.vx[so + o], W.vy[so + o], ins, seismo);
+            }
+        }
 }
 
 template <int ND, bool VISCO, bool TTIK>
