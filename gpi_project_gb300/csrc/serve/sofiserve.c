@@ -386,7 +386,9 @@ static int make_resident(sofi_server *s, req_t *q)
     q->priority = s->o.use_priorities ? sofi_server_priority(work, s->prio_least, s->prio_greatest) : 0;
     if ((rc = sofi_create_with_priority(&q->cfg, s->o.device, q->priority, &q->ctx)))
         return rc;
-    if (s->o.persistent) {
+    /* solves share the GPU: no blocks parked waiting for their predecessor */
+    rc = sofi_set_pdl(q->ctx, 0);
+    if (s->o.persistent && !rc) {
         int on = 0, blocks = 0;
         if ((rc = sofi_persistent(q->ctx, &on, &blocks)) == 0 && blocks && !on)
             rc = sofi_set_persistent(q->ctx, 1);

@@ -32,8 +32,50 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 namespace sofi {
+
+// Programmatic dependent launch. The step's main kernels are launched with
+// programmatic stream serialisation (launch_pdl), so the GPU may schedule one
+// while the previous kernel of the stream is still running. Each such kernel
+// calls pdl_begin() before touching memory: griddepcontrol.wait returns once
+// the previous kernel has completed and its writes are visible (a no-op after
+// an ordinary launch), then launch_dependents lets the next kernel be
+// scheduled. The launch of one kernel thus overlaps the tail of the last, and
+// no kernel reads or writes anything before its predecessor has finished.
+__device__ __forceinline__ void pdl_begin()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Whether launch_pdl uses programmatic serialisation on this host thread; the
+// context whose step is being launched sets it (off: ordinary launches of the
+// same kernels).
+inline bool &pdl_flag()
+{
+    static thread_local bool on = true;
+    return on;
+}
+
+// Launch k on st with programmatic stream serialisation (k begins with
+// pdl_begin()).
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args)
+{
+    if (!pdl_flag()) {
+        k<<<grid, block, smem, st>>>(args...);
+        return;
+    }
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid, cfg.blockDim = block, cfg.dynamicSmemBytes = smem, cfg.stream = st;
+    cfg.attrs = at, cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, args...);  // an error stays with cudaGetLastError()
+}
 
 constexpr int HX = 8;
 constexpr int HY = 8;

@@ -33,6 +33,7 @@ __device__ __forceinline__ void force_shot(const Geo &G, const Wave &W, const Mo
 
 static __global__ void k_force_src(Geo G, Wave W, Model M, Acq A)
 {
+    pdl_begin();
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s < G.nshots)
         force_shot(G, W, M, A, s);
@@ -47,6 +48,7 @@ static __global__ void k_force_src(Geo G, Wave W, Model M, Acq A)
 template <int ND, int R>
 __global__ void __launch_bounds__(BX *BY, R == 1 ? 8 : 1) k_update_v(Geo G, Wave W, Model M)
 {
+    pdl_begin();
     int bx, s;
     block_xs(G, bx, s);
     const int i = bx * BX + threadIdx.x + 1;
@@ -418,6 +420,7 @@ __device__ __forceinline__ void vw_tile(const Geo &G, const Wave &W, const Model
 template <int ND, int VW, bool SXY = true, bool FWI = false>
 __global__ void __launch_bounds__(BX *BY, VW == 4 ? 4 : 1) k_update_vw(Geo G, Wave W, Model M)
 {
+    pdl_begin();
     vw_tile<ND, VW, SXY, false, FWI>(G, W, M, blockIdx);
 }
 
@@ -450,6 +453,7 @@ static __global__ void k_wrap_x(Geo G, float *a, float *b, float *c, int nd)
 template <int ND, int KIND, bool VISCO, int LT>
 __global__ void __launch_bounds__(BX *BY) k_update_s(Geo G, Wave W, Model M)
 {
+    pdl_begin();
     int bx, s;
     block_xs(G, bx, s);
     const int i = bx * BX + threadIdx.x + 1;
@@ -775,6 +779,7 @@ __device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model
 template <int ND, int KIND, bool VISCO, int LT, int VW, bool FWI = false>
 __global__ void __launch_bounds__(BX *BY, VW == 4 ? 2 : 1) k_update_sw(Geo G, Wave W, Model M)
 {
+    pdl_begin();
     sw_tile<ND, KIND, VISCO, LT, VW, false, FWI>(G, W, M, blockIdx);
 }
 
@@ -880,6 +885,7 @@ __device__ __forceinline__ void sac_tile(const Geo &G, const Wave &W, const Mode
 template <int ND, int VW>
 __global__ void __launch_bounds__(BX *BY) k_update_s_ac(Geo G, Wave W, Model M)
 {
+    pdl_begin();
     sac_tile<ND, VW, false>(G, W, M, blockIdx);
 }
 
@@ -1031,6 +1037,7 @@ __global__ void __launch_bounds__(BX *BY) k_tti_fused(Geo G, Wave W, Model M)
     constexpr int RING = 2 * SX + 2 * BY;
     static_assert(RING <= BX * BY, "ring cells exceed the block");
     __shared__ float sd[NB][4][SY][SX];  // [raw, stretched][vxx vyy vyx vxy][y][x]
+    pdl_begin();
     int bx, s;
     block_xs(G, bx, s);
     const int i0 = bx * BX + 1, j0 = blockIdx.y * BY + 1;
@@ -1383,6 +1390,7 @@ __device__ __forceinline__ void post_column(const Geo &G, Wave W, const Model &M
 template <int ND, bool VISCO, bool TTIK>
 __global__ void k_post(Geo G, Wave W, Model M, Acq A)
 {
+    pdl_begin();
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (i <= G.nx)
         post_column<ND, VISCO, TTIK>(G, W, M, A, i, blockIdx.y);

@@ -14,20 +14,20 @@ void stress_w(const Geo &G, const Wave &W, const Model &M, int nd, dim3 grd, cud
     [[maybe_unused]] const int L = VISCO ? G.L : 0;
     if constexpr (KIND == ISO && !VISCO && VW == 4)
         if (W.fu_x) {  // a storing step of an FWI forward run
-            DISPATCH_ND(nd, (k_update_sw<ND, ISO, false, 0, 4, true><<<grd, blk, 0, st>>>(G, W, M)))
+            DISPATCH_ND(nd, (launch_pdl(k_update_sw<ND, ISO, false, 0, 4, true>, grd, blk, 0, st, G, W, M)))
             return;
         }
     if constexpr (!VISCO) {
-        DISPATCH_ND(nd, (k_update_sw<ND, KIND, false, 0, VW><<<grd, blk, 0, st>>>(G, W, M)))
+        DISPATCH_ND(nd, (launch_pdl(k_update_sw<ND, KIND, false, 0, VW>, grd, blk, 0, st, G, W, M)))
     } else {
         if (L == 1)
-            DISPATCH_ND(nd, (k_update_sw<ND, KIND, true, 1, VW><<<grd, blk, 0, st>>>(G, W, M)))
+            DISPATCH_ND(nd, (launch_pdl(k_update_sw<ND, KIND, true, 1, VW>, grd, blk, 0, st, G, W, M)))
         else if (L == 2)
-            DISPATCH_ND(nd, (k_update_sw<ND, KIND, true, 2, VW><<<grd, blk, 0, st>>>(G, W, M)))
+            DISPATCH_ND(nd, (launch_pdl(k_update_sw<ND, KIND, true, 2, VW>, grd, blk, 0, st, G, W, M)))
         else if (L == 3)
-            DISPATCH_ND(nd, (k_update_sw<ND, KIND, true, 3, VW><<<grd, blk, 0, st>>>(G, W, M)))
+            DISPATCH_ND(nd, (launch_pdl(k_update_sw<ND, KIND, true, 3, VW>, grd, blk, 0, st, G, W, M)))
         else
-            DISPATCH_ND(nd, (k_update_sw<ND, KIND, true, 0, VW><<<grd, blk, 0, st>>>(G, W, M)))
+            DISPATCH_ND(nd, (launch_pdl(k_update_sw<ND, KIND, true, 0, VW>, grd, blk, 0, st, G, W, M)))
     }
 }
 
@@ -41,16 +41,16 @@ void launch_stress_kv(const Geo &G, const Wave &W, const Model &M, int nd, int s
     const dim3 blk(BX, BY);
     [[maybe_unused]] const int L = VISCO ? G.L : 0;
     if constexpr (!VISCO) {
-        DISPATCH_ND(nd, (k_update_s<ND, KIND, false, 0><<<grd, blk, 0, st>>>(G, W, M)))
+        DISPATCH_ND(nd, (launch_pdl(k_update_s<ND, KIND, false, 0>, grd, blk, 0, st, G, W, M)))
     } else {
         if (L == 1)
-            DISPATCH_ND(nd, (k_update_s<ND, KIND, true, 1><<<grd, blk, 0, st>>>(G, W, M)))
+            DISPATCH_ND(nd, (launch_pdl(k_update_s<ND, KIND, true, 1>, grd, blk, 0, st, G, W, M)))
         else if (L == 2)
-            DISPATCH_ND(nd, (k_update_s<ND, KIND, true, 2><<<grd, blk, 0, st>>>(G, W, M)))
+            DISPATCH_ND(nd, (launch_pdl(k_update_s<ND, KIND, true, 2>, grd, blk, 0, st, G, W, M)))
         else if (L == 3)
-            DISPATCH_ND(nd, (k_update_s<ND, KIND, true, 3><<<grd, blk, 0, st>>>(G, W, M)))
+            DISPATCH_ND(nd, (launch_pdl(k_update_s<ND, KIND, true, 3>, grd, blk, 0, st, G, W, M)))
         else
-            DISPATCH_ND(nd, (k_update_s<ND, KIND, true, 0><<<grd, blk, 0, st>>>(G, W, M)))
+            DISPATCH_ND(nd, (launch_pdl(k_update_s<ND, KIND, true, 0>, grd, blk, 0, st, G, W, M)))
     }
 }
 

@@ -9,11 +9,11 @@ void launch_stress_ac(const Geo &G, const Wave &W, const Model &M, int nd, int s
 {
     const dim3 blk(BX, BY);
     if (sw == 4)
-        DISPATCH_ND(nd, (k_update_s_ac<ND, 4><<<grd, blk, 0, st>>>(G, W, M)))
+        DISPATCH_ND(nd, (launch_pdl(k_update_s_ac<ND, 4>, grd, blk, 0, st, G, W, M)))
     else if (sw == 2)
-        DISPATCH_ND(nd, (k_update_s_ac<ND, 2><<<grd, blk, 0, st>>>(G, W, M)))
+        DISPATCH_ND(nd, (launch_pdl(k_update_s_ac<ND, 2>, grd, blk, 0, st, G, W, M)))
     else
-        DISPATCH_ND(nd, (k_update_s_ac<ND, 1><<<grd, blk, 0, st>>>(G, W, M)))
+        DISPATCH_ND(nd, (launch_pdl(k_update_s_ac<ND, 1>, grd, blk, 0, st, G, W, M)))
 }
 
 }  // namespace sofi

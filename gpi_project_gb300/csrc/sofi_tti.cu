@@ -10,13 +10,13 @@ void launch_tti_fused(const Geo &G, const Wave &W, const Model &M, int nd, bool 
 {
     const dim3 blk(BX, BY);
     if (visco && cpml) {
-        DISPATCH_ND(nd, (k_tti_fused<ND, true, true><<<grd, blk, 0, st>>>(G, W, M)));
+        DISPATCH_ND(nd, (launch_pdl(k_tti_fused<ND, true, true>, grd, blk, 0, st, G, W, M)));
     } else if (visco) {
-        DISPATCH_ND(nd, (k_tti_fused<ND, true, false><<<grd, blk, 0, st>>>(G, W, M)));
+        DISPATCH_ND(nd, (launch_pdl(k_tti_fused<ND, true, false>, grd, blk, 0, st, G, W, M)));
     } else if (cpml) {
-        DISPATCH_ND(nd, (k_tti_fused<ND, false, true><<<grd, blk, 0, st>>>(G, W, M)));
+        DISPATCH_ND(nd, (launch_pdl(k_tti_fused<ND, false, true>, grd, blk, 0, st, G, W, M)));
     } else {
-        DISPATCH_ND(nd, (k_tti_fused<ND, false, false><<<grd, blk, 0, st>>>(G, W, M)));
+        DISPATCH_ND(nd, (launch_pdl(k_tti_fused<ND, false, false>, grd, blk, 0, st, G, W, M)));
     }
 }
 

@@ -16,25 +16,25 @@ void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw
     const dim3 blk(BX, BY);
     if (acoustic) {
         if (vw == 4)
-            DISPATCH_ND(nd, (k_update_vw<ND, 4, false><<<gv, blk, 0, st>>>(G, W, M)))
+            DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 4, false>, gv, blk, 0, st, G, W, M)))
         else if (vw == 2)
-            DISPATCH_ND(nd, (k_update_vw<ND, 2, false><<<gv, blk, 0, st>>>(G, W, M)))
+            DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 2, false>, gv, blk, 0, st, G, W, M)))
         else
-            DISPATCH_ND(nd, (k_update_vw<ND, 1, false><<<gv, blk, 0, st>>>(G, W, M)))
+            DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 1, false>, gv, blk, 0, st, G, W, M)))
         return;
     }
     if (vw == 4 && W.fa_x)  // a storing step of an FWI forward run
-        DISPATCH_ND(nd, (k_update_vw<ND, 4, true, true><<<gv, blk, 0, st>>>(G, W, M)))
+        DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 4, true, true>, gv, blk, 0, st, G, W, M)))
     else if (vw == 4)
-        DISPATCH_ND(nd, (k_update_vw<ND, 4><<<gv, blk, 0, st>>>(G, W, M)))
+        DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 4>, gv, blk, 0, st, G, W, M)))
     else if (vw == 2)
-        DISPATCH_ND(nd, (k_update_vw<ND, 2><<<gv, blk, 0, st>>>(G, W, M)))
+        DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 2>, gv, blk, 0, st, G, W, M)))
     else if (vrows == 2)
-        DISPATCH_ND(nd, (k_update_v<ND, 2><<<gv, blk, 0, st>>>(G, W, M)))
+        DISPATCH_ND(nd, (launch_pdl(k_update_v<ND, 2>, gv, blk, 0, st, G, W, M)))
     else if (vrows == 4)
-        DISPATCH_ND(nd, (k_update_v<ND, 4><<<gv, blk, 0, st>>>(G, W, M)))
+        DISPATCH_ND(nd, (launch_pdl(k_update_v<ND, 4>, gv, blk, 0, st, G, W, M)))
     else
-        DISPATCH_ND(nd, (k_update_v<ND, 1><<<gv, blk, 0, st>>>(G, W, M)))
+        DISPATCH_ND(nd, (launch_pdl(k_update_v<ND, 1>, gv, blk, 0, st, G, W, M)))
 }
 
 namespace {

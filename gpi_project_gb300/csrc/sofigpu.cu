@@ -221,6 +221,7 @@ struct sofi_ctx {
     // CUDA graph of kGraphSteps time steps, replayed for every chunk without
     // snapshot or timed steps (the step number lives in G.step_ctr)
     bool use_graph = true;
+    bool pdl = true;  // programmatic dependent launch of the step kernels (launch_pdl)
     bool graph_dirty = true;
     cudaGraphExec_t graph_exec = nullptr;   // the step graph (fused mode: current buffers are the first set)
     cudaGraphExec_t graph_exec1 = nullptr;  // fused mode, current buffers the second set
@@ -809,7 +810,7 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
     int kind = kind_of(cf.weq);
     bool visco = is_visco(cf.weq);
     if (c->has_force) {
-        k_force_src<<<nb, 128, 0, st>>>(G, c->W, c->M, c->A);
+        launch_pdl(k_force_src, nb, 128, 0, st, G, c->W, c->M, c->A);
         c->launches++;
     }
     if (c->fwi_back) {  // adjoint signals at the receivers, then the density term
@@ -876,11 +877,11 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
 post:
     dim3 pg((cf.nx + 127) / 128, S);
     if (kind == TTI)
-        DISPATCH_ND(c->nd, (k_post<ND, false, true><<<pg, 128, 0, st>>>(G, c->W, c->M, c->A)))
+        DISPATCH_ND(c->nd, (launch_pdl(k_post<ND, false, true>, pg, 128, 0, st, G, c->W, c->M, c->A)))
     else if (visco)
-        DISPATCH_ND(c->nd, (k_post<ND, true, false><<<pg, 128, 0, st>>>(G, c->W, c->M, c->A)))
+        DISPATCH_ND(c->nd, (launch_pdl(k_post<ND, true, false>, pg, 128, 0, st, G, c->W, c->M, c->A)))
     else
-        DISPATCH_ND(c->nd, (k_post<ND, false, false><<<pg, 128, 0, st>>>(G, c->W, c->M, c->A)))
+        DISPATCH_ND(c->nd, (launch_pdl(k_post<ND, false, false>, pg, 128, 0, st, G, c->W, c->M, c->A)))
     c->launches++;
     if (cf.boundary) {
         k_wrap_x<<<dim3((cf.ny + 127) / 128, S), 128, 0, st>>>(G, c->W.sxx, c->W.syy, c->W.sxy, c->nd);
@@ -1167,6 +1168,8 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
     c->d_bar = reinterpret_cast<unsigned *>(c->d_status + cfg->nshots + 2);
     if (const char *e = getenv("SOFI_GRAPH"))
         c->use_graph = atoi(e) != 0;
+    if (const char *e = getenv("SOFI_PDL"))
+        c->pdl = atoi(e) != 0;
     c->A.status = c->d_status;
     // the TMA-fed velocity pipeline, offered to the autotuner where it applies
     // (vplan.segs stays 0 where a tensor map or the launch shape is unavailable)
@@ -1443,6 +1446,7 @@ int sofi_run(sofi_ctx *c, int nsteps)
     if (c->step + nsteps > c->cfg.nt)
         return fail(SOFI_E_ARG, "step %d + %d exceeds NT=%d", c->step, nsteps, c->cfg.nt);
     CK(cudaSetDevice(c->device));
+    pdl_flag() = c->pdl;  // every kernel of this run is launched from this thread
     if (c->G.abs_type == 1 && !c->M.K_x)
         return fail(SOFI_E_STATE, "CPML profiles not set");
     if (c->acq_dirty) {
@@ -1905,6 +1909,25 @@ int sofi_set_persistent(sofi_ctx *c, int on)
     c->persist = on != 0;
     if (c->persist)
         c->fused = false;
+    c->graph_dirty = true;
+    return 0;
+}
+
+int sofi_pdl(sofi_ctx *c, int *on)
+{
+    if (!c || !on)
+        return fail(SOFI_E_ARG, "null argument");
+    *on = c->pdl ? 1 : 0;
+    return 0;
+}
+
+int sofi_set_pdl(sofi_ctx *c, int on)
+{
+    if (!c)
+        return fail(SOFI_E_ARG, "null context");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    c->pdl = on != 0;
     c->graph_dirty = true;
     return 0;
 }

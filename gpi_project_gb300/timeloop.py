@@ -154,6 +154,15 @@ class TimeLoop:
     def set_fused(self, on: bool) -> None:
         N.check(self.lib.sofi_set_fused(self.h, int(bool(on))))
 
+    def pdl(self) -> bool:
+        """Whether the step kernels use programmatic dependent launch."""
+        a = ctypes.c_int()
+        N.check(self.lib.sofi_pdl(self.h, ctypes.byref(a)))
+        return bool(a.value)
+
+    def set_pdl(self, on: bool) -> None:
+        N.check(self.lib.sofi_set_pdl(self.h, int(bool(on))))
+
     def persistent(self) -> tuple:
         """(on, blocks per launch) of the persistent step kernel."""
         a, b = ctypes.c_int(), ctypes.c_int()

@@ -254,6 +254,16 @@ int sofi_set_fused(sofi_ctx *ctx, int on);
  * unavailable); the autotuner does not run while it is on. */
 int sofi_persistent(sofi_ctx *ctx, int *on, int *blocks);
 int sofi_set_persistent(sofi_ctx *ctx, int on);
+/* Programmatic dependent launch of the step kernels: each may be scheduled
+ * while the previous kernel on the context's stream finishes, and waits in
+ * hardware for that kernel's completion before it touches memory, so a
+ * kernel's launch overlaps the tail of the one before. On by default
+ * (SOFI_PDL=0 turns it off for every new context). The request loop of
+ * sofiserve.h turns it off for its contexts: with many solves sharing the
+ * GPU, waiting blocks hold SM slots that other solves' kernels could use.
+ * Results are the same either way. */
+int sofi_pdl(sofi_ctx *ctx, int *on);
+int sofi_set_pdl(sofi_ctx *ctx, int on);
 /* 1 when the velocity update in use is the TMA-fed pipeline (stress tiles
  * copied into a ring of shared-memory stages, blocks marching down column
  * strips; second-order time stepping, not acoustic; SOFI_VROWS=t4 fixes it),
