@@ -58,8 +58,11 @@ void launch_stress_kv(const Geo &G, const Wave &W, const Model &M, int nd, int s
 void launch_stress_ac(const Geo &G, const Wave &W, const Model &M, int nd, int sw, dim3 grid, cudaStream_t st);
 // FDORDER_TIME = 4: step counter, velocity update, stress update (one cell per thread)
 void launch_ab4_begin(const Geo &G, cudaStream_t st);
-void launch_ab4_v(const Geo &G, const Wave &W, const Model &M, int nd, dim3 grid, cudaStream_t st);
-void launch_ab4_s(const Geo &G, const Wave &W, const Model &M, int nd, bool visco, dim3 grid, cudaStream_t st);
+// 4th-order time stepping: `wide` four cells per thread in x (own grid), else
+// one cell per thread on `grid`
+void launch_ab4_v(const Geo &G, const Wave &W, const Model &M, int nd, bool wide, dim3 grid, cudaStream_t st);
+void launch_ab4_s(const Geo &G, const Wave &W, const Model &M, int nd, bool visco, bool wide, dim3 grid,
+                  cudaStream_t st);
 // TTI stress update: one pass (derivatives in shared memory) or the two-kernel
 // form (derivative fields in W.draw / W.dcor)
 void launch_tti_fused(const Geo &G, const Wave &W, const Model &M, int nd, bool visco, bool cpml, dim3 grid,

@@ -559,6 +559,13 @@ void launch_v(sofi_ctx *c, const Geo &G, cudaStream_t st)
     launch_velocity(G, step_wave(c), c->M, c->nd, vw, R, ac, gv, st);
 }
 
+// 4th-order time stepping has no autotuning: four cells per thread in both
+// updates unless SOFI_VROWS=1|2|4 (velocity) or SOFI_SW=0 (stress) asks for one.
+static bool ab4_wide_s(const sofi_ctx *c)
+{
+    return !(c->sw_fixed && c->sw == 0);
+}
+
 // The fused step applies to ISO / VTI media with second-order time stepping,
 // no periodic edge and none of the other step forms (y-marching, persistent,
 // FWI pass).
@@ -847,7 +854,7 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
         goto post;
     }
     if (G.ab4)
-        launch_ab4_v(G, c->W, c->M, c->nd, grd, st);
+        launch_ab4_v(G, c->W, c->M, c->nd, c->vw != 0, grd, st);
     else
         launch_v(c, G, st);
     c->launches++;
@@ -860,7 +867,7 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
     if (timed && cf.boundary)
         CK(cudaEventRecord(e1, st));
     if (G.ab4) {
-        launch_ab4_s(G, c->W, c->M, c->nd, visco, grd, st);
+        launch_ab4_s(G, c->W, c->M, c->nd, visco, ab4_wide_s(c), grd, st);
     } else if (kind == TTI && c->tti_split) {
         c->launches++;
         launch_tti_split(G, c->W, c->M, c->nd, visco, grd, st);
@@ -1604,7 +1611,7 @@ int sofi_velocity_variant(sofi_ctx *c, int *cells_per_thread, int *rows_per_thre
     if (!c || !cells_per_thread || !rows_per_thread)
         return fail(SOFI_E_ARG, "null argument");
     const int vw = c->persist ? 4 : c->vw;
-    *cells_per_thread = (vw && !c->G.ab4) ? vw : 1;  // 4th order: one cell per thread
+    *cells_per_thread = !vw ? 1 : c->G.ab4 ? 4 : vw;  // 4th order: four cells or one
     *rows_per_thread = (vw || c->G.ab4) ? 1 : c->vrows;
     return 0;
 }
@@ -1954,7 +1961,10 @@ int sofi_stress_variant(sofi_ctx *c, int *cells_per_thread)
     if (!c || !cells_per_thread)
         return fail(SOFI_E_ARG, "null argument");
     const int sw = c->persist ? 4 : c->sw;
-    *cells_per_thread = (kind_of(c->cfg.weq) == TTI || c->G.ab4) ? 1 : (sw ? sw : 1);
+    if (c->G.ab4)
+        *cells_per_thread = ab4_wide_s(c) ? 4 : 1;
+    else
+        *cells_per_thread = kind_of(c->cfg.weq) == TTI ? 1 : (sw ? sw : 1);
     return 0;
 }
 
