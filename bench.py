@@ -386,16 +386,17 @@ def main_fwi(args):
     updates = 2.0 * nx * ny * nt
     value = updates / sec / 1e9
     peak, peak_kind = measured_peaks()
-    # algorithmic bytes per cell update: the EL_ISO step (60 B) plus, forward, the kernels' gradient
-    # quantities (20 B written) and their copy into the store (20 B read, 20 B written); backward, the
-    # density term (v, store 2 x 4 B, sum read + written: 24 B) and the lambda / mu terms (store 3 x 4,
-    # stresses 12, model 4 x 4, two sums read + written: 56 B); a checkpointed pass runs the forward steps
-    # twice (the first time without the store copy) and counts the recompute as work
-    bpc = (60 + 20 + 40 + 60 + 24 + 56) / 2.0
+    # algorithmic bytes per cell update: the EL_ISO step (60 B) plus, on a stored forward step, the five
+    # gradient quantities written to the store once (20 B); backward, the density term (v, store 2 x 4 B,
+    # sum read + written: 24 B) and the lambda / mu terms (store 3 x 4, stresses 12, model 4 x 4, two sums
+    # read + written: 56 B); a checkpointed pass runs the forward steps twice (the first time storing
+    # nothing) and counts the recompute as work. The velocity terms' trip through two scratch fields (16 B)
+    # is not credited.
+    bpc = (60 + 20 + 60 + 24 + 56) / 2.0
     if ck[0][0]:
         updates = 3.0 * nx * ny * nt
         value = updates / sec / 1e9
-        bpc = (60 + 20 + 60 + 20 + 40 + 60 + 24 + 56) / 3.0
+        bpc = (60 + 60 + 20 + 60 + 24 + 56) / 3.0
     store_gb = 5.0 * nx * ny * nt * 4 / 1e9
     t.close()
     if rank != 0:

@@ -123,9 +123,13 @@ struct Wave {
     long long ab_lvl, ab_mlvl;
     // MODE = FWI forward pass (null otherwise): the velocity update writes
     // rip (sxx_x + sxy_y) / DH and rjp (sxy_x + syy_y) / DH of every cell
-    // (wavefield_update_v.c:31-35), the EL_ISO stress update u1..u3 / DT
-    // (wavefield_update_s_el.c:43-47; VELOCITY = 1)
-    float *fa_x, *fa_y, *fu_x, *fu_y, *fu_xy;
+    // (wavefield_update_v.c:31-35) to fa_x / fa_y. On a stored step with
+    // VELOCITY = 1, fstore is the store ([slots][5][NY][NX], one shot) and the
+    // EL_ISO stress update writes slot nt - 1 - *fbase itself: fa_x, fa_y and
+    // its u2, u3, u1 / DT (wavefield_update_s_el.c:43-47).
+    float *fa_x, *fa_y;
+    float *fstore;
+    const int *fbase;
 };
 
 // Device state of an FWI gradient pass (sofi_fwi.cu); one shot per context.

@@ -3,11 +3,13 @@
 // with the residuals injected at the receivers (update_v_interior.c:72-90) and
 // calc_conv.c's correlation at every step (time_loop.c:288-303, DTINV = 1).
 //
-// Forward: the velocity and stress kernels write this step's gradient
-// quantities (Wave::fa_*, fu_*); k_fwi_store copies them, or the stresses for
-// VELOCITY = 0, into the store ([slots][5][NY][NX] floats): slot nt - 1 when
-// the whole run is kept, slot nt - 1 - base for a recomputed segment of a
-// checkpointed pass (base = the segment's first step - 1).
+// Forward: the store holds [slots][5][NY][NX] floats, slot nt - 1 when the
+// whole run is kept, slot nt - 1 - base for a recomputed segment of a
+// checkpointed pass (base = the segment's first step - 1). The velocity
+// kernel writes this step's rip / rjp terms (Wave::fa_*); with VELOCITY = 1
+// the stress kernel then fills the whole slot (those two and its own u / DT),
+// with VELOCITY = 0 k_fwi_store copies them and the stresses after the free
+// surface.
 // Backward, per step: k_fwi_adj adds the adjoint signals at the receivers
 // before the velocity update; k_fwi_rho forms the reference's pvxp1 / pvyp1
 // (the injected velocity, or its running sum times DT for VELOCITY = 0) and
@@ -20,6 +22,7 @@
 
 namespace sofi {
 
+// VELOCITY = 0 only
 __global__ void k_fwi_store(Geo G, Wave W, FwiDev F)
 {
     const long long n = (long long)G.nx * G.ny;
@@ -32,11 +35,7 @@ __global__ void k_fwi_store(Geo G, Wave W, FwiDev F)
     float *slot = F.store + (long long)(nt - 1 - *F.base) * 5 * n + q;
     slot[0] = W.fa_x[o];
     slot[n] = W.fa_y[o];
-    if (F.velocity) {
-        slot[2 * n] = W.fu_x[o], slot[3 * n] = W.fu_y[o], slot[4 * n] = W.fu_xy[o];
-    } else {
-        slot[2 * n] = W.sxx[o], slot[3 * n] = W.syy[o], slot[4 * n] = W.sxy[o];
-    }
+    slot[2 * n] = W.sxx[o], slot[3 * n] = W.syy[o], slot[4 * n] = W.sxy[o];
 }
 
 // One thread per receiver cell; a cell's receivers in the reference's order.

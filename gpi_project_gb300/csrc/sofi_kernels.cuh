@@ -686,9 +686,12 @@ __device__ __forceinline__ void s_update(const Geo &G, const Wave &Wr, const Wav
             float gd = m0[c] * (dxx + dyy);
             u2 = gd - 2.0f * m1[c] * dyy;
             u3 = gd - 2.0f * m1[c] * dxx;
-            if (FWI && !VISCO && ic <= G.nx) {
-                const long long q = (long long)s * G.fsz + o + c;
-                W.fu_xy[q] = u1 / G.dt, W.fu_x[q] = u2 / G.dt, W.fu_y[q] = u3 / G.dt;
+            if (FWI && !VISCO && W.fstore && ic <= G.nx) {
+                const long long n = (long long)G.nx * G.ny;
+                float *slot = W.fstore + (long long)(*G.step_ctr - 1 - *W.fbase) * 5 * n +
+                              ((long long)(j - 1) * G.nx + (ic - 1));
+                slot[0] = W.fa_x[(long long)s * G.fsz + o + c], slot[n] = W.fa_y[(long long)s * G.fsz + o + c];
+                slot[2 * n] = u2 / G.dt, slot[3 * n] = u3 / G.dt, slot[4 * n] = u1 / G.dt;
             }
         } else {
             u1 = m3[c] * (dxy + dyx);

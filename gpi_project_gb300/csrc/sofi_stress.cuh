@@ -13,7 +13,7 @@ void stress_w(const Geo &G, const Wave &W, const Model &M, int nd, dim3 grd, cud
     const dim3 blk(BX, BY);
     [[maybe_unused]] const int L = VISCO ? G.L : 0;
     if constexpr (KIND == ISO && !VISCO && VW == 4)
-        if (W.fu_x) {  // a storing step of an FWI forward run
+        if (W.fa_x) {  // a step of an FWI forward run
             DISPATCH_ND(nd, (launch_pdl(k_update_sw<ND, ISO, false, 0, 4, true>, grd, blk, 0, st, G, W, M)))
             return;
         }

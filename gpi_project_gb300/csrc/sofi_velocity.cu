@@ -23,7 +23,7 @@ void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw
             DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 1, false>, gv, blk, 0, st, G, W, M)))
         return;
     }
-    if (vw == 4 && W.fa_x)  // a storing step of an FWI forward run
+    if (vw == 4 && W.fa_x)  // a step of an FWI forward run
         DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 4, true, true>, gv, blk, 0, st, G, W, M)))
     else if (vw == 4)
         DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 4>, gv, blk, 0, st, G, W, M)))

@@ -522,15 +522,19 @@ void launch_cell_s(const Geo &G, const Wave &W, const Model &M, int nd, int kind
 }
 
 // The wave fields a step's kernels get: the gradient quantities of an FWI
-// pass (Wave::fa_* / fu_*) only on its forward steps, so that the backward
-// steps and every run outside a pass use the kernels that do not write them.
-// All forward steps, stored or not, run the same kernels: a segment
-// recomputed from a checkpoint then repeats the first run's arithmetic.
+// pass (Wave::fa_*) only on its forward steps, so that the backward steps and
+// every run outside a pass use the kernels that do not write them; the store
+// (Wave::fstore) only on the stored steps of a VELOCITY = 1 pass. All forward
+// steps, stored or not, run the same kernels: a segment recomputed from a
+// checkpoint then repeats the first run's arithmetic.
 Wave step_wave(const sofi_ctx *c)
 {
     Wave W = c->W;
+    W.fstore = nullptr, W.fbase = c->F.base;
     if (!c->fwi || c->fwi_back)
-        W.fa_x = W.fa_y = W.fu_x = W.fu_y = W.fu_xy = nullptr;
+        W.fa_x = W.fa_y = nullptr;
+    else if (c->fwi_store_on && c->F.velocity)
+        W.fstore = c->F.store;
     return W;
 }
 
@@ -895,11 +899,13 @@ post:
         c->launches++;
     }
     if (c->fwi && (c->fwi_back || c->fwi_store_on)) {  // time_loop.c:288-296
-        if (c->fwi_back)
+        if (c->fwi_back) {
             launch_fwi_conv(G, c->W, c->M, c->F, st);
-        else
+            c->launches++;
+        } else if (!c->F.velocity) {  // VELOCITY = 1: the stress kernel stored the step
             launch_fwi_store(G, c->W, c->F, st);
-        c->launches++;
+            c->launches++;
+        }
     }
     if (!capture && !c->fwi_nosnap && cf.snap && nt >= cf.snap_first && nt <= cf.snap_last &&
         (nt == cf.snap_first || (cf.snap_inc > 0 && (nt - cf.snap_first) % cf.snap_inc == 0)) &&
@@ -1684,7 +1690,7 @@ int sofi_fwi_begin(sofi_ctx *c, int velocity, int adjoint_type, const float *vp,
     const size_t slot = 5 * n * sizeof(float), state = c->fwi_state * sizeof(float);
     size_t fr = 0, tot = 0;
     CK(cudaMemGetInfo(&fr, &tot));
-    const size_t reserve = (16 * n) * sizeof(float) + 5 * f + (64u << 20);
+    const size_t reserve = (16 * n) * sizeof(float) + 2 * f + (64u << 20);
     const size_t have = (c->F.store ? c->fwi_slots * slot : 0) + (c->fwi_ckpt ? c->fwi_ckpt_cap * state : 0) + fr;
     int K = 0;
     if (const char *e = getenv("SOFI_FWI_CHECKPOINT"))
@@ -1724,7 +1730,7 @@ int sofi_fwi_begin(sofi_ctx *c, int velocity, int adjoint_type, const float *vp,
         c->F.vp = m[0], c->F.vs = m[1], c->F.rho = m[2];
         if ((rc = dalloc(c, (void **)&c->F.rc, 3 * n * sizeof(double))))
             return rc;
-        float **wf[] = {&c->W.fa_x, &c->W.fa_y, &c->W.fu_x, &c->W.fu_y, &c->W.fu_xy};
+        float **wf[] = {&c->W.fa_x, &c->W.fa_y};
         for (auto p : wf)
             if ((rc = dalloc(c, (void **)p, f)))
                 return rc;
