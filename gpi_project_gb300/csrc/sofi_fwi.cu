@@ -16,7 +16,8 @@
 // adds the density term; after the stress update and the free surface
 // k_fwi_conv adds the lambda and mu terms against forward slot NT - nt + 1.
 // Every kernel takes the step number from the device counter, so the steps
-// replay from the captured graph like the plain ones.
+// replay from the captured graph like the plain ones; the per-step kernels
+// are launched as programmatic dependents (pdl_begin) like the step's own.
 #include "sofi_common.cuh"
 #include "sofi_launch.h"
 
@@ -25,6 +26,7 @@ namespace sofi {
 // VELOCITY = 0 only
 __global__ void k_fwi_store(Geo G, Wave W, FwiDev F)
 {
+    pdl_begin();
     const long long n = (long long)G.nx * G.ny;
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n)
@@ -41,6 +43,7 @@ __global__ void k_fwi_store(Geo G, Wave W, FwiDev F)
 // One thread per receiver cell; a cell's receivers in the reference's order.
 __global__ void k_fwi_adj(Geo G, Wave W, FwiDev F)
 {
+    pdl_begin();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= F.ncell)
         return;
@@ -59,6 +62,7 @@ __global__ void k_fwi_adj(Geo G, Wave W, FwiDev F)
 
 __global__ void k_fwi_rho(Geo G, Wave W, FwiDev F)
 {
+    pdl_begin();
     const long long n = (long long)G.nx * G.ny;
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n)
@@ -102,6 +106,7 @@ __global__ void k_fwi_coef(int n, FwiDev F)
 // before the rounding to float).
 __global__ void k_fwi_conv(Geo G, Wave W, Model M, FwiDev F)
 {
+    pdl_begin();
     const long long n = (long long)G.nx * G.ny;
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n)
@@ -132,21 +137,21 @@ void launch_fwi_coef(int n, const FwiDev &F, cudaStream_t st)
 void launch_fwi_store(const Geo &G, const Wave &W, const FwiDev &F, cudaStream_t st)
 {
     const long long n = (long long)G.nx * G.ny;
-    k_fwi_store<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(G, W, F);
+    launch_pdl(k_fwi_store, (unsigned)((n + 255) / 256), 256, 0, st, G, W, F);
 }
 
 void launch_fwi_backward_pre(const Geo &G, const Wave &W, const FwiDev &F, cudaStream_t st)
 {
     const long long n = (long long)G.nx * G.ny;
     if (F.ncell)
-        k_fwi_adj<<<(F.ncell + 127) / 128, 128, 0, st>>>(G, W, F);
-    k_fwi_rho<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(G, W, F);
+        launch_pdl(k_fwi_adj, (unsigned)((F.ncell + 127) / 128), 128, 0, st, G, W, F);
+    launch_pdl(k_fwi_rho, (unsigned)((n + 255) / 256), 256, 0, st, G, W, F);
 }
 
 void launch_fwi_conv(const Geo &G, const Wave &W, const Model &M, const FwiDev &F, cudaStream_t st)
 {
     const long long n = (long long)G.nx * G.ny;
-    k_fwi_conv<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(G, W, M, F);
+    launch_pdl(k_fwi_conv, (unsigned)((n + 255) / 256), 256, 0, st, G, W, M, F);
 }
 
 }  // namespace sofi

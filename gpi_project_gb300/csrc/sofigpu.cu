@@ -717,7 +717,7 @@ int autotune(sofi_ctx *c)
             for (int k = 0; k < 3; k++) {
                 const int w = cand[k];
                 if ((rc = time_launches(
-                         c, [&] { launch_cell_s(G, c->W, c->M, c->nd, kind, visco, w, cf.nx, cf.ny, cf.nshots, c->stream); },
+                         c, [&] { launch_cell_s(G, step_wave(c), c->M, c->nd, kind, visco, w, cf.nx, cf.ny, cf.nshots, c->stream); },
                          &ms)))
                     return rc;
                 t[k] = ms < t[k] ? ms : t[k];
@@ -1810,16 +1810,30 @@ int sofi_fwi_backward(sofi_ctx *c, const float *adj_x, const float *adj_y)
     // zero_wavefield.c, and no source but the residuals (time_loop.c:248-253 with sw = 1)
     if ((rc = sofi_reset(c, -1)))
         return rc;
+    // The backward steps write no gradient quantities: they run the variants
+    // the autotuner picks for plain steps of this grid (timed now, on the
+    // zeroed state, or taken from the cache); forward and recomputed steps
+    // keep the four-cell FWI kernels.
+    c->fwi_back = true, c->tuned = false;
+    rc = autotune(c);
+    const int bvw = c->vw, bvrows = c->vrows, bsw = c->sw;
+    const bool bvpipe = c->vpipe;
+    c->fwi_back = false;
+    if (rc)
+        return rc;
     const size_t n = (size_t)c->cfg.nx * c->cfg.ny;
     CK(cudaMemsetAsync(c->F.px, 0, n * sizeof(float), c->stream));
     CK(cudaMemsetAsync(c->F.py, 0, n * sizeof(float), c->stream));
     const Acq saved = c->A;
     const bool saved_force = c->has_force;
     auto backward_mode = [&](bool on) {
-        if (on)
+        if (on) {
             c->A.src_off = c->d_noacq, c->A.last_type = c->d_noacq, c->has_force = false;
-        else
+            c->vw = bvw, c->vrows = bvrows, c->sw = bsw, c->vpipe = bvpipe;
+        } else {
             c->A = saved, c->has_force = saved_force;
+            c->vw = 4, c->vrows = 1, c->sw = 4, c->vpipe = false;
+        }
         c->fwi_back = on, c->graph_dirty = true;
     };
     if (!c->fwi_K) {

@@ -132,3 +132,19 @@ def test_gpu_fwi_checkpointed_equals_whole_store(case, monkeypatch):
         fwd, ck = gpu_fwi(case, g["obs_vx"], g["obs_vy"])
         for name in ("vp", "vs", "rho"):
             np.testing.assert_array_equal(ck[name], whole[name], err_msg=f"{case['name']} K={k} {name}")
+
+
+@pytest.mark.parametrize("case", FWI_CASES, ids=[c["name"] for c in FWI_CASES])
+def test_gpu_fwi_pdl_equals_ordinary_launches(case, monkeypatch):
+    """The pass's per-step kernels launched as programmatic dependents give the
+    same seismograms and gradients as ordinary launches, bit for bit."""
+    g = np.load(os.path.join(HERE, "golden", f"ref_{case['name']}.npz"))
+    monkeypatch.delenv("SOFI_FWI_CHECKPOINT", raising=False)
+    monkeypatch.setenv("SOFI_PDL", "0")
+    fwd0, ref = gpu_fwi(case, g["obs_vx"], g["obs_vy"])
+    monkeypatch.setenv("SOFI_PDL", "1")
+    fwd1, got = gpu_fwi(case, g["obs_vx"], g["obs_vy"])
+    for name in ("vp", "vs", "rho"):
+        np.testing.assert_array_equal(got[name], ref[name], err_msg=f"{case['name']} {name}")
+    for k in fwd0:
+        np.testing.assert_array_equal(fwd1[k], fwd0[k], err_msg=f"{case['name']} forward {k}")
