@@ -340,15 +340,19 @@ __device__ __forceinline__ void v_derivs(const Geo &G, LD ld, float *sxx_x, floa
 // SXY = false: the acoustic update (wavefield_update_v_ac.c), which has no
 // sxy: vx += sxx_x * DT/DH * rip, vy += syy_y * DT/DH * rjp (sxx and syy are
 // one pressure array); VW may then also be 1.
-template <int ND, int VW, bool SXY, bool COH, bool FWI = false>
+// TBX: threads of a block in x (BX, or 8 for narrow grids: 32 columns by 32
+// rows per block of four-cell threads, so a 400-cell row leaves 4 % of the
+// last block idle instead of 22 %).
+template <int ND, int VW, bool SXY, bool COH, bool FWI = false, int TBX = BX>
 __device__ __forceinline__ void vw_tile(const Geo &G, const Wave &W, const Model &M, const uint3 b)
 {
     constexpr int K = (ND + VW - 1) / VW;
     constexpr int NXS = VW * (2 * K + 1);  // stencil row: columns i - VW K .. i + VW K + VW - 1
+    constexpr int TBY = BX * BY / TBX;
     int bx, s;
     block_xs(G, b, bx, s);
-    const int i = (bx * BX + threadIdx.x) * VW + 1;
-    const int j = b.y * BY + threadIdx.y + 1;
+    const int i = (bx * TBX + threadIdx.x) * VW + 1;
+    const int j = b.y * TBY + threadIdx.y + 1;
     if (G.step_ctr && b.x == 0 && b.y == 0 && b.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
         *G.step_ctr += 1;
     if (i > G.nx || j > G.ny)
@@ -417,11 +421,11 @@ __device__ __forceinline__ void vw_tile(const Geo &G, const Wave &W, const Model
 // FWI: the forward run of an FWI gradient pass also writes the gradient
 // quantities (Wave::fa_x / fa_y); a separate instantiation, so that the plain
 // kernels carry no trace of it
-template <int ND, int VW, bool SXY = true, bool FWI = false>
+template <int ND, int VW, bool SXY = true, bool FWI = false, int TBX = BX>
 __global__ void __launch_bounds__(BX *BY, VW == 4 ? 4 : 1) k_update_vw(Geo G, Wave W, Model M)
 {
     pdl_begin();
-    vw_tile<ND, VW, SXY, false, FWI>(G, W, M, blockIdx);
+    vw_tile<ND, VW, SXY, false, FWI, TBX>(G, W, M, blockIdx);
 }
 
 // Periodic x (BOUNDARY = 1): ghost columns copy the opposite edge, as the one-
@@ -758,13 +762,14 @@ __device__ __forceinline__ void s_update(const Geo &G, const Wave &Wr, const Wav
     }
 }
 
-template <int ND, int KIND, bool VISCO, int LT, int VW, bool COH, bool FWI = false>
+template <int ND, int KIND, bool VISCO, int LT, int VW, bool COH, bool FWI = false, int TBX = BX>
 __device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model &M, const uint3 b)
 {
+    constexpr int TBY = BX * BY / TBX;  // TBX: as in vw_tile
     int bx, s;
     block_xs(G, b, bx, s);
-    const int i = (bx * BX + threadIdx.x) * VW + 1;
-    const int j = b.y * BY + threadIdx.y + 1;
+    const int i = (bx * TBX + threadIdx.x) * VW + 1;
+    const int j = b.y * TBY + threadIdx.y + 1;
     if (i > G.nx || j > G.ny)
         return;
     const int P = G.pitch;
@@ -779,11 +784,11 @@ __device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model
     s_update<ND, KIND, VISCO, LT, VW, FWI>(G, W, W, M, s, i, j, o, mo, vxx, vyx, vxy, vyy);
 }
 
-template <int ND, int KIND, bool VISCO, int LT, int VW, bool FWI = false>
+template <int ND, int KIND, bool VISCO, int LT, int VW, bool FWI = false, int TBX = BX>
 __global__ void __launch_bounds__(BX *BY, VW == 4 ? 2 : 1) k_update_sw(Geo G, Wave W, Model M)
 {
     pdl_begin();
-    sw_tile<ND, KIND, VISCO, LT, VW, false, FWI>(G, W, M, blockIdx);
+    sw_tile<ND, KIND, VISCO, LT, VW, false, FWI, TBX>(G, W, M, blockIdx);
 }
 
 // Acoustic stress update (wavefield_update_s_ac.c, update_s_acoustic_{interior,

@@ -36,8 +36,9 @@ void launch_march_v(const Geo &G, const Wave &W, const Model &M, int nd, int sy,
 void launch_march_s(const Geo &G, const Wave &W, const Model &M, int nd, int kind, bool visco, int sy,
                     cudaStream_t st);
 // velocity update: vw cells per thread in x (4 or 2), else vrows rows per thread (1, 2, 4);
+// narrow (vw 4, not acoustic): blocks of 8 x 32 threads, 32 columns by 32 rows (grid sized for that);
 // acoustic: no sxy terms, vw 4, 2 or else one cell per thread
-void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw, int vrows, bool acoustic,
+void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw, int vrows, bool narrow, bool acoustic,
                      dim3 grid, cudaStream_t st);
 // The TMA-fed velocity pipeline (k_update_vt): tensor maps of sxx / sxy / syy
 // over all shots' padded fields, and the number of row segments per strip
@@ -51,9 +52,23 @@ struct VtPlan {
 const char *plan_velocity_pipeline(const Geo &G, const Wave &W, int nd, int device, VtPlan *plan);
 void launch_velocity_pipeline(const Geo &G, const Wave &W, const Model &M, int nd, const VtPlan &plan,
                               cudaStream_t st);
-// ISO / VTI stress update (KIND 0 ISO, 1 VTI): sw cells per thread in x (4, 2 or 0 = one)
+// Where the narrow four-cell blocks (8 x 32 threads, 32 columns by 32 rows)
+// exist: the velocity update of non-acoustic media and the ISO / VTI stress
+// update of elastic media or L <= 3, neither on an FWI forward step. The
+// launchers and the grids they are given both follow these.
+inline bool narrow_v_applies(bool acoustic, bool fwi_step)
+{
+    return !acoustic && !fwi_step;
+}
+inline bool narrow_s_applies(bool visco, int L, bool fwi_step)
+{
+    return !fwi_step && (!visco || (L >= 1 && L <= 3));
+}
+// ISO / VTI stress update (KIND 0 ISO, 1 VTI): sw cells per thread in x (4, 2 or 0 = one);
+// narrow (sw 4, where narrow_s_applies): blocks of 8 x 32 threads
 template <int KIND, bool VISCO>
-void launch_stress_kv(const Geo &G, const Wave &W, const Model &M, int nd, int sw, dim3 grid, cudaStream_t st);
+void launch_stress_kv(const Geo &G, const Wave &W, const Model &M, int nd, int sw, bool narrow, dim3 grid,
+                      cudaStream_t st);
 // acoustic stress update: sw cells per thread in x (4, 2 or 0/1 = one)
 void launch_stress_ac(const Geo &G, const Wave &W, const Model &M, int nd, int sw, dim3 grid, cudaStream_t st);
 // FDORDER_TIME = 4: step counter, velocity update, stress update (one cell per thread)

@@ -8,10 +8,25 @@
 namespace sofi {
 
 template <int KIND, bool VISCO, int VW>
-void stress_w(const Geo &G, const Wave &W, const Model &M, int nd, dim3 grd, cudaStream_t st)
+void stress_w(const Geo &G, const Wave &W, const Model &M, int nd, bool narrow, dim3 grd, cudaStream_t st)
 {
     const dim3 blk(BX, BY);
     [[maybe_unused]] const int L = VISCO ? G.L : 0;
+    if constexpr (VW == 4)
+        if (narrow && narrow_s_applies(VISCO, L, W.fa_x != nullptr)) {  // 8 x 32 threads, 32 x 32 cells
+            const dim3 nb(8, BX * BY / 8);
+            if constexpr (!VISCO) {
+                DISPATCH_ND(nd, (launch_pdl(k_update_sw<ND, KIND, false, 0, 4, false, 8>, grd, nb, 0, st, G, W, M)))
+            } else {
+                if (L == 1)
+                    DISPATCH_ND(nd, (launch_pdl(k_update_sw<ND, KIND, true, 1, 4, false, 8>, grd, nb, 0, st, G, W, M)))
+                else if (L == 2)
+                    DISPATCH_ND(nd, (launch_pdl(k_update_sw<ND, KIND, true, 2, 4, false, 8>, grd, nb, 0, st, G, W, M)))
+                else
+                    DISPATCH_ND(nd, (launch_pdl(k_update_sw<ND, KIND, true, 3, 4, false, 8>, grd, nb, 0, st, G, W, M)))
+            }
+            return;
+        }
     if constexpr (KIND == ISO && !VISCO && VW == 4)
         if (W.fa_x) {  // a step of an FWI forward run
             DISPATCH_ND(nd, (launch_pdl(k_update_sw<ND, ISO, false, 0, 4, true>, grd, blk, 0, st, G, W, M)))
@@ -32,12 +47,13 @@ void stress_w(const Geo &G, const Wave &W, const Model &M, int nd, dim3 grd, cud
 }
 
 template <int KIND, bool VISCO>
-void launch_stress_kv(const Geo &G, const Wave &W, const Model &M, int nd, int sw, dim3 grd, cudaStream_t st)
+void launch_stress_kv(const Geo &G, const Wave &W, const Model &M, int nd, int sw, bool narrow, dim3 grd,
+                      cudaStream_t st)
 {
     if (sw == 4)
-        return stress_w<KIND, VISCO, 4>(G, W, M, nd, grd, st);
+        return stress_w<KIND, VISCO, 4>(G, W, M, nd, narrow, grd, st);
     if (sw == 2)
-        return stress_w<KIND, VISCO, 2>(G, W, M, nd, grd, st);
+        return stress_w<KIND, VISCO, 2>(G, W, M, nd, false, grd, st);
     const dim3 blk(BX, BY);
     [[maybe_unused]] const int L = VISCO ? G.L : 0;
     if constexpr (!VISCO) {

@@ -2,5 +2,6 @@
 #include "sofi_stress.cuh"
 
 namespace sofi {
-template void launch_stress_kv<VTI, false>(const Geo &, const Wave &, const Model &, int, int, dim3, cudaStream_t);
+template void launch_stress_kv<VTI, false>(const Geo &, const Wave &, const Model &, int, int, bool, dim3,
+                                        cudaStream_t);
 }

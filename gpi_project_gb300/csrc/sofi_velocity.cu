@@ -10,10 +10,14 @@
 
 namespace sofi {
 
-void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw, int vrows, bool acoustic,
+void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw, int vrows, bool narrow, bool acoustic,
                      dim3 gv, cudaStream_t st)
 {
     const dim3 blk(BX, BY);
+    if (narrow && vw == 4 && narrow_v_applies(acoustic, W.fa_x != nullptr)) {
+        DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 4, true, false, 8>, gv, dim3(8, BX * BY / 8), 0, st, G, W, M)))
+        return;
+    }
     if (acoustic) {
         if (vw == 4)
             DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 4, false>, gv, blk, 0, st, G, W, M)))

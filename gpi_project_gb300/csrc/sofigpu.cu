@@ -214,6 +214,8 @@ struct sofi_ctx {
     bool fwi_nosnap = false;   // a recomputed segment takes no snapshots
     int *d_fwi_base = nullptr; // device: FwiDev::base
     int sw = 0;                // ISO / VTI stress kernel: cells per thread in x (4 or 2), 0 = one
+    bool vnarrow = false;      // four-cell velocity / stress kernels on 8 x 32-thread blocks
+    bool snarrow = false;      //   (narrow_v_applies / narrow_s_applies)
     bool sw_fixed = false;     // SOFI_SW chose it
     bool tuned = false;        // autotuner ran (or was skipped) for this context
     bool tune_fixed = false;   // SOFI_VROWS chose the variant
@@ -507,18 +509,21 @@ dim3 grid2d(const sofi_ctx *c)
 }
 
 // The ISO / VTI stress kernel with sw cells per thread in x (0: one).
-void launch_cell_s(const Geo &G, const Wave &W, const Model &M, int nd, int kind, bool visco, int sw, int nx,
-                   int ny, int nshots, cudaStream_t st)
+void launch_cell_s(const Geo &G, const Wave &W, const Model &M, int nd, int kind, bool visco, int sw, bool narrow,
+                   int nx, int ny, int nshots, cudaStream_t st)
 {
-    const int cx = sw ? sw : 1;
-    const unsigned tx = (nx + cx * BX - 1) / (cx * BX), ty = (ny + BY - 1) / BY;
+    narrow = narrow && sw == 4 && kind != AC && narrow_s_applies(visco, visco ? G.L : 0, W.fa_x != nullptr);
+    const int cx = sw ? sw : 1, bxt = narrow ? 8 : BX, byt = BX * BY / bxt;
+    const unsigned tx = (nx + cx * bxt - 1) / (cx * bxt), ty = (ny + byt - 1) / byt;
     const dim3 grd = G.shot_fast ? dim3(tx * nshots, ty, 1) : dim3(tx, ty, nshots);
     if (kind == AC)
         launch_stress_ac(G, W, M, nd, sw, grd, st);
     else if (kind == ISO)
-        visco ? launch_stress_kv<ISO, true>(G, W, M, nd, sw, grd, st) : launch_stress_kv<ISO, false>(G, W, M, nd, sw, grd, st);
+        visco ? launch_stress_kv<ISO, true>(G, W, M, nd, sw, narrow, grd, st)
+              : launch_stress_kv<ISO, false>(G, W, M, nd, sw, narrow, grd, st);
     else
-        visco ? launch_stress_kv<VTI, true>(G, W, M, nd, sw, grd, st) : launch_stress_kv<VTI, false>(G, W, M, nd, sw, grd, st);
+        visco ? launch_stress_kv<VTI, true>(G, W, M, nd, sw, narrow, grd, st)
+              : launch_stress_kv<VTI, false>(G, W, M, nd, sw, narrow, grd, st);
 }
 
 // The wave fields a step's kernels get: the gradient quantities of an FWI
@@ -557,10 +562,12 @@ void launch_v(sofi_ctx *c, const Geo &G, cudaStream_t st)
         return;
     }
     const int vw = c->persist ? 4 : c->vw;  // the persistent kernel's steps run the four-cell bodies
-    const int R = (vw || ac) ? 1 : c->vrows, cx = vw ? vw : 1;
-    const unsigned tx = (cf.nx + cx * BX - 1) / (cx * BX), ty = (cf.ny + BY * R - 1) / (BY * R);
+    const Wave W = step_wave(c);
+    const bool narrow = !c->persist && c->vnarrow && vw == 4 && narrow_v_applies(ac, W.fa_x != nullptr);
+    const int R = (vw || ac) ? 1 : c->vrows, cx = vw ? vw : 1, bxt = narrow ? 8 : BX, byt = BX * BY / bxt;
+    const unsigned tx = (cf.nx + cx * bxt - 1) / (cx * bxt), ty = (cf.ny + byt * R - 1) / (byt * R);
     const dim3 gv = G.shot_fast ? dim3(tx * S, ty, 1) : dim3(tx, ty, S);
-    launch_velocity(G, step_wave(c), c->M, c->nd, vw, R, ac, gv, st);
+    launch_velocity(G, W, c->M, c->nd, vw, R, narrow, ac, gv, st);
 }
 
 // 4th-order time stepping has no autotuning: four cells per thread in both
@@ -626,7 +633,7 @@ static void launch_fused(sofi_ctx *c, const Geo &G, cudaStream_t st)
 // the process. SOFI_VROWS / SOFI_SW fix a choice.
 struct Tuned {
     int vw, vrows, sw;
-    bool vpipe, fused;
+    bool vpipe, vnarrow, snarrow;
 };
 std::mutex g_tune_mu;
 std::map<std::string, Tuned> g_tune;
@@ -675,9 +682,10 @@ int autotune(sofi_ctx *c)
         auto it = g_tune.find(key);
         if (it != g_tune.end()) {
             if (!c->tune_fixed)
-                c->vw = it->second.vw, c->vrows = it->second.vrows, c->vpipe = it->second.vpipe;
+                c->vw = it->second.vw, c->vrows = it->second.vrows, c->vpipe = it->second.vpipe,
+                c->vnarrow = it->second.vnarrow;
             if (tune_s)
-                c->sw = it->second.sw;
+                c->sw = it->second.sw, c->snarrow = it->second.snarrow;
             c->graph_dirty = true;
             return 0;
         }
@@ -686,7 +694,7 @@ int autotune(sofi_ctx *c)
         return 0;  // state not known to be zero: keep the default variants
     Geo G = c->G;
     G.step_ctr = nullptr;  // tuning launches are not steps
-    Tuned pick{c->vw, c->vrows, c->sw, c->vpipe, false};
+    Tuned pick{c->vw, c->vrows, c->sw, c->vpipe, c->vnarrow, c->snarrow};
     float best = 1e30f, ms = 0.f;
     int rc;
     // two interleaved rounds over the candidates, each candidate's best time:
@@ -694,43 +702,55 @@ int autotune(sofi_ctx *c)
     // L2, which would otherwise penalise whichever candidate goes first
     constexpr int kRounds = 2;
     if (!c->tune_fixed) {
-        // {cells per thread, rows per thread, pipeline}; the acoustic update has no pipelined form
-        const int cand[4][3] = {{4, 1, 0}, {2, 1, 0}, {0, 1, 0}, {4, 1, 1}};
-        const int nc = (cf.weq == SOFI_AC_ISO || !c->vplan.segs) ? 3 : 4;
-        float t[4] = {1e30f, 1e30f, 1e30f, 1e30f};
+        // {cells per thread, rows per thread, pipeline, narrow blocks}; the acoustic
+        // update has neither the pipelined nor the narrow form
+        const bool ac = cf.weq == SOFI_AC_ISO;
+        const int all[5][4] = {{4, 1, 0, 0}, {2, 1, 0, 0}, {0, 1, 0, 0}, {4, 1, 0, 1}, {4, 1, 1, 0}};
+        int cand[5][4], nc = 0;
+        for (auto &cd : all)
+            if (!(ac && (cd[2] || cd[3])) && !(cd[2] && !c->vplan.segs))
+                std::copy(cd, cd + 4, cand[nc++]);
+        float t[5] = {1e30f, 1e30f, 1e30f, 1e30f, 1e30f};
         for (int r = 0; r < kRounds; r++)
             for (int k = 0; k < nc; k++) {
-                c->vw = cand[k][0], c->vrows = cand[k][1], c->vpipe = cand[k][2];
+                c->vw = cand[k][0], c->vrows = cand[k][1], c->vpipe = cand[k][2], c->vnarrow = cand[k][3];
                 if ((rc = time_launches(c, [&] { launch_v(c, G, c->stream); }, &ms)))
                     return rc;
                 t[k] = ms < t[k] ? ms : t[k];
             }
         for (int k = 0; k < nc; k++)
             if (t[k] < best)
-                best = t[k], pick.vw = cand[k][0], pick.vrows = cand[k][1], pick.vpipe = cand[k][2];
-        c->vw = pick.vw, c->vrows = pick.vrows, c->vpipe = pick.vpipe;
+                best = t[k], pick.vw = cand[k][0], pick.vrows = cand[k][1], pick.vpipe = cand[k][2],
+                pick.vnarrow = cand[k][3];
+        c->vw = pick.vw, c->vrows = pick.vrows, c->vpipe = pick.vpipe, c->vnarrow = pick.vnarrow;
     }
     if (tune_s) {
-        const int cand[3] = {4, 2, 0};
-        float t[3] = {1e30f, 1e30f, 1e30f};
+        // {cells per thread, narrow blocks}
+        const int cand[4][2] = {{4, 0}, {2, 0}, {0, 0}, {4, 1}};
+        const int nc = (kind != AC && narrow_s_applies(visco, visco ? c->G.L : 0, false)) ? 4 : 3;
+        float t[4] = {1e30f, 1e30f, 1e30f, 1e30f};
         for (int r = 0; r < kRounds; r++)
-            for (int k = 0; k < 3; k++) {
-                const int w = cand[k];
-                if ((rc = time_launches(
-                         c, [&] { launch_cell_s(G, step_wave(c), c->M, c->nd, kind, visco, w, cf.nx, cf.ny, cf.nshots, c->stream); },
-                         &ms)))
+            for (int k = 0; k < nc; k++) {
+                const int w = cand[k][0];
+                const bool nw = cand[k][1] != 0;
+                if ((rc = time_launches(c,
+                                        [&] {
+                                            launch_cell_s(G, step_wave(c), c->M, c->nd, kind, visco, w, nw, cf.nx,
+                                                          cf.ny, cf.nshots, c->stream);
+                                        },
+                                        &ms)))
                     return rc;
                 t[k] = ms < t[k] ? ms : t[k];
             }
         best = 1e30f;
-        for (int k = 0; k < 3; k++)
+        for (int k = 0; k < nc; k++)
             if (t[k] < best)
-                best = t[k], pick.sw = cand[k];
-        c->sw = pick.sw;
+                best = t[k], pick.sw = cand[k][0], pick.snarrow = cand[k][1] != 0;
+        c->sw = pick.sw, c->snarrow = pick.snarrow;
     }
     c->graph_dirty = true;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune[key] = Tuned{c->vw, c->vrows, c->sw, c->vpipe, c->fused};
+    g_tune[key] = Tuned{c->vw, c->vrows, c->sw, c->vpipe, c->vnarrow, c->snarrow};
     return 0;
 }
 
@@ -880,7 +900,8 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
     } else if (c->march && kind != AC) {
         launch_march_s(G, c->W, c->M, c->nd, kind, visco, c->march_sy, st);
     } else {
-        launch_cell_s(G, step_wave(c), c->M, c->nd, kind, visco, c->persist ? 4 : c->sw, cf.nx, cf.ny, S, st);
+        launch_cell_s(G, step_wave(c), c->M, c->nd, kind, visco, c->persist ? 4 : c->sw, c->snarrow && !c->persist,
+                      cf.nx, cf.ny, S, st);
     }
     c->launches++;
     if (timed)
@@ -1062,16 +1083,20 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
     if (const char *e = getenv("SOFI_VROWS"))
     {
         // SOFI_VROWS: "w4" / "w2" cells per thread in x, "t4" the TMA-fed pipeline
-        // (four cells per thread), "1" / "2" / "4" rows per thread
-        const bool wide = e[0] == 'w' || e[0] == 't';
+        // (four cells per thread), "n4" four cells on narrow blocks, "1" / "2" /
+        // "4" rows per thread
+        const bool wide = e[0] == 'w' || e[0] == 't' || e[0] == 'n';
         const int v = wide ? atoi(e + 1) : atoi(e);
         c->vw = wide ? (v == 2 && e[0] == 'w' ? 2 : 4) : 0;
         c->vpipe = e[0] == 't';
+        c->vnarrow = e[0] == 'n';
         c->vrows = (v == 2 || v == 4) ? v : 1;
         c->tune_fixed = true;
     }
-    if (const char *e = getenv("SOFI_SW")) {
-        c->sw = (atoi(e) == 2 || atoi(e) == 4) ? atoi(e) : 0;
+    if (const char *e = getenv("SOFI_SW")) {  // "4" / "2" / "0" cells per thread, "n4" four on narrow blocks
+        const int v = e[0] == 'n' ? 4 : atoi(e);
+        c->sw = (v == 2 || v == 4) ? v : 0;
+        c->snarrow = e[0] == 'n';
         c->sw_fixed = true;
     }
     if (const char *e = getenv("SOFI_MARCH_ROWS"))
@@ -1751,6 +1776,7 @@ int sofi_fwi_begin(sofi_ctx *c, int velocity, int adjoint_type, const float *vp,
     c->F.nt = cf.nt, c->F.velocity = velocity, c->F.adjoint = adjoint_type;
     // the kernels whose bodies write the gradient quantities, fixed for the pass
     c->vw = 4, c->vrows = 1, c->vpipe = false, c->sw = 4, c->persist = false, c->fused = false, c->tuned = true;
+    c->vnarrow = c->snarrow = false;
     c->fwi = true, c->fwi_back = false, c->graph_dirty = true;
     return 0;
 }
@@ -1817,7 +1843,7 @@ int sofi_fwi_backward(sofi_ctx *c, const float *adj_x, const float *adj_y)
     c->fwi_back = true, c->tuned = false;
     rc = autotune(c);
     const int bvw = c->vw, bvrows = c->vrows, bsw = c->sw;
-    const bool bvpipe = c->vpipe;
+    const bool bvpipe = c->vpipe, bvnarrow = c->vnarrow, bsnarrow = c->snarrow;
     c->fwi_back = false;
     if (rc)
         return rc;
@@ -1829,10 +1855,11 @@ int sofi_fwi_backward(sofi_ctx *c, const float *adj_x, const float *adj_y)
     auto backward_mode = [&](bool on) {
         if (on) {
             c->A.src_off = c->d_noacq, c->A.last_type = c->d_noacq, c->has_force = false;
-            c->vw = bvw, c->vrows = bvrows, c->sw = bsw, c->vpipe = bvpipe;
+            c->vw = bvw, c->vrows = bvrows, c->sw = bsw, c->vpipe = bvpipe, c->vnarrow = bvnarrow,
+            c->snarrow = bsnarrow;
         } else {
             c->A = saved, c->has_force = saved_force;
-            c->vw = 4, c->vrows = 1, c->sw = 4, c->vpipe = false;
+            c->vw = 4, c->vrows = 1, c->sw = 4, c->vpipe = false, c->vnarrow = c->snarrow = false;
         }
         c->fwi_back = on, c->graph_dirty = true;
     };

@@ -1,7 +1,8 @@
 """Batched shots: S resident shots advanced by one sofi_run give, shot for shot,
 the sections a single-shot context gives (same kernels, same arithmetic), for a
-shared model and for one model per shot, with the four-cell velocity kernel
-and with the TMA-fed velocity pipeline (whose tensor maps span all shots)."""
+shared model and for one model per shot, with the four-cell kernels on wide
+and on narrow blocks and with the TMA-fed velocity pipeline (whose tensor maps
+span all shots)."""
 import os
 
 import numpy as np
@@ -46,10 +47,11 @@ def _run(cfg, fields_per_model, vecs, shots, rec, shared):
     return out
 
 
-@pytest.mark.parametrize("vrows", ["w4", "t4"])
+@pytest.mark.parametrize("vrows", ["w4", "t4", "n4"])
 @pytest.mark.parametrize("name", ["el_cpml_fd8", "visc_cpml_fs_l3", "tti_cpml"])
 def test_batch_equals_single_shots(name, vrows, monkeypatch):
     monkeypatch.setenv("SOFI_VROWS", vrows)
+    monkeypatch.setenv("SOFI_SW", "n4" if vrows == "n4" else "4")
     o, cfg, fields, vecs, shots = _inputs(name, 5)
     rec = case_receivers(case_by_name(name), cfg)
     batched = _run(cfg, [fields], vecs, shots, rec, shared=True)
@@ -60,9 +62,10 @@ def test_batch_equals_single_shots(name, vrows, monkeypatch):
     o.close()
 
 
-@pytest.mark.parametrize("vrows", ["w4", "t4"])
+@pytest.mark.parametrize("vrows", ["w4", "t4", "n4"])
 def test_batch_with_a_model_per_shot(vrows, monkeypatch):
     monkeypatch.setenv("SOFI_VROWS", vrows)
+    monkeypatch.setenv("SOFI_SW", "n4" if vrows == "n4" else "4")
     o, cfg, fields, vecs, shots = _inputs("el_abs_fd10", 3)
     rec = case_receivers(case_by_name("el_abs_fd10"), cfg)
     models = [fields, {k: v * 1.01 if k in ("prip", "prjp") else v for k, v in fields.items()},
