@@ -622,7 +622,8 @@ def main():
                 "d2h_bytes_per_step": int(d2h_bytes)},
         "roofline": roof, "step_roofline": step_roof, "gpu_launches": int(launches),
         "autotune": {**dict(zip(["velocity_cells_per_thread", "velocity_rows_per_thread"], t.velocity_variant())),
-                     "velocity_pipelined": t.velocity_pipelined(), "stress_cells_per_thread": t.stress_variant()},
+                     "velocity_pipelined": t.velocity_pipelined(), "stress_cells_per_thread": t.stress_variant(),
+                     **dict(zip(["velocity_block_threads_x", "stress_block_threads_x"], t.block_threads_x()))},
         **({"batched": batched} if batched else {}),
         "clocks": clk.summary(),
     }

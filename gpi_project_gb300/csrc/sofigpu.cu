@@ -2003,6 +2003,19 @@ int sofi_velocity_pipelined(sofi_ctx *c, int *pipelined)
     return 0;
 }
 
+int sofi_block_threads_x(sofi_ctx *c, int *velocity, int *stress)
+{
+    if (!c || !velocity || !stress)
+        return fail(SOFI_E_ARG, "null argument");
+    const bool ac = c->cfg.weq == SOFI_AC_ISO, visco = is_visco(c->cfg.weq);
+    const int kind = kind_of(c->cfg.weq);
+    *velocity = (c->vnarrow && c->vw == 4 && !c->persist && !c->G.ab4 && !c->march && !c->vpipe &&
+                 narrow_v_applies(ac, false)) ? 8 : BX;
+    *stress = (c->snarrow && c->sw == 4 && !c->persist && !c->G.ab4 && !c->march && kind != AC && kind != TTI &&
+               narrow_s_applies(visco, visco ? c->G.L : 0, false)) ? 8 : BX;
+    return 0;
+}
+
 int sofi_stress_variant(sofi_ctx *c, int *cells_per_thread)
 {
     if (!c || !cells_per_thread)

@@ -178,6 +178,12 @@ class TimeLoop:
         N.check(self.lib.sofi_velocity_pipelined(self.h, ctypes.byref(a)))
         return bool(a.value)
 
+    def block_threads_x(self) -> tuple:
+        """Threads per block along x of the four-cell (velocity, stress) kernels: 32, or 8 for narrow blocks."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        N.check(self.lib.sofi_block_threads_x(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
     def stress_variant(self) -> int:
         """Cells per thread in x of the stress kernel."""
         a = ctypes.c_int()

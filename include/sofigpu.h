@@ -272,6 +272,12 @@ int sofi_velocity_pipelined(sofi_ctx *ctx, int *pipelined);
 /* Stress-kernel variant in use: cells per thread along x (1, 2 or 4; TTI: 1),
  * chosen by the same autotuning run; SOFI_SW=0|2|4 fixes it. */
 int sofi_stress_variant(sofi_ctx *ctx, int *cells_per_thread);
+/* Threads per block along x of the four-cell velocity and stress kernels in
+ * use: 32 (blocks of 32 x 8 threads, 128 columns by 8 rows) or 8 (8 x 32
+ * threads, 32 columns by 32 rows, which leave less of a block idle at the
+ * edge of a narrow grid); chosen by the same autotuning run, SOFI_VROWS=n4 /
+ * SOFI_SW=n4 fix the narrow form. */
+int sofi_block_threads_x(sofi_ctx *ctx, int *velocity, int *stress);
 /* Kernels launched by sofi_run since the context was created. */
 int sofi_launch_count(sofi_ctx *ctx, long long *launches);
 /* The context's CUDA stream (a cudaStream_t), for callers that order their own

@@ -27,3 +27,16 @@ def test_narrow_blocks_equal_wide_blocks(name, monkeypatch):
     for k in wide:
         np.testing.assert_array_equal(narrow[k], wide[k], err_msg=f"{name} {k}")
     o.close()
+
+
+def test_block_threads_reported(monkeypatch):
+    from gpi_project_gb300 import TimeLoop
+    from tests.helpers import gpu_config_from
+    case = case_by_name("el_cpml_fd8")
+    o = run_oracle_case(case, nthreads=os.cpu_count() or 1, nsteps=1)
+    for vr, sw, want in (("n4", "n4", (8, 8)), ("w4", "4", (32, 32)), ("n4", "4", (8, 32))):
+        monkeypatch.setenv("SOFI_VROWS", vr)
+        monkeypatch.setenv("SOFI_SW", sw)
+        with TimeLoop(gpu_config_from(o.cfg)) as t:
+            assert t.block_threads_x() == want, (vr, sw)
+    o.close()
