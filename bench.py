@@ -571,7 +571,7 @@ def main():
     traffic = traffic_from_profiles("update_s", W["name"])
     kname = {0: "k_update_s_ac (pressure)", 6: "k_tti_fused (TTI stress)", 7: "k_tti_fused (TTI stress + memory variables)"}
     if par.get("fdorder_time", 2) == 4:
-        kname = {par["weq"]: "k_update_s_ab4 (Adams-Bashforth stress, histories, memory variables)"}
+        kname = {par["weq"]: "k_update_s_ab4w (Adams-Bashforth stress, histories, memory variables)"}
     roof = {"kernel": kname.get(par["weq"], "k_update_sw / k_update_s (stress + memory variables)"), "bound": "hbm",
             "achieved": round(ach_s, 1) if ach_s else None, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
             "frac": round(ach_s / peak, 4) if ach_s else None,
