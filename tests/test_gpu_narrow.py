@@ -14,8 +14,11 @@ from tests.test_gpu_pdl import _run
 
 pytestmark = pytest.mark.gpu
 
+# tti_cpml: narrow velocity blocks beside the one-pass TTI stress kernel;
+# ac_cpml_fd8: no narrow form for acoustic media, n4 runs the wide kernels
 CASES = ["el_cpml_fd8", "el_abs_fd10", "el_cpml_fd12", "el_fs_abs_force", "el_fs_cpml", "visc_cpml_fs_l3",
-         "visc_abs_l1", "vti_cpml", "vvti_cpml_l2", "el_periodic_cpml", "el_mixed_sources"]
+         "visc_abs_l1", "vti_cpml", "vvti_cpml_l2", "el_periodic_cpml", "el_mixed_sources", "tti_cpml",
+         "ac_cpml_fd8"]
 
 
 @pytest.mark.parametrize("name", CASES)
