@@ -190,13 +190,20 @@ static void *worker_main(void *arg)
     while (!s->stop) {
         double now = sofi_server_clock(s), next = -1.0;
         req_t *pick = NULL;
+        double most = -1.0;
         for (int k = 0; k < s->n; k++) {
             req_t *q = s->reqs[k];
             if (q->state != SOFI_REQ_WAITING)
                 continue;
             if (q->arrival <= now) {
-                pick = q;
-                break;
+                if (!s->o.largest_first) {
+                    pick = q;
+                    break;
+                }
+                const double work = (double)q->r.par.nx * (double)q->r.par.ny * (double)q->r.par.nt;
+                if (work > most)
+                    most = work, pick = q;
+                continue;
             }
             if (next < 0.0 || q->arrival < next)
                 next = q->arrival;
