@@ -195,7 +195,10 @@ int sofi_kernel_time(sofi_ctx *ctx, const char *name, double *avg_ms, long long 
 /* Velocity-kernel variant in use: cells per thread along x (1, 2 or 4) and
  * rows per thread (1, 2 or 4). The first sofi_run after sofi_reset(ctx, -1)
  * times the variants on the zeroed arrays (where each leaves them zero) and
- * keeps the fastest for the grid shape; SOFI_VROWS=w4|w2|t4|1|2|4 fixes it. */
+ * keeps the fastest for the grid shape; SOFI_VROWS=w4|w2|t4|n4|1|2|4 fixes it
+ * (t4: the TMA-fed pipeline, which the timing run does not try; n4: four
+ * cells on narrow blocks, see sofi_block_threads_x). 4th-order time stepping
+ * is not timed: four cells per thread unless SOFI_VROWS asks for rows. */
 int sofi_velocity_variant(sofi_ctx *ctx, int *cells_per_thread, int *rows_per_thread);
 /* ---- FWI gradient pass of one shot (MODE = FWI, ITERMAX 1, DTINV 1) ------
  * Replaces the gradient part of the reference's inversion()
@@ -270,7 +273,8 @@ int sofi_set_pdl(sofi_ctx *ctx, int on);
  * else 0. */
 int sofi_velocity_pipelined(sofi_ctx *ctx, int *pipelined);
 /* Stress-kernel variant in use: cells per thread along x (1, 2 or 4; TTI: 1),
- * chosen by the same autotuning run; SOFI_SW=0|2|4 fixes it. */
+ * chosen by the same autotuning run; SOFI_SW=0|2|4|n4 fixes it (4th-order time
+ * stepping: four unless SOFI_SW=0). */
 int sofi_stress_variant(sofi_ctx *ctx, int *cells_per_thread);
 /* Threads per block along x of the four-cell velocity and stress kernels in
  * use: 32 (blocks of 32 x 8 threads, 128 columns by 8 rows) or 8 (8 x 32
