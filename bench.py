@@ -58,6 +58,24 @@ def dist_info():
     return rank, world, local
 
 
+def max_over_ranks(x: float, device: str = "cuda") -> float:
+    """The largest of every rank's x (a duration: the job ends with its slowest
+    replica); x itself when there is one rank."""
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank: float, world: int, seconds: float) -> float:
+    """Whole-job throughput of `world` replicas that each processed
+    units_per_rank, in the slowest one's `seconds` (weak scaling)."""
+    return units_per_rank * world / seconds
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons during the timed region."""
 
@@ -539,11 +557,8 @@ def main():
     ms_s, n_s = t.kernel_time("update_s")
     ms_v, n_v = t.kernel_time("update_v")
     t.set_kernel_timing(0)
-    if world > 1:
-        tt = torch.tensor([dev_ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        dev_ms = float(tt.item())
-    value = cells * args.steps * world / (dev_ms * 1e-3) / 1e9
+    dev_ms = max_over_ranks(dev_ms)
+    value = job_rate(cells * args.steps, world, dev_ms * 1e-3) / 1e9
 
     # ---- end to end through the C ABI: host buffers in, sections out ----
     ntr = len(W["rec"][0])
@@ -561,8 +576,8 @@ def main():
                 sec = t.section(c, shot=s)
                 d2h_bytes += sec.nbytes
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - w0
-    e2e_val = cells * args.steps * world / e2e_s / 1e9
+    e2e_s = max_over_ranks(time.perf_counter() - w0)
+    e2e_val = job_rate(cells * args.steps, world, e2e_s) / 1e9
     d2h_bytes //= max(args.steps, 1)
 
     # ---- roofline of the dominant kernel ----
