@@ -157,7 +157,10 @@ def host_par(W):
 
 
 def cpu_sample(W, nsteps, nthreads):
-    """Gcell-updates/s of the oracle on `nsteps` time steps of the workload grid."""
+    """Gcell-updates/s of the oracle on `nsteps` time steps of the workload grid,
+    timed after a few warm-up steps (the first touch of the freshly allocated
+    fields and the thread pool's start stay out of the sample, as the GPU's
+    warm-up steps do)."""
     from oracle import oracle as O
     par = W["par"]
     cfg = O.SofiConfig()
@@ -172,6 +175,9 @@ def cpu_sample(W, nsteps, nthreads):
     src = W["src"] if isinstance(W["src"], np.ndarray) else W["src"][0]
     o.set_sources(src, O.wavelet(1, cfg.nt, cfg.dt, src))
     o.set_receivers(*W["rec"])
+    warm = min(max(2, nsteps // 10), cfg.nt - nsteps)
+    if warm > 0:
+        o.run(warm)
     t0 = time.perf_counter()
     o.run(nsteps)
     dt = time.perf_counter() - t0
