@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=0, help="time steps of the CPU sample (0 = auto)")
     ap.add_argument("--served-requests", type=int, default=24,
                     help="requests of the served (c5) leg added to the line; 0 = none")
+    ap.add_argument("--batched-leg", default="c4",
+                    help="batched workload timed after the main line and added to it ('' = none)")
     ap.add_argument("--nt", type=int, default=0,
                     help="time steps per solve (default: the workload's NT; a small value keeps profiler captures short)")
     return ap.parse_args()
@@ -156,6 +158,78 @@ def host_par(W):
     return host.make_par(**W["par"])
 
 
+def working_set_bytes(W) -> float:
+    """Device bytes the workload's solves keep resident: the state arrays of
+    every shot and the per-cell coefficient arrays (CPML frames and
+    receivers not counted)."""
+    from gpi_project_gb300 import workloads
+    par = W["par"]
+    L = par.get("L", 0)
+    state = 5 + 3 * L
+    bpc = workloads.bytes_per_cell(par["weq"], L, par.get("fdorder_time", 2))["step"]
+    coeff = max(0, (bpc - 8 * state) // 4)
+    return 4.0 * par["nx"] * par["ny"] * (state * W["nshots"] + coeff)
+
+
+def config_of(W, world: int) -> dict:
+    """The `config` object of the line, the same for both arms."""
+    par = W["par"]
+    ws = working_set_bytes(W)
+    l2 = (f"inputs larger than L2 (resident working set ~{ws / 1e9:.2f} GB)" if ws > 129e6 else
+          f"working set ~{ws / 1e6:.0f} MB stays in L2 between steps (part of this workload)")
+    return {"workload": W["name"], "nx": par["nx"], "ny": par["ny"], "nt": par["nt"], "weq": par["weq"],
+            "fdorder": par["fdorder"], "L": par.get("L", 0), "fw": par["fw"], "shots": W["nshots"],
+            "free_surf": par.get("free_surf", 0), "receivers": len(W["rec"][0]), "l2": l2,
+            "parallelism": f"replicas x{world}"}
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return "unknown"
+
+
+def cpu_leg(args, workload: str) -> dict:
+    """cpu_baseline of the main line: the reference arm's own measurement
+    (`--impl reference`, all host threads), run as a fresh process before
+    this one loads CUDA or torch, so both readings come from the same code in
+    the same process state."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--workload", workload,
+           "--steps", "3", "--warmup", "1"]
+    if args.nt:
+        cmd += ["--nt", str(args.nt)]
+    if args.cpu_steps:
+        cmd += ["--cpu-steps", str(args.cpu_steps)]
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "LOCAL_WORLD_SIZE")}
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env, timeout=900)
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    if r.returncode or not lines:
+        raise SystemExit(f"CPU baseline leg failed (rc {r.returncode}): {r.stderr[-2000:]}")
+    return json.loads(lines[-1])["cpu_baseline"]
+
+
+def parity_record(workload: str):
+    """The error table of the GPU path against the float32 oracle and the
+    float64 arbiter at this workload's full size, as the config-parity GPU
+    test recorded it (profiles/parity_configs.json), or None."""
+    p = os.path.join(REPO, "profiles", "parity_configs.json")
+    try:
+        with open(p) as fh:
+            d = json.load(fh)[workload]
+    except (OSError, KeyError, ValueError):
+        return None
+    return {"source": "tests/test_gpu_xl_configs.py on GB300, recorded in profiles/parity_configs.json",
+            "nt": d["nt"], "full_nt": d["full_nt"], "shots_checked": d["shots_checked"],
+            "bar": {"rel_l2": 1e-4, "rel_max": 1e-3},
+            "errors_rel_l2_rel_max": {c: {p: [float(f"{x:.3g}") for x in v] for p, v in e.items()}
+                                      for c, e in d["errors"].items()}}
+
+
 def cpu_sample(W, nsteps, nthreads):
     """Gcell-updates/s of the oracle on `nsteps` time steps of the workload grid,
     timed after a few warm-up steps (the first touch of the freshly allocated
@@ -215,12 +289,15 @@ def run_reference(args, W):
     par = W["par"]
     line = {
         "impl": "reference", "metric": "Gcell-updates/s", "value": round(val, 4), "unit": "Gcell-updates/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * secs / args.steps, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": W["name"], "nx": par["nx"], "ny": par["ny"], "nt": par["nt"], "weq": par["weq"],
-                   "fdorder": par["fdorder"], "L": par.get("L", 0), "sample_time_steps": n},
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * secs / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded; gpi_project_gb300/workloads.py)",
+        "config": config_of(W, world),
         "cpu_baseline": {"value": round(val, 4), "unit": "Gcell-updates/s", "cores": nth, "kind": "port",
-                         "sample": f"{n} time steps of the {par['nx']}x{par['ny']} grid per step"},
+                         "cpu_model": cpu_model(), "spread": [round(min(rates), 4), round(max(rates), 4)],
+                         "sample": f"{n} time steps of the {par['nx']}x{par['ny']} grid per step, after "
+                                   f"{args.warmup} warm-up samples; first shot only"},
         "e2e": {"value": round(val, 4), "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -489,28 +566,19 @@ def main():
         run_reference(args, W)
         return
 
+    cpu_base = None
+    if not args.no_cpu_baseline and rank == 0:
+        cpu_base = cpu_leg(args, W["name"])
+
     import torch
-    from gpi_project_gb300 import TimeLoop, make_config, host
     torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
     par = W["par"]
-    p = host_par(W)
-    fields, vecs = host.prepare(p, W["mats"])
-    dt_max = float(vecs.pop("_dt_max")[0])
-    stable = int(vecs.pop("_stable")[0])
-    if not stable:
-        raise SystemExit(f"workload {W['name']} violates the stability bound (DT_max {dt_max})")
     nshots = W["nshots"]
-    cfg = make_config(weq=par["weq"], nx=par["nx"], ny=par["ny"], fdorder=par["fdorder"], fdorder_time=par.get("fdorder_time", 2),
-                      maxrelerror=par["maxrelerror"], L=par.get("L", 0), dt=par["dt"], dh=par["dh"], nt=par["nt"],
-                      fw=par["fw"], abs_type=par["abs_type"], free_surf=par.get("free_surf", 0), seismo=par["seismo"],
-                      ndt=par["ndt"], nshots=nshots, shared_model=1)
-    t = TimeLoop(cfg, device=local)
-    srcs = W["src"] if isinstance(W["src"], list) else [W["src"]]
-    sigs = [host.wavelet(1, par["nt"], par["dt"], s) for s in srcs]
+    t, fields, vecs, srcs, sigs = workloads.gpu_loop(W, device=local)
 
     # pinned host copies of every input, for the end-to-end leg
     def pinned(a):
@@ -528,7 +596,6 @@ def main():
             t.set_sources(srcs[s % len(srcs)], sigs[s % len(sigs)], shot=s)
             t.set_receivers(*W["rec"], shot=s)
 
-    upload_all()
     stream = torch.cuda.ExternalStream(t.stream_handle())
     cells = par["nx"] * par["ny"] * par["nt"] * nshots
 
@@ -604,30 +671,8 @@ def main():
                  "update_v_mean_ms": round(ms_v, 4), "update_s_mean_ms": round(ms_s, 4)}
     batched = None
     if nshots > 1:
-        # the same shots one at a time: a single-shot context on the same model
-        t1 = TimeLoop(make_config(weq=par["weq"], nx=par["nx"], ny=par["ny"], fdorder=par["fdorder"], fdorder_time=par.get("fdorder_time", 2),
-                                  maxrelerror=par["maxrelerror"], L=par.get("L", 0), dt=par["dt"], dh=par["dh"],
-                                  nt=par["nt"], fw=par["fw"], abs_type=par["abs_type"],
-                                  free_surf=par.get("free_surf", 0), seismo=par["seismo"], ndt=par["ndt"]),
-                      device=local)
-        t1.set_model(fields)
-        t1.set_vectors(vecs)
-        t1.set_sources(srcs[0], sigs[0])
-        t1.set_receivers(*W["rec"])
-        t1.reset()
-        t1.run()
-        torch.cuda.synchronize()
-        w1 = time.perf_counter()
-        nplain = 2
-        for _ in range(nplain):
-            t1.reset()
-            t1.run()
-        t1.synchronize()
-        plain_s = (time.perf_counter() - w1) / nplain
-        t1.close()
-        batched = {"shots": nshots, "shots_per_s": round(nshots * args.steps * world / (dev_ms * 1e-3), 3),
-                   "plain_shots_per_s": round(1.0 / plain_s, 3),
-                   "speedup_vs_plain": round(nshots * args.steps / (dev_ms * 1e-3) * plain_s, 3)}
+        batched = plain_vs_batched(W, local, fields, vecs, srcs, dev_ms / args.steps)
+        batched["shots_per_s"] = round(nshots * args.steps * world / (dev_ms * 1e-3), 3)
     if rank != 0:
         return
     out = {
@@ -635,33 +680,104 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded; gpi_project_gb300/workloads.py)",
-        "config": {"workload": W["name"], "nx": par["nx"], "ny": par["ny"], "nt": par["nt"], "weq": par["weq"],
-                   "fdorder": par["fdorder"], "L": par.get("L", 0), "fw": par["fw"], "shots": nshots,
-                   "free_surf": par.get("free_surf", 0), "receivers": ntr,
-                   "l2": "inputs larger than L2 (wavefield + model ~0.85 GB)", "parallelism": f"replicas x{world}"},
+        "config": config_of(W, world),
         "e2e": {"value": round(e2e_val, 4), "unit": "Gcell-updates/s", "h2d_bytes_per_step": int(h2d_bytes),
                 "d2h_bytes_per_step": int(d2h_bytes)},
         "roofline": roof, "step_roofline": step_roof, "gpu_launches": int(launches),
         "autotune": {**dict(zip(["velocity_cells_per_thread", "velocity_rows_per_thread"], t.velocity_variant())),
-                     "velocity_pipelined": t.velocity_pipelined(), "stress_cells_per_thread": t.stress_variant(),
+                     "stress_cells_per_thread": t.stress_variant(),
                      **dict(zip(["velocity_block_threads_x", "stress_block_threads_x"], t.block_threads_x()))},
         **({"batched": batched} if batched else {}),
         "clocks": clk.summary(),
     }
+    par_rec = parity_record(W["name"])
+    if par_rec:
+        out["parity"] = par_rec
+    t.close()
     if args.served_requests > 0 and world == 1:
-        t.close()
         with ClockSampler(local) as clk2:
             out["served"] = served_leg(args.served_requests, local)
         out["served"]["clocks"] = clk2.summary()
-    if not args.no_cpu_baseline and rank == 0:
-        n = args.cpu_steps or auto_cpu_steps(W)
-        from oracle import oracle as O
-        O.build()
-        r, s = cpu_sample(W, n, cpu_threads())
-        out["cpu_baseline"] = {"value": round(r, 4), "unit": "Gcell-updates/s", "cores": cpu_threads(),
-                               "kind": "port", "sample": f"{n} time steps of the {par['nx']}x{par['ny']} grid ({s:.1f} s)"}
+    if args.batched_leg and args.batched_leg != W["name"] and world == 1:
+        with ClockSampler(local) as clk3:
+            out["batched_" + args.batched_leg] = batched_leg(args.batched_leg, local)
+        out["batched_" + args.batched_leg]["clocks"] = clk3.summary()
+    if cpu_base:
+        out["cpu_baseline"] = cpu_base
     print(json.dumps(out), flush=True)
+
+
+def plain_vs_batched(W, device, fields, vecs, srcs, batched_ms):
+    """Shots/s of W's batched solve (one launch per kernel per step covers
+    every shot) against the same shots run one after another as plain
+    single-shot solves on the same GPU (the first shot's solve, timed twice
+    with CUDA events after one warm-up solve that also tunes)."""
+    import torch
+    from gpi_project_gb300 import workloads
+    W1 = dict(W, nshots=1, src=srcs[0])
+    t1, *_ = workloads.gpu_loop(W1, device=device, fields=fields, vecs=vecs)
+    stream = torch.cuda.ExternalStream(t1.stream_handle())
+    t1.reset()
+    t1.run()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nplain = 2
+    with torch.cuda.stream(stream):
+        ev0.record()
+    for _ in range(nplain):
+        t1.reset()
+        t1.run(sync=False)
+    with torch.cuda.stream(stream):
+        ev1.record()
+    t1.synchronize()
+    plain_ms = ev0.elapsed_time(ev1) / nplain
+    t1.close()
+    n = W["nshots"]
+    return {"shots": n, "shots_per_s": round(n / (batched_ms * 1e-3), 3),
+            "plain_shots_per_s": round(1.0 / (plain_ms * 1e-3), 3),
+            "speedup_vs_plain": round(n * plain_ms / batched_ms, 3),
+            "batched_ms_per_solve": round(batched_ms, 2), "plain_ms_per_shot": round(plain_ms, 2)}
+
+
+def batched_leg(name: str, device: int, warmup: int = 1, steps: int = 1) -> dict:
+    """Workload `name` (c4: 64 viscoelastic shots on 2000 x 1000, NT 4000) as a
+    batched solve: Gcell-updates/s and shots/s with inputs resident, the HBM
+    roofline of the whole step, and the gain over plain single-shot solves."""
+    import torch
+    from gpi_project_gb300 import workloads
+    W = workloads.workload(name)
+    par = W["par"]
+    t, fields, vecs, srcs, _ = workloads.gpu_loop(W, device=device)
+    stream = torch.cuda.ExternalStream(t.stream_handle())
+    for _ in range(warmup):
+        t.reset()
+        t.run(sync=False)
+    t.synchronize()
+    launches0 = t.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        ev0.record()
+    for _ in range(steps):
+        t.reset()
+        t.run(sync=False)
+    with torch.cuda.stream(stream):
+        ev1.record()
+    t.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    launches = t.launch_count() - launches0
+    variant = {"velocity_cells_per_thread": t.velocity_variant()[0], "stress_cells_per_thread": t.stress_variant(),
+               "block_threads_x": list(t.block_threads_x())}
     t.close()
+    cells = float(par["nx"]) * par["ny"] * par["nt"] * W["nshots"]
+    value = cells / (ms * 1e-3) / 1e9
+    bpc = workloads.bytes_per_cell(par["weq"], par.get("L", 0))["step"]
+    peak, peak_kind = measured_peaks()
+    out = {"config": config_of(W, 1), "gcell_per_s": round(value, 4), "steps": steps, "warmup": warmup,
+           "step_roofline": {"bytes_per_cell": bpc, "achieved": round(bpc * value, 1),
+                             "frac": round(bpc * value / peak, 4), "peak": peak, "peak_kind": peak_kind,
+                             "unit": "GB/s"},
+           "gpu_launches": int(launches), "autotune": variant}
+    out.update(plain_vs_batched(W, device, fields, vecs, srcs, ms))
+    return out
 
 
 if __name__ == "__main__":

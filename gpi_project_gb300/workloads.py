@@ -195,6 +195,41 @@ def workload(name: str) -> dict:
     return dict(name=name, par=par, mats=mats, src=src, rec=rec, nshots=nshots)
 
 
+def gpu_loop(W: dict, device: int = 0, fields=None, vecs=None):
+    """A TimeLoop holding workload W through the product path.
+
+    The model is prepared on the host by libsofihost (``sofih_prepare``, the
+    reference's prepmod / av_* / prepare_update_s_* / PML_pro set-up), the
+    wavelets by ``sofih_wavelet``; every shot gets its source and the common
+    receiver line. Variants are left to the autotuner. Returns the loop, the
+    prepared fields and vectors (for re-upload) and the per-shot sources and
+    signals."""
+    from . import host
+    from .timeloop import TimeLoop, make_config
+    par = W["par"]
+    if fields is None:
+        fields, vecs = host.prepare(host.make_par(**par), W["mats"])
+    vecs = dict(vecs)
+    dt_max = float(vecs.pop("_dt_max", [0.0])[0])
+    if not int(vecs.pop("_stable", [1])[0]):
+        raise ValueError(f"workload {W['name']} violates the stability bound (DT_max {dt_max})")
+    nshots = W["nshots"]
+    cfg = make_config(weq=par["weq"], nx=par["nx"], ny=par["ny"], fdorder=par["fdorder"],
+                      fdorder_time=par.get("fdorder_time", 2), maxrelerror=par["maxrelerror"], L=par.get("L", 0),
+                      dt=par["dt"], dh=par["dh"], nt=par["nt"], fw=par["fw"], abs_type=par["abs_type"],
+                      free_surf=par.get("free_surf", 0), seismo=par["seismo"], ndt=par["ndt"], nshots=nshots,
+                      shared_model=1)
+    t = TimeLoop(cfg, device=device)
+    srcs = W["src"] if isinstance(W["src"], list) else [W["src"]]
+    sigs = [host.wavelet(1, par["nt"], par["dt"], s) for s in srcs]
+    t.set_model(fields)
+    t.set_vectors(vecs)
+    for s in range(nshots):
+        t.set_sources(srcs[s % len(srcs)], sigs[s % len(sigs)], shot=s)
+        t.set_receivers(*W["rec"], shot=s)
+    return t, fields, vecs, srcs, sigs
+
+
 # Algorithmic bytes per cell-update (each evolving state array read and written
 # once, each per-cell coefficient array read once; CPML frame memory, sources
 # and receivers not credited).
