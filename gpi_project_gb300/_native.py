@@ -103,10 +103,6 @@ def load():
         "sofi_launch_count": ([vp, P(ctypes.c_longlong)], ctypes.c_int),
         "sofi_velocity_variant": ([vp, P(ctypes.c_int), P(ctypes.c_int)], ctypes.c_int),
         "sofi_stress_variant": ([vp, P(ctypes.c_int)], ctypes.c_int),
-        "sofi_velocity_pipelined": ([vp, P(ctypes.c_int)], ctypes.c_int),
-        "sofi_persistent": ([vp, P(ctypes.c_int), P(ctypes.c_int)], ctypes.c_int),
-        "sofi_fused": ([vp, P(ctypes.c_int)], ctypes.c_int),
-        "sofi_set_fused": ([vp, ctypes.c_int], ctypes.c_int),
         "sofi_pdl": ([vp, P(ctypes.c_int)], ctypes.c_int),
         "sofi_block_threads_x": ([vp, P(ctypes.c_int), P(ctypes.c_int)], ctypes.c_int),
         "sofi_set_pdl": ([vp, ctypes.c_int], ctypes.c_int),
@@ -115,7 +111,6 @@ def load():
         "sofi_fwi_backward": ([vp, P(ctypes.c_float), P(ctypes.c_float)], ctypes.c_int),
         "sofi_fwi_gradients": ([vp, P(ctypes.c_float), P(ctypes.c_float), P(ctypes.c_float)], ctypes.c_int),
         "sofi_fwi_checkpoints": ([vp, P(ctypes.c_int), P(ctypes.c_int)], ctypes.c_int),
-        "sofi_set_persistent": ([vp, ctypes.c_int], ctypes.c_int),
         "sofi_get_stream": ([vp, P(vp)], ctypes.c_int),
         "sofi_tti_stress_noalloc": ([P(SofiConfig), P(TtiStressArgs), vp], ctypes.c_int),
     }

@@ -395,11 +395,6 @@ static int make_resident(sofi_server *s, req_t *q)
         return rc;
     /* solves share the GPU: no blocks parked waiting for their predecessor */
     rc = sofi_set_pdl(q->ctx, 0);
-    if (s->o.persistent && !rc) {
-        int on = 0, blocks = 0;
-        if ((rc = sofi_persistent(q->ctx, &on, &blocks)) == 0 && blocks && !on)
-            rc = sofi_set_persistent(q->ctx, 1);
-    }
     for (int k = 0; k < sofih_prep_num_fields(q->prep) && !rc; k++)
         rc = sofi_set_model_field(q->ctx, 0, sofih_prep_field_name(q->prep, k), sofih_prep_field(q->prep, k),
                                   q->cfg.nx, 1);

@@ -6,9 +6,6 @@
 //                  R rows per thread), CPML / damping frame by predicate
 //                  (update_v_interior.c, update_v_PML.c, update_v_abs.c); advances
 //                  the device step counter
-//   k_update_vt    the same velocity update fed by TMA copies of the stress tiles
-//                  into a ring of shared-memory stages, marching down column
-//                  strips (sofi_vpipe.cuh)
 //   k_wrap_x       periodic x only: ghost columns (exchange_v.c / exchange_s.c, one rank)
 //   k_update_sw    ISO / VTI stress update, 2 or 4 cells per thread (k_update_s: one
 //                  cell), velocity derivatives recomputed from v in registers
@@ -97,7 +94,6 @@ struct Geo {
     int shot_fast;          // block index: shot varies fastest (model tiles shared in L2)
     int seismo, ndt;        // sampling (gv->SEISMO, gv->NDT)
     int *step_ctr;          // device: time steps completed; the velocity kernel advances it
-    int *fault;             // device: bits set by a pipelined kernel whose bounded wait gave up
     // TTI CPML memory of the velocity derivatives in two buffers (psi_pp = 1):
     // step n reads buffer (n - 1) & 1 and writes buffer n & 1; the second
     // buffer starts psi_xsz / psi_ysz floats after the first
@@ -146,15 +142,6 @@ struct FwiDev {
     int ncell, ntr, nt, velocity, adjoint;
 };
 
-// Launch arguments of the persistent step kernel (sofi_persist.cuh).
-struct PersistArgs {
-    int nsteps;
-    int has_force;
-    unsigned vg[3];   // velocity tiles: the plain launch's grid (x, y, z)
-    unsigned sg[3];   // stress tiles
-    unsigned *bar;    // [0] arrivals, [1] generation
-};
-
 // Prepared model arrays (one per shot or shared) and 1-D vectors.
 struct Model {
     const float *prip, *prjp;
@@ -193,7 +180,7 @@ __device__ __forceinline__ long long cell(const Geo &G, int j, int i)
 // Tile column and shot of this block. With a shared model and several shots
 // the shot varies fastest in blockIdx.x, so the blocks that run together read
 // the same model tile and only the first of them fetches it from DRAM.
-// `b` is blockIdx for a plain launch, or a persistent kernel's tile.
+// `b` is the block index.
 __device__ __forceinline__ void block_xs(const Geo &G, const uint3 &b, int &bx, int &s)
 {
     if (G.shot_fast) {

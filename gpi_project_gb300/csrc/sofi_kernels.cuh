@@ -149,19 +149,16 @@ __global__ void __launch_bounds__(BX *BY, R == 1 ? 8 : 1) k_update_v(Geo G, Wave
 // (< pitch for VW = 2; for VW = 4 possibly the next row's first columns); the
 // values past column NX + ND only feed cells past NX, which are never stored.
 // Rows j - ND .. j + ND stay inside the HY ghost rows.
-// COH: the array changes while the kernel runs (a persistent kernel's later
-// phase writes it), so the load bypasses L1 (ld.global.cg) instead of going
-// through the read-only path.
-template <int VW, bool COH = false>
+template <int VW>
 __device__ __forceinline__ void ldv(const float *p, float *out)
 {
     if (VW == 1) {
-        out[0] = COH ? __ldcg(p) : __ldg(p);
+        out[0] = __ldg(p);
     } else if (VW == 4) {
-        const float4 a = COH ? __ldcg(reinterpret_cast<const float4 *>(p)) : __ldg(reinterpret_cast<const float4 *>(p));
+        const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
         out[0] = a.x, out[1] = a.y, out[2] = a.z, out[3] = a.w;
     } else {
-        const float2 a = COH ? __ldcg(reinterpret_cast<const float2 *>(p)) : __ldg(reinterpret_cast<const float2 *>(p));
+        const float2 a = __ldg(reinterpret_cast<const float2 *>(p));
         out[0] = a.x, out[1] = a.y;
     }
 }
@@ -281,7 +278,7 @@ __device__ __forceinline__ void v_finish(const Geo &G, const Wave &W, const Mode
 // The stress derivatives of VW adjacent cells for the velocity update
 // (op_v_fdN, initfd.c:97-183, unscaled): ld(f, dy, dx, out) loads VW values
 // of sxx (f = 0), sxy (1) or syy (2) at row j + dy, columns i + dx ..
-// i + dx + VW - 1. The fused step kernel uses it; vw_tile writes the same
+// i + dx + VW - 1. The 4th-order kernels use it; vw_tile writes the same
 // expressions out inline (through a loader they cost the 64-register
 // four-cell kernel a spill).
 template <int ND, int VW, bool SXY, class LD>
@@ -343,7 +340,7 @@ __device__ __forceinline__ void v_derivs(const Geo &G, LD ld, float *sxx_x, floa
 // TBX: threads of a block in x (BX, or 8 for narrow grids: 32 columns by 32
 // rows per block of four-cell threads, so a 400-cell row leaves 4 % of the
 // last block idle instead of 22 %).
-template <int ND, int VW, bool SXY, bool COH, bool FWI = false, int TBX = BX>
+template <int ND, int VW, bool SXY, bool FWI = false, int TBX = BX>
 __device__ __forceinline__ void vw_tile(const Geo &G, const Wave &W, const Model &M, const uint3 b)
 {
     constexpr int K = (ND + VW - 1) / VW;
@@ -369,9 +366,9 @@ __device__ __forceinline__ void vw_tile(const Geo &G, const Wave &W, const Model
         float X[NXS], Y[NXS];  // X[k] = sxx(j, i - VW K + k), Y[k] = sxy(j, i - VW K + k)
 #pragma unroll
         for (int q = 0; q < 2 * K + 1; q++) {
-            ldv<VW, COH>(sxx + o + VW * (q - K), X + VW * q);
+            ldv<VW>(sxx + o + VW * (q - K), X + VW * q);
             if (SXY)
-                ldv<VW, COH>(sxy + o + VW * (q - K), Y + VW * q);
+                ldv<VW>(sxy + o + VW * (q - K), Y + VW * q);
         }
         constexpr int C = VW * K;  // index of column i
 #pragma unroll
@@ -390,8 +387,8 @@ __device__ __forceinline__ void vw_tile(const Geo &G, const Wave &W, const Model
         // y stencils: sxy rows j - ND .. j + ND - 1, syy rows j - ND + 1 .. j + ND
         float a1[VW], a0[VW], b1[VW], b0[VW];
         if (SXY)
-            ldv<VW, COH>(sxy + o, a1), ldv<VW, COH>(sxy + o - P, a0);
-        ldv<VW, COH>(syy + o + P, b1), ldv<VW, COH>(syy + o, b0);
+            ldv<VW>(sxy + o, a1), ldv<VW>(sxy + o - P, a0);
+        ldv<VW>(syy + o + P, b1), ldv<VW>(syy + o, b0);
 #pragma unroll
         for (int c = 0; c < VW; c++) {
             sxy_y[c] = SXY ? hc[1] * (a1[c] - a0[c]) : 0.f;
@@ -400,8 +397,8 @@ __device__ __forceinline__ void vw_tile(const Geo &G, const Wave &W, const Model
 #pragma unroll
         for (int m = 2; m <= ND; m++) {
             if (SXY)
-                ldv<VW, COH>(sxy + o + (m - 1) * P, a1), ldv<VW, COH>(sxy + o - m * P, a0);
-            ldv<VW, COH>(syy + o + m * P, b1), ldv<VW, COH>(syy + o - (m - 1) * P, b0);
+                ldv<VW>(sxy + o + (m - 1) * P, a1), ldv<VW>(sxy + o - m * P, a0);
+            ldv<VW>(syy + o + m * P, b1), ldv<VW>(syy + o - (m - 1) * P, b0);
 #pragma unroll
             for (int c = 0; c < VW; c++) {
                 if (SXY)
@@ -425,7 +422,7 @@ template <int ND, int VW, bool SXY = true, bool FWI = false, int TBX = BX>
 __global__ void __launch_bounds__(BX *BY, VW == 4 ? 4 : 1) k_update_vw(Geo G, Wave W, Model M)
 {
     pdl_begin();
-    vw_tile<ND, VW, SXY, false, FWI, TBX>(G, W, M, blockIdx);
+    vw_tile<ND, VW, SXY, FWI, TBX>(G, W, M, blockIdx);
 }
 
 // Periodic x (BOUNDARY = 1): ghost columns copy the opposite edge, as the one-
@@ -762,7 +759,7 @@ __device__ __forceinline__ void s_update(const Geo &G, const Wave &Wr, const Wav
     }
 }
 
-template <int ND, int KIND, bool VISCO, int LT, int VW, bool COH, bool FWI = false, int TBX = BX>
+template <int ND, int KIND, bool VISCO, int LT, int VW, bool FWI = false, int TBX = BX>
 __device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model &M, const uint3 b)
 {
     constexpr int TBY = BX * BY / TBX;  // TBX: as in vw_tile
@@ -779,7 +776,7 @@ __device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model
     const float *__restrict__ vy = W.vy + so;
     float vxx[VW], vyx[VW], vxy[VW], vyy[VW];
     s_derivs<ND, VW>(
-        G, [&](int f, int dy, int dx, float *out) { ldv<VW, COH>((f ? vy : vx) + o + dy * P + dx, out); }, vxx, vyx,
+        G, [&](int f, int dy, int dx, float *out) { ldv<VW>((f ? vy : vx) + o + dy * P + dx, out); }, vxx, vyx,
         vxy, vyy);
     s_update<ND, KIND, VISCO, LT, VW, FWI>(G, W, W, M, s, i, j, o, mo, vxx, vyx, vxy, vyy);
 }
@@ -788,7 +785,7 @@ template <int ND, int KIND, bool VISCO, int LT, int VW, bool FWI = false, int TB
 __global__ void __launch_bounds__(BX *BY, VW == 4 ? 2 : 1) k_update_sw(Geo G, Wave W, Model M)
 {
     pdl_begin();
-    sw_tile<ND, KIND, VISCO, LT, VW, false, FWI, TBX>(G, W, M, blockIdx);
+    sw_tile<ND, KIND, VISCO, LT, VW, FWI, TBX>(G, W, M, blockIdx);
 }
 
 // Acoustic stress update (wavefield_update_s_ac.c, update_s_acoustic_{interior,
@@ -798,7 +795,7 @@ __global__ void __launch_bounds__(BX *BY, VW == 4 ? 2 : 1) k_update_sw(Geo G, Wa
 // the same array for its x and y derivatives. CPML stretches vxx in the left /
 // right frame and vyy in the top / bottom frame (cpml_update_s_x_ac,
 // cpml_update_s_y_ac); the damping frame multiplies p once (abs_update_s_ac2).
-template <int ND, int VW, bool COH>
+template <int ND, int VW>
 __device__ __forceinline__ void sac_tile(const Geo &G, const Wave &W, const Model &M, const uint3 b)
 {
     constexpr int K = (ND + VW - 1) / VW;
@@ -821,7 +818,7 @@ __device__ __forceinline__ void sac_tile(const Geo &G, const Wave &W, const Mode
         float X[NXS];  // X[k] = vx(j, i - VW K + k)
 #pragma unroll
         for (int q = 0; q < 2 * K + 1; q++)
-            ldv<VW, COH>(vx + o + VW * (q - K), X + VW * q);
+            ldv<VW>(vx + o + VW * (q - K), X + VW * q);
         constexpr int C = VW * K;
 #pragma unroll
         for (int c = 0; c < VW; c++) {
@@ -833,13 +830,13 @@ __device__ __forceinline__ void sac_tile(const Geo &G, const Wave &W, const Mode
     }
     {
         float b1[VW], b0[VW];  // vy rows j - ND .. j + ND - 1
-        ldv<VW, COH>(vy + o, b1), ldv<VW, COH>(vy + o - P, b0);
+        ldv<VW>(vy + o, b1), ldv<VW>(vy + o - P, b0);
 #pragma unroll
         for (int c = 0; c < VW; c++)
             vyy[c] = hc[1] * (b1[c] - b0[c]);
 #pragma unroll
         for (int m = 2; m <= ND; m++) {
-            ldv<VW, COH>(vy + o + (m - 1) * P, b1), ldv<VW, COH>(vy + o - m * P, b0);
+            ldv<VW>(vy + o + (m - 1) * P, b1), ldv<VW>(vy + o - m * P, b0);
 #pragma unroll
             for (int c = 0; c < VW; c++)
                 vyy[c] += hc[m] * (b1[c] - b0[c]);
@@ -894,7 +891,7 @@ template <int ND, int VW>
 __global__ void __launch_bounds__(BX *BY) k_update_s_ac(Geo G, Wave W, Model M)
 {
     pdl_begin();
-    sac_tile<ND, VW, false>(G, W, M, blockIdx);
+    sac_tile<ND, VW>(G, W, M, blockIdx);
 }
 
 // ------------------------------------------------------------------ TTI

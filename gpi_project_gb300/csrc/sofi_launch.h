@@ -1,7 +1,6 @@
 // sofi_launch.h -- host launchers of kernels compiled in other translation
 // units (so that the template instantiations compile in parallel).
 #pragma once
-#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace sofi {
@@ -9,7 +8,6 @@ struct Geo;
 struct Wave;
 struct Model;
 struct Acq;
-struct PersistArgs;
 struct FwiDev;
 // FWI gradient pass (sofi_fwi.cu): forward storage after a step; adjoint
 // injection and the density term before the velocity update; the lambda /
@@ -18,40 +16,11 @@ void launch_fwi_coef(int n, const FwiDev &F, cudaStream_t st);  // the model-onl
 void launch_fwi_store(const Geo &G, const Wave &W, const FwiDev &F, cudaStream_t st);
 void launch_fwi_backward_pre(const Geo &G, const Wave &W, const FwiDev &F, cudaStream_t st);
 void launch_fwi_conv(const Geo &G, const Wave &W, const Model &M, const FwiDev &F, cudaStream_t st);
-// The persistent step kernel of ISO / VTI / acoustic media (sofi_persist.cuh;
-// instantiated beside the stress kernels of each kind): how many of its blocks
-// fit the GPU at once, and a cooperative launch of `blocks` of them.
-template <int KIND, bool VISCO>
-int persist_capacity_kv(int nd, int L, int device);
-// The fused velocity + stress step (sofi_fused.cuh, ISO / VTI): reads the
-// current buffers Wc, writes v, s and the velocity CPML memory to Wn.
-template <int KIND, bool VISCO>
-void launch_fused_kv(const Geo &G, const Wave &Wc, const Wave &Wn, const Model &M, int nd, cudaStream_t st);
-template <int KIND, bool VISCO>
-cudaError_t launch_persist_kv(const Geo &G, const Wave &W, const Model &M, const Acq &A, int nd,
-                              const PersistArgs &P, int blocks, cudaStream_t st);
-// velocity update, y-marching (any WEQ): rows per block `sy`
-void launch_march_v(const Geo &G, const Wave &W, const Model &M, int nd, int sy, cudaStream_t st);
-// stress update of isotropic / VTI media, y-marching
-void launch_march_s(const Geo &G, const Wave &W, const Model &M, int nd, int kind, bool visco, int sy,
-                    cudaStream_t st);
 // velocity update: vw cells per thread in x (4 or 2), else vrows rows per thread (1, 2, 4);
 // narrow (vw 4, not acoustic): blocks of 8 x 32 threads, 32 columns by 32 rows (grid sized for that);
 // acoustic: no sxy terms, vw 4, 2 or else one cell per thread
 void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw, int vrows, bool narrow, bool acoustic,
                      dim3 grid, cudaStream_t st);
-// The TMA-fed velocity pipeline (k_update_vt): tensor maps of sxx / sxy / syy
-// over all shots' padded fields, and the number of row segments per strip
-// that fills the GPU's resident blocks once.
-struct VtPlan {
-    CUtensorMap xx, xy, yy;
-    int segs = 0;      // 0: the pipeline is not available for this context
-    int strips = 0;
-};
-// 0, or a message (static storage) naming what failed
-const char *plan_velocity_pipeline(const Geo &G, const Wave &W, int nd, int device, VtPlan *plan);
-void launch_velocity_pipeline(const Geo &G, const Wave &W, const Model &M, int nd, const VtPlan &plan,
-                              cudaStream_t st);
 // Where the narrow four-cell blocks (8 x 32 threads, 32 columns by 32 rows)
 // exist: the velocity update of non-acoustic media and the ISO / VTI stress
 // update of elastic media or L <= 3, neither on an FWI forward step. The

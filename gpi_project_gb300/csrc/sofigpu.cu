@@ -185,15 +185,8 @@ struct sofi_ctx {
     int step = 0;
     float last_ms = 0.f;
     bool run_pending = false;  // ev0/ev1 recorded by a sofi_run not yet synchronised
-    bool march = false;        // y-marching kernels (ISO/VTI stress, all velocity updates)
     int vw = 4;                // velocity kernel: cells per thread in x (4 or 2), 0 = vrows rows per thread
     int vrows = 1;             // rows per thread of the one-cell velocity kernel (1, 2 or 4)
-    bool vpipe = false;        // the TMA-fed velocity pipeline (needs vplan.segs > 0)
-    VtPlan vplan;              // its tensor maps and segments (segs 0: not available)
-    // persistent step kernel (k_persist): chunks of steps in one cooperative launch
-    bool persist = false;
-    int persist_blocks = 0;    // blocks per launch (0: not available for this configuration)
-    unsigned *d_bar = nullptr; // its grid barrier: arrivals, generation (after the status words)
     // FWI gradient pass of one shot (sofi_fwi_*; sofi_fwi.cu)
     bool fwi = false;          // the forward runs store the gradient quantities
     bool fwi_back = false;     // the backward run is being issued
@@ -225,19 +218,9 @@ struct sofi_ctx {
     bool use_graph = true;
     bool pdl = true;  // programmatic dependent launch of the step kernels (launch_pdl)
     bool graph_dirty = true;
-    cudaGraphExec_t graph_exec = nullptr;   // the step graph (fused mode: current buffers are the first set)
-    cudaGraphExec_t graph_exec1 = nullptr;  // fused mode, current buffers the second set
-    bool graph_ok[2] = {false, false};
+    cudaGraphExec_t graph_exec = nullptr;   // the step graph
+    bool graph_ok = false;
     long long graph_launches = 0;  // kernels per replay
-    // fused velocity + stress step (sofi_fused.cuh): v, s and the velocity CPML
-    // memory held twice; W is always the current set, W2 the other, swapped
-    // after every fused launch; parity says which allocation W holds
-    bool fused = false;
-    bool fused_fixed = false;  // SOFI_FUSED chose it
-    bool w2_ready = false;
-    Wave W2{};
-    int parity = 0;
-    int march_sy = 32;         // rows per block of the y-marching kernels
     bool tti_split = false;    // TTI: derivative fields through HBM (two kernels) instead of fused
     // snapshots
     int snap_nx = 0, snap_ny = 0, snap_total = 0, nsnap = 0;
@@ -256,12 +239,11 @@ struct sofi_ctx {
 
 static void drop_graphs(sofi_ctx *c)
 {
-    for (cudaGraphExec_t *g : {&c->graph_exec, &c->graph_exec1})
-        if (*g) {
-            cudaGraphExecDestroy(*g);
-            *g = nullptr;
-        }
-    c->graph_ok[0] = c->graph_ok[1] = false;
+    if (c->graph_exec) {
+        cudaGraphExecDestroy(c->graph_exec);
+        c->graph_exec = nullptr;
+    }
+    c->graph_ok = false;
 }
 
 namespace {
@@ -299,12 +281,6 @@ int count_snapshots(const sofi_config &c)
     return n;
 }
 
-bool fused_env_on()
-{
-    const char *e = getenv("SOFI_FUSED");
-    return e && atoi(e) != 0;
-}
-
 long long fields_bytes(const sofi_config &c)
 {
     long long pitch = pitch_for(c.nx), fsz = pitch * (c.ny + 2 * HY);
@@ -321,10 +297,6 @@ long long fields_bytes(const sofi_config &c)
     long long psi = (c.abs_type == 1 && c.fw > 0) ? (tti && !split ? 6 : 4) * ((long long)c.ny * fw2 + fw2 * c.nx) : 0;
     long long nmod = c.shared_model ? 1 : c.nshots;
     long long nfields = (long long)needed_fields(c).size();
-    // the fused step (opt-in, SOFI_FUSED=1 / sofi_set_fused) holds v, s and the
-    // velocity CPML memory twice
-    if (fused_env_on() && (kind_of(c.weq) == ISO || kind_of(c.weq) == VTI) && !ab && !c.boundary)
-        per_shot += 5, psi += psi / 2;
     long long bytes = 4 * (fsz * per_shot * c.nshots + psi * c.nshots + fsz * nfields * nmod);
     int nsnap = count_snapshots(c);
     if (nsnap) {
@@ -546,24 +518,15 @@ Wave step_wave(const sofi_ctx *c)
 // One time step. `capture`: being recorded into the step graph, so no host-
 // side step number exists (no timing events, no snapshot).
 // The velocity kernel in the context's variant: c->vw cells per thread in x
-// (2 or 4), else c->vrows rows per thread, the TMA-fed pipeline (c->vpipe)
-// or the y-marching kernel.
+// (2 or 4), else c->vrows rows per thread.
 void launch_v(sofi_ctx *c, const Geo &G, cudaStream_t st)
 {
     const sofi_config &cf = c->cfg;
     const int S = cf.nshots;
-    if (c->march) {
-        launch_march_v(G, c->W, c->M, c->nd, c->march_sy, st);
-        return;
-    }
     const bool ac = cf.weq == SOFI_AC_ISO;  // acoustic: one cell per thread when not vectorised
-    if (c->vpipe && c->vplan.segs && !ac && !c->persist) {
-        launch_velocity_pipeline(G, c->W, c->M, c->nd, c->vplan, st);
-        return;
-    }
-    const int vw = c->persist ? 4 : c->vw;  // the persistent kernel's steps run the four-cell bodies
+    const int vw = c->vw;
     const Wave W = step_wave(c);
-    const bool narrow = !c->persist && c->vnarrow && vw == 4 && narrow_v_applies(ac, W.fa_x != nullptr);
+    const bool narrow = c->vnarrow && vw == 4 && narrow_v_applies(ac, W.fa_x != nullptr);
     const int R = (vw || ac) ? 1 : c->vrows, cx = vw ? vw : 1, bxt = narrow ? 8 : BX, byt = BX * BY / bxt;
     const unsigned tx = (cf.nx + cx * bxt - 1) / (cx * bxt), ty = (cf.ny + byt * R - 1) / (byt * R);
     const dim3 gv = G.shot_fast ? dim3(tx * S, ty, 1) : dim3(tx, ty, S);
@@ -577,53 +540,6 @@ static bool ab4_wide_s(const sofi_ctx *c)
     return !(c->sw_fixed && c->sw == 0);
 }
 
-// The fused step applies to ISO / VTI media with second-order time stepping,
-// no periodic edge and none of the other step forms (y-marching, persistent,
-// FWI pass).
-static bool fused_applies(const sofi_ctx *c)
-{
-    const int kind = kind_of(c->cfg.weq);
-    return (kind == ISO || kind == VTI) && !c->G.ab4 && !c->cfg.boundary && !c->march && !c->persist && !c->fwi;
-}
-
-// The second buffer set: v, s and the velocity CPML memory of every shot.
-static int alloc_w2(sofi_ctx *c)
-{
-    if (c->w2_ready)
-        return 0;
-    Wave W2 = c->W;
-    const size_t f = (size_t)c->G.fsz * c->cfg.nshots * sizeof(float);
-    int rc;
-    for (float **p : {&W2.vx, &W2.vy, &W2.sxx, &W2.syy, &W2.sxy})
-        if ((rc = dalloc(c, (void **)p, f)))
-            return rc;
-    if (c->G.abs_type == 1) {
-        const size_t px = sizeof(float) * (size_t)c->cfg.nshots * c->cfg.ny * c->G.fw2;
-        const size_t py = sizeof(float) * (size_t)c->cfg.nshots * c->G.fw2 * c->cfg.nx;
-        for (float **p : {&W2.psi_sxx_x, &W2.psi_sxy_x})
-            if ((rc = dalloc(c, (void **)p, px)))
-                return rc;
-        for (float **p : {&W2.psi_syy_y, &W2.psi_sxy_y})
-            if ((rc = dalloc(c, (void **)p, py)))
-                return rc;
-    }
-    c->W2 = W2;
-    c->w2_ready = true;
-    return 0;
-}
-
-static void launch_fused(sofi_ctx *c, const Geo &G, cudaStream_t st)
-{
-    const int kind = kind_of(c->cfg.weq);
-    const bool visco = is_visco(c->cfg.weq);
-    if (kind == ISO)
-        visco ? launch_fused_kv<ISO, true>(G, c->W, c->W2, c->M, c->nd, st)
-              : launch_fused_kv<ISO, false>(G, c->W, c->W2, c->M, c->nd, st);
-    else
-        visco ? launch_fused_kv<VTI, true>(G, c->W, c->W2, c->M, c->nd, st)
-              : launch_fused_kv<VTI, false>(G, c->W, c->W2, c->M, c->nd, st);
-}
-
 // Autotuner of the velocity and (ISO / VTI) stress kernels. Which variant is
 // fastest depends on the grid: several cells per thread issue the fewest
 // loads but leave few blocks on a small grid. The candidates are timed (CUDA
@@ -633,7 +549,7 @@ static void launch_fused(sofi_ctx *c, const Geo &G, cudaStream_t st)
 // the process. SOFI_VROWS / SOFI_SW fix a choice.
 struct Tuned {
     int vw, vrows, sw;
-    bool vpipe, vnarrow, snarrow;
+    bool vnarrow, snarrow;
 };
 std::mutex g_tune_mu;
 std::map<std::string, Tuned> g_tune;
@@ -673,7 +589,7 @@ static bool narrow_useful(int nx)
 int autotune(sofi_ctx *c)
 {
     c->tuned = true;
-    if (c->march || c->G.ab4 || c->persist)
+    if (c->G.ab4)
         return 0;
     const sofi_config &cf = c->cfg;
     const int kind = kind_of(cf.weq);
@@ -690,8 +606,7 @@ int autotune(sofi_ctx *c)
         auto it = g_tune.find(key);
         if (it != g_tune.end()) {
             if (!c->tune_fixed)
-                c->vw = it->second.vw, c->vrows = it->second.vrows, c->vpipe = it->second.vpipe,
-                c->vnarrow = it->second.vnarrow;
+                c->vw = it->second.vw, c->vrows = it->second.vrows, c->vnarrow = it->second.vnarrow;
             if (tune_s)
                 c->sw = it->second.sw, c->snarrow = it->second.snarrow;
             c->graph_dirty = true;
@@ -702,7 +617,7 @@ int autotune(sofi_ctx *c)
         return 0;  // state not known to be zero: keep the default variants
     Geo G = c->G;
     G.step_ctr = nullptr;  // tuning launches are not steps
-    Tuned pick{c->vw, c->vrows, c->sw, c->vpipe, c->vnarrow, c->snarrow};
+    Tuned pick{c->vw, c->vrows, c->sw, c->vnarrow, c->snarrow};
     float best = 1e30f, ms = 0.f;
     int rc;
     // two interleaved rounds over the candidates, each candidate's best time:
@@ -710,28 +625,26 @@ int autotune(sofi_ctx *c)
     // L2, which would otherwise penalise whichever candidate goes first
     constexpr int kRounds = 2;
     if (!c->tune_fixed) {
-        // {cells per thread, rows per thread, pipeline, narrow blocks}. The TMA-fed
-        // pipeline has won on no grid measured and is left to SOFI_VROWS=t4;
-        // the acoustic update has no narrow form.
+        // {cells per thread, rows per thread, narrow blocks}; the acoustic update
+        // has no narrow form.
         const bool ac = cf.weq == SOFI_AC_ISO;
-        const int all[4][4] = {{4, 1, 0, 0}, {2, 1, 0, 0}, {0, 1, 0, 0}, {4, 1, 0, 1}};
-        int cand[4][4], nc = 0;
+        const int all[4][3] = {{4, 1, 0}, {2, 1, 0}, {0, 1, 0}, {4, 1, 1}};
+        int cand[4][3], nc = 0;
         for (auto &cd : all)
-            if (!(cd[3] && (ac || !narrow_useful(cf.nx))))
-                std::copy(cd, cd + 4, cand[nc++]);
+            if (!(cd[2] && (ac || !narrow_useful(cf.nx))))
+                std::copy(cd, cd + 3, cand[nc++]);
         float t[4] = {1e30f, 1e30f, 1e30f, 1e30f};
         for (int r = 0; r < kRounds; r++)
             for (int k = 0; k < nc; k++) {
-                c->vw = cand[k][0], c->vrows = cand[k][1], c->vpipe = cand[k][2], c->vnarrow = cand[k][3];
+                c->vw = cand[k][0], c->vrows = cand[k][1], c->vnarrow = cand[k][2];
                 if ((rc = time_launches(c, [&] { launch_v(c, G, c->stream); }, &ms)))
                     return rc;
                 t[k] = ms < t[k] ? ms : t[k];
             }
         for (int k = 0; k < nc; k++)
             if (t[k] < best)
-                best = t[k], pick.vw = cand[k][0], pick.vrows = cand[k][1], pick.vpipe = cand[k][2],
-                pick.vnarrow = cand[k][3];
-        c->vw = pick.vw, c->vrows = pick.vrows, c->vpipe = pick.vpipe, c->vnarrow = pick.vnarrow;
+                best = t[k], pick.vw = cand[k][0], pick.vrows = cand[k][1], pick.vnarrow = cand[k][2];
+        c->vw = pick.vw, c->vrows = pick.vrows, c->vnarrow = pick.vnarrow;
     }
     if (tune_s) {
         // {cells per thread, narrow blocks}
@@ -759,83 +672,7 @@ int autotune(sofi_ctx *c)
     }
     c->graph_dirty = true;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune[key] = Tuned{c->vw, c->vrows, c->sw, c->vpipe, c->vnarrow, c->snarrow};
-    return 0;
-}
-
-// Tiles of the four-cells-per-thread velocity and stress grids.
-static void tile_grid(const sofi_ctx *c, unsigned g[3])
-{
-    const unsigned tx = (c->cfg.nx + 4 * BX - 1) / (4 * BX), ty = (c->cfg.ny + BY - 1) / BY;
-    const unsigned S = c->cfg.nshots;
-    g[0] = c->G.shot_fast ? tx * S : tx, g[1] = ty, g[2] = c->G.shot_fast ? 1 : S;
-}
-
-// The persistent step kernel serves ISO / VTI / acoustic media with second-
-// order time stepping and no periodic edge, as many blocks as fit the GPU at
-// once (capped by the work of the widest phase). Where it is on, the plain
-// steps (snapshot and timed steps) use the same four-cell kernels. It is off
-// unless asked for: on a 400 x 400 grid a step costs 30 us in it against
-// 12.6 us for the captured graph of plain kernels (its grid barrier takes
-// 2.0-2.3 us, a graph's kernel boundary about 1 us, and each phase is a
-// chain of L2 round trips either way).
-constexpr int kPersistSteps = 128;  // steps per launch at most
-
-void plan_persist(sofi_ctx *c)
-{
-    const sofi_config &cf = c->cfg;
-    const int kind = kind_of(cf.weq);
-    const bool visco = is_visco(cf.weq);
-    c->persist = false, c->persist_blocks = 0;
-    if (kind == TTI || c->G.ab4 || c->march || cf.boundary)
-        return;
-    int cap = 0;
-    if (kind == AC)
-        cap = persist_capacity_kv<AC, false>(c->nd, 0, c->device);
-    else if (kind == ISO)
-        cap = visco ? persist_capacity_kv<ISO, true>(c->nd, c->G.L, c->device)
-                    : persist_capacity_kv<ISO, false>(c->nd, 0, c->device);
-    else
-        cap = visco ? persist_capacity_kv<VTI, true>(c->nd, c->G.L, c->device)
-                    : persist_capacity_kv<VTI, false>(c->nd, 0, c->device);
-    if (cap <= 0)
-        return;
-    unsigned g[3];
-    tile_grid(c, g);
-    const long long tiles = (long long)g[0] * g[1] * g[2];
-    const long long cols = ((long long)cf.nx * cf.nshots + BX * BY - 1) / (BX * BY);
-    const long long want = tiles > cols ? tiles : cols;
-    c->persist_blocks = (int)(want < cap ? want : cap);
-    if (const char *e = getenv("SOFI_PERSIST_BLOCKS"))  // fewer blocks per launch (1 .. capacity)
-        if (atoi(e) > 0 && atoi(e) < cap)
-            c->persist_blocks = atoi(e);
-    const char *e = getenv("SOFI_PERSIST");
-    c->persist = e && atoi(e) != 0;
-}
-
-int launch_persist(sofi_ctx *c, int nsteps)
-{
-    const sofi_config &cf = c->cfg;
-    const int kind = kind_of(cf.weq);
-    const bool visco = is_visco(cf.weq);
-    PersistArgs P;
-    P.nsteps = nsteps;
-    P.has_force = c->has_force ? 1 : 0;
-    tile_grid(c, P.vg);
-    tile_grid(c, P.sg);
-    P.bar = c->d_bar;
-    cudaError_t e;
-    if (kind == AC)
-        e = launch_persist_kv<AC, false>(c->G, c->W, c->M, c->A, c->nd, P, c->persist_blocks, c->stream);
-    else if (kind == ISO)
-        e = visco ? launch_persist_kv<ISO, true>(c->G, c->W, c->M, c->A, c->nd, P, c->persist_blocks, c->stream)
-                  : launch_persist_kv<ISO, false>(c->G, c->W, c->M, c->A, c->nd, P, c->persist_blocks, c->stream);
-    else
-        e = visco ? launch_persist_kv<VTI, true>(c->G, c->W, c->M, c->A, c->nd, P, c->persist_blocks, c->stream)
-                  : launch_persist_kv<VTI, false>(c->G, c->W, c->M, c->A, c->nd, P, c->persist_blocks, c->stream);
-    if (e != cudaSuccess)
-        return fail(SOFI_E_CUDA, "persistent step kernel: %s", cudaGetErrorString(e));
-    c->launches++;
+    g_tune[key] = Tuned{c->vw, c->vrows, c->sw, c->vnarrow, c->snarrow};
     return 0;
 }
 
@@ -875,17 +712,6 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
         c->tev_used += 3;
         CK(cudaEventRecord(e0, st));
     }
-    if (c->fused) {  // velocity and stress in one kernel (timed as the stress update); then the next buffers are current
-        if (timed)
-            CK(cudaEventRecord(e1, st));
-        launch_fused(c, G, st);
-        std::swap(c->W, c->W2);
-        c->parity ^= 1;
-        c->launches++;
-        if (timed)
-            CK(cudaEventRecord(e2, st));
-        goto post;
-    }
     if (G.ab4)
         launch_ab4_v(G, c->W, c->M, c->nd, c->vw != 0, grd, st);
     else
@@ -906,16 +732,12 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
         launch_tti_split(G, c->W, c->M, c->nd, visco, grd, st);
     } else if (kind == TTI) {
         launch_tti_fused(G, c->W, c->M, c->nd, visco, G.abs_type == 1, grd, st);
-    } else if (c->march && kind != AC) {
-        launch_march_s(G, c->W, c->M, c->nd, kind, visco, c->march_sy, st);
     } else {
-        launch_cell_s(G, step_wave(c), c->M, c->nd, kind, visco, c->persist ? 4 : c->sw, c->snarrow && !c->persist,
-                      cf.nx, cf.ny, S, st);
+        launch_cell_s(G, step_wave(c), c->M, c->nd, kind, visco, c->sw, c->snarrow, cf.nx, cf.ny, S, st);
     }
     c->launches++;
     if (timed)
         CK(cudaEventRecord(e2, st));
-post:
     dim3 pg((cf.nx + 127) / 128, S);
     if (kind == TTI)
         DISPATCH_ND(c->nd, (launch_pdl(k_post<ND, false, true>, pg, 128, 0, st, G, c->W, c->M, c->A)))
@@ -954,12 +776,9 @@ post:
 
 int check_status(sofi_ctx *c)
 {
-    std::vector<int> st(c->cfg.nshots + 2);  // shots, step counter, fault word
+    std::vector<int> st(c->cfg.nshots);
     CK(cudaMemcpyAsync(st.data(), c->d_status, sizeof(int) * st.size(), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    if (st[c->cfg.nshots + 1])
-        return fail(SOFI_E_CUDA, "velocity pipeline: a bounded shared-memory stage wait gave up (fault bits %#x)",
-                    st[c->cfg.nshots + 1]);
     for (int s = 0; s < c->cfg.nshots; s++)
         if (st[s])
             return fail(SOFI_E_UNSTABLE, "shot %d: simulation is unstable (NaN at the probe cell after step %d)", s,
@@ -1087,17 +906,13 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
     c->nd = cfg->fdorder / 2;
     c->nmodels = cfg->shared_model ? 1 : cfg->nshots;
     c->acq.resize(cfg->nshots);
-    if (const char *e = getenv("SOFI_KERNELS"))
-        c->march = strcmp(e, "march") == 0;
     if (const char *e = getenv("SOFI_VROWS"))
     {
-        // SOFI_VROWS: "w4" / "w2" cells per thread in x, "t4" the TMA-fed pipeline
-        // (four cells per thread), "n4" four cells on narrow blocks, "1" / "2" /
-        // "4" rows per thread
-        const bool wide = e[0] == 'w' || e[0] == 't' || e[0] == 'n';
+        // SOFI_VROWS: "w4" / "w2" cells per thread in x, "n4" four cells on
+        // narrow blocks, "1" / "2" / "4" rows per thread
+        const bool wide = e[0] == 'w' || e[0] == 'n';
         const int v = wide ? atoi(e + 1) : atoi(e);
         c->vw = wide ? (v == 2 && e[0] == 'w' ? 2 : 4) : 0;
-        c->vpipe = e[0] == 't';
         c->vnarrow = e[0] == 'n';
         c->vrows = (v == 2 || v == 4) ? v : 1;
         c->tune_fixed = true;
@@ -1108,8 +923,6 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
         c->snarrow = e[0] == 'n';
         c->sw_fixed = true;
     }
-    if (const char *e = getenv("SOFI_MARCH_ROWS"))
-        c->march_sy = atoi(e) > 0 ? atoi(e) : c->march_sy;
     if (const char *e = getenv("SOFI_TTI"))
         c->tti_split = strcmp(e, "split") == 0;
     e = cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, priority);
@@ -1208,37 +1021,14 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
             goto bad;
         *slot_ptr(c->M, n.c_str(), true) = p;
     }
-    if ((rc = dalloc(c, (void **)&c->d_status, sizeof(int) * (cfg->nshots + 4))))
+    if ((rc = dalloc(c, (void **)&c->d_status, sizeof(int) * (cfg->nshots + 1))))
         goto bad;
     c->G.step_ctr = c->d_status + cfg->nshots;  // zeroed with the status words
-    c->G.fault = c->d_status + cfg->nshots + 1;
-    c->d_bar = reinterpret_cast<unsigned *>(c->d_status + cfg->nshots + 2);
     if (const char *e = getenv("SOFI_GRAPH"))
         c->use_graph = atoi(e) != 0;
     if (const char *e = getenv("SOFI_PDL"))
         c->pdl = atoi(e) != 0;
     c->A.status = c->d_status;
-    // the TMA-fed velocity pipeline, offered to the autotuner where it applies
-    // (vplan.segs stays 0 where a tensor map or the launch shape is unavailable)
-    if (!G.ab4 && !c->march && cfg->weq != SOFI_AC_ISO) {
-        plan_velocity_pipeline(G, c->W, c->nd, device, &c->vplan);
-        // SOFI_VT_SEGS: row segments per strip (1 .. chunks of 8 rows), instead of one wave
-        if (const char *e = getenv("SOFI_VT_SEGS"))
-            if (c->vplan.segs && atoi(e) > 0) {
-                const int nck = (cfg->ny + 7) / 8;
-                c->vplan.segs = atoi(e) < nck ? atoi(e) : nck;
-            }
-    }
-    plan_persist(c);
-    // SOFI_FUSED=0|1: the fused velocity + stress step off / on (where it applies)
-    if (const char *e = getenv("SOFI_FUSED")) {
-        c->fused_fixed = true;
-        if (atoi(e) != 0 && fused_applies(c)) {
-            if ((rc = alloc_w2(c)))
-                goto bad;
-            c->fused = true;
-        }
-    }
     c->snap_total = count_snapshots(*cfg);
     if (c->snap_total) {
         c->snap_nx = (cfg->nx - 1) / cfg->idx + 1;
@@ -1427,7 +1217,7 @@ int sofi_reset(sofi_ctx *c, int shot)
             CK(cudaMemsetAsync(c->W.dcor + 4LL * s * c->G.fsz, 0, 4 * f, c->stream));
         }
     }
-    CK(cudaMemsetAsync(c->d_status, 0, sizeof(int) * (c->cfg.nshots + 4), c->stream));  // + counter, fault, barrier
+    CK(cudaMemsetAsync(c->d_status, 0, sizeof(int) * (c->cfg.nshots + 1), c->stream));  // + step counter
     if (c->d_sec && !c->acq_dirty) {
         size_t n = (size_t)c->total_rec * 5 * (c->A.ns > 0 ? c->A.ns : 1);
         CK(cudaMemsetAsync(c->d_sec, 0, n * sizeof(float), c->stream));
@@ -1453,12 +1243,10 @@ static bool chunk_has_event(const sofi_ctx *c, int first, int n)
     return false;
 }
 
-// Graph of kGraphSteps steps from the current buffer parity (an even number of
-// steps: the fused mode's swaps leave the parity where the capture began).
+// Graph of kGraphSteps steps.
 static int build_graph(sofi_ctx *c)
 {
-    const int slot = c->fused ? c->parity : 0;
-    cudaGraphExec_t &gx = slot ? c->graph_exec1 : c->graph_exec;
+    cudaGraphExec_t &gx = c->graph_exec;
     if (gx) {
         cudaGraphExecDestroy(gx);
         gx = nullptr;
@@ -1480,7 +1268,7 @@ static int build_graph(sofi_ctx *c)
         return fail(SOFI_E_CUDA, "graph instantiation: %s", cudaGetErrorString(e));
     c->graph_launches = c->launches - before;
     c->launches = before;
-    c->graph_ok[slot] = true;
+    c->graph_ok = true;
     return 0;
 }
 
@@ -1512,32 +1300,18 @@ int sofi_run(sofi_ctx *c, int nsteps)
     const bool ckpt_fwd = c->fwi && c->fwi_K && !c->fwi_back && !c->fwi_store_on;
     int left = nsteps;
     while (left > 0) {
-        if (c->persist) {
-            int k = 0;  // steps before the next snapshot or timed step
-            while (k < left && k < kPersistSteps && !chunk_has_event(c, c->step + 1 + k, 1))
-                k++;
-            if (k > 0) {
-                int rc = launch_persist(c, k);
-                if (rc)
-                    return rc;
-                c->step += k;
-                left -= k;
-                continue;
-            }
-        }
         const int lim = ckpt_fwd ? std::min(left, c->fwi_K - c->step % c->fwi_K) : left;
         if (c->use_graph && lim >= kGraphSteps && !chunk_has_event(c, c->step + 1, kGraphSteps)) {
             if (c->graph_dirty) {
                 drop_graphs(c);
                 c->graph_dirty = false;
             }
-            const int slot = c->fused ? c->parity : 0;
-            if (!c->graph_ok[slot]) {
+            if (!c->graph_ok) {
                 int rc = build_graph(c);
                 if (rc)
                     return rc;
             }
-            CK(cudaGraphLaunch(slot ? c->graph_exec1 : c->graph_exec, c->stream));
+            CK(cudaGraphLaunch(c->graph_exec, c->stream));
             c->launches += c->graph_launches;
             c->step += kGraphSteps;
             left -= kGraphSteps;
@@ -1650,7 +1424,7 @@ int sofi_velocity_variant(sofi_ctx *c, int *cells_per_thread, int *rows_per_thre
 {
     if (!c || !cells_per_thread || !rows_per_thread)
         return fail(SOFI_E_ARG, "null argument");
-    const int vw = c->persist ? 4 : c->vw;
+    const int vw = c->vw;
     *cells_per_thread = !vw ? 1 : c->G.ab4 ? 4 : vw;  // 4th order: four cells or one
     *rows_per_thread = (vw || c->G.ab4) ? 1 : c->vrows;
     return 0;
@@ -1705,7 +1479,7 @@ int sofi_fwi_begin(sofi_ctx *c, int velocity, int adjoint_type, const float *vp,
     if (!c || !vp || !vs || !rho)
         return fail(SOFI_E_ARG, "null argument");
     const sofi_config &cf = c->cfg;
-    if (cf.weq != SOFI_EL_ISO || cf.nshots != 1 || c->G.ab4 || c->march)
+    if (cf.weq != SOFI_EL_ISO || cf.nshots != 1 || c->G.ab4)
         return fail(SOFI_E_ARG, "FWI gradients need WEQ = EL_ISO, one shot, FDORDER_TIME = 2 and the plain kernels");
     if (cf.ndt != 1 || (cf.seismo != 1 && cf.seismo != 4))
         return fail(SOFI_E_ARG, "FWI gradients need NDT = 1 and vx / vy seismograms (SEISMO 1 or 4)");
@@ -1784,7 +1558,7 @@ int sofi_fwi_begin(sofi_ctx *c, int velocity, int adjoint_type, const float *vp,
     CK(cudaStreamSynchronize(c->stream));
     c->F.nt = cf.nt, c->F.velocity = velocity, c->F.adjoint = adjoint_type;
     // the kernels whose bodies write the gradient quantities, fixed for the pass
-    c->vw = 4, c->vrows = 1, c->vpipe = false, c->sw = 4, c->persist = false, c->fused = false, c->tuned = true;
+    c->vw = 4, c->vrows = 1, c->sw = 4, c->tuned = true;
     c->vnarrow = c->snarrow = false;
     c->fwi = true, c->fwi_back = false, c->graph_dirty = true;
     return 0;
@@ -1852,7 +1626,7 @@ int sofi_fwi_backward(sofi_ctx *c, const float *adj_x, const float *adj_y)
     c->fwi_back = true, c->tuned = false;
     rc = autotune(c);
     const int bvw = c->vw, bvrows = c->vrows, bsw = c->sw;
-    const bool bvpipe = c->vpipe, bvnarrow = c->vnarrow, bsnarrow = c->snarrow;
+    const bool bvnarrow = c->vnarrow, bsnarrow = c->snarrow;
     c->fwi_back = false;
     if (rc)
         return rc;
@@ -1864,11 +1638,10 @@ int sofi_fwi_backward(sofi_ctx *c, const float *adj_x, const float *adj_y)
     auto backward_mode = [&](bool on) {
         if (on) {
             c->A.src_off = c->d_noacq, c->A.last_type = c->d_noacq, c->has_force = false;
-            c->vw = bvw, c->vrows = bvrows, c->sw = bsw, c->vpipe = bvpipe, c->vnarrow = bvnarrow,
-            c->snarrow = bsnarrow;
+            c->vw = bvw, c->vrows = bvrows, c->sw = bsw, c->vnarrow = bvnarrow, c->snarrow = bsnarrow;
         } else {
             c->A = saved, c->has_force = saved_force;
-            c->vw = 4, c->vrows = 1, c->sw = 4, c->vpipe = false, c->vnarrow = c->snarrow = false;
+            c->vw = 4, c->vrows = 1, c->sw = 4, c->vnarrow = c->snarrow = false;
         }
         c->fwi_back = on, c->graph_dirty = true;
     };
@@ -1933,49 +1706,6 @@ int sofi_fwi_gradients(sofi_ctx *c, float *lam, float *mu, float *rhos)
     return 0;
 }
 
-int sofi_fused(sofi_ctx *c, int *on)
-{
-    if (!c || !on)
-        return fail(SOFI_E_ARG, "null argument");
-    *on = c->fused ? 1 : 0;
-    return 0;
-}
-
-int sofi_set_fused(sofi_ctx *c, int on)
-{
-    if (!c)
-        return fail(SOFI_E_ARG, "null context");
-    if (on && !fused_applies(c))
-        return fail(SOFI_E_STATE, "no fused step for this configuration");
-    CK(cudaSetDevice(c->device));
-    CK(cudaStreamSynchronize(c->stream));
-    if (on) {
-        int rc = alloc_w2(c);
-        if (rc)
-            return rc;
-    }
-    c->fused = on != 0;
-    c->fused_fixed = true;
-    c->graph_dirty = true;
-    return 0;
-}
-
-int sofi_set_persistent(sofi_ctx *c, int on)
-{
-    if (!c)
-        return fail(SOFI_E_ARG, "null context");
-    if (on && !c->persist_blocks)
-        return fail(SOFI_E_STATE, "no persistent step kernel for this configuration");
-    if (on && c->fwi)
-        return fail(SOFI_E_STATE, "the FWI gradient pass runs the plain kernels");
-    CK(cudaStreamSynchronize(c->stream));
-    c->persist = on != 0;
-    if (c->persist)
-        c->fused = false;
-    c->graph_dirty = true;
-    return 0;
-}
-
 int sofi_pdl(sofi_ctx *c, int *on)
 {
     if (!c || !on)
@@ -1995,32 +1725,14 @@ int sofi_set_pdl(sofi_ctx *c, int on)
     return 0;
 }
 
-int sofi_persistent(sofi_ctx *c, int *on, int *blocks)
-{
-    if (!c || !on || !blocks)
-        return fail(SOFI_E_ARG, "null argument");
-    *on = c->persist ? 1 : 0;
-    *blocks = c->persist_blocks;
-    return 0;
-}
-
-int sofi_velocity_pipelined(sofi_ctx *c, int *pipelined)
-{
-    if (!c || !pipelined)
-        return fail(SOFI_E_ARG, "null argument");
-    *pipelined = c->vpipe && c->vplan.segs && !c->G.ab4 && !c->march && !c->persist && c->cfg.weq != SOFI_AC_ISO;
-    return 0;
-}
-
 int sofi_block_threads_x(sofi_ctx *c, int *velocity, int *stress)
 {
     if (!c || !velocity || !stress)
         return fail(SOFI_E_ARG, "null argument");
     const bool ac = c->cfg.weq == SOFI_AC_ISO, visco = is_visco(c->cfg.weq);
     const int kind = kind_of(c->cfg.weq);
-    *velocity = (c->vnarrow && c->vw == 4 && !c->persist && !c->G.ab4 && !c->march && !c->vpipe &&
-                 narrow_v_applies(ac, false)) ? 8 : BX;
-    *stress = (c->snarrow && c->sw == 4 && !c->persist && !c->G.ab4 && !c->march && kind != AC && kind != TTI &&
+    *velocity = (c->vnarrow && c->vw == 4 && !c->G.ab4 && narrow_v_applies(ac, false)) ? 8 : BX;
+    *stress = (c->snarrow && c->sw == 4 && !c->G.ab4 && kind != AC && kind != TTI &&
                narrow_s_applies(visco, visco ? c->G.L : 0, false)) ? 8 : BX;
     return 0;
 }
@@ -2029,7 +1741,7 @@ int sofi_stress_variant(sofi_ctx *c, int *cells_per_thread)
 {
     if (!c || !cells_per_thread)
         return fail(SOFI_E_ARG, "null argument");
-    const int sw = c->persist ? 4 : c->sw;
+    const int sw = c->sw;
     if (c->G.ab4)
         *cells_per_thread = ab4_wide_s(c) ? 4 : 1;
     else

@@ -42,7 +42,7 @@ class SofiServerStats(ctypes.Structure):
 class SofiServerOptions(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("hbm_budget", ctypes.c_longlong), ("max_resident", ctypes.c_int),
                 ("chunk_steps", ctypes.c_int), ("depth", ctypes.c_int), ("prep_threads", ctypes.c_int),
-                ("prep_omp_threads", ctypes.c_int), ("use_priorities", ctypes.c_int), ("persistent", ctypes.c_int),
+                ("prep_omp_threads", ctypes.c_int), ("use_priorities", ctypes.c_int),
                 ("largest_first", ctypes.c_int)]
 
 
@@ -113,14 +113,13 @@ class Server:
 
     def __init__(self, device: int = 0, hbm_budget: int = 0, max_resident: int = 64, chunk_steps: int = 32,
                  depth: int = 2, prep_threads: int = 2, prep_omp_threads: int = 0, use_priorities: bool = True,
-                 persistent: bool = False, largest_first: bool = False):
+                 largest_first: bool = False):
         self.lib = load()
         o = SofiServerOptions()
         self.lib.sofi_server_default_options(ctypes.byref(o))
         o.device, o.hbm_budget, o.max_resident, o.chunk_steps = device, hbm_budget, max_resident, chunk_steps
         o.depth, o.prep_threads, o.prep_omp_threads = depth, prep_threads, prep_omp_threads
         o.use_priorities = 1 if use_priorities else 0
-        o.persistent = 1 if persistent else 0
         o.largest_first = 1 if largest_first else 0
         self.h = ctypes.c_void_p()
         _check(self.lib.sofi_server_create(ctypes.byref(o), ctypes.byref(self.h)))

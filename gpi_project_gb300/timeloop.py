@@ -145,15 +145,6 @@ class TimeLoop:
         N.check(self.lib.sofi_fwi_gradients(self.h, *[_fp(a) for a in out]))
         return tuple(out)
 
-    def fused(self) -> bool:
-        """Whether the fused velocity + stress step is in use."""
-        a = ctypes.c_int()
-        N.check(self.lib.sofi_fused(self.h, ctypes.byref(a)))
-        return bool(a.value)
-
-    def set_fused(self, on: bool) -> None:
-        N.check(self.lib.sofi_set_fused(self.h, int(bool(on))))
-
     def pdl(self) -> bool:
         """Whether the step kernels use programmatic dependent launch."""
         a = ctypes.c_int()
@@ -162,21 +153,6 @@ class TimeLoop:
 
     def set_pdl(self, on: bool) -> None:
         N.check(self.lib.sofi_set_pdl(self.h, int(bool(on))))
-
-    def persistent(self) -> tuple:
-        """(on, blocks per launch) of the persistent step kernel."""
-        a, b = ctypes.c_int(), ctypes.c_int()
-        N.check(self.lib.sofi_persistent(self.h, ctypes.byref(a), ctypes.byref(b)))
-        return bool(a.value), b.value
-
-    def set_persistent(self, on: bool) -> None:
-        N.check(self.lib.sofi_set_persistent(self.h, int(bool(on))))
-
-    def velocity_pipelined(self) -> bool:
-        """Whether the velocity update is the TMA-fed pipeline."""
-        a = ctypes.c_int()
-        N.check(self.lib.sofi_velocity_pipelined(self.h, ctypes.byref(a)))
-        return bool(a.value)
 
     def block_threads_x(self) -> tuple:
         """Threads per block along x of the four-cell (velocity, stress) kernels: 32, or 8 for narrow blocks."""

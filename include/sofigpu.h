@@ -195,10 +195,10 @@ int sofi_kernel_time(sofi_ctx *ctx, const char *name, double *avg_ms, long long 
 /* Velocity-kernel variant in use: cells per thread along x (1, 2 or 4) and
  * rows per thread (1, 2 or 4). The first sofi_run after sofi_reset(ctx, -1)
  * times the variants on the zeroed arrays (where each leaves them zero) and
- * keeps the fastest for the grid shape; SOFI_VROWS=w4|w2|t4|n4|1|2|4 fixes it
- * (t4: the TMA-fed pipeline, which the timing run does not try; n4: four
- * cells on narrow blocks, see sofi_block_threads_x). 4th-order time stepping
- * is not timed: four cells per thread unless SOFI_VROWS asks for rows. */
+ * keeps the fastest for the grid shape; SOFI_VROWS=w4|w2|n4|1|2|4 fixes it
+ * (n4: four cells on narrow blocks, see sofi_block_threads_x). 4th-order
+ * time stepping is not timed: four cells per thread unless SOFI_VROWS asks
+ * for rows. */
 int sofi_velocity_variant(sofi_ctx *ctx, int *cells_per_thread, int *rows_per_thread);
 /* ---- FWI gradient pass of one shot (MODE = FWI, ITERMAX 1, DTINV 1) ------
  * Replaces the gradient part of the reference's inversion()
@@ -233,30 +233,6 @@ int sofi_fwi_backward(sofi_ctx *ctx, const float *adj_x, const float *adj_y);
 int sofi_fwi_gradients(sofi_ctx *ctx, float *grad_lam, float *grad_mu, float *grad_rhos);
 int sofi_fwi_checkpoints(sofi_ctx *ctx, int *interval, int *segments);
 
-/* The fused step (ISO / VTI, FDORDER_TIME 2, no periodic edge): the velocity
- * and the stress update of a step in one kernel. Each tile computes the new
- * velocities on itself and an ND-cell halo into shared memory and the new
- * stresses of its own cells from them, so the stresses are read once per
- * step instead of twice; v, s and the velocity CPML memory are then held
- * twice and swapped every step. It is off unless SOFI_FUSED=1 (then
- * sofi_device_bytes counts the second set) or sofi_set_fused turns it on: on
- * the grids measured the two separate kernels are faster. Results equal the
- * four-cell kernels' bit for bit. */
-int sofi_fused(sofi_ctx *ctx, int *on);
-int sofi_set_fused(sofi_ctx *ctx, int on);
-
-/* The persistent step kernel: chunks of up to 128 time steps (until the next
- * snapshot or timed step) run as one cooperative launch whose blocks step
- * through the velocity, stress and post phases with a grid-wide barrier
- * between them. Available for ISO / VTI / acoustic media with FDORDER_TIME 2
- * and no periodic edge; off unless SOFI_PERSIST=1 or sofi_set_persistent turns
- * it on (the captured graph of plain kernels is faster on the grids measured).
- * `blocks`: blocks per launch (0: unavailable).
- * Steps outside the persistent launches then run the four-cell kernels, the
- * same arithmetic. sofi_set_persistent switches it (SOFI_E_STATE where it is
- * unavailable); the autotuner does not run while it is on. */
-int sofi_persistent(sofi_ctx *ctx, int *on, int *blocks);
-int sofi_set_persistent(sofi_ctx *ctx, int on);
 /* Programmatic dependent launch of the step kernels: each may be scheduled
  * while the previous kernel on the context's stream finishes, and waits in
  * hardware for that kernel's completion before it touches memory, so a
@@ -267,11 +243,6 @@ int sofi_set_persistent(sofi_ctx *ctx, int on);
  * Results are the same either way. */
 int sofi_pdl(sofi_ctx *ctx, int *on);
 int sofi_set_pdl(sofi_ctx *ctx, int on);
-/* 1 when the velocity update in use is the TMA-fed pipeline (stress tiles
- * copied into a ring of shared-memory stages, blocks marching down column
- * strips; second-order time stepping, not acoustic; SOFI_VROWS=t4 fixes it),
- * else 0. */
-int sofi_velocity_pipelined(sofi_ctx *ctx, int *pipelined);
 /* Stress-kernel variant in use: cells per thread along x (1, 2 or 4; TTI: 1),
  * chosen by the same autotuning run; SOFI_SW=0|2|4|n4 fixes it (4th-order time
  * stepping: four unless SOFI_SW=0). */

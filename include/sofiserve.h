@@ -88,8 +88,6 @@ typedef struct {
     int prep_threads;       /* host workers; <= 0: 2 */
     int prep_omp_threads;   /* OpenMP threads per worker; <= 0: cores / workers */
     int use_priorities;     /* 1: smaller solves get more urgent streams */
-    int persistent;         /* 1: solves run the persistent step kernel where it is
-                               available (sofi_set_persistent); 0: as the context sets it */
     int largest_first;      /* 1: of the requests that have arrived, the workers prepare
                                the one with the most cell updates (NX NY NT) first, so
                                the longest solves start early; 0: arrival order */

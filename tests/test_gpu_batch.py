@@ -47,7 +47,7 @@ def _run(cfg, fields_per_model, vecs, shots, rec, shared):
     return out
 
 
-@pytest.mark.parametrize("vrows", ["w4", "t4", "n4"])
+@pytest.mark.parametrize("vrows", ["w4", "n4"])
 @pytest.mark.parametrize("name", ["el_cpml_fd8", "visc_cpml_fs_l3", "tti_cpml"])
 def test_batch_equals_single_shots(name, vrows, monkeypatch):
     monkeypatch.setenv("SOFI_VROWS", vrows)
@@ -62,7 +62,7 @@ def test_batch_equals_single_shots(name, vrows, monkeypatch):
     o.close()
 
 
-@pytest.mark.parametrize("vrows", ["w4", "t4", "n4"])
+@pytest.mark.parametrize("vrows", ["w4", "n4"])
 def test_batch_with_a_model_per_shot(vrows, monkeypatch):
     monkeypatch.setenv("SOFI_VROWS", vrows)
     monkeypatch.setenv("SOFI_SW", "n4" if vrows == "n4" else "4")

@@ -85,33 +85,6 @@ def test_gpu_matches_oracle_examples(name):
     o.close()
 
 
-@pytest.mark.parametrize("name", ["el_cpml_fd8", "visc_cpml_fs_l3", "vvti_cpml_l2", "el_abs_fd10"])
-def test_march_kernels_match_simple_kernels(name, monkeypatch):
-    """The y-marching kernels and the one-cell-per-thread kernels compute the same
-    step, to float32 rounding grown over the run: the two instruction streams
-    contract the stencil sums into fused multiply-adds differently (the bound
-    of the vector-width tests)."""
-    from oracle import oracle as O
-    from tests.golden.cases import case_by_name
-    from tests.helpers import case_receivers, case_sources
-    case = case_by_name(name)
-    o = run_oracle_case(case, nthreads=os.cpu_count() or 1, nsteps=1)
-    cfg = o.cfg
-    sp = case_sources(case, cfg)
-    sig = O.wavelet(1, cfg.nt, cfg.dt, sp)
-    out = {}
-    monkeypatch.setenv("SOFI_VROWS", "1")  # the one-cell kernels beside the marching ones
-    monkeypatch.setenv("SOFI_SW", "0")
-    for variant in ["simple", "march"]:
-        monkeypatch.setenv("SOFI_KERNELS", variant)
-        t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
-        out[variant] = {k: t.field(k) for k in ["vx", "vy", "sxx", "syy", "sxy"]}
-        t.close()
-    for k in out["march"]:
-        assert rel_l2(out["march"][k], out["simple"][k]) < 5e-5, (name, k, rel_l2(out["march"][k], out["simple"][k]))
-    o.close()
-
-
 @pytest.mark.parametrize("name", ["visc_cpml_fs_l3", "el_mixed_sources", "tti_cpml", "el_periodic_cpml"])
 def test_graph_replay_equals_direct_launches(name, monkeypatch):
     """Steps replayed from the captured 32-step graph equal directly launched steps."""
@@ -194,59 +167,16 @@ def test_velocity_kernel_vector_widths_match_one_cell(name, monkeypatch):
     sp = case_sources(case, cfg)
     sig = O.wavelet(1, cfg.nt, cfg.dt, sp)
     out = {}
-    for variant in ["1", "w4", "w2", "t4"]:
+    for variant in ["1", "w4", "w2"]:
         monkeypatch.setenv("SOFI_VROWS", variant)
         t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
-        assert t.velocity_variant() == {"1": (1, 1), "w4": (4, 1), "w2": (2, 1), "t4": (4, 1)}[variant]
-        assert t.velocity_pipelined() == (variant == "t4")
+        assert t.velocity_variant() == {"1": (1, 1), "w4": (4, 1), "w2": (2, 1)}[variant]
         out[variant] = {k: t.field(k) for k in ["vx", "vy", "sxx", "syy", "sxy"]}
         out[variant].update({c: t.section(c) for c in ["vx", "vy", "div"]})
         t.close()
-    # the pipelined kernel (TMA copies of the stress tiles into shared memory)
-    # sums the same values in the same order as the four-cell kernel; it is
-    # held to the same bound, as the compiler may contract the sums differently
-    for w in ["w4", "w2", "t4"]:
+    for w in ["w4", "w2"]:
         for k in out[w]:
             assert rel_l2(out[w][k], out["1"][k]) < 5e-5, (name, w, k, rel_l2(out[w][k], out["1"][k]))
-    o.close()
-
-
-@pytest.mark.parametrize("name", ["el_cpml_fd8", "el_cpml_fd12", "el_abs_fd2", "visc_cpml_fs_l3",
-                                  "el_periodic_cpml", "tti_abs"])
-def test_velocity_pipeline_segments(name, monkeypatch):
-    """The TMA-fed velocity pipeline gives the same step whatever the number of
-    row segments per strip: one segment walks all chunks of a strip through
-    the six-stage ring (it wraps), the planned count gives each block one or
-    two chunks. Every segment count is bit-identical, and matches the four-
-    cell kernel to float32 rounding."""
-    from oracle import oracle as O
-    from tests.golden.cases import case_by_name
-    from tests.helpers import case_receivers, case_sources
-    case = case_by_name(name)
-    o = run_oracle_case(case, nthreads=os.cpu_count() or 1, nsteps=1)
-    cfg = o.cfg
-    sp = case_sources(case, cfg)
-    sig = O.wavelet(1, cfg.nt, cfg.dt, sp)
-    out = {}
-    for vrows, segs in [("w4", None), ("t4", None), ("t4", "1"), ("t4", "2"), ("t4", "5")]:
-        monkeypatch.setenv("SOFI_VROWS", vrows)
-        if segs:
-            monkeypatch.setenv("SOFI_VT_SEGS", segs)
-        else:
-            monkeypatch.delenv("SOFI_VT_SEGS", raising=False)
-        t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
-        assert t.velocity_pipelined() == (vrows == "t4")
-        out[(vrows, segs)] = {k: t.field(k) for k in ["vx", "vy", "sxx", "syy", "sxy"]}
-        out[(vrows, segs)].update({"section " + c: t.section(c) for c in ["vx", "vy"]})
-        t.close()
-    ref = out[("t4", None)]
-    for key, d in out.items():
-        for k in d:
-            if key[0] == "t4":
-                np.testing.assert_array_equal(d[k], ref[k], err_msg=f"{name} segments {key[1]} {k}")
-            else:
-                assert rel_l2(d[k], ref[k]) < 5e-5, (name, k, rel_l2(d[k], ref[k]))
-            assert np.abs(d[k]).max() > 0
     o.close()
 
 
@@ -266,7 +196,6 @@ def test_autotuned_run_equals_fixed_variant(name, monkeypatch):
     monkeypatch.delenv("SOFI_VROWS", raising=False)
     t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
     cells, rows = t.velocity_variant()
-    piped = t.velocity_pipelined()
 
     def outputs(t):
         d = {"field " + k: t.field(k) for k in ["vx", "vy", "sxx", "syy", "sxy"]}
@@ -275,9 +204,9 @@ def test_autotuned_run_equals_fixed_variant(name, monkeypatch):
 
     tuned = outputs(t)
     t.close()
-    monkeypatch.setenv("SOFI_VROWS", "t4" if piped else (f"w{cells}" if cells > 1 else str(rows)))
+    monkeypatch.setenv("SOFI_VROWS", f"w{cells}" if cells > 1 else str(rows))
     t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
-    assert t.velocity_variant() == (cells, rows) and t.velocity_pipelined() == piped
+    assert t.velocity_variant() == (cells, rows)
     fixed = outputs(t)
     t.close()
     for k in tuned:
