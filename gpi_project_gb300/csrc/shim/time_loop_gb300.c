@@ -3,7 +3,7 @@
  * the loop on one GPU through libsofigpu.so.
  *
  * Build it with the reference's own headers and link it instead of
- * src/time_loop.c (see INTEGRATION.md):
+ * src/time_loop.c:
  *     cc -c -I<sofi2d>/src -I<repo>/include time_loop_gb300.c
  *     ... link the reference's objects minus time_loop.o, plus -lsofigpu
  *

@@ -13,7 +13,7 @@ Two kinds of fixture, both small enough to commit:
   grid sizes. Models are regenerated from the seed by ``synthetic_model`` (a
   CRC of the model bytes is stored to catch a drift).
 
-    python tests/golden/make_fixtures.py [--reference /root/reference]
+    python tests/golden/make_fixtures.py [--reference <reference source tree>]
 """
 from __future__ import annotations
 
@@ -176,9 +176,13 @@ def run_reference_fwi(case, exe):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=None,
+                    help="reference source tree (default: the one oracle/_ref was built from)")
     ap.add_argument("--only", default="")
     a = ap.parse_args()
+    if a.reference is None:
+        with open(os.path.join(REPO, "oracle", "_ref", "source_dir.txt")) as fh:
+            a.reference = fh.read().strip()
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle", "ref"), f"REFERENCE={a.reference}"],
                    check=True)
     exe = os.path.join(REPO, "oracle", "_ref", "sofi2D")

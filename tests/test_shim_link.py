@@ -8,7 +8,18 @@ import subprocess
 import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+
+
+def _reference_tree():
+    """The reference source tree oracle/_ref was built from (build() records it)."""
+    try:
+        with open(os.path.join(REPO, "oracle", "_ref", "source_dir.txt")) as fh:
+            return fh.read().strip()
+    except OSError:
+        return ""
+
+
+REF = _reference_tree()
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")), reason="reference sources not present")
