@@ -2,11 +2,13 @@
  * acq_io.c -- model files, sources, receivers, wavelets and outputs.
  *
  *   model files      NX traces of NY float32 samples (readmod_elastic.c:103-111)
- *   source file      x y tshift fc amp [azimuth [type]] per line, '#' comments
- *                    (sources.c:60-118); grid index floor(x/DH)+1 (splitsrc.c:34-36)
+ *   source file      x y tshift fc amp [azimuth [type]] per line (Berlage and Klauder
+ *                    wavelets: their parameters too), '#' comments (sources.c:60-316);
+ *                    grid index floor(x/DH)+1 (splitsrc.c:34-36)
  *   receiver file    x y per line, '#'/'%' comments; duplicates dropped
  *                    (receiver.c:48-110); or a line XREC1..XREC2 every NGEOPH
- *   wavelets         Ricker, Fuchs-Mueller, sin^3 (wavelet.c:56-81)
+ *   wavelets         Ricker, Fuchs-Mueller, file, sin^3, Berlage, Klauder (wavelet.c:33-149,
+ *                    read_srcsig.c:38-184)
  *   SU traces        240-byte trace header + float32 samples (outseis_glob.c:40-81)
  *   snapshots        float32 stream per component (snap_ssg.c, SNAP_FORMAT=3)
  */
@@ -148,22 +150,37 @@ int sofih_read_sources(const sofih_par *p, const char *path, float **srcpos, flo
     while (fgets(line, sizeof line, fp)) {
         if (!is_data_line(line, 0))
             continue;
-        float v[7] = {0};
-        int k = sscanf(line, "%f%f%f%f%f%f%f", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6]);
-        if (k < 5) {
+        /* columns (sources.c:60-316): x y tshift, then
+         *   SOURCE_SHAPE <= 4  fc amp [azimuth [type]]
+         *   5 (Berlage)        fc amp exponent decay phase [azimuth [type]]
+         *   6 (Klauder)        fmin fmax amp sweep-length width [azimuth [type]]  (fc = (fmin + fmax) / 2) */
+        float v[10] = {0};
+        const int k = sscanf(line, "%f%f%f%f%f%f%f%f%f%f", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6], &v[7],
+                             &v[8], &v[9]);
+        const int shape = p->source_shape, need = shape == 5 || shape == 6 ? 8 : 5;
+        if (k < need) {
             fclose(fp);
             free(sp), free(pos);
-            sofih_set_error("%s: source %d lacks time shift, frequency or amplitude", path, l + 1);
+            sofih_set_error("%s: source %d lacks %s", path, l + 1,
+                            shape == 5   ? "time shift, frequency, amplitude, exponent, decay or phase"
+                            : shape == 6 ? "time shift, frequencies, amplitude, sweep length or width"
+                                         : "time shift, frequency or amplitude");
             return 1;
         }
-        if (k < 6)
-            v[5] = 0.0f;
-        if (k < 7)
-            v[6] = (float)p->source_type;
+        float az = k > need ? v[need] : 0.0f, type = k > need + 1 ? v[need + 1] : (float)p->source_type;
         sp[0 * n + l] = (float)((int)floor(v[0] / p->dh) + 1);
         sp[1 * n + l] = (float)((int)floor(v[1] / p->dh) + 1);
-        sp[3 * n + l] = v[2], sp[4 * n + l] = v[3], sp[5 * n + l] = v[4];
-        sp[6 * n + l] = v[5], sp[7 * n + l] = v[6];
+        sp[3 * n + l] = v[2];
+        if (shape == 6) {
+            sp[8 * n + l] = v[3], sp[9 * n + l] = v[4], sp[5 * n + l] = v[5], sp[10 * n + l] = v[6];
+            sp[11 * n + l] = v[7];
+            sp[4 * n + l] = (v[3] + v[4]) / 2;
+        } else {
+            sp[4 * n + l] = v[3], sp[5 * n + l] = v[4];
+            if (shape == 5)
+                sp[8 * n + l] = v[5], sp[9 * n + l] = v[6], sp[10 * n + l] = v[7];
+        }
+        sp[6 * n + l] = az, sp[7 * n + l] = type;
         pos[l] = v[0], pos[n + l] = v[1];
         l++;
     }
@@ -172,34 +189,221 @@ int sofih_read_sources(const sofih_par *p, const char *path, float **srcpos, flo
     return 0;
 }
 
+/* One source's signal (wavelet.c:48-142). The operand types follow the
+ * reference's (float variables, double constants and libm calls), so the
+ * samples equal its own bit for bit: srcpos row 3 time shift, 4 centre
+ * frequency, 5 amplitude, rows 8..11 the Berlage (time exponent, decay,
+ * initial phase [deg]) or Klauder (lowest / highest frequency, sweep length,
+ * half width in centre periods) parameters; `file` the samples of a
+ * SOURCE_SHAPE 3 signal file. */
+static int one_wavelet(int shape, int nt, float dt, int nsrc, int k, const float *srcpos, const float *file,
+                       int nfile, float *sig)
+{
+    const float tshift = srcpos[3 * nsrc + k], fc = srcpos[4 * nsrc + k], a = srcpos[5 * nsrc + k];
+    const float ts = 1.0 / fc;
+    float sigmax = 0.0;
+    for (int n = 1; n <= nt; n++) {
+        const float t = (float)n * dt;
+        float amp = 0.0, tau;
+        switch (shape) {
+          case 1: /* Ricker */
+              tau = PI * (t - 1.5 * ts - tshift) / (ts);
+              amp = (((1.0 - 2.0 * tau * tau) * exp(-tau * tau)));
+              break;
+          case 2: /* Fuchs-Mueller */
+              amp = ((t < tshift) || (t > (tshift + ts)))
+                        ? 0.0
+                        : (sin(2.0 * PI * (t - tshift) * fc) - 0.5 * sin(4.0 * PI * (t - tshift) * fc));
+              break;
+          case 3: /* samples of SIGNAL_FILE */
+              amp = n <= nfile ? file[n - 1] : 0.0f;
+              break;
+          case 4: /* sin^3 */
+              amp = ((t < tshift) || (t > (tshift + ts))) ? 0.0 : pow(sin(PI * (t - tshift) / ts), 3.0);
+              break;
+          case 5: { /* Berlage (Aldridge 1990), wavelet.c:82-96 */
+              const float ex = srcpos[8 * nsrc + k], alpha = srcpos[9 * nsrc + k];
+              const float phi0 = srcpos[10 * nsrc + k] * PI / 180;
+              if (ex <= 0) {
+                  sofih_set_error("source %d: the Berlage wavelet needs a time exponent > 0", k + 1);
+                  return 1;
+              }
+              amp = (t < tshift) ? 0.0
+                                 : a * pow((t - tshift), ex) * exp(-alpha * (t - tshift)) *
+                                       cos(2 * PI * fc * (t - tshift) + phi0);
+              break;
+          }
+          case 6: { /* Klauder, wavelet.c:97-125. The reference's exp() of the complex
+                     * carrier sees only its real part (no <tgmath.h>): exp(0) = 1, so
+                     * the wavelet is the sweep's envelope without the carrier */
+              const float fmin = srcpos[8 * nsrc + k], fmax = srcpos[9 * nsrc + k];
+              const float T = srcpos[10 * nsrc + k], width = srcpos[11 * nsrc + k];
+              const float f2 = (fmax - fmin) / T;
+              tau = (width / fc);
+              if ((t < tshift) || (t > (tau * 2) + tshift)) {
+                  amp = 0.0;
+              } else {
+                  const float tp = t - tau - tshift;
+                  amp = sin(PI * f2 * tp * (T - tp)) / (PI * f2 * tp) * 1.0;
+                  if (t < (tau * 0.2) + tshift) {
+                      const float taper = (1 - cos(((t - tshift) / tau / 0.2) * PI)) / 2;
+                      amp = amp * taper;
+                  } else if (t > (tau * 1.8) + tshift) {
+                      const float taper = (1 - cos(((2 * tau + tshift - t) / 0.2 / tau) * PI)) / 2;
+                      amp = amp * taper;
+                  }
+              }
+              break;
+          }
+          default:
+              sofih_set_error("SOURCE_SHAPE %d is not supported (1 Ricker, 2 Fuchs-Mueller, 3 file, 4 sin^3, "
+                              "5 Berlage, 6 Klauder)", shape);
+              return 1;
+        }
+        if (fabs(amp) > sigmax)
+            sigmax = fabs(amp);
+        sig[n - 1] = amp * a;
+    }
+    if (0.0 == sigmax) {
+        sofih_set_error("source %d: the source signal contains only zeros", k + 1);
+        return 1;
+    }
+    if (shape == 5 || shape == 6) /* normalised to the amplitude */
+        for (int n = 0; n < nt; n++)
+            sig[n] = sig[n] / sigmax;
+    return 0;
+}
+
 int sofih_wavelet(int shape, int nt, float dt, int nsrc, const float *srcpos, float *signals)
 {
-    for (int k = 0; k < nsrc; k++) {
-        float tshift = srcpos[3 * nsrc + k], fc = srcpos[4 * nsrc + k], a = srcpos[5 * nsrc + k];
-        float ts = 1.0 / fc;
-        for (int n = 1; n <= nt; n++) {
-            float t = (float)n * dt, amp = 0.0, tau;
-            switch (shape) {
-              case 1:
-                  tau = PI * (t - 1.5 * ts - tshift) / (ts);
-                  amp = (((1.0 - 2.0 * tau * tau) * exp(-tau * tau)));
-                  break;
-              case 2:
-                  amp = ((t < tshift) || (t > (tshift + ts)))
-                            ? 0.0
-                            : (sin(2.0 * PI * (t - tshift) * fc) - 0.5 * sin(4.0 * PI * (t - tshift) * fc));
-                  break;
-              case 4:
-                  amp = ((t < tshift) || (t > (tshift + ts))) ? 0.0 : pow(sin(PI * (t - tshift) / ts), 3.0);
-                  break;
-              default:
-                  sofih_set_error("SOURCE_SHAPE %d is not supported (1 Ricker, 2 Fuchs-Mueller, 4 sin^3)", shape);
-                  return 1;
-            }
-            signals[(size_t)k * nt + (n - 1)] = amp * a;
-        }
+    if (shape == 3) {
+        sofih_set_error("SOURCE_SHAPE 3 reads SIGNAL_FILE: use sofih_wavelet_file");
+        return 1;
     }
+    for (int k = 0; k < nsrc; k++)
+        if (one_wavelet(shape, nt, dt, nsrc, k, srcpos, NULL, 0, signals + (size_t)k * nt))
+            return 1;
     return 0;
+}
+
+int sofih_read_signal(const char *path, float dt, float **samples, int *ns)
+{
+    *samples = NULL, *ns = 0;
+    float sdt = 0.f;
+    int dt_found = 0;
+    float *sig = NULL;
+    FILE *fp = NULL;
+    /* the file type from the name: ".su" anywhere (case-insensitive) is SU,
+     * anything else is ASCII (read_srcsig.c:55-62) */
+    char low[1024];
+    size_t L = strlen(path);
+    if (L >= sizeof low)
+        L = sizeof low - 1;
+    for (size_t c = 0; c < L; c++)
+        low[c] = (char)((path[c] >= 'A' && path[c] <= 'Z') ? path[c] - 'A' + 'a' : path[c]);
+    low[L] = 0;
+    if (strstr(low, ".su")) {
+        fp = fopen(path, "rb");
+        if (!fp) {
+            sofih_set_error("cannot open signal file %s", path);
+            return 1;
+        }
+        unsigned char h[240];
+        if (fread(h, 1, 240, fp) != 240) {
+            fclose(fp);
+            sofih_set_error("short read in SU file %s", path);
+            return 1;
+        }
+        unsigned short suns, sudt;
+        short delrt;
+        memcpy(&delrt, h + 108, 2), memcpy(&suns, h + 114, 2), memcpy(&sudt, h + 116, 2);
+        if (suns < 1 || delrt != 0) {
+            fclose(fp);
+            sofih_set_error("SU signal file %s: no samples, or a delay recording time (unsupported)", path);
+            return 1;
+        }
+        sig = (float *)calloc(suns, sizeof(float));
+        if (fread(sig, sizeof(float), suns, fp) != suns) {
+            fclose(fp), free(sig);
+            sofih_set_error("short read in SU file %s", path);
+            return 1;
+        }
+        fclose(fp);
+        *ns = suns;
+        if (sudt > 0)
+            sdt = sudt * 1e-6, dt_found = 1;
+    } else {
+        fp = fopen(path, "r");
+        if (!fp) {
+            sofih_set_error("cannot open signal file %s", path);
+            return 1;
+        }
+        char line[256];
+        int n = 0;
+        /* first pass: count samples; a comment line "# ... DT ... = <value>" gives the interval */
+        while (fgets(line, sizeof line, fp)) {
+            char *q = line;
+            while (*q == ' ' || *q == '\t' || *q == '\n' || *q == '\r' || *q == '\v' || *q == '\f')
+                q++;
+            if (!*q)
+                continue;
+            if (*q == '#') {
+                char lc[256];
+                size_t m = strlen(q + 1);
+                for (size_t c = 0; c <= m; c++)
+                    lc[c] = (char)((q[1 + c] >= 'A' && q[1 + c] <= 'Z') ? q[1 + c] - 'A' + 'a' : q[1 + c]);
+                if (!strstr(lc, "dt") || !strchr(q + 1, '='))
+                    continue;
+                char *v = strchr(q + 1, '=') + 1;
+                while (*v == ' ' || *v == '\t')
+                    v++;
+                if (sscanf(v, "%e", &sdt) == 1)
+                    dt_found = 1;
+                continue;
+            }
+            n++;
+        }
+        if (!n) {
+            fclose(fp);
+            sofih_set_error("signal file %s holds no samples", path);
+            return 1;
+        }
+        sig = (float *)calloc((size_t)n, sizeof(float));
+        rewind(fp);
+        int i = 0;
+        while (fgets(line, sizeof line, fp) && i < n) {
+            char *q = line;
+            while (*q == ' ' || *q == '\t' || *q == '\n' || *q == '\r' || *q == '\v' || *q == '\f')
+                q++;
+            if (!*q || *q == '#')
+                continue;
+            if (sscanf(q, "%e", &sig[i]) != 1)
+                sig[i] = 0.0f;
+            i++;
+        }
+        fclose(fp);
+        *ns = n;
+    }
+    if (dt_found && sdt != dt) {
+        free(sig);
+        sofih_set_error("signal file %s: sampling interval %g s differs from DT %g s", path, sdt, dt);
+        return 1;
+    }
+    *samples = sig;
+    return 0;
+}
+
+int sofih_wavelet_file(const char *signal_file, int nt, float dt, int nsrc, const float *srcpos, float *signals)
+{
+    float *f = NULL;
+    int nf = 0;
+    if (sofih_read_signal(signal_file, dt, &f, &nf))
+        return 1;
+    int rc = 0;
+    for (int k = 0; k < nsrc && !rc; k++)
+        rc = one_wavelet(3, nt, dt, nsrc, k, srcpos, f, nf, signals + (size_t)k * nt);
+    free(f);
+    return rc;
 }
 
 int sofih_read_receivers(const sofih_par *p, const char *path, int **ix, int **iy, int *ntr)

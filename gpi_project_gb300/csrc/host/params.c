@@ -203,6 +203,8 @@ int sofih_read_par(const char *path, sofih_par *p)
     p->fwi_dtinv = geti(kv, "DTINV", 1);
     gets_(kv, "DATA_DIR", p->data_dir, sizeof p->data_dir);
     gets_(kv, "GRADIENT", p->gradient, sizeof p->gradient);
+    p->readmod = geti(kv, "READMOD", 1), p->tau = getf(kv, "TAU", 0.0001f);
+    gets_(kv, "SIGNAL_FILE", p->signal_file, sizeof p->signal_file);
     free(kv);
     return 0;
 }

@@ -173,7 +173,8 @@ int main(int argc, char **argv)
     if (sofih_read_sources(&p, p.source_file, &srcpos, &srcxy, &nsrc))
         DIE_H();
     float *sig = (float *)malloc(sizeof(float) * (size_t)(nsrc ? nsrc : 1) * p.nt);
-    if (sofih_wavelet(p.source_shape, p.nt, p.dt, nsrc, srcpos, sig))
+    if (p.source_shape == 3 ? sofih_wavelet_file(p.signal_file, p.nt, p.dt, nsrc, srcpos, sig)
+                            : sofih_wavelet(p.source_shape, p.nt, p.dt, nsrc, srcpos, sig))
         DIE_H();
     int *rix = NULL, *riy = NULL, ntr = 0;
     if (p.seismo && sofih_read_receivers(&p, p.rec_file, &rix, &riy, &ntr))

@@ -156,7 +156,8 @@ static int prepare_request(const sofi_server *s, req_t *q)
         q->signals = (float *)malloc(sizeof(float) * (size_t)q->r.nsrc * (size_t)p->nt);
         if (!q->signals)
             return fail(SOFI_E_NOMEM, "host memory for %d wavelets", q->r.nsrc);
-        if (sofih_wavelet(p->source_shape, p->nt, p->dt, q->r.nsrc, q->r.srcpos, q->signals))
+        if (p->source_shape == 3 ? sofih_wavelet_file(p->signal_file, p->nt, p->dt, q->r.nsrc, q->r.srcpos, q->signals)
+                                 : sofih_wavelet(p->source_shape, p->nt, p->dt, q->r.nsrc, q->r.srcpos, q->signals))
             return fail(SOFI_E_ARG, "wavelet: %s", sofih_last_error());
     }
     sofi_config *c = &q->cfg;

@@ -32,7 +32,8 @@ class SofihPar(ctypes.Structure):
                 ("sigout_file", ctypes.c_char * 256), ("fdorder_time", ctypes.c_int),
                 ("mode_fwi", ctypes.c_int), ("fwi_itermax", ctypes.c_int), ("fwi_velocity", ctypes.c_int),
                 ("fwi_adjoint", ctypes.c_int), ("fwi_lnorm", ctypes.c_int), ("fwi_dtinv", ctypes.c_int),
-                ("data_dir", ctypes.c_char * 256), ("gradient", ctypes.c_char * 256)]
+                ("data_dir", ctypes.c_char * 256), ("gradient", ctypes.c_char * 256), ("readmod", ctypes.c_int),
+                ("tau", ctypes.c_float), ("signal_file", ctypes.c_char * 256)]
 
 
 _LIB = None
@@ -59,6 +60,8 @@ def load():
         L.sofih_holberg.argtypes = [ctypes.c_int, ctypes.c_int, fp]
         L.sofih_check_cfl.argtypes = [P(SofihPar), vp, fp]
         L.sofih_wavelet.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int, fp, fp]
+        L.sofih_wavelet_file.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_float, ctypes.c_int, fp, fp]
+        L.sofih_read_signal.argtypes = [ctypes.c_char_p, ctypes.c_float, P(fp), ip]
         L.sofih_read_sources.argtypes = [P(SofihPar), ctypes.c_char_p, P(fp), P(fp), ip]
         L.sofih_read_receivers.argtypes = [P(SofihPar), ctypes.c_char_p, P(ip), P(ip), ip]
         L.sofih_write_signal.argtypes = [P(SofihPar), ctypes.c_int, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -96,6 +99,7 @@ def make_par(**kw) -> SofihPar:
     p = SofihPar()
     p.npower, p.k_max_cpml, p.damping, p.ndt, p.idx, p.idy, p.readrec = 2.0, 1.0, 8.0, 1, 1, 1, 1
     p.fdorder_time = 2
+    p.readmod, p.tau = 1, 0.0001
     for k, v in kw.items():
         if k == "fl":
             for i, f in enumerate(v):
@@ -145,11 +149,27 @@ def holberg(fdorder: int, maxrelerror: int) -> np.ndarray:
     return hc
 
 
-def wavelet(shape: int, nt: int, dt: float, srcpos: np.ndarray) -> np.ndarray:
+def wavelet(shape: int, nt: int, dt: float, srcpos: np.ndarray, signal_file: str | None = None) -> np.ndarray:
+    """Source signals [nsrc][nt] (wavelet.c); SOURCE_SHAPE 3 reads `signal_file`."""
     sp = np.ascontiguousarray(srcpos, dtype=np.float32)
     out = np.empty((sp.shape[1], nt), np.float32)
-    if load().sofih_wavelet(shape, nt, dt, sp.shape[1], _fp(sp), _fp(out)):
+    if shape == 3:
+        rc = load().sofih_wavelet_file((signal_file or "").encode(), nt, dt, sp.shape[1], _fp(sp), _fp(out))
+    else:
+        rc = load().sofih_wavelet(shape, nt, dt, sp.shape[1], _fp(sp), _fp(out))
+    if rc:
         raise _err()
+    return out
+
+
+def read_signal(path: str, dt: float) -> np.ndarray:
+    """Samples of a SOURCE_SHAPE 3 signal file (read_srcsig.c)."""
+    smp, n = ctypes.POINTER(ctypes.c_float)(), ctypes.c_int()
+    L = load()
+    if L.sofih_read_signal(path.encode(), dt, ctypes.byref(smp), ctypes.byref(n)):
+        raise _err()
+    out = np.ctypeslib.as_array(smp, shape=(n.value,)).copy()
+    ctypes.CDLL(None).free(smp)
     return out
 
 

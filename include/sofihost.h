@@ -53,6 +53,12 @@ typedef struct {
     int mode_fwi;
     int fwi_itermax, fwi_velocity, fwi_adjoint, fwi_lnorm, fwi_dtinv;
     char data_dir[256], gradient[256];
+    /* the model: 1 from MFILE files, 0 the reference's built-in half space of
+     * hh_elastic.c / hh_visco.c / hh_*_VTI.c / hh_*_TTI.c (READMOD); TAU: the
+     * built-in anisotropic viscoelastic models' tau (read_par_json.c:447-449) */
+    int readmod;
+    float tau;
+    char signal_file[256];      /* SOURCE_SHAPE 3: the signal (read_srcsig.c), ASCII or SU */
 } sofih_par;
 
 const char *sofih_last_error(void);
@@ -96,7 +102,19 @@ int sofih_check_cfl(const sofih_par *p, const sofih_prep *m, float *dt_max);
 /* Sources: srcpos [12][nsrc] row-major in grid indices (reference srcpos_loc
  * layout after splitsrc.c); xy [2][nsrc] physical coordinates. */
 int sofih_read_sources(const sofih_par *p, const char *path, float **srcpos, float **xy, int *nsrc);
+/* Source signals [nsrc][nt] (wavelet.c): SOURCE_SHAPE 1 Ricker, 2 Fuchs-Mueller,
+ * 4 sin^3, 5 Berlage, 6 Klauder (5 and 6 normalised to the amplitude; their
+ * parameters in srcpos rows 8..11 as sofih_read_sources fills them).
+ * SOURCE_SHAPE 3 takes the samples of SIGNAL_FILE: sofih_wavelet_file. */
 int sofih_wavelet(int shape, int nt, float dt, int nsrc, const float *srcpos, float *signals);
+/* The samples of a signal file (read_srcsig.c:38-184): SU (a name holding
+ * ".su", first trace) or ASCII (one value per line, '#' comments, a comment
+ * "DT = <s>" gives the interval); a stated interval must equal dt. The
+ * caller frees *samples with free(). */
+int sofih_read_signal(const char *path, float dt, float **samples, int *ns);
+/* SOURCE_SHAPE 3: every source's signal is the file's samples (zero past
+ * them) times its amplitude. */
+int sofih_wavelet_file(const char *signal_file, int nt, float dt, int nsrc, const float *srcpos, float *signals);
 /* Receivers (grid indices, duplicates removed, reference receiver.c). */
 int sofih_read_receivers(const sofih_par *p, const char *path, int **ix, int **iy, int *ntr);
 

@@ -79,6 +79,7 @@ def _lib(precision: str = "f32"):
         lib.orc_set_sources.argtypes = [ctypes.c_void_p, ctypes.c_int, fp, fp]
         lib.orc_set_receivers.argtypes = [ctypes.c_void_p, ctypes.c_int, ip, ip]
         lib.orc_wavelet.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int, fp, fp]
+        lib.orc_wavelet_samples.argtypes = [ctypes.c_int, ctypes.c_float, ctypes.c_int, fp, fp, ctypes.c_int, fp]
         lib.orc_reset.argtypes = [ctypes.c_void_p]
         lib.orc_run.argtypes = [ctypes.c_void_p, ctypes.c_int]
         lib.orc_current_step.argtypes = [ctypes.c_void_p]
@@ -484,13 +485,63 @@ def fwi_model_gradients(lam, mu, rhos, vp, vs, rho) -> tuple:
     return gvp, gvs, grho
 
 
-def wavelet(shape: int, nt: int, dt: float, srcpos: np.ndarray, precision: str = "f32") -> np.ndarray:
+def wavelet(shape: int, nt: int, dt: float, srcpos: np.ndarray, precision: str = "f32",
+            samples: np.ndarray | None = None) -> np.ndarray:
+    """Source signals [nsrc][nt] (wavelet.c); SOURCE_SHAPE 3 takes the signal
+    file's samples (``read_srcsig``)."""
     sp = np.ascontiguousarray(srcpos, dtype=np.float32)
     out = np.empty((sp.shape[1], nt), dtype=np.float32)
-    rc = _lib(precision).orc_wavelet(shape, nt, dt, sp.shape[1], _fptr(sp), _fptr(out))
+    if shape == 3:
+        smp = np.ascontiguousarray(samples, dtype=np.float32)
+        rc = _lib(precision).orc_wavelet_samples(nt, dt, sp.shape[1], _fptr(sp), _fptr(smp), smp.size, _fptr(out))
+    else:
+        rc = _lib(precision).orc_wavelet(shape, nt, dt, sp.shape[1], _fptr(sp), _fptr(out))
+    if rc == 2:
+        raise ValueError("source signal contains only zeros")
     if rc:
-        raise ValueError(f"unsupported SOURCE_SHAPE {shape}")
+        raise ValueError(f"unsupported SOURCE_SHAPE {shape} or wavelet parameters")
     return out
+
+
+def read_srcsig(path: str, dt: float) -> np.ndarray:
+    """Samples of a SOURCE_SHAPE 3 signal file (reference src/read_srcsig.c:38-184):
+    SU when the name holds ".su" (any case; first trace, ns and dt from its
+    header, delrt must be 0), else ASCII: one value per line, '#' comment
+    lines, of which one holding "DT" and "=" states the interval. A stated
+    interval must equal DT (as float32)."""
+    dt32, sdt = np.float32(dt), None
+    if ".su" in path.lower():
+        b = np.fromfile(path, dtype=np.uint8)
+        ns = int(b[114:116].view(np.uint16)[0])
+        sudt = int(b[116:118].view(np.uint16)[0])
+        if ns < 1 or int(b[108:110].view(np.int16)[0]) != 0:
+            raise ValueError("SU signal file without samples or with a delay recording time")
+        samples = b[240:240 + 4 * ns].view(np.float32).copy()
+        if sudt > 0:
+            sdt = np.float32(sudt * 1e-6)
+    else:
+        vals = []
+        with open(path) as fh:
+            for line in fh:
+                q = line.lstrip()
+                if not q:
+                    continue
+                if q.startswith("#"):
+                    body = q[1:]
+                    if "dt" in body.lower() and "=" in body:
+                        try:
+                            sdt = np.float32(float(body.split("=", 1)[1].split()[0]))
+                        except (ValueError, IndexError):
+                            pass
+                    continue
+                try:
+                    vals.append(np.float32(float(q.split()[0])))
+                except ValueError:
+                    vals.append(np.float32(0.0))
+        samples = np.array(vals, dtype=np.float32)
+    if sdt is not None and sdt != dt32:
+        raise ValueError(f"signal file interval {sdt} differs from DT {dt32}")
+    return samples
 
 
 def run_example(json_path: str, workdir: str, precision: str = "f32", nthreads: int = 0,

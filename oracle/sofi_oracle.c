@@ -948,39 +948,111 @@ int orc_prepare(orc_ctx *c)
 
 /* ------------------------------------------------------------- wavelet */
 
+/* wavelet.c:48-142 for one source k: `file` holds the samples of a
+ * SOURCE_SHAPE 3 signal (read_srcsig.c), nfile of them. Float variables,
+ * double constants and libm calls as the reference mixes them. */
+static int wavelet_one(int shape, int nt, float dt, int nsrc, int k, const float *srcpos, const float *file,
+                       int nfile, float *out)
+{
+    float tshift = srcpos[3 * nsrc + k];
+    float fc = srcpos[4 * nsrc + k];
+    float a = srcpos[5 * nsrc + k];
+    float ts = 1.0 / fc;
+    float sigmax = 0.0;
+    for (int n = 1; n <= nt; n++) {
+        float t = (float)n * dt;
+        float amp = 0.0, tau;
+        switch (shape) {
+          case 1:
+              tau = PI * (t - 1.5 * ts - tshift) / (ts);
+              amp = (((1.0 - 2.0 * tau * tau) * exp(-tau * tau)));
+              break;
+          case 2:
+              if ((t < tshift) || (t > (tshift + ts)))
+                  amp = 0.0;
+              else
+                  amp = (sin(2.0 * PI * (t - tshift) * fc) - 0.5 * sin(4.0 * PI * (t - tshift) * fc));
+              break;
+          case 3: /* wavelet.c:70-75 */
+              amp = n <= nfile ? file[n - 1] : 0.0;
+              break;
+          case 4:
+              if ((t < tshift) || (t > (tshift + ts)))
+                  amp = 0.0;
+              else
+                  amp = pow(sin(PI * (t - tshift) / ts), 3.0);
+              break;
+          case 5: { /* Berlage, wavelet.c:82-96: rows 9, 10, 11 */
+              float ex = srcpos[8 * nsrc + k], alpha = srcpos[9 * nsrc + k];
+              float phi0 = srcpos[10 * nsrc + k] * PI / 180;
+              if (ex <= 0)
+                  return 1;
+              if (t < tshift)
+                  amp = 0.0;
+              else
+                  amp = a * pow((t - tshift), ex) * exp(-alpha * (t - tshift)) * cos(2 * PI * fc * (t - tshift) + phi0);
+              break;
+          }
+          case 6: { /* Klauder, wavelet.c:97-125: rows 9..12. The carrier
+                     * exp(2 pi i fc t') goes through the real exp() of
+                     * <math.h> (no <tgmath.h> in the reference), which takes
+                     * the argument's real part, 0: the factor is 1. */
+              float fmin = srcpos[8 * nsrc + k], fmax = srcpos[9 * nsrc + k];
+              float T = srcpos[10 * nsrc + k], width = srcpos[11 * nsrc + k];
+              float f2 = (fmax - fmin) / T, taper;
+              tau = (width / fc);
+              if ((t < tshift) || (t > (tau * 2) + tshift)) {
+                  amp = 0.0;
+              } else if (t < (tau * 0.2) + tshift) {
+                  amp = sin(PI * f2 * (t - tau - tshift) * (T - (t - tau - tshift))) / (PI * f2 * (t - tau - tshift)) *
+                        exp(0.0);
+                  taper = (1 - cos(((t - tshift) / tau / 0.2) * PI)) / 2;
+                  amp = amp * taper;
+              } else if (t > (tau * 1.8) + tshift) {
+                  amp = sin(PI * f2 * (t - tau - tshift) * (T - (t - tau - tshift))) / (PI * f2 * (t - tau - tshift)) *
+                        exp(0.0);
+                  taper = (1 - cos(((2 * tau + tshift - t) / 0.2 / tau) * PI)) / 2;
+                  amp = amp * taper;
+              } else {
+                  amp = sin(PI * f2 * (t - tau - tshift) * (T - (t - tau - tshift))) / (PI * f2 * (t - tau - tshift)) *
+                        exp(0.0);
+              }
+              break;
+          }
+          default:
+              return 1;
+        }
+        if (fabs(amp) > sigmax)
+            sigmax = fabs(amp);
+        out[n - 1] = amp * a;
+    }
+    if (0.0 == sigmax) /* wavelet.c:135-136 */
+        return 2;
+    if (shape == 5 || shape == 6)
+        for (int n = 1; n <= nt; n++)
+            out[n - 1] = out[n - 1] / sigmax;
+    return 0;
+}
+
 int orc_wavelet(int shape, int nt, float dt, int nsrc, const float *srcpos, float *out)
 {
-    /* wavelet.c:46-130; srcpos rows are 1-based in the reference: row r -> srcpos[(r-1)*nsrc + k] */
+    /* wavelet.c:46-142; srcpos rows are 1-based in the reference: row r -> srcpos[(r-1)*nsrc + k] */
+    if (shape == 3)
+        return 1;
     for (int k = 0; k < nsrc; k++) {
-        float tshift = srcpos[3 * nsrc + k];
-        float fc = srcpos[4 * nsrc + k];
-        float a = srcpos[5 * nsrc + k];
-        float ts = 1.0 / fc;
-        for (int n = 1; n <= nt; n++) {
-            float t = (float)n * dt;
-            float amp = 0.0, tau;
-            switch (shape) {
-              case 1:
-                  tau = PI * (t - 1.5 * ts - tshift) / (ts);
-                  amp = (((1.0 - 2.0 * tau * tau) * exp(-tau * tau)));
-                  break;
-              case 2:
-                  if ((t < tshift) || (t > (tshift + ts)))
-                      amp = 0.0;
-                  else
-                      amp = (sin(2.0 * PI * (t - tshift) * fc) - 0.5 * sin(4.0 * PI * (t - tshift) * fc));
-                  break;
-              case 4:
-                  if ((t < tshift) || (t > (tshift + ts)))
-                      amp = 0.0;
-                  else
-                      amp = pow(sin(PI * (t - tshift) / ts), 3.0);
-                  break;
-              default:
-                  return 1;
-            }
-            out[(size_t)k * nt + (n - 1)] = amp * a;
-        }
+        int rc = wavelet_one(shape, nt, dt, nsrc, k, srcpos, NULL, 0, out + (size_t)k * nt);
+        if (rc)
+            return rc;
+    }
+    return 0;
+}
+
+int orc_wavelet_samples(int nt, float dt, int nsrc, const float *srcpos, const float *samples, int ns, float *out)
+{
+    for (int k = 0; k < nsrc; k++) {
+        int rc = wavelet_one(3, nt, dt, nsrc, k, srcpos, samples, ns, out + (size_t)k * nt);
+        if (rc)
+            return rc;
     }
     return 0;
 }

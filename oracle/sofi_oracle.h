@@ -74,6 +74,8 @@ int orc_set_receivers(orc_ctx *c, int ntr, const int *ix, const int *iy);
 /* Wavelet (reference src/wavelet.c:33-149), shapes 1 (Ricker), 2 (Fuchs-Mueller),
  * 4 (sin^3). srcpos as above; out is [nsrc][nt]. */
 int orc_wavelet(int shape, int nt, float dt, int nsrc, const float *srcpos, float *out);
+/* SOURCE_SHAPE 3: the samples of the signal file (read_srcsig.c) times each source's amplitude */
+int orc_wavelet_samples(int nt, float dt, int nsrc, const float *srcpos, const float *samples, int ns, float *out);
 
 /* zero_wavefield + snapshot counter reset, then steps nt = 1..nsteps of the
  * reference time loop (continuing from the current step on later calls). */

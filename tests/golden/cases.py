@@ -70,6 +70,55 @@ CASES = [
     _case("el_fdt4_cpml", fdorder=6, fdorder_time=4, dt=1.0e-4, nt=600, seed=43, compiled_ref=False),
 ]
 
+# Source wavelets (wavelet.c, read_srcsig.c) on a 40 x 40 grid, NT 600, DT
+# 1e-4 s: the source-file line (x y tshift, then the shape's columns), and for
+# SOURCE_SHAPE 3 the signal file. The reference writes the first source's
+# signal with SIGOUT = 1 (initsrc.c:64-93), as float32 (SIGOUT_FORMAT 3).
+WAVELET_NT, WAVELET_DT = 600, 1.0e-4
+
+
+def _signal_samples(n, seed):
+    rng = np.random.default_rng(seed)
+    t = np.arange(n) * WAVELET_DT
+    return (np.sin(2 * np.pi * 35.0 * t) * np.exp(-((t - 0.01) / 0.006) ** 2)
+            + 0.01 * rng.standard_normal(n)).astype(np.float32)
+
+
+WAVELET_CASES = [
+    dict(name="ricker", shape=1, line="41.0 41.0 0.002 40.0 1.5"),
+    dict(name="fuchs_mueller", shape=2, line="41.0 41.0 0.01 35.0 0.75"),
+    dict(name="sin3", shape=4, line="41.0 41.0 0.005 25.0 2.0 0.0 3"),
+    dict(name="berlage", shape=5, line="41.0 41.0 0.005 30.0 2.0 2.0 150.0 -90.0"),
+    dict(name="berlage_typed", shape=5, line="41.0 41.0 0.0 45.0 0.5 0.5 60.0 30.0 0.0 2"),
+    dict(name="klauder", shape=6, line="41.0 41.0 0.0 10.0 60.0 1.0 0.5 3.0"),
+    dict(name="klauder_late", shape=6, line="41.0 41.0 0.004 20.0 80.0 2.5 1.0 2.0 0.0 1"),
+    dict(name="file_ascii", shape=3, line="41.0 41.0 0.0 30.0 1.25", signal_file="signal.dat",
+         signal=_signal_samples(450, 5), signal_dt_line="# DT = 1.0e-04"),
+    dict(name="file_su", shape=3, line="41.0 41.0 0.0 30.0 0.8", signal_file="signal.su",
+         signal=_signal_samples(700, 6)),
+]
+
+
+def write_signal_file(case, work):
+    """The SOURCE_SHAPE 3 signal file of a wavelet case: ASCII one value per
+    line (repr, exact in float32) after a DT comment, or an SU trace whose
+    header states ns and dt [us] (su_struct.h offsets 114 and 116)."""
+    path = os.path.join(work, case["signal_file"])
+    sig = case["signal"]
+    if path.endswith(".su"):
+        hdr = np.zeros(240, np.uint8)
+        hdr[114:116] = np.array([sig.size], np.uint16).view(np.uint8)
+        hdr[116:118] = np.array([int(round(WAVELET_DT * 1e6))], np.uint16).view(np.uint8)
+        with open(path, "wb") as fh:
+            fh.write(hdr.tobytes() + sig.astype(np.float32).tobytes())
+    else:
+        with open(path, "w") as fh:
+            fh.write(case["signal_dt_line"] + "\n")
+            for v in sig:
+                fh.write(f"{float(v)!r}\n")
+    return path
+
+
 # MODE = FWI (one gradient pass, ITERMAX 1, DTINV 1, LNORM 2): EL_ISO only,
 # NDT = 1 and full-grid gradients (IDX = IDY = 1). The observed data come from
 # the same acquisition on `true_model` (a faster, denser blob).

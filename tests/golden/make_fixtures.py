@@ -31,7 +31,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
-from tests.golden.cases import CASES, FWI_CASES, fwi_json_text, json_text, synthetic_model, true_model, write_case  # noqa: E402
+from tests.golden.cases import (CASES, FWI_CASES, WAVELET_CASES, WAVELET_DT, WAVELET_NT, _case, fwi_json_text,  # noqa: E402
+                                json_text, synthetic_model, true_model, write_case, write_signal_file)
 
 SHIPPED = {"weq3": "EL_ISO", "weq4": "VEL_ISO", "weq5": "EL_VTI", "weq6": "VEL_VTI", "weq7": "EL_TTI",
            "weq8": "VEL_TTI", "weq3_fy": "EL_ISO", "weq8_fy": "VEL_TTI", "weq3_fdt4": "EL_ISO",
@@ -132,6 +133,41 @@ def ref_examples(reference, exe):
             shutil.rmtree(work, ignore_errors=True)
 
 
+def ref_wavelets(exe):
+    """The first source's signal as the compiled reference computes it
+    (wavelet.c) for every SOURCE_SHAPE, written by its SIGOUT output in
+    float32: ref_wavelets.npz holds, per case, the signal and the inputs."""
+    out = {}
+    for wc in WAVELET_CASES:
+        work = tempfile.mkdtemp(prefix="sofi_wav_")
+        try:
+            case = _case("wav_" + wc["name"], nx=40, ny=40, dh=2.0, dt=WAVELET_DT, nt=WAVELET_NT, fw=0, abs_type=0,
+                         seismo=1, ndt=1, snap=0, seed=3)
+            jpath, _ = write_case(case, work)
+            with open(os.path.join(work, "source.dat"), "w") as fh:
+                fh.write(wc["line"] + "\n")
+            txt = open(jpath).read()
+            sigfile = "none"
+            if wc["shape"] == 3:
+                write_signal_file(wc, work)
+                sigfile = "./" + wc["signal_file"]
+            txt = txt.replace('"SOURCE_SHAPE" : "1"', f'"SOURCE_SHAPE" : "{wc["shape"]}"')
+            txt = txt.replace('"SIGNAL_FILE" : "none"', f'"SIGNAL_FILE" : "{sigfile}"')
+            txt = txt.replace('"SIGOUT" : "0",', '"SIGOUT" : "1",\n"SIGOUT_FORMAT" : "3",\n"SIGOUT_FILE" : "./out/sig",')
+            with open(jpath, "w") as fh:
+                fh.write(txt)
+            r = subprocess.run([exe, jpath], cwd=work, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"{wc['name']}: reference failed\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}")
+            sig = np.fromfile(os.path.join(work, "out", "sig.shot1.bin"), dtype=np.float32)
+            assert sig.size == WAVELET_NT, (wc["name"], sig.size)
+            out[f"{wc['name']}_signal"] = sig
+            print("wrote wavelet", wc["name"], float(np.abs(sig).max()))
+        finally:
+            shutil.rmtree(work, ignore_errors=True)
+    np.savez_compressed(os.path.join(HERE, "ref_wavelets.npz"), **out)
+
+
 def run_reference_fwi(case, exe):
     """Observed data from a forward run on the case's true model, then one
     FWI gradient pass on its model (MODE = FWI), both with the compiled
@@ -191,6 +227,10 @@ def main():
         ref_examples(a.reference, exe)
     if not a.only or a.only == "sigout":
         shipped_sigout(a.reference)
+        if a.only:
+            return
+    if not a.only or a.only == "wavelets":
+        ref_wavelets(exe)
         if a.only:
             return
     for case in FWI_CASES:

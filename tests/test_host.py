@@ -9,7 +9,7 @@ import os
 import numpy as np
 import pytest
 
-from tests.golden.cases import CASES, synthetic_model
+from tests.golden.cases import CASES, WAVELET_CASES, WAVELET_DT, WAVELET_NT, synthetic_model, write_signal_file
 from tests.helpers import case_config, prepared_model, GOLDEN
 
 
@@ -52,6 +52,46 @@ def test_host_wavelet_equals_oracle(H, oracle_mod):
     sp[5] = [1.0, 2.0, 0.5]
     for shape in (1, 2, 4):
         np.testing.assert_array_equal(H.wavelet(shape, 500, 1e-4, sp), oracle_mod.wavelet(shape, 500, 1e-4, sp))
+
+
+@pytest.mark.parametrize("wc", WAVELET_CASES, ids=[w["name"] for w in WAVELET_CASES])
+def test_wavelets_equal_compiled_reference(H, oracle_mod, wc, tmp_path):
+    """Every SOURCE_SHAPE: the source-file columns read by the host library,
+    the signal file (SOURCE_SHAPE 3, ASCII and SU), and the signal of the
+    host library and of the oracle equal the compiled reference's SIGOUT
+    output bit for bit (tests/golden/ref_wavelets.npz, wavelet.c,
+    read_srcsig.c, sources.c)."""
+    ref = np.load(os.path.join(GOLDEN, "ref_wavelets.npz"))[f"{wc['name']}_signal"]
+    src = tmp_path / "source.dat"
+    src.write_text("# a comment line\n" + wc["line"] + "\n")
+    p = H.make_par(weq=2, nx=40, ny=40, dh=2.0, dt=WAVELET_DT, nt=WAVELET_NT, source_shape=wc["shape"],
+                   source_type=1)
+    sp, xy = H.read_sources(p, str(src))
+    assert sp.shape == (12, 1) and xy[0, 0] == 41.0
+    sigfile = write_signal_file(wc, str(tmp_path)) if wc["shape"] == 3 else None
+    got = H.wavelet(wc["shape"], WAVELET_NT, WAVELET_DT, sp, signal_file=sigfile)[0]
+    np.testing.assert_array_equal(got, ref, err_msg=wc["name"])
+    samples = oracle_mod.read_srcsig(sigfile, WAVELET_DT) if sigfile else None
+    if sigfile:
+        np.testing.assert_array_equal(H.read_signal(sigfile, WAVELET_DT), samples)
+    orc = oracle_mod.wavelet(wc["shape"], WAVELET_NT, WAVELET_DT, sp, samples=samples)[0]
+    np.testing.assert_array_equal(orc, ref, err_msg=wc["name"])
+
+
+def test_wavelet_errors(H, tmp_path):
+    """A Berlage exponent <= 0, an all-zero signal and a signal file whose DT
+    differs are errors (wavelet.c:88-89,135-136, read_srcsig.c:172-175)."""
+    sp = np.zeros((12, 1), np.float32)
+    sp[4], sp[5], sp[8] = 30.0, 1.0, 0.0
+    with pytest.raises(RuntimeError, match="exponent"):
+        H.wavelet(5, 100, 1e-4, sp)
+    sp[3] = 1.0  # sin^3 starting after the last step: all zero
+    with pytest.raises(RuntimeError, match="zeros"):
+        H.wavelet(4, 100, 1e-4, sp)
+    f = tmp_path / "s.txt"
+    f.write_text("# DT = 2.0e-04\n0.5\n1.0\n")
+    with pytest.raises(RuntimeError, match="interval"):
+        H.read_signal(str(f), 1e-4)
 
 
 def test_host_holberg_table(H, oracle_mod):
