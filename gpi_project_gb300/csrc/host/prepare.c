@@ -250,6 +250,100 @@ static void damping_frame(const sofih_par *p, sofih_prep *m)
     free(coeff);
 }
 
+/* The reference's built-in models (READMOD = 0, readmod.c:60-83), MemModel
+ * arrays as they leave it. hh_elastic.c / hh_visco.c: a half space below
+ * y = 100 m (vp 3500, vs 2000, rho 2000) under a layer with vp 0, vs 1,
+ * rho 1; the viscoelastic one with tau 0.01 (2.0 for 95 <= y <= 110 m).
+ * hh_elastic_VTI.c / hh_elastic_TTI.c / hh_visco_VTI.c / hh_visco_TTI.c: a
+ * homogeneous medium, c11 34.3, c33 22.7, c55 5.4, c13 10.7 GPa, rho 2000
+ * (Jones and Wang 1981), tilted by 0 (elastic TTI) or 30 degrees
+ * (viscoelastic TTI), tau = TAU. Float variables as the reference's. */
+static void builtin_media(const sofih_par *p, int L, const float *pts, float ws, h1 prho, h1 ppi, h1 pu, h1 taus,
+                          h1 taup, h1 c11, h1 c13, h1 c33, h1 c55, h1 c15, h1 c35, h1 t11, h1 t13, h1 t33, h1 t55,
+                          h1 t15, h1 t35, float *vpmin, float *vpmax, float *vsmin, float *vsmax)
+{
+    const int weq = p->weq, NX = p->nx, NY = p->ny;
+    if (weq == 2 || weq == 3) {
+        const float vp1 = 0.0, vs1 = 1.0, rho1 = 1.0, h = 100.0;
+        const float vp2 = 3500.0, vs2 = 2000.0, rho2 = 2000.0;
+        const float tp1 = 0.01, ts1 = 0.01, tp2 = 0.01, ts2 = 0.01, h1_ = 95.0, h2_ = 110.0, tlp = 2.0, tls = 2.0;
+        for (int i = 1; i <= NX; i++)
+            for (int j = 1; j <= NY; j++) {
+                const float y = (float)j * p->dh;
+                const int top = y <= h;
+                const float Vp = top ? vp1 : vp2, Vs = top ? vs1 : vs2, Rhov = top ? rho1 : rho2;
+                if (weq == 2) {
+                    H(pu, j, i) = Vs * Vs * Rhov;
+                    H(ppi, j, i) = Vp * Vp * Rhov;
+                } else {
+                    float tp = top ? tp1 : tp2, ts = top ? ts1 : ts2;
+                    if ((y >= h1_) && (y <= h2_))
+                        tp = tlp, ts = tls;
+                    float sumu = 0.0, sumpi = 0.0;
+                    for (int l = 1; l <= L; l++) {
+                        sumu = sumu + ((ws * ws * pts[l] * pts[l] * ts) / (1.0 + ws * ws * pts[l] * pts[l]));
+                        sumpi = sumpi + ((ws * ws * pts[l] * pts[l] * tp) / (1.0 + ws * ws * pts[l] * pts[l]));
+                    }
+                    H(taus, j, i) = ts, H(taup, j, i) = tp;
+                    H(pu, j, i) = Vs * Vs * Rhov / (1.0 + sumu);
+                    H(ppi, j, i) = Vp * Vp * Rhov / (1.0 + sumpi);
+                }
+                H(prho, j, i) = Rhov;
+            }
+        *vpmin = *vpmax = vp2, *vsmin = *vsmax = vs2;
+        return;
+    }
+    const float C11 = 34.3e9, C33 = 22.7e9, C55 = 5.4e9, C13 = 10.7e9, RHO = 2000.0;
+    float c11v = C11, c33v = C33, c55v = C55, c13v = C13, tau11 = 0, tau13 = 0, tau55 = 0;
+    if (L) {
+        const float tau = p->tau;
+        float sumc11 = 0.0, sumc33 = 0.0, sumc55 = 0.0, sumc13 = 0.0;
+        for (int l = 1; l <= L; l++) {
+            sumc11 = sumc11 + ((ws * ws * pts[l] * pts[l] * tau) / (1.0 + ws * ws * pts[l] * pts[l]));
+            sumc33 = sumc33 + ((ws * ws * pts[l] * pts[l] * tau) / (1.0 + ws * ws * pts[l] * pts[l]));
+            sumc55 = sumc55 + ((ws * ws * pts[l] * pts[l] * tau) / (1.0 + ws * ws * pts[l] * pts[l]));
+        }
+        c11v = c11v / (1.0 + sumc11);
+        c33v = c33v / (1.0 + sumc33);
+        c55v = c55v / (1.0 + sumc55);
+        tau11 = tau, tau55 = tau;
+        tau13 = (c11v * L * tau11 - 2.0 * c55v * L * tau55) / (c11v - 2.0 * c55v);
+        for (int l = 1; l <= L; l++)
+            sumc13 = sumc13 + ((ws * ws * pts[l] * pts[l] * tau13) / (1.0 + ws * ws * pts[l] * pts[l]));
+        c13v = c13v / (1.0 + sumc13);
+    }
+    float o[6] = {c11v, c33v, c13v, c55v, 0.f, 0.f};
+    if (is_tti(weq)) {
+        const float THETA = weq == 7 ? 30.0 : 0.0;
+        const float t = THETA * PI / 180.0;
+        const float l1 = cos(t), l2 = sin(t);
+        const float l12 = l1 * l1, l22 = l2 * l2, l14 = l12 * l12, l24 = l22 * l22, l13 = l1 * l12, l23 = l2 * l22;
+        const float a1 = 2.0 * c13v + 4.0 * c55v, a3 = c11v + c33v - 4.0 * c55v, a4 = c11v + c33v - 2.0 * c13v;
+        const float a5 = c13v - c11v + 2.0 * c55v, a6 = c13v - c33v + 2.0 * c55v;
+        o[0] = c11v * l14 + c33v * l24 + a1 * l12 * l22;
+        o[1] = c11v * l24 + c33v * l14 + a1 * l12 * l22;
+        o[2] = a3 * l12 * l22 + c13v * (l14 + l24);
+        o[3] = a4 * l12 * l22 + c55v * (l12 - l22) * (l12 - l22);
+        o[4] = a5 * l13 * l2 - a6 * l1 * l23;
+        o[5] = a5 * l23 * l1 - a6 * l2 * l13;
+    }
+    for (int i = 1; i <= NX; i++)
+        for (int j = 1; j <= NY; j++) {
+            H(prho, j, i) = RHO;
+            H(c11, j, i) = o[0], H(c33, j, i) = o[1], H(c13, j, i) = o[2], H(c55, j, i) = o[3];
+            if (is_tti(weq))
+                H(c15, j, i) = o[4], H(c35, j, i) = o[5];
+            if (L) {
+                H(t11, j, i) = tau11, H(t33, j, i) = tau11, H(t13, j, i) = tau13, H(t55, j, i) = tau55;
+                if (is_tti(weq))
+                    H(t15, j, i) = tau13, H(t35, j, i) = tau13;
+            }
+        }
+    /* phase velocities of the medium: vertical / horizontal P, S */
+    const float vv = sqrtf(c33v / RHO), vh = sqrtf(c11v / RHO), vs = sqrtf(c55v / RHO);
+    *vpmin = vv < vh ? vv : vh, *vpmax = vv > vh ? vv : vh, *vsmin = *vsmax = vs;
+}
+
 int sofih_prepare(const sofih_par *p, const float *vp, const float *vs, const float *rho, const float *qp,
                   const float *qs, const float *eps, const float *del, const float *theta, int nthreads,
                   sofih_prep **out)
@@ -260,7 +354,17 @@ int sofih_prepare(const sofih_par *p, const float *vp, const float *vs, const fl
         sofih_set_error("prepare: unsupported WEQ %d or empty grid", weq);
         return 1;
     }
-    if (!vp || (!vs && weq != 0) || !rho || (L && (!qp || !qs)) || (weq >= 4 && (!eps || !del)) || (is_tti(weq) && !theta)) {
+    if (!p->readmod && (weq == 0 || p->mode_fwi)) {
+        sofih_set_error("prepare: the built-in model (READMOD = 0) exists for WEQ 2..7 in MODE = FW only");
+        return 1;
+    }
+    if (!p->readmod && (vp || vs || rho)) {
+        sofih_set_error("prepare: READMOD = 0 selects the built-in model, but material arrays were given "
+                        "(set READMOD = 1 to use them)");
+        return 1;
+    }
+    if (p->readmod && (!vp || (!vs && weq != 0) || !rho || (L && (!qp || !qs)) || (weq >= 4 && (!eps || !del)) ||
+                       (is_tti(weq) && !theta))) {
         sofih_set_error("prepare: missing material arrays for WEQ %d", weq);
         return 1;
     }
@@ -300,6 +404,10 @@ int sofih_prepare(const sofih_par *p, const float *vp, const float *vs, const fl
         }
     }
     float vpmin = 1e30f, vpmax = 0.f, vsmin = 1e30f, vsmax = 0.f;
+    if (!p->readmod) {
+        builtin_media(p, L, pts, ws, prho, ppi, pu, taus, taup, c11, c13, c33, c55, c15, c35, t11, t13, t33, t55, t15,
+                      t35, &vpmin, &vpmax, &vsmin, &vsmax);
+    } else
 #pragma omp parallel for schedule(static) reduction(min : vpmin, vsmin) reduction(max : vpmax, vsmax)
     for (int i = 1; i <= NX; i++)
         for (int j = 1; j <= NY; j++) {

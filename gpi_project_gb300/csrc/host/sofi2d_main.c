@@ -151,10 +151,11 @@ int main(int argc, char **argv)
     if (sofih_read_par(argv[1], &p))
         DIE_H();
     float *mat[8] = {0};
-    if (sofih_read_model(&p, p.mfile, mat, 8))
+    /* READMOD = 0: the reference's built-in model, no model files (readmod.c:60-83) */
+    if (p.readmod && sofih_read_model(&p, p.mfile, mat, 8))
         DIE_H();
     const char *names[8];
-    int nm = sofih_model_suffixes(p.weq, names, 8);
+    int nm = p.readmod ? sofih_model_suffixes(p.weq, names, 8) : 0;
     float *vp = NULL, *vs = NULL, *rho = NULL, *qp = NULL, *qs = NULL, *eps = NULL, *del = NULL, *tet = NULL;
     for (int k = 0; k < nm; k++) {
         float **dst = !strcmp(names[k], "vp") ? &vp : !strcmp(names[k], "vs") ? &vs : !strcmp(names[k], "rho") ? &rho

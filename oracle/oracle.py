@@ -54,7 +54,8 @@ class OrcParams(ctypes.Structure):
                 ("f_ref", ctypes.c_float), ("fl", ctypes.c_float * 8), ("seismo", ctypes.c_int),
                 ("ndt", ctypes.c_int), ("snap", ctypes.c_int), ("tsnap1", ctypes.c_float),
                 ("tsnap2", ctypes.c_float), ("tsnapinc", ctypes.c_float), ("idx", ctypes.c_int),
-                ("idy", ctypes.c_int), ("nthreads", ctypes.c_int), ("fdorder_time", ctypes.c_int)]
+                ("idy", ctypes.c_int), ("nthreads", ctypes.c_int), ("fdorder_time", ctypes.c_int),
+                ("readmod", ctypes.c_int), ("tau", ctypes.c_float)]
 
 
 _LIBS: dict = {}
@@ -155,6 +156,8 @@ class SofiConfig:
     idx: int = 1
     idy: int = 1
     mfile: str = ""
+    readmod: int = 1
+    tau: float = 0.0001
     seis_file: str = ""
     snap_file: str = ""
 
@@ -174,6 +177,7 @@ class SofiConfig:
         p.idx, p.idy = self.idx, self.idy
         p.nthreads = nthreads
         p.fdorder_time = self.fdorder_time
+        p.readmod, p.tau = self.readmod, self.tau
         return p
 
 

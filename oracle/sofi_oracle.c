@@ -914,9 +914,106 @@ static void absorb(orc_ctx *c)
     }
 }
 
+/* The built-in models of readmod.c:60-83 (READMOD = 0): hh_elastic.c:31-71,
+ * hh_visco.c:31-104, hh_elastic_VTI.c, hh_elastic_TTI.c (Bond transformation
+ * at THETA = 0), hh_visco_VTI.c:31-107, hh_visco_TTI.c (THETA = 30). */
+static int hh_model(orc_ctx *c)
+{
+    int weq = c->P.weq, L = c->P.L;
+    real pts[ORC_MAX_L + 1], ws = 0;
+    if (is_visco(weq))
+        visco_pts(c, pts, &ws);
+    if (weq == ORC_EL_ISO || weq == ORC_VEL_ISO) {
+        const real vp1 = 0.0, vs1 = 1.0, rho1 = 1.0, tp1 = 0.01, ts1 = 0.01, h = 100.0;
+        const real vp2 = 3500.0, vs2 = 2000.0, rho2 = 2000.0, tp2 = 0.01, ts2 = 0.01;
+        const real h1 = 95.0, h2 = 110.0, tlp = 2.0, tls = 2.0;
+        for (int i = 1; i <= c->P.nx; i++)
+            for (int j = 1; j <= c->P.ny; j++) {
+                real y = (real)j * c->DH, Vp, Vs, Rhov, tp, ts;
+                if (y <= h)
+                    Vp = vp1, Vs = vs1, Rhov = rho1, tp = tp1, ts = ts1;
+                else
+                    Vp = vp2, Vs = vs2, Rhov = rho2, tp = tp2, ts = ts2;
+                if (weq == ORC_EL_ISO) {
+                    A(c->pu, j, i) = Vs * Vs * Rhov;
+                    A(c->ppi, j, i) = Vp * Vp * Rhov;
+                } else {
+                    if ((y >= h1) && (y <= h2))
+                        tp = tlp, ts = tls;
+                    real sumu = 0.0, sumpi = 0.0;
+                    for (int l = 1; l <= L; l++) {
+                        sumu = sumu + ((ws * ws * pts[l] * pts[l] * ts) / (1.0 + ws * ws * pts[l] * pts[l]));
+                        sumpi = sumpi + ((ws * ws * pts[l] * pts[l] * tp) / (1.0 + ws * ws * pts[l] * pts[l]));
+                    }
+                    A(c->ptaus, j, i) = ts;
+                    A(c->ptaup, j, i) = tp;
+                    A(c->pu, j, i) = Vs * Vs * Rhov / (1.0 + sumu);
+                    A(c->ppi, j, i) = Vp * Vp * Rhov / (1.0 + sumpi);
+                }
+                A(c->prho, j, i) = Rhov;
+            }
+        return 0;
+    }
+    if (is_iso(weq)) {
+        snprintf(c->err, sizeof c->err, "Internal model for your chosen WEQ not implemented.");
+        return 1;
+    }
+    /* Jones and Wang (1981) */
+    const real C11 = 34.3e9, C33 = 22.7e9, C55 = 5.4e9, C13 = 10.7e9, RHO = 2000.0;
+    real c11 = C11, c33 = C33, c55 = C55, c13 = C13, tau11 = 0, tau13 = 0, tau55 = 0;
+    if (is_visco(weq)) {
+        const real TAU = c->P.tau;
+        real sumc11 = 0.0, sumc33 = 0.0, sumc55 = 0.0, sumc13 = 0.0;
+        for (int l = 1; l <= L; l++) {
+            sumc11 = sumc11 + ((ws * ws * pts[l] * pts[l] * TAU) / (1.0 + ws * ws * pts[l] * pts[l]));
+            sumc33 = sumc33 + ((ws * ws * pts[l] * pts[l] * TAU) / (1.0 + ws * ws * pts[l] * pts[l]));
+            sumc55 = sumc55 + ((ws * ws * pts[l] * pts[l] * TAU) / (1.0 + ws * ws * pts[l] * pts[l]));
+        }
+        c11 = c11 / (1.0 + sumc11);
+        c33 = c33 / (1.0 + sumc33);
+        c55 = c55 / (1.0 + sumc55);
+        tau11 = TAU, tau55 = TAU;
+        tau13 = (c11 * L * tau11 - 2.0 * c55 * L * tau55) / (c11 - 2.0 * c55);
+        for (int l = 1; l <= L; l++)
+            sumc13 = sumc13 + ((ws * ws * pts[l] * pts[l] * tau13) / (1.0 + ws * ws * pts[l] * pts[l]));
+        c13 = c13 / (1.0 + sumc13);
+    }
+    real o[6] = {c11, c33, c13, c55, 0, 0};
+    if (is_tti(weq))
+        bond_tti(c11, c13, c33, c55, weq == ORC_VEL_TTI ? 30.0 : 0.0, o);
+    for (int i = 1; i <= c->P.nx; i++)
+        for (int j = 1; j <= c->P.ny; j++) {
+            A(c->prho, j, i) = RHO;
+            A(c->pc11, j, i) = o[0];
+            A(c->pc33, j, i) = o[1];
+            A(c->pc13, j, i) = o[2];
+            A(c->pc55, j, i) = o[3];
+            if (is_tti(weq)) {
+                A(c->pc15, j, i) = o[4];
+                A(c->pc35, j, i) = o[5];
+            }
+            if (is_visco(weq)) {
+                A(c->ptau11, j, i) = tau11;
+                A(c->ptau33, j, i) = tau11;
+                A(c->ptau13, j, i) = tau13;
+                A(c->ptau55, j, i) = tau55;
+                if (is_tti(weq)) {
+                    A(c->ptau15, j, i) = tau13;
+                    A(c->ptau35, j, i) = tau13;
+                }
+            }
+        }
+    return 0;
+}
+
 int orc_prepare(orc_ctx *c)
 {
     int weq = c->P.weq;
+    if (!c->P.readmod) {
+        if (hh_model(c))
+            return 1;
+        goto prepared_media;
+    }
     if (!c->mat_vp || (!c->mat_vs && !is_ac(weq)) || !c->mat_rho) {
         snprintf(c->err, sizeof c->err, "vp/vs/rho missing");
         return 1;
@@ -937,6 +1034,7 @@ int orc_prepare(orc_ctx *c)
         readmod_visco(c);
     else
         readmod_aniso(c);
+prepared_media:
     if (c->P.fw > 0 && c->P.abs_type == 1)
         pml_pro(c);
     if (c->P.fw > 0 && c->P.abs_type == 2)

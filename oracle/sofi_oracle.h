@@ -48,6 +48,8 @@ typedef struct {
     int idx, idy;
     int nthreads;           /* OpenMP threads for the cell loops (0 = default) */
     int fdorder_time;       /* 2 (or 0) leapfrog, 4 Adams-Bashforth (gv->FDORDER_TIME) */
+    int readmod;            /* 1: materials from orc_set_material, 0: the reference's built-in model (READMOD) */
+    float tau;              /* gv->TAU of the built-in anisotropic viscoelastic models */
 } orc_params;
 
 typedef struct orc_ctx orc_ctx;

@@ -68,6 +68,17 @@ CASES = [
     _case("visc_fdt4_abs", weq=3, L=1, fl=[30.0], f_ref=30.0, fdorder=8, maxrelerror=1, abs_type=2, fdorder_time=4,
           dt=1.0e-4, nt=600, seed=42),
     _case("el_fdt4_cpml", fdorder=6, fdorder_time=4, dt=1.0e-4, nt=600, seed=43, compiled_ref=False),
+    # the reference's built-in models (READMOD = 0, hh_*.c): a half space below
+    # 100 m under a vp = 0 layer (isotropic), or a homogeneous VTI / TTI medium
+    _case("hh_el", readmod=0, nx=90, ny=80, fdorder=4, seed=51, sources=[[91.0, 131.0, 0.0, 40.0, 1.0]]),
+    _case("hh_visc_l2", readmod=0, weq=3, L=2, fl=[10.0, 50.0], f_ref=25.0, nx=90, ny=80, fdorder=6, seed=52,
+          sources=[[91.0, 131.0, 0.0, 40.0, 1.0]]),
+    _case("hh_vti", readmod=0, weq=4, dt=1.5e-4, nt=500, nx=90, ny=80, seed=53),
+    _case("hh_vvti_l1", readmod=0, weq=5, L=1, fl=[30.0], f_ref=30.0, tau=0.05, dt=1.5e-4, nt=500, nx=90, ny=80,
+          seed=54),
+    _case("hh_tti", readmod=0, weq=6, dt=1.5e-4, nt=500, fdorder=6, nx=90, ny=80, seed=55),
+    _case("hh_vtti_l2", readmod=0, weq=7, L=2, fl=[10.0, 50.0], f_ref=25.0, tau=0.05, dt=1.5e-4, nt=500, nx=90,
+          ny=80, seed=56),
 ]
 
 # Source wavelets (wavelet.c, read_srcsig.c) on a 40 x 40 grid, NT 600, DT
@@ -203,7 +214,8 @@ def json_text(case) -> str:
         "DH": repr(case["dh"]), "TIME": repr(case["nt"] * case["dt"]), "DT": repr(case["dt"]), "WEQ": weq,
         "SOURCE_SHAPE": "1", "SIGNAL_FILE": "none", "SIGOUT": "0", "SOURCE_TYPE": str(case["source_type"]),
         "SRCREC": "1", "SOURCE_FILE": "./source.dat", "RUN_MULTIPLE_SHOTS": "0", "PLANE_WAVE_DEPTH": "0.0",
-        "PLANE_WAVE_ANGLE": "0.0", "TS": "0.2", "READMOD": "1", "MFILE": "./model/m", "WRITE_MODELFILES": "0",
+        "PLANE_WAVE_ANGLE": "0.0", "TS": "0.2", "READMOD": str(case.get("readmod", 1)), "TAU": repr(case.get("tau", 1e-4)),
+        "MFILE": "./model/m", "WRITE_MODELFILES": "0",
         "L": str(case["L"]), "F_REF": repr(case["f_ref"]), "FREE_SURF": str(case["free_surf"]),
         "BOUNDARY": str(case["boundary"]), "FW": str(case["fw"]), "ABS_TYPE": str(case["abs_type"]),
         "NPOWER": repr(case["npower"]), "K_MAX_CPML": repr(case["k_max_cpml"]), "VPPML": repr(case["vppml"]),

@@ -30,6 +30,7 @@ def case_config(case):
     c.tsnap1 = c.tsnap2 = float(np.float32(case["tsnap"]))
     c.tsnapinc = 1.0
     c.source_type = case["source_type"]
+    c.readmod, c.tau = case.get("readmod", 1), float(np.float32(case.get("tau", 1e-4)))
     return c
 
 

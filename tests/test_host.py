@@ -25,7 +25,7 @@ def par_from_case(H, case, cfg):
                       maxrelerror=cfg.maxrelerror, L=cfg.L, f_ref=cfg.f_ref, fl=cfg.fl, fw=cfg.fw,
                       abs_type=cfg.abs_type, free_surf=cfg.free_surf, boundary=cfg.boundary, npower=cfg.npower,
                       k_max_cpml=cfg.k_max_cpml, vppml=cfg.vppml, fpml=cfg.fpml, damping=cfg.damping,
-                      fdorder_time=cfg.fdorder_time)
+                      fdorder_time=cfg.fdorder_time, readmod=cfg.readmod, tau=cfg.tau)
 
 
 @pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
@@ -36,7 +36,7 @@ def test_host_prepare_equals_oracle(H, case, oracle_mod):
     o = O.Oracle(cfg, "f32", 1)
     o.set_material(mats)
     ref_f, ref_v = prepared_model(o, cfg)
-    got_f, got_v = H.prepare(par_from_case(H, case, cfg), mats, nthreads=4)
+    got_f, got_v = H.prepare(par_from_case(H, case, cfg), mats if case.get("readmod", 1) else {}, nthreads=4)
     for k, a in ref_f.items():
         assert k in got_f, k
         np.testing.assert_array_equal(got_f[k], a, err_msg=f"{case['name']} {k}")
@@ -92,6 +92,22 @@ def test_wavelet_errors(H, tmp_path):
     f.write_text("# DT = 2.0e-04\n0.5\n1.0\n")
     with pytest.raises(RuntimeError, match="interval"):
         H.read_signal(str(f), 1e-4)
+
+
+def test_builtin_model_takes_no_material_arrays(H):
+    """READMOD = 0 selects the reference's built-in model: material arrays
+    given with it are an error (a zeroed parameter struct would otherwise
+    drop them silently), and acoustic media have no built-in model."""
+    n = 30 * 20
+    mats = {"vp": np.full(n, 3000.0, np.float32), "vs": np.full(n, 1700.0, np.float32),
+            "rho": np.full(n, 2000.0, np.float32)}
+    p = H.make_par(weq=2, nx=30, ny=20, dh=2.0, dt=1e-4, nt=10, fdorder=4, readmod=0)
+    with pytest.raises(RuntimeError, match="READMOD"):
+        H.prepare(p, mats)
+    f, _ = H.prepare(p, {})
+    assert f["pu"].max() == np.float32(2000.0) * np.float32(2000.0) * np.float32(2000.0)  # half space mu
+    with pytest.raises(RuntimeError, match="built-in"):
+        H.prepare(H.make_par(weq=0, nx=30, ny=20, dh=2.0, dt=1e-4, nt=10, fdorder=4, readmod=0), {})
 
 
 def test_host_holberg_table(H, oracle_mod):
