@@ -98,14 +98,15 @@ def test_builtin_model_takes_no_material_arrays(H):
     """READMOD = 0 selects the reference's built-in model: material arrays
     given with it are an error (a zeroed parameter struct would otherwise
     drop them silently), and acoustic media have no built-in model."""
-    n = 30 * 20
+    n = 30 * 80
     mats = {"vp": np.full(n, 3000.0, np.float32), "vs": np.full(n, 1700.0, np.float32),
             "rho": np.full(n, 2000.0, np.float32)}
-    p = H.make_par(weq=2, nx=30, ny=20, dh=2.0, dt=1e-4, nt=10, fdorder=4, readmod=0)
+    p = H.make_par(weq=2, nx=30, ny=80, dh=2.0, dt=1e-4, nt=10, fdorder=4, readmod=0)
     with pytest.raises(RuntimeError, match="READMOD"):
         H.prepare(p, mats)
     f, _ = H.prepare(p, {})
-    assert f["pu"].max() == np.float32(2000.0) * np.float32(2000.0) * np.float32(2000.0)  # half space mu
+    # mu of the layer above 100 m and of the half space below
+    assert f["pu"].min() == 1.0 and f["pu"].max() == np.float32(2000.0) * np.float32(2000.0) * np.float32(2000.0)
     with pytest.raises(RuntimeError, match="built-in"):
         H.prepare(H.make_par(weq=0, nx=30, ny=20, dh=2.0, dt=1e-4, nt=10, fdorder=4, readmod=0), {})
 
