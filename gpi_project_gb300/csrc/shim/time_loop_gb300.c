@@ -14,10 +14,21 @@
  * the final wavefield in *mpw and the snapshot files of snap().
  * Supported: MODE=FW (sw = 0), FDORDER_TIME = 2 (and 4 for EL_ISO / VEL_ISO without
  * free surface; the moduli are uploaded as prepmod() left them), one domain (NPROCX = NPROCY = 1),
- * WEQ AC_ISO and EL_ISO..VEL_TTI; anything else stops the run through log_fatal like the
- * reference's own checks. The GPU context (device 0, or $SOFI_GPU_DEVICE)
- * is created on the first call and reused while the configuration holds;
- * the model is uploaded once per iteration `iter` (prepmod runs per iteration).
+ * WEQ AC_ISO and EL_ISO..VEL_TTI; and MODE=FWI for EL_ISO with NDT 1, DTINV 1,
+ * LNORM 2, ADJOINT_TYPE 1..3: the forward call (sw = 0) keeps the gradient
+ * quantities of every step on the GPU (snap_store.c's store stays in device
+ * memory), the backward call (sw = 1, the residuals of calc_res.c as signals
+ * at the receivers, inversion.c:222) runs the adjoint steps with the
+ * correlation of calc_conv.c and adds the shot's gradients to
+ * minv->gradLam_shot / gradMu_shot / gradRhos_shot. Anything else stops the
+ * run through log_fatal like the reference's own checks. The GPU context
+ * (device 0, or $SOFI_GPU_DEVICE) is created on the first call and reused
+ * while the configuration holds; the model is uploaded once per iteration
+ * `iter` (prepmod runs per iteration). *perf accumulates as time_loop.c:94-116,
+ * 264-279,312-314 does: the reference samples steps 1, 1 + OUTNTIMESTEPINFO,
+ * ...; here each sampled step counts the GPU's mean velocity- and
+ * stress-kernel times and the run's mean step time (no exchanges on one
+ * domain).
  */
 #include "fd.h"
 #include "logging.h"
@@ -161,13 +172,46 @@ static void write_snapshots(GlobVar *gv)
     free(frame);
 }
 
+/* One shot's time-loop statistics into *perf (time_loop.c:94-116,264-279,312-314). */
+static void fill_perform(Perform *perf, const GlobVar *gv)
+{
+    const int every = gv->OUTNTIMESTEPINFO > 0 ? gv->OUTNTIMESTEPINFO : 1;
+    const int k = (gv->NT - 1) / every + 1; /* steps nt with (nt - 1) % every == 0 */
+    float ms = 0.f;
+    double vms = 0, sms = 0;
+    long long nv = 0, ns = 0;
+    GPU_CHECK(sofi_last_run_ms(g_ctx, &ms));
+    GPU_CHECK(sofi_kernel_time(g_ctx, "update_v", &vms, &nv));
+    GPU_CHECK(sofi_kernel_time(g_ctx, "update_s", &sms, &ns));
+    perf->infocounter += k;
+    perf->time_av_v_update += k * vms * 1e-3;
+    perf->time_av_s_update += k * sms * 1e-3;
+    perf->time_av_timestep += k * (ms * 1e-3 / gv->NT);
+}
+
+/* A 1-based NR matrix m[1..NY][1..NX] into a contiguous [NY][NX] buffer. */
+static float *dense(float **m, const GlobVar *gv)
+{
+    float *d = (float *)malloc(sizeof(float) * (size_t)gv->NX * gv->NY);
+    for (int j = 1; j <= gv->NY; j++)
+        memcpy(d + (size_t)(j - 1) * gv->NX, &m[j][1], sizeof(float) * gv->NX);
+    return d;
+}
+
 void time_loop(int iter, int ishot, int snapcheck, float *hc, float **srcpos_loc, float **signalx,
                float **signaly, int nsrc, int sw, AcqVar *acq, MemModel *mpm, MemWavefield *mpw,
                MemInv *minv, GlobVar *gv, GlobVarInv *vinv, Perform *perf)
 {
-    (void)signaly, (void)minv, (void)vinv, (void)perf, (void)ishot;
-    if (sw != 0 || gv->MODE != FW)
-        log_fatal("GPU time loop: only forward modelling (MODE=FW) is supported\n");
+    (void)ishot;
+    const int fwi = gv->MODE == FWI;
+    if (gv->MODE != FW && !fwi)
+        log_fatal("GPU time loop: MODE must be FW or FWI\n");
+    if (sw != 0 && !fwi)
+        log_fatal("GPU time loop: the backward pass (sw = 1) belongs to MODE=FWI\n");
+    if (fwi && (gv->WEQ != EL_ISO || gv->NDT != 1 || (gv->SEISMO != 1 && gv->SEISMO != 4) || vinv->DTINV != 1 ||
+                vinv->LNORM != 2 || vinv->ADJOINT_TYPE < 1 || vinv->ADJOINT_TYPE > 3 || gv->FDORDER_TIME != 2))
+        log_fatal("GPU time loop: MODE=FWI needs WEQ=EL_ISO, NDT=1, SEISMO 1 or 4, DTINV=1, LNORM=2, "
+                  "ADJOINT_TYPE 1..3 and FDORDER_TIME=2\n");
     if (gv->FDORDER_TIME != 2 && gv->FDORDER_TIME != 4)
         log_fatal("GPU time loop: FDORDER_TIME must be 2 or 4\n");
     if (gv->NPROCX != 1 || gv->NPROCY != 1)
@@ -198,6 +242,45 @@ void time_loop(int iter, int ishot, int snapcheck, float *hc, float **srcpos_loc
         upload_model(mpm, gv, hc);
         g_model_iter = iter;
     }
+    const int every = gv->OUTNTIMESTEPINFO > 64 ? gv->OUTNTIMESTEPINFO : 64;
+    GPU_CHECK(sofi_set_kernel_timing(g_ctx, 0)); /* clears the totals */
+    GPU_CHECK(sofi_set_kernel_timing(g_ctx, every));
+    if (sw == 1) {
+        /* inversion.c:214-222: the adjoint signals at the receivers (srcpos_loc
+         * holds their grid positions, nsrc = NTR, signals [1..NTR][1..NT]) */
+        if (nsrc != gv->NTR)
+            log_fatal("GPU time loop: the backward pass injects at the NTR receivers\n");
+        float *ax = (float *)calloc((size_t)(nsrc > 0 ? nsrc : 1) * gv->NT, sizeof(float));
+        float *ay = (float *)calloc((size_t)(nsrc > 0 ? nsrc : 1) * gv->NT, sizeof(float));
+        for (int l = 1; l <= nsrc; l++) {
+            memcpy(ax + (size_t)(l - 1) * gv->NT, &signalx[l][1], sizeof(float) * gv->NT);
+            memcpy(ay + (size_t)(l - 1) * gv->NT, &signaly[l][1], sizeof(float) * gv->NT);
+        }
+        int rc = sofi_fwi_backward(g_ctx, ax, ay);
+        free(ax), free(ay);
+        if (rc == SOFI_E_UNSTABLE)
+            log_fatal("Simulation is unstable! (%s)\n", sofi_last_error());
+        GPU_CHECK(rc);
+        /* calc_conv.c adds each step's correlation to the shot's gradients */
+        float *g[3];
+        for (int k = 0; k < 3; k++)
+            g[k] = (float *)malloc(sizeof(float) * (size_t)gv->NX * gv->NY);
+        GPU_CHECK(sofi_fwi_gradients(g_ctx, g[0], g[1], g[2]));
+        float **dst[3] = {minv->gradLam_shot, minv->gradMu_shot, minv->gradRhos_shot};
+        for (int k = 0; k < 3; k++) {
+            for (int j = 1; j <= gv->NY; j++)
+                for (int i = 1; i <= gv->NX; i++)
+                    dst[k][j][i] += g[k][(size_t)(j - 1) * gv->NX + (i - 1)];
+            free(g[k]);
+        }
+        goto outputs;
+    }
+    if (fwi) {
+        /* the forward run of the gradient pass keeps its gradient quantities (snap_store.c) */
+        float *vp = dense(minv->Vp0, gv), *vs = dense(minv->Vs0, gv), *rho = dense(minv->Rho0, gv);
+        GPU_CHECK(sofi_fwi_begin(g_ctx, vinv->VELOCITY, vinv->ADJOINT_TYPE, vp, vs, rho));
+        free(vp), free(vs), free(rho);
+    }
     /* sources: srcpos_loc rows 1..12, columns 1..nsrc -> [12][nsrc] */
     float *sp = (float *)calloc((size_t)12 * (nsrc > 0 ? nsrc : 1), sizeof(float));
     float *sig = (float *)calloc((size_t)(nsrc > 0 ? nsrc : 1) * gv->NT, sizeof(float));
@@ -226,6 +309,8 @@ void time_loop(int iter, int ishot, int snapcheck, float *hc, float **srcpos_loc
         log_fatal("Simulation is unstable! (%s)\n", sofi_last_error());
     GPU_CHECK(rc);
 
+outputs:
+    fill_perform(perf, gv);
     /* sections: gv->SECTION*[1..NTR][1..NS] */
     if (gv->SEISMO && gv->NTR > 0) {
         int ns = 0;
