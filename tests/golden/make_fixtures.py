@@ -105,9 +105,11 @@ def run_reference(case, exe):
 
 
 def ref_examples(reference, exe):
-    """One-rank compiled-reference runs of the TTI examples (seismograms only)."""
+    """One-rank compiled-reference runs of the TTI examples and of weq3
+    (seismograms and their SU headers; the shipped weq3 files were written by
+    an older version whose headers place receivers at index * DH)."""
     ex = os.path.join(reference, "examples")
-    for name in ["weq7", "weq8", "weq8_fy"]:
+    for name in ["weq3", "weq7", "weq8", "weq8_fy"]:
         work = tempfile.mkdtemp(prefix="sofi_ex_")
         try:
             for d in ["model", "sources", "receiver"]:
@@ -126,7 +128,7 @@ def ref_examples(reference, exe):
             suffix = "_fy" if name.endswith("_fy") else ""
             out = {}
             for comp in ["vx", "vy", "p", "div", "curl"]:
-                _, out[f"seis_{comp}"] = read_su(os.path.join(work, base, f"seis{suffix}_{comp}.su"))
+                out[f"hdr_{comp}"], out[f"seis_{comp}"] = read_su(os.path.join(work, base, f"seis{suffix}_{comp}.su"))
             np.savez_compressed(os.path.join(HERE, f"ref1x1_{name}.npz"), **out)
             print("wrote ref1x1", name)
         finally:
@@ -224,7 +226,10 @@ def main():
     exe = os.path.join(REPO, "oracle", "_ref", "sofi2D")
     if not a.only:
         shipped(a.reference)
+    if not a.only or a.only == "examples":
         ref_examples(a.reference, exe)
+        if a.only:
+            return
     if not a.only or a.only == "sigout":
         shipped_sigout(a.reference)
         if a.only:
