@@ -93,7 +93,6 @@ struct Geo {
     int el_tti_rb_short;    // EL_TTI CPML: right-bottom corner pass stops at NY-1
     int shot_fast;          // block index: shot varies fastest (model tiles shared in L2)
     int seismo, ndt;        // sampling (gv->SEISMO, gv->NDT)
-    int *step_ctr;          // device: time steps completed; the velocity kernel advances it
     // TTI CPML memory of the velocity derivatives in two buffers (psi_pp = 1):
     // step n reads buffer (n - 1) & 1 and writes buffer n & 1; the second
     // buffer starts psi_xsz / psi_ysz floats after the first
@@ -103,6 +102,9 @@ struct Geo {
     float dhi4;             // 1.0 / DH rounded to float, as the 4th-order updates compute it
     float dt, dh, dtdh, dhi, dthalbe;
     float hc[7];
+    // device: time steps completed; the velocity kernel advances it. Kept last:
+    // with it here the four-cell velocity kernel fits 64 registers unspilled
+    int *step_ctr;
 };
 
 // Wavefield and CPML memory (per shot).

@@ -1872,6 +1872,7 @@ static __device__ __align__(256) float g_noalloc_scratch[8 * SOFI_NOALLOC_MAX_CE
 namespace {
 constexpr int kMaxDevices = 64;
 float *g_noalloc_ptr[kMaxDevices] = {};
+std::mutex g_noalloc_mu;  // first calls from several host threads look the address up once
 }  // namespace
 
 int sofi_tti_stress_noalloc(const sofi_config *cfg, const sofi_tti_stress_args *a, void *stream)
@@ -1912,10 +1913,15 @@ int sofi_tti_stress_noalloc(const sofi_config *cfg, const sofi_tti_stress_args *
     CK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices)
         return fail(SOFI_E_ARG, "device %d beyond the %d the scratch table covers", dev, kMaxDevices);
-    if (!g_noalloc_ptr[dev]) {
-        void *p = nullptr;
-        CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        g_noalloc_ptr[dev] = static_cast<float *>(p);
+    float *scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void *p = nullptr;
+            CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+            g_noalloc_ptr[dev] = static_cast<float *>(p);
+        }
+        scratch = g_noalloc_ptr[dev];
     }
     Geo G{};
     G.nx = cfg->nx, G.ny = cfg->ny, G.pitch = pitch, G.nshots = 1, G.fsz = fsz;
@@ -1935,8 +1941,8 @@ int sofi_tti_stress_noalloc(const sofi_config *cfg, const sofi_tti_stress_args *
     W.vx = const_cast<float *>(a->vx), W.vy = const_cast<float *>(a->vy);
     W.sxx = a->sxx, W.syy = a->syy, W.sxy = a->sxy, W.r = a->r, W.p = a->p, W.q = a->q;
     W.psi_vxx = a->psi_vxx, W.psi_vyx = a->psi_vyx, W.psi_vyy = a->psi_vyy, W.psi_vxy = a->psi_vxy;
-    W.draw = g_noalloc_ptr[dev];
-    W.dcor = g_noalloc_ptr[dev] + 4 * fsz;
+    W.draw = scratch;
+    W.dcor = scratch + 4 * fsz;
     Model M{};
     M.c11 = a->c11, M.c13 = a->c13, M.c33 = a->c33, M.c15 = a->c15, M.c35 = a->c35;
     M.c55ipjp = a->c55ipjp, M.c15ipjp = a->c15ipjp, M.c35ipjp = a->c35ipjp;

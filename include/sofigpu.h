@@ -309,6 +309,14 @@ typedef struct {
  * stream. Every value read from the array is written earlier in the same call,
  * so nothing has to be cleared between calls.
  *
+ * The free-surface correction (surface_elastic.c / surface.c, which
+ * time_loop.c applies after the stress update) and the source injection are
+ * not part of this update: a caller with FREE_SURF applies them after the
+ * call, as time_loop() does; FREE_SURF here only sets the CPML region order
+ * (no top frame, GY[2] = 0). With periodic x (BOUNDARY 1) the caller fills
+ * the ghost columns of vx and vy (the opposite edge's columns) first, as
+ * exchange_v does in the reference.
+ *
  * cfg: WEQ must be SOFI_EL_TTI or SOFI_VEL_TTI; nshots and the acquisition
  * fields are ignored. stream: a cudaStream_t (NULL = legacy default stream).
  * Returns after the work is queued; errors of the launch are reported. */

@@ -23,11 +23,17 @@ pytestmark = pytest.mark.gpu
 L2_TOL, MAX_TOL = 1e-4, 1e-3
 
 
-def _pad(torch, a, nx, ny):
+def _pad(torch, a, nx, ny, periodic=False):
+    """[NY][NX] into the padded device layout; periodic: the 8 ghost columns on
+    either side hold the opposite edge's columns (what exchange_v leaves)."""
     from gpi_project_gb300 import _native as N
     rows, pitch = N.padded_shape(nx, ny)
     t = torch.zeros((rows, pitch), dtype=torch.float32)
-    t[8:8 + ny, 8:8 + nx] = torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32))
+    a = torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32))
+    t[8:8 + ny, 8:8 + nx] = a
+    if periodic:
+        t[8:8 + ny, 0:8] = a[:, nx - 8:nx]
+        t[8:8 + ny, 8 + nx:16 + nx] = a[:, 0:8]
     return t.cuda()
 
 
@@ -35,12 +41,17 @@ def _unpad(t, nx, ny):
     return t[8:8 + ny, 8:8 + nx].cpu().numpy()
 
 
-@pytest.mark.parametrize("name", ["tti_cpml", "vtti_cpml_l1"])
-def test_noalloc_tti_stress_matches_context(name):
+CASES = [("tti_cpml", {}), ("vtti_cpml_l1", {}), ("tti_abs", {}), ("tti_cpml", {"boundary": 1})]
+
+
+@pytest.mark.parametrize("name,over", CASES, ids=[n + "".join(f"-{k}{v}" for k, v in o.items()) for n, o in CASES])
+def test_noalloc_tti_stress_matches_context(name, over):
+    """CPML (elastic, viscoelastic), the damping frame, and periodic x with the
+    caller filling the velocity ghost columns."""
     torch = pytest.importorskip("torch")
     from oracle import oracle as O
     from gpi_project_gb300 import TimeLoop, _native as N
-    case = dict(case_by_name(name))
+    case = dict(case_by_name(name), **over)
     cfg = case_config(case)
     cfg.seismo, cfg.snap = 0, 0
     o = O.Oracle(cfg)
@@ -69,6 +80,9 @@ def test_noalloc_tti_stress_matches_context(name):
         for k in "rpq":
             dev[k] = torch.zeros((L, rows, pitch), dtype=torch.float32, device="cuda")
     fw2 = 2 * cfg.fw
+    cpml, periodic = cfg.abs_type == 1, bool(cfg.boundary)
+    if cfg.abs_type == 2:
+        dev["absorb"] = _pad(torch, fields["absorb"], nx, ny)
     for k in ["psi_vxx", "psi_vyx"]:
         dev[k] = torch.zeros((ny, fw2), dtype=torch.float32, device="cuda")
     for k in ["psi_vyy", "psi_vxy"]:
@@ -81,7 +95,8 @@ def test_noalloc_tti_stress_matches_context(name):
             dev[m + "d_base"] = _pad(torch, fields[m + "d_base"], nx, ny)
     for k in ["K_x", "a_x", "b_x", "K_x_half", "a_x_half", "b_x_half", "K_y", "a_y", "b_y", "K_y_half",
               "a_y_half", "b_y_half"]:
-        dev[k] = torch.from_numpy(np.ascontiguousarray(vecs[k], dtype=np.float32)).cuda()
+        if cpml:
+            dev[k] = torch.from_numpy(np.ascontiguousarray(vecs[k], dtype=np.float32)).cuda()
 
     args = N.TtiStressArgs()
     for k, v in dev.items():
@@ -97,15 +112,15 @@ def test_noalloc_tti_stress_matches_context(name):
     stream = torch.cuda.current_stream().cuda_stream
     for call in range(2):
         t.run(1)  # velocity + stress update of one step through the context
-        dev["vx"] = _pad(torch, t.field("vx"), nx, ny)
-        dev["vy"] = _pad(torch, t.field("vy"), nx, ny)
+        dev["vx"] = _pad(torch, t.field("vx"), nx, ny, periodic)
+        dev["vy"] = _pad(torch, t.field("vy"), nx, ny, periodic)
         args.vx, args.vy = dev["vx"].data_ptr(), dev["vy"].data_ptr()
         torch.cuda.synchronize()
         N.check(lib.sofi_tti_stress_noalloc(ctypes.byref(gcfg), ctypes.byref(args), ctypes.c_void_p(stream)))
         torch.cuda.synchronize()
         for k in ["sxx", "syy", "sxy"]:
             got, ref = _unpad(dev[k], nx, ny), t.field(k)
-            assert rel_l2(got, ref) <= L2_TOL and rel_max(got, ref) <= MAX_TOL, (name, call, k)
+            assert rel_l2(got, ref) <= L2_TOL and rel_max(got, ref) <= MAX_TOL, (name, over, call, k)
         if visco:
             for k in "rpq":
                 for l in range(L):
