@@ -672,7 +672,7 @@ def main():
     ncell = par["nx"] * par["ny"] * nshots
     ach_s = bpc["update_s"] * ncell / (ms_s * 1e-3) / 1e9 if ms_s else None
     traffic = traffic_from_profiles("update_s", W["name"])
-    kname = {0: "k_update_s_ac (pressure)", 6: "k_tti_fused (TTI stress)", 7: "k_tti_fused (TTI stress + memory variables)"}
+    kname = {0: "k_update_s_ac (pressure)", 6: "k_tti_tiles (TTI stress)", 7: "k_tti_tiles (TTI stress + memory variables)"}
     if par.get("fdorder_time", 2) == 4:
         kname = {par["weq"]: "k_update_s_ab4w (Adams-Bashforth stress, histories, memory variables)"}
     roof = {"kernel": kname.get(par["weq"], "k_update_sw / k_update_s (stress + memory variables)"), "bound": "hbm",

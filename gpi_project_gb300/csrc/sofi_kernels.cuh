@@ -1035,18 +1035,19 @@ __global__ void __launch_bounds__(BX *BY) k_update_s_tti(Geo G, Wave W, Model M)
 // which write their CPML memory: every block reads the memory of the previous
 // step's buffer and only the owner of a cell writes this step's buffer
 // (Geo::psi_pp), so no block sees a value another block has already advanced.
+// tti_tile: the tile with origin (i0, j0) of shot s, thread (tx, ty) of the
+// 32 x 8 block, sd: NB [4][BY + 2][BX + 2] arrays of shared memory; cells in
+// [ki0, ki1] x [kj0, kj1] are left to another block (their derivatives still
+// feed this tile's averages).
 template <int ND, bool VISCO, bool CPML>
-__global__ void __launch_bounds__(BX *BY) k_tti_fused(Geo G, Wave W, Model M)
+__device__ __forceinline__ void tti_tile(const Geo &G, const Wave &W, const Model &M, int s, int i0, int j0, int tx,
+                                         int ty, float (*sd)[4][BY + 2][BX + 2], int ki0 = 1, int ki1 = 0,
+                                         int kj0 = 1, int kj1 = 0)
 {
     constexpr int SX = BX + 2, SY = BY + 2, NB = CPML ? 2 : 1;
     constexpr int RING = 2 * SX + 2 * BY;
     static_assert(RING <= BX * BY, "ring cells exceed the block");
-    __shared__ float sd[NB][4][SY][SX];  // [raw, stretched][vxx vyy vyx vxy][y][x]
-    pdl_begin();
-    int bx, s;
-    block_xs(G, bx, s);
-    const int i0 = bx * BX + 1, j0 = blockIdx.y * BY + 1;
-    const int tid = threadIdx.y * BX + threadIdx.x;
+    const int tid = ty * BX + tx;
     const long long so = (long long)s * G.fsz;
     const float *vx = W.vx + so, *vy = W.vy + so;
     Wave Wn = W, Wo = W;
@@ -1062,7 +1063,7 @@ __global__ void __launch_bounds__(BX *BY) k_tti_fused(Geo G, Wave W, Model M)
     for (int pass = 0; pass < 2; pass++) {
         int ly, lx;
         if (pass == 0) {
-            ly = threadIdx.y + 1, lx = threadIdx.x + 1;
+            ly = ty + 1, lx = tx + 1;
         } else {
             if (tid >= RING)
                 break;
@@ -1117,22 +1118,22 @@ __global__ void __launch_bounds__(BX *BY) k_tti_fused(Geo G, Wave W, Model M)
         }
     }
     __syncthreads();
-    const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
-    if (i > G.nx || j > G.ny)
+    const int i = i0 + tx, j = j0 + ty;
+    if (i > G.nx || j > G.ny || (i >= ki0 && i <= ki1 && j >= kj0 && j <= kj1))
         return;
     const int xr = xside(G, i), yr = yside(G, j);
     if (tti_pml_skipped(G, i, j, xr, yr))
         return;
     const int rc = frame ? region(G, i, j) : 0;
-    const int ty = threadIdx.y + 1, tx = threadIdx.x + 1;
+    const int sy = ty + 1, sx = tx + 1;
     // derivative k of neighbour (j + dy, i + dx) as the update of this cell sees it
     auto D = [&](int k, int dy, int dx) -> float {
         if (!frame)
-            return sd[0][k][ty + dy][tx + dx];
+            return sd[0][k][sy + dy][sx + dx];
         const int jn = j + dy, in = i + dx;
         if (jn < 1 || jn > G.ny || in < 1 || in > G.nx)
-            return sd[0][k][ty + dy][tx + dx];
-        return region(G, in, jn) <= rc ? sd[NB - 1][k][ty + dy][tx + dx] : sd[0][k][ty + dy][tx + dx];
+            return sd[0][k][sy + dy][sx + dx];
+        return region(G, in, jn) <= rc ? sd[NB - 1][k][sy + dy][sx + dx] : sd[0][k][sy + dy][sx + dx];
     };
     const float vxx = D(0, 0, 0), vyy = D(1, 0, 0);
     const float vxxipjp = 0.25f * (vxx + D(0, 1, 0) + D(0, 0, 1) + D(0, 1, 1));
@@ -1141,6 +1142,270 @@ __global__ void __launch_bounds__(BX *BY) k_tti_fused(Geo G, Wave W, Model M)
     const float vyxij = 0.25f * (vyx0 + D(2, -1, 0) + D(2, 0, -1) + D(2, -1, -1));
     const float vxyij = 0.25f * (vxy0 + D(3, -1, 0) + D(3, 0, -1) + D(3, -1, -1));
     tti_update<VISCO>(G, W, M, s, cell(G, j, i), xr, yr, vxx, vyy, vxxipjp, vyyipjp, vyx0, vxy0, vyxij, vxyij);
+}
+
+template <int ND, bool VISCO, bool CPML>
+__global__ void __launch_bounds__(BX *BY) k_tti_fused(Geo G, Wave W, Model M)
+{
+    __shared__ float sd[CPML ? 2 : 1][4][BY + 2][BX + 2];  // [raw, stretched][vxx vyy vyx vxy][y][x]
+    pdl_begin();
+    int bx, s;
+    block_xs(G, bx, s);
+    tti_tile<ND, VISCO, CPML>(G, W, M, s, bx * BX + 1, blockIdx.y * BY + 1, threadIdx.x, threadIdx.y, sd);
+}
+
+// The TTI stress update over two kinds of tile in one launch. The interior
+// rectangle [fi0, fi1] x [fj0, fj1] holds the cells whose one-cell ring lies
+// inside the grid and inside the CPML (or damping) frame's interior (every
+// cell and neighbour in region 0: no stretch, no damping); its width is a
+// multiple of 4 and fi0 - 1 a multiple of 4 (16-byte aligned rows). It is cut
+// into tiles of up to 64 x 32 cells (origin (fi0 + 64 a, fj0 + 32 b)) that
+// take tti_tile4. The 32 x 8 tiles of the grid not wholly inside the
+// rectangle take tti_tile, the one-pass form above, and skip the cells that
+// lie inside it. The frame's tiles come first in the launch, so their longer
+// blocks start before the bulk of the interior ones.
+struct TtiMap {
+    int nsx, nsy;              // 32 x 8 tiles of the grid, per row and column
+    int sxa, sxb, sya, syb;    // the 32 x 8 tiles wholly inside the rectangle (inclusive; none: sya = nsy)
+    int nframe;                // 32 x 8 tiles outside that range: blocks 0 .. nframe - 1
+    int fi0, fi1, fj0, fj1;    // the interior rectangle (empty: fi1 < fi0)
+    int nfx, nfy;              // its tiles: blocks nframe + b * nfx + a, a < nfx, b < nfy
+};
+constexpr int T4X = 64, T4Y = 32;       // cells of an interior tile
+constexpr int T4W = 72, T4P = 34 * 72;  // shared row (column 3: i0 - 1, 4 ..: the tile, 68: i0 + 64), plane
+
+// 32 x 8 tile (sx, sy) of frame block b: the rows above the 64 x 32 tiles,
+// then per row of theirs the tiles left and right of them, then the rows below.
+__device__ __forceinline__ void tti_frame_tile(const TtiMap &T, int b, int &sx, int &sy)
+{
+    const int top = T.sya * T.nsx;
+    if (b < top) {
+        sy = b / T.nsx, sx = b - sy * T.nsx;
+        return;
+    }
+    b -= top;
+    const int side = T.sxa + (T.nsx - 1 - T.sxb), mid = (T.syb - T.sya + 1) * side;
+    if (b < mid) {
+        const int r = b / side, k = b - r * side;
+        sy = T.sya + r, sx = k < T.sxa ? k : T.sxb + 1 + (k - T.sxa);
+        return;
+    }
+    b -= mid;
+    const int r = b / T.nsx;
+    sy = T.syb + 1 + r, sx = b - r * T.nsx;
+}
+
+__device__ __forceinline__ void lds4(const float *p, float *out)
+{
+    const float4 a = *reinterpret_cast<const float4 *>(p);
+    out[0] = a.x, out[1] = a.y, out[2] = a.z, out[3] = a.w;
+}
+
+// tti_update for the four cells o .. o + 3 of one row (interior: no damping),
+// model, memory variables and stresses as 16-byte vectors; per cell the
+// expressions of tti_update, term by term.
+template <bool VISCO>
+__device__ __forceinline__ void tti_update4(const Geo &G, const Wave &W, const Model &M, int s, int o, long long mo,
+                                            const float *vxx, const float *vyy, const float *vxxipjp,
+                                            const float *vyyipjp, const float *vyx0, const float *vxy0,
+                                            const float *vyxij, const float *vxyij)
+{
+    const long long so = (long long)s * G.fsz;
+    float u1[4], u2[4], u3[4];
+    {
+        float a[4], b[4], c[4];
+        ldv<4>(M.c55ipjp + mo + o, a), ldv<4>(M.c15ipjp + mo + o, b), ldv<4>(M.c35ipjp + mo + o, c);
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            u1[k] = a[k] * (vxy0[k] + vyx0[k]) + b[k] * vxxipjp[k] + c[k] * vyyipjp[k];
+    }
+    {
+        float c11[4], c13[4], c33[4], c15[4], c35[4];
+        ldv<4>(M.c11 + mo + o, c11), ldv<4>(M.c13 + mo + o, c13), ldv<4>(M.c33 + mo + o, c33);
+        ldv<4>(M.c15 + mo + o, c15), ldv<4>(M.c35 + mo + o, c35);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const float vij = vyxij[k] + vxyij[k];
+            u2[k] = c11[k] * vxx[k] + c13[k] * vyy[k] + c15[k] * vij;
+            u3[k] = c13[k] * vxx[k] + c33[k] * vyy[k] + c35[k] * vij;
+        }
+    }
+    if (VISCO) {
+        float sro[4], spo[4], sqo[4], sr[4], sp[4], sq[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            sro[k] = spo[k] = sqo[k] = sr[k] = sp[k] = sq[k] = 0.f;
+        for (int l = 0; l < G.L; l++) {
+            const long long lo = ((long long)s * G.L + l) * G.fsz + o;
+            const float pe = M.peta[l], bb = M.bip[l], cc = M.cip[l];
+            float r[4], p[4], q[4], x[4], y[4], z[4];
+            ldv_rw<4>(W.r + lo, r), ldv_rw<4>(W.p + lo, p), ldv_rw<4>(W.q + lo, q);
+            ldv<4>(M.c55ipjpb + mo + o, x), ldv<4>(M.c15ipjpb + mo + o, y), ldv<4>(M.c35ipjpb + mo + o, z);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                sro[k] += r[k];
+                r[k] = bb * (r[k] * cc - (x[k] * pe) * (vxy0[k] + vyx0[k]) - (y[k] * pe) * vxxipjp[k] -
+                             (z[k] * pe) * vyyipjp[k]);
+                sr[k] += r[k];
+            }
+            stv<4>(W.r + lo, r);
+            ldv<4>(M.c11b + mo + o, x), ldv<4>(M.c13b + mo + o, y), ldv<4>(M.c15b + mo + o, z);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                spo[k] += p[k];
+                p[k] = bb * (p[k] * cc - (x[k] * pe) * vxx[k] - (y[k] * pe) * vyy[k] -
+                             (z[k] * pe) * (vyxij[k] + vxyij[k]));
+                sp[k] += p[k];
+            }
+            stv<4>(W.p + lo, p);
+            ldv<4>(M.c33b + mo + o, x), ldv<4>(M.c35b + mo + o, z);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                sqo[k] += q[k];
+                q[k] = bb * (q[k] * cc - (y[k] * pe) * vxx[k] - (x[k] * pe) * vyy[k] -
+                             (z[k] * pe) * (vyxij[k] + vxyij[k]));
+                sq[k] += q[k];
+            }
+            stv<4>(W.q + lo, q);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            u1[k] += G.dthalbe * (sro[k] + sr[k]);
+            u2[k] += G.dthalbe * (spo[k] + sp[k]);
+            u3[k] += G.dthalbe * (sqo[k] + sq[k]);
+        }
+    }
+    float t[4];
+    ldv_rw<4>(W.sxy + so + o, t);
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        t[k] += u1[k];
+    stv<4>(W.sxy + so + o, t);
+    ldv_rw<4>(W.sxx + so + o, t);
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        t[k] += u2[k];
+    stv<4>(W.sxx + so + o, t);
+    ldv_rw<4>(W.syy + so + o, t);
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        t[k] += u3[k];
+    stv<4>(W.syy + so + o, t);
+}
+
+// One interior tile with origin (i0, j0) of cols x rows cells (cols a multiple
+// of 4, at most 64; rows at most 32), 256 threads: each thread derives four
+// adjacent cells of two rows (16-byte loads, s_derivs), warps 0-3 derive the
+// ring (the rows above and below as four-cell groups, the columns left and
+// right cell by cell), all into sm ([vxx vyy vyx vxy][34][72]: row 0 is
+// j0 - 1, column 3 is i0 - 1); then each thread updates its cells from there.
+// No cell of the tile or its ring is in the frame, so raw and stretched
+// derivatives coincide.
+template <int ND, bool VISCO>
+__device__ __forceinline__ void tti_tile4(const Geo &G, const Wave &W, const Model &M, int s, int i0, int j0,
+                                          int cols, int rows, float *sm)
+{
+    const int t = threadIdx.x, gx = t & 15, gy = t >> 4, w = t >> 5, lane = t & 31;
+    const int P = G.pitch;
+    const long long so = (long long)s * G.fsz;
+    const float *__restrict__ vx = W.vx + so;
+    const float *__restrict__ vy = W.vy + so;
+    // four-cell group at row j, columns i .. i + 3 -> shared row r, column x
+    auto group = [&](int j, int i, int r, int x) {
+        const int o = (j - 1 + HY) * P + (i - 1 + HX);
+        float dxx[4], dyx[4], dxy[4], dyy[4];
+        s_derivs<ND, 4>(
+            G, [&](int f, int dy, int dx, float *out) { ldv<4>((f ? vy : vx) + o + dy * P + dx, out); }, dxx, dyx,
+            dxy, dyy);
+        float *q = sm + r * T4W + x;
+        stv<4>(q, dxx), stv<4>(q + T4P, dyy), stv<4>(q + 2 * T4P, dyx), stv<4>(q + 3 * T4P, dxy);
+    };
+    // one cell (j, i) -> shared row r, column x
+    auto single = [&](int j, int i, int r, int x) {
+        float d0, d1, d2, d3;
+        op_s<ND>(vx, vy, cell(G, j, i), P, G.hc, G.dhi, d0, d2, d3, d1);
+        float *q = sm + r * T4W + x;
+        q[0] = d0, q[T4P] = d1, q[2 * T4P] = d2, q[3 * T4P] = d3;
+    };
+    const bool gon = 4 * gx < cols;
+    if (gon && gy < rows)
+        group(j0 + gy, i0 + 4 * gx, gy + 1, 4 + 4 * gx);
+    if (gon && gy + 16 < rows)
+        group(j0 + gy + 16, i0 + 4 * gx, gy + 17, 4 + 4 * gx);
+    if (w == 0) {  // rows j0 - 1 (lanes 0-15) and j0 + rows (lanes 16-31)
+        const int top = lane < 16, g = lane & 15;
+        if (4 * g < cols)
+            group(top ? j0 - 1 : j0 + rows, i0 + 4 * g, top ? 0 : rows + 1, 4 + 4 * g);
+    } else if (w == 1) {  // column i0 - 1, rows j0 - 1 .. j0 + min(rows, 31) - 1
+        if (lane <= rows)
+            single(j0 - 1 + lane, i0 - 1, lane, 3);
+    } else if (w == 2) {  // column i0 + cols, rows j0 + 1 .. j0 + rows
+        if (lane < rows)
+            single(j0 + 1 + lane, i0 + cols, lane + 2, 4 + cols);
+    } else if (w == 3) {  // (j0 + 31, i0 - 1) when rows = 32, and (j0, i0 + cols)
+        if (lane == 0 && rows == T4Y)
+            single(j0 + T4Y - 1, i0 - 1, T4Y, 3);
+        else if (lane == 1)
+            single(j0, i0 + cols, 1, 4 + cols);
+    }
+    __syncthreads();
+    if (!gon)
+        return;
+    const long long mo = moff(G, s);
+#pragma unroll 1
+    for (int r = gy; r < rows; r += 16) {
+        const int j = j0 + r, i = i0 + 4 * gx;
+        const int o = (j - 1 + HY) * P + (i - 1 + HX);
+        const float *q = sm + (r + 1) * T4W + 4 + 4 * gx;  // (j, i)
+        float vxx[4], vyy[4], vxxipjp[4], vyyipjp[4], vyx0[4], vxy0[4], vyxij[4], vxyij[4];
+        {
+            // (j, i .. i + 4) and (j + 1, i .. i + 4)
+            float a[5], b[5];
+            lds4(q, a), a[4] = q[4];
+            lds4(q + T4W, b), b[4] = q[T4W + 4];
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                vxx[k] = a[k], vxxipjp[k] = 0.25f * (a[k] + b[k] + a[k + 1] + b[k + 1]);
+            lds4(q + T4P, a), a[4] = q[T4P + 4];
+            lds4(q + T4P + T4W, b), b[4] = q[T4P + T4W + 4];
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                vyy[k] = a[k], vyyipjp[k] = 0.25f * (a[k] + b[k] + a[k + 1] + b[k + 1]);
+            // (j, i - 1 .. i + 3) and (j - 1, i - 1 .. i + 3)
+            lds4(q + 2 * T4P, a + 1), a[0] = q[2 * T4P - 1];
+            lds4(q + 2 * T4P - T4W, b + 1), b[0] = q[2 * T4P - T4W - 1];
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                vyx0[k] = a[k + 1], vyxij[k] = 0.25f * (a[k + 1] + b[k + 1] + a[k] + b[k]);
+            lds4(q + 3 * T4P, a + 1), a[0] = q[3 * T4P - 1];
+            lds4(q + 3 * T4P - T4W, b + 1), b[0] = q[3 * T4P - T4W - 1];
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                vxy0[k] = a[k + 1], vxyij[k] = 0.25f * (a[k + 1] + b[k + 1] + a[k] + b[k]);
+        }
+        tti_update4<VISCO>(G, W, M, s, o, mo, vxx, vyy, vxxipjp, vyyipjp, vyx0, vxy0, vyxij, vxyij);
+    }
+}
+
+template <int ND, bool VISCO, bool CPML>
+__global__ void __launch_bounds__(BX *BY, VISCO ? 2 : 4) k_tti_tiles(Geo G, Wave W, Model M, TtiMap T)
+{
+    __shared__ __align__(16) float sm[4 * T4P];
+    static_assert(sizeof(float) * (CPML ? 2 : 1) * 4 * (BY + 2) * (BX + 2) <= sizeof(sm), "frame tile overflow");
+    pdl_begin();
+    int b, s;
+    block_xs(G, b, s);
+    if (b >= T.nframe) {
+        b -= T.nframe;
+        const int a = b % T.nfx, c = b / T.nfx;
+        const int i0 = T.fi0 + a * T4X, j0 = T.fj0 + c * T4Y;
+        tti_tile4<ND, VISCO>(G, W, M, s, i0, j0, min(T4X, T.fi1 - i0 + 1), min(T4Y, T.fj1 - j0 + 1), sm);
+        return;
+    }
+    int sx, sy;
+    tti_frame_tile(T, b, sx, sy);
+    tti_tile<ND, VISCO, CPML>(G, W, M, s, sx * BX + 1, sy * BY + 1, threadIdx.x & (BX - 1), threadIdx.x / BX,
+                              reinterpret_cast<float(*)[4][BY + 2][BX + 2]>(sm), T.fi0, T.fi1, T.fj0, T.fj1);
 }
 
 // ------------------------------------------------ after the stress update

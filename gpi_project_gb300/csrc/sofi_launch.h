@@ -52,4 +52,6 @@ void launch_ab4_s(const Geo &G, const Wave &W, const Model &M, int nd, bool visc
 void launch_tti_fused(const Geo &G, const Wave &W, const Model &M, int nd, bool visco, bool cpml, dim3 grid,
                       cudaStream_t st);
 void launch_tti_split(const Geo &G, const Wave &W, const Model &M, int nd, bool visco, dim3 grid, cudaStream_t st);
+// the one-pass form on 32 x 8 tiles in the frame, 64 x 32 four-cell tiles elsewhere (own grid)
+void launch_tti_tiles(const Geo &G, const Wave &W, const Model &M, int nd, bool visco, bool cpml, cudaStream_t st);
 }  // namespace sofi

@@ -222,6 +222,7 @@ struct sofi_ctx {
     bool graph_ok = false;
     long long graph_launches = 0;  // kernels per replay
     bool tti_split = false;    // TTI: derivative fields through HBM (two kernels) instead of fused
+    bool tti_fused = false;    // TTI: the one-pass kernel on 32 x 8 tiles everywhere (no four-cell interior tiles)
     // snapshots
     int snap_nx = 0, snap_ny = 0, snap_total = 0, nsnap = 0;
     float *d_snap = nullptr;
@@ -730,8 +731,10 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
     } else if (kind == TTI && c->tti_split) {
         c->launches++;
         launch_tti_split(G, c->W, c->M, c->nd, visco, grd, st);
-    } else if (kind == TTI) {
+    } else if (kind == TTI && c->tti_fused) {
         launch_tti_fused(G, c->W, c->M, c->nd, visco, G.abs_type == 1, grd, st);
+    } else if (kind == TTI) {
+        launch_tti_tiles(G, c->W, c->M, c->nd, visco, G.abs_type == 1, st);
     } else {
         launch_cell_s(G, step_wave(c), c->M, c->nd, kind, visco, c->sw, c->snarrow, cf.nx, cf.ny, S, st);
     }
@@ -923,8 +926,10 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
         c->snarrow = e[0] == 'n';
         c->sw_fixed = true;
     }
-    if (const char *e = getenv("SOFI_TTI"))
+    if (const char *e = getenv("SOFI_TTI")) {  // "split", "fused"; else the tiled one-pass form
         c->tti_split = strcmp(e, "split") == 0;
+        c->tti_fused = strcmp(e, "fused") == 0;
+    }
     e = cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, priority);
     if (e != cudaSuccess) {
         delete c;

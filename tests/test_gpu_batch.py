@@ -1,8 +1,8 @@
 """Batched shots: S resident shots advanced by one sofi_run give, shot for shot,
 the sections a single-shot context gives (same kernels, same arithmetic), for a
 shared model and for one model per shot, with the four-cell kernels on wide
-and on narrow blocks and with the TMA-fed velocity pipeline (whose tensor maps
-span all shots)."""
+and on narrow blocks, and with the TTI stress kernel's interior and frame
+tiles."""
 import os
 
 import numpy as np
@@ -14,9 +14,9 @@ from tests.helpers import case_config, case_receivers, gpu_config_from, prepared
 pytestmark = pytest.mark.gpu
 
 
-def _inputs(name, nshift):
+def _inputs(name, nshift, **over):
     from oracle import oracle as O
-    case = dict(case_by_name(name))
+    case = dict(case_by_name(name), **over)
     cfg = case_config(case)
     o = O.Oracle(cfg)
     o.set_material(synthetic_model(case))
@@ -76,4 +76,22 @@ def test_batch_with_a_model_per_shot(vrows, monkeypatch):
         for c in alone:
             np.testing.assert_array_equal(batched[s][c], alone[c], err_msg=f"model-per-shot {s} {c}")
     assert rel_l2(batched[0]["vx"], batched[1]["vx"]) > 1e-6  # the models differ
+    o.close()
+
+
+@pytest.mark.parametrize("shared", [True, False], ids=["shared-model", "model-per-shot"])
+def test_tti_batch_interior_tiles(shared):
+    """TTI on 300 x 120: six 64 x 32 interior tiles per shot beside the frame's
+    32 x 8 tiles; the shot is the fastest block index with a shared model and
+    the slowest with a model per shot."""
+    over = {"nx": 300, "ny": 120}
+    o, cfg, fields, vecs, shots = _inputs("tti_cpml", 3, **over)
+    rec = case_receivers(dict(case_by_name("tti_cpml"), **over), cfg)
+    models = [fields] if shared else [fields, {k: v * 1.01 if k.startswith("c1") else v for k, v in fields.items()},
+                                      {k: v * 0.99 if k.startswith("c3") else v for k, v in fields.items()}]
+    batched = _run(cfg, models, vecs, shots, rec, shared=shared)
+    for s in range(3):
+        alone = _run(cfg, [models[0 if shared else s]], vecs, [shots[s]], rec, shared=True)[0]
+        for c in alone:
+            np.testing.assert_array_equal(batched[s][c], alone[c], err_msg=f"tti shot {s} {c}")
     o.close()

@@ -16,8 +16,10 @@ with the reference compiled here on one rank (tests/golden/ref1x1_weq3.npz):
     from an older version that placed receivers at index * DH, not
     (index - 1) * DH, so their position fields differ),
   * samples within relative L2 1e-4 and relative max 1e-3 per component of
-    both (curl's denominator floored at 1 % of div's: an explosion in a
-    homogeneous medium has no curl but rounding noise),
+    both. An explosion in a homogeneous medium has no curl but rounding
+    noise: 3e-6 of div's norm in both reference files, whose curls differ by
+    1.4 times curl's own norm. So curl's difference is measured against
+    div's norm and maximum, as for the snapshots,
   * snapshot frames (snap_ssg.c:28-209, merged as snapmerge writes them) on the
     shipped 25 x 25 subsample and by frame norm, within the same bar,
   * the wavelet file's samples equal the reference's shipped signal_out file.
@@ -83,8 +85,8 @@ def test_cli_mode_fw_writes_the_reference_files(tmp_path):
         np.testing.assert_array_equal(hdr, r1[f"hdr_{comp}"], err_msg=f"SU headers of {comp}")
         secs[comp] = data
     for ref_set in (g, r1):
-        floor2 = 1e-2 * np.linalg.norm(ref_set["seis_div"].astype(np.float64))
-        floorm = 1e-2 * float(np.abs(ref_set["seis_div"]).max())
+        floor2 = np.linalg.norm(ref_set["seis_div"].astype(np.float64))
+        floorm = float(np.abs(ref_set["seis_div"]).max())
         for comp, data in secs.items():
             ref = ref_set[f"seis_{comp}"]
             f2, fm = (floor2, floorm) if comp == "curl" else (None, None)

@@ -116,17 +116,23 @@ def test_graph_replay_equals_direct_launches(name, monkeypatch):
 TTI_VARIANTS = [("tti_cpml", {}), ("vtti_cpml_l1", {}), ("tti_abs", {}), ("tti_cpml", {"boundary": 1}),
                 ("vtti_cpml_l1", {"boundary": 1}), ("tti_cpml", {"free_surf": 1, "nt": 60}),
                 ("tti_abs", {"free_surf": 1, "nt": 60}), ("tti_cpml", {"boundary": 1, "free_surf": 1, "nt": 60}),
-                # tiles clear of the CPML frame beside frame tiles
+                # tiles clear of the CPML frame beside frame tiles; 64 x 32 four-cell
+                # interior tiles (six on 300 x 120) beside 32 x 8 one-cell tiles
                 ("tti_cpml", {"nx": 300, "ny": 120}), ("vtti_cpml_l1", {"nx": 300, "ny": 120}),
-                ("tti_abs", {"nx": 300, "ny": 120}), ("tti_cpml", {"nx": 300, "ny": 120, "boundary": 1})]
+                ("tti_abs", {"nx": 300, "ny": 120}), ("tti_cpml", {"nx": 300, "ny": 120, "boundary": 1}),
+                ("tti_cpml", {"nx": 300, "ny": 120, "fdorder": 12}), ("tti_abs", {"nx": 300, "ny": 120, "fdorder": 2}),
+                ("tti_cpml", {"nx": 300, "ny": 120, "free_surf": 1, "nt": 60}),
+                ("vtti_cpml_l1", {"nx": 300, "ny": 120, "fdorder": 8, "boundary": 1})]
 
 
 @pytest.mark.parametrize("name,over", TTI_VARIANTS,
                          ids=[n + "".join(f"-{k}{v}" for k, v in o.items()) for n, o in TTI_VARIANTS])
 def test_tti_fused_equals_two_kernel_form_and_oracle(name, over, monkeypatch):
     """The one-pass TTI stress kernel (derivatives in shared memory, CPML memory
-    in two buffers) computes exactly what the two-kernel form computes, and
-    both match the oracle, also with periodic x and a free surface."""
+    in two buffers), on 32 x 8 tiles everywhere ("fused") or with four-cell
+    64 x 32 tiles in the interior ("tiles", the default), computes exactly
+    what the two-kernel form computes, and all match the oracle, also with
+    periodic x and a free surface."""
     from oracle import oracle as O
     from tests.golden.cases import case_by_name
     from tests.helpers import case_receivers, case_sources
@@ -136,17 +142,18 @@ def test_tti_fused_equals_two_kernel_form_and_oracle(name, over, monkeypatch):
     sp = case_sources(case, cfg)
     sig = O.wavelet(1, cfg.nt, cfg.dt, sp)
     out = {}
-    for variant in ["split", "fused"]:
+    for variant in ["split", "fused", "tiles"]:
         monkeypatch.setenv("SOFI_TTI", variant)
         t = gpu_run_like(o, cfg, sp, sig, *case_receivers(case, cfg))
         out[variant] = {k: t.field(k) for k in ["vx", "vy", "sxx", "syy", "sxy"]}
         out[variant].update({c: t.section(c) for c in COMPS})
         out[variant]["snap_div"] = t.snapshots("div")
-        if variant == "fused":
+        if variant == "tiles":
             compare_sections(t, o, case["seismo"], name)
         t.close()
-    for k in out["fused"]:
-        np.testing.assert_array_equal(out["fused"][k], out["split"][k], err_msg=f"{name} {over} {k}")
+    for v in ("fused", "tiles"):
+        for k in out[v]:
+            np.testing.assert_array_equal(out[v][k], out["split"][k], err_msg=f"{name} {over} {v} {k}")
     o.close()
 
 
