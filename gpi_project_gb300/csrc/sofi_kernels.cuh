@@ -177,6 +177,32 @@ __device__ __forceinline__ void ldv_rw(const float *p, float *out)  // arrays th
     }
 }
 
+// VW-wide loads of operands each thread reads once, kept out of L1 (16-byte
+// loads; narrower ones are plain) so that the stencil rows the threads of a
+// block share stay there: read-only data through the non-coherent path, and
+// data the kernel writes (each cell by the thread that read it).
+template <int VW>
+__device__ __forceinline__ void ldv_once(const float *p, float *out)
+{
+    if (VW == 4)
+        asm("ld.global.nc.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+            : "=f"(out[0]), "=f"(out[1]), "=f"(out[2]), "=f"(out[3])
+            : "l"(p));
+    else
+        ldv<VW>(p, out);
+}
+
+template <int VW>
+__device__ __forceinline__ void ldv_rw_once(const float *p, float *out)
+{
+    if (VW == 4)
+        asm("ld.global.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+            : "=f"(out[0]), "=f"(out[1]), "=f"(out[2]), "=f"(out[3])
+            : "l"(p));
+    else
+        ldv_rw<VW>(p, out);
+}
+
 template <int VW>
 __device__ __forceinline__ void stv(float *p, const float *v)
 {
@@ -410,8 +436,8 @@ __device__ __forceinline__ void vw_tile(const Geo &G, const Wave &W, const Model
     float *__restrict__ vx = W.vx + so;
     float *__restrict__ vy = W.vy + so;
     float ox[VW], oy[VW], rp[VW], rq[VW];
-    ldv_rw<VW>(vx + o, ox), ldv_rw<VW>(vy + o, oy);
-    ldv<VW>(M.prip + mo + o, rp), ldv<VW>(M.prjp + mo + o, rq);
+    ldv_rw_once<VW>(vx + o, ox), ldv_rw_once<VW>(vy + o, oy);
+    ldv_once<VW>(M.prip + mo + o, rp), ldv_once<VW>(M.prjp + mo + o, rq);
     v_finish<VW, SXY, FWI>(G, W, M, s, i, j, o, mo, vx, vy, ox, oy, rp, rq, sxx_x, sxy_x, sxy_y, syy_y);
 }
 
@@ -1214,15 +1240,15 @@ __device__ __forceinline__ void tti_update4(const Geo &G, const Wave &W, const M
     float u1[4], u2[4], u3[4];
     {
         float a[4], b[4], c[4];
-        ldv<4>(M.c55ipjp + mo + o, a), ldv<4>(M.c15ipjp + mo + o, b), ldv<4>(M.c35ipjp + mo + o, c);
+        ldv_once<4>(M.c55ipjp + mo + o, a), ldv_once<4>(M.c15ipjp + mo + o, b), ldv_once<4>(M.c35ipjp + mo + o, c);
 #pragma unroll
         for (int k = 0; k < 4; k++)
             u1[k] = a[k] * (vxy0[k] + vyx0[k]) + b[k] * vxxipjp[k] + c[k] * vyyipjp[k];
     }
     {
         float c11[4], c13[4], c33[4], c15[4], c35[4];
-        ldv<4>(M.c11 + mo + o, c11), ldv<4>(M.c13 + mo + o, c13), ldv<4>(M.c33 + mo + o, c33);
-        ldv<4>(M.c15 + mo + o, c15), ldv<4>(M.c35 + mo + o, c35);
+        ldv_once<4>(M.c11 + mo + o, c11), ldv_once<4>(M.c13 + mo + o, c13), ldv_once<4>(M.c33 + mo + o, c33);
+        ldv_once<4>(M.c15 + mo + o, c15), ldv_once<4>(M.c35 + mo + o, c35);
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             const float vij = vyxij[k] + vxyij[k];
@@ -1239,8 +1265,8 @@ __device__ __forceinline__ void tti_update4(const Geo &G, const Wave &W, const M
             const long long lo = ((long long)s * G.L + l) * G.fsz + o;
             const float pe = M.peta[l], bb = M.bip[l], cc = M.cip[l];
             float r[4], p[4], q[4], x[4], y[4], z[4];
-            ldv_rw<4>(W.r + lo, r), ldv_rw<4>(W.p + lo, p), ldv_rw<4>(W.q + lo, q);
-            ldv<4>(M.c55ipjpb + mo + o, x), ldv<4>(M.c15ipjpb + mo + o, y), ldv<4>(M.c35ipjpb + mo + o, z);
+            ldv_rw_once<4>(W.r + lo, r), ldv_rw_once<4>(W.p + lo, p), ldv_rw_once<4>(W.q + lo, q);
+            ldv_once<4>(M.c55ipjpb + mo + o, x), ldv_once<4>(M.c15ipjpb + mo + o, y), ldv_once<4>(M.c35ipjpb + mo + o, z);
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 sro[k] += r[k];
@@ -1249,7 +1275,7 @@ __device__ __forceinline__ void tti_update4(const Geo &G, const Wave &W, const M
                 sr[k] += r[k];
             }
             stv<4>(W.r + lo, r);
-            ldv<4>(M.c11b + mo + o, x), ldv<4>(M.c13b + mo + o, y), ldv<4>(M.c15b + mo + o, z);
+            ldv_once<4>(M.c11b + mo + o, x), ldv_once<4>(M.c13b + mo + o, y), ldv_once<4>(M.c15b + mo + o, z);
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 spo[k] += p[k];
@@ -1258,7 +1284,7 @@ __device__ __forceinline__ void tti_update4(const Geo &G, const Wave &W, const M
                 sp[k] += p[k];
             }
             stv<4>(W.p + lo, p);
-            ldv<4>(M.c33b + mo + o, x), ldv<4>(M.c35b + mo + o, z);
+            ldv_once<4>(M.c33b + mo + o, x), ldv_once<4>(M.c35b + mo + o, z);
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 sqo[k] += q[k];
@@ -1275,22 +1301,12 @@ __device__ __forceinline__ void tti_update4(const Geo &G, const Wave &W, const M
             u3[k] += G.dthalbe * (sqo[k] + sq[k]);
         }
     }
-    float t[4];
-    ldv_rw<4>(W.sxy + so + o, t);
+    float oxy[4], oxx[4], oyy[4];
+    ldv_rw_once<4>(W.sxy + so + o, oxy), ldv_rw_once<4>(W.sxx + so + o, oxx), ldv_rw_once<4>(W.syy + so + o, oyy);
 #pragma unroll
     for (int k = 0; k < 4; k++)
-        t[k] += u1[k];
-    stv<4>(W.sxy + so + o, t);
-    ldv_rw<4>(W.sxx + so + o, t);
-#pragma unroll
-    for (int k = 0; k < 4; k++)
-        t[k] += u2[k];
-    stv<4>(W.sxx + so + o, t);
-    ldv_rw<4>(W.syy + so + o, t);
-#pragma unroll
-    for (int k = 0; k < 4; k++)
-        t[k] += u3[k];
-    stv<4>(W.syy + so + o, t);
+        oxy[k] += u1[k], oxx[k] += u2[k], oyy[k] += u3[k];
+    stv<4>(W.sxy + so + o, oxy), stv<4>(W.sxx + so + o, oxx), stv<4>(W.syy + so + o, oyy);
 }
 
 // One interior tile with origin (i0, j0) of cols x rows cells (cols a multiple
