@@ -105,6 +105,7 @@ def load():
         "sofi_stress_variant": ([vp, P(ctypes.c_int)], ctypes.c_int),
         "sofi_pdl": ([vp, P(ctypes.c_int)], ctypes.c_int),
         "sofi_block_threads_x": ([vp, P(ctypes.c_int), P(ctypes.c_int)], ctypes.c_int),
+        "sofi_post_fused": ([vp, P(ctypes.c_int)], ctypes.c_int),
         "sofi_set_pdl": ([vp, ctypes.c_int], ctypes.c_int),
         "sofi_fwi_begin": ([vp, ctypes.c_int, ctypes.c_int, P(ctypes.c_float), P(ctypes.c_float),
                             P(ctypes.c_float)], ctypes.c_int),

@@ -172,6 +172,10 @@ struct Acq {
     float *sec;              // [total receivers][5][ns]
     int nt, ns;
     int *status;             // [nshots] 0 ok, else first unstable step
+    // [nshots][NY][NX] (row-major, cell (j, i) at (j-1) NX + i-1; null unless
+    // the stress kernel may do the post work): bit 0 an explosive injection of
+    // the shot at the cell, bit 1 a receiver
+    const unsigned char *cell_flag;
 };
 
 __device__ __forceinline__ long long cell(const Geo &G, int j, int i)

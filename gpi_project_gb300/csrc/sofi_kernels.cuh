@@ -473,20 +473,94 @@ static __global__ void k_wrap_x(Geo G, float *a, float *b, float *c, int nd)
 
 // --------------------------------------------------------- stress update
 
+// k_post's work at cell (j, i) of shot s, done by the thread that has just
+// updated and stored its stresses (nxx, nyy in sxx[o], syy[o]) from the
+// CPML-stretched velocity derivatives: psource.c's explosive sources of step
+// nt in source order (time_loop.c:248-253), then the seismograms of
+// seismo_ssg.c:28-67 at the cell's receivers (div / curl from the
+// derivatives, p after the sources) and the NaN probe of time_loop.c:44-47 --
+// what post_column does for the cell, term by term.
+__device__ __forceinline__ void post_cell(const Geo &G, const Wave &W, const Model &M, const Acq &A, int s, int i,
+                                          int j, int o, long long mo, float *sxx, float *syy, float nxx, float nyy,
+                                          float vxx, float vyx, float vxy, float vyy, unsigned flag)
+{
+    const bool probe = i == (G.nx / 2 > 0 ? G.nx / 2 : 1) && j == (G.ny / 2 > 0 ? G.ny / 2 : 1);
+    if (!flag && !probe)
+        return;
+    const int nt = *G.step_ctr;  // the velocity kernel of this step advanced it
+    if (flag & 1) {  // the shot's last source is explosive and one source is here
+        const int NT = A.nt;
+        for (int k = A.src_off[s]; k < A.src_off[s + 1]; k++) {
+            if (A.src_ix[k] != i || A.src_iy[k] != j)
+                continue;
+            const float *sig = A.signals + (long long)k * NT - 1;  // 1-based
+            float amp = 0.0f;
+            const float d2 = 2.0f * G.dh * G.dh;
+            if (NT >= 2) {
+                if (nt == 1)
+                    amp = sig[2] / d2;
+                else if (nt < NT)
+                    amp = (sig[nt + 1] - sig[nt - 1]) / d2;
+                else
+                    amp = -sig[nt - 1] / d2;
+            }
+            nxx += amp;
+            nyy += amp;
+            sxx[o] = nxx;
+            syy[o] = nyy;
+        }
+    }
+    const long long so = (long long)s * G.fsz;
+    const int seismo = G.seismo;
+    const int ins = (seismo && G.ndt > 0 && nt % G.ndt == 0 && nt < A.nt) ? nt / G.ndt : 0;
+    if ((flag & 2) && ins) {
+        const int *roff = A.rec_col_off + (long long)s * (G.nx + 1);
+        for (int r = roff[i - 1]; r < roff[i]; r++) {
+            const int k = A.rec_col_idx[r];
+            if (A.rec_iy[k] != j)
+                continue;
+            float *sec = A.sec + (long long)k * 5 * A.ns + (ins - 1);
+            if (seismo == 3 || seismo == 4) {
+                sec[3 * A.ns] = (vxx + vyy) * sqrtf(M.ppi[mo + o]);
+                sec[4 * A.ns] = (vxy - vyx) * sqrtf(M.pu[mo + o]);
+            }
+            if (seismo == 1 || seismo == 4) {
+                sec[0] = W.vx[so + o];
+                sec[A.ns] = W.vy[so + o];
+            }
+            if (seismo == 2 || seismo == 4) {
+                float p = -nxx - nyy;
+                if (seismo == 2) {
+                    sec[2 * A.ns] = p;
+                } else {
+                    float ppi = M.ppi[mo + o], pu = M.pu[mo + o];
+                    sec[2 * A.ns] = ((3.0f * ppi - 4.0f * pu) / (2.0f * ppi - 2.0f * pu)) * p / 3.0f;
+                }
+            }
+        }
+    }
+    if (probe && isnan(W.vy[so + o]) && A.status[s] == 0)
+        A.status[s] = nt;
+}
+
 // Isotropic and VTI stress update, one thread per cell (wavefield_update_s_el.c,
 // _visc.c, _el_vti.c, _visc_VTI.c). Viscoelastic modulus defects are the
 // stored base (modulus * tau) times peta[l]; LT > 0 fixes the number of
 // mechanisms at compile time so every memory variable is loaded up front.
-template <int ND, int KIND, bool VISCO, int LT>
-__global__ void __launch_bounds__(BX *BY) k_update_s(Geo G, Wave W, Model M)
+// POST (k_update_s_post): the cell's share of k_post as well -- explosive
+// sources, seismograms, the NaN probe -- for steps without a free surface or
+// moment-tensor sources, so that the step needs no post kernel.
+template <int ND, int KIND, bool VISCO, int LT, bool POST>
+__device__ __forceinline__ void s_one(const Geo &G, const Wave &W, const Model &M, const Acq &A)
 {
-    pdl_begin();
     int bx, s;
     block_xs(G, bx, s);
     const int i = bx * BX + threadIdx.x + 1;
     const int j = blockIdx.y * BY + threadIdx.y + 1;
     if (i > G.nx || j > G.ny)
         return;
+    // POST: the cell's source / receiver flags, loaded with the operands
+    const unsigned pflag = POST ? __ldg(A.cell_flag + ((long long)s * G.ny + (j - 1)) * G.nx + (i - 1)) : 0u;
     const int P = G.pitch;
     const int o = (j - 1 + HY) * P + (i - 1 + HX);
     const long long so = (long long)s * G.fsz, mo = moff(G, s);
@@ -588,6 +662,23 @@ __global__ void __launch_bounds__(BX *BY) k_update_s(Geo G, Wave W, Model M)
     sxy[o] = nxy;
     sxx[o] = nxx;
     syy[o] = nyy;
+    if (POST)
+        post_cell(G, W, M, A, s, i, j, o, mo, sxx, syy, nxx, nyy, vxx, vyx, vxy, vyy, pflag);
+}
+
+template <int ND, int KIND, bool VISCO, int LT>
+__global__ void __launch_bounds__(BX *BY) k_update_s(Geo G, Wave W, Model M)
+{
+    pdl_begin();
+    const Acq none{};  // not read without POST
+    s_one<ND, KIND, VISCO, LT, false>(G, W, M, none);
+}
+
+template <int ND, int KIND, bool VISCO, int LT>
+__global__ void __launch_bounds__(BX *BY, 6) k_update_s_post(Geo G, Wave W, Model M, Acq A)
+{
+    pdl_begin();
+    s_one<ND, KIND, VISCO, LT, true>(G, W, M, A);
 }
 
 // The stress update with VW adjacent cells per thread (VW = 2 or 4), the

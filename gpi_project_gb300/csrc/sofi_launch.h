@@ -34,10 +34,11 @@ inline bool narrow_s_applies(bool visco, int L, bool fwi_step)
     return !fwi_step && (!visco || (L >= 1 && L <= 3));
 }
 // ISO / VTI stress update (KIND 0 ISO, 1 VTI): sw cells per thread in x (4, 2 or 0 = one);
-// narrow (sw 4, where narrow_s_applies): blocks of 8 x 32 threads
+// narrow (sw 4, where narrow_s_applies): blocks of 8 x 32 threads; post (sw 0 only, else
+// null): the one-cell kernel also does k_post's work with that acquisition
 template <int KIND, bool VISCO>
 void launch_stress_kv(const Geo &G, const Wave &W, const Model &M, int nd, int sw, bool narrow, dim3 grid,
-                      cudaStream_t st);
+                      cudaStream_t st, const Acq *post = nullptr);
 // acoustic stress update: sw cells per thread in x (4, 2 or 0/1 = one)
 void launch_stress_ac(const Geo &G, const Wave &W, const Model &M, int nd, int sw, dim3 grid, cudaStream_t st);
 // FDORDER_TIME = 4: step counter, velocity update, stress update (one cell per thread)

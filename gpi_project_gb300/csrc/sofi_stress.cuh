@@ -48,7 +48,7 @@ void stress_w(const Geo &G, const Wave &W, const Model &M, int nd, bool narrow, 
 
 template <int KIND, bool VISCO>
 void launch_stress_kv(const Geo &G, const Wave &W, const Model &M, int nd, int sw, bool narrow, dim3 grd,
-                      cudaStream_t st)
+                      cudaStream_t st, const Acq *post)
 {
     if (sw == 4)
         return stress_w<KIND, VISCO, 4>(G, W, M, nd, narrow, grd, st);
@@ -56,6 +56,22 @@ void launch_stress_kv(const Geo &G, const Wave &W, const Model &M, int nd, int s
         return stress_w<KIND, VISCO, 2>(G, W, M, nd, false, grd, st);
     const dim3 blk(BX, BY);
     [[maybe_unused]] const int L = VISCO ? G.L : 0;
+    if (post) {  // one cell per thread with k_post's work (k_update_s_post)
+        const Acq &A = *post;
+        if constexpr (!VISCO) {
+            DISPATCH_ND(nd, (launch_pdl(k_update_s_post<ND, KIND, false, 0>, grd, blk, 0, st, G, W, M, A)))
+        } else {
+            if (L == 1)
+                DISPATCH_ND(nd, (launch_pdl(k_update_s_post<ND, KIND, true, 1>, grd, blk, 0, st, G, W, M, A)))
+            else if (L == 2)
+                DISPATCH_ND(nd, (launch_pdl(k_update_s_post<ND, KIND, true, 2>, grd, blk, 0, st, G, W, M, A)))
+            else if (L == 3)
+                DISPATCH_ND(nd, (launch_pdl(k_update_s_post<ND, KIND, true, 3>, grd, blk, 0, st, G, W, M, A)))
+            else
+                DISPATCH_ND(nd, (launch_pdl(k_update_s_post<ND, KIND, true, 0>, grd, blk, 0, st, G, W, M, A)))
+        }
+        return;
+    }
     if constexpr (!VISCO) {
         DISPATCH_ND(nd, (launch_pdl(k_update_s<ND, KIND, false, 0>, grd, blk, 0, st, G, W, M)))
     } else {

@@ -3,5 +3,5 @@
 
 namespace sofi {
 template void launch_stress_kv<ISO, true>(const Geo &, const Wave &, const Model &, int, int, bool, dim3,
-                                        cudaStream_t);
+                                        cudaStream_t, const Acq *);
 }

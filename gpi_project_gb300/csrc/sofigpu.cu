@@ -181,6 +181,7 @@ struct sofi_ctx {
     int total_src = 0, total_rec = 0;
     void *acq_buf = nullptr;
     float *d_sec = nullptr;
+    unsigned char *d_cellflag = nullptr;  // Acq::cell_flag
     int *d_status = nullptr;
     int step = 0;
     float last_ms = 0.f;
@@ -221,6 +222,7 @@ struct sofi_ctx {
     cudaGraphExec_t graph_exec = nullptr;   // the step graph
     bool graph_ok = false;
     long long graph_launches = 0;  // kernels per replay
+    bool postf = true;         // k_post's work inside the one-cell stress kernel where it applies (SOFI_POSTF=0: off)
     bool tti_split = false;    // TTI: derivative fields through HBM (two kernels) instead of fused
     bool tti_fused = false;    // TTI: the one-pass kernel on 32 x 8 tiles everywhere (no four-cell interior tiles)
     // snapshots
@@ -299,6 +301,9 @@ long long fields_bytes(const sofi_config &c)
     long long nmod = c.shared_model ? 1 : c.nshots;
     long long nfields = (long long)needed_fields(c).size();
     long long bytes = 4 * (fsz * per_shot * c.nshots + psi * c.nshots + fsz * nfields * nmod);
+    const int kind = kind_of(c.weq);
+    if ((kind == ISO || kind == VTI) && !c.free_surf && !ab)  // the per-cell flags of the post work (upload_acq)
+        bytes += (long long)c.nx * c.ny * c.nshots;
     int nsnap = count_snapshots(c);
     if (nsnap) {
         long long sx = (c.nx - 1) / c.idx + 1, sy = (c.ny - 1) / c.idy + 1;
@@ -468,6 +473,35 @@ int upload_acq(sofi_ctx *c)
     A.status = c->d_status;
     c->total_src = ns_src;
     c->total_rec = nrec;
+    // the per-cell flags of the stress kernel that does the post work, where
+    // the configuration lets it (its memory: one byte per cell and shot)
+    if (c->d_cellflag) {
+        CK(cudaFreeAsync(c->d_cellflag, c->stream));
+        for (auto &p : c->allocs)
+            if (p == c->d_cellflag)
+                p = nullptr;
+        c->d_cellflag = nullptr;
+    }
+    A.cell_flag = nullptr;
+    const int kind = kind_of(c->cfg.weq);
+    if (c->postf && (kind == ISO || kind == VTI) && !c->cfg.free_surf && c->cfg.fdorder_time != 4) {
+        const size_t n = (size_t)S * c->cfg.ny * c->cfg.nx;
+        std::vector<unsigned char> fl(n, 0);
+        for (int s = 0; s < S; s++) {
+            const auto &a = c->acq[s];
+            unsigned char *f = fl.data() + (size_t)s * c->cfg.ny * c->cfg.nx;
+            if (last[s] == 1)
+                for (size_t k = 0; k < a.ix.size(); k++)
+                    f[(size_t)(a.iy[k] - 1) * c->cfg.nx + (a.ix[k] - 1)] |= 1;
+            for (size_t k = 0; k < a.rix.size(); k++)
+                f[(size_t)(a.riy[k] - 1) * c->cfg.nx + (a.rix[k] - 1)] |= 2;
+        }
+        if ((rc = dalloc(c, (void **)&c->d_cellflag, n)))
+            return rc;
+        CK(cudaMemcpyAsync(c->d_cellflag, fl.data(), n, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        A.cell_flag = c->d_cellflag;
+    }
     c->acq_dirty = false;
     c->graph_dirty = true;
     return 0;
@@ -483,7 +517,7 @@ dim3 grid2d(const sofi_ctx *c)
 
 // The ISO / VTI stress kernel with sw cells per thread in x (0: one).
 void launch_cell_s(const Geo &G, const Wave &W, const Model &M, int nd, int kind, bool visco, int sw, bool narrow,
-                   int nx, int ny, int nshots, cudaStream_t st)
+                   int nx, int ny, int nshots, cudaStream_t st, const Acq *post = nullptr)
 {
     narrow = narrow && sw == 4 && kind != AC && narrow_s_applies(visco, visco ? G.L : 0, W.fa_x != nullptr);
     const int cx = sw ? sw : 1, bxt = narrow ? 8 : BX, byt = BX * BY / bxt;
@@ -492,11 +526,11 @@ void launch_cell_s(const Geo &G, const Wave &W, const Model &M, int nd, int kind
     if (kind == AC)
         launch_stress_ac(G, W, M, nd, sw, grd, st);
     else if (kind == ISO)
-        visco ? launch_stress_kv<ISO, true>(G, W, M, nd, sw, narrow, grd, st)
-              : launch_stress_kv<ISO, false>(G, W, M, nd, sw, narrow, grd, st);
+        visco ? launch_stress_kv<ISO, true>(G, W, M, nd, sw, narrow, grd, st, post)
+              : launch_stress_kv<ISO, false>(G, W, M, nd, sw, narrow, grd, st, post);
     else
-        visco ? launch_stress_kv<VTI, true>(G, W, M, nd, sw, narrow, grd, st)
-              : launch_stress_kv<VTI, false>(G, W, M, nd, sw, narrow, grd, st);
+        visco ? launch_stress_kv<VTI, true>(G, W, M, nd, sw, narrow, grd, st, post)
+              : launch_stress_kv<VTI, false>(G, W, M, nd, sw, narrow, grd, st, post);
 }
 
 // The wave fields a step's kernels get: the gradient quantities of an FWI
@@ -677,6 +711,23 @@ int autotune(sofi_ctx *c)
     return 0;
 }
 
+// Whether the one-cell ISO / VTI stress kernel does k_post's work in this
+// step (k_update_s_post): no free surface (its correction needs the column's
+// updated rows), no moment-tensor source (it reaches a neighbouring cell),
+// few sources per shot (every thread scans them), 2nd-order time, no FWI run.
+constexpr size_t kFusedSources = 8;
+static bool post_fused(const sofi_ctx *c)
+{
+    const int kind = kind_of(c->cfg.weq);
+    if (!c->postf || !c->A.cell_flag || c->sw != 0 || (kind != ISO && kind != VTI) || c->cfg.free_surf ||
+        c->G.ab4 || c->fwi)
+        return false;
+    for (const auto &a : c->acq)
+        if ((!a.type.empty() && a.type.back() == 5) || a.ix.size() > kFusedSources)
+            return false;
+    return true;
+}
+
 int launch_step(sofi_ctx *c, int nt, bool capture = false)
 {
     const sofi_config &cf = c->cfg;
@@ -687,6 +738,7 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
     int nb = (S + 127) / 128;
     int kind = kind_of(cf.weq);
     bool visco = is_visco(cf.weq);
+    const bool fused_post = post_fused(c);
     if (c->has_force) {
         launch_pdl(k_force_src, nb, 128, 0, st, G, c->W, c->M, c->A);
         c->launches++;
@@ -736,19 +788,22 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
     } else if (kind == TTI) {
         launch_tti_tiles(G, c->W, c->M, c->nd, visco, G.abs_type == 1, st);
     } else {
-        launch_cell_s(G, step_wave(c), c->M, c->nd, kind, visco, c->sw, c->snarrow, cf.nx, cf.ny, S, st);
+        launch_cell_s(G, step_wave(c), c->M, c->nd, kind, visco, c->sw, c->snarrow, cf.nx, cf.ny, S, st,
+                      fused_post ? &c->A : nullptr);
     }
     c->launches++;
     if (timed)
         CK(cudaEventRecord(e2, st));
     dim3 pg((cf.nx + 127) / 128, S);
-    if (kind == TTI)
+    if (fused_post) {
+    } else if (kind == TTI) {
         DISPATCH_ND(c->nd, (launch_pdl(k_post<ND, false, true>, pg, 128, 0, st, G, c->W, c->M, c->A)))
-    else if (visco)
+    } else if (visco) {
         DISPATCH_ND(c->nd, (launch_pdl(k_post<ND, true, false>, pg, 128, 0, st, G, c->W, c->M, c->A)))
-    else
+    } else {
         DISPATCH_ND(c->nd, (launch_pdl(k_post<ND, false, false>, pg, 128, 0, st, G, c->W, c->M, c->A)))
-    c->launches++;
+    }
+    c->launches += fused_post ? 0 : 1;
     if (cf.boundary) {
         k_wrap_x<<<dim3((cf.ny + 127) / 128, S), 128, 0, st>>>(G, c->W.sxx, c->W.syy, c->W.sxy, c->nd);
         c->launches++;
@@ -926,6 +981,8 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
         c->snarrow = e[0] == 'n';
         c->sw_fixed = true;
     }
+    if (const char *e = getenv("SOFI_POSTF"))
+        c->postf = atoi(e) != 0;
     if (const char *e = getenv("SOFI_TTI")) {  // "split", "fused"; else the tiled one-pass form
         c->tti_split = strcmp(e, "split") == 0;
         c->tti_fused = strcmp(e, "fused") == 0;
@@ -1727,6 +1784,14 @@ int sofi_set_pdl(sofi_ctx *c, int on)
     CK(cudaStreamSynchronize(c->stream));
     c->pdl = on != 0;
     c->graph_dirty = true;
+    return 0;
+}
+
+int sofi_post_fused(sofi_ctx *c, int *on)
+{
+    if (!c || !on)
+        return fail(SOFI_E_ARG, "null argument");
+    *on = post_fused(c) ? 1 : 0;
     return 0;
 }
 

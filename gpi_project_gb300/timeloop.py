@@ -154,6 +154,13 @@ class TimeLoop:
     def set_pdl(self, on: bool) -> None:
         N.check(self.lib.sofi_set_pdl(self.h, int(bool(on))))
 
+    def post_fused(self) -> bool:
+        """Whether the stress kernel also does the post-stress kernel's work
+        (sources, seismograms, NaN probe) on the current settings."""
+        n = ctypes.c_int()
+        N.check(self.lib.sofi_post_fused(self.h, ctypes.byref(n)))
+        return bool(n.value)
+
     def block_threads_x(self) -> tuple:
         """Threads per block along x of the four-cell (velocity, stress) kernels: 32, or 8 for narrow blocks."""
         a, b = ctypes.c_int(), ctypes.c_int()

@@ -253,6 +253,13 @@ int sofi_stress_variant(sofi_ctx *ctx, int *cells_per_thread);
  * edge of a narrow grid); chosen by the same autotuning run, SOFI_VROWS=n4 /
  * SOFI_SW=n4 fix the narrow form. */
 int sofi_block_threads_x(sofi_ctx *ctx, int *velocity, int *stress);
+/* 1 when the steps of a sofi_run on the current settings launch no separate
+ * post-stress kernel: the one-cell stress kernel (sofi_stress_variant 1)
+ * injects the explosive sources, samples the seismograms and probes for NaN
+ * itself. It applies to ISO and VTI media with 2nd-order time, no free
+ * surface, no moment-tensor source and at most 8 sources per shot, outside
+ * FWI runs; SOFI_POSTF=0 turns it off. Results are bit-identical either way. */
+int sofi_post_fused(sofi_ctx *ctx, int *on);
 /* Kernels launched by sofi_run since the context was created. */
 int sofi_launch_count(sofi_ctx *ctx, long long *launches);
 /* The context's CUDA stream (a cudaStream_t), for callers that order their own
