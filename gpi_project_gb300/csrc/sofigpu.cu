@@ -621,6 +621,8 @@ static bool narrow_useful(int nx)
     return (w - nx) * 100 >= 8 * w;
 }
 
+static bool post_fused(const sofi_ctx *c);
+
 int autotune(sofi_ctx *c)
 {
     c->tuned = true;
@@ -699,6 +701,39 @@ int autotune(sofi_ctx *c)
                     return rc;
                 t[k] = ms < t[k] ? ms : t[k];
             }
+        // where the one-cell kernel would do the post work (post_fused), it
+        // saves a k_post launch per step: credit it with one, timed on an
+        // empty acquisition and a zero step count (it then reads only the
+        // zero state and writes nothing); one shot, as d_noacq holds two ints
+        const int keep_sw = c->sw;
+        c->sw = 0;
+        const bool fusable = cf.nshots == 1 && (kind == ISO || kind == VTI) && post_fused(c);
+        c->sw = keep_sw;
+        if (fusable && !c->d_noacq && (rc = dalloc(c, (void **)&c->d_noacq, 2 * sizeof(int))))
+            return rc;
+        if (fusable) {
+            Geo Gp = G;
+            Gp.step_ctr = c->d_noacq;
+            Acq E = c->A;
+            E.src_off = c->d_noacq, E.last_type = c->d_noacq, E.rec_col_off = nullptr;
+            const dim3 pg((cf.nx + 127) / 128, 1);
+            float tp = 1e30f;
+            for (int r = 0; r < kRounds; r++) {
+                if ((rc = time_launches(c,
+                                        [&] {
+                                            if (visco)
+                                                DISPATCH_ND(c->nd, (launch_pdl(k_post<ND, true, false>, pg, 128, 0,
+                                                                               c->stream, Gp, step_wave(c), c->M, E)))
+                                            else
+                                                DISPATCH_ND(c->nd, (launch_pdl(k_post<ND, false, false>, pg, 128, 0,
+                                                                               c->stream, Gp, step_wave(c), c->M, E)))
+                                        },
+                                        &ms)))
+                    return rc;
+                tp = ms < tp ? ms : tp;
+            }
+            t[2] -= tp;  // cand[2]: one cell per thread
+        }
         best = 1e30f;
         for (int k = 0; k < nc; k++)
             if (t[k] < best)
@@ -714,7 +749,7 @@ int autotune(sofi_ctx *c)
 // Whether the one-cell ISO / VTI stress kernel does k_post's work in this
 // step (k_update_s_post): no free surface (its correction needs the column's
 // updated rows), no moment-tensor source (it reaches a neighbouring cell),
-// few sources per shot (every thread scans them), 2nd-order time, no FWI run.
+// few sources per shot (a flagged cell scans them), 2nd-order time, no FWI run.
 constexpr size_t kFusedSources = 8;
 static bool post_fused(const sofi_ctx *c)
 {
