@@ -899,7 +899,7 @@ __device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model
 }
 
 template <int ND, int KIND, bool VISCO, int LT, int VW, bool FWI = false, int TBX = BX>
-__global__ void __launch_bounds__(BX *BY, VW == 4 ? 2 : 1) k_update_sw(Geo G, Wave W, Model M)
+__global__ void __launch_bounds__(BX *BY, VW == 4 ? (VISCO ? 2 : 3) : 1) k_update_sw(Geo G, Wave W, Model M)
 {
     pdl_begin();
     sw_tile<ND, KIND, VISCO, LT, VW, FWI, TBX>(G, W, M, blockIdx);

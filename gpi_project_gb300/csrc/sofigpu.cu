@@ -702,12 +702,14 @@ int autotune(sofi_ctx *c)
                 t[k] = ms < t[k] ? ms : t[k];
             }
         // where the one-cell kernel would do the post work (post_fused), it
-        // saves a k_post launch per step: credit it with one, timed on an
-        // empty acquisition and a zero step count (it then reads only the
-        // zero state and writes nothing); one shot, as d_noacq holds two ints
+        // saves a k_post launch per step: on launch-bound grids (at most
+        // 512 x 512 cells) credit it with one, timed on an empty acquisition
+        // and a zero step count (it then reads only the zero state and
+        // writes nothing); one shot, as d_noacq holds two ints
         const int keep_sw = c->sw;
         c->sw = 0;
-        const bool fusable = cf.nshots == 1 && (kind == ISO || kind == VTI) && post_fused(c);
+        const bool fusable = cf.nshots == 1 && (long long)cf.nx * cf.ny <= 512 * 512 &&
+                             (kind == ISO || kind == VTI) && post_fused(c);
         c->sw = keep_sw;
         if (fusable && !c->d_noacq && (rc = dalloc(c, (void **)&c->d_noacq, 2 * sizeof(int))))
             return rc;
