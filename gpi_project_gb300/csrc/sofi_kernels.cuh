@@ -1520,15 +1520,18 @@ __global__ void __launch_bounds__(BX *BY, VISCO ? 2 : 4) k_tti_tiles(Geo G, Wave
 // psource.c:27-54 / eqsource.c:25-52 restricted to the cells of column i:
 // every source of the shot, in order, when the last source's type selects the
 // injection (time_loop.c:248-253); a moment tensor also reaches column i-1.
-__device__ __forceinline__ void post_sources(const Geo &G, const Wave &W, const Acq &A, int s, int i, int nt)
+// lt, ka, kb: the shot's last source type and source range (A.last_type[s],
+// A.src_off[s], A.src_off[s + 1]), loaded by the caller with its other
+// independent loads.
+__device__ __forceinline__ void post_sources(const Geo &G, const Wave &W, const Acq &A, int s, int i, int nt, int lt,
+                                             int ka, int kb)
 {
-    const int lt = A.last_type[s];
     if (lt != 1 && lt != 5)
         return;
     const long long so = (long long)s * G.fsz;
     float *sxx = W.sxx + so, *syy = W.syy + so, *sxy = W.sxy + so;
     const int NT = A.nt;
-    for (int k = A.src_off[s]; k < A.src_off[s + 1]; k++) {
+    for (int k = ka; k < kb; k++) {
         const int si = A.src_ix[k], sj = A.src_iy[k];
         if (si != i && !(lt == 5 && si - 1 == i))
             continue;
@@ -1725,6 +1728,8 @@ template <int ND, bool VISCO, bool TTIK>
 __device__ __forceinline__ void post_column(const Geo &G, Wave W, const Model &M, const Acq &A, int i, int s)
 {
     const int nt = *G.step_ctr;  // the velocity kernel of this step advanced it
+    // the shot's sources, loaded with the receiver range below (independent loads)
+    const int lt = A.last_type[s], ka = A.src_off[s], kb = A.src_off[s + 1];
     const int seismo = G.seismo;
     psi_buffers(G, W, false);    // TTI: the CPML memory this step's stress update wrote
     // time_loop.c:282: sample at nt = NDT, 2 NDT, ... while nt < NT
@@ -1744,7 +1749,7 @@ __device__ __forceinline__ void post_column(const Geo &G, Wave W, const Model &M
     if (ins && (seismo == 3 || seismo == 4))
         for (int r = r0; r < r1; r++)
             sample_div_curl<ND, TTIK>(G, W, M, A, s, A.rec_col_idx[r], ins);
-    post_sources(G, W, A, s, i, nt);
+    post_sources(G, W, A, s, i, nt, lt, ka, kb);
     if (G.free_surf)
         post_surface<ND, VISCO>(G, W, M, s, i);
     if (i == (G.nx / 2 > 0 ? G.nx / 2 : 1)) {
