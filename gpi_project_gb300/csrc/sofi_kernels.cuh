@@ -1400,9 +1400,88 @@ __device__ __forceinline__ void tti_update4(const Geo &G, const Wave &W, const M
     stv<4>(W.sxy + so + o, oxy), stv<4>(W.sxx + so + o, oxx), stv<4>(W.syy + so + o, oyy);
 }
 
+// The velocity derivatives of the four-cell groups of rows j and j + 1
+// (columns i .. i + 3, padded offset o of (j, i)), stored to shared memory at
+// q (row j) and q + row (row j + 1), planes plane apart: vxx vyy vyx vxy. The
+// y stencils of both rows come from one window of 2 ND + 1 rows of vx and of
+// vy; per cell the expressions of s_derivs, term by term.
+template <int ND>
+__device__ __forceinline__ void s_derivs_pair(const Geo &G, const float *__restrict__ vx,
+                                              const float *__restrict__ vy, int o, int P, float *q, int row,
+                                              int plane)
+{
+    const float *hc = G.hc;
+    constexpr int K = (ND + 3) / 4, NXS = 4 * (2 * K + 1), C = 4 * K;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {  // x stencils, row by row
+        float X[NXS], Y[NXS];
+#pragma unroll
+        for (int u = 0; u < 2 * K + 1; u++) {
+            ldv<4>(vx + o + h * P + 4 * (u - K), X + 4 * u);
+            ldv<4>(vy + o + h * P + 4 * (u - K), Y + 4 * u);
+        }
+        float dxx[4], dyx[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            dxx[c] = hc[1] * (X[C + c] - X[C + c - 1]);
+            dyx[c] = hc[1] * (Y[C + c + 1] - Y[C + c]);
+#pragma unroll
+            for (int m = 2; m <= ND; m++) {
+                dxx[c] += hc[m] * (X[C + c + m - 1] - X[C + c - m]);
+                dyx[c] += hc[m] * (Y[C + c + m] - Y[C + c - m + 1]);
+            }
+            dxx[c] *= G.dhi, dyx[c] *= G.dhi;
+        }
+        stv<4>(q + h * row, dxx), stv<4>(q + h * row + 2 * plane, dyx);
+    }
+    {
+        // vx rows j - ND + 1 .. j + ND + 1: R[d] = vx(j - ND + 1 + d)
+        float R[2 * ND + 1][4];
+#pragma unroll
+        for (int d = 0; d < 2 * ND + 1; d++)
+            ldv<4>(vx + o + (d - ND + 1) * P, R[d]);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int z = ND - 1 + h;  // index of row j + h
+            float dxy[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                dxy[c] = hc[1] * (R[z + 1][c] - R[z][c]);
+#pragma unroll
+                for (int m = 2; m <= ND; m++)
+                    dxy[c] += hc[m] * (R[z + m][c] - R[z - (m - 1)][c]);
+                dxy[c] *= G.dhi;
+            }
+            stv<4>(q + h * row + 3 * plane, dxy);
+        }
+    }
+    {
+        // vy rows j - ND .. j + ND: R[d] = vy(j - ND + d)
+        float R[2 * ND + 1][4];
+#pragma unroll
+        for (int d = 0; d < 2 * ND + 1; d++)
+            ldv<4>(vy + o + (d - ND) * P, R[d]);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int z = ND + h;  // index of row j + h
+            float dyy[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                dyy[c] = hc[1] * (R[z][c] - R[z - 1][c]);
+#pragma unroll
+                for (int m = 2; m <= ND; m++)
+                    dyy[c] += hc[m] * (R[z + m - 1][c] - R[z - m][c]);
+                dyy[c] *= G.dhi;
+            }
+            stv<4>(q + h * row + plane, dyy);
+        }
+    }
+}
+
 // One interior tile with origin (i0, j0) of cols x rows cells (cols a multiple
 // of 4, at most 64; rows at most 32), 256 threads: each thread derives four
-// adjacent cells of two rows (16-byte loads, s_derivs), warps 0-3 derive the
+// adjacent cells of two adjacent rows (16-byte loads, s_derivs_pair: one
+// window of rows for both rows' y stencils), warps 0-3 derive the
 // ring (the rows above and below as four-cell groups, the columns left and
 // right cell by cell), all into sm ([vxx vyy vyx vxy][34][72]: row 0 is
 // j0 - 1, column 3 is i0 - 1); then each thread updates its cells from there.
@@ -1435,10 +1514,12 @@ __device__ __forceinline__ void tti_tile4(const Geo &G, const Wave &W, const Mod
         q[0] = d0, q[T4P] = d1, q[2 * T4P] = d2, q[3 * T4P] = d3;
     };
     const bool gon = 4 * gx < cols;
-    if (gon && gy < rows)
-        group(j0 + gy, i0 + 4 * gx, gy + 1, 4 + 4 * gx);
-    if (gon && gy + 16 < rows)
-        group(j0 + gy + 16, i0 + 4 * gx, gy + 17, 4 + 4 * gx);
+    const int r0 = 2 * gy;  // this thread's rows: r0 and r0 + 1
+    if (gon && r0 + 1 < rows)
+        s_derivs_pair<ND>(G, vx, vy, (j0 + r0 - 1 + HY) * P + (i0 + 4 * gx - 1 + HX), P,
+                          sm + (r0 + 1) * T4W + 4 + 4 * gx, T4W, T4P);
+    else if (gon && r0 < rows)
+        group(j0 + r0, i0 + 4 * gx, r0 + 1, 4 + 4 * gx);
     if (w == 0) {  // rows j0 - 1 (lanes 0-15) and j0 + rows (lanes 16-31)
         const int top = lane < 16, g = lane & 15;
         if (4 * g < cols)
@@ -1460,7 +1541,7 @@ __device__ __forceinline__ void tti_tile4(const Geo &G, const Wave &W, const Mod
         return;
     const long long mo = moff(G, s);
 #pragma unroll 1
-    for (int r = gy; r < rows; r += 16) {
+    for (int r = r0; r < rows && r < r0 + 2; r++) {
         const int j = j0 + r, i = i0 + 4 * gx;
         const int o = (j - 1 + HY) * P + (i - 1 + HX);
         const float *q = sm + (r + 1) * T4W + 4 + 4 * gx;  // (j, i)
