@@ -284,6 +284,16 @@ int count_snapshots(const sofi_config &c)
     return n;
 }
 
+// Where upload_acq builds the per-cell flags that let the one-cell ISO / VTI
+// stress kernel do the post work (post_fused): no free surface, 2nd-order
+// time, and grids small enough (all shots) that a saved launch matters.
+bool post_flags_apply(const sofi_config &c)
+{
+    const int kind = kind_of(c.weq);
+    return (kind == ISO || kind == VTI) && !c.free_surf && c.fdorder_time != 4 &&
+           (long long)c.nx * c.ny * c.nshots <= (4LL << 20);
+}
+
 long long fields_bytes(const sofi_config &c)
 {
     long long pitch = pitch_for(c.nx), fsz = pitch * (c.ny + 2 * HY);
@@ -301,8 +311,7 @@ long long fields_bytes(const sofi_config &c)
     long long nmod = c.shared_model ? 1 : c.nshots;
     long long nfields = (long long)needed_fields(c).size();
     long long bytes = 4 * (fsz * per_shot * c.nshots + psi * c.nshots + fsz * nfields * nmod);
-    const int kind = kind_of(c.weq);
-    if ((kind == ISO || kind == VTI) && !c.free_surf && !ab)  // the per-cell flags of the post work (upload_acq)
+    if (post_flags_apply(c))  // the per-cell flags of the post work (upload_acq)
         bytes += (long long)c.nx * c.ny * c.nshots;
     int nsnap = count_snapshots(c);
     if (nsnap) {
@@ -483,8 +492,7 @@ int upload_acq(sofi_ctx *c)
         c->d_cellflag = nullptr;
     }
     A.cell_flag = nullptr;
-    const int kind = kind_of(c->cfg.weq);
-    if (c->postf && (kind == ISO || kind == VTI) && !c->cfg.free_surf && c->cfg.fdorder_time != 4) {
+    if (c->postf && post_flags_apply(c->cfg)) {
         const size_t n = (size_t)S * c->cfg.ny * c->cfg.nx;
         std::vector<unsigned char> fl(n, 0);
         for (int s = 0; s < S; s++) {

@@ -257,8 +257,10 @@ int sofi_block_threads_x(sofi_ctx *ctx, int *velocity, int *stress);
  * post-stress kernel: the one-cell stress kernel (sofi_stress_variant 1)
  * injects the explosive sources, samples the seismograms and probes for NaN
  * itself. It applies to ISO and VTI media with 2nd-order time, no free
- * surface, no moment-tensor source and at most 8 sources per shot, outside
- * FWI runs; SOFI_POSTF=0 turns it off. Results are bit-identical either way. */
+ * surface, no moment-tensor source and at most 8 sources per shot, on grids
+ * of at most 2^22 cells over all shots, outside FWI runs; SOFI_POSTF=0 turns
+ * it off. Results are bit-identical either way for ISO media; for VTI media
+ * the two stress kernels agree to float32 rounding. */
 int sofi_post_fused(sofi_ctx *ctx, int *on);
 /* Kernels launched by sofi_run since the context was created. */
 int sofi_launch_count(sofi_ctx *ctx, long long *launches);
