@@ -7,36 +7,52 @@ namespace sofi {
 // -------------------------------------------------------------- sources
 
 // update_v_interior.c:49-71. Runs before the velocity kernel advances the
-// step counter, so the step being computed is counter + 1. (static: the
+// step counter, so the step being computed is counter + 1. The sources and
+// the model do not change during a run: the shot's source range, its first
+// source's type and cell and the buoyancy there load before the wait for the
+// previous kernel, the step number and the velocities after it. (static: the
 // header is included by several translation units; only sofigpu.cu launches it)
-__device__ __forceinline__ void force_shot(const Geo &G, const Wave &W, const Model &M, const Acq &A, int s)
+__device__ __forceinline__ void force_shot(const Geo &G, const Wave &W, const Model &M, const Acq &A, int s, bool live)
 {
-    const int nt = *G.step_ctr + 1;
     const float *prip = M.prip + moff(G, s), *prjp = M.prjp + moff(G, s);
+    int ka = 0, kb = 0, t0 = 0;
+    long long o0 = 0;
+    float rx0 = 0.f, ry0 = 0.f;
+    if (live) {
+        ka = A.src_off[s], kb = A.src_off[s + 1];
+        if (ka < kb) {
+            t0 = A.src_type[ka];
+            o0 = cell(G, A.src_iy[ka], A.src_ix[ka]);
+            rx0 = prip[o0], ry0 = prjp[o0];
+        }
+    }
+    pdl_begin();
+    if (!live)
+        return;
+    const int nt = *G.step_ctr + 1;
     float *vx = W.vx + (long long)s * G.fsz, *vy = W.vy + (long long)s * G.fsz;
-    for (int k = A.src_off[s]; k < A.src_off[s + 1]; k++) {
-        int t = A.src_type[k];
+    for (int k = ka; k < kb; k++) {
+        const int t = k == ka ? t0 : A.src_type[k];
         if (t < 2 || t > 4)
             continue;
-        long long o = cell(G, A.src_iy[k], A.src_ix[k]);
+        const long long o = k == ka ? o0 : cell(G, A.src_iy[k], A.src_ix[k]);
+        const float rx = k == ka ? rx0 : prip[o], ry = k == ka ? ry0 : prjp[o];
         float amp = (G.dt * A.signals[(long long)k * A.nt + (nt - 1)]) / (G.dh * G.dh);
         if (t == 2)
-            vx[o] += prip[o] * amp;
+            vx[o] += rx * amp;
         else if (t == 3)
-            vy[o] += prjp[o] * amp;
+            vy[o] += ry * amp;
         else {
-            vx[o] += A.src_sin[k] * (prip[o] * amp);
-            vy[o] += A.src_cos[k] * (prjp[o] * amp);
+            vx[o] += A.src_sin[k] * (rx * amp);
+            vy[o] += A.src_cos[k] * (ry * amp);
         }
     }
 }
 
 static __global__ void k_force_src(Geo G, Wave W, Model M, Acq A)
 {
-    pdl_begin();
     int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < G.nshots)
-        force_shot(G, W, M, A, s);
+    force_shot(G, W, M, A, s, s < G.nshots);
 }
 
 // ------------------------------------------------------- velocity update
@@ -1604,8 +1620,9 @@ __global__ void __launch_bounds__(BX *BY, VISCO ? 2 : 4) k_tti_tiles(Geo G, Wave
 // lt, ka, kb: the shot's last source type and source range (A.last_type[s],
 // A.src_off[s], A.src_off[s + 1]), loaded by the caller with its other
 // independent loads.
+// (si0, sj0): the first source's cell (k = ka), loaded by the caller too.
 __device__ __forceinline__ void post_sources(const Geo &G, const Wave &W, const Acq &A, int s, int i, int nt, int lt,
-                                             int ka, int kb)
+                                             int ka, int kb, int si0, int sj0)
 {
     if (lt != 1 && lt != 5)
         return;
@@ -1613,7 +1630,7 @@ __device__ __forceinline__ void post_sources(const Geo &G, const Wave &W, const 
     float *sxx = W.sxx + so, *syy = W.syy + so, *sxy = W.sxy + so;
     const int NT = A.nt;
     for (int k = ka; k < kb; k++) {
-        const int si = A.src_ix[k], sj = A.src_iy[k];
+        const int si = k == ka ? si0 : A.src_ix[k], sj = k == ka ? sj0 : A.src_iy[k];
         if (si != i && !(lt == 5 && si - 1 == i))
             continue;
         const float *sig = A.signals + (long long)k * NT - 1;  // 1-based: sig[1..NT]
@@ -1799,6 +1816,32 @@ __device__ __forceinline__ void sample_v_p(const Geo &G, const Wave &W, const Mo
     }
 }
 
+// The part of a column's post work that depends only on the acquisition,
+// which no kernel writes: the shot's last source type and source range, the
+// first source's cell, the column's receiver range and its first receiver's
+// cell. k_post loads it before it waits for the stress kernel.
+struct PostCol {
+    int lt, ka, kb, si0, sj0, r0, r1, k0;
+    long long o0;
+};
+
+__device__ __forceinline__ PostCol post_acq(const Geo &G, const Acq &A, int i, int s)
+{
+    PostCol p;
+    p.lt = A.last_type[s], p.ka = A.src_off[s], p.kb = A.src_off[s + 1];
+    const int *roff = A.rec_col_off ? A.rec_col_off + (long long)s * (G.nx + 1) : nullptr;
+    p.r0 = roff ? roff[i - 1] : 0, p.r1 = roff ? roff[i] : 0;
+    p.si0 = p.sj0 = p.k0 = 0;
+    p.o0 = 0;
+    if (p.ka < p.kb)
+        p.si0 = A.src_ix[p.ka], p.sj0 = A.src_iy[p.ka];
+    if (p.r0 < p.r1) {
+        p.k0 = A.rec_col_idx[p.r0];
+        p.o0 = cell(G, A.rec_iy[p.k0], A.rec_ix[p.k0]);
+    }
+    return p;
+}
+
 // Everything of time_loop.c:247-285 after the stress update, one thread per
 // column: every operation below reads and writes only cells of its own column
 // (a moment tensor's column-(i-1) term is applied by that column's thread), so
@@ -1806,42 +1849,35 @@ __device__ __forceinline__ void sample_v_p(const Geo &G, const Wave &W, const Mo
 // sampling (from the stress update's derivatives), source injection, free
 // surface, the NaN probe of time_loop.c:44-47, vx/vy/p sampling.
 template <int ND, bool VISCO, bool TTIK>
-__device__ __forceinline__ void post_column(const Geo &G, Wave W, const Model &M, const Acq &A, int i, int s)
+__device__ __forceinline__ void post_column(const Geo &G, Wave W, const Model &M, const Acq &A, int i, int s,
+                                            const PostCol &pc)
 {
     const int nt = *G.step_ctr;  // the velocity kernel of this step advanced it
-    // the shot's sources, loaded with the receiver range below (independent loads)
-    const int lt = A.last_type[s], ka = A.src_off[s], kb = A.src_off[s + 1];
     const int seismo = G.seismo;
     psi_buffers(G, W, false);    // TTI: the CPML memory this step's stress update wrote
     // time_loop.c:282: sample at nt = NDT, 2 NDT, ... while nt < NT
     const int ins = (seismo && G.ndt > 0 && nt % G.ndt == 0 && nt < A.nt) ? nt / G.ndt : 0;
-    const int *roff = A.rec_col_off ? A.rec_col_off + (long long)s * (G.nx + 1) : nullptr;
-    const int r0 = roff ? roff[i - 1] : 0, r1 = roff ? roff[i] : 0;
-    // the column's first receiver, loaded ahead of the stores below
+    const int r0 = pc.r0, r1 = pc.r1;
+    // the column's first receiver's velocities, loaded ahead of the stores below
     const long long so = (long long)s * G.fsz;
-    int k0 = 0;
-    long long o0 = 0;
     float vx0 = 0.f, vy0 = 0.f;
-    if (r0 < r1) {
-        k0 = A.rec_col_idx[r0];
-        o0 = cell(G, A.rec_iy[k0], A.rec_ix[k0]);
-        vx0 = W.vx[so + o0], vy0 = W.vy[so + o0];
-    }
+    if (r0 < r1)
+        vx0 = W.vx[so + pc.o0], vy0 = W.vy[so + pc.o0];
     if (ins && (seismo == 3 || seismo == 4))
         for (int r = r0; r < r1; r++)
             sample_div_curl<ND, TTIK>(G, W, M, A, s, A.rec_col_idx[r], ins);
-    post_sources(G, W, A, s, i, nt, lt, ka, kb);
+    post_sources(G, W, A, s, i, nt, pc.lt, pc.ka, pc.kb, pc.si0, pc.sj0);
     if (G.free_surf)
         post_surface<ND, VISCO>(G, W, M, s, i);
     if (i == (G.nx / 2 > 0 ? G.nx / 2 : 1)) {
-        long long pc = cell(G, G.ny / 2 > 0 ? G.ny / 2 : 1, i);
-        if (isnan(W.vy[so + pc]) && A.status[s] == 0)
+        long long pcell = cell(G, G.ny / 2 > 0 ? G.ny / 2 : 1, i);
+        if (isnan(W.vy[so + pcell]) && A.status[s] == 0)
             A.status[s] = nt;
     }
     if (ins && seismo != 3)
         for (int r = r0; r < r1; r++) {
             if (r == r0) {
-                sample_v_p(G, W, M, A, s, k0, o0, vx0, vy0, ins, seismo);
+                sample_v_p(G, W, M, A, s, pc.k0, pc.o0, vx0, vy0, ins, seismo);
             } else {
                 const int k = A.rec_col_idx[r];
                 const long long o = cell(G, A.rec_iy[k], A.rec_ix[k]);
@@ -1853,10 +1889,13 @@ __device__ __forceinline__ void post_column(const Geo &G, Wave W, const Model &M
 template <int ND, bool VISCO, bool TTIK>
 __global__ void k_post(Geo G, Wave W, Model M, Acq A)
 {
-    pdl_begin();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, s = blockIdx.y;
+    PostCol pc{};
     if (i <= G.nx)
-        post_column<ND, VISCO, TTIK>(G, W, M, A, i, blockIdx.y);
+        pc = post_acq(G, A, i, s);
+    pdl_begin();
+    if (i <= G.nx)
+        post_column<ND, VISCO, TTIK>(G, W, M, A, i, s, pc);
 }
 
 // snap_ssg.c:86-205: one snapshot frame, file order (x outer, y inner).
