@@ -36,11 +36,13 @@ namespace sofi {
 // Programmatic dependent launch. The step's main kernels are launched with
 // programmatic stream serialisation (launch_pdl), so the GPU may schedule one
 // while the previous kernel of the stream is still running. Each such kernel
-// calls pdl_begin() before touching memory: griddepcontrol.wait returns once
+// calls pdl_begin() before touching the wave fields: griddepcontrol.wait returns once
 // the previous kernel has completed and its writes are visible (a no-op after
 // an ordinary launch), then launch_dependents lets the next kernel be
 // scheduled. The launch of one kernel thus overlaps the tail of the last, and
-// no kernel reads or writes anything before its predecessor has finished.
+// no kernel reads or writes a wave field before its predecessor has finished
+// (k_post and k_force_src load acquisition and model arrays, which no kernel
+// writes, before their wait).
 __device__ __forceinline__ void pdl_begin()
 {
     asm volatile("griddepcontrol.wait;" ::: "memory");
