@@ -489,73 +489,118 @@ static __global__ void k_wrap_x(Geo G, float *a, float *b, float *c, int nd)
 
 // --------------------------------------------------------- stress update
 
+// The acquisition of a flagged cell's post work (below), loaded by
+// k_update_s_post before it waits for the velocity kernel: no kernel writes the
+// acquisition arrays. Bit b of smask: source ka + b of the shot is at the cell
+// (a shot has at most 8 sources here); kr: the cell's first receiver (-1:
+// none), then positions rr .. r1 - 1 of the column's receiver list are left
+// to search for more. Set for the cells whose flag has a bit, and read only
+// under that bit.
+struct CellAcq {
+    unsigned smask;
+    int ka, kr, rr, r1;
+};
+
+__device__ __forceinline__ CellAcq cell_acq(const Geo &G, const Acq &A, int s, int i, int j, unsigned flag)
+{
+    CellAcq c{0u, 0, -1, 0, 0};
+    if (flag & 1) {
+        c.ka = A.src_off[s];
+        const int kb = A.src_off[s + 1];
+        for (int k = c.ka; k < kb; k++)
+            if (A.src_ix[k] == i && A.src_iy[k] == j)
+                c.smask |= 1u << (k - c.ka);
+    }
+    if (flag & 2) {
+        const int *roff = A.rec_col_off + (long long)s * (G.nx + 1);
+        int r = roff[i - 1];
+        c.r1 = roff[i];
+        for (; r < c.r1; r++) {
+            const int k = A.rec_col_idx[r];
+            if (A.rec_iy[k] == j) {
+                c.kr = k;
+                break;
+            }
+        }
+        c.rr = r + 1;
+    }
+    return c;
+}
+
+// seismo_ssg.c:28-67 for receiver k at the cell (p after the sources).
+__device__ __forceinline__ void sample_cell(const Geo &G, const Model &M, const Acq &A, int k, int o, long long mo,
+                                            int ins, float nxx, float nyy, float vxo, float vyo, float vxx,
+                                            float vyx, float vxy, float vyy)
+{
+    const int seismo = G.seismo;
+    float *sec = A.sec + (long long)k * 5 * A.ns + (ins - 1);
+    if (seismo == 3 || seismo == 4) {
+        sec[3 * A.ns] = (vxx + vyy) * sqrtf(M.ppi[mo + o]);
+        sec[4 * A.ns] = (vxy - vyx) * sqrtf(M.pu[mo + o]);
+    }
+    if (seismo == 1 || seismo == 4) {
+        sec[0] = vxo;
+        sec[A.ns] = vyo;
+    }
+    if (seismo == 2 || seismo == 4) {
+        float p = -nxx - nyy;
+        if (seismo == 2) {
+            sec[2 * A.ns] = p;
+        } else {
+            float ppi = M.ppi[mo + o], pu = M.pu[mo + o];
+            sec[2 * A.ns] = ((3.0f * ppi - 4.0f * pu) / (2.0f * ppi - 2.0f * pu)) * p / 3.0f;
+        }
+    }
+}
+
 // k_post's work at cell (j, i) of shot s, done by the thread that has just
 // updated and stored its stresses (nxx, nyy in sxx[o], syy[o]) from the
 // CPML-stretched velocity derivatives: psource.c's explosive sources of step
 // nt in source order (time_loop.c:248-253), then the seismograms of
 // seismo_ssg.c:28-67 at the cell's receivers (div / curl from the
 // derivatives, p after the sources) and the NaN probe of time_loop.c:44-47 --
-// what post_column does for the cell, term by term.
-__device__ __forceinline__ void post_cell(const Geo &G, const Wave &W, const Model &M, const Acq &A, int s, int i,
-                                          int j, int o, long long mo, float *sxx, float *syy, float nxx, float nyy,
-                                          float vxx, float vyx, float vxy, float vyy, unsigned flag)
+// what post_column does for the cell, term by term. (vxo, vyo): the cell's
+// velocities, which the stress update has loaded; ca: its acquisition.
+__device__ __forceinline__ void post_cell(const Geo &G, const Model &M, const Acq &A, int s, int i, int j, int o,
+                                          long long mo, float *sxx, float *syy, float nxx, float nyy, float vxo,
+                                          float vyo, float vxx, float vyx, float vxy, float vyy, unsigned flag,
+                                          const CellAcq &ca)
 {
     const bool probe = i == (G.nx / 2 > 0 ? G.nx / 2 : 1) && j == (G.ny / 2 > 0 ? G.ny / 2 : 1);
     if (!flag && !probe)
         return;
     const int nt = *G.step_ctr;  // the velocity kernel of this step advanced it
-    if (flag & 1) {  // the shot's last source is explosive and one source is here
+    // ca is only read under the flag bits (it is not set for other cells)
+    for (unsigned m = (flag & 1) ? ca.smask : 0u; m; m &= m - 1) {  // the shot's last source is explosive
         const int NT = A.nt;
-        for (int k = A.src_off[s]; k < A.src_off[s + 1]; k++) {
-            if (A.src_ix[k] != i || A.src_iy[k] != j)
-                continue;
-            const float *sig = A.signals + (long long)k * NT - 1;  // 1-based
-            float amp = 0.0f;
-            const float d2 = 2.0f * G.dh * G.dh;
-            if (NT >= 2) {
-                if (nt == 1)
-                    amp = sig[2] / d2;
-                else if (nt < NT)
-                    amp = (sig[nt + 1] - sig[nt - 1]) / d2;
-                else
-                    amp = -sig[nt - 1] / d2;
-            }
-            nxx += amp;
-            nyy += amp;
-            sxx[o] = nxx;
-            syy[o] = nyy;
+        const int k = ca.ka + __ffs(m) - 1;
+        const float *sig = A.signals + (long long)k * NT - 1;  // 1-based
+        float amp = 0.0f;
+        const float d2 = 2.0f * G.dh * G.dh;
+        if (NT >= 2) {
+            if (nt == 1)
+                amp = sig[2] / d2;
+            else if (nt < NT)
+                amp = (sig[nt + 1] - sig[nt - 1]) / d2;
+            else
+                amp = -sig[nt - 1] / d2;
         }
+        nxx += amp;
+        nyy += amp;
+        sxx[o] = nxx;
+        syy[o] = nyy;
     }
-    const long long so = (long long)s * G.fsz;
     const int seismo = G.seismo;
     const int ins = (seismo && G.ndt > 0 && nt % G.ndt == 0 && nt < A.nt) ? nt / G.ndt : 0;
-    if ((flag & 2) && ins) {
-        const int *roff = A.rec_col_off + (long long)s * (G.nx + 1);
-        for (int r = roff[i - 1]; r < roff[i]; r++) {
+    if ((flag & 2) && ins && ca.kr >= 0) {
+        sample_cell(G, M, A, ca.kr, o, mo, ins, nxx, nyy, vxo, vyo, vxx, vyx, vxy, vyy);
+        for (int r = ca.rr; r < ca.r1; r++) {
             const int k = A.rec_col_idx[r];
-            if (A.rec_iy[k] != j)
-                continue;
-            float *sec = A.sec + (long long)k * 5 * A.ns + (ins - 1);
-            if (seismo == 3 || seismo == 4) {
-                sec[3 * A.ns] = (vxx + vyy) * sqrtf(M.ppi[mo + o]);
-                sec[4 * A.ns] = (vxy - vyx) * sqrtf(M.pu[mo + o]);
-            }
-            if (seismo == 1 || seismo == 4) {
-                sec[0] = W.vx[so + o];
-                sec[A.ns] = W.vy[so + o];
-            }
-            if (seismo == 2 || seismo == 4) {
-                float p = -nxx - nyy;
-                if (seismo == 2) {
-                    sec[2 * A.ns] = p;
-                } else {
-                    float ppi = M.ppi[mo + o], pu = M.pu[mo + o];
-                    sec[2 * A.ns] = ((3.0f * ppi - 4.0f * pu) / (2.0f * ppi - 2.0f * pu)) * p / 3.0f;
-                }
-            }
+            if (A.rec_iy[k] == j)
+                sample_cell(G, M, A, k, o, mo, ins, nxx, nyy, vxo, vyo, vxx, vyx, vxy, vyy);
         }
     }
-    if (probe && isnan(W.vy[so + o]) && A.status[s] == 0)
+    if (probe && isnan(vyo) && A.status[s] == 0)
         A.status[s] = nt;
 }
 
@@ -566,8 +611,10 @@ __device__ __forceinline__ void post_cell(const Geo &G, const Wave &W, const Mod
 // POST (k_update_s_post): the cell's share of k_post as well -- explosive
 // sources, seismograms, the NaN probe -- for steps without a free surface or
 // moment-tensor sources, so that the step needs no post kernel.
+// POST: pflag and ca are the cell's flags and acquisition (cell_acq).
 template <int ND, int KIND, bool VISCO, int LT, bool POST>
-__device__ __forceinline__ void s_one(const Geo &G, const Wave &W, const Model &M, const Acq &A)
+__device__ __forceinline__ void s_one(const Geo &G, const Wave &W, const Model &M, const Acq &A, unsigned pflag,
+                                      const CellAcq &ca)
 {
     int bx, s;
     block_xs(G, bx, s);
@@ -575,8 +622,6 @@ __device__ __forceinline__ void s_one(const Geo &G, const Wave &W, const Model &
     const int j = blockIdx.y * BY + threadIdx.y + 1;
     if (i > G.nx || j > G.ny)
         return;
-    // POST: the cell's source / receiver flags, loaded with the operands
-    const unsigned pflag = POST ? __ldg(A.cell_flag + ((long long)s * G.ny + (j - 1)) * G.nx + (i - 1)) : 0u;
     const int P = G.pitch;
     const int o = (j - 1 + HY) * P + (i - 1 + HX);
     const long long so = (long long)s * G.fsz, mo = moff(G, s);
@@ -679,7 +724,8 @@ __device__ __forceinline__ void s_one(const Geo &G, const Wave &W, const Model &
     sxx[o] = nxx;
     syy[o] = nyy;
     if (POST)
-        post_cell(G, W, M, A, s, i, j, o, mo, sxx, syy, nxx, nyy, vxx, vyx, vxy, vyy, pflag);
+        post_cell(G, M, A, s, i, j, o, mo, sxx, syy, nxx, nyy, __ldg(vx + o), __ldg(vy + o), vxx, vyx, vxy, vyy,
+                  pflag, ca);
 }
 
 template <int ND, int KIND, bool VISCO, int LT>
@@ -687,14 +733,31 @@ __global__ void __launch_bounds__(BX *BY) k_update_s(Geo G, Wave W, Model M)
 {
     pdl_begin();
     const Acq none{};  // not read without POST
-    s_one<ND, KIND, VISCO, LT, false>(G, W, M, none);
+    s_one<ND, KIND, VISCO, LT, false>(G, W, M, none, 0u, CellAcq{});
 }
 
+// The cell's flags and acquisition load before the wait for the velocity
+// kernel, so that a source's or a receiver's cell, the slowest threads of a
+// launch-bound grid, has fewer dependent memory round trips after it. The
+// acquisition waits in shared memory (a slot per thread), not in registers
+// held across the stress update; at 48 registers (five blocks per SM) the
+// elastic kernels do not spill, and a 400 x 400 grid is still one wave.
 template <int ND, int KIND, bool VISCO, int LT>
-__global__ void __launch_bounds__(BX *BY, 6) k_update_s_post(Geo G, Wave W, Model M, Acq A)
+__global__ void __launch_bounds__(BX *BY, 5) k_update_s_post(Geo G, Wave W, Model M, Acq A)
 {
+    __shared__ CellAcq slot[BX * BY];
+    int bx, s;
+    block_xs(G, bx, s);
+    const int i = bx * BX + threadIdx.x + 1, j = blockIdx.y * BY + threadIdx.y + 1;
+    CellAcq &ca = slot[threadIdx.y * BX + threadIdx.x];
+    unsigned flag = 0;
+    if (i <= G.nx && j <= G.ny) {
+        flag = __ldg(A.cell_flag + ((long long)s * G.ny + (j - 1)) * G.nx + (i - 1));
+        if (flag)
+            ca = cell_acq(G, A, s, i, j, flag);
+    }
     pdl_begin();
-    s_one<ND, KIND, VISCO, LT, true>(G, W, M, A);
+    s_one<ND, KIND, VISCO, LT, true>(G, W, M, A, flag, ca);
 }
 
 // The stress update with VW adjacent cells per thread (VW = 2 or 4), the

@@ -92,3 +92,35 @@ def test_fused_post_batched_shots(monkeypatch):
         for c in out["0"][s]:
             np.testing.assert_array_equal(out["1"][s][c], out["0"][s][c], err_msg=f"shot {s} {c}")
     o.close()
+
+
+@pytest.mark.parametrize("seismo", [1, 4])
+def test_fused_post_receivers_sharing_columns(seismo, monkeypatch):
+    """Receivers down two columns (a cell's receiver found after others of its
+    column in the column's list), two receivers on one cell, and a source on a
+    receiver's cell: the fused post work equals the post kernel bit for bit."""
+    from oracle import oracle as O
+    case = dict(case_by_name("el_cpml_fd8"), seismo=seismo)
+    o = run_oracle_case(case, nthreads=os.cpu_count() or 1, nsteps=1)
+    cfg = o.cfg
+    sp = case_sources(case, cfg)
+    si, sj = int(sp[0, 0]), int(sp[1, 0])  # the source's cell
+    col = cfg.nx // 3
+    ix = [col] * 8 + [col + 5] * 4 + [col, si, 30, 31, 32]
+    iy = [25 + 6 * k for k in range(8)] + [60 - 9 * k for k in range(4)] + [25 + 6 * 3, sj, 40, 40, 40]
+    ix, iy = np.array(ix, np.int32), np.array(iy, np.int32)
+    sig = O.wavelet(1, cfg.nt, cfg.dt, sp)
+    out = {}
+    for postf in ("1", "0"):
+        monkeypatch.setenv("SOFI_SW", "0")
+        monkeypatch.setenv("SOFI_POSTF", postf)
+        t = gpu_run_like(o, cfg, sp, sig, ix, iy)
+        assert t.post_fused() == (postf == "1")
+        out[postf] = {c: t.section(c) for c in COMPS}
+        out[postf]["sxx"] = t.field("sxx")
+        t.close()
+    for c in out["0"]:
+        np.testing.assert_array_equal(out["1"][c], out["0"][c], err_msg=f"seismo {seismo} {c}")
+    assert np.abs(out["1"]["vx"][8]).max() > 0  # the column's receivers recorded the wave
+    np.testing.assert_array_equal(out["1"]["vx"][3], out["1"]["vx"][12])  # one cell, two receivers
+    o.close()
