@@ -49,6 +49,33 @@ __device__ __forceinline__ void pdl_begin()
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// A source's signal samples c0 - 1 .. c0 + 2 (1-based, 0 outside 1 .. NT),
+// loaded before griddepcontrol.wait, where c0 is the step counter read there:
+// the velocity kernel of the step may be advancing it, so c0 is this step or
+// the one before, and the samples a step's injection needs are then in the
+// window. at() takes a sample from the window where its index lies in it and
+// loads it otherwise, so the result does not depend on the value read.
+struct SigWindow {
+    int c0;
+    float w[4];
+    __device__ __forceinline__ void load(const int *step_ctr, const float *sig, int NT)
+    {
+        asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(c0) : "l"(step_ctr));
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int n = c0 - 1 + q;
+            w[q] = (n >= 1 && n <= NT) ? sig[n] : 0.f;
+        }
+    }
+    __device__ __forceinline__ float at(const float *sig, int n) const
+    {
+        const int q = n - c0 + 1;  // selected, not indexed: w stays in registers
+        if (q < 0 || q > 3)
+            return sig[n];
+        return q == 0 ? w[0] : (q == 1 ? w[1] : (q == 2 ? w[2] : w[3]));
+    }
+};
+
 // Whether launch_pdl uses programmatic serialisation on this host thread; the
 // context whose step is being launched sets it (off: ordinary launches of the
 // same kernels).

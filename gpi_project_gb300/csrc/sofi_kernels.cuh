@@ -499,6 +499,7 @@ static __global__ void k_wrap_x(Geo G, float *a, float *b, float *c, int nd)
 struct CellAcq {
     unsigned smask;
     int ka, kr, rr, r1;
+    SigWindow sw;  // the cell's first source's signal around this step
 };
 
 __device__ __forceinline__ CellAcq cell_acq(const Geo &G, const Acq &A, int s, int i, int j, unsigned flag)
@@ -510,6 +511,8 @@ __device__ __forceinline__ CellAcq cell_acq(const Geo &G, const Acq &A, int s, i
         for (int k = c.ka; k < kb; k++)
             if (A.src_ix[k] == i && A.src_iy[k] == j)
                 c.smask |= 1u << (k - c.ka);
+        if (c.smask)
+            c.sw.load(G.step_ctr, A.signals + (long long)(c.ka + __ffs(c.smask) - 1) * A.nt - 1, A.nt);
     }
     if (flag & 2) {
         const int *roff = A.rec_col_off + (long long)s * (G.nx + 1);
@@ -575,15 +578,18 @@ __device__ __forceinline__ void post_cell(const Geo &G, const Model &M, const Ac
         const int NT = A.nt;
         const int k = ca.ka + __ffs(m) - 1;
         const float *sig = A.signals + (long long)k * NT - 1;  // 1-based
+        // the first source's samples from the window loaded before the wait
+        const bool first = m == ca.smask;
+        auto sg = [&](int n) { return first ? ca.sw.at(sig, n) : sig[n]; };
         float amp = 0.0f;
         const float d2 = 2.0f * G.dh * G.dh;
         if (NT >= 2) {
             if (nt == 1)
-                amp = sig[2] / d2;
+                amp = sg(2) / d2;
             else if (nt < NT)
-                amp = (sig[nt + 1] - sig[nt - 1]) / d2;
+                amp = (sg(nt + 1) - sg(nt - 1)) / d2;
             else
-                amp = -sig[nt - 1] / d2;
+                amp = -sg(nt - 1) / d2;
         }
         nxx += amp;
         nyy += amp;
@@ -1683,9 +1689,12 @@ __global__ void __launch_bounds__(BX *BY, VISCO ? 2 : 4) k_tti_tiles(Geo G, Wave
 // lt, ka, kb: the shot's last source type and source range (A.last_type[s],
 // A.src_off[s], A.src_off[s + 1]), loaded by the caller with its other
 // independent loads.
-// (si0, sj0): the first source's cell (k = ka), loaded by the caller too.
+// (si0, sj0): the first source's cell (k = ka), loaded by the caller too; sw:
+// its signal around this step (SigWindow), with (sx0, sy0) the stresses at
+// its cell as the stress update left them, loaded with the step number.
 __device__ __forceinline__ void post_sources(const Geo &G, const Wave &W, const Acq &A, int s, int i, int nt, int lt,
-                                             int ka, int kb, int si0, int sj0)
+                                             int ka, int kb, int si0, int sj0, const SigWindow &sw, float sx0,
+                                             float sy0)
 {
     if (lt != 1 && lt != 5)
         return;
@@ -1698,6 +1707,7 @@ __device__ __forceinline__ void post_sources(const Geo &G, const Wave &W, const 
             continue;
         const float *sig = A.signals + (long long)k * NT - 1;  // 1-based: sig[1..NT]
         const long long o = cell(G, sj, si);
+        auto sg = [&](int n) { return k == ka ? sw.at(sig, n) : sig[n]; };
         if (lt == 1) {
             // central difference of the signal (psource.c:41-49); a one-step
             // run has no neighbouring sample and injects nothing
@@ -1705,16 +1715,21 @@ __device__ __forceinline__ void post_sources(const Geo &G, const Wave &W, const 
             const float d2 = 2.0f * G.dh * G.dh;
             if (NT >= 2) {
                 if (nt == 1)
-                    amp = sig[2] / d2;
+                    amp = sg(2) / d2;
                 else if (nt < NT)
-                    amp = (sig[nt + 1] - sig[nt - 1]) / d2;
+                    amp = (sg(nt + 1) - sg(nt - 1)) / d2;
                 else
-                    amp = -sig[nt - 1] / d2;
+                    amp = -sg(nt - 1) / d2;
             }
-            sxx[o] += amp;
-            syy[o] += amp;
+            if (k == ka) {  // acoustic: sxx and syy are one array, which takes amp twice
+                sxx[o] = sx0 + amp;
+                syy[o] = (syy == sxx ? sx0 + amp : sy0) + amp;
+            } else {
+                sxx[o] += amp;
+                syy[o] += amp;
+            }
         } else {
-            const float amp = A.src_amp[k] * (G.dt / (G.dh * G.dh)) * sig[nt];
+            const float amp = A.src_amp[k] * (G.dt / (G.dh * G.dh)) * sg(nt);
             const float m11 = -A.src_sin2[k], m12 = -A.src_cos2[k], m22 = A.src_sin2[k];
             if (si == i) {
                 sxx[o] += amp * m11;
@@ -1886,6 +1901,7 @@ __device__ __forceinline__ void sample_v_p(const Geo &G, const Wave &W, const Mo
 struct PostCol {
     int lt, ka, kb, si0, sj0, r0, r1, k0;
     long long o0;
+    SigWindow sw;  // the first source's signal around this step, where this column injects it
 };
 
 __device__ __forceinline__ PostCol post_acq(const Geo &G, const Acq &A, int i, int s)
@@ -1896,8 +1912,11 @@ __device__ __forceinline__ PostCol post_acq(const Geo &G, const Acq &A, int i, i
     p.r0 = roff ? roff[i - 1] : 0, p.r1 = roff ? roff[i] : 0;
     p.si0 = p.sj0 = p.k0 = 0;
     p.o0 = 0;
-    if (p.ka < p.kb)
+    if (p.ka < p.kb) {
         p.si0 = A.src_ix[p.ka], p.sj0 = A.src_iy[p.ka];
+        if ((p.lt == 1 || p.lt == 5) && (p.si0 == i || (p.lt == 5 && p.si0 - 1 == i)))
+            p.sw.load(G.step_ctr, A.signals + (long long)p.ka * A.nt - 1, A.nt);
+    }
     if (p.r0 < p.r1) {
         p.k0 = A.rec_col_idx[p.r0];
         p.o0 = cell(G, A.rec_iy[p.k0], A.rec_ix[p.k0]);
@@ -1923,13 +1942,17 @@ __device__ __forceinline__ void post_column(const Geo &G, Wave W, const Model &M
     const int r0 = pc.r0, r1 = pc.r1;
     // the column's first receiver's velocities, loaded ahead of the stores below
     const long long so = (long long)s * G.fsz;
-    float vx0 = 0.f, vy0 = 0.f;
+    float vx0 = 0.f, vy0 = 0.f, sx0 = 0.f, sy0 = 0.f;
     if (r0 < r1)
         vx0 = W.vx[so + pc.o0], vy0 = W.vy[so + pc.o0];
+    if (pc.lt == 1 && pc.ka < pc.kb && pc.si0 == i) {  // the first source's cell, before any injection
+        const long long o = so + cell(G, pc.sj0, pc.si0);
+        sx0 = W.sxx[o], sy0 = W.syy[o];
+    }
     if (ins && (seismo == 3 || seismo == 4))
         for (int r = r0; r < r1; r++)
             sample_div_curl<ND, TTIK>(G, W, M, A, s, A.rec_col_idx[r], ins);
-    post_sources(G, W, A, s, i, nt, pc.lt, pc.ka, pc.kb, pc.si0, pc.sj0);
+    post_sources(G, W, A, s, i, nt, pc.lt, pc.ka, pc.kb, pc.si0, pc.sj0, pc.sw, sx0, sy0);
     if (G.free_surf)
         post_surface<ND, VISCO>(G, W, M, s, i);
     if (i == (G.nx / 2 > 0 ? G.nx / 2 : 1)) {
