@@ -9,21 +9,25 @@ namespace sofi {
 // update_v_interior.c:49-71. Runs before the velocity kernel advances the
 // step counter, so the step being computed is counter + 1. The sources and
 // the model do not change during a run: the shot's source range, its first
-// source's type and cell and the buoyancy there load before the wait for the
-// previous kernel, the step number and the velocities after it. (static: the
-// header is included by several translation units; only sofigpu.cu launches it)
+// source's type and cell, the buoyancy there and its signal around the step
+// (SigWindow) load before the wait for the previous kernel, the step number
+// and the velocities after it. (static: the header is included by several
+// translation units; only sofigpu.cu launches it)
 __device__ __forceinline__ void force_shot(const Geo &G, const Wave &W, const Model &M, const Acq &A, int s, bool live)
 {
     const float *prip = M.prip + moff(G, s), *prjp = M.prjp + moff(G, s);
     int ka = 0, kb = 0, t0 = 0;
     long long o0 = 0;
     float rx0 = 0.f, ry0 = 0.f;
+    SigWindow sw{};
     if (live) {
         ka = A.src_off[s], kb = A.src_off[s + 1];
         if (ka < kb) {
             t0 = A.src_type[ka];
             o0 = cell(G, A.src_iy[ka], A.src_ix[ka]);
             rx0 = prip[o0], ry0 = prjp[o0];
+            if (t0 >= 2 && t0 <= 4)
+                sw.load(G.step_ctr, A.signals + (long long)ka * A.nt - 1, A.nt);
         }
     }
     pdl_begin();
@@ -37,7 +41,8 @@ __device__ __forceinline__ void force_shot(const Geo &G, const Wave &W, const Mo
             continue;
         const long long o = k == ka ? o0 : cell(G, A.src_iy[k], A.src_ix[k]);
         const float rx = k == ka ? rx0 : prip[o], ry = k == ka ? ry0 : prjp[o];
-        float amp = (G.dt * A.signals[(long long)k * A.nt + (nt - 1)]) / (G.dh * G.dh);
+        const float *sig = A.signals + (long long)k * A.nt - 1;  // 1-based
+        float amp = (G.dt * (k == ka ? sw.at(sig, nt) : sig[nt])) / (G.dh * G.dh);
         if (t == 2)
             vx[o] += rx * amp;
         else if (t == 3)
