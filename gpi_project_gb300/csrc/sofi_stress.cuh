@@ -27,9 +27,9 @@ void stress_w(const Geo &G, const Wave &W, const Model &M, int nd, bool narrow, 
             }
             return;
         }
-    if constexpr (KIND == ISO && !VISCO && VW == 4)
+    if constexpr (KIND == ISO && !VISCO)
         if (W.fa_x) {  // a step of an FWI forward run
-            DISPATCH_ND(nd, (launch_pdl(k_update_sw<ND, ISO, false, 0, 4, true>, grd, blk, 0, st, G, W, M)))
+            DISPATCH_ND(nd, (launch_pdl(k_update_sw<ND, ISO, false, 0, VW, true>, grd, blk, 0, st, G, W, M)))
             return;
         }
     if constexpr (!VISCO) {
@@ -56,6 +56,11 @@ void launch_stress_kv(const Geo &G, const Wave &W, const Model &M, int nd, int s
         return stress_w<KIND, VISCO, 2>(G, W, M, nd, false, grd, st);
     const dim3 blk(BX, BY);
     [[maybe_unused]] const int L = VISCO ? G.L : 0;
+    if constexpr (KIND == ISO && !VISCO)
+        if (W.fa_x) {  // a step of an FWI forward run, one cell per thread
+            DISPATCH_ND(nd, (launch_pdl(k_update_sw<ND, ISO, false, 0, 1, true>, grd, blk, 0, st, G, W, M)))
+            return;
+        }
     if (post) {  // one cell per thread with k_post's work (k_update_s_post)
         const Acq &A = *post;
         if constexpr (!VISCO) {

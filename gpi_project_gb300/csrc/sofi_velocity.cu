@@ -22,9 +22,16 @@ void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw
             DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 1, false>, gv, blk, 0, st, G, W, M)))
         return;
     }
-    if (vw == 4 && W.fa_x)  // a step of an FWI forward run
-        DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 4, true, true>, gv, blk, 0, st, G, W, M)))
-    else if (vw == 4)
+    if (W.fa_x) {  // a step of an FWI forward run: 4, 2 or 1 cells per thread (vrows is 1 then)
+        if (vw == 4)
+            DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 4, true, true>, gv, blk, 0, st, G, W, M)))
+        else if (vw == 2)
+            DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 2, true, true>, gv, blk, 0, st, G, W, M)))
+        else
+            DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 1, true, true>, gv, blk, 0, st, G, W, M)))
+        return;
+    }
+    if (vw == 4)
         DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 4>, gv, blk, 0, st, G, W, M)))
     else if (vw == 2)
         DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 2>, gv, blk, 0, st, G, W, M)))

@@ -188,6 +188,7 @@ struct sofi_ctx {
     bool run_pending = false;  // ev0/ev1 recorded by a sofi_run not yet synchronised
     int vw = 4;                // velocity kernel: cells per thread in x (4 or 2), 0 = vrows rows per thread
     int vrows = 1;             // rows per thread of the one-cell velocity kernel (1, 2 or 4)
+    int fwi_vw = 4, fwi_sw = 4; // an FWI pass's forward steps: cells per thread of the FWI kernels
     // FWI gradient pass of one shot (sofi_fwi_*; sofi_fwi.cu)
     bool fwi = false;          // the forward runs store the gradient quantities
     bool fwi_back = false;     // the backward run is being issued
@@ -1397,9 +1398,23 @@ int sofi_run(sofi_ctx *c, int nsteps)
             return rc;
     }
     if (!c->tuned && c->step == 0 && nsteps > 0) {
+        // an FWI pass's forward run tunes the plain kernels (step_wave drops
+        // the gradient quantities while fwi_back is set), then runs the FWI
+        // instantiations of the winners: 4, 2 or 1 cells per thread on wide blocks
+        const bool fb = c->fwi_back;
+        if (c->fwi)
+            c->fwi_back = true;
         int rc = autotune(c);
+        c->fwi_back = fb;
         if (rc)
             return rc;
+        if (c->fwi && !c->fwi_back) {
+            if (c->vw == 0)
+                c->vrows = 1;
+            c->vnarrow = c->snarrow = false;
+            c->fwi_vw = c->vw, c->fwi_sw = c->sw;
+            c->graph_dirty = true;
+        }
     }
     c->pristine = false;
     CK(cudaEventRecord(c->ev0, c->stream));
@@ -1664,9 +1679,17 @@ int sofi_fwi_begin(sofi_ctx *c, int velocity, int adjoint_type, const float *vp,
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->stream));
     c->F.nt = cf.nt, c->F.velocity = velocity, c->F.adjoint = adjoint_type;
-    // the kernels whose bodies write the gradient quantities, fixed for the pass
-    c->vw = 4, c->vrows = 1, c->sw = 4, c->tuned = true;
+    // the forward steps run the kernels whose bodies write the gradient
+    // quantities, in the variant the autotuner picks for plain steps of this
+    // grid at the pass's first sofi_run (four cells per thread until then;
+    // SOFI_VROWS / SOFI_SW keep the variant they fix)
+    if (!c->tune_fixed)
+        c->vw = 4, c->vrows = 1;
+    if (!c->sw_fixed)
+        c->sw = 4;
+    c->tuned = false;
     c->vnarrow = c->snarrow = false;
+    c->fwi_vw = c->vw, c->fwi_sw = c->sw;
     c->fwi = true, c->fwi_back = false, c->graph_dirty = true;
     return 0;
 }
@@ -1728,8 +1751,8 @@ int sofi_fwi_backward(sofi_ctx *c, const float *adj_x, const float *adj_y)
         return rc;
     // The backward steps write no gradient quantities: they run the variants
     // the autotuner picks for plain steps of this grid (timed now, on the
-    // zeroed state, or taken from the cache); forward and recomputed steps
-    // keep the four-cell FWI kernels.
+    // zeroed state, or taken from the cache); recomputed forward steps run the
+    // FWI kernels of the first forward run (fwi_vw, fwi_sw).
     c->fwi_back = true, c->tuned = false;
     rc = autotune(c);
     const int bvw = c->vw, bvrows = c->vrows, bsw = c->sw;
@@ -1748,7 +1771,7 @@ int sofi_fwi_backward(sofi_ctx *c, const float *adj_x, const float *adj_y)
             c->vw = bvw, c->vrows = bvrows, c->sw = bsw, c->vnarrow = bvnarrow, c->snarrow = bsnarrow;
         } else {
             c->A = saved, c->has_force = saved_force;
-            c->vw = 4, c->vrows = 1, c->sw = 4, c->vnarrow = c->snarrow = false;
+            c->vw = c->fwi_vw, c->vrows = 1, c->sw = c->fwi_sw, c->vnarrow = c->snarrow = false;
         }
         c->fwi_back = on, c->graph_dirty = true;
     };

@@ -20,7 +20,7 @@ L2_TOL, MAX_TOL = 1e-4, 1e-3
 GRAD_L2, GRAD_MAX = 1e-3, 1e-2
 
 
-def gpu_fwi(case, obs_vx, obs_vy):
+def gpu_fwi(case, obs_vx, obs_vy, variants=None):
     from oracle import oracle as O
     from gpi_project_gb300 import TimeLoop
     from gpi_project_gb300 import host as H
@@ -40,6 +40,8 @@ def gpu_fwi(case, obs_vx, obs_vy):
     t.fwi_begin(*model, velocity=case["velocity"], adjoint_type=case["adjoint_type"])
     t.reset()
     t.run()
+    if variants is not None:  # what the forward steps ran
+        variants.append((t.velocity_variant(), t.stress_variant()))
     fwd = {"vx": t.section("vx"), "vy": t.section("vy")}
     rx, _ = H.fwi_residual(fwd["vx"], obs_vx, case["velocity"], cfg.dt)
     ry, _ = H.fwi_residual(fwd["vy"], obs_vy, case["velocity"], cfg.dt)
@@ -63,6 +65,32 @@ def test_gpu_fwi_gradient_matches_compiled_reference(case):
         e2, em = rel_l2(grads[k], ref), rel_max(grads[k], ref)
         print(case["name"], k, "rel L2", e2, "rel max", em)
         assert e2 <= GRAD_L2 and em <= GRAD_MAX, (case["name"], k, e2, em)
+
+
+FWD_VARIANTS = [("w4", "4", (4, 1), 4), ("w2", "2", (2, 1), 2), ("1", "0", (1, 1), 1), ("2", "4", (1, 1), 4)]
+
+
+@pytest.mark.parametrize("vrows,sw,v_used,s_used", FWD_VARIANTS, ids=[f"v{v[0]}-s{v[1]}" for v in FWD_VARIANTS])
+@pytest.mark.parametrize("case", FWI_CASES, ids=[c["name"] for c in FWI_CASES])
+def test_gpu_fwi_forward_variants_match_compiled_reference(case, vrows, sw, v_used, s_used, monkeypatch):
+    """The forward steps run the FWI instantiations of the variant the
+    autotuner picks for plain steps of the grid: four, two or one cell per
+    thread in each update (rows per thread of the one-cell velocity kernel
+    become one). Each, fixed by SOFI_VROWS / SOFI_SW, gives seismograms and
+    gradients within the bar of the compiled reference's."""
+    monkeypatch.setenv("SOFI_VROWS", vrows)
+    monkeypatch.setenv("SOFI_SW", sw)
+    g = np.load(os.path.join(HERE, "golden", f"ref_{case['name']}.npz"))
+    used = []
+    fwd, grads = gpu_fwi(case, g["obs_vx"], g["obs_vy"], used)
+    assert used[0] == (v_used, s_used), used
+    for c in ("vx", "vy"):
+        ref = g[f"fwd_{c}"]
+        assert rel_l2(fwd[c], ref) <= L2_TOL and rel_max(fwd[c], ref) <= MAX_TOL, (case["name"], c)
+    for k in ("vp", "vs", "rho"):
+        ref = g[f"grad_{k}"]
+        e2, em = rel_l2(grads[k], ref), rel_max(grads[k], ref)
+        assert e2 <= GRAD_L2 and em <= GRAD_MAX, (case["name"], vrows, sw, k, e2, em)
 
 
 def test_gpu_fwi_rejects_unsupported(monkeypatch):
