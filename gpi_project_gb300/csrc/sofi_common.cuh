@@ -169,7 +169,8 @@ struct FwiDev {
     double *rc;                     // [3][NY][NX]: 1 / (4 (lam+mu)^2), 1 / mu^2, 1 / (lam+mu)^2 (calc_conv.c)
     const float *adj;               // [2][ntr][NT] adjoint signals (x, y)
     const int *cell_off, *cell_rec; // receivers by cell: cell k holds cell_rec[cell_off[k] .. cell_off[k+1])
-    const int *cell_ix, *cell_iy;
+    const int *cell_map;            // [NY][NX]: k + 1 at receiver cell k, else 0
+    int *bstep;                     // device: the backward step last completed (k_fwi_conv writes it)
     int ncell, ntr, nt, velocity, adjoint;
 };
 

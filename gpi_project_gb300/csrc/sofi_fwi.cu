@@ -10,11 +10,13 @@
 // the stress kernel then fills the whole slot (those two and its own u / DT),
 // with VELOCITY = 0 k_fwi_store copies them and the stresses after the free
 // surface.
-// Backward, per step: k_fwi_adj adds the adjoint signals at the receivers
-// before the velocity update; k_fwi_rho forms the reference's pvxp1 / pvyp1
-// (the injected velocity, or its running sum times DT for VELOCITY = 0) and
-// adds the density term; after the stress update and the free surface
-// k_fwi_conv adds the lambda and mu terms against forward slot NT - nt + 1.
+// Backward, per step: the velocity kernel (k_update_vw_bwd) adds the adjoint
+// signals at the receivers before its update, forms the reference's pvxp1 /
+// pvyp1 (the injected velocity, or its running sum times DT for VELOCITY =
+// 0) and adds the density term; after the stress update and the free surface
+// k_fwi_conv adds the lambda and mu terms against forward slot NT - nt + 1
+// and records the step it completed (FwiDev::bstep) for the next velocity
+// kernel, which advances the step counter while its blocks run.
 // Every kernel takes the step number from the device counter, so the steps
 // replay from the captured graph like the plain ones; the per-step kernels
 // are launched as programmatic dependents (pdl_begin) like the step's own.
@@ -38,48 +40,6 @@ __global__ void k_fwi_store(Geo G, Wave W, FwiDev F)
     slot[0] = W.fa_x[o];
     slot[n] = W.fa_y[o];
     slot[2 * n] = W.sxx[o], slot[3 * n] = W.syy[o], slot[4 * n] = W.sxy[o];
-}
-
-// One thread per receiver cell; a cell's receivers in the reference's order.
-__global__ void k_fwi_adj(Geo G, Wave W, FwiDev F)
-{
-    pdl_begin();
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= F.ncell)
-        return;
-    const int nt = *G.step_ctr + 1;  // before the velocity kernel advances it
-    const long long o = cell(G, F.cell_iy[k], F.cell_ix[k]);
-    float vx = W.vx[o], vy = W.vy[o];
-    for (int r = F.cell_off[k]; r < F.cell_off[k + 1]; r++) {
-        const int l = F.cell_rec[r];
-        if (F.adjoint == 1 || F.adjoint == 3)
-            vx += F.adj[(long long)l * F.nt + (nt - 1)];
-        if (F.adjoint == 1 || F.adjoint == 2)
-            vy += F.adj[((long long)F.ntr + l) * F.nt + (nt - 1)];
-    }
-    W.vx[o] = vx, W.vy[o] = vy;
-}
-
-__global__ void k_fwi_rho(Geo G, Wave W, FwiDev F)
-{
-    pdl_begin();
-    const long long n = (long long)G.nx * G.ny;
-    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n)
-        return;
-    const int nt = *G.step_ctr + 1;
-    const int j = (int)(q / G.nx) + 1, i = (int)(q % G.nx) + 1;
-    const long long o = cell(G, j, i);
-    float px = W.vx[o], py = W.vy[o];
-    if (!F.velocity) {  // wavefield_update_v.c:37-39
-        px = __fadd_rn(F.px[q], __fmul_rn(px, G.dt));
-        py = __fadd_rn(F.py[q], __fmul_rn(py, G.dt));
-        F.px[q] = px, F.py[q] = py;
-    }
-    const float *slot = F.store + (long long)(F.nt - nt - *F.base) * 5 * n + q;
-    // each product and sum rounded on its own, as the reference evaluates it
-    const float t = __fadd_rn(__fmul_rn(px, slot[0]), __fmul_rn(py, slot[n]));
-    F.g_rhos[q] = __fadd_rn(F.g_rhos[q], __fmul_rn(-G.dt, t));
 }
 
 // The model-only divisors of calc_conv.c:42-67, once per pass: muss / lamss
@@ -109,9 +69,11 @@ __global__ void k_fwi_conv(Geo G, Wave W, Model M, FwiDev F)
     pdl_begin();
     const long long n = (long long)G.nx * G.ny;
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int nt = *G.step_ctr;
+    if (q == 0)
+        *F.bstep = nt;
     if (q >= n)
         return;
-    const int nt = *G.step_ctr;
     const int j = (int)(q / G.nx) + 1, i = (int)(q % G.nx) + 1;
     const long long o = cell(G, j, i);
     const float *slot = F.store + (long long)(F.nt - nt - *F.base) * 5 * n + q;
@@ -138,14 +100,6 @@ void launch_fwi_store(const Geo &G, const Wave &W, const FwiDev &F, cudaStream_t
 {
     const long long n = (long long)G.nx * G.ny;
     launch_pdl(k_fwi_store, (unsigned)((n + 255) / 256), 256, 0, st, G, W, F);
-}
-
-void launch_fwi_backward_pre(const Geo &G, const Wave &W, const FwiDev &F, cudaStream_t st)
-{
-    const long long n = (long long)G.nx * G.ny;
-    if (F.ncell)
-        launch_pdl(k_fwi_adj, (unsigned)((F.ncell + 127) / 128), 128, 0, st, G, W, F);
-    launch_pdl(k_fwi_rho, (unsigned)((n + 255) / 256), 256, 0, st, G, W, F);
 }
 
 void launch_fwi_conv(const Geo &G, const Wave &W, const Model &M, const FwiDev &F, cudaStream_t st)

@@ -322,6 +322,46 @@ __device__ __forceinline__ void v_finish(const Geo &G, const Wave &W, const Mode
     }
 }
 
+// A backward step of an FWI pass, before the velocity update of VW adjacent
+// cells (columns i .., row j; ox / oy their velocities): the adjoint signals
+// of the receivers at a cell in the reference's order (update_v_interior.c:
+// 72-90, adjoint type 1-3), then pvxp1 / pvyp1 (wavefield_update_v.c:36-41:
+// the injected velocity, or with VELOCITY = 0 its running sum times DT) and
+// the density term of calc_conv.c:49-51 against forward slot NT - nt + 1.
+// Each product and sum is rounded on its own, as the reference evaluates
+// them. The step number comes from FwiDev::bstep, which the previous step's
+// correlation kernel wrote: this kernel advances the step counter itself.
+template <int VW>
+__device__ __forceinline__ void bwd_cells(const Geo &G, const FwiDev &F, int i, int j, float *ox, float *oy)
+{
+    const int nt = *F.bstep + 1;
+    const long long n = (long long)G.nx * G.ny;
+    const float *slot = F.store + (long long)(F.nt - nt - *F.base) * 5 * n;
+#pragma unroll
+    for (int c = 0; c < VW; c++) {
+        if (i + c > G.nx)
+            continue;
+        const long long q = (long long)(j - 1) * G.nx + (i + c - 1);
+        const int k = F.cell_map[q] - 1;
+        if (k >= 0)
+            for (int r = F.cell_off[k]; r < F.cell_off[k + 1]; r++) {
+                const int l = F.cell_rec[r];
+                if (F.adjoint == 1 || F.adjoint == 3)
+                    ox[c] += F.adj[(long long)l * F.nt + (nt - 1)];
+                if (F.adjoint == 1 || F.adjoint == 2)
+                    oy[c] += F.adj[((long long)F.ntr + l) * F.nt + (nt - 1)];
+            }
+        float px = ox[c], py = oy[c];
+        if (!F.velocity) {
+            px = __fadd_rn(F.px[q], __fmul_rn(px, G.dt));
+            py = __fadd_rn(F.py[q], __fmul_rn(py, G.dt));
+            F.px[q] = px, F.py[q] = py;
+        }
+        const float t = __fadd_rn(__fmul_rn(px, slot[q]), __fmul_rn(py, slot[n + q]));
+        F.g_rhos[q] = __fadd_rn(F.g_rhos[q], __fmul_rn(-G.dt, t));
+    }
+}
+
 // The stress derivatives of VW adjacent cells for the velocity update
 // (op_v_fdN, initfd.c:97-183, unscaled): ld(f, dy, dx, out) loads VW values
 // of sxx (f = 0), sxy (1) or syy (2) at row j + dy, columns i + dx ..
@@ -387,8 +427,9 @@ __device__ __forceinline__ void v_derivs(const Geo &G, LD ld, float *sxx_x, floa
 // TBX: threads of a block in x (BX, or 8 for narrow grids: 32 columns by 32
 // rows per block of four-cell threads, so a 400-cell row leaves 4 % of the
 // last block idle instead of 22 %).
-template <int ND, int VW, bool SXY, bool FWI = false, int TBX = BX>
-__device__ __forceinline__ void vw_tile(const Geo &G, const Wave &W, const Model &M, const uint3 b)
+template <int ND, int VW, bool SXY, bool FWI = false, int TBX = BX, bool BWD = false>
+__device__ __forceinline__ void vw_tile(const Geo &G, const Wave &W, const Model &M, const uint3 b,
+                                        const FwiDev *F = nullptr)
 {
     constexpr int K = (ND + VW - 1) / VW;
     constexpr int NXS = VW * (2 * K + 1);  // stencil row: columns i - VW K .. i + VW K + VW - 1
@@ -459,6 +500,8 @@ __device__ __forceinline__ void vw_tile(const Geo &G, const Wave &W, const Model
     float ox[VW], oy[VW], rp[VW], rq[VW];
     ldv_rw_once<VW>(vx + o, ox), ldv_rw_once<VW>(vy + o, oy);
     ldv_once<VW>(M.prip + mo + o, rp), ldv_once<VW>(M.prjp + mo + o, rq);
+    if constexpr (BWD)
+        bwd_cells<VW>(G, *F, i, j, ox, oy);
     v_finish<VW, SXY, FWI>(G, W, M, s, i, j, o, mo, vx, vy, ox, oy, rp, rq, sxx_x, sxy_x, sxy_y, syy_y);
 }
 
@@ -470,6 +513,16 @@ __global__ void __launch_bounds__(BX *BY, VW == 4 ? 4 : 1) k_update_vw(Geo G, Wa
 {
     pdl_begin();
     vw_tile<ND, VW, SXY, FWI, TBX>(G, W, M, blockIdx);
+}
+
+// A backward step of an FWI pass: the adjoint injection and the density term
+// (bwd_cells) in the velocity kernel, VW = 4, 2 or 1 cells per thread; the
+// four-cell form at three blocks per SM (at four it spills 36 bytes)
+template <int ND, int VW>
+__global__ void __launch_bounds__(BX *BY, VW == 4 ? 3 : 1) k_update_vw_bwd(Geo G, Wave W, Model M, FwiDev F)
+{
+    pdl_begin();
+    vw_tile<ND, VW, true, false, BX, true>(G, W, M, blockIdx, &F);
 }
 
 // Periodic x (BOUNDARY = 1): ghost columns copy the opposite edge, as the one-

@@ -9,18 +9,19 @@ struct Wave;
 struct Model;
 struct Acq;
 struct FwiDev;
-// FWI gradient pass (sofi_fwi.cu): forward storage after a step; adjoint
-// injection and the density term before the velocity update; the lambda /
-// mu terms after the post kernel
+// FWI gradient pass (sofi_fwi.cu): forward storage after a step; the lambda /
+// mu terms after the post kernel (the adjoint injection and the density term
+// are part of the backward steps' velocity kernel)
 void launch_fwi_coef(int n, const FwiDev &F, cudaStream_t st);  // the model-only divisors, once per pass
 void launch_fwi_store(const Geo &G, const Wave &W, const FwiDev &F, cudaStream_t st);
-void launch_fwi_backward_pre(const Geo &G, const Wave &W, const FwiDev &F, cudaStream_t st);
 void launch_fwi_conv(const Geo &G, const Wave &W, const Model &M, const FwiDev &F, cudaStream_t st);
 // velocity update: vw cells per thread in x (4 or 2), else vrows rows per thread (1, 2, 4);
 // narrow (vw 4, not acoustic): blocks of 8 x 32 threads, 32 columns by 32 rows (grid sized for that);
-// acoustic: no sxy terms, vw 4, 2 or else one cell per thread
+// acoustic: no sxy terms, vw 4, 2 or else one cell per thread;
+// bwd (a backward step of an FWI pass): also the adjoint injection and the
+// density term, vw 4, 2 or else one cell per thread, wide blocks
 void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw, int vrows, bool narrow, bool acoustic,
-                     dim3 grid, cudaStream_t st);
+                     dim3 grid, cudaStream_t st, const FwiDev *bwd = nullptr);
 // Where the narrow four-cell blocks (8 x 32 threads, 32 columns by 32 rows)
 // exist: the velocity update of non-acoustic media and the ISO / VTI stress
 // update of elastic media or L <= 3, neither on an FWI forward step. The

@@ -6,9 +6,19 @@
 namespace sofi {
 
 void launch_velocity(const Geo &G, const Wave &W, const Model &M, int nd, int vw, int vrows, bool narrow, bool acoustic,
-                     dim3 gv, cudaStream_t st)
+                     dim3 gv, cudaStream_t st, const FwiDev *bwd)
 {
     const dim3 blk(BX, BY);
+    if (bwd) {  // a backward step of an FWI pass: 4, 2 or 1 cells per thread (vrows is 1 then)
+        const FwiDev &F = *bwd;
+        if (vw == 4)
+            DISPATCH_ND(nd, (launch_pdl(k_update_vw_bwd<ND, 4>, gv, blk, 0, st, G, W, M, F)))
+        else if (vw == 2)
+            DISPATCH_ND(nd, (launch_pdl(k_update_vw_bwd<ND, 2>, gv, blk, 0, st, G, W, M, F)))
+        else
+            DISPATCH_ND(nd, (launch_pdl(k_update_vw_bwd<ND, 1>, gv, blk, 0, st, G, W, M, F)))
+        return;
+    }
     if (narrow && vw == 4 && narrow_v_applies(acoustic, W.fa_x != nullptr)) {
         DISPATCH_ND(nd, (launch_pdl(k_update_vw<ND, 4, true, false, 8>, gv, dim3(8, BX * BY / 8), 0, st, G, W, M)))
         return;

@@ -189,6 +189,7 @@ struct sofi_ctx {
     int vw = 4;                // velocity kernel: cells per thread in x (4 or 2), 0 = vrows rows per thread
     int vrows = 1;             // rows per thread of the one-cell velocity kernel (1, 2 or 4)
     int fwi_vw = 4, fwi_sw = 4; // an FWI pass's forward steps: cells per thread of the FWI kernels
+    bool tuning = false;       // the autotuner's launches are being issued (plain kernels only)
     // FWI gradient pass of one shot (sofi_fwi_*; sofi_fwi.cu)
     bool fwi = false;          // the forward runs store the gradient quantities
     bool fwi_back = false;     // the backward run is being issued
@@ -574,7 +575,7 @@ void launch_v(sofi_ctx *c, const Geo &G, cudaStream_t st)
     const int R = (vw || ac) ? 1 : c->vrows, cx = vw ? vw : 1, bxt = narrow ? 8 : BX, byt = BX * BY / bxt;
     const unsigned tx = (cf.nx + cx * bxt - 1) / (cx * bxt), ty = (cf.ny + byt * R - 1) / (byt * R);
     const dim3 gv = G.shot_fast ? dim3(tx * S, ty, 1) : dim3(tx, ty, S);
-    launch_velocity(G, W, c->M, c->nd, vw, R, narrow, ac, gv, st);
+    launch_velocity(G, W, c->M, c->nd, vw, R, narrow, ac, gv, st, c->fwi_back && !c->tuning ? &c->F : nullptr);
 }
 
 // 4th-order time stepping has no autotuning: four cells per thread in both
@@ -632,7 +633,20 @@ static bool narrow_useful(int nx)
 
 static bool post_fused(const sofi_ctx *c);
 
+static int autotune_(sofi_ctx *c);
+
+// The tuner's launches run the plain kernels: none of them is a step (no step
+// counter), and on a backward FWI step they carry no adjoint injection or
+// density term.
 int autotune(sofi_ctx *c)
+{
+    c->tuning = true;
+    const int rc = autotune_(c);
+    c->tuning = false;
+    return rc;
+}
+
+static int autotune_(sofi_ctx *c)
 {
     c->tuned = true;
     if (c->G.ab4)
@@ -788,10 +802,6 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
     if (c->has_force) {
         launch_pdl(k_force_src, nb, 128, 0, st, G, c->W, c->M, c->A);
         c->launches++;
-    }
-    if (c->fwi_back) {  // adjoint signals at the receivers, then the density term
-        launch_fwi_backward_pre(G, c->W, c->F, st);
-        c->launches += c->F.ncell ? 2 : 1;
     }
     if (G.ab4) {  // 4th order: every block of the velocity kernel reads the step number
         launch_ab4_begin(G, st);
@@ -1129,9 +1139,10 @@ int sofi_create_with_priority(const sofi_config *cfg, int device, int priority, 
             goto bad;
         *slot_ptr(c->M, n.c_str(), true) = p;
     }
-    if ((rc = dalloc(c, (void **)&c->d_status, sizeof(int) * (cfg->nshots + 1))))
+    if ((rc = dalloc(c, (void **)&c->d_status, sizeof(int) * (cfg->nshots + 2))))
         goto bad;
     c->G.step_ctr = c->d_status + cfg->nshots;  // zeroed with the status words
+    c->F.bstep = c->d_status + cfg->nshots + 1; // the same
     if (const char *e = getenv("SOFI_GRAPH"))
         c->use_graph = atoi(e) != 0;
     if (const char *e = getenv("SOFI_PDL"))
@@ -1325,7 +1336,7 @@ int sofi_reset(sofi_ctx *c, int shot)
             CK(cudaMemsetAsync(c->W.dcor + 4LL * s * c->G.fsz, 0, 4 * f, c->stream));
         }
     }
-    CK(cudaMemsetAsync(c->d_status, 0, sizeof(int) * (c->cfg.nshots + 1), c->stream));  // + step counter
+    CK(cudaMemsetAsync(c->d_status, 0, sizeof(int) * (c->cfg.nshots + 2), c->stream));  // + step counters
     if (c->d_sec && !c->acq_dirty) {
         size_t n = (size_t)c->total_rec * 5 * (c->A.ns > 0 ? c->A.ns : 1);
         CK(cudaMemsetAsync(c->d_sec, 0, n * sizeof(float), c->stream));
@@ -1591,6 +1602,7 @@ static int fwi_set_step(sofi_ctx *c, int step, int base)
 {
     c->step = step;
     CK(cudaMemcpyAsync(c->G.step_ctr, &step, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->F.bstep, &step, sizeof(int), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->d_fwi_base, &base, sizeof(int), cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));  // the host ints above are locals
     return 0;
@@ -1716,32 +1728,39 @@ int sofi_fwi_backward(sofi_ctx *c, const float *adj_x, const float *adj_y)
             order.push_back(key);
         cells[key].push_back(l);
     }
-    std::vector<int> off(1, 0), rec, cx, cy;
+    // the backward velocity kernel finds a cell's receivers through a map of
+    // the grid (k + 1 at receiver cell k)
+    const size_t n = (size_t)c->cfg.nx * c->cfg.ny;
+    std::vector<int> off(1, 0), rec, map(n, 0);
     for (auto &k : order) {
         for (int l : cells[k])
             rec.push_back(l);
         off.push_back((int)rec.size());
-        cy.push_back(k.first), cx.push_back(k.second);
+        map[(size_t)(k.first - 1) * c->cfg.nx + (k.second - 1)] = (int)off.size() - 1;
     }
     const size_t nc = order.size();
     if (nc + 1 > c->fwi_cells_cap || !c->F.adj) {
         int *ib;
         float *adj;
         const size_t cap = (nc + 1) > 1 ? nc + 1 : 2;
-        if ((rc = dalloc(c, (void **)&ib, (4 * cap + (size_t)ntr) * sizeof(int))) ||
+        if ((rc = dalloc(c, (void **)&ib, (cap + (size_t)ntr) * sizeof(int))) ||
             (rc = dalloc(c, (void **)&adj, 2 * (size_t)(ntr > 0 ? ntr : 1) * NT * sizeof(float))))
             return rc;
-        c->F.cell_off = ib, c->F.cell_ix = ib + cap, c->F.cell_iy = ib + 2 * cap, c->F.cell_rec = ib + 3 * cap;
+        c->F.cell_off = ib, c->F.cell_rec = ib + cap;
         c->F.adj = adj;
         c->fwi_cells_cap = cap;
     }
+    if (!c->F.cell_map) {
+        int *mp;
+        if ((rc = dalloc(c, (void **)&mp, n * sizeof(int))))
+            return rc;
+        c->F.cell_map = mp;
+    }
     CK(cudaMemcpyAsync((void *)c->F.cell_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    if (nc) {
-        CK(cudaMemcpyAsync((void *)c->F.cell_ix, cx.data(), nc * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-        CK(cudaMemcpyAsync((void *)c->F.cell_iy, cy.data(), nc * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync((void *)c->F.cell_map, map.data(), n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    if (nc)
         CK(cudaMemcpyAsync((void *)c->F.cell_rec, rec.data(), rec.size() * sizeof(int), cudaMemcpyHostToDevice,
                            c->stream));
-    }
     const size_t m = (size_t)ntr * NT;
     CK(cudaMemcpyAsync((void *)c->F.adj, adj_x, m * sizeof(float), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync((void *)(c->F.adj + m), adj_y, m * sizeof(float), cudaMemcpyHostToDevice, c->stream));
@@ -1751,16 +1770,17 @@ int sofi_fwi_backward(sofi_ctx *c, const float *adj_x, const float *adj_y)
         return rc;
     // The backward steps write no gradient quantities: they run the variants
     // the autotuner picks for plain steps of this grid (timed now, on the
-    // zeroed state, or taken from the cache); recomputed forward steps run the
-    // FWI kernels of the first forward run (fwi_vw, fwi_sw).
+    // zeroed state, or taken from the cache), the velocity update in its
+    // backward form (four, two or one cell per thread on wide blocks, which
+    // also injects the residuals and adds the density term); recomputed
+    // forward steps run the FWI kernels of the first forward run (fwi_vw, fwi_sw).
     c->fwi_back = true, c->tuned = false;
     rc = autotune(c);
-    const int bvw = c->vw, bvrows = c->vrows, bsw = c->sw;
-    const bool bvnarrow = c->vnarrow, bsnarrow = c->snarrow;
+    const int bvw = c->vw, bvrows = 1, bsw = c->sw;
+    const bool bvnarrow = false, bsnarrow = c->snarrow;
     c->fwi_back = false;
     if (rc)
         return rc;
-    const size_t n = (size_t)c->cfg.nx * c->cfg.ny;
     CK(cudaMemsetAsync(c->F.px, 0, n * sizeof(float), c->stream));
     CK(cudaMemsetAsync(c->F.py, 0, n * sizeof(float), c->stream));
     const Acq saved = c->A;
