@@ -1019,14 +1019,52 @@ __device__ __forceinline__ void s_update(const Geo &G, const Wave &Wr, const Wav
     }
 }
 
-template <int ND, int KIND, bool VISCO, int LT, int VW, bool FWI = false, int TBX = BX>
-__device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model &M, const uint3 b)
+// A backward step of an FWI pass without a free surface, after the stress
+// update of VW adjacent cells: calc_conv.c:34-71's lambda and mu terms
+// against forward slot NT - nt + 1, formed in double and rounded into the
+// float sums as the reference evaluates them (k_fwi_conv's arithmetic), from
+// the stresses this thread has just stored. The reference divides by
+// (lamss + muss)^2 and muss^2; their double reciprocals (FwiDev::rc) multiply.
+template <int VW>
+__device__ __forceinline__ void bwd_conv(const Geo &G, const FwiDev &F, const Model &M, const float *sxx,
+                                         const float *syy, const float *sxy, int i, int j, int o, long long mo)
+{
+    const int nt = *G.step_ctr;
+    const long long n = (long long)G.nx * G.ny;
+    const float *slot = F.store + (long long)(F.nt - nt - *F.base) * 5 * n;
+    const double mDT = -(double)G.dt;
+#pragma unroll
+    for (int c = 0; c < VW; c++) {
+        if (i + c > G.nx)
+            continue;
+        const long long q = (long long)(j - 1) * G.nx + (i + c - 1);
+        const float fx = slot[2 * n + q], fy = slot[3 * n + q], fu = slot[4 * n + q];
+        const float xx = sxx[o + c], yy = syy[o + c], xy = sxy[o + c];
+        const float sum_f = __fmul_rn(__fadd_rn(fx, fy), __fadd_rn(xx, yy));
+        F.g_lam[q] = (float)__dadd_rn((double)F.g_lam[q], __dmul_rn(__dmul_rn(mDT, F.rc[q]), (double)sum_f));
+        if (M.pu[mo + o + c] > 0.0f) {
+            const double r_mm = F.rc[n + q], r_lm2 = F.rc[2 * n + q];
+            const double t1 = __dmul_rn(r_mm, (double)__fmul_rn(fu, xy));
+            const double t2 = __dmul_rn(__dmul_rn(0.25, (double)sum_f), r_lm2);
+            const double t3 = __dmul_rn(__dmul_rn(0.25, (double)__fmul_rn(__fsub_rn(fx, fy), __fsub_rn(xx, yy))), r_mm);
+            F.g_mu[q] = (float)__dadd_rn((double)F.g_mu[q], __dmul_rn(mDT, __dadd_rn(__dadd_rn(t1, t2), t3)));
+        }
+    }
+}
+
+template <int ND, int KIND, bool VISCO, int LT, int VW, bool FWI = false, int TBX = BX, bool BWD = false>
+__device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model &M, const uint3 b,
+                                        const FwiDev *F = nullptr)
 {
     constexpr int TBY = BX * BY / TBX;  // TBX: as in vw_tile
     int bx, s;
     block_xs(G, b, bx, s);
     const int i = (bx * TBX + threadIdx.x) * VW + 1;
     const int j = b.y * TBY + threadIdx.y + 1;
+    // the step this kernel completes, for the next backward velocity kernel
+    // (nothing writes the step counter while it runs)
+    if (BWD && b.x == 0 && b.y == 0 && b.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+        *F->bstep = *G.step_ctr;
     if (i > G.nx || j > G.ny)
         return;
     const int P = G.pitch;
@@ -1039,6 +1077,8 @@ __device__ __forceinline__ void sw_tile(const Geo &G, const Wave &W, const Model
         G, [&](int f, int dy, int dx, float *out) { ldv<VW>((f ? vy : vx) + o + dy * P + dx, out); }, vxx, vyx,
         vxy, vyy);
     s_update<ND, KIND, VISCO, LT, VW, FWI>(G, W, W, M, s, i, j, o, mo, vxx, vyx, vxy, vyy);
+    if constexpr (BWD)
+        bwd_conv<VW>(G, *F, M, W.sxx + so, W.syy + so, W.sxy + so, i, j, o, mo);
 }
 
 template <int ND, int KIND, bool VISCO, int LT, int VW, bool FWI = false, int TBX = BX>
@@ -1046,6 +1086,16 @@ __global__ void __launch_bounds__(BX *BY, VW == 4 ? (VISCO ? 2 : 3) : 1) k_updat
 {
     pdl_begin();
     sw_tile<ND, KIND, VISCO, LT, VW, FWI, TBX>(G, W, M, blockIdx);
+}
+
+// A backward step of an FWI pass (EL_ISO) without a free surface: the
+// elastic stress update of VW = 4, 2 or 1 cells per thread, then the lambda /
+// mu correlation (bwd_conv) in the same kernel.
+template <int ND, int VW>
+__global__ void __launch_bounds__(BX *BY, VW == 4 ? 2 : 1) k_update_sw_bwd(Geo G, Wave W, Model M, FwiDev F)
+{
+    pdl_begin();
+    sw_tile<ND, ISO, false, 0, VW, false, BX, true>(G, W, M, blockIdx, &F);
 }
 
 // Acoustic stress update (wavefield_update_s_ac.c, update_s_acoustic_{interior,

@@ -799,6 +799,9 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
     int kind = kind_of(cf.weq);
     bool visco = is_visco(cf.weq);
     const bool fused_post = post_fused(c);
+    // a backward FWI step without a free surface: the stress kernel also
+    // correlates (the post kernel then changes no stress)
+    const bool conv_fused = c->fwi_back && !cf.free_surf && kind == ISO && !visco && !G.ab4;
     if (c->has_force) {
         launch_pdl(k_force_src, nb, 128, 0, st, G, c->W, c->M, c->A);
         c->launches++;
@@ -843,6 +846,10 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
         launch_tti_fused(G, c->W, c->M, c->nd, visco, G.abs_type == 1, grd, st);
     } else if (kind == TTI) {
         launch_tti_tiles(G, c->W, c->M, c->nd, visco, G.abs_type == 1, st);
+    } else if (conv_fused) {
+        const int cx = c->sw ? c->sw : 1;
+        const dim3 sg((cf.nx + cx * BX - 1) / (cx * BX), (cf.ny + BY - 1) / BY, 1);
+        launch_stress_bwd(G, step_wave(c), c->M, c->F, c->nd, c->sw, sg, st);
     } else {
         launch_cell_s(G, step_wave(c), c->M, c->nd, kind, visco, c->sw, c->snarrow, cf.nx, cf.ny, S, st,
                       fused_post ? &c->A : nullptr);
@@ -865,9 +872,10 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
         c->launches++;
     }
     if (c->fwi && (c->fwi_back || c->fwi_store_on)) {  // time_loop.c:288-296
-        if (c->fwi_back) {
+        if (c->fwi_back && !conv_fused) {
             launch_fwi_conv(G, c->W, c->M, c->F, st);
             c->launches++;
+        } else if (c->fwi_back) {
         } else if (!c->F.velocity) {  // VELOCITY = 1: the stress kernel stored the step
             launch_fwi_store(G, c->W, c->F, st);
             c->launches++;
