@@ -872,10 +872,11 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
         c->launches++;
     }
     if (c->fwi && (c->fwi_back || c->fwi_store_on)) {  // time_loop.c:288-296
-        if (c->fwi_back && !conv_fused) {
-            launch_fwi_conv(G, c->W, c->M, c->F, st);
-            c->launches++;
-        } else if (c->fwi_back) {
+        if (c->fwi_back) {
+            if (!conv_fused) {  // else the stress kernel has correlated
+                launch_fwi_conv(G, c->W, c->M, c->F, st);
+                c->launches++;
+            }
         } else if (!c->F.velocity) {  // VELOCITY = 1: the stress kernel stored the step
             launch_fwi_store(G, c->W, c->F, st);
             c->launches++;
