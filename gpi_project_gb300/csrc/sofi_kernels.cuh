@@ -676,7 +676,9 @@ __device__ __forceinline__ void post_cell(const Geo &G, const Model &M, const Ac
 // sources, seismograms, the NaN probe -- for steps without a free surface or
 // moment-tensor sources, so that the step needs no post kernel.
 // POST: pflag and ca are the cell's flags and acquisition (cell_acq).
-template <int ND, int KIND, bool VISCO, int LT, bool POST>
+// FWI (EL_ISO, a stored step of an FWI forward run with VELOCITY = 1,
+// Wave::fstore set): also the store slot, as s_update writes it.
+template <int ND, int KIND, bool VISCO, int LT, bool POST, bool FWI = false>
 __device__ __forceinline__ void s_one(const Geo &G, const Wave &W, const Model &M, const Acq &A, unsigned pflag,
                                       const CellAcq &ca)
 {
@@ -747,6 +749,13 @@ __device__ __forceinline__ void s_one(const Geo &G, const Wave &W, const Model &
         float gd = m0 * (vxx + vyy);
         u2 = gd - 2.0f * m1 * vyy;
         u3 = gd - 2.0f * m1 * vxx;
+        if (FWI && !VISCO && W.fstore) {
+            const long long n = (long long)G.nx * G.ny;
+            float *slot = W.fstore + (long long)(*G.step_ctr - 1 - *W.fbase) * 5 * n +
+                          ((long long)(j - 1) * G.nx + (i - 1));
+            slot[0] = W.fa_x[so + o], slot[n] = W.fa_y[so + o];
+            slot[2 * n] = u2 / G.dt, slot[3 * n] = u3 / G.dt, slot[4 * n] = u1 / G.dt;
+        }
     } else {
         u1 = m3 * (vxy + vyx);
         u2 = m0 * vxx + m1 * vyy;
@@ -822,6 +831,66 @@ __global__ void __launch_bounds__(BX *BY, 5) k_update_s_post(Geo G, Wave W, Mode
     }
     pdl_begin();
     s_one<ND, KIND, VISCO, LT, true>(G, W, M, A, flag, ca);
+}
+
+// A backward step of an FWI pass without a free surface, after the stress
+// update of VW adjacent cells: calc_conv.c:34-71's lambda and mu terms
+// against forward slot NT - nt + 1, formed in double and rounded into the
+// float sums as the reference evaluates them (k_fwi_conv's arithmetic), from
+// the stresses this thread has just stored. The reference divides by
+// (lamss + muss)^2 and muss^2; their double reciprocals (FwiDev::rc) multiply.
+template <int VW>
+__device__ __forceinline__ void bwd_conv(const Geo &G, const FwiDev &F, const Model &M, const float *sxx,
+                                         const float *syy, const float *sxy, int i, int j, int o, long long mo)
+{
+    const int nt = *G.step_ctr;
+    const long long n = (long long)G.nx * G.ny;
+    const float *slot = F.store + (long long)(F.nt - nt - *F.base) * 5 * n;
+    const double mDT = -(double)G.dt;
+#pragma unroll
+    for (int c = 0; c < VW; c++) {
+        if (i + c > G.nx)
+            continue;
+        const long long q = (long long)(j - 1) * G.nx + (i + c - 1);
+        const float fx = slot[2 * n + q], fy = slot[3 * n + q], fu = slot[4 * n + q];
+        const float xx = sxx[o + c], yy = syy[o + c], xy = sxy[o + c];
+        const float sum_f = __fmul_rn(__fadd_rn(fx, fy), __fadd_rn(xx, yy));
+        F.g_lam[q] = (float)__dadd_rn((double)F.g_lam[q], __dmul_rn(__dmul_rn(mDT, F.rc[q]), (double)sum_f));
+        if (M.pu[mo + o + c] > 0.0f) {
+            const double r_mm = F.rc[n + q], r_lm2 = F.rc[2 * n + q];
+            const double t1 = __dmul_rn(r_mm, (double)__fmul_rn(fu, xy));
+            const double t2 = __dmul_rn(__dmul_rn(0.25, (double)sum_f), r_lm2);
+            const double t3 = __dmul_rn(__dmul_rn(0.25, (double)__fmul_rn(__fsub_rn(fx, fy), __fsub_rn(xx, yy))), r_mm);
+            F.g_mu[q] = (float)__dadd_rn((double)F.g_mu[q], __dmul_rn(mDT, __dadd_rn(__dadd_rn(t1, t2), t3)));
+        }
+    }
+}
+
+// The same for the steps of an FWI pass (EL_ISO, one shot): a forward step
+// also writes the store slot (s_one's FWI); a backward step without a free
+// surface then adds the lambda / mu correlation from the stresses the cell
+// holds after the post work (bwd_conv) and records the step it completes for
+// the next backward velocity kernel.
+template <int ND, bool BWD>
+__global__ void __launch_bounds__(BX *BY, 4) k_update_s_post_fwi(Geo G, Wave W, Model M, Acq A, FwiDev F)
+{
+    __shared__ CellAcq slot[BX * BY];
+    const int i = blockIdx.x * BX + threadIdx.x + 1, j = blockIdx.y * BY + threadIdx.y + 1;
+    CellAcq &ca = slot[threadIdx.y * BX + threadIdx.x];
+    unsigned flag = 0;
+    if (i <= G.nx && j <= G.ny) {
+        flag = __ldg(A.cell_flag + (long long)(j - 1) * G.nx + (i - 1));
+        if (flag)
+            ca = cell_acq(G, A, 0, i, j, flag);
+    }
+    pdl_begin();
+    if (BWD && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+        *F.bstep = *G.step_ctr;
+    s_one<ND, ISO, false, 0, true, !BWD>(G, W, M, A, flag, ca);
+    if (BWD && i <= G.nx && j <= G.ny) {
+        const int o = (j - 1 + HY) * G.pitch + (i - 1 + HX);
+        bwd_conv<1>(G, F, M, W.sxx, W.syy, W.sxy, i, j, o, 0);
+    }
 }
 
 // The stress update with VW adjacent cells per thread (VW = 2 or 4), the
@@ -1015,39 +1084,6 @@ __device__ __forceinline__ void s_update(const Geo &G, const Wave &Wr, const Wav
                     }
             }
             sxy[o + c] = nxy[c], sxx[o + c] = nxx[c], syy[o + c] = nyy[c];
-        }
-    }
-}
-
-// A backward step of an FWI pass without a free surface, after the stress
-// update of VW adjacent cells: calc_conv.c:34-71's lambda and mu terms
-// against forward slot NT - nt + 1, formed in double and rounded into the
-// float sums as the reference evaluates them (k_fwi_conv's arithmetic), from
-// the stresses this thread has just stored. The reference divides by
-// (lamss + muss)^2 and muss^2; their double reciprocals (FwiDev::rc) multiply.
-template <int VW>
-__device__ __forceinline__ void bwd_conv(const Geo &G, const FwiDev &F, const Model &M, const float *sxx,
-                                         const float *syy, const float *sxy, int i, int j, int o, long long mo)
-{
-    const int nt = *G.step_ctr;
-    const long long n = (long long)G.nx * G.ny;
-    const float *slot = F.store + (long long)(F.nt - nt - *F.base) * 5 * n;
-    const double mDT = -(double)G.dt;
-#pragma unroll
-    for (int c = 0; c < VW; c++) {
-        if (i + c > G.nx)
-            continue;
-        const long long q = (long long)(j - 1) * G.nx + (i + c - 1);
-        const float fx = slot[2 * n + q], fy = slot[3 * n + q], fu = slot[4 * n + q];
-        const float xx = sxx[o + c], yy = syy[o + c], xy = sxy[o + c];
-        const float sum_f = __fmul_rn(__fadd_rn(fx, fy), __fadd_rn(xx, yy));
-        F.g_lam[q] = (float)__dadd_rn((double)F.g_lam[q], __dmul_rn(__dmul_rn(mDT, F.rc[q]), (double)sum_f));
-        if (M.pu[mo + o + c] > 0.0f) {
-            const double r_mm = F.rc[n + q], r_lm2 = F.rc[2 * n + q];
-            const double t1 = __dmul_rn(r_mm, (double)__fmul_rn(fu, xy));
-            const double t2 = __dmul_rn(__dmul_rn(0.25, (double)sum_f), r_lm2);
-            const double t3 = __dmul_rn(__dmul_rn(0.25, (double)__fmul_rn(__fsub_rn(fx, fy), __fsub_rn(xx, yy))), r_mm);
-            F.g_mu[q] = (float)__dadd_rn((double)F.g_mu[q], __dmul_rn(mDT, __dadd_rn(__dadd_rn(t1, t2), t3)));
         }
     }
 }

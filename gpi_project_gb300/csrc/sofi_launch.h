@@ -42,9 +42,10 @@ void launch_stress_kv(const Geo &G, const Wave &W, const Model &M, int nd, int s
                       cudaStream_t st, const Acq *post = nullptr);
 // A backward step of an FWI pass (EL_ISO) without a free surface: the stress
 // update with the lambda / mu correlation, sw cells per thread in x (4, 2 or
-// 0 = one), wide blocks
+// 0 = one), wide blocks; post (sw 0 only, else null): the one-cell kernel
+// also does k_post's work with that acquisition
 void launch_stress_bwd(const Geo &G, const Wave &W, const Model &M, const FwiDev &F, int nd, int sw, dim3 grid,
-                       cudaStream_t st);
+                       cudaStream_t st, const Acq *post = nullptr);
 // acoustic stress update: sw cells per thread in x (4, 2 or 0/1 = one)
 void launch_stress_ac(const Geo &G, const Wave &W, const Model &M, int nd, int sw, dim3 grid, cudaStream_t st);
 // FDORDER_TIME = 4: step counter, velocity update, stress update (one cell per thread)

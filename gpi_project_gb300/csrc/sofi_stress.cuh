@@ -58,7 +58,11 @@ void launch_stress_kv(const Geo &G, const Wave &W, const Model &M, int nd, int s
     [[maybe_unused]] const int L = VISCO ? G.L : 0;
     if constexpr (KIND == ISO && !VISCO)
         if (W.fa_x) {  // a step of an FWI forward run, one cell per thread
-            DISPATCH_ND(nd, (launch_pdl(k_update_sw<ND, ISO, false, 0, 1, true>, grd, blk, 0, st, G, W, M)))
+            if (post)  // with k_post's work (the FwiDev argument is not read)
+                DISPATCH_ND(nd, (launch_pdl(k_update_s_post_fwi<ND, false>, grd, blk, 0, st, G, W, M, *post,
+                                            FwiDev{})))
+            else
+                DISPATCH_ND(nd, (launch_pdl(k_update_sw<ND, ISO, false, 0, 1, true>, grd, blk, 0, st, G, W, M)))
             return;
         }
     if (post) {  // one cell per thread with k_post's work (k_update_s_post)

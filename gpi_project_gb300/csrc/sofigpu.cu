@@ -772,15 +772,16 @@ static int autotune_(sofi_ctx *c)
 }
 
 // Whether the one-cell ISO / VTI stress kernel does k_post's work in this
-// step (k_update_s_post): no free surface (its correction needs the column's
-// updated rows), no moment-tensor source (it reaches a neighbouring cell),
-// few sources per shot (a flagged cell scans them), 2nd-order time, no FWI run.
+// step (k_update_s_post, and k_update_s_post_fwi on the steps of an FWI
+// pass): no free surface (its correction needs the column's updated rows), no
+// moment-tensor source (it reaches a neighbouring cell), few sources per shot
+// (a flagged cell scans them), 2nd-order time.
 constexpr size_t kFusedSources = 8;
 static bool post_fused(const sofi_ctx *c)
 {
     const int kind = kind_of(c->cfg.weq);
     if (!c->postf || !c->A.cell_flag || c->sw != 0 || (kind != ISO && kind != VTI) || c->cfg.free_surf ||
-        c->G.ab4 || c->fwi)
+        c->G.ab4)
         return false;
     for (const auto &a : c->acq)
         if ((!a.type.empty() && a.type.back() == 5) || a.ix.size() > kFusedSources)
@@ -849,7 +850,7 @@ int launch_step(sofi_ctx *c, int nt, bool capture = false)
     } else if (conv_fused) {
         const int cx = c->sw ? c->sw : 1;
         const dim3 sg((cf.nx + cx * BX - 1) / (cx * BX), (cf.ny + BY - 1) / BY, 1);
-        launch_stress_bwd(G, step_wave(c), c->M, c->F, c->nd, c->sw, sg, st);
+        launch_stress_bwd(G, step_wave(c), c->M, c->F, c->nd, c->sw, sg, st, fused_post ? &c->A : nullptr);
     } else {
         launch_cell_s(G, step_wave(c), c->M, c->nd, kind, visco, c->sw, c->snarrow, cf.nx, cf.ny, S, st,
                       fused_post ? &c->A : nullptr);
@@ -1824,7 +1825,12 @@ int sofi_fwi_backward(sofi_ctx *c, const float *adj_x, const float *adj_y)
                 break;
             backward_mode(false);
             c->fwi_store_on = true, c->fwi_nosnap = true;
-            if ((rc = sofi_run(c, k)))
+            // a recomputed segment records no seismograms: the sections keep
+            // the backward run's samples, as after a whole-store pass
+            c->G.seismo = 0;
+            rc = sofi_run(c, k);
+            c->G.seismo = c->cfg.seismo;
+            if (rc)
                 break;
             if ((rc = fwi_copy_state(c, done ? c->fwi_tmp : nullptr, false)) || (rc = fwi_set_step(c, done, s0)))
                 break;

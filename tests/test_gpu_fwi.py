@@ -20,7 +20,7 @@ L2_TOL, MAX_TOL = 1e-4, 1e-3
 GRAD_L2, GRAD_MAX = 1e-3, 1e-2
 
 
-def gpu_fwi(case, obs_vx, obs_vy, variants=None):
+def gpu_fwi(case, obs_vx, obs_vy, variants=None, backward_sections=None):
     from oracle import oracle as O
     from gpi_project_gb300 import TimeLoop
     from gpi_project_gb300 import host as H
@@ -46,6 +46,8 @@ def gpu_fwi(case, obs_vx, obs_vy, variants=None):
     rx, _ = H.fwi_residual(fwd["vx"], obs_vx, case["velocity"], cfg.dt)
     ry, _ = H.fwi_residual(fwd["vy"], obs_vy, case["velocity"], cfg.dt)
     t.fwi_backward(rx, ry)
+    if backward_sections is not None:  # what the backward run recorded at the receivers
+        backward_sections.update(vx=t.section("vx"), vy=t.section("vy"))
     lam, mu, rhos = t.fwi_gradients()
     grads = dict(zip(("vp", "vs", "rho"), H.fwi_model_gradients(lam, mu, rhos, *model)))
     t.close()
@@ -151,15 +153,23 @@ def test_gpu_fwi_checkpointed_equals_whole_store(case, monkeypatch):
     store), each segment's forward steps are recomputed from its checkpoint
     before the backward steps that read them: the same kernels on the same
     state, so the gradients equal the whole-store pass bit for bit, for
-    segment lengths that divide NT and that do not."""
+    segment lengths that divide NT and that do not. The recomputed segments
+    record no seismograms: the sections after the pass hold the backward
+    run's samples, as after the whole-store pass (a drop-in time_loop()
+    hands them back to the caller after sw = 1)."""
     g = np.load(os.path.join(HERE, "golden", f"ref_{case['name']}.npz"))
     monkeypatch.delenv("SOFI_FWI_CHECKPOINT", raising=False)
-    _, whole = gpu_fwi(case, g["obs_vx"], g["obs_vy"])
+    bw_whole = {}
+    _, whole = gpu_fwi(case, g["obs_vx"], g["obs_vy"], backward_sections=bw_whole)
+    assert np.abs(bw_whole["vx"]).max() + np.abs(bw_whole["vy"]).max() > 0
     for k in ("7", "64", str(case["nt"])):
         monkeypatch.setenv("SOFI_FWI_CHECKPOINT", k)
-        fwd, ck = gpu_fwi(case, g["obs_vx"], g["obs_vy"])
+        bw = {}
+        fwd, ck = gpu_fwi(case, g["obs_vx"], g["obs_vy"], backward_sections=bw)
         for name in ("vp", "vs", "rho"):
             np.testing.assert_array_equal(ck[name], whole[name], err_msg=f"{case['name']} K={k} {name}")
+        for c in ("vx", "vy"):
+            np.testing.assert_array_equal(bw[c], bw_whole[c], err_msg=f"{case['name']} K={k} backward {c}")
 
 
 @pytest.mark.parametrize("case", FWI_CASES, ids=[c["name"] for c in FWI_CASES])
