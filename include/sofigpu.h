@@ -224,7 +224,9 @@ int sofi_velocity_variant(sofi_ctx *ctx, int *cells_per_thread, int *rows_per_th
  * forward run keeps the wavefield and CPML memory after steps K, 2K, ...
  * (about sqrt(NT) states), and sofi_fwi_backward recomputes each segment's
  * forward steps from its checkpoint before the backward steps that read
- * them -- one extra forward run, the same gradients bit for bit.
+ * them -- one extra forward run, the same gradients bit for bit; the
+ * recomputed steps record no seismograms, so the sections after the pass
+ * hold the backward run's samples as after a whole-store pass.
  * sofi_fwi_checkpoints reports the interval (0: the whole run is stored) and
  * the number of segments. */
 int sofi_fwi_begin(sofi_ctx *ctx, int velocity, int adjoint_type, const float *vp, const float *vs,
