@@ -124,6 +124,50 @@ int sofih_read_model(const sofih_par *p, const char *mfile, float **out, int max
     return 0;
 }
 
+int sofih_scan_topo(const sofih_par *p, const char *mfile, int *topo)
+{
+    const size_t cnt = (size_t)p->nx * (size_t)p->ny;
+    float *vp = (float *)malloc(cnt * sizeof(float));
+    if (!vp) {
+        sofih_set_error("out of host memory scanning the topography");
+        return 1;
+    }
+    char path[600];
+    snprintf(path, sizeof path, "%s.vp.su", mfile);
+    FILE *fp = fopen(path, "rb");
+    int rc = 0;
+    if (fp) { /* scan_topo.c:35-45: the SU model when it is readable */
+        fclose(fp);
+        rc = read_su_model(path, p->nx, p->ny, vp);
+    } else {
+        snprintf(path, sizeof path, "%s.vp", mfile);
+        fp = fopen(path, "rb");
+        if (!fp) {
+            free(vp);
+            sofih_set_error("could not open the P-wave velocity model %s to scan the topography", path);
+            return 1;
+        }
+        const size_t got = fread(vp, sizeof(float), cnt, fp);
+        fclose(fp);
+        if (got != cnt) {
+            sofih_set_error("%s holds %zu values, NX*NY = %zu needed", path, got, cnt);
+            rc = 1;
+        }
+    }
+    for (int i = 0; i < p->nx && !rc; i++) { /* scan_topo.c:58-68 */
+        const float *tr = vp + (size_t)i * p->ny;
+        int t = 1;
+        for (int j = 2; j <= p->ny; j++)
+            if (tr[j - 1] != tr[0]) {
+                t = j;
+                break;
+            }
+        topo[i] = t;
+    }
+    free(vp);
+    return rc;
+}
+
 static int is_data_line(const char *s, int allow_percent)
 {
     if (strchr(s, '#') || (allow_percent && strchr(s, '%')))
@@ -132,10 +176,55 @@ static int is_data_line(const char *s, int allow_percent)
     return sscanf(s, "%63s", tok) == 1;
 }
 
+/* SRCREC 2 (sources.c:337-371): one source per column at the plane wave's
+ * depth, no time shift, centre frequency 1 / TS, unit amplitude, the run's
+ * SOURCE_TYPE; the operand types follow the reference's. */
+static int plane_wave_sources(const sofih_par *p, float **srcpos, float **xy, int *nsrc)
+{
+    const float tan_phi = (float)tan(p->plane_wave_angle * PI / 180.0);
+    const float dz = (float)(p->nx - 1) * p->dh * tan_phi;
+    if (p->plane_wave_depth + dz > (p->ny - 1) * p->dh) {
+        sofih_set_error("the plane wave's maximum depth %g m exceeds the model depth", p->plane_wave_depth + dz);
+        return 1;
+    }
+    const int n = p->nx;
+    float *sp = (float *)calloc((size_t)12 * n, sizeof(float));
+    float *pos = (float *)calloc((size_t)2 * n, sizeof(float));
+    if (!sp || !pos) {
+        free(sp), free(pos);
+        sofih_set_error("out of host memory");
+        return 1;
+    }
+    for (int i = 1; i <= n; i++) {
+        const int l = i - 1;
+        const float x = (i - 1) * p->dh;
+        const float y = p->plane_wave_depth + (tan_phi * x);
+        const float fc = 1.0 / p->ts;
+        sp[0 * n + l] = (float)((int)floor(x / p->dh) + 1);
+        sp[1 * n + l] = (float)((int)floor(y / p->dh) + 1);
+        sp[3 * n + l] = 0.0f, sp[4 * n + l] = fc, sp[5 * n + l] = 1.0f;
+        sp[6 * n + l] = 0.0f, sp[7 * n + l] = (float)p->source_type;
+        pos[l] = x, pos[n + l] = y;
+    }
+    *srcpos = sp, *xy = pos, *nsrc = n;
+    return 0;
+}
+
 int sofih_read_sources(const sofih_par *p, const char *path, float **srcpos, float **xy, int *nsrc)
 {
+    if (p->srcrec == 2)
+        return plane_wave_sources(p, srcpos, xy, nsrc);
+    int *topo = NULL;
+    if (p->source_topo) {
+        topo = (int *)malloc(sizeof(int) * (size_t)p->nx);
+        if (!topo || sofih_scan_topo(p, p->mfile, topo)) {
+            free(topo);
+            return 1;
+        }
+    }
     FILE *fp = fopen(path, "r");
     if (!fp) {
+        free(topo);
         sofih_set_error("cannot open source file %s", path);
         return 1;
     }
@@ -160,7 +249,7 @@ int sofih_read_sources(const sofih_par *p, const char *path, float **srcpos, flo
         const int shape = p->source_shape, need = shape == 5 || shape == 6 ? 8 : 5;
         if (k < need) {
             fclose(fp);
-            free(sp), free(pos);
+            free(sp), free(pos), free(topo);
             sofih_set_error("%s: source %d lacks %s", path, l + 1,
                             shape == 5   ? "time shift, frequency, amplitude, exponent, decay or phase"
                             : shape == 6 ? "time shift, frequencies, amplitude, sweep length or width"
@@ -168,6 +257,16 @@ int sofih_read_sources(const sofih_par *p, const char *path, float **srcpos, flo
             return 1;
         }
         float az = k > need ? v[need] : 0.0f, type = k > need + 1 ? v[need + 1] : (float)p->source_type;
+        if (topo) { /* sources.c:122-127: the depth below the topography at the source's column */
+            const int xidx = (int)floor(v[0] / p->dh) + 1;
+            if (xidx < 1 || xidx > p->nx) {
+                fclose(fp);
+                free(sp), free(pos), free(topo);
+                sofih_set_error("%s: source %d lies outside the model's columns", path, l + 1);
+                return 1;
+            }
+            v[1] = (topo[xidx - 1] - 1) * p->dh + v[1];
+        }
         sp[0 * n + l] = (float)((int)floor(v[0] / p->dh) + 1);
         sp[1 * n + l] = (float)((int)floor(v[1] / p->dh) + 1);
         sp[3 * n + l] = v[2];
@@ -185,6 +284,7 @@ int sofih_read_sources(const sofih_par *p, const char *path, float **srcpos, flo
         l++;
     }
     fclose(fp);
+    free(topo);
     *srcpos = sp, *xy = pos, *nsrc = n;
     return 0;
 }
@@ -406,60 +506,130 @@ int sofih_wavelet_file(const char *signal_file, int nt, float dt, int nsrc, cons
     return rc;
 }
 
-int sofih_read_receivers(const sofih_par *p, const char *path, int **ix, int **iy, int *ntr)
+typedef struct {
+    int *x, *y, *t;
+    int n, cap;
+} reclist;
+
+static int rec_push(reclist *r, int x, int y, int t)
 {
-    int cap = 64, n = 0;
-    int *x = (int *)malloc(sizeof(int) * cap), *y = (int *)malloc(sizeof(int) * cap);
-    if (p->readrec) {
+    if (r->n == r->cap) {
+        const int cap = r->cap ? 2 * r->cap : 64;
+        int *nx = (int *)realloc(r->x, sizeof(int) * cap), *ny = (int *)realloc(r->y, sizeof(int) * cap),
+            *nt = (int *)realloc(r->t, sizeof(int) * cap);
+        if (nx)
+            r->x = nx;
+        if (ny)
+            r->y = ny;
+        if (nt)
+            r->t = nt;
+        if (!nx || !ny || !nt) {
+            sofih_set_error("out of host memory");
+            return 1;
+        }
+        r->cap = cap;
+    }
+    r->x[r->n] = x, r->y[r->n] = y, r->t[r->n] = t;
+    r->n++;
+    return 0;
+}
+
+int sofih_read_receiver_traces(const sofih_par *p, const char *path, int **ix, int **iy, int **trace, int *ntr)
+{
+    reclist r = {0};
+    int rc = 0;
+    if (p->readrec) { /* receiver.c:41-99 */
+        int *topo = NULL;
+        if (p->rec_topo) {
+            topo = (int *)malloc(sizeof(int) * (size_t)p->nx);
+            if (!topo || sofih_scan_topo(p, p->mfile, topo)) {
+                free(topo);
+                return 1;
+            }
+        }
         FILE *fp = fopen(path, "r");
         if (!fp) {
-            free(x), free(y);
+            free(topo);
             sofih_set_error("cannot open receiver file %s", path);
             return 1;
         }
         char line[512];
-        while (fgets(line, sizeof line, fp)) {
+        int itr = 0;
+        while (!rc && fgets(line, sizeof line, fp)) {
             if (!is_data_line(line, 1))
                 continue;
             float xr, yr;
             if (sscanf(line, "%f%f", &xr, &yr) != 2)
                 continue;
-            if (n == cap)
-                cap *= 2, x = realloc(x, sizeof(int) * cap), y = realloc(y, sizeof(int) * cap);
-            x[n] = (int)floor((xr + p->refrec[0]) / p->dh) + 1;
-            y[n] = (int)floor((yr + p->refrec[1]) / p->dh) + 1;
-            n++;
+            itr++;
+            const int x = (int)floor((xr + p->refrec[0]) / p->dh) + 1;
+            int y;
+            if (topo) { /* receiver.c:68-70: the depth counted from the column's topography */
+                if (x < 1 || x > p->nx) {
+                    sofih_set_error("%s: receiver %d lies outside the model's columns", path, itr);
+                    rc = 1;
+                    break;
+                }
+                y = topo[x - 1] + (int)floor(yr / p->dh);
+            } else {
+                y = (int)floor((yr + p->refrec[1]) / p->dh) + 1;
+            }
+            rc = rec_push(&r, x, y, itr);
         }
         fclose(fp);
-    } else {
-        int x1 = (int)floor(p->xrec1 / p->dh) + 1, y1 = (int)floor(p->yrec1 / p->dh) + 1;
-        int x2 = (int)floor(p->xrec2 / p->dh) + 1, y2 = (int)floor(p->yrec2 / p->dh) + 1;
-        int step = p->ngeoph > 0 ? p->ngeoph : 1;
+        free(topo);
+        /* co-located receivers: the first keeps the grid point, its trace number stays */
+        int m = 0;
+        for (int k = 0; k < r.n && !rc; k++) {
+            int dup = 0;
+            for (int q = 0; q < m && !dup; q++)
+                dup = (r.x[q] == r.x[k] && r.y[q] == r.y[k]);
+            if (!dup)
+                r.x[m] = r.x[k], r.y[m] = r.y[k], r.t[m] = r.t[k], m++;
+        }
+        r.n = m;
+    } else if (p->rec_array > 0) { /* receiver.c:101-116: receiver planes */
+        int itr = 0;
+        for (int n = 0; n <= p->rec_array - 1 && !rc; n++) {
+            const float depth = p->rec_array_depth + p->rec_array_dist * (float)n;
+            const int j = IROUND(depth / p->dh);
+            for (int i = p->fw; i <= p->nx - p->fw && !rc; i += p->drx)
+                rc = rec_push(&r, i, j, ++itr);
+        }
+    } else { /* receiver.c:117-164: one point, or a horizontal or vertical line */
+        const int x1 = (int)floor(p->xrec1 / p->dh) + 1, y1 = (int)floor(p->yrec1 / p->dh) + 1;
+        const int x2 = (int)floor(p->xrec2 / p->dh) + 1, y2 = (int)floor(p->yrec2 / p->dh) + 1;
+        const int step = p->ngeoph > 0 ? p->ngeoph : 1;
         if (y1 != y2 && x1 != x2) {
-            free(x), free(y);
-            sofih_set_error("oblique receiver lines are not supported");
+            sofih_set_error("no horizontal or vertical receiver line: an oblique one needs a receiver file (READREC 1)");
             return 1;
         }
-        int len = (y1 == y2) ? x2 - x1 : y2 - y1;
-        for (int k = 0; k <= len; k += step) {
-            if (n == cap)
-                cap *= 2, x = realloc(x, sizeof(int) * cap), y = realloc(y, sizeof(int) * cap);
-            x[n] = (y1 == y2) ? x1 + k : x1;
-            y[n] = (y1 == y2) ? y1 : y1 + k;
-            n++;
-        }
+        const int len = (y1 == y2) ? x2 - x1 : y2 - y1;
+        for (int k = 0, itr = 1; k <= len && !rc; k += step, itr++)
+            rc = rec_push(&r, (y1 == y2) ? x1 + k : x1, (y1 == y2) ? y1 : y1 + k, itr);
     }
-    /* drop repeated grid points, keeping the first */
-    int m = 0;
-    for (int k = 0; k < n; k++) {
-        int dup = 0;
-        for (int q = 0; q < m && !dup; q++)
-            dup = (x[q] == x[k] && y[q] == y[k]);
-        if (!dup)
-            x[m] = x[k], y[m] = y[k], m++;
+    if (rc) {
+        free(r.x), free(r.y), free(r.t);
+        return 1;
     }
-    *ix = x, *iy = y, *ntr = m;
-    return 0;
+    for (int k = 0; k < r.n; k++) { /* receiver.c:166-171 */
+        if (r.x[k] == 0)
+            r.x[k] = 1;
+        if (r.y[k] == 0)
+            r.y[k] = 1;
+    }
+    if (!r.n) /* callers free what they get */
+        rc = rec_push(&r, 0, 0, 0), r.n = 0;
+    *ix = r.x, *iy = r.y, *trace = r.t, *ntr = r.n;
+    return rc;
+}
+
+int sofih_read_receivers(const sofih_par *p, const char *path, int **ix, int **iy, int *ntr)
+{
+    int *trace = NULL;
+    const int rc = sofih_read_receiver_traces(p, path, ix, iy, &trace, ntr);
+    free(trace);
+    return rc;
 }
 
 /* SEG-Y trace header fields written by outseis_glob.c:46-81 (byte offsets of
@@ -520,6 +690,13 @@ int sofih_write_su(const char *path, const float *section, int ntr, int ns, cons
 {
     (void)comp; /* outseis_glob.c:55,79: ep is set to comp, then to ishot */
     return write_su_traces(path, section, ntr, ns, ix, iy, NULL, xs, ys, p, ishot);
+}
+
+int sofih_write_su_traces(const char *path, const float *section, int ntr, int ns, const int *ix, const int *iy,
+                          const int *trace, float xs, float ys, const sofih_par *p, int ishot, int comp)
+{
+    (void)comp;
+    return write_su_traces(path, section, ntr, ns, ix, iy, trace, xs, ys, p, ishot);
 }
 
 int sofih_write_signal(const sofih_par *p, int ishot, const float *signal, int nt, int ix, int iy, float xs,

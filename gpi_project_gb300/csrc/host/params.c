@@ -205,6 +205,35 @@ int sofih_read_par(const char *path, sofih_par *p)
     gets_(kv, "GRADIENT", p->gradient, sizeof p->gradient);
     p->readmod = geti(kv, "READMOD", 1), p->tau = getf(kv, "TAU", 0.0001f);
     gets_(kv, "SIGNAL_FILE", p->signal_file, sizeof p->signal_file);
+    /* receiver planes and topography (read_par_json.c:242-246, 347-403, 425-427) */
+    p->rec_array = geti(kv, "REC_ARRAY", 0), p->drx = geti(kv, "DRX", 0);
+    p->rec_array_depth = getf(kv, "REC_ARRAY_DEPTH", 0.f), p->rec_array_dist = getf(kv, "REC_ARRAY_DIST", 0.f);
+    p->rec_topo = p->seismo > 0 ? geti(kv, "REC_TOPO", 0) : 0;
+    p->srcrec = geti(kv, "SRCREC", 1);
+    p->source_topo = p->srcrec == 1 ? geti(kv, "SOURCE_TOPO", 0) : 0;
+    p->plane_wave_depth = getf(kv, "PLANE_WAVE_DEPTH", 0.f), p->plane_wave_angle = getf(kv, "PLANE_WAVE_ANGLE", 0.f);
+    p->ts = getf(kv, "TS", 0.f);
+    const char *bad = NULL;
+    if (p->rec_topo < 0 || p->rec_topo > 1)
+        bad = "REC_TOPO needs to be 0 or 1";
+    else if (p->source_topo < 0 || p->source_topo > 1)
+        bad = "SOURCE_TOPO needs to be 0 or 1";
+    else if ((p->rec_topo || p->source_topo) && p->free_surf)
+        bad = "source or receiver topography cannot be combined with FREE_SURF";
+    else if (p->seismo > 0 && !p->readrec && p->rec_array > 0 && p->drx < 1)
+        bad = "REC_ARRAY > 0 needs DRX >= 1";
+    else if (p->srcrec != 1 && p->srcrec != 2)
+        bad = "SRCREC must be 1 (source file) or 2 (plane wave)";
+    else if (p->srcrec == 2 && p->plane_wave_depth <= 0.f)
+        bad = "SRCREC 2 (plane wave) needs PLANE_WAVE_DEPTH > 0";
+    else if (p->srcrec == 2 && p->source_shape > 4)
+        bad = "a plane wave takes SOURCE_SHAPE 1-4 only";
+    else if (p->srcrec == 2 && p->ts <= 0.f)
+        bad = "a plane wave needs TS > 0";
     free(kv);
+    if (bad) {
+        sofih_set_error("%s: %s", path, bad);
+        return 1;
+    }
     return 0;
 }

@@ -64,8 +64,8 @@ static float *transpose_xy(const float *a, int nx, int ny)
 
 /* One FWI gradient pass over the shots (inversion.c, output_gradient.c). */
 static int run_fwi(const sofih_par *p, sofi_ctx *ctx, int nsrc, const float *srcpos, const float *srcxy,
-                   const float *sig, int ntr, const int *rix, const int *riy, const float *vp, const float *vs,
-                   const float *rho)
+                   const float *sig, int ntr, const int *rix, const int *riy, const int *rtr, const float *vp,
+                   const float *vs, const float *rho)
 {
     if (p->weq != 2 || p->fwi_lnorm != 2 || p->fwi_dtinv != 1) {
         fprintf(stderr, "sofi2d_gb300: MODE = FWI needs WEQ = EL_ISO, LNORM = 2 and DTINV = 1\n");
@@ -104,8 +104,8 @@ static int run_fwi(const sofih_par *p, sofi_ctx *ctx, int nsrc, const float *src
         const int src = nshots == 1 ? 0 : s;
         for (int q = 0; q < 2; q++) { /* the forward seismograms, as the reference writes them in FWI mode */
             snprintf(path, sizeof path, "%s_%s.su.shot%d", p->seis_file, q ? "vy" : "vx", s + 1);
-            if (sofih_write_su(path, q ? cy : cx, ntr, nt, rix, riy, srcxy[src], srcxy[nsrc + src], p, s + 1,
-                               q + 1))
+            if (sofih_write_su_traces(path, q ? cy : cx, ntr, nt, rix, riy, rtr, srcxy[src], srcxy[nsrc + src], p,
+                                      s + 1, q + 1))
                 DIE_H();
         }
         double l2x = 0, l2y = 0;
@@ -177,8 +177,8 @@ int main(int argc, char **argv)
     if (p.source_shape == 3 ? sofih_wavelet_file(p.signal_file, p.nt, p.dt, nsrc, srcpos, sig)
                             : sofih_wavelet(p.source_shape, p.nt, p.dt, nsrc, srcpos, sig))
         DIE_H();
-    int *rix = NULL, *riy = NULL, ntr = 0;
-    if (p.seismo && sofih_read_receivers(&p, p.rec_file, &rix, &riy, &ntr))
+    int *rix = NULL, *riy = NULL, *rtr = NULL, ntr = 0;
+    if (p.seismo && sofih_read_receiver_traces(&p, p.rec_file, &rix, &riy, &rtr, &ntr))
         DIE_H();
     /* source wavelet files (initsrc.c:64-93): per shot, the first source of the
      * shot, at its grid position and with its coordinates */
@@ -221,7 +221,7 @@ int main(int argc, char **argv)
     if (p.mode_fwi) {
         if (ntr)
             CHECK_G(sofi_set_receivers(ctx, 0, ntr, rix, riy));
-        int rc = run_fwi(&p, ctx, nsrc, srcpos, srcxy, sig, ntr, rix, riy, vp, vs, rho);
+        int rc = run_fwi(&p, ctx, nsrc, srcpos, srcxy, sig, ntr, rix, riy, rtr, vp, vs, rho);
         sofi_destroy(ctx);
         sofih_prep_free(prep);
         printf("sofi2d_gb300: total %.3f s\n", now_s() - t0);
@@ -270,8 +270,8 @@ int main(int argc, char **argv)
                 else
                     snprintf(path, sizeof path, "%s_%s.su", p.seis_file, cn[comps[q]]);
                 int src = nshots == 1 ? 0 : s;
-                if (sofih_write_su(path, sec, ntr, ns, rix, riy, srcxy[src], srcxy[nsrc + src], &p, s + 1,
-                                   comps[q]))
+                if (sofih_write_su_traces(path, sec, ntr, ns, rix, riy, rtr, srcxy[src], srcxy[nsrc + src], &p,
+                                          s + 1, comps[q]))
                     DIE_H();
             }
         free(sec);

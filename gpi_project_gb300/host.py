@@ -33,7 +33,10 @@ class SofihPar(ctypes.Structure):
                 ("mode_fwi", ctypes.c_int), ("fwi_itermax", ctypes.c_int), ("fwi_velocity", ctypes.c_int),
                 ("fwi_adjoint", ctypes.c_int), ("fwi_lnorm", ctypes.c_int), ("fwi_dtinv", ctypes.c_int),
                 ("data_dir", ctypes.c_char * 256), ("gradient", ctypes.c_char * 256), ("readmod", ctypes.c_int),
-                ("tau", ctypes.c_float), ("signal_file", ctypes.c_char * 256)]
+                ("tau", ctypes.c_float), ("signal_file", ctypes.c_char * 256), ("rec_array", ctypes.c_int),
+                ("drx", ctypes.c_int), ("rec_array_depth", ctypes.c_float), ("rec_array_dist", ctypes.c_float),
+                ("rec_topo", ctypes.c_int), ("source_topo", ctypes.c_int), ("srcrec", ctypes.c_int),
+                ("plane_wave_depth", ctypes.c_float), ("plane_wave_angle", ctypes.c_float), ("ts", ctypes.c_float)]
 
 
 _LIB = None
@@ -70,6 +73,10 @@ def load():
         L.sofih_model_suffixes.argtypes = [ctypes.c_int, P(ctypes.c_char_p), ctypes.c_int]
         L.sofih_write_su.argtypes = [ctypes.c_char_p, fp, ctypes.c_int, ctypes.c_int, ip, ip, ctypes.c_float,
                                      ctypes.c_float, P(SofihPar), ctypes.c_int, ctypes.c_int]
+        L.sofih_write_su_traces.argtypes = [ctypes.c_char_p, fp, ctypes.c_int, ctypes.c_int, ip, ip, ip,
+                                            ctypes.c_float, ctypes.c_float, P(SofihPar), ctypes.c_int, ctypes.c_int]
+        L.sofih_read_receiver_traces.argtypes = [P(SofihPar), ctypes.c_char_p, P(ip), P(ip), P(ip), ip]
+        L.sofih_scan_topo.argtypes = [P(SofihPar), ctypes.c_char_p, ip]
         L.sofih_fwi_read_data.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, fp]
         L.sofih_fwi_residual.argtypes = [fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, fp,
                                          P(ctypes.c_double)]
@@ -191,13 +198,37 @@ def read_receivers(p: SofihPar, path: str):
     return (np.ctypeslib.as_array(ix, shape=(n,)).copy(), np.ctypeslib.as_array(iy, shape=(n,)).copy())
 
 
-def write_su(path: str, section, ix, iy, xs: float, ys: float, p: SofihPar, ishot: int = 1, comp: int = 1):
+def read_receiver_traces(p: SofihPar, path: str):
+    """(ix, iy, trace numbers) as sofih_read_receiver_traces gives them."""
+    L = load()
+    ipp = ctypes.POINTER(ctypes.c_int)
+    ix, iy, tr, n = ipp(), ipp(), ipp(), ctypes.c_int()
+    if L.sofih_read_receiver_traces(ctypes.byref(p), path.encode(), ctypes.byref(ix), ctypes.byref(iy),
+                                    ctypes.byref(tr), ctypes.byref(n)):
+        raise _err()
+    n = n.value
+    return tuple(np.ctypeslib.as_array(a, shape=(n,)).copy() for a in (ix, iy, tr))
+
+
+def scan_topo(p: SofihPar, mfile: str) -> np.ndarray:
+    """The topography row of every column (sofih_scan_topo)."""
+    topo = np.zeros(p.nx, dtype=np.int32)
+    if load().sofih_scan_topo(ctypes.byref(p), mfile.encode(), topo.ctypes.data_as(ctypes.POINTER(ctypes.c_int))):
+        raise _err()
+    return topo
+
+
+def write_su(path: str, section, ix, iy, xs: float, ys: float, p: SofihPar, ishot: int = 1, comp: int = 1,
+             trace=None):
+    """One SU file; trace: the traces' numbers (None: 1..ntr)."""
     sec = np.ascontiguousarray(section, dtype=np.float32)
     ix = np.ascontiguousarray(ix, dtype=np.int32)
     iy = np.ascontiguousarray(iy, dtype=np.int32)
     ipp = ctypes.POINTER(ctypes.c_int)
-    if load().sofih_write_su(path.encode(), _fp(sec), sec.shape[0], sec.shape[1], ix.ctypes.data_as(ipp),
-                             iy.ctypes.data_as(ipp), xs, ys, ctypes.byref(p), ishot, comp):
+    tr = None if trace is None else np.ascontiguousarray(trace, dtype=np.int32)
+    if load().sofih_write_su_traces(path.encode(), _fp(sec), sec.shape[0], sec.shape[1], ix.ctypes.data_as(ipp),
+                                    iy.ctypes.data_as(ipp), None if tr is None else tr.ctypes.data_as(ipp), xs, ys,
+                                    ctypes.byref(p), ishot, comp):
         raise _err()
 
 

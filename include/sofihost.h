@@ -59,6 +59,20 @@ typedef struct {
     int readmod;
     float tau;
     char signal_file[256];      /* SOURCE_SHAPE 3: the signal (read_srcsig.c), ASCII or SU */
+    /* receiver planes without a receiver file (REC_ARRAY > 0, receiver.c:101-116):
+     * REC_ARRAY rows at depths REC_ARRAY_DEPTH + n REC_ARRAY_DIST, every DRX-th
+     * column from FW to NX - FW */
+    int rec_array, drx;
+    float rec_array_depth, rec_array_dist;
+    /* receivers (REC_TOPO) / sources (SOURCE_TOPO) placed below the topography
+     * that sofih_scan_topo finds in MFILE.vp (acq_read.c:31-60); neither
+     * combines with FREE_SURF (read_par_json.c:425-427) */
+    int rec_topo, source_topo;
+    /* SRCREC 1: sources from SOURCE_FILE; 2: a plane wave, one source per
+     * column at PLANE_WAVE_DEPTH + x tan(PLANE_WAVE_ANGLE), centre frequency
+     * 1 / TS (sources.c:337-371) */
+    int srcrec;
+    float plane_wave_depth, plane_wave_angle, ts;
 } sofih_par;
 
 const char *sofih_last_error(void);
@@ -99,8 +113,14 @@ int sofih_holberg(int fdorder, int maxrelerror, float *hc);
 int sofih_check_cfl(const sofih_par *p, const sofih_prep *m, float *dt_max);
 
 /* ---- acquisition ---- */
+/* Topography (scan_topo.c:27-76): for each column i = 1..NX the first row
+ * j >= 2 whose P velocity differs from row 1's, 1 when none does, from
+ * MFILE.vp.su when that file exists, else MFILE.vp. topo holds NX ints. */
+int sofih_scan_topo(const sofih_par *p, const char *mfile, int *topo);
 /* Sources: srcpos [12][nsrc] row-major in grid indices (reference srcpos_loc
- * layout after splitsrc.c); xy [2][nsrc] physical coordinates. */
+ * layout after splitsrc.c); xy [2][nsrc] physical coordinates. SRCREC 2
+ * ignores path and builds the plane wave; SOURCE_TOPO 1 counts a file
+ * source's depth from the topography below its x (sources.c:122-127). */
 int sofih_read_sources(const sofih_par *p, const char *path, float **srcpos, float **xy, int *nsrc);
 /* Source signals [nsrc][nt] (wavelet.c): SOURCE_SHAPE 1 Ricker, 2 Fuchs-Mueller,
  * 4 sin^3, 5 Berlage, 6 Klauder (5 and 6 normalised to the amplitude; their
@@ -115,14 +135,26 @@ int sofih_read_signal(const char *path, float dt, float **samples, int *ns);
 /* SOURCE_SHAPE 3: every source's signal is the file's samples (zero past
  * them) times its amplitude. */
 int sofih_wavelet_file(const char *signal_file, int nt, float dt, int nsrc, const float *srcpos, float *signals);
-/* Receivers (grid indices, duplicates removed, reference receiver.c). */
+/* Receivers (grid indices, reference receiver.c:41-173): from the receiver
+ * file (READREC 1; co-located receivers after the first dropped; REC_TOPO 1:
+ * the depth counted from the column's topography), as receiver planes
+ * (REC_ARRAY > 0) or on the line XREC1..XREC2 every NGEOPH grid points; an
+ * index 0 becomes 1. */
 int sofih_read_receivers(const sofih_par *p, const char *path, int **ix, int **iy, int *ntr);
+/* The same with each receiver's trace number (recpos[3]: its place in the
+ * receiver file, which keeps the gaps of dropped co-located receivers; 1..ntr
+ * otherwise); the caller frees all three arrays. */
+int sofih_read_receiver_traces(const sofih_par *p, const char *path, int **ix, int **iy, int **trace, int *ntr);
 
 /* ---- output ---- */
 /* One SU file of a component; ep = energy source point (comp for the trace
  * header's 'ep' as outseis_glob.c writes it). xs, ys: source position [m]. */
 int sofih_write_su(const char *path, const float *section, int ntr, int ns, const int *ix, const int *iy,
                    float xs, float ys, const sofih_par *p, int ishot, int comp);
+/* The same with the traces numbered as sofih_read_receiver_traces gives them
+ * (tracl, tracr and cdp, outseis_glob.c:53-75; NULL: 1..ntr). */
+int sofih_write_su_traces(const char *path, const float *section, int ntr, int ns, const int *ix, const int *iy,
+                          const int *trace, float xs, float ys, const sofih_par *p, int ishot, int comp);
 /* The source wavelet file of initsrc.c:64-93: <SIGOUT_FILE>.shot<ishot>.<su|txt|bin>
  * holding signal[0..nt-1] as one trace (format 1 SU, 2 one value per line
  * "%e", 3 float32). (ix, iy): the source's grid position, (xs, ys) its

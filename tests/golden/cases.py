@@ -146,6 +146,37 @@ FWI_CASES = [
 ]
 
 
+# Acquisition set-ups of receiver.c / sources.c beyond a receiver file and a
+# source file: receivers and sources placed below the topography (REC_TOPO,
+# SOURCE_TOPO) with co-located receivers in the file and REFRECX; receiver
+# planes (REC_ARRAY, the first at depth 0 whose row 0 becomes 1) with a plane
+# wave of sources (SRCREC 2). `par` sets or adds parameter-file keys.
+_LINE = [[3.0 + 5.0 * k, 4.0] for k in range(10)]
+ACQ_CASES = [
+    _case("acq_topo", nx=60, ny=50, nt=250, fw=10, seismo=1, ndt=1, snap=0, seed=41, topo=True,
+          sources=[[61.0, 6.0, 0.0, 60.0, 1.0]], receivers=[[30.2, 4.0]] + _LINE[:5] + [[30.9, 4.0]] + _LINE[5:],
+          par={"REC_TOPO": "1", "SOURCE_TOPO": "1", "REFRECX": "1.0"}),
+    _case("acq_planes", nx=60, ny=50, nt=250, fw=10, seismo=1, ndt=1, snap=0, seed=42,
+          sources=[[61.0, 61.0, 0.0, 60.0, 1.0]],
+          par={"READREC": "0", "XREC1": "10.0", "XREC2": "100.0", "YREC1": "10.0", "YREC2": "10.0",
+               "REC_ARRAY": "3", "DRX": "7", "REC_ARRAY_DEPTH": "0.0", "REC_ARRAY_DIST": "9.0"}),
+]
+# A plane wave of sources (SRCREC 2). The compiled reference builds it
+# (sources.c:337-367) into a source matrix of 8 rows and then reads rows 9-11
+# of it in splitsrc.c:50-51, past the allocation, and crashes there; its log's
+# source table (sources.c:386-404, printed before the crash, two decimals) is
+# what pins the positions.
+PLANE_WAVE_CASE = _case("acq_plane_wave", nx=60, ny=50, nt=250, fw=10, seismo=1, ndt=1, snap=0, seed=43,
+                        par={"SRCREC": "2", "PLANE_WAVE_DEPTH": "20.0", "PLANE_WAVE_ANGLE": "12.0", "TS": "0.025",
+                             "LOG_VERBOSITY": "INFO"})
+
+
+def topo_rows(case):
+    """Rows of the constant low-velocity cover over each column of a case
+    with topography (the scan finds the row below them)."""
+    return 5 + (np.arange(case["nx"]) * 3) % 9
+
+
 def _smooth(a, w=7):
     """Separable moving average over w cells (edges replicated), as float32."""
     k = np.ones(w) / w
@@ -167,6 +198,9 @@ def synthetic_model(case) -> dict:
     vp = (vp1[None, :] * pert).astype(np.float32)
     vs = (vp / 1.73).astype(np.float32)
     rho = (rho1[None, :] * (1.0 + 0.02 * rng.standard_normal((nx, ny)))).astype(np.float32)
+    if case.get("topo"):
+        cover = np.arange(ny)[None, :] < topo_rows(case)[:, None]
+        vp[cover], vs[cover], rho[cover] = 1600.0, 925.0, 1800.0
     mats = {"vp": vp, "vs": vs, "rho": rho}
     weq = case["weq"]
     if weq in (4, 5, 6, 7):
@@ -234,6 +268,21 @@ def json_text(case) -> str:
     return "\n".join(lines + ["}"]) + "\n"
 
 
+def acq_json_text(case) -> str:
+    """json_text with the keys of case['par'] set, or added where json_text has none."""
+    lines = json_text(case).rstrip().splitlines()
+    par = dict(case.get("par", {}))
+    out = []
+    for ln in lines[1:-1]:
+        key = ln.split('"')[1]
+        if key in par:
+            ln = f'"{key}" : "{par.pop(key)}",'
+        out.append(ln.rstrip(",") + ",")
+    out += [f'"{k}" : "{v}",' for k, v in par.items()]
+    out[-1] = out[-1].rstrip(",")
+    return "\n".join(["{"] + out + ["}"]) + "\n"
+
+
 def write_case(case, work):
     os.makedirs(os.path.join(work, "model"), exist_ok=True)
     os.makedirs(os.path.join(work, "out"), exist_ok=True)
@@ -249,7 +298,7 @@ def write_case(case, work):
             fh.write(f"{r[0]!r} {r[1]!r}\n")
     jpath = os.path.join(work, "case.json")
     with open(jpath, "w") as fh:
-        fh.write(json_text(case))
+        fh.write(acq_json_text(case) if case.get("par") else json_text(case))
     return jpath, mats
 
 

@@ -10,7 +10,9 @@ Two kinds of fixture, both small enough to commit:
   synthetic cases that the shipped files do not cover: CPML, FDORDER 2-12,
   MAXRELERROR 1-4, free surface (elastic and viscoelastic), L = 3, VTI/TTI with
   CPML, periodic x, force / custom-force / moment-tensor sources and ragged
-  grid sizes. Models are regenerated from the seed by ``synthetic_model`` (a
+  grid sizes; and the acquisition set-ups of ACQ_CASES (receiver planes,
+  receivers and sources below the topography, co-located receivers) and the
+  plane wave's source table (``ref_acq_plane_wave.npz``). Models are regenerated from the seed by ``synthetic_model`` (a
   CRC of the model bytes is stored to catch a drift).
 
     python tests/golden/make_fixtures.py [--reference <reference source tree>]
@@ -31,8 +33,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
-from tests.golden.cases import (CASES, FWI_CASES, WAVELET_CASES, WAVELET_DT, WAVELET_NT, _case, fwi_json_text,  # noqa: E402
-                                json_text, synthetic_model, true_model, write_case, write_signal_file)
+from tests.golden.cases import (ACQ_CASES, CASES, FWI_CASES, PLANE_WAVE_CASE, WAVELET_CASES, WAVELET_DT,  # noqa: E402
+                                WAVELET_NT, _case, fwi_json_text, json_text, synthetic_model, true_model,
+                                write_case, write_signal_file)
 
 SHIPPED = {"weq3": "EL_ISO", "weq4": "VEL_ISO", "weq5": "EL_VTI", "weq6": "VEL_VTI", "weq7": "EL_TTI",
            "weq8": "VEL_TTI", "weq3_fy": "EL_ISO", "weq8_fy": "VEL_TTI", "weq3_fdt4": "EL_ISO",
@@ -170,6 +173,30 @@ def ref_wavelets(exe):
     np.savez_compressed(os.path.join(HERE, "ref_wavelets.npz"), **out)
 
 
+def ref_plane_wave(exe):
+    """The plane-wave sources as the compiled reference logs them: it builds
+    them and prints its source table, then crashes reading past its 8-row
+    source matrix (splitsrc.c:50-51). ref_acq_plane_wave.npz holds the table
+    (shot, x, y, tshift, fc, amp, azimuth, type) of the first 50 sources."""
+    case = PLANE_WAVE_CASE
+    work = tempfile.mkdtemp(prefix="sofi_pw_")
+    try:
+        jpath, _ = write_case(case, work)
+        r = subprocess.run([exe, jpath], cwd=work, capture_output=True, text=True)
+        assert r.returncode != 0, "the reference's plane-wave path ran through: read its seismograms instead"
+        rows = []
+        for ln in r.stdout.splitlines():
+            t = ln.split("]", 1)[-1].split()
+            if ln.startswith("INFO") and len(t) == 8 and t[0].isdigit():
+                rows.append([float(v) for v in t])
+        assert len(rows) == 50, len(rows)
+        np.savez_compressed(os.path.join(HERE, "ref_acq_plane_wave.npz"), table=np.array(rows),
+                            case=np.frombuffer(json.dumps(case, sort_keys=True).encode(), dtype=np.uint8))
+        print("wrote acq_plane_wave", len(rows), "sources; the reference exited with", r.returncode)
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+
+
 def run_reference_fwi(case, exe):
     """Observed data from a forward run on the case's true model, then one
     FWI gradient pass on its model (MODE = FWI), both with the compiled
@@ -238,6 +265,16 @@ def main():
         ref_wavelets(exe)
         if a.only:
             return
+    if not a.only or a.only == "acq_plane_wave":
+        ref_plane_wave(exe)
+        if a.only:
+            return
+    for case in ACQ_CASES:  # receiver planes, topography, co-located receivers
+        if a.only and case["name"] != a.only:
+            continue
+        out = run_reference(case, exe)
+        np.savez_compressed(os.path.join(HERE, f"ref_{case['name']}.npz"), **out)
+        print("wrote", case["name"], out["hdr_vx"].shape)
     for case in FWI_CASES:
         if a.only and case["name"] != a.only:
             continue

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from tests.golden.cases import CASES, WAVELET_CASES, WAVELET_DT, WAVELET_NT, synthetic_model, write_signal_file
-from tests.helpers import case_config, prepared_model, GOLDEN
+from tests.helpers import case_config, prepared_model, rel_max, GOLDEN
 
 
 @pytest.fixture(scope="module")
@@ -250,3 +250,97 @@ def test_parameter_file_fdorder_time_and_fwi_keys(tmp_path):
     assert (p.mode_fwi, p.fwi_velocity, p.fwi_adjoint, p.fwi_lnorm, p.fwi_dtinv) == (
         1, case["velocity"], case["adjoint_type"], 2, 1)
     assert p.data_dir.decode() == "./obs/seis" and p.gradient.decode() == "./grad/g"
+
+
+@pytest.mark.parametrize("name", ["acq_topo", "acq_planes"])
+def test_acquisition_matches_compiled_reference(H, name, tmp_path, oracle_mod):
+    """Receivers and sources as the compiled reference's receiver.c / sources.c
+    place them: below the topography of the P-wave model (REC_TOPO,
+    SOURCE_TOPO), with a co-located receiver of the file dropped and its trace
+    number left out, with REFRECX, and as receiver planes (REC_ARRAY) whose
+    first row 0 becomes 1. The oracle run on the host library's acquisition
+    reproduces the reference's seismograms, and the SU file written with the
+    host's receivers, trace numbers and source position carries the
+    reference's trace headers byte for byte."""
+    from tests.golden.cases import ACQ_CASES, write_case
+    O = oracle_mod
+    case = next(c for c in ACQ_CASES if c["name"] == name)
+    g = np.load(os.path.join(GOLDEN, f"ref_{name}.npz"))
+    write_case(case, str(tmp_path))
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        p = H.read_par("case.json")
+        sp, xy = H.read_sources(p, p.source_file.decode())
+        ix, iy, tr = H.read_receiver_traces(p, p.rec_file.decode())
+        np.testing.assert_array_equal(H.read_receivers(p, p.rec_file.decode())[0], ix)
+    finally:
+        os.chdir(cwd)
+    assert len(ix) == g["hdr_vx"].shape[0]
+    cfg = case_config(case)
+    o = O.Oracle(cfg, "f32", os.cpu_count() or 1)
+    o.set_material(synthetic_model(case))
+    o.set_sources(sp, H.wavelet(p.source_shape, cfg.nt, cfg.dt, sp))
+    o.set_receivers(ix, iy)
+    o.run()
+    for comp in ("vx", "vy"):
+        a, b = o.section(comp), g[f"seis_{comp}"]
+        assert np.abs(b).max() > 0
+        assert rel_max(a, b, floor=1e-30) < 1e-5, (name, comp, rel_max(a, b, floor=1e-30))
+    out = str(tmp_path / "x.su")
+    H.write_su(out, o.section("vx"), ix, iy, xy[0, 0], xy[1, 0], p, 1, 1, trace=tr)
+    rec = 240 + 4 * g["seis_vx"].shape[1]
+    np.testing.assert_array_equal(np.fromfile(out, np.uint8).reshape(-1, rec)[:, :240], g["hdr_vx"])
+    o.close()
+
+
+def test_topography_scan(H, tmp_path):
+    """sofih_scan_topo: the first row whose P velocity differs from the top
+    row's, per column, from the binary model and from the SU model."""
+    from tests.golden.cases import ACQ_CASES, topo_rows, write_case
+    case = ACQ_CASES[0]
+    write_case(case, str(tmp_path))
+    p = H.read_par(str(tmp_path / "case.json"))
+    want = topo_rows(case) + 1
+    np.testing.assert_array_equal(H.scan_topo(p, str(tmp_path / "model" / "m")), want)
+    vp = np.fromfile(tmp_path / "model" / "m.vp", np.float32).reshape(case["nx"], case["ny"])
+    H.write_su(str(tmp_path / "model" / "s.vp.su"), vp, np.arange(1, case["nx"] + 1), np.ones(case["nx"]), 0.0,
+               0.0, p)
+    np.testing.assert_array_equal(H.scan_topo(p, str(tmp_path / "model" / "s")), want)
+
+
+def test_plane_wave_sources_match_reference_log(H, tmp_path):
+    """SRCREC 2: one source per column at PLANE_WAVE_DEPTH + x tan(angle),
+    no time shift, centre frequency 1 / TS, unit amplitude (sources.c:337-367).
+    The compiled reference logs its source table (two decimals) before it
+    crashes reading past its 8-row source matrix; the host's sources equal
+    that table."""
+    from tests.golden.cases import PLANE_WAVE_CASE, write_case
+    g = np.load(os.path.join(GOLDEN, "ref_acq_plane_wave.npz"))["table"]
+    write_case(PLANE_WAVE_CASE, str(tmp_path))
+    p = H.read_par(str(tmp_path / "case.json"))
+    assert p.srcrec == 2
+    sp, xy = H.read_sources(p, "unused")
+    assert sp.shape == (12, PLANE_WAVE_CASE["nx"])
+    n = g.shape[0]
+    np.testing.assert_allclose(xy[0, :n], g[:, 1], atol=0.006)
+    np.testing.assert_allclose(xy[1, :n], g[:, 2], atol=0.006)
+    for row, col in ((3, 3), (4, 4), (5, 5), (6, 6), (7, 7)):  # tshift, fc, amp, azimuth, type
+        np.testing.assert_allclose(sp[row, :n], g[:, col], atol=0.006)
+    dh = np.float32(p.dh)
+    np.testing.assert_array_equal(sp[1], np.floor(xy[1] / dh) + 1)
+
+
+@pytest.mark.parametrize("par,msg", [({"REC_TOPO": "1", "FREE_SURF": "1"}, "FREE_SURF"),
+                                     ({"SOURCE_TOPO": "2"}, "SOURCE_TOPO"),
+                                     ({"READREC": "0", "REC_ARRAY": "2"}, "DRX"),
+                                     ({"SRCREC": "2", "PLANE_WAVE_DEPTH": "0.0"}, "PLANE_WAVE_DEPTH"),
+                                     ({"SRCREC": "2", "PLANE_WAVE_DEPTH": "5.0", "SOURCE_SHAPE": "5"},
+                                      "SOURCE_SHAPE")])
+def test_acquisition_settings_the_reference_rejects(H, tmp_path, par, msg):
+    """The combinations read_par_json.c / sources.c stop on are errors here too."""
+    from tests.golden.cases import _case, write_case
+    case = _case("bad", nx=40, ny=40, nt=10, fw=5, seismo=1, ndt=1, snap=0, seed=5, par=par)
+    write_case(case, str(tmp_path))
+    with pytest.raises(Exception, match=msg):
+        H.read_par(str(tmp_path / "case.json"))
