@@ -692,6 +692,15 @@ int sofih_write_su(const char *path, const float *section, int ntr, int ns, cons
     return write_su_traces(path, section, ntr, ns, ix, iy, NULL, xs, ys, p, ishot);
 }
 
+int sofih_snapshot_shots(const sofih_par *p, int nshots, int *shots)
+{
+    int n = 0;
+    for (int s = 1; s <= nshots && p->snap > 0 && p->snapshot_incr > 0; s++)
+        if ((s - p->snapshot_start) % p->snapshot_incr == 0 && s <= p->snapshot_start)
+            shots[n++] = s;
+    return n;
+}
+
 int sofih_write_su_traces(const char *path, const float *section, int ntr, int ns, const int *ix, const int *iy,
                           const int *trace, float xs, float ys, const sofih_par *p, int ishot, int comp)
 {

@@ -213,6 +213,8 @@ int sofih_read_par(const char *path, sofih_par *p)
     p->source_topo = p->srcrec == 1 ? geti(kv, "SOURCE_TOPO", 0) : 0;
     p->plane_wave_depth = getf(kv, "PLANE_WAVE_DEPTH", 0.f), p->plane_wave_angle = getf(kv, "PLANE_WAVE_ANGLE", 0.f);
     p->ts = getf(kv, "TS", 0.f);
+    p->snapshot_start = geti(kv, "SNAPSHOT_START", 1), p->snapshot_end = geti(kv, "SNAPSHOT_END", -9999);
+    p->snapshot_incr = geti(kv, "SNAPSHOT_INCR", 1);
     const char *bad = NULL;
     if (p->rec_topo < 0 || p->rec_topo > 1)
         bad = "REC_TOPO needs to be 0 or 1";
@@ -230,6 +232,8 @@ int sofih_read_par(const char *path, sofih_par *p)
         bad = "a plane wave takes SOURCE_SHAPE 1-4 only";
     else if (p->srcrec == 2 && p->ts <= 0.f)
         bad = "a plane wave needs TS > 0";
+    else if (p->snap > 0 && p->snapshot_incr < 1)
+        bad = "SNAPSHOT_INCR must be at least 1";
     free(kv);
     if (bad) {
         sofih_set_error("%s: %s", path, bad);

@@ -276,10 +276,12 @@ int main(int argc, char **argv)
             }
         free(sec);
     }
-    /* snapshots of the first shot (initsrc.c:96-98) */
+    /* snapshots: the frames of every shot that writes them, shot after shot (initsrc.c:96-98) */
     int nsnap = 0, fsz = 0;
     sofi_num_snapshots(ctx, &nsnap, &fsz);
-    if (nsnap) {
+    int *snap_shots = (int *)malloc(sizeof(int) * (size_t)nshots);
+    const int nss = snap_shots ? sofih_snapshot_shots(&p, nshots, snap_shots) : 0;
+    if (nsnap && nss) {
         float *frame = (float *)malloc(sizeof(float) * (size_t)fsz);
         const char *cn[6] = {0, "vx", "vy", "p", "div", "curl"};
         for (int comp = 1; comp <= 5; comp++) {
@@ -289,11 +291,12 @@ int main(int argc, char **argv)
                 continue;
             char path[700];
             snprintf(path, sizeof path, "%s.bin.%s", p.snap_file, cn[comp]);
-            for (int k = 0; k < nsnap; k++) {
-                CHECK_G(sofi_get_snapshot(ctx, 0, k, comp, frame));
-                if (sofih_write_snap(path, frame, fsz, k > 0))
-                    DIE_H();
-            }
+            for (int q = 0; q < nss; q++)
+                for (int k = 0; k < nsnap; k++) {
+                    CHECK_G(sofi_get_snapshot(ctx, snap_shots[q] - 1, k, comp, frame));
+                    if (sofih_write_snap(path, frame, fsz, q > 0 || k > 0))
+                        DIE_H();
+                }
         }
         free(frame);
     }

@@ -36,7 +36,8 @@ class SofihPar(ctypes.Structure):
                 ("tau", ctypes.c_float), ("signal_file", ctypes.c_char * 256), ("rec_array", ctypes.c_int),
                 ("drx", ctypes.c_int), ("rec_array_depth", ctypes.c_float), ("rec_array_dist", ctypes.c_float),
                 ("rec_topo", ctypes.c_int), ("source_topo", ctypes.c_int), ("srcrec", ctypes.c_int),
-                ("plane_wave_depth", ctypes.c_float), ("plane_wave_angle", ctypes.c_float), ("ts", ctypes.c_float)]
+                ("plane_wave_depth", ctypes.c_float), ("plane_wave_angle", ctypes.c_float), ("ts", ctypes.c_float),
+                ("snapshot_start", ctypes.c_int), ("snapshot_end", ctypes.c_int), ("snapshot_incr", ctypes.c_int)]
 
 
 _LIB = None
@@ -77,6 +78,7 @@ def load():
                                             ctypes.c_float, ctypes.c_float, P(SofihPar), ctypes.c_int, ctypes.c_int]
         L.sofih_read_receiver_traces.argtypes = [P(SofihPar), ctypes.c_char_p, P(ip), P(ip), P(ip), ip]
         L.sofih_scan_topo.argtypes = [P(SofihPar), ctypes.c_char_p, ip]
+        L.sofih_snapshot_shots.argtypes = [P(SofihPar), ctypes.c_int, ip]
         L.sofih_fwi_read_data.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, fp]
         L.sofih_fwi_residual.argtypes = [fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, fp,
                                          P(ctypes.c_double)]
@@ -216,6 +218,13 @@ def scan_topo(p: SofihPar, mfile: str) -> np.ndarray:
     if load().sofih_scan_topo(ctypes.byref(p), mfile.encode(), topo.ctypes.data_as(ctypes.POINTER(ctypes.c_int))):
         raise _err()
     return topo
+
+
+def snapshot_shots(p: SofihPar, nshots: int) -> list:
+    """The 1-based shots whose snapshots the files hold, in order, after nshots shots."""
+    out = np.zeros(max(nshots, 1), dtype=np.int32)
+    n = load().sofih_snapshot_shots(ctypes.byref(p), nshots, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return [int(v) for v in out[:n]]
 
 
 def write_su(path: str, section, ix, iy, xs: float, ys: float, p: SofihPar, ishot: int = 1, comp: int = 1,

@@ -73,6 +73,8 @@ typedef struct {
      * 1 / TS (sources.c:337-371) */
     int srcrec;
     float plane_wave_depth, plane_wave_angle, ts;
+    /* the shots that write snapshots (SNAPSHOT_START / _END / _INCR, read_par_json.c:320-330) */
+    int snapshot_start, snapshot_end, snapshot_incr;
 } sofih_par;
 
 const char *sofih_last_error(void);
@@ -147,6 +149,14 @@ int sofih_read_receivers(const sofih_par *p, const char *path, int **ix, int **i
 int sofih_read_receiver_traces(const sofih_par *p, const char *path, int **ix, int **iy, int **trace, int *ntr);
 
 /* ---- output ---- */
+/* The shots (1-based, in order) whose snapshots the snapshot files hold
+ * after a run of nshots shots; returns their count (shots holds nshots ints).
+ * initsrc.c:96-98 lets shot s write snapshots when SNAP is set,
+ * (s - SNAPSHOT_START) is a multiple of SNAPSHOT_INCR and s <= SNAPSHOT_START;
+ * time_loop.c:36 numbers snapshots across shots, so only the very first
+ * truncates the files (snap_ssg.c:78-83) and each such shot's frames follow
+ * the previous shot's. */
+int sofih_snapshot_shots(const sofih_par *p, int nshots, int *shots);
 /* One SU file of a component; ep = energy source point (comp for the trace
  * header's 'ep' as outseis_glob.c writes it). xs, ys: source position [m]. */
 int sofih_write_su(const char *path, const float *section, int ntr, int ns, const int *ix, const int *iy,

@@ -161,6 +161,12 @@ ACQ_CASES = [
           par={"READREC": "0", "XREC1": "10.0", "XREC2": "100.0", "YREC1": "10.0", "YREC2": "10.0",
                "REC_ARRAY": "3", "DRX": "7", "REC_ARRAY_DEPTH": "0.0", "REC_ARRAY_DIST": "9.0"}),
 ]
+# Three shots (RUN_MULTIPLE_SHOTS 1) of which shots 1 and 2 write snapshots
+# (SNAPSHOT_START 2): the files hold shot 1's frames, then shot 2's.
+SNAP_SHOTS_CASE = _case("snap_shots", nx=60, ny=50, nt=250, fw=10, seismo=1, ndt=1, snap=1, tsnap=0.03, idx=1, idy=1,
+                        seed=44, sources=[[31.0, 31.0, 0.0, 60.0, 1.0], [61.0, 41.0, 0.0, 60.0, 1.0],
+                                          [91.0, 61.0, 0.0, 60.0, 1.0]],
+                        par={"RUN_MULTIPLE_SHOTS": "1", "SNAPSHOT_START": "2", "SNAPSHOT_INCR": "1"})
 # A plane wave of sources (SRCREC 2). The compiled reference builds it
 # (sources.c:337-367) into a source matrix of 8 rows and then reads rows 9-11
 # of it in splitsrc.c:50-51, past the allocation, and crashes there; its log's

@@ -33,9 +33,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
-from tests.golden.cases import (ACQ_CASES, CASES, FWI_CASES, PLANE_WAVE_CASE, WAVELET_CASES, WAVELET_DT,  # noqa: E402
-                                WAVELET_NT, _case, fwi_json_text, json_text, synthetic_model, true_model,
-                                write_case, write_signal_file)
+from tests.golden.cases import (ACQ_CASES, CASES, FWI_CASES, PLANE_WAVE_CASE, SNAP_SHOTS_CASE,  # noqa: E402
+                                WAVELET_CASES, WAVELET_DT, WAVELET_NT, _case, fwi_json_text, json_text,
+                                synthetic_model, true_model, write_case, write_signal_file)
 
 SHIPPED = {"weq3": "EL_ISO", "weq4": "VEL_ISO", "weq5": "EL_VTI", "weq6": "VEL_VTI", "weq7": "EL_TTI",
            "weq8": "VEL_TTI", "weq3_fy": "EL_ISO", "weq8_fy": "VEL_TTI", "weq3_fdt4": "EL_ISO",
@@ -267,6 +267,12 @@ def main():
             return
     if not a.only or a.only == "acq_plane_wave":
         ref_plane_wave(exe)
+        if a.only:
+            return
+    if not a.only or a.only == SNAP_SHOTS_CASE["name"]:  # which shot's snapshots the files keep
+        out = run_reference(SNAP_SHOTS_CASE, exe)
+        np.savez_compressed(os.path.join(HERE, f"ref_{SNAP_SHOTS_CASE['name']}.npz"), **out)
+        print("wrote", SNAP_SHOTS_CASE["name"], sorted(k for k in out if k.startswith("snap")))
         if a.only:
             return
     for case in ACQ_CASES:  # receiver planes, topography, co-located receivers

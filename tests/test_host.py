@@ -344,3 +344,45 @@ def test_acquisition_settings_the_reference_rejects(H, tmp_path, par, msg):
     write_case(case, str(tmp_path))
     with pytest.raises(Exception, match=msg):
         H.read_par(str(tmp_path / "case.json"))
+
+
+def test_snapshot_files_hold_every_snapshotting_shot(H, tmp_path, oracle_mod):
+    """Several shots (RUN_MULTIPLE_SHOTS 1): the reference numbers snapshots
+    across shots (time_loop.c:36), so the files hold the frames of every shot
+    that initsrc.c lets write them, one shot after the other (shots 1 and 2 of
+    3 with SNAPSHOT_START 2). The compiled reference's files equal the
+    oracle's snapshots of those shots run alone, concatenated, and
+    sofih_snapshot_shots names them; the rule's other cases follow
+    initsrc.c:96 as written."""
+    from tests.golden.cases import SNAP_SHOTS_CASE, write_case
+    from tests.helpers import case_receivers, case_sources
+    O = oracle_mod
+    case = SNAP_SHOTS_CASE
+    g = np.load(os.path.join(GOLDEN, f"ref_{case['name']}.npz"))
+    write_case(case, str(tmp_path))
+    p = H.read_par(str(tmp_path / "case.json"))
+    shots = H.snapshot_shots(p, 3)
+    assert shots == [1, 2]
+    cfg = case_config(case)
+    frames = {"vx": [], "vy": []}
+    for s in shots:
+        one = dict(case, sources=[case["sources"][s - 1]])
+        o = O.Oracle(cfg, "f32", os.cpu_count() or 1)
+        o.set_material(synthetic_model(case))
+        sp = case_sources(one, cfg)
+        o.set_sources(sp, O.wavelet(1, cfg.nt, cfg.dt, sp))
+        o.set_receivers(*case_receivers(one, cfg))
+        o.run()
+        for c in frames:
+            frames[c].append(o.snapshots(c).reshape(-1))
+        o.close()
+    for c, f in frames.items():
+        a = np.concatenate(f)
+        assert a.shape == g[f"snap_{c}"].shape
+        assert rel_max(a, g[f"snap_{c}"], floor=1e-30) < 1e-5, c
+    for start, incr, n, want in [(1, 1, 3, [1]), (3, 1, 2, [1, 2]), (3, 2, 3, [1, 3]), (2, 2, 3, [2]),
+                                 (4, 2, 3, [2]), (2, 3, 1, [])]:
+        p.snapshot_start, p.snapshot_incr = start, incr
+        assert H.snapshot_shots(p, n) == want, (start, incr, n)
+    p.snap = 0
+    assert H.snapshot_shots(p, 3) == []
