@@ -740,6 +740,71 @@ int sofih_write_signal(const sofih_par *p, int ishot, const float *signal, int n
     return 0;
 }
 
+int sofih_write_snap_format(const char *path, const float *frame, int n, int append, int format)
+{
+    if (format == 3)
+        return sofih_write_snap(path, frame, n, append);
+    if (format != 2) {
+        sofih_set_error(format == 1 ? "SNAP_FORMAT 1: the SU format for snapshots is not implemented (nor by "
+                                      "the reference)"
+                                    : "unknown SNAP_FORMAT %d",
+                        format);
+        return 1;
+    }
+    FILE *fp = fopen(path, append ? "a" : "w");
+    if (!fp) {
+        sofih_set_error("cannot write %s", path);
+        return 1;
+    }
+    int bad = 0;
+    for (int k = 0; k < n && !bad; k++)
+        bad = fprintf(fp, "%e\n", frame[k]) < 0;
+    bad |= fclose(fp) != 0;
+    if (bad)
+        sofih_set_error("short write on %s", path);
+    return bad;
+}
+
+const char *sofih_seis_ext(int format)
+{
+    switch (format) {
+      case 1:
+          return "su";
+      case 2:
+          return "txt";
+      case 3:
+          return "bin";
+      case 0:
+      case 4:
+      case 5:
+          return "sgy";
+    }
+    return NULL;
+}
+
+int sofih_write_seis(const char *path, const float *section, int ntr, int ns, const int *ix, const int *iy,
+                     const int *trace, float xs, float ys, const sofih_par *p, int ishot, int comp)
+{
+    if (p->seis_format == 1)
+        return sofih_write_su_traces(path, section, ntr, ns, ix, iy, trace, xs, ys, p, ishot, comp);
+    FILE *fp = fopen(path, p->seis_format == 2 ? "w" : "wb");
+    if (!fp) {
+        sofih_set_error("cannot write %s", path);
+        return 1;
+    }
+    int bad = 0;
+    const size_t n = (size_t)ntr * (size_t)ns;
+    if (p->seis_format == 2)
+        for (size_t k = 0; k < n && !bad; k++)
+            bad = fprintf(fp, "%e\n", section[k]) < 0;
+    else if (p->seis_format == 3)
+        bad = fwrite(section, sizeof(float), n, fp) != n;
+    bad |= fclose(fp) != 0;
+    if (bad)
+        sofih_set_error("short write on %s", path);
+    return bad;
+}
+
 int sofih_write_snap(const char *path, const float *frame, int n, int append)
 {
     FILE *fp = fopen(path, append ? "ab" : "wb");

@@ -234,6 +234,12 @@ int sofih_read_par(const char *path, sofih_par *p)
         bad = "a plane wave needs TS > 0";
     else if (p->snap > 0 && p->snapshot_incr < 1)
         bad = "SNAPSHOT_INCR must be at least 1";
+    else if (p->snap > 0 && p->snap_format != 2 && p->snap_format != 3)
+        bad = p->snap_format == 1 ? "SNAP_FORMAT 1: the SU format for snapshots is not implemented (nor by the "
+                                    "reference); SNAP_FORMAT 2 (ASCII) or 3 (binary)"
+                                  : "SNAP_FORMAT must be 2 (ASCII) or 3 (binary)";
+    else if (p->seismo > 0 && (p->seis_format < 0 || p->seis_format > 5))
+        bad = "SEIS_FORMAT must be 0-5 (1 SU, 2 ASCII, 3 binary; 0, 4 and 5 write empty .sgy files)";
     free(kv);
     if (bad) {
         sofih_set_error("%s: %s", path, bad);

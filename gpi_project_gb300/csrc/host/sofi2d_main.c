@@ -103,9 +103,10 @@ static int run_fwi(const sofih_par *p, sofi_ctx *ctx, int nsrc, const float *src
         char path[700];
         const int src = nshots == 1 ? 0 : s;
         for (int q = 0; q < 2; q++) { /* the forward seismograms, as the reference writes them in FWI mode */
-            snprintf(path, sizeof path, "%s_%s.su.shot%d", p->seis_file, q ? "vy" : "vx", s + 1);
-            if (sofih_write_su_traces(path, q ? cy : cx, ntr, nt, rix, riy, rtr, srcxy[src], srcxy[nsrc + src], p,
-                                      s + 1, q + 1))
+            snprintf(path, sizeof path, "%s_%s.%s.shot%d", p->seis_file, q ? "vy" : "vx",
+                     sofih_seis_ext(p->seis_format), s + 1);
+            if (sofih_write_seis(path, q ? cy : cx, ntr, nt, rix, riy, rtr, srcxy[src], srcxy[nsrc + src], p, s + 1,
+                                 q + 1))
                 DIE_H();
         }
         double l2x = 0, l2y = 0;
@@ -265,13 +266,14 @@ int main(int argc, char **argv)
             for (int q = 0; q < nc; q++) {
                 CHECK_G(sofi_get_section(ctx, s, comps[q], sec));
                 char path[700];
+                const char *ext = sofih_seis_ext(p.seis_format);
                 if (p.run_multiple_shots)
-                    snprintf(path, sizeof path, "%s_%s.su.shot%d", p.seis_file, cn[comps[q]], s + 1);
+                    snprintf(path, sizeof path, "%s_%s.%s.shot%d", p.seis_file, cn[comps[q]], ext, s + 1);
                 else
-                    snprintf(path, sizeof path, "%s_%s.su", p.seis_file, cn[comps[q]]);
+                    snprintf(path, sizeof path, "%s_%s.%s", p.seis_file, cn[comps[q]], ext);
                 int src = nshots == 1 ? 0 : s;
-                if (sofih_write_su_traces(path, sec, ntr, ns, rix, riy, rtr, srcxy[src], srcxy[nsrc + src], &p,
-                                          s + 1, comps[q]))
+                if (sofih_write_seis(path, sec, ntr, ns, rix, riy, rtr, srcxy[src], srcxy[nsrc + src], &p, s + 1,
+                                     comps[q]))
                     DIE_H();
             }
         free(sec);
@@ -290,11 +292,11 @@ int main(int argc, char **argv)
             if (!want)
                 continue;
             char path[700];
-            snprintf(path, sizeof path, "%s.bin.%s", p.snap_file, cn[comp]);
+            snprintf(path, sizeof path, "%s.%s.%s", p.snap_file, p.snap_format == 2 ? "asc" : "bin", cn[comp]);
             for (int q = 0; q < nss; q++)
                 for (int k = 0; k < nsnap; k++) {
                     CHECK_G(sofi_get_snapshot(ctx, snap_shots[q] - 1, k, comp, frame));
-                    if (sofih_write_snap(path, frame, fsz, q > 0 || k > 0))
+                    if (sofih_write_snap_format(path, frame, fsz, q > 0 || k > 0, p.snap_format))
                         DIE_H();
                 }
         }

@@ -161,11 +161,17 @@ static void write_snapshots(GlobVar *gv)
                 continue;
             GPU_CHECK(sofi_get_snapshot(g_ctx, 0, k, comp, frame));
             char path[STRING_SIZE * 2];
-            snprintf(path, sizeof path, "%s.bin.%s.%i.%i", gv->SNAP_FILE, names[comp], gv->POS[1], gv->POS[2]);
+            const int ascii = gv->SNAP_FORMAT == 2; /* snap_ssg.c:53-63, writedsk.c:36-52 */
+            snprintf(path, sizeof path, "%s.%s.%s.%i.%i", gv->SNAP_FILE, ascii ? "asc" : "bin", names[comp],
+                     gv->POS[1], gv->POS[2]);
             FILE *fp = fopen(path, g_nsnap_files == 1 ? "w" : "a");
             if (!fp)
                 log_fatal("cannot open snapshot file %s\n", path);
-            fwrite(frame, sizeof(float), (size_t)fs, fp);
+            if (ascii)
+                for (int q = 0; q < fs; q++)
+                    fprintf(fp, "%e\n", frame[q]);
+            else
+                fwrite(frame, sizeof(float), (size_t)fs, fp);
             fclose(fp);
         }
     }
@@ -216,8 +222,8 @@ void time_loop(int iter, int ishot, int snapcheck, float *hc, float **srcpos_loc
         log_fatal("GPU time loop: FDORDER_TIME must be 2 or 4\n");
     if (gv->NPROCX != 1 || gv->NPROCY != 1)
         log_fatal("GPU time loop: run one domain (NPROCX = NPROCY = 1); the GPU holds the whole grid\n");
-    if (gv->FW > 0 && gv->ABS_TYPE == 2 && gv->SNAP && gv->SNAP_FORMAT != 3)
-        log_fatal("GPU time loop: snapshots need SNAP_FORMAT=3\n");
+    if (gv->SNAP && snapcheck && gv->SNAP_FORMAT != 2 && gv->SNAP_FORMAT != 3)
+        log_fatal("Sorry, SU format for snapshots not implemented.\n"); /* writedsk.c:40 */
 
     sofi_config c;
     memset(&c, 0, sizeof c);

@@ -79,6 +79,11 @@ def load():
         L.sofih_read_receiver_traces.argtypes = [P(SofihPar), ctypes.c_char_p, P(ip), P(ip), P(ip), ip]
         L.sofih_scan_topo.argtypes = [P(SofihPar), ctypes.c_char_p, ip]
         L.sofih_snapshot_shots.argtypes = [P(SofihPar), ctypes.c_int, ip]
+        L.sofih_write_snap_format.argtypes = [ctypes.c_char_p, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.sofih_seis_ext.argtypes = [ctypes.c_int]
+        L.sofih_seis_ext.restype = ctypes.c_char_p
+        L.sofih_write_seis.argtypes = [ctypes.c_char_p, fp, ctypes.c_int, ctypes.c_int, ip, ip, ip, ctypes.c_float,
+                                       ctypes.c_float, P(SofihPar), ctypes.c_int, ctypes.c_int]
         L.sofih_fwi_read_data.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, fp]
         L.sofih_fwi_residual.argtypes = [fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, fp,
                                          P(ctypes.c_double)]
@@ -218,6 +223,32 @@ def scan_topo(p: SofihPar, mfile: str) -> np.ndarray:
     if load().sofih_scan_topo(ctypes.byref(p), mfile.encode(), topo.ctypes.data_as(ctypes.POINTER(ctypes.c_int))):
         raise _err()
     return topo
+
+
+def write_seis(path: str, section, ix, iy, xs: float, ys: float, p: SofihPar, ishot: int = 1, comp: int = 1,
+               trace=None):
+    """One seismogram file in p.seis_format (sofih_write_seis)."""
+    sec = np.ascontiguousarray(section, dtype=np.float32)
+    ix = np.ascontiguousarray(ix, dtype=np.int32)
+    iy = np.ascontiguousarray(iy, dtype=np.int32)
+    ipp = ctypes.POINTER(ctypes.c_int)
+    tr = None if trace is None else np.ascontiguousarray(trace, dtype=np.int32)
+    if load().sofih_write_seis(path.encode(), _fp(sec), sec.shape[0], sec.shape[1], ix.ctypes.data_as(ipp),
+                               iy.ctypes.data_as(ipp), None if tr is None else tr.ctypes.data_as(ipp), xs, ys,
+                               ctypes.byref(p), ishot, comp):
+        raise _err()
+
+
+def write_snap(path: str, frame, append: bool = False, fmt: int = 3):
+    """Append (or start) a snapshot file in SNAP_FORMAT fmt (sofih_write_snap_format)."""
+    f = np.ascontiguousarray(frame, dtype=np.float32).reshape(-1)
+    if load().sofih_write_snap_format(path.encode(), _fp(f), f.size, int(append), fmt):
+        raise _err()
+
+
+def seis_ext(fmt: int):
+    v = load().sofih_seis_ext(fmt)
+    return v.decode() if v is not None else None
 
 
 def snapshot_shots(p: SofihPar, nshots: int) -> list:

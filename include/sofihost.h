@@ -173,6 +173,18 @@ int sofih_write_signal(const sofih_par *p, int ishot, const float *signal, int n
                        float ys, char *path_out, int path_len);
 /* Append frames to a binary snapshot file (float32, x outer, y inner). */
 int sofih_write_snap(const char *path, const float *frame, int n, int append);
+/* The same in SNAP_FORMAT (writedsk.c:36-52): 3 float32, 2 one value per
+ * line "%e"; 1 (SU) is an error, as in the reference. */
+int sofih_write_snap_format(const char *path, const float *frame, int n, int append, int format);
+/* File-name extension of SEIS_FORMAT (saveseis_glob.c:39-57): 1 "su",
+ * 2 "txt", 3 "bin", 0 / 4 / 5 "sgy"; NULL for any other value. */
+const char *sofih_seis_ext(int format);
+/* One seismogram file in p->seis_format (outseis_glob.c:39-100): 1 SU as
+ * sofih_write_su_traces, 2 one value per line "%e" trace after trace, 3
+ * float32 trace after trace; 0, 4 and 5 leave the file empty (the reference
+ * creates it and writes nothing); returns 1 on an I/O error. */
+int sofih_write_seis(const char *path, const float *section, int ntr, int ns, const int *ix, const int *iy,
+                     const int *trace, float xs, float ys, const sofih_par *p, int ishot, int comp);
 
 /* ---- FWI gradient pass (MODE = FWI; with sofi_fwi_* of sofigpu.h) ------
  * sofih_fwi_read_data: the first ntr traces of ns samples of an observed SU

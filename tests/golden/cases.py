@@ -167,6 +167,11 @@ SNAP_SHOTS_CASE = _case("snap_shots", nx=60, ny=50, nt=250, fw=10, seismo=1, ndt
                         seed=44, sources=[[31.0, 31.0, 0.0, 60.0, 1.0], [61.0, 41.0, 0.0, 60.0, 1.0],
                                           [91.0, 61.0, 0.0, 60.0, 1.0]],
                         par={"RUN_MULTIPLE_SHOTS": "1", "SNAPSHOT_START": "2", "SNAPSHOT_INCR": "1"})
+# Seismograms and snapshots in the binary and ASCII formats (SEIS_FORMAT and
+# SNAP_FORMAT 3, then 2), written by the reference for the same run.
+FORMAT_CASE = _case("fmt_out", nx=40, ny=40, nt=60, fw=5, seismo=1, ndt=2, snap=1, tsnap=0.006, idx=1, idy=1,
+                    seed=45, sources=[[41.0, 41.0, 0.0, 60.0, 1.0]],
+                    receivers=[[20.0, 20.0], [50.0, 30.0], [60.0, 60.0]])
 # A plane wave of sources (SRCREC 2). The compiled reference builds it
 # (sources.c:337-367) into a source matrix of 8 rows and then reads rows 9-11
 # of it in splitsrc.c:50-51, past the allocation, and crashes there; its log's

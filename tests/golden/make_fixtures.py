@@ -33,9 +33,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
-from tests.golden.cases import (ACQ_CASES, CASES, FWI_CASES, PLANE_WAVE_CASE, SNAP_SHOTS_CASE,  # noqa: E402
-                                WAVELET_CASES, WAVELET_DT, WAVELET_NT, _case, fwi_json_text, json_text,
-                                synthetic_model, true_model, write_case, write_signal_file)
+from tests.golden.cases import (ACQ_CASES, CASES, FORMAT_CASE, FWI_CASES, PLANE_WAVE_CASE,  # noqa: E402
+                                SNAP_SHOTS_CASE, WAVELET_CASES, WAVELET_DT, WAVELET_NT, _case, fwi_json_text,
+                                json_text, synthetic_model, true_model, write_case, write_signal_file)
 
 SHIPPED = {"weq3": "EL_ISO", "weq4": "VEL_ISO", "weq5": "EL_VTI", "weq6": "VEL_VTI", "weq7": "EL_TTI",
            "weq8": "VEL_TTI", "weq3_fy": "EL_ISO", "weq8_fy": "VEL_TTI", "weq3_fdt4": "EL_ISO",
@@ -173,6 +173,28 @@ def ref_wavelets(exe):
     np.savez_compressed(os.path.join(HERE, "ref_wavelets.npz"), **out)
 
 
+def ref_formats(exe):
+    """The same run written with SEIS_FORMAT / SNAP_FORMAT 3 (float32) and 2
+    (ASCII): ref_fmt_out.npz holds every file's bytes."""
+    out = {}
+    for fmt, ext, sext in ((3, "bin", "bin"), (2, "txt", "asc")):
+        case = dict(FORMAT_CASE, par={"SEIS_FORMAT": str(fmt), "SNAP_FORMAT": str(fmt)})
+        work = tempfile.mkdtemp(prefix="sofi_fmt_")
+        try:
+            jpath, _ = write_case(case, work)
+            r = subprocess.run([exe, jpath], cwd=work, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"formats {fmt}: reference failed\n{r.stdout[-2000:]}")
+            for comp in ("vx", "vy"):
+                out[f"seis{fmt}_{comp}"] = np.fromfile(os.path.join(work, "out", f"seis_{comp}.{ext}"), np.uint8)
+                out[f"snap{fmt}_{comp}"] = np.fromfile(os.path.join(work, "out", f"snap.{sext}.{comp}.0.0"),
+                                                       np.uint8)
+        finally:
+            shutil.rmtree(work, ignore_errors=True)
+    np.savez_compressed(os.path.join(HERE, "ref_fmt_out.npz"), **out)
+    print("wrote fmt_out", {k: v.size for k, v in out.items()})
+
+
 def ref_plane_wave(exe):
     """The plane-wave sources as the compiled reference logs them: it builds
     them and prints its source table, then crashes reading past its 8-row
@@ -263,6 +285,10 @@ def main():
             return
     if not a.only or a.only == "wavelets":
         ref_wavelets(exe)
+        if a.only:
+            return
+    if not a.only or a.only == "fmt_out":
+        ref_formats(exe)
         if a.only:
             return
     if not a.only or a.only == "acq_plane_wave":

@@ -386,3 +386,36 @@ def test_snapshot_files_hold_every_snapshotting_shot(H, tmp_path, oracle_mod):
         assert H.snapshot_shots(p, n) == want, (start, incr, n)
     p.snap = 0
     assert H.snapshot_shots(p, 3) == []
+
+
+def test_seismogram_and_snapshot_formats_match_reference(H, tmp_path):
+    """SEIS_FORMAT 2 / 3 and SNAP_FORMAT 2 / 3 (outseis_glob.c:85-97,
+    writedsk.c:36-52): written from the same samples, the ASCII and float32
+    files equal the compiled reference's byte for byte; the file-name
+    extensions follow saveseis_glob.c:39-57, and SNAP_FORMAT 1 is refused as
+    the reference refuses it."""
+    from tests.golden.cases import FORMAT_CASE, write_case
+    g = np.load(os.path.join(GOLDEN, "ref_fmt_out.npz"))
+    write_case(FORMAT_CASE, str(tmp_path))
+    p = H.read_par(str(tmp_path / "case.json"))
+    ntr = len(FORMAT_CASE["receivers"])
+    ix = iy = np.ones(ntr, np.int32)
+    for comp in ("vx", "vy"):
+        sec = g[f"seis3_{comp}"].view(np.float32).reshape(ntr, -1)
+        for fmt in (2, 3):
+            p.seis_format = fmt
+            out = str(tmp_path / f"s{fmt}.{comp}")
+            H.write_seis(out, sec, ix, iy, 0.0, 0.0, p)
+            np.testing.assert_array_equal(np.fromfile(out, np.uint8), g[f"seis{fmt}_{comp}"], err_msg=f"{fmt} {comp}")
+        frame = g[f"snap3_{comp}"].view(np.float32)
+        for fmt in (2, 3):
+            out = str(tmp_path / f"n{fmt}.{comp}")
+            H.write_snap(out, frame[: frame.size // 2], False, fmt)
+            H.write_snap(out, frame[frame.size // 2:], True, fmt)
+            np.testing.assert_array_equal(np.fromfile(out, np.uint8), g[f"snap{fmt}_{comp}"], err_msg=f"{fmt} {comp}")
+    assert [H.seis_ext(f) for f in range(7)] == ["sgy", "su", "txt", "bin", "sgy", "sgy", None]
+    with pytest.raises(Exception, match="SU format"):
+        H.write_snap(str(tmp_path / "x"), frame, False, 1)
+    p.seis_format = 4
+    H.write_seis(str(tmp_path / "e.sgy"), sec, ix, iy, 0.0, 0.0, p)
+    assert os.path.getsize(tmp_path / "e.sgy") == 0
