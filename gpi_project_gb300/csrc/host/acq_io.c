@@ -644,6 +644,11 @@ static void put_f32(unsigned char *h, int off, float v) { memcpy(h + off, &v, 4)
 static int write_su_traces(const char *path, const float *section, int ntr, int ns, const int *ix, const int *iy,
                            const int *tracl_of, float xs, float ys, const sofih_par *p, int ishot)
 {
+    if (ns > 65535) { /* checkfd.c:119-122: the SU header holds ns in 16 bits */
+        sofih_set_error("%s: %d samples per trace, at most 65535 in SU format (SEIS_FORMAT 2 or 3 have no limit)",
+                        path, ns);
+        return 1;
+    }
     FILE *fp = fopen(path, "wb");
     if (!fp) {
         sofih_set_error("cannot write %s", path);

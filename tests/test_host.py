@@ -419,3 +419,6 @@ def test_seismogram_and_snapshot_formats_match_reference(H, tmp_path):
     p.seis_format = 4
     H.write_seis(str(tmp_path / "e.sgy"), sec, ix, iy, 0.0, 0.0, p)
     assert os.path.getsize(tmp_path / "e.sgy") == 0
+    p.seis_format = 1  # checkfd.c:119-122: SU traces hold at most 65535 samples
+    with pytest.raises(Exception, match="65535"):
+        H.write_seis(str(tmp_path / "long.su"), np.zeros((1, 65536), np.float32), ix[:1], iy[:1], 0.0, 0.0, p)
