@@ -160,6 +160,11 @@ ACQ_CASES = [
           sources=[[61.0, 61.0, 0.0, 60.0, 1.0]],
           par={"READREC": "0", "XREC1": "10.0", "XREC2": "100.0", "YREC1": "10.0", "YREC2": "10.0",
                "REC_ARRAY": "3", "DRX": "7", "REC_ARRAY_DEPTH": "0.0", "REC_ARRAY_DIST": "9.0"}),
+    # the receiver line of the parameter file, its keys in the combined form of
+    # the reference's examples ("XREC1,YREC1" : "x , y"), every NGEOPH-th point
+    _case("acq_line", nx=60, ny=50, nt=250, fw=10, seismo=1, ndt=1, snap=0, seed=46,
+          sources=[[61.0, 61.0, 0.0, 60.0, 1.0]],
+          par={"READREC": "0", "XREC1,YREC1": "10.0 , 12.0", "XREC2,YREC2": "100.0 , 12.0", "NGEOPH": "3"}),
 ]
 # Three shots (RUN_MULTIPLE_SHOTS 1) of which shots 1 and 2 write snapshots
 # (SNAPSHOT_START 2): the files hold shot 1's frames, then shot 2's.
@@ -289,9 +294,10 @@ def acq_json_text(case) -> str:
         if key in par:
             ln = f'"{key}" : "{par.pop(key)}",'
         out.append(ln.rstrip(",") + ",")
-    out += [f'"{k}" : "{v}",' for k, v in par.items()]
     out[-1] = out[-1].rstrip(",")
-    return "\n".join(["{"] + out + ["}"]) + "\n"
+    # added keys go first: the reference's parser wants an odd number of
+    # commas on a line of combined keys ("XREC1,YREC1" : "x , y",)
+    return "\n".join(["{"] + [f'"{k}" : "{v}",' for k, v in par.items()] + out + ["}"]) + "\n"
 
 
 def write_case(case, work):

@@ -252,13 +252,14 @@ def test_parameter_file_fdorder_time_and_fwi_keys(tmp_path):
     assert p.data_dir.decode() == "./obs/seis" and p.gradient.decode() == "./grad/g"
 
 
-@pytest.mark.parametrize("name", ["acq_topo", "acq_planes"])
+@pytest.mark.parametrize("name", ["acq_topo", "acq_planes", "acq_line"])
 def test_acquisition_matches_compiled_reference(H, name, tmp_path, oracle_mod):
     """Receivers and sources as the compiled reference's receiver.c / sources.c
     place them: below the topography of the P-wave model (REC_TOPO,
     SOURCE_TOPO), with a co-located receiver of the file dropped and its trace
-    number left out, with REFRECX, and as receiver planes (REC_ARRAY) whose
-    first row 0 becomes 1. The oracle run on the host library's acquisition
+    number left out, with REFRECX, as receiver planes (REC_ARRAY) whose
+    first row 0 becomes 1, and on the parameter file's line (combined
+    "XREC1,YREC1" keys, NGEOPH). The oracle run on the host library's acquisition
     reproduces the reference's seismograms, and the SU file written with the
     host's receivers, trace numbers and source position carries the
     reference's trace headers byte for byte."""
