@@ -107,6 +107,22 @@ static double param(const char *key)
     exit(2);
 }
 
+/* an optional setting of params.txt */
+static double param_or(const char *key, double dflt)
+{
+    FILE *fp = open_in("params.txt", "r");
+    char k[64];
+    double v;
+    while (fp && fscanf(fp, "%63s %lf", k, &v) == 2)
+        if (!strcmp(k, key)) {
+            fclose(fp);
+            return v;
+        }
+    if (fp)
+        fclose(fp);
+    return dflt;
+}
+
 int main(int argc, char **argv)
 {
     if (argc < 2)
@@ -120,7 +136,13 @@ int main(int argc, char **argv)
     gv.FW = (int)param("FW"), gv.ABS_TYPE = (int)param("ABS_TYPE"), gv.FREE_SURF = (int)param("FREE_SURF");
     gv.BOUNDARY = (int)param("BOUNDARY"), gv.SEISMO = (int)param("SEISMO"), gv.NDT = (int)param("NDT");
     gv.WEQ = (int)param("WEQ"), gv.MODE = (int)param("MODE"), gv.NPROCX = gv.NPROCY = 1;
-    gv.OUTNTIMESTEPINFO = (int)param("OUTNTIMESTEPINFO"), gv.SNAP = 0, gv.SNAP_FORMAT = 3;
+    gv.OUTNTIMESTEPINFO = (int)param("OUTNTIMESTEPINFO");
+    /* snapshots (optional): written by time_loop() under <dir>/snap, as snap_ssg.c names them */
+    gv.SNAP = (int)param_or("SNAP", 0), gv.SNAP_FORMAT = (int)param_or("SNAP_FORMAT", 3);
+    gv.TSNAP1 = (float)param_or("TSNAP1", 0), gv.TSNAP2 = (float)param_or("TSNAP2", 0);
+    gv.TSNAPINC = (float)param_or("TSNAPINC", 1);
+    snprintf(gv.SNAP_FILE, sizeof gv.SNAP_FILE, "%s/snap", g_dir);
+    const int shots = (int)param_or("SHOTS", 1); /* forward calls, as sofi2D.c's loop over shots */
     gv.IDX = gv.IDY = 1;
     const int NX = gv.NX, NY = gv.NY, ND = gv.ND, NT = gv.NT;
     const int nsrc = (int)param("NSRC"), ntr = (int)param("NTR"), ns = (int)param("NS");
@@ -193,7 +215,9 @@ int main(int argc, char **argv)
     memset(&perf, 0, sizeof perf);
 
     /* forward call: sofi2D.c:369-370 (MODE = FW) or inversion.c:130 (sw = 0) */
-    time_loop(1, 1, 0, hc1 + 1, srcpos, sig, sig, nsrc, 0, &acq, &mpm, &mpw, &minv, &gv, &vinv, &perf);
+    for (int s = 1; s <= shots; s++)
+        time_loop(1, s, gv.SNAP > 0, hc1 + 1, srcpos, sig, sig, nsrc, 0, &acq, &mpm, &mpw, &minv, &gv, &vinv,
+                  &perf);
     const char *cn[5] = {"vx", "vy", "p", "div", "curl"};
     for (int k = 0; k < 5; k++) {
         char name[64];

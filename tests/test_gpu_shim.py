@@ -180,3 +180,42 @@ def test_shim_fwi_passes_equal_abi(harness, case, tmp_path, monkeypatch):
         assert np.abs(a).max() > 0
     assert perf["infocounter"] == 2 * ((cfg.nt - 1) // OUT_INFO + 1)
     o.close()
+
+
+@pytest.mark.parametrize("fmt", [3, 2])
+def test_shim_snapshots_equal_abi(harness, fmt, tmp_path, monkeypatch):
+    """snap() through the shim, two shots: the snapshot files (SNAP_FORMAT 3
+    float32, 2 ASCII "%e", named as snap_ssg.c:53-68 names them) hold both
+    shots' frames one after the other (time_loop.c:36 numbers snapshots
+    across shots), each frame equal to the C ABI's snapshot of the same run."""
+    from gpi_project_gb300 import TimeLoop
+    for k, v in FIXED.items():
+        monkeypatch.setenv(k, v)
+    case = dict(case_by_name("el_cpml_fd8"), snap=1, idx=1, idy=1, tsnap=0.04)
+    o, cfg, _, sp, sig, rec = _inputs(case)
+    d = str(tmp_path)
+    _write(d, o, cfg, sp, sig, rec, mode=1)
+    with open(os.path.join(d, "params.txt"), "a") as fh:
+        fh.write(f"SNAP 1\nSNAP_FORMAT {fmt}\nTSNAP1 {cfg.tsnap1!r}\nTSNAP2 {cfg.tsnap2!r}\nTSNAPINC 1.0\nSHOTS 2\n")
+    _run(harness, d)
+    fields, vecs = prepared_model(o, cfg)
+    t = TimeLoop(gpu_config_from(cfg))
+    t.set_model(fields)
+    t.set_vectors(vecs)
+    t.set_sources(sp, sig)
+    t.set_receivers(*rec)
+    t.reset()
+    t.run()
+    ext = "bin" if fmt == 3 else "asc"
+    for c in ("vx", "vy"):
+        frames = t.snapshots(c)
+        assert frames.shape[0] == 1 and np.abs(frames).max() > 0
+        want = np.concatenate([frames.reshape(-1)] * 2)
+        path = os.path.join(d, f"snap.{ext}.{c}.0.0")
+        if fmt == 3:
+            np.testing.assert_array_equal(np.fromfile(path, np.float32), want, err_msg=c)
+        else:
+            with open(path) as fh:
+                assert fh.read() == "".join("%e\n" % v for v in want), c
+    t.close()
+    o.close()
