@@ -133,6 +133,10 @@ static void gets_(const kvlist *kv, const char *key, char *out, size_t n)
 int sofih_read_par(const char *path, sofih_par *p)
 {
     kvlist *kv = (kvlist *)calloc(1, sizeof(kvlist));
+    if (!kv) {
+        sofih_set_error("out of host memory reading %s", path);
+        return 1;
+    }
     if (parse_file(path, kv)) {
         free(kv);
         return 1;

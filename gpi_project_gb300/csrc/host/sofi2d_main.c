@@ -56,6 +56,10 @@ static double now_s(void)
 static float *transpose_xy(const float *a, int nx, int ny)
 {
     float *t = (float *)malloc(sizeof(float) * (size_t)nx * ny);
+    if (!t) {
+        fprintf(stderr, "sofi2d_gb300: out of host memory\n");
+        exit(1);
+    }
     for (int i = 0; i < nx; i++)
         for (int j = 0; j < ny; j++)
             t[(size_t)j * nx + i] = a[(size_t)i * ny + j];
