@@ -114,6 +114,7 @@ def make_par(**kw) -> SofihPar:
     p.npower, p.k_max_cpml, p.damping, p.ndt, p.idx, p.idy, p.readrec = 2.0, 1.0, 8.0, 1, 1, 1, 1
     p.fdorder_time = 2
     p.readmod, p.tau = 1, 0.0001
+    p.srcrec, p.snapshot_start, p.snapshot_end, p.snapshot_incr, p.snap_format, p.seis_format = 1, 1, -9999, 1, 3, 1
     for k, v in kw.items():
         if k == "fl":
             for i, f in enumerate(v):
