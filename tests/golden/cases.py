@@ -165,6 +165,9 @@ ACQ_CASES = [
     _case("acq_line", nx=60, ny=50, nt=250, fw=10, seismo=1, ndt=1, snap=0, seed=46,
           sources=[[61.0, 61.0, 0.0, 60.0, 1.0]],
           par={"READREC": "0", "XREC1,YREC1": "10.0 , 12.0", "XREC2,YREC2": "100.0 , 12.0", "NGEOPH": "3"}),
+    _case("acq_vline", nx=60, ny=50, nt=250, fw=10, seismo=1, ndt=1, snap=0, seed=47,
+          sources=[[61.0, 61.0, 0.0, 60.0, 1.0]],
+          par={"READREC": "0", "XREC1,YREC1": "80.0 , 8.0", "XREC2,YREC2": "80.0 , 90.0", "NGEOPH": "4"}),
 ]
 # Three shots (RUN_MULTIPLE_SHOTS 1) of which shots 1 and 2 write snapshots
 # (SNAPSHOT_START 2): the files hold shot 1's frames, then shot 2's.

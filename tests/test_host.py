@@ -252,7 +252,7 @@ def test_parameter_file_fdorder_time_and_fwi_keys(tmp_path):
     assert p.data_dir.decode() == "./obs/seis" and p.gradient.decode() == "./grad/g"
 
 
-@pytest.mark.parametrize("name", ["acq_topo", "acq_planes", "acq_line"])
+@pytest.mark.parametrize("name", ["acq_topo", "acq_planes", "acq_line", "acq_vline"])
 def test_acquisition_matches_compiled_reference(H, name, tmp_path, oracle_mod):
     """Receivers and sources as the compiled reference's receiver.c / sources.c
     place them: below the topography of the P-wave model (REC_TOPO,
